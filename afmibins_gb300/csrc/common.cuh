@@ -1,0 +1,132 @@
+// Shared device-side definitions for the afmib GB300 kernels (sm_103a).
+//
+// Field layout in HBM: every field is one flat array, x fastest,
+// i = x + nx*(y + ny*z). Velocity lives on MAC faces: u[i] at (x, y+1/2, z+1/2),
+// v[i] at (x+1/2, y, z+1/2), w[i] at (x+1/2, y+1/2, z), in units of h = 1/n.
+// In channel mode (walls at y = 0 and y = ny, the reference's domain) v keeps
+// all ny planes and plane y = 0 is the bottom wall, held at zero; the top wall
+// face y = ny is the periodic image of plane 0. With that convention the
+// advection, divergence, gradient and v-Helmholtz stencils of the channel are
+// the periodic stencils (every wall term carries a zero factor), and only the
+// pressure Laplacian, the multigrid transfers and the u/w Helmholtz wall rows
+// need channel-specific code.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace afmib {
+
+struct Dims {
+    int nx, ny, nz;  // cells
+    int n;           // cells per unit length
+    int channel;     // 1: walls in y
+    __host__ __device__ long long sxy() const { return (long long)nx * ny; }
+    __host__ __device__ long long ncell() const { return (long long)nx * ny * nz; }
+};
+
+__host__ __device__ inline int wrapi(int i, int m) {
+    i %= m;
+    return i < 0 ? i + m : i;
+}
+
+__device__ __forceinline__ long long lin(const Dims& d, int x, int y, int z) {
+    return (long long)x + (long long)d.nx * ((long long)y + (long long)d.ny * z);
+}
+
+// neighbour offsets along each axis with periodic wrap
+__device__ __forceinline__ int xm1(const Dims& d, int x) { return x == 0 ? d.nx - 1 : x - 1; }
+__device__ __forceinline__ int xp1(const Dims& d, int x) { return x == d.nx - 1 ? 0 : x + 1; }
+__device__ __forceinline__ int ym1(const Dims& d, int y) { return y == 0 ? d.ny - 1 : y - 1; }
+__device__ __forceinline__ int yp1(const Dims& d, int y) { return y == d.ny - 1 ? 0 : y + 1; }
+__device__ __forceinline__ int zm1(const Dims& d, int z) { return z == 0 ? d.nz - 1 : z - 1; }
+__device__ __forceinline__ int zp1(const Dims& d, int z) { return z == d.nz - 1 ? 0 : z + 1; }
+
+// ---------------------------------------------------------------------------
+// Deterministic grid-wide sums. Each block reduces its values with warp
+// shuffles in a fixed tree, writes one partial, and the last block to finish
+// (atomic ticket) sums the partials in a fixed order. The result therefore
+// does not depend on block scheduling. `scratch` holds the partials and the
+// ticket; the ticket is left at zero for the next launch.
+// ---------------------------------------------------------------------------
+constexpr int kRedBlock = 256;
+constexpr int kMaxRedBlocks = 2048;
+
+struct RedScratch {
+    double* partial;     // [kMaxRedBlocks * kMaxRedVals]
+    unsigned* ticket;    // [1]
+};
+constexpr int kMaxRedVals = 4;
+
+template <int NV>
+__device__ __forceinline__ void warp_sum(double (&v)[NV]) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+}
+
+// Block-wide sum of NV values (blockDim.x == kRedBlock); result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV]) {
+    __shared__ double s[kRedBlock / 32][NV];
+    warp_sum<NV>(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) s[w][k] = v[k];
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[k] = (l < kRedBlock / 32) ? s[l][k] : 0.0;
+        warp_sum<NV>(v);
+    }
+    __syncthreads();
+}
+
+// Reduce v over the whole grid into out[0..NV-1]. Must be reached by every
+// thread of every block exactly once. Returns true in exactly one thread (the
+// finisher: thread 0 of the last block), where v then holds the totals, so
+// that a caller can derive further scalars (CG coefficients) in place.
+template <int NV>
+__device__ __forceinline__ bool grid_sum(double (&v)[NV], RedScratch sc, double* out) {
+    __shared__ bool last;
+    block_sum<NV>(v);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sc.partial[(size_t)k * kMaxRedBlocks + blockIdx.x] = v[k];
+        __threadfence();
+        unsigned t = atomicAdd(sc.ticket, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        double a[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) a[k] = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+#pragma unroll
+            for (int k = 0; k < NV; ++k) a[k] += __ldcg(&sc.partial[(size_t)k * kMaxRedBlocks + b]);
+        block_sum<NV>(a);
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                out[k] = a[k];
+                v[k] = a[k];
+            }
+            *sc.ticket = 0u;
+            return true;
+        }
+    }
+    return false;
+}
+
+inline int red_blocks(long long n) {
+    long long b = (n + kRedBlock - 1) / kRedBlock;
+    if (b > kMaxRedBlocks) b = kMaxRedBlocks;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+}  // namespace afmib

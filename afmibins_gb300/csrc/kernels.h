@@ -1,0 +1,102 @@
+// Host-side launch wrappers of the afmib sm_103a kernels. Each wrapper
+// enqueues on the given stream and returns immediately; T is double (the FP64
+// drop-in) or float (the inner passes of the mixed-precision form).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace afmib {
+
+// ----- MAC stencils (kernels_field.cu) -------------------------------------
+// Conservative centred advection N(u) of src/ns/solver.h:142-236.
+template <typename T>
+void launch_advect(const Dims& d, T* ua, T* va, T* wa, const T* u, const T* v, const T* w, cudaStream_t s);
+// Divergence n*(du + dv + dw), src/alg/div.h:29-60. top/bottom (channel only,
+// nx*nz each) may be null for zero walls.
+template <typename T>
+void launch_div(const Dims& d, T* out, const T* u, const T* v, const T* w, const T* top, const T* bottom,
+                cudaStream_t s);
+// Gradient onto faces, src/alg/grad.h:29-44 (v plane 0 untouched in channel mode).
+template <typename T>
+void launch_grad(const Dims& d, T* px, T* py, T* pz, const T* p, cudaStream_t s);
+// Projection update u -= grad(phi), src/ns/projection.h:60-73. In channel
+// mode the wall-adjacent gradient rows needed by the next wall update are
+// saved into wallgrad[6][nx*nz] (may be null).
+template <typename T>
+void launch_grad_sub(const Dims& d, T* u, T* v, T* w, const T* phi, T* wallgrad, cudaStream_t s);
+// Wall-velocity correction of src/ns/projection.h:75-122 (channel only).
+// walls = [ut | ub | wt | wb], nx*nz each.
+void launch_wall_update(const Dims& d, double* walls, const double* wallgrad, cudaStream_t s);
+
+// Helmholtz right-hand side for one component.
+//   be=1: r = u_old - bdy(s_minus) + dt/2 * (f/rho - adv)
+//   be=0: r = (I + s_plus*Delta) u_old + bdy(s_plus) - bdy(s_minus) + dt*(f/rho - adv)
+// src/ns/solver.h:105-135 with src/ns/helmholtz.h:177-196. walls: [top|bottom]
+// rows of this component (null in periodic mode or for v).
+template <typename T>
+void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const T* f, const T* adv,
+                     const double* top, const double* bottom, double s_plus, double s_minus, double dt,
+                     double inv_rho, cudaStream_t s);
+// y = (I + s*Delta) x for component comp (src/ns/helmholtz.h:61-175,218-319).
+template <typename T>
+void launch_helm_apply(const Dims& d, int comp, double scale, T* y, const T* x, cudaStream_t s);
+
+// ----- CG pieces (kernels_field.cu) ------------------------------------------
+// Device scalars cgs[] = {n0, pq, n1, beta, alpha} (src/alg/cg.h:36-53).
+// init:      r = b - A x, p = r, n0 = r.r
+template <typename T>
+void launch_cg_init(const Dims& d, int comp, double scale, const T* x, const T* b, T* r, T* p, RedScratch sc,
+                    double* cgs, cudaStream_t s);
+// apply:     q = A p, pq = p.q, alpha = n0 / pq
+template <typename T>
+void launch_cg_apply(const Dims& d, int comp, double scale, const T* p, T* q, RedScratch sc, double* cgs,
+                     cudaStream_t s);
+// update:    x += alpha p, r -= alpha q, n1 = r.r, beta = n1 / n0, n0 = n1
+template <typename T>
+void launch_cg_update(long long n, T* x, T* r, const T* p, const T* q, RedScratch sc, double* cgs, cudaStream_t s);
+// direction: p = beta p + r
+template <typename T>
+void launch_cg_direction(long long n, T* p, const T* r, const double* cgs, cudaStream_t s);
+
+// ----- reductions and vector ops (kernels_field.cu) ---------------------------
+template <typename T>
+void launch_sum(long long n, const T* x, RedScratch sc, double* out, cudaStream_t s);          // sum x
+template <typename T>
+void launch_sumsq(long long n, const T* x, RedScratch sc, double* out, cudaStream_t s);        // sum x^2
+template <typename T>
+void launch_sub_scalar_scaled(long long n, T* x, const double* sum, double scale, cudaStream_t s);  // x -= sum*scale
+template <typename T>
+void launch_fill(long long n, T* x, T value, cudaStream_t s);
+template <typename T>
+void launch_axpy(long long n, T* y, const T* x, T a, cudaStream_t s);  // y += a x
+template <typename TO, typename TI>
+void launch_convert(long long n, TO* out, const TI* in, cudaStream_t s);
+
+// ----- multigrid (kernels_mg.cu) ---------------------------------------------
+// Laplacian n^2*Delta of src/mg/laplacian.h:46-153 (Neumann walls in channel mode).
+template <typename T>
+void launch_lap_apply(const Dims& d, T* y, const T* x, cudaStream_t s);
+// r = b - L x, optionally out[0] = r.r
+template <typename T>
+void launch_residual(const Dims& d, T* r, const T* x, const T* b, RedScratch* sc, double* out, cudaStream_t s);
+// One red (color 0) or black (color 1) Gauss-Seidel half sweep.
+template <typename T>
+void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s);
+// Full-weighting restriction, src/mg/solver.h:153-181 (d = fine dims).
+template <typename T>
+void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s);
+// fine += P coarse (trilinear), src/mg/solver.h:71-151 and :211-212.
+template <typename T>
+void launch_prolong_add(const Dims& d, T* fine, const T* coarse, cudaStream_t s);
+// Prolongation that assigns (for the op-level API).
+template <typename T>
+void launch_prolong_assign(const Dims& d, T* fine, const T* coarse, cudaStream_t s);
+// Coarsest-level solve (mean removal + CG on one block), src/mg/solver.h:264-271.
+// status[0] receives 0 or 3 (not converged).
+template <typename T>
+void launch_coarse_solve(const Dims& d, T* x, T* b, T* r, T* p, T* q, double tol, int maxit, int* status,
+                         cudaStream_t s);
+
+}  // namespace afmib

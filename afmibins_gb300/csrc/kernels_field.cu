@@ -1,0 +1,406 @@
+// MAC-grid stencils, Helmholtz operator, CG pieces and reductions.
+// Memory-bound (FP32) or FP64-pipe-bound (FP64) single-pass kernels: every
+// output element is produced by one thread from neighbours that the L1/L2
+// caches supply, so DRAM traffic is one read per input array and one write per
+// output array.
+#include "kernels.h"
+
+namespace afmib {
+
+namespace {
+
+constexpr int BX = 32, BY = 8;
+
+inline dim3 grid3(const Dims& d) { return dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz); }
+inline dim3 block3() { return dim3(BX, BY, 1); }
+
+#define AFMIB_XYZ                                          \
+    const int x = blockIdx.x * BX + threadIdx.x;           \
+    const int y = blockIdx.y * BY + threadIdx.y;           \
+    const int z = blockIdx.z;                              \
+    if (x >= d.nx || y >= d.ny) return;
+
+// ---------------------------------------------------------------------------
+// Advection, src/ns/solver.h:142-236. Fluxes on the periodic staggering
+//   uu(j) = (u(j)+u(j-x))^2/4        at the cell centre left of face j
+//   uv(j) = (u(j)+u(j-y))(v(j)+v(j-x))/4 at the edge (x, y, z+1/2)
+//   uw(j) = (u(j)+u(j-z))(w(j)+w(j-x))/4 at the edge (x, y+1/2, z)
+//   vw(j) = (v(j)+v(j-z))(w(j)+w(j-y))/4 at the edge (x+1/2, y, z)
+// and N = n * (flux differences). In channel mode v plane 0 is the zero wall,
+// which makes every wall flux of the reference (uvt, uvb, vwt, vwb = 0; vvb,
+// vvt from the one interior face) come out of the same formulas.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_advect(Dims d, T* __restrict__ ua, T* __restrict__ va, T* __restrict__ wa,
+                         const T* __restrict__ u, const T* __restrict__ v, const T* __restrict__ w) {
+    AFMIB_XYZ
+    const T h = T(0.5), n = T(d.n);
+    const int xm = xm1(d, x), xp = xp1(d, x), ym = ym1(d, y), yp = yp1(d, y), zm = zm1(d, z), zp = zp1(d, z);
+    const long long i = lin(d, x, y, z);
+    const long long ixm = lin(d, xm, y, z), ixp = lin(d, xp, y, z), iym = lin(d, x, ym, z), iyp = lin(d, x, yp, z),
+                    izm = lin(d, x, y, zm), izp = lin(d, x, y, zp);
+    const T u0 = u[i], v0 = v[i], w0 = w[i];
+    T q, r;
+    // shared fluxes at this cell's own corner
+    q = h * (u0 + u[iym]); r = h * (v0 + v[ixm]); const T uv0 = q * r;
+    q = h * (u[izm] + u0); r = h * (w[ixm] + w0); const T uw0 = q * r;
+    q = h * (v[izm] + v0); r = h * (w0 + w[iym]); const T vw0 = q * r;
+    // u-momentum
+    {
+        q = h * (u0 + u[ixm]); const T uu0 = q * q;
+        q = h * (u[ixp] + u0); const T uup = q * q;
+        q = h * (u[iyp] + u0); r = h * (v[iyp] + v[lin(d, xm, yp, z)]); const T uvp = q * r;
+        q = h * (u0 + u[izp]); r = h * (w[lin(d, xm, y, zp)] + w[izp]); const T uwp = q * r;
+        ua[i] = n * ((uup - uu0) + (uvp - uv0) + (uwp - uw0));
+    }
+    // v-momentum (plane 0 is the wall in channel mode)
+    if (d.channel && y == 0) {
+        va[i] = T(0);
+    } else {
+        q = h * (u[ixp] + u[lin(d, xp, ym, z)]); r = h * (v[ixp] + v0); const T uvp = q * r;
+        q = h * (v0 + v[iym]); const T vv0 = q * q;
+        q = h * (v[iyp] + v0); const T vvp = q * q;
+        q = h * (v0 + v[izp]); r = h * (w[izp] + w[lin(d, x, ym, zp)]); const T vwp = q * r;
+        va[i] = n * ((uvp - uv0) + (vvp - vv0) + (vwp - vw0));
+    }
+    // w-momentum
+    {
+        q = h * (u[lin(d, xp, y, zm)] + u[ixp]); r = h * (w[ixp] + w0); const T uwp = q * r;
+        q = h * (v[lin(d, x, yp, zm)] + v[iyp]); r = h * (w[iyp] + w0); const T vwp = q * r;
+        q = h * (w0 + w[izm]); const T ww0 = q * q;
+        q = h * (w[izp] + w0); const T wwp = q * q;
+        wa[i] = n * ((uwp - uw0) + (vwp - vw0) + (wwp - ww0));
+    }
+}
+
+// Divergence, src/alg/div.h:29-60.
+template <typename T>
+__global__ void k_div(Dims d, T* __restrict__ out, const T* __restrict__ u, const T* __restrict__ v,
+                      const T* __restrict__ w, const T* __restrict__ top, const T* __restrict__ bottom) {
+    AFMIB_XYZ
+    const long long i = lin(d, x, y, z);
+    T dv;
+    if (d.channel) {
+        const long long ixz = x + (long long)d.nx * z;
+        const T tv = top ? top[ixz] : T(0), bv = bottom ? bottom[ixz] : T(0);
+        if (d.ny == 1) dv = tv - bv;
+        else if (y == 0) dv = v[lin(d, x, 1, z)] - bv;
+        else if (y == d.ny - 1) dv = tv - v[i];
+        else dv = v[lin(d, x, y + 1, z)] - v[i];
+    } else {
+        dv = v[lin(d, x, yp1(d, y), z)] - v[i];
+    }
+    out[i] = T(d.n) * ((u[lin(d, xp1(d, x), y, z)] - u[i]) + dv + (w[lin(d, x, y, zp1(d, z))] - w[i]));
+}
+
+// Gradient, src/alg/grad.h:29-44.
+template <typename T>
+__global__ void k_grad(Dims d, T* __restrict__ px, T* __restrict__ py, T* __restrict__ pz, const T* __restrict__ p) {
+    AFMIB_XYZ
+    const long long i = lin(d, x, y, z);
+    const T n = T(d.n), p0 = p[i];
+    px[i] = n * (p0 - p[lin(d, xm1(d, x), y, z)]);
+    pz[i] = n * (p0 - p[lin(d, x, y, zm1(d, z))]);
+    if (!d.channel || y > 0) py[i] = n * (p0 - p[lin(d, x, ym1(d, y), z)]);
+}
+
+// u -= grad(phi), src/ns/projection.h:69-72, saving the wall-adjacent rows that
+// the next wall update reads (src/ns/projection.h:91-94).
+template <typename T>
+__global__ void k_grad_sub(Dims d, T* __restrict__ u, T* __restrict__ v, T* __restrict__ w, const T* __restrict__ p,
+                           T* __restrict__ wg) {
+    AFMIB_XYZ
+    const long long i = lin(d, x, y, z);
+    const T n = T(d.n), p0 = p[i];
+    const T gx = n * (p0 - p[lin(d, xm1(d, x), y, z)]);
+    const T gz = n * (p0 - p[lin(d, x, y, zm1(d, z))]);
+    u[i] = u[i] - gx;
+    w[i] = w[i] - gz;
+    if (!d.channel || y > 0) v[i] = v[i] - n * (p0 - p[lin(d, x, ym1(d, y), z)]);
+    if (d.channel && wg) {
+        const long long nxz = (long long)d.nx * d.nz, ixz = x + (long long)d.nx * z;
+        if (y == 0) { wg[0 * nxz + ixz] = gx; wg[4 * nxz + ixz] = gz; }
+        if (y == 1) wg[1 * nxz + ixz] = gx;
+        if (y == d.ny - 1) { wg[2 * nxz + ixz] = gx; wg[5 * nxz + ixz] = gz; }
+        if (y == d.ny - 2) wg[3 * nxz + ixz] = gx;
+    }
+}
+
+// src/ns/projection.h:86-104, including its slips: the loop covers
+// nx*min(ny, nz) wall entries and the w corrections read the x-gradient rows.
+__global__ void k_wall_update(Dims d, double* __restrict__ walls, const double* __restrict__ wg) {
+    const long long nxz = (long long)d.nx * d.nz;
+    const long long cnt = (long long)d.nx * (d.ny < d.nz ? d.ny : d.nz);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cnt; i += (long long)gridDim.x * blockDim.x) {
+        const double pxb1 = wg[0 * nxz + i], pxb2 = wg[1 * nxz + i], pxt1 = wg[2 * nxz + i], pxt2 = wg[3 * nxz + i];
+        const double pzb1 = wg[4 * nxz + i], pzt1 = wg[5 * nxz + i];
+        walls[0 * nxz + i] += (9 * pxt1 - pxt2) / 8;   // ut
+        walls[1 * nxz + i] += (9 * pxb1 - pxb2) / 8;   // ub
+        walls[2 * nxz + i] += (9 * pzt1 - pxt2) / 8;   // wt (pzt2 = phidtx[...])
+        walls[3 * nxz + i] += (9 * pzb1 - pxb2) / 8;   // wb (pzb2 = phidtx[...])
+    }
+}
+
+// (I + s Delta) applied at one point. Cell rows (u, w; all components in
+// periodic mode) carry the one-sided Dirichlet closure at the channel walls,
+// src/ns/helmholtz.h:90-104; v rows in channel mode treat the walls as zero
+// neighbours (plane 0 and its periodic image), src/ns/helmholtz.h:247-248.
+template <typename T>
+__device__ __forceinline__ T helm_point(const Dims& d, int comp, T s, const T* __restrict__ x, int xi, int yi, int zi) {
+    const long long i = lin(d, xi, yi, zi);
+    const T off = s * T(d.n) * T(d.n);
+    const T x0 = x[i];
+    const T sx = x[lin(d, xm1(d, xi), yi, zi)] + x[lin(d, xp1(d, xi), yi, zi)];
+    const T sz = x[lin(d, xi, yi, zm1(d, zi))] + x[lin(d, xi, yi, zp1(d, zi))];
+    if (d.channel && comp != 1) {
+        T diag = T(1) - T(6) * off;
+        T sy;
+        if (yi == 0) {
+            diag -= T(2) * off;
+            sy = (off + off / T(3)) * x[lin(d, xi, 1, zi)];
+        } else if (yi == d.ny - 1) {
+            diag -= T(2) * off;
+            sy = (off + off / T(3)) * x[lin(d, xi, yi - 1, zi)];
+        } else {
+            sy = off * (x[lin(d, xi, yi - 1, zi)] + x[lin(d, xi, yi + 1, zi)]);
+        }
+        return diag * x0 + (off * (sx + sz) + sy);
+    }
+    if (d.channel && comp == 1 && yi == 0) return x0;
+    const T sy = x[lin(d, xi, ym1(d, yi), zi)] + x[lin(d, xi, yp1(d, yi), zi)];
+    return (T(1) - T(6) * off) * x0 + off * (sx + sy + sz);
+}
+
+template <typename T>
+__global__ void k_helm_apply(Dims d, int comp, T s, T* __restrict__ out, const T* __restrict__ in) {
+    AFMIB_XYZ
+    out[lin(d, x, y, z)] = helm_point(d, comp, s, in, x, y, z);
+}
+
+// Right-hand side of the viscous solve, src/ns/solver.h:105-135.
+template <typename T>
+__global__ void k_helm_rhs(Dims d, int comp, int be, T* __restrict__ r, const T* __restrict__ uold,
+                           const T* __restrict__ f, const T* __restrict__ adv, const double* __restrict__ top,
+                           const double* __restrict__ bottom, double s_plus, double s_minus, double hdt,
+                           double inv_rho) {
+    AFMIB_XYZ
+    const long long i = lin(d, x, y, z);
+    if (d.channel && comp == 1 && y == 0) { r[i] = T(0); return; }
+    // wall term of helmholtz_periodic::boundary (u, w rows next to the walls)
+    T bm = T(0), bp = T(0);
+    if (d.channel && comp != 1 && (y == 0 || y == d.ny - 1) && top) {
+        const long long ixz = x + (long long)d.nx * z;
+        const double wv = (y == 0) ? bottom[ixz] : top[ixz];
+        bm = T(8. / 3. * s_minus * d.n * d.n * wv);
+        bp = T(8. / 3. * s_plus * d.n * d.n * wv);
+    }
+    const T src = T(hdt) * (T(inv_rho) * f[i] - adv[i]);
+    if (be) {
+        r[i] = (uold[i] + T(-1) * bm) + src;
+    } else {
+        r[i] = (helm_point(d, comp, T(s_plus), uold, x, y, z) + (bp - bm)) + src;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// CG pieces. Scalars live on the device in cgs[] = {n0, pq, n1, beta, alpha}
+// so that no host round trip sits inside an iteration except the convergence
+// test on n0 (the reference's absolute 2-norm stop, src/alg/cg.h:42).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kRedBlock) k_cg_init(Dims d, int comp, T s, const T* __restrict__ x,
+                                                      const T* __restrict__ b, T* __restrict__ r, T* __restrict__ p,
+                                                      RedScratch sc, double* cgs) {
+    const long long N = d.ncell(), sxy = d.sxy();
+    double acc[1] = {0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+        const int xi = (int)(i % d.nx), yi = (int)((i % sxy) / d.nx), zi = (int)(i / sxy);
+        const T ri = b[i] - helm_point(d, comp, s, x, xi, yi, zi);
+        r[i] = ri;
+        p[i] = ri;
+        acc[0] += (double)ri * (double)ri;
+    }
+    grid_sum<1>(acc, sc, cgs + 0);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRedBlock) k_cg_apply(Dims d, int comp, T s, const T* __restrict__ p,
+                                                       T* __restrict__ q, RedScratch sc, double* cgs) {
+    const long long N = d.ncell(), sxy = d.sxy();
+    double acc[1] = {0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+        const int xi = (int)(i % d.nx), yi = (int)((i % sxy) / d.nx), zi = (int)(i / sxy);
+        const T qi = helm_point(d, comp, s, p, xi, yi, zi);
+        q[i] = qi;
+        acc[0] += (double)p[i] * (double)qi;
+    }
+    if (grid_sum<1>(acc, sc, cgs + 1)) cgs[4] = cgs[0] / acc[0];  // alpha = n0 / (p.Ap)
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRedBlock) k_cg_update(long long N, T* __restrict__ x, T* __restrict__ r,
+                                                        const T* __restrict__ p, const T* __restrict__ q,
+                                                        RedScratch sc, double* cgs) {
+    const T alpha = T(cgs[4]);
+    double acc[1] = {0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+        x[i] = x[i] + alpha * p[i];
+        const T ri = r[i] - q[i] * alpha;
+        r[i] = ri;
+        acc[0] += (double)ri * (double)ri;
+    }
+    if (grid_sum<1>(acc, sc, cgs + 2)) {
+        cgs[3] = acc[0] / cgs[0];  // beta = n1 / n0
+        cgs[0] = acc[0];
+    }
+}
+
+template <typename T>
+__global__ void k_cg_direction(long long N, T* __restrict__ p, const T* __restrict__ r, const double* cgs) {
+    const T beta = T(cgs[3]);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
+        p[i] = p[i] * beta + r[i];
+}
+
+// ---------------------------------------------------------------------------
+// reductions and vector ops
+// ---------------------------------------------------------------------------
+template <typename T, bool SQ>
+__global__ void __launch_bounds__(kRedBlock) k_sum(long long N, const T* __restrict__ x, RedScratch sc, double* out) {
+    double acc[1] = {0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+        const double e = (double)x[i];
+        acc[0] += SQ ? e * e : e;
+    }
+    grid_sum<1>(acc, sc, out);
+}
+
+template <typename T>
+__global__ void k_sub_scalar(long long N, T* __restrict__ x, const double* sum, double scale) {
+    const T m = T(sum[0] * scale);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
+        x[i] = x[i] - m;
+}
+
+template <typename T>
+__global__ void k_fill(long long N, T* __restrict__ x, T v) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
+        x[i] = v;
+}
+
+template <typename T>
+__global__ void k_axpy(long long N, T* __restrict__ y, const T* __restrict__ x, T a) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
+        y[i] = y[i] + a * x[i];
+}
+
+template <typename TO, typename TI>
+__global__ void k_convert(long long N, TO* __restrict__ o, const TI* __restrict__ in) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
+        o[i] = (TO)in[i];
+}
+
+inline int ew_blocks(long long n) {
+    long long b = (n + 255) / 256;
+    if (b > 152 * 16) b = 152 * 16;
+    return (int)(b < 1 ? 1 : b);
+}
+
+}  // namespace
+
+template <typename T>
+void launch_advect(const Dims& d, T* ua, T* va, T* wa, const T* u, const T* v, const T* w, cudaStream_t s) {
+    k_advect<T><<<grid3(d), block3(), 0, s>>>(d, ua, va, wa, u, v, w);
+}
+template <typename T>
+void launch_div(const Dims& d, T* out, const T* u, const T* v, const T* w, const T* top, const T* bottom, cudaStream_t s) {
+    k_div<T><<<grid3(d), block3(), 0, s>>>(d, out, u, v, w, top, bottom);
+}
+template <typename T>
+void launch_grad(const Dims& d, T* px, T* py, T* pz, const T* p, cudaStream_t s) {
+    k_grad<T><<<grid3(d), block3(), 0, s>>>(d, px, py, pz, p);
+}
+template <typename T>
+void launch_grad_sub(const Dims& d, T* u, T* v, T* w, const T* phi, T* wallgrad, cudaStream_t s) {
+    k_grad_sub<T><<<grid3(d), block3(), 0, s>>>(d, u, v, w, phi, wallgrad);
+}
+void launch_wall_update(const Dims& d, double* walls, const double* wallgrad, cudaStream_t s) {
+    k_wall_update<<<ew_blocks((long long)d.nx * d.nz), 256, 0, s>>>(d, walls, wallgrad);
+}
+template <typename T>
+void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const T* f, const T* adv, const double* top,
+                     const double* bottom, double s_plus, double s_minus, double dt, double inv_rho, cudaStream_t s) {
+    k_helm_rhs<T><<<grid3(d), block3(), 0, s>>>(d, comp, be, r, uold, f, adv, top, bottom, s_plus, s_minus,
+                                                be ? dt / 2 : dt, inv_rho);
+}
+template <typename T>
+void launch_helm_apply(const Dims& d, int comp, double scale, T* y, const T* x, cudaStream_t s) {
+    k_helm_apply<T><<<grid3(d), block3(), 0, s>>>(d, comp, T(scale), y, x);
+}
+template <typename T>
+void launch_cg_init(const Dims& d, int comp, double scale, const T* x, const T* b, T* r, T* p, RedScratch sc,
+                    double* cgs, cudaStream_t s) {
+    k_cg_init<T><<<red_blocks(d.ncell()), kRedBlock, 0, s>>>(d, comp, T(scale), x, b, r, p, sc, cgs);
+}
+template <typename T>
+void launch_cg_apply(const Dims& d, int comp, double scale, const T* p, T* q, RedScratch sc, double* cgs, cudaStream_t s) {
+    k_cg_apply<T><<<red_blocks(d.ncell()), kRedBlock, 0, s>>>(d, comp, T(scale), p, q, sc, cgs);
+}
+template <typename T>
+void launch_cg_update(long long n, T* x, T* r, const T* p, const T* q, RedScratch sc, double* cgs, cudaStream_t s) {
+    k_cg_update<T><<<red_blocks(n), kRedBlock, 0, s>>>(n, x, r, p, q, sc, cgs);
+}
+template <typename T>
+void launch_cg_direction(long long n, T* p, const T* r, const double* cgs, cudaStream_t s) {
+    k_cg_direction<T><<<ew_blocks(n), 256, 0, s>>>(n, p, r, cgs);
+}
+template <typename T>
+void launch_sum(long long n, const T* x, RedScratch sc, double* out, cudaStream_t s) {
+    k_sum<T, false><<<red_blocks(n), kRedBlock, 0, s>>>(n, x, sc, out);
+}
+template <typename T>
+void launch_sumsq(long long n, const T* x, RedScratch sc, double* out, cudaStream_t s) {
+    k_sum<T, true><<<red_blocks(n), kRedBlock, 0, s>>>(n, x, sc, out);
+}
+template <typename T>
+void launch_sub_scalar_scaled(long long n, T* x, const double* sum, double scale, cudaStream_t s) {
+    k_sub_scalar<T><<<ew_blocks(n), 256, 0, s>>>(n, x, sum, scale);
+}
+template <typename T>
+void launch_fill(long long n, T* x, T value, cudaStream_t s) {
+    k_fill<T><<<ew_blocks(n), 256, 0, s>>>(n, x, value);
+}
+template <typename T>
+void launch_axpy(long long n, T* y, const T* x, T a, cudaStream_t s) {
+    k_axpy<T><<<ew_blocks(n), 256, 0, s>>>(n, y, x, a);
+}
+template <typename TO, typename TI>
+void launch_convert(long long n, TO* out, const TI* in, cudaStream_t s) {
+    k_convert<TO, TI><<<ew_blocks(n), 256, 0, s>>>(n, out, in);
+}
+
+#define AFMIB_INST(T)                                                                                          \
+    template void launch_advect<T>(const Dims&, T*, T*, T*, const T*, const T*, const T*, cudaStream_t);       \
+    template void launch_div<T>(const Dims&, T*, const T*, const T*, const T*, const T*, const T*, cudaStream_t); \
+    template void launch_grad<T>(const Dims&, T*, T*, T*, const T*, cudaStream_t);                             \
+    template void launch_grad_sub<T>(const Dims&, T*, T*, T*, const T*, T*, cudaStream_t);                     \
+    template void launch_helm_rhs<T>(const Dims&, int, int, T*, const T*, const T*, const T*, const double*,   \
+                                     const double*, double, double, double, double, cudaStream_t);             \
+    template void launch_helm_apply<T>(const Dims&, int, double, T*, const T*, cudaStream_t);                  \
+    template void launch_cg_init<T>(const Dims&, int, double, const T*, const T*, T*, T*, RedScratch, double*, \
+                                    cudaStream_t);                                                             \
+    template void launch_cg_apply<T>(const Dims&, int, double, const T*, T*, RedScratch, double*, cudaStream_t); \
+    template void launch_cg_update<T>(long long, T*, T*, const T*, const T*, RedScratch, double*, cudaStream_t); \
+    template void launch_cg_direction<T>(long long, T*, const T*, const double*, cudaStream_t);                \
+    template void launch_sum<T>(long long, const T*, RedScratch, double*, cudaStream_t);                       \
+    template void launch_sumsq<T>(long long, const T*, RedScratch, double*, cudaStream_t);                     \
+    template void launch_sub_scalar_scaled<T>(long long, T*, const double*, double, cudaStream_t);             \
+    template void launch_fill<T>(long long, T*, T, cudaStream_t);                                              \
+    template void launch_axpy<T>(long long, T*, const T*, T, cudaStream_t);
+
+AFMIB_INST(double)
+AFMIB_INST(float)
+template void launch_convert<float, double>(long long, float*, const double*, cudaStream_t);
+template void launch_convert<double, float>(long long, double*, const float*, cudaStream_t);
+
+}  // namespace afmib

@@ -1,0 +1,528 @@
+// Immersed-boundary transfer kernels: springs, marker binning by a stable
+// device radix sort, deterministic gather spreading and interpolation.
+//
+// Reference: ib::grid::interpolate (src/ib/grid.h:68-84) computes both
+// directions face by face or marker by marker with the cosine 4-point kernel
+//   phi(r) = n/4 (1 + cos(pi r n / 2)), |r n| <= 2     (src/ib/grid.h:51-55)
+// and finds neighbours with a kd-tree (src/dt/kdtree.h). Here the markers are
+// binned by cell instead: a key (tile, cell in tile) per marker is sorted with
+// a stable LSD radix sort, so the markers of every cell are contiguous and in
+// index order. Spreading then runs one block per output tile of TS^3 cells,
+// gathering from the markers binned in the tile's (TS+4)^3 neighbourhood in a
+// fixed order: no float atomics, bitwise repeatable.
+//
+// Weights: for a marker at s = X*n along an axis and faces at j + off, the
+// four faces with |j + off - s| < 2 are j = floor(s - off) - 1 + m, m = 0..3,
+// and with t = frac(s - off), S = sin(pi t / 2), C = cos(pi t / 2):
+//   phi/n = (1 - S)/4, (1 + C)/4, (1 + S)/4, (1 - C)/4      (sum = 1)
+// (cos(pi r/2) at r = -1-t, -t, 1-t, 2-t). One sincospi per axis and offset.
+#include "kernels_ib.h"
+
+namespace afmib {
+
+namespace {
+
+__device__ __forceinline__ double sinpi_cospi(double x, double* c) {
+    double s;
+    sincospi(x, &s, c);
+    return s;
+}
+__device__ __forceinline__ float sinpi_cospi(float x, float* c) {
+    float s;
+    sincospif(x, &s, c);
+    return s;
+}
+
+// G_i = k * sum_j (X_j - X_i)
+template <typename T>
+__global__ void k_springs(int M, const double* __restrict__ X, const int* __restrict__ ns, const int* __restrict__ ni,
+                          double k, T* __restrict__ G) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    const double xi = X[3 * i], yi = X[3 * i + 1], zi = X[3 * i + 2];
+    double sx = 0, sy = 0, sz = 0;
+    for (int e = ns[i]; e < ns[i + 1]; ++e) {
+        const int j = ni[e];
+        sx += X[3 * j] - xi;
+        sy += X[3 * j + 1] - yi;
+        sz += X[3 * j + 2] - zi;
+    }
+    G[i] = T(k * sx);
+    G[M + i] = T(k * sy);
+    G[2 * M + i] = T(k * sz);
+}
+
+// Per marker: bin key, wrapped cell, and for each axis and offset variant
+// (0: faces on integer positions, 1: on half-integers) the base offset
+// (first face - cell) and the four weights phi/n.
+template <typename T>
+__global__ void k_marker_prep(Dims d, int TS, int M, const double* __restrict__ X, unsigned* __restrict__ keys,
+                              int* __restrict__ vals, MarkerW<T> mw, int* __restrict__ flag) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= M) return;
+    const int ext[3] = {d.nx, d.ny, d.nz};
+    int cell[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double s = X[3 * k + a] * d.n;
+        const double fs = floor(s);
+        cell[a] = wrapi((int)fs, ext[a]);
+        if (a == 1 && d.channel && (s < 2.5 || s > d.ny - 2.5)) atomicExch(flag, 1);
+        if (!(s == s)) atomicExch(flag, 2);
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+            const double t = s - 0.5 * v;
+            const double ft = floor(t);
+            const T frac = T(t - ft);
+            mw.dbase[(k * 3 + a) * 2 + v] = (signed char)((int)ft - 1 - (int)fs);
+            T C;
+            const T S = sinpi_cospi(frac * T(0.5), &C);
+            T* w = mw.w + (((size_t)k * 3 + a) * 2 + v) * 4;
+            w[0] = T(0.25) * (T(1) - S);
+            w[1] = T(0.25) * (T(1) + C);
+            w[2] = T(0.25) * (T(1) + S);
+            w[3] = T(0.25) * (T(1) - C);
+        }
+    }
+    mw.cell[3 * k] = cell[0];
+    mw.cell[3 * k + 1] = cell[1];
+    mw.cell[3 * k + 2] = cell[2];
+    const int tx = cell[0] / TS, ty = cell[1] / TS, tz = cell[2] / TS;
+    const int ntx = d.nx / TS, nty = d.ny / TS;
+    const unsigned tile = (unsigned)(tx + ntx * (ty + nty * tz));
+    const unsigned local = (unsigned)((cell[0] % TS) + TS * ((cell[1] % TS) + TS * (cell[2] % TS)));
+    keys[k] = tile * (unsigned)(TS * TS * TS) + local;
+    vals[k] = k;
+}
+
+// ---------------------------------------------------------------------------
+// Stable LSD radix sort of (key, value) pairs, 8-bit digits.
+// ---------------------------------------------------------------------------
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 8;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const unsigned* __restrict__ keys, int n, int shift,
+                                                        unsigned* __restrict__ hist, int nblk) {
+    __shared__ unsigned cnt[256];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * RS_TILE;
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        const int i = base + r * RS_THREADS + threadIdx.x;
+        if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[threadIdx.x * nblk + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// exclusive scan of hist[256 * nblk] in one block of 1024 threads
+__global__ void __launch_bounds__(1024) k_rs_scan(unsigned* __restrict__ hist, int total) {
+    __shared__ unsigned part[1024];
+    const int per = (total + 1023) / 1024;
+    const int lo = threadIdx.x * per, hi = min(lo + per, total);
+    unsigned s = 0;
+    for (int i = lo; i < hi; ++i) s += hist[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        unsigned v = threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    unsigned run = part[threadIdx.x] - s;
+    for (int i = lo; i < hi; ++i) {
+        const unsigned c = hist[i];
+        hist[i] = run;
+        run += c;
+    }
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const unsigned* __restrict__ kin, const int* __restrict__ vin,
+                                                           unsigned* __restrict__ kout, int* __restrict__ vout, int n,
+                                                           int shift, const unsigned* __restrict__ hist, int nblk) {
+    __shared__ unsigned s_off[256];
+    __shared__ unsigned s_wcnt[RS_THREADS / 32][256];
+    __shared__ unsigned s_wpre[RS_THREADS / 32][256];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    s_off[threadIdx.x] = hist[threadIdx.x * nblk + blockIdx.x];
+    for (int w = 0; w < RS_THREADS / 32; ++w) s_wcnt[w][threadIdx.x] = 0;
+    __syncthreads();
+    const unsigned lt = (1u << lane) - 1u;
+    const int base = blockIdx.x * RS_TILE;
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        const int i = base + r * RS_THREADS + threadIdx.x;
+        const bool valid = i < n;
+        const unsigned key = valid ? kin[i] : 0u;
+        const int val = valid ? vin[i] : 0;
+        const unsigned dig = valid ? ((key >> shift) & 255u) : 256u;
+        const unsigned peers = __match_any_sync(0xffffffffu, dig);
+        const unsigned rank = __popc(peers & lt);
+        if (valid && lane == __ffs(peers) - 1) s_wcnt[warp][dig] = __popc(peers);
+        __syncthreads();
+        {
+            unsigned run = s_off[threadIdx.x];
+            for (int w = 0; w < RS_THREADS / 32; ++w) {
+                const unsigned c = s_wcnt[w][threadIdx.x];
+                s_wpre[w][threadIdx.x] = run;
+                run += c;
+                s_wcnt[w][threadIdx.x] = 0;
+            }
+            s_off[threadIdx.x] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            const unsigned pos = s_wpre[warp][dig] + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+    }
+}
+
+// tile ranges of the sorted keys: tstart/tend zeroed beforehand
+__global__ void k_tile_ranges(const unsigned* __restrict__ keys, int M, int cells_per_tile, int* __restrict__ tstart,
+                              int* __restrict__ tend) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= M) return;
+    const unsigned t = keys[p] / (unsigned)cells_per_tile;
+    if (p == 0 || keys[p - 1] / (unsigned)cells_per_tile != t) tstart[t] = p;
+    if (p == M - 1 || keys[p + 1] / (unsigned)cells_per_tile != t) tend[t] = p + 1;
+}
+
+// output tiles whose (TS+4)^3 neighbourhood holds a marker
+__global__ void k_active_tiles(int ntx, int nty, int ntz, int channel, const int* __restrict__ tstart,
+                               const int* __restrict__ tend, int* __restrict__ list, int* __restrict__ count) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntx * nty * ntz) return;
+    const int tx = t % ntx, ty = (t / ntx) % nty, tz = t / (ntx * nty);
+    bool any = false;
+    for (int dz = -1; dz <= 1 && !any; ++dz)
+        for (int dy = -1; dy <= 1 && !any; ++dy) {
+            int yy = ty + dy;
+            if (channel && (yy < 0 || yy >= nty)) continue;
+            yy = wrapi(yy, nty);
+            for (int dx = -1; dx <= 1 && !any; ++dx) {
+                const int n = wrapi(tx + dx, ntx) + ntx * (yy + nty * wrapi(tz + dz, ntz));
+                if (tend[n] > tstart[n]) any = true;
+            }
+        }
+    if (any) list[atomicAdd(count, 1)] = t;
+}
+
+// ---------------------------------------------------------------------------
+// Gather spreading. One block (TS^3 threads, one face per component each) per
+// active output tile. Candidates: markers of the 27 neighbour tiles whose
+// cell lies in E = tile grown by 2 cells per side, compacted in a fixed order
+// and counting-sorted by E-cell (x fastest) so that every row of cells is one
+// contiguous run. A face at E-local coordinate J along an axis with offset
+// off gathers cells [J-2, J+1] (off 0) or [J-2, J+2] (off 1/2).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(512) k_spread_gather(Dims d, int TS, int M, const int* __restrict__ perm,
+                                                       MarkerW<T> mw, const T* __restrict__ G,
+                                                       const double* __restrict__ vol, double scale,
+                                                       const int* __restrict__ tstart, const int* __restrict__ tend,
+                                                       const int* __restrict__ list, const int* __restrict__ count,
+                                                       int cap, T* __restrict__ fu, T* __restrict__ fv,
+                                                       T* __restrict__ fw, int* __restrict__ flag) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int E = TS + 4, E3 = E * E * E;
+    const int ntx = d.nx / TS, nty = d.ny / TS, ntz = d.nz / TS;
+    // carve shared memory
+    int* s_start = (int*)smem;                 // E3 + 1
+    int* s_first = s_start + (E3 + 1);         // E3
+    int* s_pos = s_first + E3;                 // cap: sorted position p of each compacted candidate
+    int* s_ecell = s_pos + cap;                // cap
+    int* s_order = s_ecell + cap;              // cap: slot -> compacted index
+    int* s_base = s_order + cap;               // cap: packed E-local bases (3 x 8 bit, biased by 8)
+    int* s_scan = s_base + cap;                // blockDim.x scan workspace + 2
+    T* s_w = (T*)(((uintptr_t)(s_scan + blockDim.x + 2) + 15) & ~(uintptr_t)15);  // cap * 12
+    T* s_g = s_w + (size_t)cap * 12;           // cap
+    __shared__ int s_nc;
+
+    const int ncount = *count;
+    const int tid = threadIdx.x;
+    const int lx = tid % TS, ly = (tid / TS) % TS, lz = tid / (TS * TS);
+    for (int li = blockIdx.x; li < ncount; li += gridDim.x) {
+        const int t = list[li];
+        const int tx = t % ntx, ty = (t / ntx) % nty, tz = t / (ntx * nty);
+        const int ox = tx * TS - 2, oy = ty * TS - 2, oz = tz * TS - 2;  // E origin (unwrapped)
+        for (int e = tid; e < E3; e += blockDim.x) { s_start[e] = 0; s_first[e] = 0x7fffffff; }
+        if (tid == 0) s_nc = 0;
+        __syncthreads();
+        // ---- ordered compaction of the candidates over the 27 neighbour tiles
+        for (int nb = 0; nb < 27; ++nb) {
+            const int dx = nb % 3 - 1, dy = (nb / 3) % 3 - 1, dz = nb / 9 - 1;
+            int yy = ty + dy;
+            if (d.channel && (yy < 0 || yy >= nty)) continue;
+            yy = wrapi(yy, nty);
+            const int n = wrapi(tx + dx, ntx) + ntx * (yy + nty * wrapi(tz + dz, ntz));
+            const int a = tstart[n], b = tend[n];
+            for (int r0 = a; r0 < b; r0 += blockDim.x) {
+                const int p = r0 + tid;
+                int ecell = -1;
+                if (p < b) {
+                    const int k = perm[p];
+                    const int ex = wrapi(mw.cell[3 * k] - ox, d.nx), ez = wrapi(mw.cell[3 * k + 2] - oz, d.nz);
+                    const int ey = d.channel ? mw.cell[3 * k + 1] - oy : wrapi(mw.cell[3 * k + 1] - oy, d.ny);
+                    if (ex < E && ey >= 0 && ey < E && ez < E) ecell = ex + E * (ey + E * ez);
+                }
+                // block-wide exclusive scan of the flags (fixed order)
+                const int f = ecell >= 0;
+                s_scan[tid] = f;
+                __syncthreads();
+                for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+                    const int v = tid >= o ? s_scan[tid - o] : 0;
+                    __syncthreads();
+                    s_scan[tid] += v;
+                    __syncthreads();
+                }
+                const int slot = s_nc + s_scan[tid] - f;
+                if (f && slot < cap) {
+                    s_pos[slot] = p;
+                    s_ecell[slot] = ecell;
+                }
+                __syncthreads();
+                if (tid == blockDim.x - 1) s_nc += s_scan[tid];
+                __syncthreads();
+            }
+        }
+        int nc = s_nc;
+        if (nc > cap) {
+            if (tid == 0) atomicExch(flag, 3);
+            nc = cap;
+        }
+        // ---- counting sort by E-cell; within a cell, sorted position order
+        for (int c = tid; c < nc; c += blockDim.x) {
+            atomicAdd(&s_start[s_ecell[c]], 1);
+            atomicMin(&s_first[s_ecell[c]], s_pos[c]);
+        }
+        __syncthreads();
+        {
+            // parallel exclusive scan of the E3 counts: each thread owns a
+            // contiguous run, then a block scan of the run totals
+            const int per = (E3 + blockDim.x - 1) / blockDim.x;
+            const int e0 = tid * per, e1 = min(e0 + per, E3);
+            int tot = 0;
+            for (int e = e0; e < e1; ++e) tot += s_start[e];
+            s_scan[tid] = tot;
+            __syncthreads();
+            for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+                const int v = tid >= o ? s_scan[tid - o] : 0;
+                __syncthreads();
+                s_scan[tid] += v;
+                __syncthreads();
+            }
+            int run = s_scan[tid] - tot;
+            for (int e = e0; e < e1; ++e) {
+                const int c = s_start[e];
+                s_start[e] = run;
+                run += c;
+            }
+            if (tid == blockDim.x - 1) s_start[E3] = s_scan[tid];
+        }
+        __syncthreads();
+        for (int c = tid; c < nc; c += blockDim.x) {
+            const int e = s_ecell[c];
+            s_order[s_start[e] + (s_pos[c] - s_first[e])] = c;
+        }
+        __syncthreads();
+        // ---- one component at a time
+        for (int comp = 0; comp < 3; ++comp) {
+            for (int sl = tid; sl < nc; sl += blockDim.x) {
+                const int c = s_order[sl];
+                const int k = perm[s_pos[c]];
+                const int e = s_ecell[c];
+                const int ec[3] = {e % E, (e / E) % E, e / (E * E)};
+                int packed = 0;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const int v = (a == comp) ? 0 : 1;
+                    const int b = ec[a] + mw.dbase[(k * 3 + a) * 2 + v];  // E-local first face
+                    packed |= (b + 8) << (8 * a);
+                    const T* w = mw.w + (((size_t)k * 3 + a) * 2 + v) * 4;
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) s_w[(size_t)sl * 12 + a * 4 + m] = w[m];
+                }
+                s_base[sl] = packed;
+                s_g[sl] = T((double)G[(size_t)comp * M + k] * (vol ? vol[k] : 1.0) * scale);
+            }
+            __syncthreads();
+            T* f = comp == 0 ? fu : (comp == 1 ? fv : fw);
+            const int J[3] = {lx + 2, ly + 2, lz + 2};
+            int lo[3], hi[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = J[a] - 2;
+                hi[a] = (a == comp) ? J[a] + 1 : J[a] + 2;
+            }
+            T acc = T(0);
+            for (int ez = lo[2]; ez <= hi[2]; ++ez)
+                for (int ey = lo[1]; ey <= hi[1]; ++ey) {
+                    const int row = E * (ey + E * ez);
+                    const int s0 = s_start[row + lo[0]], s1 = s_start[row + hi[0] + 1];
+                    for (int sl = s0; sl < s1; ++sl) {
+                        const int pk = s_base[sl];
+                        const int mx = J[0] - ((pk & 255) - 8);
+                        const int my = J[1] - (((pk >> 8) & 255) - 8);
+                        const int mz = J[2] - (((pk >> 16) & 255) - 8);
+                        if ((unsigned)mx < 4u && (unsigned)my < 4u && (unsigned)mz < 4u) {
+                            const T* w = s_w + (size_t)sl * 12;
+                            acc += w[mx] * w[4 + my] * w[8 + mz] * s_g[sl];
+                        }
+                    }
+                }
+            const int gx = tx * TS + lx, gy = ty * TS + ly, gz = tz * TS + lz;
+            if (!(d.channel && comp == 1 && gy == 0)) f[lin(d, gx, gy, gz)] = acc;
+            __syncthreads();
+        }
+    }
+}
+
+// Interpolation U_k = sum over 4^3 faces of (phi/n)^3 * u(face)
+// (src/ib/grid.h:68-84 with volume h^3, src/ib/eulerian_grid.h:45).
+template <typename T>
+__global__ void k_interp(Dims d, int M, const int* __restrict__ perm, MarkerW<T> mw, const T* __restrict__ u,
+                         const T* __restrict__ v, const T* __restrict__ w, double* __restrict__ U) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= M) return;
+    const int k = perm ? perm[p] : p;
+    const int ext[3] = {d.nx, d.ny, d.nz};
+    for (int comp = 0; comp < 3; ++comp) {
+        const T* src = comp == 0 ? u : (comp == 1 ? v : w);
+        int idx[3][4];
+        T wt[3][4];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const int var = (a == comp) ? 0 : 1;
+            const int b = mw.cell[3 * k + a] + mw.dbase[(k * 3 + a) * 2 + var];
+            const T* ww = mw.w + (((size_t)k * 3 + a) * 2 + var) * 4;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                idx[a][m] = wrapi(b + m, ext[a]);
+                wt[a][m] = ww[m];
+            }
+        }
+        T acc = T(0);
+#pragma unroll
+        for (int mz = 0; mz < 4; ++mz)
+#pragma unroll
+            for (int my = 0; my < 4; ++my) {
+                const T wyz = wt[1][my] * wt[2][mz];
+                const long long row = (long long)d.nx * (idx[1][my] + (long long)d.ny * idx[2][mz]);
+#pragma unroll
+                for (int mx = 0; mx < 4; ++mx) acc += wt[0][mx] * wyz * src[row + idx[0][mx]];
+            }
+        U[(size_t)comp * M + k] = (double)acc;
+    }
+}
+
+// X_out = X_in + c * U  (U component-major)
+__global__ void k_marker_axpy(int M, double* __restrict__ Xo, const double* __restrict__ Xi, const double* __restrict__ U,
+                              double c) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= M) return;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) Xo[3 * k + a] = Xi[3 * k + a] + c * U[(size_t)a * M + k];
+}
+
+}  // namespace
+
+template <typename T>
+void launch_springs(int M, const double* X, const int* nstart, const int* nidx, double k, T* G, cudaStream_t s) {
+    if (M > 0) k_springs<T><<<(M + 255) / 256, 256, 0, s>>>(M, X, nstart, nidx, k, G);
+}
+
+template <typename T>
+void launch_marker_prep(const Dims& d, int TS, int M, const double* X, unsigned* keys, int* vals, MarkerW<T> mw,
+                        int* flag, cudaStream_t s) {
+    if (M > 0) k_marker_prep<T><<<(M + 255) / 256, 256, 0, s>>>(d, TS, M, X, keys, vals, mw, flag);
+}
+
+size_t radix_sort_temp_bytes(int n) {
+    const int nblk = (n + RS_TILE - 1) / RS_TILE;
+    return (size_t)256 * (nblk > 0 ? nblk : 1) * sizeof(unsigned);
+}
+
+void radix_sort_pairs(unsigned* keys, int* vals, unsigned* keys_alt, int* vals_alt, int n, int bits, unsigned* hist,
+                      unsigned** keys_out, int** vals_out, cudaStream_t s) {
+    const int nblk = (n + RS_TILE - 1) / RS_TILE;
+    unsigned* ka = keys;
+    unsigned* kb = keys_alt;
+    int* va = vals;
+    int* vb = vals_alt;
+    for (int shift = 0; shift < bits && n > 0; shift += 8) {
+        k_rs_hist<<<nblk, RS_THREADS, 0, s>>>(ka, n, shift, hist, nblk);
+        k_rs_scan<<<1, 1024, 0, s>>>(hist, 256 * nblk);
+        k_rs_scatter<<<nblk, RS_THREADS, 0, s>>>(ka, va, kb, vb, n, shift, hist, nblk);
+        unsigned* tk = ka; ka = kb; kb = tk;
+        int* tv = va; va = vb; vb = tv;
+    }
+    *keys_out = ka;
+    *vals_out = va;
+}
+
+void launch_tile_ranges(const unsigned* keys, int M, int cells_per_tile, int* tstart, int* tend, cudaStream_t s) {
+    if (M > 0) k_tile_ranges<<<(M + 255) / 256, 256, 0, s>>>(keys, M, cells_per_tile, tstart, tend);
+}
+
+void launch_active_tiles(int ntx, int nty, int ntz, int channel, const int* tstart, const int* tend, int* list,
+                         int* count, cudaStream_t s) {
+    const int nt = ntx * nty * ntz;
+    k_active_tiles<<<(nt + 255) / 256, 256, 0, s>>>(ntx, nty, ntz, channel, tstart, tend, list, count);
+}
+
+template <typename T>
+size_t spread_smem_bytes(int TS, int cap) {
+    const int E = TS + 4, E3 = E * E * E;
+    size_t ints = (size_t)(E3 + 1) + E3 + 5 * (size_t)cap + TS * TS * TS + 2;
+    size_t bytes = ints * sizeof(int);
+    bytes = (bytes + 15) & ~(size_t)15;
+    bytes += (size_t)cap * 13 * sizeof(T);
+    return bytes;
+}
+
+template <typename T>
+void launch_spread_gather(const Dims& d, int TS, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
+                          double scale, const int* tstart, const int* tend, const int* list, const int* count,
+                          int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, cudaStream_t s) {
+    const size_t smem = spread_smem_bytes<T>(TS, cap);
+    static bool configured[2] = {false, false};
+    const int slot = sizeof(T) == 8 ? 0 : 1;
+    if (!configured[slot]) {
+        cudaFuncSetAttribute(k_spread_gather<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        configured[slot] = true;
+    }
+    int blocks = max_tiles < 152 * 2 ? max_tiles : 152 * 2;
+    if (blocks < 1) blocks = 1;
+    k_spread_gather<T><<<blocks, TS * TS * TS, smem, s>>>(d, TS, M, perm, mw, G, vol, scale, tstart, tend, list,
+                                                          count, cap, fu, fv, fw, flag);
+}
+
+template <typename T>
+void launch_interp(const Dims& d, int M, const int* perm, MarkerW<T> mw, const T* u, const T* v, const T* w, double* U,
+                   cudaStream_t s) {
+    if (M > 0) k_interp<T><<<(M + 127) / 128, 128, 0, s>>>(d, M, perm, mw, u, v, w, U);
+}
+
+void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, double c, cudaStream_t s) {
+    if (M > 0) k_marker_axpy<<<(M + 255) / 256, 256, 0, s>>>(M, Xo, Xi, U, c);
+}
+
+#define AFMIB_IB_INST(T)                                                                                        \
+    template void launch_springs<T>(int, const double*, const int*, const int*, double, T*, cudaStream_t);       \
+    template void launch_marker_prep<T>(const Dims&, int, int, const double*, unsigned*, int*, MarkerW<T>, int*, \
+                                        cudaStream_t);                                                           \
+    template size_t spread_smem_bytes<T>(int, int);                                                             \
+    template void launch_spread_gather<T>(const Dims&, int, int, const int*, MarkerW<T>, const T*, const double*, \
+                                          double, const int*, const int*, const int*, const int*, int, int, T*,  \
+                                          T*, T*, int*, cudaStream_t);                                          \
+    template void launch_interp<T>(const Dims&, int, const int*, MarkerW<T>, const T*, const T*, const T*,       \
+                                   double*, cudaStream_t);
+
+AFMIB_IB_INST(double)
+AFMIB_IB_INST(float)
+
+}  // namespace afmib

@@ -1,0 +1,54 @@
+// Immersed-boundary launch wrappers (kernels_ib.cu).
+#pragma once
+
+#include "kernels.h"
+
+namespace afmib {
+
+// Per-marker data computed once per marker configuration: wrapped cell,
+// and for each axis a and face-offset variant v (0: integer positions, 1:
+// half-integer) the first of the four faces relative to the cell and the
+// four weights phi/n.
+template <typename T>
+struct MarkerW {
+    int* cell;           // [M][3]
+    signed char* dbase;  // [M][3][2]
+    T* w;                // [M][3][2][4]
+};
+
+template <typename T>
+void launch_springs(int M, const double* X, const int* nstart, const int* nidx, double k, T* G, cudaStream_t s);
+
+// keys = tile * TS^3 + cell-in-tile, vals = marker index; flag set to 1 when a
+// marker is within 2.5h of a channel wall, 2 on a NaN position.
+template <typename T>
+void launch_marker_prep(const Dims& d, int TS, int M, const double* X, unsigned* keys, int* vals, MarkerW<T> mw,
+                        int* flag, cudaStream_t s);
+
+size_t radix_sort_temp_bytes(int n);
+// Stable LSD sort of the low `bits` bits; returns which buffers hold the result.
+void radix_sort_pairs(unsigned* keys, int* vals, unsigned* keys_alt, int* vals_alt, int n, int bits, unsigned* hist,
+                      unsigned** keys_out, int** vals_out, cudaStream_t s);
+
+void launch_tile_ranges(const unsigned* keys, int M, int cells_per_tile, int* tstart, int* tend, cudaStream_t s);
+void launch_active_tiles(int ntx, int nty, int ntz, int channel, const int* tstart, const int* tend, int* list,
+                         int* count, cudaStream_t s);
+
+template <typename T>
+size_t spread_smem_bytes(int TS, int cap);
+// f_c(face) = scale * sum_k (phi/n)^3 * vol_k * G_c,k over the active tiles
+// (faces of the other tiles are left untouched). flag = 3 when a tile holds
+// more than `cap` candidates.
+template <typename T>
+void launch_spread_gather(const Dims& d, int TS, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
+                          double scale, const int* tstart, const int* tend, const int* list, const int* count,
+                          int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, cudaStream_t s);
+
+// U[c*M + k] = sum (phi/n)^3 u_c(face); perm (may be null) orders the threads.
+template <typename T>
+void launch_interp(const Dims& d, int M, const int* perm, MarkerW<T> mw, const T* u, const T* v, const T* w, double* U,
+                   cudaStream_t s);
+
+void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, double c, cudaStream_t s);
+
+}  // namespace afmib

@@ -1,0 +1,280 @@
+// Geometric multigrid pieces for the pressure projection (src/mg/solver.h,
+// src/mg/laplacian.h): red-black Gauss–Seidel in place of the reference's
+// lexicographic CSR sweep, the reference's full-weighting restriction and
+// trilinear prolongation, and a one-block CG for the coarsest level.
+#include "kernels.h"
+
+namespace afmib {
+
+namespace {
+
+constexpr int BX = 32, BY = 8;
+inline dim3 grid3(const Dims& d) { return dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz); }
+
+// Neighbour sum and diagonal factor of the Laplacian row at (x, y, z):
+// L x = n^2 * (S - c * x_i), c = 6 in the interior and one less per channel
+// wall (Neumann, src/mg/laplacian.h:75-82).
+template <typename T>
+__device__ __forceinline__ void lap_row(const Dims& d, const T* __restrict__ x, int xi, int yi, int zi, T& S, T& c) {
+    S = (x[lin(d, xm1(d, xi), yi, zi)] + x[lin(d, xp1(d, xi), yi, zi)]) +
+        (x[lin(d, xi, yi, zm1(d, zi))] + x[lin(d, xi, yi, zp1(d, zi))]);
+    c = T(6);
+    if (d.channel) {
+        if (yi > 0) S += x[lin(d, xi, yi - 1, zi)]; else c -= T(1);
+        if (yi < d.ny - 1) S += x[lin(d, xi, yi + 1, zi)]; else c -= T(1);
+    } else {
+        S += x[lin(d, xi, ym1(d, yi), zi)] + x[lin(d, xi, yp1(d, yi), zi)];
+    }
+}
+
+template <typename T>
+__global__ void k_lap(Dims d, T* __restrict__ out, const T* __restrict__ in) {
+    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+    if (x >= d.nx || y >= d.ny) return;
+    T S, c;
+    lap_row(d, in, x, y, z, S, c);
+    const T off = T(d.n) * T(d.n);
+    out[lin(d, x, y, z)] = off * (S - c * in[lin(d, x, y, z)]);
+}
+
+template <typename T>
+__global__ void k_residual(Dims d, T* __restrict__ r, const T* __restrict__ xv, const T* __restrict__ b) {
+    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+    if (x >= d.nx || y >= d.ny) return;
+    T S, c;
+    lap_row(d, xv, x, y, z, S, c);
+    const long long i = lin(d, x, y, z);
+    const T off = T(d.n) * T(d.n);
+    r[i] = b[i] - off * (S - c * xv[i]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRedBlock) k_residual_norm(Dims d, T* __restrict__ r, const T* __restrict__ xv,
+                                                            const T* __restrict__ b, RedScratch sc, double* out) {
+    const long long N = d.ncell(), sxy = d.sxy();
+    const T off = T(d.n) * T(d.n);
+    double acc[1] = {0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+        const int xi = (int)(i % d.nx), yi = (int)((i % sxy) / d.nx), zi = (int)(i / sxy);
+        T S, c;
+        lap_row(d, xv, xi, yi, zi, S, c);
+        const T ri = b[i] - off * (S - c * xv[i]);
+        r[i] = ri;
+        acc[0] += (double)ri * (double)ri;
+    }
+    grid_sum<1>(acc, sc, out);
+}
+
+// One colour of red-black Gauss–Seidel: x_i = (b_i - n^2 S) / (-c n^2).
+template <typename T>
+__global__ void k_rbgs(Dims d, int color, T* __restrict__ xv, const T* __restrict__ b) {
+    const int y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+    const int x = 2 * (blockIdx.x * BX + threadIdx.x) + ((y + z + color) & 1);
+    if (x >= d.nx || y >= d.ny) return;
+    T S, c;
+    lap_row(d, xv, x, y, z, S, c);
+    const long long i = lin(d, x, y, z);
+    const T inv = T(1) / (T(d.n) * T(d.n));
+    const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : T(1) / c);
+    xv[i] = (S - b[i] * inv) * rc;
+}
+
+// Full weighting, src/mg/solver.h:153-181: 64 taps (1,3,3,1)^3/512 around the
+// coarse cell; y clamps at the channel walls, wraps in periodic mode.
+template <typename T>
+__global__ void k_restrict(Dims d, T* __restrict__ coarse, const T* __restrict__ fine) {
+    const int cx = d.nx / 2, cy = d.ny / 2, cz = d.nz / 2;
+    const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
+    if (xc >= cx || yc >= cy) return;
+    const int xcf = 2 * xc + 1, ycf = 2 * yc + 1, zcf = 2 * zc + 1;
+    int xs[4], ys[4], zs[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int dd = k - 2;
+        xs[k] = wrapi(xcf + dd, d.nx);
+        zs[k] = wrapi(zcf + dd, d.nz);
+        if (d.channel) {
+            int yy = ycf + (dd > -ycf ? dd : -ycf);
+            ys[k] = yy < d.ny - 1 ? yy : d.ny - 1;
+        } else {
+            ys[k] = wrapi(ycf + dd, d.ny);
+        }
+    }
+    const T wgt[4] = {T(1), T(3), T(3), T(1)};
+    T acc = T(0);
+#pragma unroll
+    for (int kz = 0; kz < 4; ++kz)
+#pragma unroll
+        for (int ky = 0; ky < 4; ++ky)
+#pragma unroll
+            for (int kx = 0; kx < 4; ++kx)
+                acc += (wgt[kx] * wgt[ky] * wgt[kz] / T(512)) * fine[lin(d, xs[kx], ys[ky], zs[kz])];
+    coarse[xc + (long long)cx * (yc + (long long)cy * zc)] = acc;
+}
+
+// Trilinear prolongation (27,9,3,1)/64, src/mg/solver.h:71-151. One thread per
+// coarse cell writes the eight fine cells between it and its +1 neighbours;
+// in channel mode the wall rows take the bilinear (9,3,1)/16 weights.
+template <typename T, bool ADD>
+__global__ void k_prolong(Dims d, T* __restrict__ fine, const T* __restrict__ coarse) {
+    const int cx = d.nx / 2, cy = d.ny / 2, cz = d.nz / 2;
+    const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
+    if (xc >= cx || yc >= cy) return;
+    auto C = [&](int a, int b, int c) { return coarse[a + (long long)cx * (b + (long long)cy * c)]; };
+    auto put = [&](int a, int b, int c, T val) {
+        const long long i = lin(d, a, b, c);
+        if (ADD) fine[i] = fine[i] + val; else fine[i] = val;
+    };
+    const int xn = (xc + 1) % cx, zn = (zc + 1) % cz;
+    const int xcf = 2 * xc + 1, zcf = 2 * zc + 1;
+    const int xnf = (xcf + 1) % d.nx, znf = (zcf + 1) % d.nz;
+    const bool interior = d.channel ? (yc < cy - 1) : true;
+    if (interior) {
+        const int yn = d.channel ? yc + 1 : (yc + 1) % cy;
+        const int ycf = 2 * yc + 1, ynf = d.channel ? ycf + 1 : (ycf + 1) % d.ny;
+        const T blb = C(xc, yc, zc), brb = C(xn, yc, zc), ulb = C(xc, yn, zc), urb = C(xn, yn, zc);
+        const T blf = C(xc, yc, zn), brf = C(xn, yc, zn), ulf = C(xc, yn, zn), urf = C(xn, yn, zn);
+        const T a = T(27) / T(64), b = T(9) / T(64), c = T(3) / T(64), e = T(1) / T(64);
+        put(xcf, ycf, zcf, a * blb + b * (brb + ulb + blf) + c * (urb + ulf + brf) + e * urf);
+        put(xnf, ycf, zcf, a * brb + b * (urb + blb + brf) + c * (ulb + blf + urf) + e * ulf);
+        put(xcf, ynf, zcf, a * ulb + b * (urb + blb + ulf) + c * (brb + blf + urf) + e * brf);
+        put(xnf, ynf, zcf, a * urb + b * (brb + ulb + urf) + c * (blb + ulf + brf) + e * blf);
+        put(xcf, ycf, znf, a * blf + b * (brf + ulf + blb) + c * (urf + ulb + brb) + e * urb);
+        put(xnf, ycf, znf, a * brf + b * (urf + blf + brb) + c * (ulf + blb + urb) + e * ulb);
+        put(xcf, ynf, znf, a * ulf + b * (urf + blf + ulb) + c * (brf + blb + urb) + e * brb);
+        put(xnf, ynf, znf, a * urf + b * (brf + ulf + urb) + c * (blf + ulb + brb) + e * blb);
+    }
+    if (d.channel && (yc == 0 || yc == cy - 1)) {
+        const T a = T(9) / T(16), b = T(3) / T(16), e = T(1) / T(16);
+        // a thread with cy == 1 owns both wall rows
+        for (int side = 0; side < 2; ++side) {
+            if (side == 0 && yc != 0) continue;
+            if (side == 1 && yc != cy - 1) continue;
+            const int ycs = side == 0 ? 0 : cy - 1, yf = side == 0 ? 0 : d.ny - 1;
+            const T bl = C(xc, ycs, zc), br = C(xn, ycs, zc), fl = C(xc, ycs, zn), fr = C(xn, ycs, zn);
+            put(xcf, yf, zcf, a * bl + b * (br + fl) + e * fr);
+            put(xnf, yf, zcf, a * br + b * (bl + fr) + e * fl);
+            put(xcf, yf, znf, a * fl + b * (fr + bl) + e * br);
+            put(xnf, yf, znf, a * fr + b * (fl + br) + e * bl);
+        }
+    }
+}
+
+// Coarsest level, src/mg/solver.h:264-271: remove the mean of b, then CG
+// warm-started from b with the absolute 2-norm stop. One block; the level is
+// a handful of cells (one cell for a cube).
+template <typename T>
+__global__ void __launch_bounds__(kRedBlock) k_coarse_cg(Dims d, T* __restrict__ xv, T* __restrict__ b, T* __restrict__ r,
+                                                        T* __restrict__ p, T* __restrict__ q, double tol, int maxit,
+                                                        int* status) {
+    const long long N = d.ncell(), sxy = d.sxy();
+    const T off = T(d.n) * T(d.n);
+    __shared__ double s_val;
+    auto bsum = [&](double v) {
+        double a[1] = {v};
+        block_sum<1>(a);
+        if (threadIdx.x == 0) s_val = a[0];
+        __syncthreads();
+        return s_val;
+    };
+    auto apply = [&](const T* in, long long i) {
+        const int xi = (int)(i % d.nx), yi = (int)((i % sxy) / d.nx), zi = (int)(i / sxy);
+        T S, c;
+        // the one-cell (or one-row) levels fold self-neighbours into the diagonal
+        lap_row(d, in, xi, yi, zi, S, c);
+        return off * (S - c * in[i]);
+    };
+    double m = 0.0;
+    for (long long i = threadIdx.x; i < N; i += blockDim.x) m += (double)b[i];
+    m = bsum(m) / (double)N;
+    for (long long i = threadIdx.x; i < N; i += blockDim.x) {
+        b[i] = b[i] - T(m);
+        xv[i] = b[i];
+    }
+    __syncthreads();
+    double rr = 0.0;
+    for (long long i = threadIdx.x; i < N; i += blockDim.x) {
+        r[i] = b[i] - apply(xv, i);
+        p[i] = r[i];
+        rr += (double)r[i] * (double)r[i];
+    }
+    double n0 = bsum(rr);
+    int it = 0;
+    while (sqrt(n0) > tol) {
+        if (it >= maxit || !(n0 == n0)) {
+            if (threadIdx.x == 0) status[0] = 3;
+            return;
+        }
+        double pq = 0.0;
+        for (long long i = threadIdx.x; i < N; i += blockDim.x) {
+            q[i] = apply(p, i);
+            pq += (double)p[i] * (double)q[i];
+        }
+        pq = bsum(pq);
+        const T alpha = T(n0 / pq);
+        double n1 = 0.0;
+        for (long long i = threadIdx.x; i < N; i += blockDim.x) {
+            xv[i] = xv[i] + alpha * p[i];
+            r[i] = r[i] - q[i] * alpha;
+            n1 += (double)r[i] * (double)r[i];
+        }
+        n1 = bsum(n1);
+        const T beta = T(n1 / n0);
+        n0 = n1;
+        for (long long i = threadIdx.x; i < N; i += blockDim.x) p[i] = p[i] * beta + r[i];
+        __syncthreads();
+        ++it;
+    }
+}
+
+}  // namespace
+
+template <typename T>
+void launch_lap_apply(const Dims& d, T* y, const T* x, cudaStream_t s) {
+    k_lap<T><<<grid3(d), dim3(BX, BY), 0, s>>>(d, y, x);
+}
+template <typename T>
+void launch_residual(const Dims& d, T* r, const T* x, const T* b, RedScratch* sc, double* out, cudaStream_t s) {
+    if (sc && out)
+        k_residual_norm<T><<<red_blocks(d.ncell()), kRedBlock, 0, s>>>(d, r, x, b, *sc, out);
+    else
+        k_residual<T><<<grid3(d), dim3(BX, BY), 0, s>>>(d, r, x, b);
+}
+template <typename T>
+void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s) {
+    dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz);
+    k_rbgs<T><<<g, dim3(BX, BY), 0, s>>>(d, color, x, b);
+}
+template <typename T>
+void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s) {
+    dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz / 2);
+    k_restrict<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine);
+}
+template <typename T>
+void launch_prolong_add(const Dims& d, T* fine, const T* coarse, cudaStream_t s) {
+    dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz / 2);
+    k_prolong<T, true><<<g, dim3(BX, BY), 0, s>>>(d, fine, coarse);
+}
+template <typename T>
+void launch_prolong_assign(const Dims& d, T* fine, const T* coarse, cudaStream_t s) {
+    dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz / 2);
+    k_prolong<T, false><<<g, dim3(BX, BY), 0, s>>>(d, fine, coarse);
+}
+template <typename T>
+void launch_coarse_solve(const Dims& d, T* x, T* b, T* r, T* p, T* q, double tol, int maxit, int* status, cudaStream_t s) {
+    k_coarse_cg<T><<<1, kRedBlock, 0, s>>>(d, x, b, r, p, q, tol, maxit, status);
+}
+
+#define AFMIB_MG_INST(T)                                                                                 \
+    template void launch_lap_apply<T>(const Dims&, T*, const T*, cudaStream_t);                          \
+    template void launch_residual<T>(const Dims&, T*, const T*, const T*, RedScratch*, double*, cudaStream_t); \
+    template void launch_rbgs<T>(const Dims&, int, T*, const T*, cudaStream_t);                          \
+    template void launch_restrict<T>(const Dims&, T*, const T*, cudaStream_t);                           \
+    template void launch_prolong_add<T>(const Dims&, T*, const T*, cudaStream_t);                        \
+    template void launch_prolong_assign<T>(const Dims&, T*, const T*, cudaStream_t);                     \
+    template void launch_coarse_solve<T>(const Dims&, T*, T*, T*, T*, T*, double, int, int*, cudaStream_t);
+
+AFMIB_MG_INST(double)
+AFMIB_MG_INST(float)
+
+}  // namespace afmib

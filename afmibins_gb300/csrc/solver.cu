@@ -1,0 +1,1054 @@
+// afmib solver: host orchestration of the sm_103a kernels behind the C ABI
+// declared in include/afmib.h.
+//
+// One solver owns the device-resident state of one simulation (velocity,
+// projection potential, multigrid hierarchy, CG workspace, markers) and
+// enqueues every kernel on one CUDA stream. Iterative loops keep their
+// scalars on the device; the host reads one convergence scalar per
+// iteration, exactly where the reference tests its stopping criterion.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "afmib.h"
+#include "kernels.h"
+#include "kernels_ib.h"
+
+using namespace afmib;
+
+struct MGLevel {
+    Dims d;
+    double *x, *b, *r;
+};
+
+struct afmib_solver {
+    afmib_config cfg{};
+    Dims d{};
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    std::vector<void*> allocs;
+    std::string err;
+    afmib_stats stats{};
+
+    // FP64 state on MAC faces (v padded to ny planes in channel mode)
+    double *u = nullptr, *v = nullptr, *w = nullptr;
+    double *uo[3] = {}, *adv[3] = {}, *rhs[3] = {}, *f[3] = {};
+    double *divb = nullptr, *walls = nullptr, *wallgrad = nullptr;
+    double *cg_r = nullptr, *cg_p = nullptr, *cg_q = nullptr;
+    double *tmp[3] = {};
+    std::vector<MGLevel> lv;
+    double *cw_p = nullptr, *cw_q = nullptr;
+    RedScratch red{};
+    double* scal = nullptr;   // device scalars: [0..4] CG, [8] sum, [9] sumsq
+    double* hscal = nullptr;  // pinned mirror
+    int* dflag = nullptr;     // device status flags [0] markers, [1] coarse solve
+    int* hflag = nullptr;
+    bool half = false;
+
+    // markers
+    int M = 0, Mcap = 0, nnz_cap = 0;
+    double *X = nullptr, *Xh = nullptr, *U1 = nullptr, *U2 = nullptr, *G = nullptr, *mvol = nullptr;
+    int *nstart = nullptr, *nidx = nullptr;
+    bool has_vol = false;
+    unsigned *keys = nullptr, *keys2 = nullptr, *hist = nullptr;
+    int *vals = nullptr, *vals2 = nullptr, *perm = nullptr;
+    int TS = 0, ntx = 0, nty = 0, ntz = 0, ntiles = 0;
+    int *tstart = nullptr, *tend = nullptr, *tlist = nullptr, *tcount = nullptr;
+    MarkerW<double> mw{};
+
+    // per-kernel event timing (afmib_profile_*): ranges recorded around each
+    // launch while enabled, resolved at the next synchronisation
+    struct ProfEntry { const char* name; long long launches; double ms; double bytes; };
+    struct ProfPending { int id; cudaEvent_t a, b; double bytes; };
+    bool prof = false;
+    std::vector<ProfEntry> prof_tab;
+    std::vector<ProfPending> prof_pend;
+    std::vector<cudaEvent_t> prof_pool;
+
+    int fail(int code, const std::string& msg) {
+        err = msg;
+        return code;
+    }
+    long long N() const { return d.ncell(); }
+    long long nxz() const { return (long long)d.nx * d.nz; }
+    long long nv_user() const { return d.channel ? (long long)d.nx * (d.ny - 1) * d.nz : N(); }
+    double s_plus() const { return cfg.mu * cfg.dt / (2 * cfg.rho); }
+    double s_minus() const { return -cfg.mu * cfg.dt / (2 * cfg.rho); }
+};
+
+namespace {
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) return s->fail(AFMIB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CKL()                                                                                 \
+    do {                                                                                      \
+        cudaError_t e_ = cudaGetLastError();                                                  \
+        if (e_ != cudaSuccess) return s->fail(AFMIB_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define TRY(expr)               \
+    do {                        \
+        int rc_ = (expr);       \
+        if (rc_ != AFMIB_OK) return rc_; \
+    } while (0)
+
+template <typename T>
+int dalloc(afmib_solver* s, T** p, size_t count) {
+    void* q = nullptr;
+    CK(cudaMalloc(&q, (count > 0 ? count : 1) * sizeof(T)));
+    s->allocs.push_back(q);
+    *p = (T*)q;
+    return AFMIB_OK;
+}
+
+bool is_even(int v) { return v % 2 == 0; }
+
+// --- layout conversions between the caller's v (ny-1 interior planes in
+// channel mode) and the padded device v (ny planes, plane 0 = wall) ---------
+int v_in(afmib_solver* s, double* dev_padded, const double* user) {
+    const Dims& d = s->d;
+    if (!d.channel) {
+        CK(cudaMemcpyAsync(dev_padded, user, s->N() * sizeof(double), cudaMemcpyDefault, s->st));
+        return AFMIB_OK;
+    }
+    CK(cudaMemsetAsync(dev_padded, 0, s->N() * sizeof(double), s->st));
+    CK(cudaMemcpy2DAsync(dev_padded + d.nx, (size_t)d.nx * d.ny * sizeof(double), user,
+                         (size_t)d.nx * (d.ny - 1) * sizeof(double), (size_t)d.nx * (d.ny - 1) * sizeof(double),
+                         d.nz, cudaMemcpyDefault, s->st));
+    return AFMIB_OK;
+}
+
+int v_out(afmib_solver* s, double* user, const double* dev_padded) {
+    const Dims& d = s->d;
+    if (!d.channel) {
+        CK(cudaMemcpyAsync(user, dev_padded, s->N() * sizeof(double), cudaMemcpyDefault, s->st));
+        return AFMIB_OK;
+    }
+    CK(cudaMemcpy2DAsync(user, (size_t)d.nx * (d.ny - 1) * sizeof(double), dev_padded + d.nx,
+                         (size_t)d.nx * d.ny * sizeof(double), (size_t)d.nx * (d.ny - 1) * sizeof(double), d.nz,
+                         cudaMemcpyDefault, s->st));
+    return AFMIB_OK;
+}
+
+int copy_in(afmib_solver* s, double* dst, const double* src, long long n) {
+    if (src) CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDefault, s->st));
+    else CK(cudaMemsetAsync(dst, 0, n * sizeof(double), s->st));
+    return AFMIB_OK;
+}
+
+int copy_out(afmib_solver* s, double* dst, const double* src, long long n) {
+    if (dst) CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDefault, s->st));
+    return AFMIB_OK;
+}
+
+void prof_flush(afmib_solver* s);
+
+int sync(afmib_solver* s) {
+    CK(cudaStreamSynchronize(s->st));
+    if (s->prof) prof_flush(s);
+    return AFMIB_OK;
+}
+
+// ---- per-kernel profiling -------------------------------------------------
+enum ProfId {
+    P_ADVECT, P_HELM_RHS, P_CG_INIT, P_CG_APPLY, P_CG_UPDATE, P_CG_DIR, P_RBGS, P_RESID, P_RESID_NORM,
+    P_RESTRICT, P_PROLONG, P_COARSE, P_DIV, P_GRAD_SUB, P_MEAN, P_WALL, P_SPRINGS, P_PREP, P_SORT,
+    P_TILES, P_SPREAD, P_INTERP, P_MARKER, P_COUNT
+};
+const char* kProfNames[P_COUNT] = {
+    "advect", "helm_rhs", "cg_init", "cg_apply", "cg_update", "cg_direction", "mg_rbgs", "mg_residual",
+    "mg_residual_norm", "mg_restrict", "mg_prolong_add", "mg_coarse_cg", "div", "grad_sub", "mean_removal",
+    "wall_update", "springs", "marker_prep", "radix_sort", "tile_bins", "spread_gather", "interp", "marker_update"};
+
+cudaEvent_t prof_event(afmib_solver* s) {
+    if (!s->prof_pool.empty()) {
+        cudaEvent_t e = s->prof_pool.back();
+        s->prof_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void prof_flush(afmib_solver* s) {
+    for (auto& p : s->prof_pend) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            auto& e = s->prof_tab[p.id];
+            e.launches++;
+            e.ms += ms;
+            e.bytes += p.bytes;
+        }
+        s->prof_pool.push_back(p.a);
+        s->prof_pool.push_back(p.b);
+    }
+    s->prof_pend.clear();
+}
+
+// Brackets one (or a fixed group of) kernel launch(es) with events when
+// profiling is on; counts the launches either way.
+struct ProfScope {
+    afmib_solver* s;
+    int id;
+    double bytes;
+    cudaEvent_t a = nullptr;
+    ProfScope(afmib_solver* s_, int id_, double bytes_, int launches = 1) : s(s_), id(id_), bytes(bytes_) {
+        s->stats.kernel_launches += launches;
+        if (s->prof) {
+            a = prof_event(s);
+            cudaEventRecord(a, s->st);
+        }
+    }
+    ~ProfScope() {
+        if (s->prof && a) {
+            cudaEvent_t b = prof_event(s);
+            cudaEventRecord(b, s->st);
+            s->prof_pend.push_back({id, a, b, bytes});
+        }
+    }
+};
+
+// read n doubles of the device scalar block into the pinned mirror
+int read_scalars(afmib_solver* s, int first, int n) {
+    CK(cudaMemcpyAsync(s->hscal + first, s->scal + first, n * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    return sync(s);
+}
+
+// ---------------------------------------------------------------------------
+// CG, src/alg/cg.h:32-56 (absolute 2-norm stop, warm start from x), bounded.
+// Algorithmic bytes per launch (s = 8): init 4N s, apply 2N s, update 6N s,
+// direction 3N s.
+// ---------------------------------------------------------------------------
+int cg_solve(afmib_solver* s, int comp, double scale, double* x, const double* b, int* iters) {
+    const Dims& d = s->d;
+    const long long N = s->N();
+    const double Ns = (double)N * sizeof(double);
+    {
+        ProfScope ps(s, P_CG_INIT, 4 * Ns);
+        launch_cg_init<double>(d, comp, scale, x, b, s->cg_r, s->cg_p, s->red, s->scal, s->st);
+    }
+    CKL();
+    TRY(read_scalars(s, 0, 1));
+    int it = 0;
+    int status = AFMIB_OK;
+    while (std::sqrt(s->hscal[0]) > s->cfg.tol) {
+        if (!std::isfinite(s->hscal[0])) { status = s->fail(AFMIB_ERR_NAN, "CG residual is not finite"); break; }
+        if (it >= s->cfg.max_cg_iters) { status = s->fail(AFMIB_ERR_NOCONV, "CG iteration cap reached"); break; }
+        {
+            ProfScope ps(s, P_CG_APPLY, 2 * Ns);
+            launch_cg_apply<double>(d, comp, scale, s->cg_p, s->cg_q, s->red, s->scal, s->st);
+        }
+        {
+            ProfScope ps(s, P_CG_UPDATE, 6 * Ns);
+            launch_cg_update<double>(N, x, s->cg_r, s->cg_p, s->cg_q, s->red, s->scal, s->st);
+        }
+        CK(cudaMemcpyAsync(s->hscal, s->scal, sizeof(double), cudaMemcpyDeviceToHost, s->st));
+        {
+            ProfScope ps(s, P_CG_DIR, 3 * Ns);
+            launch_cg_direction<double>(N, s->cg_p, s->cg_r, s->scal, s->st);
+        }
+        CKL();
+        TRY(sync(s));
+        ++it;
+    }
+    s->stats.cg_iters += it;
+    s->stats.last_cg_norm = std::sqrt(s->hscal[0]);
+    if (iters) *iters = it;
+    return status;
+}
+
+// ---------------------------------------------------------------------------
+// Multigrid, src/mg/solver.h. V(nu1, nu2) cycles with red-black Gauss–Seidel,
+// the reference's full-weighting restriction and trilinear prolongation, and
+// the coarsest level solved by mean removal + CG (src/mg/solver.h:264-271).
+// Algorithmic bytes: a full red+black sweep reads x and b and writes x once
+// (3N s, so 1.5N s per colour launch); residual 3N s; restriction N s + N/8 s;
+// prolongation-add 2N s + N/8 s.
+// ---------------------------------------------------------------------------
+int smooth(afmib_solver* s, MGLevel& L, int sweeps) {
+    const double Ns = (double)L.d.ncell() * sizeof(double);
+    for (int j = 0; j < sweeps; ++j) {
+        {
+            ProfScope ps(s, P_RBGS, 1.5 * Ns);
+            launch_rbgs<double>(L.d, 0, L.x, L.b, s->st);
+        }
+        {
+            ProfScope ps(s, P_RBGS, 1.5 * Ns);
+            launch_rbgs<double>(L.d, 1, L.x, L.b, s->st);
+        }
+    }
+    CKL();
+    return AFMIB_OK;
+}
+
+int vcycle(afmib_solver* s, size_t l) {
+    MGLevel& L = s->lv[l];
+    const double Ns = (double)L.d.ncell() * sizeof(double);
+    if (l + 1 == s->lv.size()) {
+        {
+            ProfScope ps(s, P_COARSE, 3 * Ns);
+            launch_coarse_solve<double>(L.d, L.x, L.b, L.r, s->cw_p, s->cw_q, s->cfg.tol, s->cfg.max_cg_iters,
+                                        s->dflag + 1, s->st);
+        }
+        CKL();
+        return AFMIB_OK;
+    }
+    TRY(smooth(s, L, s->cfg.nu1));
+    {
+        ProfScope ps(s, P_RESID, 3 * Ns);
+        launch_residual<double>(L.d, L.r, L.x, L.b, nullptr, nullptr, s->st);
+    }
+    MGLevel& C = s->lv[l + 1];
+    {
+        ProfScope ps(s, P_RESTRICT, Ns + Ns / 8);
+        launch_restrict<double>(L.d, C.b, L.r, s->st);
+    }
+    CK(cudaMemsetAsync(C.x, 0, C.d.ncell() * sizeof(double), s->st));
+    CKL();
+    TRY(vcycle(s, l + 1));
+    {
+        ProfScope ps(s, P_PROLONG, 2 * Ns + Ns / 8);
+        launch_prolong_add<double>(L.d, L.x, C.x, s->st);
+    }
+    TRY(smooth(s, L, s->cfg.nu2));
+    return AFMIB_OK;
+}
+
+// Solve L x = b on level 0 (b in lv[0].b, destroyed; x in lv[0].x), the
+// reference's solve loop: remove the mean of b, then cycle until
+// RMS(b - L x) <= tol (src/mg/solver.h:218-237).
+int mg_solve(afmib_solver* s, int* cycles) {
+    MGLevel& L = s->lv[0];
+    const long long N = L.d.ncell();
+    const double Ns = (double)N * sizeof(double);
+    {
+        ProfScope ps(s, P_MEAN, 3 * Ns, 2);
+        launch_sum<double>(N, L.b, s->red, s->scal + 8, s->st);
+        launch_sub_scalar_scaled<double>(N, L.b, s->scal + 8, 1.0 / (double)N, s->st);
+    }
+    CK(cudaMemsetAsync(L.x, 0, N * sizeof(double), s->st));
+    CK(cudaMemsetAsync(s->dflag + 1, 0, sizeof(int), s->st));
+    int status = AFMIB_OK;
+    int c = 0;
+    if (s->lv.size() == 1) {
+        TRY(vcycle(s, 0));
+    } else {
+        for (;;) {
+            {
+                ProfScope ps(s, P_RESID_NORM, 3 * Ns);
+                launch_residual<double>(L.d, L.r, L.x, L.b, &s->red, s->scal + 9, s->st);
+            }
+            CKL();
+            TRY(read_scalars(s, 9, 1));
+            const double rms = std::sqrt(s->hscal[9]) / std::sqrt((double)N);
+            s->stats.last_mg_rms = rms;
+            if (!std::isfinite(rms)) { status = s->fail(AFMIB_ERR_NAN, "multigrid residual is not finite"); break; }
+            if (rms <= s->cfg.tol) break;
+            if (c >= s->cfg.max_mg_cycles) { status = s->fail(AFMIB_ERR_NOCONV, "multigrid cycle cap reached"); break; }
+            TRY(vcycle(s, 0));
+            ++c;
+        }
+    }
+    CK(cudaMemcpyAsync(s->hflag + 1, s->dflag + 1, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    TRY(sync(s));
+    if (status == AFMIB_OK && s->hflag[1] != 0) status = s->fail(AFMIB_ERR_NOCONV, "coarsest-level CG did not converge");
+    s->stats.mg_cycles += c;
+    if (cycles) *cycles = c;
+    return status;
+}
+
+// ns::projection::project, src/ns/projection.h:60-73
+int project(afmib_solver* s) {
+    const double Ns = (double)s->N() * sizeof(double);
+    {
+        ProfScope ps(s, P_DIV, 4 * Ns);
+        launch_div<double>(s->d, s->lv[0].b, s->u, s->v, s->w, nullptr, nullptr, s->st);
+    }
+    CKL();
+    TRY(mg_solve(s, nullptr));
+    {
+        ProfScope ps(s, P_GRAD_SUB, 7 * Ns);
+        launch_grad_sub<double>(s->d, s->u, s->v, s->w, s->lv[0].x, s->d.channel ? s->wallgrad : nullptr, s->st);
+    }
+    CKL();
+    return AFMIB_OK;
+}
+
+// ns::solver::step, src/ns/solver.h:90-140; forces already in s->f.
+int substep(afmib_solver* s) {
+    const Dims& d = s->d;
+    const long long N = s->N();
+    const double Ns = (double)N * sizeof(double);
+    {
+        ProfScope ps(s, P_ADVECT, 6 * Ns);
+        launch_advect<double>(d, s->adv[0], s->adv[1], s->adv[2], s->u, s->v, s->w, s->st);
+    }
+    CKL();
+    const bool be = !s->half;
+    if (be) {
+        CK(cudaMemcpyAsync(s->uo[0], s->u, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+        CK(cudaMemcpyAsync(s->uo[1], s->v, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+        CK(cudaMemcpyAsync(s->uo[2], s->w, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+    }
+    if (d.channel) {
+        ProfScope ps(s, P_WALL, 10.0 * s->nxz() * sizeof(double));
+        launch_wall_update(d, s->walls, s->wallgrad, s->st);
+    }
+    const long long nxz = s->nxz();
+    const double* ut = s->walls;
+    const double* ub = s->walls + nxz;
+    const double* wt = s->walls + 2 * nxz;
+    const double* wb = s->walls + 3 * nxz;
+    const double inv_rho = 1 / s->cfg.rho;
+    for (int c = 0; c < 3; ++c) {
+        const double* top = (!d.channel || c == 1) ? nullptr : (c == 0 ? ut : wt);
+        const double* bot = (!d.channel || c == 1) ? nullptr : (c == 0 ? ub : wb);
+        ProfScope ps(s, P_HELM_RHS, 4 * Ns);
+        launch_helm_rhs<double>(d, c, be ? 1 : 0, s->rhs[c], s->uo[c], s->f[c], s->adv[c], top, bot, s->s_plus(),
+                                s->s_minus(), s->cfg.dt, inv_rho, s->st);
+    }
+    CKL();
+    double* vel[3] = {s->u, s->v, s->w};
+    for (int c = 0; c < 3; ++c) TRY(cg_solve(s, c, s->s_minus(), vel[c], s->rhs[c], nullptr));
+    TRY(project(s));
+    s->half = !s->half;
+    s->stats.half = s->half ? 1 : 0;
+    s->stats.substeps++;
+    return AFMIB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Immersed boundary
+// ---------------------------------------------------------------------------
+// (re)allocate a device buffer, keeping the first `keep` elements
+template <typename T>
+int regrow(afmib_solver* s, T** p, size_t count, size_t keep) {
+    T* q = nullptr;
+    TRY(dalloc(s, &q, count));
+    if (*p) {
+        if (keep) CK(cudaMemcpyAsync(q, *p, keep * sizeof(T), cudaMemcpyDeviceToDevice, s->st));
+        CK(cudaStreamSynchronize(s->st));
+        for (auto& a : s->allocs)
+            if (a == (void*)*p) { cudaFree(a); a = nullptr; }
+    }
+    *p = q;
+    return AFMIB_OK;
+}
+
+// Grow the marker buffers to M markers and nnz neighbour entries. The
+// solver's own marker set (X, nstart, nidx, vol) survives a growth; the
+// other buffers are per-call workspace.
+int marker_alloc(afmib_solver* s, int M, int nnz) {
+    if (M > s->Mcap) {
+        const size_t keep = (size_t)s->M;
+        TRY(regrow(s, &s->X, 3 * (size_t)M, 3 * keep));
+        TRY(regrow(s, &s->nstart, (size_t)M + 1, keep ? keep + 1 : 0));
+        TRY(regrow(s, &s->mvol, (size_t)M, keep));
+        TRY(regrow(s, &s->Xh, 3 * (size_t)M, 0));
+        TRY(regrow(s, &s->U1, 3 * (size_t)M, 0));
+        TRY(regrow(s, &s->U2, 3 * (size_t)M, 0));
+        TRY(regrow(s, &s->G, 3 * (size_t)M, 0));
+        TRY(regrow(s, &s->keys, (size_t)M, 0));
+        TRY(regrow(s, &s->keys2, (size_t)M, 0));
+        TRY(regrow(s, &s->vals, (size_t)M, 0));
+        TRY(regrow(s, &s->vals2, (size_t)M, 0));
+        TRY(regrow(s, &s->hist, radix_sort_temp_bytes(M) / sizeof(unsigned) + 256, 0));
+        TRY(regrow(s, &s->mw.cell, 3 * (size_t)M, 0));
+        TRY(regrow(s, &s->mw.dbase, 6 * (size_t)M, 0));
+        TRY(regrow(s, &s->mw.w, 24 * (size_t)M, 0));
+        s->Mcap = M;
+    }
+    if (nnz > s->nnz_cap) {
+        TRY(regrow(s, &s->nidx, (size_t)nnz, 0));
+        s->nnz_cap = nnz;
+    }
+    return AFMIB_OK;
+}
+
+int key_bits(afmib_solver* s) {
+    const unsigned long long top = (unsigned long long)s->ntiles * s->TS * s->TS * s->TS;
+    int b = 0;
+    while ((1ull << b) < top) ++b;
+    return b;
+}
+
+// weights + bins of the markers at P (device, [M][3])
+int bin_markers(afmib_solver* s, const double* P) {
+    const int M = s->M;
+    const int passes = (key_bits(s) + 7) / 8;
+    {
+        ProfScope ps(s, P_PREP, (double)M * (24 + 4 + 4 + 12 + 6 + 24 * 8));
+        launch_marker_prep<double>(s->d, s->TS, M, P, s->keys, s->vals, s->mw, s->dflag, s->st);
+    }
+    unsigned* ko;
+    int* vo;
+    {
+        ProfScope ps(s, P_SORT, (double)passes * M * 16, 3 * passes);
+        radix_sort_pairs(s->keys, s->vals, s->keys2, s->vals2, M, key_bits(s), s->hist, &ko, &vo, s->st);
+    }
+    s->perm = vo;
+    CK(cudaMemsetAsync(s->tstart, 0, s->ntiles * sizeof(int), s->st));
+    CK(cudaMemsetAsync(s->tend, 0, s->ntiles * sizeof(int), s->st));
+    CK(cudaMemsetAsync(s->tcount, 0, sizeof(int), s->st));
+    {
+        ProfScope ps(s, P_TILES, (double)M * 4 + 3.0 * s->ntiles * 4, 2);
+        launch_tile_ranges(ko, M, s->TS * s->TS * s->TS, s->tstart, s->tend, s->st);
+        launch_active_tiles(s->ntx, s->nty, s->ntz, s->d.channel, s->tstart, s->tend, s->tlist, s->tcount, s->st);
+    }
+    CKL();
+    return AFMIB_OK;
+}
+
+// f = spread(G) with the bins and weights of the last bin_markers call.
+// Algorithmic bytes: M (24 + 3s + 8 + 8) + 3 N_touched s with N_touched
+// taken as the faces of the active tiles (from the previous spreading).
+int spread_forces(afmib_solver* s, const double* vol, double* fu, double* fv, double* fw) {
+    const long long N = s->N();
+    CK(cudaMemsetAsync(fu, 0, N * sizeof(double), s->st));
+    CK(cudaMemsetAsync(fv, 0, N * sizeof(double), s->st));
+    CK(cudaMemsetAsync(fw, 0, N * sizeof(double), s->st));
+    const double n3 = (double)s->d.n * s->d.n * s->d.n;
+    const int cap = 1536;
+    const double touched = (double)s->stats.spread_tiles * s->TS * s->TS * s->TS;
+    {
+        ProfScope ps(s, P_SPREAD, (double)s->M * (24 + 3 * 8 + 8 + 8) + 3 * touched * 8);
+        launch_spread_gather<double>(s->d, s->TS, s->M, s->perm, s->mw, s->G, vol, n3, s->tstart, s->tend, s->tlist,
+                                     s->tcount, s->ntiles, cap, fu, fv, fw, s->dflag, s->st);
+    }
+    CKL();
+    return AFMIB_OK;
+}
+
+int check_marker_flag(afmib_solver* s) {
+    CK(cudaMemcpyAsync(s->hflag, s->dflag, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaMemcpyAsync(s->hflag + 2, s->tcount, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    TRY(sync(s));
+    s->stats.spread_tiles = s->hflag[2];
+    const int f = s->hflag[0];
+    if (f == 1) return s->fail(AFMIB_ERR_BOUNDS, "a marker came within 2.5h of a channel wall");
+    if (f == 2) return s->fail(AFMIB_ERR_NAN, "a marker position is not finite");
+    if (f == 3) return s->fail(AFMIB_ERR_CAPACITY, "too many markers near one spreading tile");
+    return AFMIB_OK;
+}
+
+int interp_markers(afmib_solver* s, const double* u, const double* v, const double* w, double* U) {
+    const double touched = (double)s->stats.spread_tiles * s->TS * s->TS * s->TS;
+    ProfScope ps(s, P_INTERP, 3 * touched * 8 + (double)s->M * (24 + 3 * 8 + 8));
+    launch_interp<double>(s->d, s->M, s->perm, s->mw, u, v, w, U, s->st);
+    return AFMIB_OK;
+}
+
+int ib_one_step(afmib_solver* s) {
+    const int M = s->M;
+    const double dt = s->cfg.dt;
+    const double* vol = s->has_vol ? s->mvol : nullptr;
+    const double mbytes = (double)M * (24 + 24 + 24);
+    CK(cudaMemsetAsync(s->dflag, 0, sizeof(int), s->st));
+    // BE half: forces at X^n
+    {
+        ProfScope ps(s, P_SPRINGS, mbytes);
+        launch_springs<double>(M, s->X, s->nstart, s->nidx, s->cfg.k_spring, s->G, s->st);
+    }
+    TRY(bin_markers(s, s->X));
+    TRY(spread_forces(s, vol, s->f[0], s->f[1], s->f[2]));
+    TRY(substep(s));
+    // velocity at t+dt/2: at X^n for the half-step, then at X^{n+1/2}
+    TRY(interp_markers(s, s->u, s->v, s->w, s->U1));
+    {
+        ProfScope ps(s, P_MARKER, mbytes);
+        launch_marker_axpy(M, s->Xh, s->X, s->U1, dt / 2, s->st);
+    }
+    TRY(bin_markers(s, s->Xh));
+    TRY(interp_markers(s, s->u, s->v, s->w, s->U2));
+    // CN step with forces at X^{n+1/2}
+    {
+        ProfScope ps(s, P_SPRINGS, mbytes);
+        launch_springs<double>(M, s->Xh, s->nstart, s->nidx, s->cfg.k_spring, s->G, s->st);
+    }
+    CKL();
+    TRY(spread_forces(s, vol, s->f[0], s->f[1], s->f[2]));
+    TRY(substep(s));
+    {
+        ProfScope ps(s, P_MARKER, mbytes);
+        launch_marker_axpy(M, s->X, s->X, s->U2, dt, s->st);
+    }
+    CKL();
+    TRY(check_marker_flag(s));
+    s->stats.ib_steps++;
+    return AFMIB_OK;
+}
+
+int setup_tiles(afmib_solver* s) {
+    const Dims& d = s->d;
+    auto ok = [&](int ts) {
+        return d.nx % ts == 0 && d.ny % ts == 0 && d.nz % ts == 0 && d.nx >= ts + 4 && d.ny >= ts + 4 && d.nz >= ts + 4;
+    };
+    if (ok(8)) s->TS = 8;
+    else if (ok(4)) s->TS = 4;
+    else return s->fail(AFMIB_ERR_ARG, "immersed boundary needs every extent a multiple of 4 and at least 8 cells");
+    s->ntx = d.nx / s->TS;
+    s->nty = d.ny / s->TS;
+    s->ntz = d.nz / s->TS;
+    s->ntiles = s->ntx * s->nty * s->ntz;
+    TRY(dalloc(s, &s->tstart, s->ntiles));
+    TRY(dalloc(s, &s->tend, s->ntiles));
+    TRY(dalloc(s, &s->tlist, s->ntiles));
+    TRY(dalloc(s, &s->tcount, 1));
+    return AFMIB_OK;
+}
+
+int create(afmib_solver* s, const afmib_config* c, void* stream) {
+    s->cfg = *c;
+    afmib_config& g = s->cfg;
+    if (g.n <= 0) g.n = g.nx;
+    if (g.nu1 <= 0) g.nu1 = 2;
+    if (g.nu2 <= 0) g.nu2 = 2;
+    if (g.max_cg_iters <= 0) g.max_cg_iters = 1000;
+    if (g.max_mg_cycles <= 0) g.max_mg_cycles = 200;
+    if (g.inner_tol <= 0) g.inner_tol = 1e-5;
+    if (g.nx < 2 || g.ny < 2 || g.nz < 2) return s->fail(AFMIB_ERR_ARG, "every extent must be at least 2 cells");
+    if (g.bc != AFMIB_BC_PERIODIC && g.bc != AFMIB_BC_CHANNEL) return s->fail(AFMIB_ERR_ARG, "bc must be periodic or channel");
+    if (g.precision != AFMIB_FP64) return s->fail(AFMIB_ERR_ARG, "only the FP64 form is available in this build");
+    if (!(g.rho > 0) || !(g.dt > 0) || !(g.mu >= 0) || !(g.tol > 0)) return s->fail(AFMIB_ERR_ARG, "mu, rho, dt, tol");
+    s->d = Dims{g.nx, g.ny, g.nz, g.n, g.bc == AFMIB_BC_CHANNEL ? 1 : 0};
+    if (stream) {
+        s->st = (cudaStream_t)stream;
+    } else {
+        CK(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+        s->own_stream = true;
+    }
+    const long long N = s->N();
+    TRY(dalloc(s, &s->u, N));
+    TRY(dalloc(s, &s->v, N));
+    TRY(dalloc(s, &s->w, N));
+    for (int k = 0; k < 3; ++k) {
+        TRY(dalloc(s, &s->uo[k], N));
+        TRY(dalloc(s, &s->adv[k], N));
+        TRY(dalloc(s, &s->rhs[k], N));
+        TRY(dalloc(s, &s->f[k], N));
+        TRY(dalloc(s, &s->tmp[k], N));
+    }
+    TRY(dalloc(s, &s->divb, N));
+    TRY(dalloc(s, &s->walls, 4 * s->nxz()));
+    TRY(dalloc(s, &s->wallgrad, 6 * s->nxz()));
+    TRY(dalloc(s, &s->cg_r, N));
+    TRY(dalloc(s, &s->cg_p, N));
+    TRY(dalloc(s, &s->cg_q, N));
+    TRY(dalloc(s, &s->red.partial, (size_t)kMaxRedBlocks * kMaxRedVals));
+    TRY(dalloc(s, &s->red.ticket, 1));
+    TRY(dalloc(s, &s->scal, 16));
+    TRY(dalloc(s, &s->dflag, 4));
+    CK(cudaMallocHost((void**)&s->hscal, 16 * sizeof(double)));
+    CK(cudaMallocHost((void**)&s->hflag, 4 * sizeof(int)));
+    CK(cudaMemsetAsync(s->red.ticket, 0, sizeof(unsigned), s->st));
+    CK(cudaMemsetAsync(s->dflag, 0, 4 * sizeof(int), s->st));
+    CK(cudaMemsetAsync(s->walls, 0, 4 * s->nxz() * sizeof(double), s->st));
+    CK(cudaMemsetAsync(s->wallgrad, 0, 6 * s->nxz() * sizeof(double), s->st));
+    CK(cudaMemsetAsync(s->u, 0, N * sizeof(double), s->st));
+    CK(cudaMemsetAsync(s->v, 0, N * sizeof(double), s->st));
+    CK(cudaMemsetAsync(s->w, 0, N * sizeof(double), s->st));
+    for (int k = 0; k < 3; ++k) CK(cudaMemsetAsync(s->f[k], 0, N * sizeof(double), s->st));
+
+    // multigrid hierarchy
+    int levels = g.mg_levels;
+    if (levels <= 0) {
+        levels = 0;
+        Dims t = s->d;
+        while (is_even(t.nx) && is_even(t.ny) && is_even(t.nz) && t.nx >= 2 && t.ny >= 2 && t.nz >= 2) {
+            t.nx /= 2; t.ny /= 2; t.nz /= 2; t.n /= 2;
+            ++levels;
+            if (t.nx == 1 || t.ny == 1 || t.nz == 1) break;
+        }
+    }
+    Dims t = s->d;
+    for (int l = 0; l <= levels; ++l) {
+        if (l > 0) {
+            if (!is_even(t.nx) || !is_even(t.ny) || !is_even(t.nz))
+                return s->fail(AFMIB_ERR_ARG, "mg_levels exceeds the number of halvings of the grid");
+            t.nx /= 2; t.ny /= 2; t.nz /= 2; t.n = t.n / 2 > 0 ? t.n / 2 : 1;
+        }
+        MGLevel L{t, nullptr, nullptr, nullptr};
+        const long long n = t.ncell();
+        TRY(dalloc(s, &L.x, n));
+        TRY(dalloc(s, &L.b, n));
+        TRY(dalloc(s, &L.r, n));
+        s->lv.push_back(L);
+    }
+    // smoothed levels need even extents for the red-black colouring
+    for (size_t l = 0; l + 1 < s->lv.size(); ++l) {
+        const Dims& q = s->lv[l].d;
+        if (!is_even(q.nx)) return s->fail(AFMIB_ERR_ARG, "smoothed multigrid levels need an even x extent");
+    }
+    const long long nc = s->lv.back().d.ncell();
+    TRY(dalloc(s, &s->cw_p, nc));
+    TRY(dalloc(s, &s->cw_q, nc));
+    CK(cudaStreamSynchronize(s->st));
+    return AFMIB_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* afmib_error_string(int status) {
+    switch (status) {
+        case AFMIB_OK: return "ok";
+        case AFMIB_ERR_ARG: return "invalid argument";
+        case AFMIB_ERR_CUDA: return "CUDA error";
+        case AFMIB_ERR_NOCONV: return "iteration cap reached";
+        case AFMIB_ERR_BOUNDS: return "marker too close to a wall";
+        case AFMIB_ERR_NAN: return "non-finite value";
+        case AFMIB_ERR_STATE: return "call out of order";
+        case AFMIB_ERR_CAPACITY: return "too many markers near one tile";
+        default: return "unknown status";
+    }
+}
+
+const char* afmib_last_error(const afmib_solver* s) { return s ? s->err.c_str() : "null solver"; }
+
+int afmib_create(const afmib_config* cfg, void* stream, afmib_solver** out) {
+    if (!cfg || !out) return AFMIB_ERR_ARG;
+    afmib_solver* s = new afmib_solver();
+    const int rc = create(s, cfg, stream);
+    *out = s;  // returned even on failure so that afmib_last_error can be read
+    return rc;
+}
+
+int afmib_destroy(afmib_solver* s) {
+    if (!s) return AFMIB_OK;
+    if (s->st) cudaStreamSynchronize(s->st);
+    for (void* p : s->allocs)
+        if (p) cudaFree(p);
+    for (auto& p : s->prof_pend) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+    for (auto e : s->prof_pool) cudaEventDestroy(e);
+    if (s->hscal) cudaFreeHost(s->hscal);
+    if (s->hflag) cudaFreeHost(s->hflag);
+    if (s->own_stream && s->st) cudaStreamDestroy(s->st);
+    delete s;
+    return AFMIB_OK;
+}
+
+int afmib_get_stats(const afmib_solver* s, afmib_stats* out) {
+    if (!s || !out) return AFMIB_ERR_ARG;
+    *out = s->stats;
+    return AFMIB_OK;
+}
+
+int afmib_synchronize(afmib_solver* s) {
+    if (!s) return AFMIB_ERR_ARG;
+    return sync(s);
+}
+
+int afmib_set_velocity(afmib_solver* s, const double* u, const double* v, const double* w) {
+    if (!s) return AFMIB_ERR_ARG;
+    TRY(copy_in(s, s->u, u, s->N()));
+    if (v) TRY(v_in(s, s->v, v));
+    else CK(cudaMemsetAsync(s->v, 0, s->N() * sizeof(double), s->st));
+    TRY(copy_in(s, s->w, w, s->N()));
+    return sync(s);
+}
+
+int afmib_get_velocity(afmib_solver* s, double* u, double* v, double* w) {
+    if (!s) return AFMIB_ERR_ARG;
+    TRY(copy_out(s, u, s->u, s->N()));
+    if (v) TRY(v_out(s, v, s->v));
+    TRY(copy_out(s, w, s->w, s->N()));
+    return sync(s);
+}
+
+int afmib_get_pressure(afmib_solver* s, double* p) {
+    if (!s || !p) return AFMIB_ERR_ARG;
+    launch_helm_apply<double>(s->d, 0, s->s_minus(), s->tmp[0], s->lv[0].x, s->st);
+    CKL();
+    TRY(copy_out(s, p, s->tmp[0], s->N()));
+    return sync(s);
+}
+
+int afmib_set_walls(afmib_solver* s, const double* ut, const double* ub, const double* wt, const double* wb) {
+    if (!s) return AFMIB_ERR_ARG;
+    const long long n = s->nxz();
+    TRY(copy_in(s, s->walls, ut, n));
+    TRY(copy_in(s, s->walls + n, ub, n));
+    TRY(copy_in(s, s->walls + 2 * n, wt, n));
+    TRY(copy_in(s, s->walls + 3 * n, wb, n));
+    return sync(s);
+}
+
+int afmib_get_walls(afmib_solver* s, double* ut, double* ub, double* wt, double* wb) {
+    if (!s) return AFMIB_ERR_ARG;
+    const long long n = s->nxz();
+    TRY(copy_out(s, ut, s->walls, n));
+    TRY(copy_out(s, ub, s->walls + n, n));
+    TRY(copy_out(s, wt, s->walls + 2 * n, n));
+    TRY(copy_out(s, wb, s->walls + 3 * n, n));
+    return sync(s);
+}
+
+int afmib_project(afmib_solver* s) {
+    if (!s) return AFMIB_ERR_ARG;
+    TRY(project(s));
+    return sync(s);
+}
+
+int afmib_ns_step(afmib_solver* s, const double* fx, const double* fy, const double* fz) {
+    if (!s) return AFMIB_ERR_ARG;
+    TRY(copy_in(s, s->f[0], fx, s->N()));
+    if (fy) TRY(v_in(s, s->f[1], fy));
+    else CK(cudaMemsetAsync(s->f[1], 0, s->N() * sizeof(double), s->st));
+    TRY(copy_in(s, s->f[2], fz, s->N()));
+    TRY(substep(s));
+    return sync(s);
+}
+
+int afmib_set_markers(afmib_solver* s, int M, const double* X, const int* nstart, const int* nidx, const double* vol) {
+    if (!s || M < 0 || (M > 0 && !X)) return AFMIB_ERR_ARG;
+    if (!s->TS) TRY(setup_tiles(s));
+    int nnz = 0;
+    std::vector<int> hstart;
+    if (nstart) {
+        hstart.resize(M + 1);
+        CK(cudaMemcpy(hstart.data(), nstart, (M + 1) * sizeof(int), cudaMemcpyDefault));
+        nnz = hstart[M];
+        if (hstart[0] != 0 || nnz < 0) return s->fail(AFMIB_ERR_ARG, "nstart must start at 0");
+        for (int i = 0; i < M; ++i)
+            if (hstart[i + 1] < hstart[i]) return s->fail(AFMIB_ERR_ARG, "nstart must be non-decreasing");
+        if (nnz > 0 && !nidx) return s->fail(AFMIB_ERR_ARG, "nidx missing");
+        if (nnz > 0) {
+            std::vector<int> hidx(nnz);
+            CK(cudaMemcpy(hidx.data(), nidx, nnz * sizeof(int), cudaMemcpyDefault));
+            for (int e = 0; e < nnz; ++e)
+                if (hidx[e] < 0 || hidx[e] >= M) return s->fail(AFMIB_ERR_ARG, "neighbour index out of range");
+        }
+    }
+    TRY(marker_alloc(s, M, nnz));
+    s->M = M;
+    TRY(copy_in(s, s->X, X, 3 * (long long)M));
+    if (nstart) {
+        CK(cudaMemcpyAsync(s->nstart, hstart.data(), (M + 1) * sizeof(int), cudaMemcpyHostToDevice, s->st));
+        if (nnz > 0) CK(cudaMemcpyAsync(s->nidx, nidx, nnz * sizeof(int), cudaMemcpyDefault, s->st));
+    } else {
+        CK(cudaMemsetAsync(s->nstart, 0, (M + 1) * sizeof(int), s->st));
+    }
+    s->has_vol = vol != nullptr;
+    if (vol) TRY(copy_in(s, s->mvol, vol, M));
+    return sync(s);
+}
+
+int afmib_set_marker_positions(afmib_solver* s, const double* X) {
+    if (!s || !X) return AFMIB_ERR_ARG;
+    if (s->M <= 0) return s->fail(AFMIB_ERR_STATE, "no markers set");
+    TRY(copy_in(s, s->X, X, 3 * (long long)s->M));
+    return AFMIB_OK;
+}
+
+int afmib_get_markers(afmib_solver* s, double* X) {
+    if (!s || !X) return AFMIB_ERR_ARG;
+    TRY(copy_out(s, X, s->X, 3 * (long long)s->M));
+    return sync(s);
+}
+
+int afmib_ib_step(afmib_solver* s, int nsteps) {
+    if (!s) return AFMIB_ERR_ARG;
+    if (s->M <= 0) return s->fail(AFMIB_ERR_STATE, "no markers set");
+    for (int k = 0; k < nsteps; ++k) TRY(ib_one_step(s));
+    return AFMIB_OK;
+}
+
+// ---- single operators ------------------------------------------------------
+
+int afmib_div(afmib_solver* s, double* dout, const double* u, const double* v, const double* w, const double* top,
+              const double* bottom) {
+    if (!s || !dout || !u || !v || !w) return AFMIB_ERR_ARG;
+    const long long N = s->N(), nxz = s->nxz();
+    TRY(copy_in(s, s->tmp[0], u, N));
+    TRY(v_in(s, s->tmp[1], v));
+    TRY(copy_in(s, s->tmp[2], w, N));
+    TRY(copy_in(s, s->adv[0], top, nxz));
+    TRY(copy_in(s, s->adv[1], bottom, nxz));
+    launch_div<double>(s->d, s->divb, s->tmp[0], s->tmp[1], s->tmp[2], s->adv[0], s->adv[1], s->st);
+    CKL();
+    TRY(copy_out(s, dout, s->divb, N));
+    return sync(s);
+}
+
+int afmib_grad(afmib_solver* s, double* px, double* py, double* pz, const double* p) {
+    if (!s || !px || !py || !pz || !p) return AFMIB_ERR_ARG;
+    const long long N = s->N();
+    TRY(copy_in(s, s->divb, p, N));
+    CK(cudaMemsetAsync(s->tmp[1], 0, N * sizeof(double), s->st));
+    launch_grad<double>(s->d, s->tmp[0], s->tmp[1], s->tmp[2], s->divb, s->st);
+    CKL();
+    TRY(copy_out(s, px, s->tmp[0], N));
+    TRY(v_out(s, py, s->tmp[1]));
+    TRY(copy_out(s, pz, s->tmp[2], N));
+    return sync(s);
+}
+
+int afmib_advection(afmib_solver* s, double* ua, double* va, double* wa, const double* u, const double* v,
+                    const double* w) {
+    if (!s || !ua || !va || !wa || !u || !v || !w) return AFMIB_ERR_ARG;
+    const long long N = s->N();
+    TRY(copy_in(s, s->tmp[0], u, N));
+    TRY(v_in(s, s->tmp[1], v));
+    TRY(copy_in(s, s->tmp[2], w, N));
+    launch_advect<double>(s->d, s->rhs[0], s->rhs[1], s->rhs[2], s->tmp[0], s->tmp[1], s->tmp[2], s->st);
+    CKL();
+    TRY(copy_out(s, ua, s->rhs[0], N));
+    TRY(v_out(s, va, s->rhs[1]));
+    TRY(copy_out(s, wa, s->rhs[2], N));
+    return sync(s);
+}
+
+int afmib_mg_solve(afmib_solver* s, double* rhs, int* cycles) {
+    if (!s || !rhs) return AFMIB_ERR_ARG;
+    TRY(copy_in(s, s->lv[0].b, rhs, s->N()));
+    const int rc = mg_solve(s, cycles);
+    TRY(copy_out(s, rhs, s->lv[0].x, s->N()));
+    TRY(sync(s));
+    return rc;
+}
+
+int afmib_lap_apply(afmib_solver* s, double* y, const double* x) {
+    if (!s || !y || !x) return AFMIB_ERR_ARG;
+    TRY(copy_in(s, s->tmp[0], x, s->N()));
+    launch_lap_apply<double>(s->d, s->tmp[1], s->tmp[0], s->st);
+    CKL();
+    TRY(copy_out(s, y, s->tmp[1], s->N()));
+    return sync(s);
+}
+
+int afmib_helm_apply(afmib_solver* s, int comp, double scale, double* y, const double* x) {
+    if (!s || !y || !x || comp < 0 || comp > 2) return AFMIB_ERR_ARG;
+    if (comp == 1) TRY(v_in(s, s->tmp[0], x));
+    else TRY(copy_in(s, s->tmp[0], x, s->N()));
+    launch_helm_apply<double>(s->d, comp, scale, s->tmp[1], s->tmp[0], s->st);
+    CKL();
+    if (comp == 1) TRY(v_out(s, y, s->tmp[1]));
+    else TRY(copy_out(s, y, s->tmp[1], s->N()));
+    return sync(s);
+}
+
+int afmib_helmholtz_cg(afmib_solver* s, int comp, double scale, double* x, const double* b, int* iters) {
+    if (!s || !x || !b || comp < 0 || comp > 2) return AFMIB_ERR_ARG;
+    if (comp == 1) {
+        TRY(v_in(s, s->tmp[0], x));
+        TRY(v_in(s, s->tmp[1], b));
+    } else {
+        TRY(copy_in(s, s->tmp[0], x, s->N()));
+        TRY(copy_in(s, s->tmp[1], b, s->N()));
+    }
+    const int rc = cg_solve(s, comp, scale, s->tmp[0], s->tmp[1], iters);
+    if (comp == 1) TRY(v_out(s, x, s->tmp[0]));
+    else TRY(copy_out(s, x, s->tmp[0], s->N()));
+    TRY(sync(s));
+    return rc;
+}
+
+int afmib_restrict(afmib_solver* s, double* coarse, const double* fine) {
+    if (!s || !coarse || !fine) return AFMIB_ERR_ARG;
+    const Dims& d = s->d;
+    if (!is_even(d.nx) || !is_even(d.ny) || !is_even(d.nz)) return s->fail(AFMIB_ERR_ARG, "odd extent");
+    TRY(copy_in(s, s->tmp[0], fine, s->N()));
+    launch_restrict<double>(d, s->tmp[1], s->tmp[0], s->st);
+    CKL();
+    TRY(copy_out(s, coarse, s->tmp[1], s->N() / 8));
+    return sync(s);
+}
+
+int afmib_prolong(afmib_solver* s, double* fine, const double* coarse) {
+    if (!s || !coarse || !fine) return AFMIB_ERR_ARG;
+    const Dims& d = s->d;
+    if (!is_even(d.nx) || !is_even(d.ny) || !is_even(d.nz)) return s->fail(AFMIB_ERR_ARG, "odd extent");
+    TRY(copy_in(s, s->tmp[0], coarse, s->N() / 8));
+    launch_prolong_assign<double>(d, s->tmp[1], s->tmp[0], s->st);
+    CKL();
+    TRY(copy_out(s, fine, s->tmp[1], s->N()));
+    return sync(s);
+}
+
+int afmib_spread(afmib_solver* s, int M, const double* X, const double* F, const double* vol, double* fx, double* fy,
+                 double* fz) {
+    if (!s || M <= 0 || !X || !F || !fx || !fy || !fz) return AFMIB_ERR_ARG;
+    if (!s->TS) TRY(setup_tiles(s));
+    const int keepM = s->M;
+    TRY(marker_alloc(s, M, 0));
+    s->M = M;
+    TRY(copy_in(s, s->Xh, X, 3 * (long long)M));
+    TRY(copy_in(s, s->G, F, 3 * (long long)M));
+    if (vol) TRY(copy_in(s, s->U1, vol, M));
+    CK(cudaMemsetAsync(s->dflag, 0, sizeof(int), s->st));
+    TRY(bin_markers(s, s->Xh));
+    TRY(spread_forces(s, vol ? s->U1 : nullptr, s->tmp[0], s->tmp[1], s->tmp[2]));
+    int rc = check_marker_flag(s);
+    s->M = keepM;
+    TRY(copy_out(s, fx, s->tmp[0], s->N()));
+    TRY(v_out(s, fy, s->tmp[1]));
+    TRY(copy_out(s, fz, s->tmp[2], s->N()));
+    TRY(sync(s));
+    return rc;
+}
+
+int afmib_interp(afmib_solver* s, int M, const double* X, const double* u, const double* v, const double* w,
+                 double* U) {
+    if (!s || M <= 0 || !X || !u || !v || !w || !U) return AFMIB_ERR_ARG;
+    if (!s->TS) TRY(setup_tiles(s));
+    const int keepM = s->M;
+    TRY(marker_alloc(s, M, 0));
+    s->M = M;
+    TRY(copy_in(s, s->Xh, X, 3 * (long long)M));
+    TRY(copy_in(s, s->tmp[0], u, s->N()));
+    TRY(v_in(s, s->tmp[1], v));
+    TRY(copy_in(s, s->tmp[2], w, s->N()));
+    CK(cudaMemsetAsync(s->dflag, 0, sizeof(int), s->st));
+    TRY(bin_markers(s, s->Xh));
+    TRY(interp_markers(s, s->tmp[0], s->tmp[1], s->tmp[2], s->U2));
+    CKL();
+    int rc = check_marker_flag(s);
+    s->M = keepM;
+    TRY(copy_out(s, U, s->U2, 3 * (long long)M));
+    TRY(sync(s));
+    return rc;
+}
+
+// ---- per-kernel profiling ----------------------------------------------------
+
+int afmib_profile_enable(afmib_solver* s, int on) {
+    if (!s) return AFMIB_ERR_ARG;
+    TRY(sync(s));
+    if (s->prof_tab.empty())
+        for (int i = 0; i < P_COUNT; ++i) s->prof_tab.push_back({kProfNames[i], 0, 0.0, 0.0});
+    s->prof = on != 0;
+    return AFMIB_OK;
+}
+
+int afmib_profile_reset(afmib_solver* s) {
+    if (!s) return AFMIB_ERR_ARG;
+    TRY(sync(s));
+    for (auto& e : s->prof_tab) { e.launches = 0; e.ms = 0.0; e.bytes = 0.0; }
+    return AFMIB_OK;
+}
+
+int afmib_profile_count(const afmib_solver* s) { return s ? (int)s->prof_tab.size() : 0; }
+
+int afmib_profile_get(afmib_solver* s, int i, const char** name, long long* launches, double* ms, double* bytes) {
+    if (!s || i < 0 || i >= (int)s->prof_tab.size()) return AFMIB_ERR_ARG;
+    TRY(sync(s));
+    const auto& e = s->prof_tab[i];
+    if (name) *name = e.name;
+    if (launches) *launches = e.launches;
+    if (ms) *ms = e.ms;
+    if (bytes) *bytes = e.bytes;
+    return AFMIB_OK;
+}
+
+}  // extern "C"

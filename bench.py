@@ -1,0 +1,319 @@
+"""Benchmark: immersed-boundary steps per second on one GB300.
+
+Workload (the configuration the headline metric is quoted on): periodic unit
+cube on a 256^3 MAC grid, mu = 0.005, rho = 1, dt = 2e-5; 200,000 markers on
+10 spherical shells of radius 0.08 (spherical Fibonacci lattice, 6-nearest-
+neighbour zero-rest-length springs, k = 0.5), centres drawn from a seed with
+minimum separation 0.2, each perturbed radially by 0.01*Y_2^m with seeded m;
+initial velocity a seeded solenoidal random field (spectrum peaked at
+|k| = 4, RMS 0.1). Seeded synthetic inputs stand in for any dataset.
+
+One step = one IB step (BE and CN sub-steps, two spreads, two
+interpolations). `value` is measured with the state resident in HBM; `e2e`
+adds, every step, the upload of the state (u, v, w, X) from pinned host memory
+and the download of the new state through the C ABI.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "IB steps/s @256^3+200k markers: FP32/FP64-refined vs FP64 GPU at 1e-8 err; HBM GB/s"
+UNIT = "IB steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--shells", type=int, default=10)
+    ap.add_argument("--per-shell", type=int, default=20000)
+    ap.add_argument("--radius", type=float, default=0.08)
+    ap.add_argument("--min-sep", type=float, default=0.2)
+    ap.add_argument("--mu", type=float, default=0.005)
+    ap.add_argument("--dt", type=float, default=2e-5)
+    ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--profile-steps", type=int, default=2)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-n", type=int, default=64,
+                    help="grid of the CPU sample (the workload at reduced resolution, scaled by the cell count)")
+    return ap.parse_args()
+
+
+def workload(n, shells, per_shell, radius, min_sep, seed_offset=0):
+    from afmibins_gb300 import markers as mk
+    X, nstart, nidx = mk.multi_shell(shells, per_shell, radius, min_sep, 0.01, seed=mk.SEED + 3 + seed_offset)
+    u, v, w = mk.random_solenoidal_velocity(n, n, n, rms=0.1, k_peak=4.0, seed=mk.SEED + 3 + seed_offset)
+    return X, nstart, nidx, u, v, w
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                out, _ = self.p.communicate(timeout=5)
+            except Exception:
+                self.p.kill()
+                out, _ = self.p.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            c = [x.strip() for x in l.split(",")]
+            if len(c) < 9:
+                continue
+            try:
+                sm.append(float(c[1]))
+                smax = float(c[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if c[5 + k].lower() in ("active", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(args, kind_note=""):
+    """One IB step of the workload at reduced resolution on the CPU oracle
+    (single thread), scaled to the full grid by the cell count. Returns
+    (steps_per_s_scaled, seconds, description)."""
+    from oracle import pyoracle as po
+    ns = args.cpu_sample_n
+    scale_cells = (args.n / ns) ** 3
+    per = max(200, int(args.per_shell * (ns / args.n) ** 2))
+    X, nstart, nidx, u, v, w = workload(ns, args.shells, per, args.radius, args.min_sep)
+    g = po.Grid(ns, ns, ns, ns, channel=False)
+    t0 = time.perf_counter()
+    s = po.NSSolver(g, args.mu, 1.0, args.dt, args.tol, u, v, w)
+    t1 = time.perf_counter()
+    Xo, st = s.ib_step(X, nstart, nidx, 0.5)
+    t2 = time.perf_counter()
+    sec = t2 - t1
+    desc = (f"1 IB step of the workload at {ns}^3 with {args.shells}x{per} markers on 1 thread of the host CPU "
+            f"({sec:.2f} s), time scaled x{scale_cells:.0f} to {args.n}^3 cells")
+    return 1.0 / (sec * scale_cells), sec, desc
+
+
+def run_reference(args, rank, world):
+    """The reference path timed on the host cores: the CPU oracle (a port of
+    the reference's algorithm; the reference headers are not present on the
+    GPU host), bounded sample per step."""
+    if rank != 0:
+        return
+    vals = []
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_sample(args)
+    for _ in range(args.steps):
+        v, sec, desc = cpu_sample(args)
+        vals.append(sec)
+    sec = float(np.mean(vals))
+    scale_cells = (args.n / args.cpu_sample_n) ** 3
+    value = 1.0 / (sec * scale_cells)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+        "steps": args.steps, "warmup": min(args.warmup, 1), "ms_per_step": 1000.0 / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_dict(args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(args):
+    return {"workload": f"IB step, periodic {args.n}^3 MAC grid, {args.shells * args.per_shell} markers "
+                        f"({args.shells} shells x {args.per_shell}), mu={args.mu}, dt={args.dt}",
+            "grid": args.n, "markers": args.shells * args.per_shell, "bc": "periodic",
+            "precision": args.precision, "tol": args.tol,
+            "l2": "inputs larger than L2 (each field 134 MB at 256^3 FP64, ~30 fields resident)"}
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from afmibins_gb300 import capi
+
+    X, nstart, nidx, u, v, w = workload(args.n, args.shells, args.per_shell, args.radius, args.min_sep,
+                                        seed_offset=rank)
+    M = X.shape[0]
+    stream = torch.cuda.Stream()
+    prec = capi.FP64 if args.precision == "fp64" else capi.MIXED
+    sv = capi.Solver(args.n, mu=args.mu, rho=1.0, dt=args.dt, tol=args.tol, k_spring=0.5, precision=prec,
+                     stream=stream.cuda_stream)
+    dev = torch.device("cuda", local)
+    ud, vd, wd = (torch.from_numpy(a).to(dev) for a in (u, v, w))
+    Xd = torch.from_numpy(X).to(dev)
+    torch.cuda.synchronize()
+    sv.set_velocity(ud, vd, wd)
+    sv.project()
+    sv.set_markers(Xd, nstart, nidx)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        sv.ib_step(1)
+    sv.synchronize()
+
+    # ---- timed region: state resident in HBM
+    l0 = sv.stats()["kernel_launches"]
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                sv.ib_step(1)
+            e1.record(stream)
+        stream.synchronize()
+        wall = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    launches = sv.stats()["kernel_launches"] - l0
+    ms_max = ms
+    if dist is not None:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = world * args.steps / (ms_max / 1000.0)
+    st = sv.stats()
+
+    # ---- e2e through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        N = args.n ** 3
+        hu, hv, hw = (torch.empty(N, dtype=torch.float64, pin_memory=True) for _ in range(3))
+        hX = torch.empty((M, 3), dtype=torch.float64, pin_memory=True)
+        sv.get_velocity((hu, hv, hw))
+        sv.get_markers(hX)
+        ke = max(1, min(args.steps, 5))
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            sv.set_velocity(hu, hv, hw)
+            sv.set_marker_positions(hX)
+            sv.ib_step(1)
+            sv.get_velocity((hu, hv, hw))
+            sv.get_markers(hX)
+        torch.cuda.synchronize()
+        we = time.perf_counter() - t0
+        if dist is not None:
+            t = torch.tensor([we], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            we = float(t.item())
+        bio = 3 * N * 8 + M * 24
+        e2e = {"value": world * ke / we, "unit": UNIT, "h2d_bytes_per_step": bio, "d2h_bytes_per_step": bio,
+               "steps": ke}
+
+    # ---- per-kernel durations over profiled steps (events on the solver's stream)
+    sv.profile(True)
+    sv.profile_reset()
+    for _ in range(args.profile_steps):
+        sv.ib_step(1)
+    table = sv.profile_table()
+    sv.profile(False)
+    peak, peak_kind = measured_peaks()
+    total_ms = sum(v[1] for v in table.values())
+    dom = max(table.items(), key=lambda kv: kv[1][1])
+    name, (nl, kms, kbytes) = dom
+    achieved = (kbytes / nl) / ((kms / nl) * 1e-3) / 1e9
+    kernels = {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / total_ms, 4),
+                   "GB_s": round(v[2] / (v[1] * 1e-3) / 1e9, 1) if v[1] > 0 else None}
+               for k, v in sorted(table.items(), key=lambda kv: -kv[1][1])}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cv, csec, desc = cpu_sample(args)
+        cpu = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic (seeded shells and solenoidal field)", "config": config_dict(args),
+            "roofline": {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "traffic": None, "bytes_per_launch": kbytes / nl, "ms_per_launch": kms / nl},
+            "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clk.summary(),
+            "solver": {"cg_iters_per_step": st["cg_iters"] / max(1, st["ib_steps"]),
+                       "mg_cycles_per_step": st["mg_cycles"] / max(1, st["ib_steps"]),
+                       "spread_tiles": st["spread_tiles"], "wall_s": wall},
+            "kernels": kernels,
+        }
+        print(json.dumps(line), flush=True)
+    sv.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

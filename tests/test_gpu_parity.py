@@ -1,0 +1,227 @@
+"""FP64 parity of the CUDA path (through the C ABI) with the reference.
+
+Channel mode (the reference's own domain) is checked against the golden
+vectors of the compiled reference (tests/golden/); periodic mode against the
+CPU restatement (oracle/), run live on the same seeded inputs. The bar is the
+FP64 drop-in tolerance: 1e-10 relative (max-norm) for fields and markers
+after the stated steps; single stencils agree to ~1e-13 (FMA contraction);
+pressure is compared after removing its mean (the singular Neumann/periodic
+Poisson problem fixes phi only up to a constant)."""
+import numpy as np
+import pytest
+
+from afmibins_gb300 import capi, markers as mk
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+OPS_TOL = 1e-13
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def demean(p):
+    return p - p.mean()
+
+
+def test_single_operators_channel(golden):
+    d = golden("ops_8")
+    s = float(d["s"])
+    with capi.Solver(8, bc=capi.BC_CHANNEL, tol=1e-12) as sv:
+        assert rel(sv.lap_apply(d["x"]), d["lap"]) < OPS_TOL
+        assert rel(sv.restrict(d["x"]), d["restrict"]) < OPS_TOL
+        assert rel(sv.prolong(d["c"]), d["prolong"]) < OPS_TOL
+        assert rel(sv.div(d["u"], d["v"], d["w"], d["top"], d["bottom"]), d["div"]) < OPS_TOL
+        assert rel(np.concatenate(sv.grad(d["x"])), d["grad"]) < OPS_TOL
+        assert rel(np.concatenate(sv.advection(d["u"], d["v"], d["w"])), d["advect"]) < OPS_TOL
+        h = np.concatenate([sv.helm_apply(0, s, d["u"]), sv.helm_apply(1, s, d["v"]), sv.helm_apply(2, s, d["w"])])
+        assert rel(h, d["helm"][: h.size]) < OPS_TOL
+        x, it = sv.helmholtz_cg(0, s, d["x0"], d["b"])
+        assert rel(x, d["cg_x"]) < TOL
+
+
+def test_restriction_known_answer(golden):
+    d = golden("restr_test")
+    with capi.Solver(2, bc=capi.BC_CHANNEL) as sv:
+        np.testing.assert_allclose(sv.restrict(d["fine"]), d["coarse"], rtol=1e-15, atol=1e-40)
+
+
+@pytest.mark.parametrize("name", ["mg_test_16", "mg_test3_16"])
+def test_mg_reference_rhs(golden, name):
+    d = golden(name)
+    b, tol = d["rhs"], float(d["tol"])
+    g = po.Grid(16, 16, 16, 16, channel=True)
+    with capi.Solver(16, bc=capi.BC_CHANNEL, tol=tol) as sv:
+        x, cycles = sv.mg_solve(b)
+    r = (b - b.mean()) - po.lap_apply(g, x)
+    assert np.sqrt(np.mean(r ** 2)) <= tol
+    scale = max(np.max(np.abs(demean(d["x"]))), 1e-300)
+    assert np.max(np.abs(demean(x) - demean(d["x"]))) <= max(TOL * scale, 1e-12 / 256)
+
+
+def test_mg_box_mean_removal(golden):
+    # test/mg_test2.cc: geometry<1,8,8,8>, an 8^3 coarsest level, L x = b - mean(b)
+    d = golden("mg_test2_box")
+    with capi.Solver(16, bc=capi.BC_CHANNEL, n=2, mg_levels=1, tol=float(d["tol"])) as sv:
+        x, cycles = sv.mg_solve(d["rhs"])
+        lx = sv.lap_apply(x)
+    b = d["rhs"]
+    np.testing.assert_allclose(lx, b - b.mean(), atol=1e-9)
+    assert rel(demean(x), demean(d["x"])) < 1e-9
+
+
+def test_ns_substeps_channel(golden):
+    d = golden("ns_16")
+    with capi.Solver(16, bc=capi.BC_CHANNEL, mu=float(d["mu"]), rho=float(d["rho"]), dt=float(d["dt"]),
+                     tol=float(d["tol"])) as sv:
+        sv.set_velocity(d["u0"], d["v0"], d["w0"])
+        sv.project()
+        for _ in range(int(d["substeps"])):
+            sv.ns_step(d["fx"], d["fy"], d["fz"])
+        u, v, w = sv.get_velocity()
+        p = sv.get_pressure()
+        walls = np.concatenate(sv.get_walls())
+    assert rel(u, d["u"]) < TOL
+    assert rel(v, d["v"]) < TOL
+    assert rel(w, d["w"]) < TOL
+    assert rel(demean(p), demean(d["p"])) < TOL
+    assert rel(walls, d["walls"]) < TOL
+
+
+def test_spread_interp_channel(golden):
+    d = golden("ib_16")
+    with capi.Solver(16, bc=capi.BC_CHANNEL) as sv:
+        fx, fy, fz = sv.spread(d["X"], d["F"], d["vol"])
+        U = sv.interp(d["X"], d["ue"], d["ve"], d["we"])
+    assert rel(np.concatenate([fx, fy, fz]), d["spread"]) < OPS_TOL
+    assert rel(U.ravel(), d["interp"]) < OPS_TOL
+
+
+def test_ib_steps_channel(golden):
+    d = golden("ib_16")
+    with capi.Solver(16, bc=capi.BC_CHANNEL, mu=float(d["mu"]), rho=float(d["rho"]), dt=float(d["dt"]),
+                     tol=float(d["tol"]), k_spring=float(d["k"])) as sv:
+        sv.set_velocity(d["u0"], d["v0"], d["w0"])
+        sv.project()
+        sv.set_markers(d["X"], d["nstart"], d["nidx"])
+        sv.ib_step(int(d["steps"]))
+        u, v, w = sv.get_velocity()
+        p = sv.get_pressure()
+        X = sv.get_markers()
+    assert rel(u, d["u"]) < TOL and rel(v, d["v"]) < TOL and rel(w, d["w"]) < TOL
+    assert rel(demean(p), demean(d["p"])) < TOL
+    assert rel(X, d["Xout"]) < TOL
+
+
+def _periodic_case(n, M=600, seed=7):
+    rng = np.random.default_rng(seed)
+    g = po.Grid(n, n, n, n, channel=False)
+    u, v, w = (0.1 * rng.standard_normal(g.ncell) for _ in range(3))
+    P = mk.fibonacci_sphere(M)
+    lists = [l[:6] for l in mk.knn_lists(P, 6)]
+    X, _ = mk.shell(P, lists, (0.45, 0.52, 0.5), 0.22, 0.02, 0)
+    nstart, nidx = mk._csr_from_lists(lists)
+    return g, u, v, w, X, nstart, nidx
+
+
+@pytest.mark.parametrize("n", [16, 32])
+def test_ns_substeps_periodic(n):
+    g, u, v, w, _, _, _ = _periodic_case(n)
+    rng = np.random.default_rng(11)
+    f = [rng.standard_normal(g.ncell) for _ in range(3)]
+    mu, rho, dt, tol = 0.01, 1.0, 1e-3, 1e-10
+    ref = po.NSSolver(g, mu, rho, dt, tol, u, v, w)
+    for _ in range(4):
+        assert ref.step(*f) == 0
+    ru, rv, rw, rp = ref.get()
+    with capi.Solver(n, mu=mu, rho=rho, dt=dt, tol=tol) as sv:
+        sv.set_velocity(u, v, w)
+        sv.project()
+        for _ in range(4):
+            sv.ns_step(*f)
+        gu, gv, gw = sv.get_velocity()
+        gp = sv.get_pressure()
+    assert rel(gu, ru) < TOL and rel(gv, rv) < TOL and rel(gw, rw) < TOL
+    assert rel(demean(gp), demean(rp)) < TOL
+
+
+def test_ib_steps_periodic():
+    n = 32
+    g, u, v, w, X, nstart, nidx = _periodic_case(n, M=2000)
+    mu, rho, dt, tol, k = 0.01, 1.0, 5e-4, 1e-10, 0.5
+    ref = po.NSSolver(g, mu, rho, dt, tol, u, v, w)
+    Xr = X.copy()
+    for _ in range(3):
+        Xr, st = ref.ib_step(Xr, nstart, nidx, k)
+        assert st == 0
+    ru, rv, rw, _ = ref.get()
+    with capi.Solver(n, mu=mu, rho=rho, dt=dt, tol=tol, k_spring=k) as sv:
+        sv.set_velocity(u, v, w)
+        sv.project()
+        sv.set_markers(X, nstart, nidx)
+        sv.ib_step(3)
+        gu, gv, gw = sv.get_velocity()
+        Xg = sv.get_markers()
+    assert rel(gu, ru) < TOL and rel(gv, rv) < TOL and rel(gw, rw) < TOL
+    assert rel(Xg - X, Xr - X) < 1e-8          # displacement, the sensitive part
+    assert np.max(np.abs(Xg - Xr)) < 1e-12
+
+
+def test_spread_periodic_wraps_images():
+    n = 16
+    g = po.Grid(n, n, n, n, channel=False)
+    rng = np.random.default_rng(3)
+    M = 500
+    X = rng.uniform(0.0, 1.0, (M, 3))   # markers everywhere, including next to the faces
+    F = rng.standard_normal((3, M))
+    with capi.Solver(n) as sv:
+        fx, fy, fz = sv.spread(X, F)
+        U = sv.interp(X, fx, fy, fz)
+    ref = [po.spread(g, c, X, F[c].copy()) for c in range(3)]
+    assert rel(np.concatenate([fx, fy, fz]), np.concatenate(ref)) < OPS_TOL
+    refU = np.stack([po.interp(g, c, X, r) for c, r in enumerate(ref)])
+    assert rel(U, refU) < OPS_TOL
+    # total force is conserved: sum f h^3 = sum F
+    np.testing.assert_allclose(np.array([fx.sum(), fy.sum(), fz.sum()]) / n ** 3, F.sum(1), rtol=1e-12, atol=1e-12)
+
+
+def test_spread_bitwise_repeatable():
+    n = 32
+    _, _, _, _, X, _, _ = _periodic_case(n, M=3000)
+    F = np.random.default_rng(4).standard_normal((3, X.shape[0]))
+    with capi.Solver(n) as sv:
+        a = sv.spread(X, F)
+        b = sv.spread(X, F)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_failure_statuses_are_reported():
+    n = 16
+    # a marker next to a channel wall: refused with a status, no fault
+    with capi.Solver(n, bc=capi.BC_CHANNEL) as sv:
+        X = np.array([[0.5, 0.05, 0.5]])
+        with pytest.raises(capi.AfmibError) as e:
+            sv.interp(X, np.zeros(sv.ncell), np.zeros(sv.nv), np.zeros(sv.ncell))
+        assert e.value.status == capi.AFMIB_ERR_BOUNDS
+    # a CG cap that is too small: bounded, reported
+    with capi.Solver(n, tol=1e-14, max_cg_iters=1) as sv:
+        b = np.random.default_rng(0).standard_normal(sv.ncell)
+        with pytest.raises(capi.AfmibError) as e:
+            sv.helmholtz_cg(0, -0.3, np.zeros(sv.ncell), b)
+        assert e.value.status == capi.AFMIB_ERR_NOCONV
+    # NaN in the input: the residual check reports it
+    with capi.Solver(n, tol=1e-10) as sv:
+        b = np.zeros(sv.ncell)
+        b[5] = np.nan
+        with pytest.raises(capi.AfmibError) as e:
+            sv.mg_solve(b)
+        assert e.value.status == capi.AFMIB_ERR_NAN
+    # bad configuration
+    with pytest.raises(capi.AfmibError) as e:
+        capi.Solver(16, mu=0.01, rho=-1.0)
+    assert e.value.status == capi.AFMIB_ERR_ARG
