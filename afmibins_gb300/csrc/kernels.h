@@ -11,8 +11,9 @@ namespace afmib {
 
 // ----- MAC stencils (kernels_field.cu) -------------------------------------
 // Conservative centred advection N(u) of src/ns/solver.h:142-236.
-template <typename T>
-void launch_advect(const Dims& d, T* ua, T* va, T* wa, const T* u, const T* v, const T* w, cudaStream_t s);
+// TI: storage type of the velocity, T: arithmetic and output type.
+template <typename TI, typename T>
+void launch_advect(const Dims& d, T* ua, T* va, T* wa, const TI* u, const TI* v, const TI* w, cudaStream_t s);
 // Divergence n*(du + dv + dw), src/alg/div.h:29-60. top/bottom (channel only,
 // nx*nz each) may be null for zero walls.
 template <typename T>
@@ -35,10 +36,20 @@ void launch_wall_update(const Dims& d, double* walls, const double* wallgrad, cu
 //   be=0: r = (I + s_plus*Delta) u_old + bdy(s_plus) - bdy(s_minus) + dt*(f/rho - adv)
 // src/ns/solver.h:105-135 with src/ns/helmholtz.h:177-196. walls: [top|bottom]
 // rows of this component (null in periodic mode or for v).
-template <typename T>
-void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const T* f, const T* adv,
+template <typename T, typename TF>
+void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const TF* f, const TF* adv,
                      const double* top, const double* bottom, double s_plus, double s_minus, double dt,
                      double inv_rho, cudaStream_t s);
+// Mixed form: r = b - (I + s Delta) x in FP64, stored as TD, out[0] = ||r||^2.
+template <typename TD>
+void launch_helm_defect(const Dims& d, int comp, double scale, const double* x, const double* b, TD* r, RedScratch sc,
+                        double* out, cudaStream_t s);
+// x = 0, r = p = b, cgs[0] = b.b
+template <typename T>
+void launch_cg_init_zero(long long n, const T* b, T* x, T* r, T* p, RedScratch sc, double* cgs, cudaStream_t s);
+// x (FP64) += e
+template <typename TE>
+void launch_add_correction(long long n, double* x, const TE* e, cudaStream_t s);
 // y = (I + s*Delta) x for component comp (src/ns/helmholtz.h:61-175,218-319).
 template <typename T>
 void launch_helm_apply(const Dims& d, int comp, double scale, T* y, const T* x, cudaStream_t s);
@@ -81,6 +92,9 @@ void launch_lap_apply(const Dims& d, T* y, const T* x, cudaStream_t s);
 // r = b - L x, optionally out[0] = r.r
 template <typename T>
 void launch_residual(const Dims& d, T* r, const T* x, const T* b, RedScratch* sc, double* out, cudaStream_t s);
+// Mixed form: r = b - L x evaluated in FP64 (x, b FP64), stored as TD; out[0] = r.r
+template <typename TD>
+void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, RedScratch sc, double* out, cudaStream_t s);
 // One red (color 0) or black (color 1) Gauss-Seidel half sweep.
 template <typename T>
 void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s);

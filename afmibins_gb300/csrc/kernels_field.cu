@@ -30,10 +30,15 @@ inline dim3 block3() { return dim3(BX, BY, 1); }
 // which makes every wall flux of the reference (uvt, uvb, vwt, vwb = 0; vvb,
 // vvt from the one interior face) come out of the same formulas.
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename TI, typename T>
 __global__ void k_advect(Dims d, T* __restrict__ ua, T* __restrict__ va, T* __restrict__ wa,
-                         const T* __restrict__ u, const T* __restrict__ v, const T* __restrict__ w) {
+                         const TI* __restrict__ ui, const TI* __restrict__ vi, const TI* __restrict__ wi) {
     AFMIB_XYZ
+    // loads in the storage type TI, arithmetic in T (FP32 for the mixed form)
+    struct Ld {
+        const TI* p;
+        __device__ T operator[](long long k) const { return T(p[k]); }
+    } u{ui}, v{vi}, w{wi};
     const T h = T(0.5), n = T(d.n);
     const int xm = xm1(d, x), xp = xp1(d, x), ym = ym1(d, y), yp = yp1(d, y), zm = zm1(d, z), zp = zp1(d, z);
     const long long i = lin(d, x, y, z);
@@ -178,9 +183,9 @@ __global__ void k_helm_apply(Dims d, int comp, T s, T* __restrict__ out, const T
 }
 
 // Right-hand side of the viscous solve, src/ns/solver.h:105-135.
-template <typename T>
+template <typename T, typename TF>
 __global__ void k_helm_rhs(Dims d, int comp, int be, T* __restrict__ r, const T* __restrict__ uold,
-                           const T* __restrict__ f, const T* __restrict__ adv, const double* __restrict__ top,
+                           const TF* __restrict__ f, const TF* __restrict__ adv, const double* __restrict__ top,
                            const double* __restrict__ bottom, double s_plus, double s_minus, double hdt,
                            double inv_rho) {
     AFMIB_XYZ
@@ -194,7 +199,7 @@ __global__ void k_helm_rhs(Dims d, int comp, int be, T* __restrict__ r, const T*
         bm = T(8. / 3. * s_minus * d.n * d.n * wv);
         bp = T(8. / 3. * s_plus * d.n * d.n * wv);
     }
-    const T src = T(hdt) * (T(inv_rho) * f[i] - adv[i]);
+    const T src = T(hdt) * (T(inv_rho) * T(f[i]) - T(adv[i]));
     if (be) {
         r[i] = (uold[i] + T(-1) * bm) + src;
     } else {
@@ -263,6 +268,48 @@ __global__ void k_cg_direction(long long N, T* __restrict__ p, const T* __restri
 }
 
 // ---------------------------------------------------------------------------
+// Defect-correction pieces of the mixed form: the residual of the FP64 state
+// evaluated in FP64 and handed to the FP32 inner solve as an FP32 defect, and
+// the FP64 update x += e with the FP32 correction.
+// ---------------------------------------------------------------------------
+template <typename TD>
+__global__ void __launch_bounds__(kRedBlock) k_helm_defect(Dims d, int comp, double s, const double* __restrict__ x,
+                                                          const double* __restrict__ b, TD* __restrict__ r,
+                                                          RedScratch sc, double* out) {
+    const long long N = d.ncell(), sxy = d.sxy();
+    double acc[1] = {0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+        const int xi = (int)(i % d.nx), yi = (int)((i % sxy) / d.nx), zi = (int)(i / sxy);
+        const double ri = b[i] - helm_point(d, comp, s, x, xi, yi, zi);
+        r[i] = TD(ri);
+        acc[0] += ri * ri;
+    }
+    grid_sum<1>(acc, sc, out);
+}
+
+// CG started from zero: r = p = b, n0 = b.b
+template <typename T>
+__global__ void __launch_bounds__(kRedBlock) k_cg_init_zero(long long N, const T* __restrict__ b, T* __restrict__ x,
+                                                           T* __restrict__ r, T* __restrict__ p, RedScratch sc,
+                                                           double* cgs) {
+    double acc[1] = {0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+        const T bi = b[i];
+        x[i] = T(0);
+        r[i] = bi;
+        p[i] = bi;
+        acc[0] += (double)bi * (double)bi;
+    }
+    grid_sum<1>(acc, sc, cgs + 0);
+}
+
+template <typename TE>
+__global__ void k_add_correction(long long N, double* __restrict__ x, const TE* __restrict__ e) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
+        x[i] = x[i] + (double)e[i];
+}
+
+// ---------------------------------------------------------------------------
 // reductions and vector ops
 // ---------------------------------------------------------------------------
 template <typename T, bool SQ>
@@ -308,9 +355,9 @@ inline int ew_blocks(long long n) {
 
 }  // namespace
 
-template <typename T>
-void launch_advect(const Dims& d, T* ua, T* va, T* wa, const T* u, const T* v, const T* w, cudaStream_t s) {
-    k_advect<T><<<grid3(d), block3(), 0, s>>>(d, ua, va, wa, u, v, w);
+template <typename TI, typename T>
+void launch_advect(const Dims& d, T* ua, T* va, T* wa, const TI* u, const TI* v, const TI* w, cudaStream_t s) {
+    k_advect<TI, T><<<grid3(d), block3(), 0, s>>>(d, ua, va, wa, u, v, w);
 }
 template <typename T>
 void launch_div(const Dims& d, T* out, const T* u, const T* v, const T* w, const T* top, const T* bottom, cudaStream_t s) {
@@ -327,11 +374,24 @@ void launch_grad_sub(const Dims& d, T* u, T* v, T* w, const T* phi, T* wallgrad,
 void launch_wall_update(const Dims& d, double* walls, const double* wallgrad, cudaStream_t s) {
     k_wall_update<<<ew_blocks((long long)d.nx * d.nz), 256, 0, s>>>(d, walls, wallgrad);
 }
-template <typename T>
-void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const T* f, const T* adv, const double* top,
+template <typename T, typename TF>
+void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const TF* f, const TF* adv, const double* top,
                      const double* bottom, double s_plus, double s_minus, double dt, double inv_rho, cudaStream_t s) {
-    k_helm_rhs<T><<<grid3(d), block3(), 0, s>>>(d, comp, be, r, uold, f, adv, top, bottom, s_plus, s_minus,
-                                                be ? dt / 2 : dt, inv_rho);
+    k_helm_rhs<T, TF><<<grid3(d), block3(), 0, s>>>(d, comp, be, r, uold, f, adv, top, bottom, s_plus, s_minus,
+                                                    be ? dt / 2 : dt, inv_rho);
+}
+template <typename TD>
+void launch_helm_defect(const Dims& d, int comp, double scale, const double* x, const double* b, TD* r, RedScratch sc,
+                        double* out, cudaStream_t s) {
+    k_helm_defect<TD><<<red_blocks(d.ncell()), kRedBlock, 0, s>>>(d, comp, scale, x, b, r, sc, out);
+}
+template <typename T>
+void launch_cg_init_zero(long long n, const T* b, T* x, T* r, T* p, RedScratch sc, double* cgs, cudaStream_t s) {
+    k_cg_init_zero<T><<<red_blocks(n), kRedBlock, 0, s>>>(n, b, x, r, p, sc, cgs);
+}
+template <typename TE>
+void launch_add_correction(long long n, double* x, const TE* e, cudaStream_t s) {
+    k_add_correction<TE><<<ew_blocks(n), 256, 0, s>>>(n, x, e);
 }
 template <typename T>
 void launch_helm_apply(const Dims& d, int comp, double scale, T* y, const T* x, cudaStream_t s) {
@@ -380,12 +440,9 @@ void launch_convert(long long n, TO* out, const TI* in, cudaStream_t s) {
 }
 
 #define AFMIB_INST(T)                                                                                          \
-    template void launch_advect<T>(const Dims&, T*, T*, T*, const T*, const T*, const T*, cudaStream_t);       \
     template void launch_div<T>(const Dims&, T*, const T*, const T*, const T*, const T*, const T*, cudaStream_t); \
     template void launch_grad<T>(const Dims&, T*, T*, T*, const T*, cudaStream_t);                             \
     template void launch_grad_sub<T>(const Dims&, T*, T*, T*, const T*, T*, cudaStream_t);                     \
-    template void launch_helm_rhs<T>(const Dims&, int, int, T*, const T*, const T*, const T*, const double*,   \
-                                     const double*, double, double, double, double, cudaStream_t);             \
     template void launch_helm_apply<T>(const Dims&, int, double, T*, const T*, cudaStream_t);                  \
     template void launch_cg_init<T>(const Dims&, int, double, const T*, const T*, T*, T*, RedScratch, double*, \
                                     cudaStream_t);                                                             \
@@ -400,6 +457,21 @@ void launch_convert(long long n, TO* out, const TI* in, cudaStream_t s) {
 
 AFMIB_INST(double)
 AFMIB_INST(float)
+template void launch_advect<double, double>(const Dims&, double*, double*, double*, const double*, const double*,
+                                            const double*, cudaStream_t);
+template void launch_advect<double, float>(const Dims&, float*, float*, float*, const double*, const double*,
+                                           const double*, cudaStream_t);
+template void launch_helm_rhs<double, double>(const Dims&, int, int, double*, const double*, const double*,
+                                              const double*, const double*, const double*, double, double, double,
+                                              double, cudaStream_t);
+template void launch_helm_rhs<double, float>(const Dims&, int, int, double*, const double*, const float*, const float*,
+                                             const double*, const double*, double, double, double, double,
+                                             cudaStream_t);
+template void launch_helm_defect<float>(const Dims&, int, double, const double*, const double*, float*, RedScratch,
+                                        double*, cudaStream_t);
+template void launch_cg_init_zero<float>(long long, const float*, float*, float*, float*, RedScratch, double*,
+                                         cudaStream_t);
+template void launch_add_correction<float>(long long, double*, const float*, cudaStream_t);
 template void launch_convert<float, double>(long long, float*, const double*, cudaStream_t);
 template void launch_convert<double, float>(long long, double*, const float*, cudaStream_t);
 

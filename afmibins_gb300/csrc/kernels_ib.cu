@@ -383,15 +383,15 @@ __global__ void __launch_bounds__(512) k_spread_gather(Dims d, int TS, int M, co
 
 // Interpolation U_k = sum over 4^3 faces of (phi/n)^3 * u(face)
 // (src/ib/grid.h:68-84 with volume h^3, src/ib/eulerian_grid.h:45).
-template <typename T>
-__global__ void k_interp(Dims d, int M, const int* __restrict__ perm, MarkerW<T> mw, const T* __restrict__ u,
-                         const T* __restrict__ v, const T* __restrict__ w, double* __restrict__ U) {
+template <typename T, typename TF>
+__global__ void k_interp(Dims d, int M, const int* __restrict__ perm, MarkerW<T> mw, const TF* __restrict__ u,
+                         const TF* __restrict__ v, const TF* __restrict__ w, double* __restrict__ U) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= M) return;
     const int k = perm ? perm[p] : p;
     const int ext[3] = {d.nx, d.ny, d.nz};
     for (int comp = 0; comp < 3; ++comp) {
-        const T* src = comp == 0 ? u : (comp == 1 ? v : w);
+        const TF* src = comp == 0 ? u : (comp == 1 ? v : w);
         int idx[3][4];
         T wt[3][4];
 #pragma unroll
@@ -413,7 +413,7 @@ __global__ void k_interp(Dims d, int M, const int* __restrict__ perm, MarkerW<T>
                 const T wyz = wt[1][my] * wt[2][mz];
                 const long long row = (long long)d.nx * (idx[1][my] + (long long)d.ny * idx[2][mz]);
 #pragma unroll
-                for (int mx = 0; mx < 4; ++mx) acc += wt[0][mx] * wyz * src[row + idx[0][mx]];
+                for (int mx = 0; mx < 4; ++mx) acc += wt[0][mx] * wyz * T(src[row + idx[0][mx]]);
             }
         U[(size_t)comp * M + k] = (double)acc;
     }
@@ -489,11 +489,14 @@ void launch_spread_gather(const Dims& d, int TS, int M, const int* perm, MarkerW
                           double scale, const int* tstart, const int* tend, const int* list, const int* count,
                           int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, cudaStream_t s) {
     const size_t smem = spread_smem_bytes<T>(TS, cap);
-    static bool configured[2] = {false, false};
+    // opt in to exactly the dynamic shared memory this launch uses (the
+    // kernel's static shared memory counts against the same 227 KB)
+    static size_t configured[2] = {0, 0};
     const int slot = sizeof(T) == 8 ? 0 : 1;
-    if (!configured[slot]) {
-        cudaFuncSetAttribute(k_spread_gather<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        configured[slot] = true;
+    if (configured[slot] < smem) {
+        if (cudaFuncSetAttribute(k_spread_gather<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return;  // the launch error is reported by the caller's cudaGetLastError
+        configured[slot] = smem;
     }
     int blocks = max_tiles < 152 * 2 ? max_tiles : 152 * 2;
     if (blocks < 1) blocks = 1;
@@ -501,10 +504,10 @@ void launch_spread_gather(const Dims& d, int TS, int M, const int* perm, MarkerW
                                                           count, cap, fu, fv, fw, flag);
 }
 
-template <typename T>
-void launch_interp(const Dims& d, int M, const int* perm, MarkerW<T> mw, const T* u, const T* v, const T* w, double* U,
+template <typename T, typename TF>
+void launch_interp(const Dims& d, int M, const int* perm, MarkerW<T> mw, const TF* u, const TF* v, const TF* w, double* U,
                    cudaStream_t s) {
-    if (M > 0) k_interp<T><<<(M + 127) / 128, 128, 0, s>>>(d, M, perm, mw, u, v, w, U);
+    if (M > 0) k_interp<T, TF><<<(M + 127) / 128, 128, 0, s>>>(d, M, perm, mw, u, v, w, U);
 }
 
 void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, double c, cudaStream_t s) {
@@ -519,8 +522,8 @@ void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, do
     template void launch_spread_gather<T>(const Dims&, int, int, const int*, MarkerW<T>, const T*, const double*, \
                                           double, const int*, const int*, const int*, const int*, int, int, T*,  \
                                           T*, T*, int*, cudaStream_t);                                          \
-    template void launch_interp<T>(const Dims&, int, const int*, MarkerW<T>, const T*, const T*, const T*,       \
-                                   double*, cudaStream_t);
+    template void launch_interp<T, double>(const Dims&, int, const int*, MarkerW<T>, const double*, const double*, \
+                                           const double*, double*, cudaStream_t);
 
 AFMIB_IB_INST(double)
 AFMIB_IB_INST(float)

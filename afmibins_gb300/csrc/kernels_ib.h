@@ -45,8 +45,9 @@ void launch_spread_gather(const Dims& d, int TS, int M, const int* perm, MarkerW
                           int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, cudaStream_t s);
 
 // U[c*M + k] = sum (phi/n)^3 u_c(face); perm (may be null) orders the threads.
-template <typename T>
-void launch_interp(const Dims& d, int M, const int* perm, MarkerW<T> mw, const T* u, const T* v, const T* w, double* U,
+// T: weight and arithmetic type, TF: field storage type
+template <typename T, typename TF>
+void launch_interp(const Dims& d, int M, const int* perm, MarkerW<T> mw, const TF* u, const TF* v, const TF* w, double* U,
                    cudaStream_t s);
 
 void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, double c, cudaStream_t s);

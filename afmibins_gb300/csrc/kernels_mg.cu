@@ -65,6 +65,25 @@ __global__ void __launch_bounds__(kRedBlock) k_residual_norm(Dims d, T* __restri
     grid_sum<1>(acc, sc, out);
 }
 
+// Mixed form: defect of the FP64 potential, r = b - L x evaluated in FP64 and
+// stored in TD for the FP32 inner V-cycles; out[0] = r.r.
+template <typename TD>
+__global__ void __launch_bounds__(kRedBlock) k_lap_defect(Dims d, TD* __restrict__ r, const double* __restrict__ xv,
+                                                         const double* __restrict__ b, RedScratch sc, double* out) {
+    const long long N = d.ncell(), sxy = d.sxy();
+    const double off = double(d.n) * double(d.n);
+    double acc[1] = {0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+        const int xi = (int)(i % d.nx), yi = (int)((i % sxy) / d.nx), zi = (int)(i / sxy);
+        double S, c;
+        lap_row(d, xv, xi, yi, zi, S, c);
+        const double ri = b[i] - off * (S - c * xv[i]);
+        r[i] = TD(ri);
+        acc[0] += ri * ri;
+    }
+    grid_sum<1>(acc, sc, out);
+}
+
 // One colour of red-black Gauss–Seidel: x_i = (b_i - n^2 S) / (-c n^2).
 template <typename T>
 __global__ void k_rbgs(Dims d, int color, T* __restrict__ xv, const T* __restrict__ b) {
@@ -260,6 +279,13 @@ void launch_prolong_assign(const Dims& d, T* fine, const T* coarse, cudaStream_t
     dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz / 2);
     k_prolong<T, false><<<g, dim3(BX, BY), 0, s>>>(d, fine, coarse);
 }
+template <typename TD>
+void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, RedScratch sc, double* out, cudaStream_t s) {
+    k_lap_defect<TD><<<red_blocks(d.ncell()), kRedBlock, 0, s>>>(d, r, x, b, sc, out);
+}
+template void launch_lap_defect<float>(const Dims&, float*, const double*, const double*, RedScratch, double*,
+                                       cudaStream_t);
+
 template <typename T>
 void launch_coarse_solve(const Dims& d, T* x, T* b, T* r, T* p, T* q, double tol, int maxit, int* status, cudaStream_t s) {
     k_coarse_cg<T><<<1, kRedBlock, 0, s>>>(d, x, b, r, p, q, tol, maxit, status);

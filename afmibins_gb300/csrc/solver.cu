@@ -18,10 +18,12 @@
 
 using namespace afmib;
 
-struct MGLevel {
+template <typename T>
+struct MGLevelT {
     Dims d;
-    double *x, *b, *r;
+    T *x, *b, *r;
 };
+typedef MGLevelT<double> MGLevel;
 
 struct afmib_solver {
     afmib_config cfg{};
@@ -40,6 +42,16 @@ struct afmib_solver {
     double *tmp[3] = {};
     std::vector<MGLevel> lv;
     double *cw_p = nullptr, *cw_q = nullptr;
+
+    // mixed form: FP32 inner workspaces (advection, forces, defects,
+    // corrections, CG vectors, FP32 multigrid hierarchy) and the FP64 copy of
+    // the coarsest level, which is solved in FP64
+    bool mixed = false;
+    float *adv32[3] = {}, *f32[3] = {}, *d32 = nullptr, *e32 = nullptr;
+    float *cg32_r = nullptr, *cg32_p = nullptr, *cg32_q = nullptr;
+    std::vector<MGLevelT<float>> lv32;
+    double *cx64 = nullptr, *cb64 = nullptr, *cr64 = nullptr;
+    int inner_cycles = 3;
     RedScratch red{};
     double* scal = nullptr;   // device scalars: [0..4] CG, [8] sum, [9] sumsq
     double* hscal = nullptr;  // pinned mirror
@@ -57,6 +69,8 @@ struct afmib_solver {
     int TS = 0, ntx = 0, nty = 0, ntz = 0, ntiles = 0;
     int *tstart = nullptr, *tend = nullptr, *tlist = nullptr, *tcount = nullptr;
     MarkerW<double> mw{};
+    MarkerW<float> mw32{};
+    float* G32 = nullptr;
 
     // per-kernel event timing (afmib_profile_*): ranges recorded around each
     // launch while enabled, resolved at the next synchronisation
@@ -159,12 +173,13 @@ int sync(afmib_solver* s) {
 enum ProfId {
     P_ADVECT, P_HELM_RHS, P_CG_INIT, P_CG_APPLY, P_CG_UPDATE, P_CG_DIR, P_RBGS, P_RESID, P_RESID_NORM,
     P_RESTRICT, P_PROLONG, P_COARSE, P_DIV, P_GRAD_SUB, P_MEAN, P_WALL, P_SPRINGS, P_PREP, P_SORT,
-    P_TILES, P_SPREAD, P_INTERP, P_MARKER, P_COUNT
+    P_TILES, P_SPREAD, P_INTERP, P_MARKER, P_HELM_DEFECT, P_LAP_DEFECT, P_CORRECT, P_COUNT
 };
 const char* kProfNames[P_COUNT] = {
     "advect", "helm_rhs", "cg_init", "cg_apply", "cg_update", "cg_direction", "mg_rbgs", "mg_residual",
     "mg_residual_norm", "mg_restrict", "mg_prolong_add", "mg_coarse_cg", "div", "grad_sub", "mean_removal",
-    "wall_update", "springs", "marker_prep", "radix_sort", "tile_bins", "spread_gather", "interp", "marker_update"};
+    "wall_update", "springs", "marker_prep", "radix_sort", "tile_bins", "spread_gather", "interp", "marker_update",
+    "helm_defect_fp64", "lap_defect_fp64", "add_correction_fp64"};
 
 cudaEvent_t prof_event(afmib_solver* s) {
     if (!s->prof_pool.empty()) {
@@ -272,50 +287,73 @@ int cg_solve(afmib_solver* s, int comp, double scale, double* x, const double* b
 // (3N s, so 1.5N s per colour launch); residual 3N s; restriction N s + N/8 s;
 // prolongation-add 2N s + N/8 s.
 // ---------------------------------------------------------------------------
-int smooth(afmib_solver* s, MGLevel& L, int sweeps) {
-    const double Ns = (double)L.d.ncell() * sizeof(double);
+template <typename T>
+std::vector<MGLevelT<T>>& levels(afmib_solver* s);
+template <>
+std::vector<MGLevelT<double>>& levels<double>(afmib_solver* s) { return s->lv; }
+template <>
+std::vector<MGLevelT<float>>& levels<float>(afmib_solver* s) { return s->lv32; }
+
+template <typename T>
+int smooth(afmib_solver* s, MGLevelT<T>& L, int sweeps) {
+    const double Ns = (double)L.d.ncell() * sizeof(T);
     for (int j = 0; j < sweeps; ++j) {
         {
             ProfScope ps(s, P_RBGS, 1.5 * Ns);
-            launch_rbgs<double>(L.d, 0, L.x, L.b, s->st);
+            launch_rbgs<T>(L.d, 0, L.x, L.b, s->st);
         }
         {
             ProfScope ps(s, P_RBGS, 1.5 * Ns);
-            launch_rbgs<double>(L.d, 1, L.x, L.b, s->st);
+            launch_rbgs<T>(L.d, 1, L.x, L.b, s->st);
         }
     }
     CKL();
     return AFMIB_OK;
 }
 
+// coarsest level: FP64 solve (the FP32 hierarchy hands its level to FP64)
+int coarse(afmib_solver* s, MGLevelT<double>& L) {
+    ProfScope ps(s, P_COARSE, 3.0 * L.d.ncell() * sizeof(double));
+    launch_coarse_solve<double>(L.d, L.x, L.b, L.r, s->cw_p, s->cw_q, s->cfg.tol, s->cfg.max_cg_iters, s->dflag + 1,
+                                s->st);
+    return AFMIB_OK;
+}
+int coarse(afmib_solver* s, MGLevelT<float>& L) {
+    const long long n = L.d.ncell();
+    ProfScope ps(s, P_COARSE, 3.0 * n * sizeof(double), 3);
+    launch_convert<double, float>(n, s->cb64, L.b, s->st);
+    launch_coarse_solve<double>(L.d, s->cx64, s->cb64, s->cr64, s->cw_p, s->cw_q, s->cfg.tol, s->cfg.max_cg_iters,
+                                s->dflag + 1, s->st);
+    launch_convert<float, double>(n, L.x, s->cx64, s->st);
+    return AFMIB_OK;
+}
+
+template <typename T>
 int vcycle(afmib_solver* s, size_t l) {
-    MGLevel& L = s->lv[l];
-    const double Ns = (double)L.d.ncell() * sizeof(double);
-    if (l + 1 == s->lv.size()) {
-        {
-            ProfScope ps(s, P_COARSE, 3 * Ns);
-            launch_coarse_solve<double>(L.d, L.x, L.b, L.r, s->cw_p, s->cw_q, s->cfg.tol, s->cfg.max_cg_iters,
-                                        s->dflag + 1, s->st);
-        }
+    auto& lv = levels<T>(s);
+    MGLevelT<T>& L = lv[l];
+    const double Ns = (double)L.d.ncell() * sizeof(T);
+    if (l + 1 == lv.size()) {
+        TRY(coarse(s, L));
         CKL();
         return AFMIB_OK;
     }
     TRY(smooth(s, L, s->cfg.nu1));
     {
         ProfScope ps(s, P_RESID, 3 * Ns);
-        launch_residual<double>(L.d, L.r, L.x, L.b, nullptr, nullptr, s->st);
+        launch_residual<T>(L.d, L.r, L.x, L.b, nullptr, nullptr, s->st);
     }
-    MGLevel& C = s->lv[l + 1];
+    MGLevelT<T>& C = lv[l + 1];
     {
         ProfScope ps(s, P_RESTRICT, Ns + Ns / 8);
-        launch_restrict<double>(L.d, C.b, L.r, s->st);
+        launch_restrict<T>(L.d, C.b, L.r, s->st);
     }
-    CK(cudaMemsetAsync(C.x, 0, C.d.ncell() * sizeof(double), s->st));
+    CK(cudaMemsetAsync(C.x, 0, C.d.ncell() * sizeof(T), s->st));
     CKL();
-    TRY(vcycle(s, l + 1));
+    TRY(vcycle<T>(s, l + 1));
     {
         ProfScope ps(s, P_PROLONG, 2 * Ns + Ns / 8);
-        launch_prolong_add<double>(L.d, L.x, C.x, s->st);
+        launch_prolong_add<T>(L.d, L.x, C.x, s->st);
     }
     TRY(smooth(s, L, s->cfg.nu2));
     return AFMIB_OK;
@@ -338,7 +376,7 @@ int mg_solve(afmib_solver* s, int* cycles) {
     int status = AFMIB_OK;
     int c = 0;
     if (s->lv.size() == 1) {
-        TRY(vcycle(s, 0));
+        TRY(vcycle<double>(s, 0));
     } else {
         for (;;) {
             {
@@ -352,7 +390,7 @@ int mg_solve(afmib_solver* s, int* cycles) {
             if (!std::isfinite(rms)) { status = s->fail(AFMIB_ERR_NAN, "multigrid residual is not finite"); break; }
             if (rms <= s->cfg.tol) break;
             if (c >= s->cfg.max_mg_cycles) { status = s->fail(AFMIB_ERR_NOCONV, "multigrid cycle cap reached"); break; }
-            TRY(vcycle(s, 0));
+            TRY(vcycle<double>(s, 0));
             ++c;
         }
     }
@@ -360,6 +398,121 @@ int mg_solve(afmib_solver* s, int* cycles) {
     TRY(sync(s));
     if (status == AFMIB_OK && s->hflag[1] != 0) status = s->fail(AFMIB_ERR_NOCONV, "coarsest-level CG did not converge");
     s->stats.mg_cycles += c;
+    if (cycles) *cycles = c;
+    return status;
+}
+
+// ---------------------------------------------------------------------------
+// Mixed form. FP64 defect correction around FP32 inner solves: the residual
+// of the FP64 iterate is evaluated in FP64 and handed to the FP32 solver as an
+// FP32 defect; the FP32 correction is added to the FP64 iterate. The stopping
+// tests are the reference's (CG: ||r||_2 <= tol, MG: RMS(r) <= tol) on the
+// FP64 residual, so the converged iterate has the FP64 form's accuracy.
+// ---------------------------------------------------------------------------
+int cg_inner32(afmib_solver* s, int comp, double scale, double rel_tol, int* iters) {
+    const Dims& d = s->d;
+    const long long N = s->N();
+    const double Ns = (double)N * sizeof(float);
+    {
+        ProfScope ps(s, P_CG_INIT, 4 * Ns);
+        launch_cg_init_zero<float>(N, s->d32, s->e32, s->cg32_r, s->cg32_p, s->red, s->scal, s->st);
+    }
+    CKL();
+    TRY(read_scalars(s, 0, 1));
+    const double stop = rel_tol * std::sqrt(s->hscal[0]);
+    int it = 0;
+    while (std::sqrt(s->hscal[0]) > stop && it < s->cfg.max_cg_iters) {
+        if (!std::isfinite(s->hscal[0])) return s->fail(AFMIB_ERR_NAN, "inner CG residual is not finite");
+        {
+            ProfScope ps(s, P_CG_APPLY, 2 * Ns);
+            launch_cg_apply<float>(d, comp, scale, s->cg32_p, s->cg32_q, s->red, s->scal, s->st);
+        }
+        {
+            ProfScope ps(s, P_CG_UPDATE, 6 * Ns);
+            launch_cg_update<float>(N, s->e32, s->cg32_r, s->cg32_p, s->cg32_q, s->red, s->scal, s->st);
+        }
+        CK(cudaMemcpyAsync(s->hscal, s->scal, sizeof(double), cudaMemcpyDeviceToHost, s->st));
+        {
+            ProfScope ps(s, P_CG_DIR, 3 * Ns);
+            launch_cg_direction<float>(N, s->cg32_p, s->cg32_r, s->scal, s->st);
+        }
+        CKL();
+        TRY(sync(s));
+        ++it;
+    }
+    s->stats.cg_iters += it;
+    if (iters) *iters = it;
+    return AFMIB_OK;
+}
+
+int helm_solve_mixed(afmib_solver* s, int comp, double scale, double* x, const double* b) {
+    const long long N = s->N();
+    int outer = 0;
+    for (;;) {
+        {
+            ProfScope ps(s, P_HELM_DEFECT, (double)N * (8 + 8 + 4));
+            launch_helm_defect<float>(s->d, comp, scale, x, b, s->d32, s->red, s->scal + 10, s->st);
+        }
+        CKL();
+        TRY(read_scalars(s, 10, 1));
+        const double nr = std::sqrt(s->hscal[10]);
+        s->stats.last_cg_norm = nr;
+        if (!std::isfinite(nr)) return s->fail(AFMIB_ERR_NAN, "Helmholtz residual is not finite");
+        if (nr <= s->cfg.tol) break;
+        if (outer >= s->cfg.max_mg_cycles) return s->fail(AFMIB_ERR_NOCONV, "defect-correction cap reached (Helmholtz)");
+        TRY(cg_inner32(s, comp, scale, s->cfg.inner_tol, nullptr));
+        {
+            ProfScope ps(s, P_CORRECT, (double)N * (8 + 4 + 8));
+            launch_add_correction<float>(N, x, s->e32, s->st);
+        }
+        CKL();
+        ++outer;
+    }
+    s->stats.outer_iters += outer;
+    return AFMIB_OK;
+}
+
+int mg_solve_mixed(afmib_solver* s, int* cycles) {
+    MGLevel& L = s->lv[0];
+    MGLevelT<float>& L32 = s->lv32[0];
+    const long long N = L.d.ncell();
+    const double Ns = (double)N * sizeof(double);
+    {
+        ProfScope ps(s, P_MEAN, 3 * Ns, 2);
+        launch_sum<double>(N, L.b, s->red, s->scal + 8, s->st);
+        launch_sub_scalar_scaled<double>(N, L.b, s->scal + 8, 1.0 / (double)N, s->st);
+    }
+    CK(cudaMemsetAsync(L.x, 0, N * sizeof(double), s->st));
+    CK(cudaMemsetAsync(s->dflag + 1, 0, sizeof(int), s->st));
+    int c = 0, outer = 0;
+    int status = AFMIB_OK;
+    for (;;) {
+        {
+            ProfScope ps(s, P_LAP_DEFECT, (double)N * (8 + 8 + 4));
+            launch_lap_defect<float>(L.d, L32.b, L.x, L.b, s->red, s->scal + 9, s->st);
+        }
+        CKL();
+        TRY(read_scalars(s, 9, 1));
+        const double rms = std::sqrt(s->hscal[9]) / std::sqrt((double)N);
+        s->stats.last_mg_rms = rms;
+        if (!std::isfinite(rms)) { status = s->fail(AFMIB_ERR_NAN, "multigrid residual is not finite"); break; }
+        if (rms <= s->cfg.tol) break;
+        if (c >= s->cfg.max_mg_cycles) { status = s->fail(AFMIB_ERR_NOCONV, "multigrid cycle cap reached"); break; }
+        CK(cudaMemsetAsync(L32.x, 0, N * sizeof(float), s->st));
+        for (int k = 0; k < s->inner_cycles; ++k) TRY(vcycle<float>(s, 0));
+        c += s->inner_cycles;
+        {
+            ProfScope ps(s, P_CORRECT, (double)N * (8 + 4 + 8));
+            launch_add_correction<float>(N, L.x, L32.x, s->st);
+        }
+        CKL();
+        ++outer;
+    }
+    CK(cudaMemcpyAsync(s->hflag + 1, s->dflag + 1, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    TRY(sync(s));
+    if (status == AFMIB_OK && s->hflag[1] != 0) status = s->fail(AFMIB_ERR_NOCONV, "coarsest-level CG did not converge");
+    s->stats.mg_cycles += c;
+    s->stats.outer_iters += outer;
     if (cycles) *cycles = c;
     return status;
 }
@@ -372,7 +525,8 @@ int project(afmib_solver* s) {
         launch_div<double>(s->d, s->lv[0].b, s->u, s->v, s->w, nullptr, nullptr, s->st);
     }
     CKL();
-    TRY(mg_solve(s, nullptr));
+    if (s->mixed) TRY(mg_solve_mixed(s, nullptr));
+    else TRY(mg_solve(s, nullptr));
     {
         ProfScope ps(s, P_GRAD_SUB, 7 * Ns);
         launch_grad_sub<double>(s->d, s->u, s->v, s->w, s->lv[0].x, s->d.channel ? s->wallgrad : nullptr, s->st);
@@ -381,14 +535,18 @@ int project(afmib_solver* s) {
     return AFMIB_OK;
 }
 
-// ns::solver::step, src/ns/solver.h:90-140; forces already in s->f.
+// ns::solver::step, src/ns/solver.h:90-140; forces already in s->f (FP64
+// form) or s->f32 (mixed form).
 int substep(afmib_solver* s) {
     const Dims& d = s->d;
     const long long N = s->N();
     const double Ns = (double)N * sizeof(double);
-    {
+    if (s->mixed) {
+        ProfScope ps(s, P_ADVECT, (double)N * (3 * 8 + 3 * 4));
+        launch_advect<double, float>(d, s->adv32[0], s->adv32[1], s->adv32[2], s->u, s->v, s->w, s->st);
+    } else {
         ProfScope ps(s, P_ADVECT, 6 * Ns);
-        launch_advect<double>(d, s->adv[0], s->adv[1], s->adv[2], s->u, s->v, s->w, s->st);
+        launch_advect<double, double>(d, s->adv[0], s->adv[1], s->adv[2], s->u, s->v, s->w, s->st);
     }
     CKL();
     const bool be = !s->half;
@@ -410,13 +568,22 @@ int substep(afmib_solver* s) {
     for (int c = 0; c < 3; ++c) {
         const double* top = (!d.channel || c == 1) ? nullptr : (c == 0 ? ut : wt);
         const double* bot = (!d.channel || c == 1) ? nullptr : (c == 0 ? ub : wb);
-        ProfScope ps(s, P_HELM_RHS, 4 * Ns);
-        launch_helm_rhs<double>(d, c, be ? 1 : 0, s->rhs[c], s->uo[c], s->f[c], s->adv[c], top, bot, s->s_plus(),
-                                s->s_minus(), s->cfg.dt, inv_rho, s->st);
+        if (s->mixed) {
+            ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 4 + 4 + 8));
+            launch_helm_rhs<double, float>(d, c, be ? 1 : 0, s->rhs[c], s->uo[c], s->f32[c], s->adv32[c], top, bot,
+                                           s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
+        } else {
+            ProfScope ps(s, P_HELM_RHS, 4 * Ns);
+            launch_helm_rhs<double, double>(d, c, be ? 1 : 0, s->rhs[c], s->uo[c], s->f[c], s->adv[c], top, bot,
+                                            s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
+        }
     }
     CKL();
     double* vel[3] = {s->u, s->v, s->w};
-    for (int c = 0; c < 3; ++c) TRY(cg_solve(s, c, s->s_minus(), vel[c], s->rhs[c], nullptr));
+    for (int c = 0; c < 3; ++c) {
+        if (s->mixed) TRY(helm_solve_mixed(s, c, s->s_minus(), vel[c], s->rhs[c]));
+        else TRY(cg_solve(s, c, s->s_minus(), vel[c], s->rhs[c], nullptr));
+    }
     TRY(project(s));
     s->half = !s->half;
     s->stats.half = s->half ? 1 : 0;
@@ -463,6 +630,10 @@ int marker_alloc(afmib_solver* s, int M, int nnz) {
         TRY(regrow(s, &s->mw.cell, 3 * (size_t)M, 0));
         TRY(regrow(s, &s->mw.dbase, 6 * (size_t)M, 0));
         TRY(regrow(s, &s->mw.w, 24 * (size_t)M, 0));
+        TRY(regrow(s, &s->mw32.cell, 3 * (size_t)M, 0));
+        TRY(regrow(s, &s->mw32.dbase, 6 * (size_t)M, 0));
+        TRY(regrow(s, &s->mw32.w, 24 * (size_t)M, 0));
+        TRY(regrow(s, &s->G32, 3 * (size_t)M, 0));
         s->Mcap = M;
     }
     if (nnz > s->nnz_cap) {
@@ -480,10 +651,13 @@ int key_bits(afmib_solver* s) {
 }
 
 // weights + bins of the markers at P (device, [M][3])
-int bin_markers(afmib_solver* s, const double* P) {
+int bin_markers(afmib_solver* s, const double* P, bool fp32 = false) {
     const int M = s->M;
     const int passes = (key_bits(s) + 7) / 8;
-    {
+    if (fp32) {
+        ProfScope ps(s, P_PREP, (double)M * (24 + 4 + 4 + 12 + 6 + 24 * 4));
+        launch_marker_prep<float>(s->d, s->TS, M, P, s->keys, s->vals, s->mw32, s->dflag, s->st);
+    } else {
         ProfScope ps(s, P_PREP, (double)M * (24 + 4 + 4 + 12 + 6 + 24 * 8));
         launch_marker_prep<double>(s->d, s->TS, M, P, s->keys, s->vals, s->mw, s->dflag, s->st);
     }
@@ -526,6 +700,22 @@ int spread_forces(afmib_solver* s, const double* vol, double* fu, double* fv, do
     return AFMIB_OK;
 }
 
+int spread_forces32(afmib_solver* s, const double* vol) {
+    const long long N = s->N();
+    for (int c = 0; c < 3; ++c) CK(cudaMemsetAsync(s->f32[c], 0, N * sizeof(float), s->st));
+    const double n3 = (double)s->d.n * s->d.n * s->d.n;
+    const int cap = 2560;
+    const double touched = (double)s->stats.spread_tiles * s->TS * s->TS * s->TS;
+    {
+        ProfScope ps(s, P_SPREAD, (double)s->M * (24 + 3 * 4 + 8 + 8) + 3 * touched * 4);
+        launch_spread_gather<float>(s->d, s->TS, s->M, s->perm, s->mw32, s->G32, vol, n3, s->tstart, s->tend,
+                                    s->tlist, s->tcount, s->ntiles, cap, s->f32[0], s->f32[1], s->f32[2], s->dflag,
+                                    s->st);
+    }
+    CKL();
+    return AFMIB_OK;
+}
+
 int check_marker_flag(afmib_solver* s) {
     CK(cudaMemcpyAsync(s->hflag, s->dflag, sizeof(int), cudaMemcpyDeviceToHost, s->st));
     CK(cudaMemcpyAsync(s->hflag + 2, s->tcount, sizeof(int), cudaMemcpyDeviceToHost, s->st));
@@ -538,10 +728,11 @@ int check_marker_flag(afmib_solver* s) {
     return AFMIB_OK;
 }
 
-int interp_markers(afmib_solver* s, const double* u, const double* v, const double* w, double* U) {
+int interp_markers(afmib_solver* s, const double* u, const double* v, const double* w, double* U, bool fp32 = false) {
     const double touched = (double)s->stats.spread_tiles * s->TS * s->TS * s->TS;
     ProfScope ps(s, P_INTERP, 3 * touched * 8 + (double)s->M * (24 + 3 * 8 + 8));
-    launch_interp<double>(s->d, s->M, s->perm, s->mw, u, v, w, U, s->st);
+    if (fp32) launch_interp<float, double>(s->d, s->M, s->perm, s->mw32, u, v, w, U, s->st);
+    else launch_interp<double, double>(s->d, s->M, s->perm, s->mw, u, v, w, U, s->st);
     return AFMIB_OK;
 }
 
@@ -550,30 +741,31 @@ int ib_one_step(afmib_solver* s) {
     const double dt = s->cfg.dt;
     const double* vol = s->has_vol ? s->mvol : nullptr;
     const double mbytes = (double)M * (24 + 24 + 24);
+    const bool f32 = s->mixed;
+    auto springs = [&](const double* P) {
+        ProfScope ps(s, P_SPRINGS, mbytes);
+        if (f32) launch_springs<float>(M, P, s->nstart, s->nidx, s->cfg.k_spring, s->G32, s->st);
+        else launch_springs<double>(M, P, s->nstart, s->nidx, s->cfg.k_spring, s->G, s->st);
+    };
+    auto spread = [&]() { return f32 ? spread_forces32(s, vol) : spread_forces(s, vol, s->f[0], s->f[1], s->f[2]); };
     CK(cudaMemsetAsync(s->dflag, 0, sizeof(int), s->st));
     // BE half: forces at X^n
-    {
-        ProfScope ps(s, P_SPRINGS, mbytes);
-        launch_springs<double>(M, s->X, s->nstart, s->nidx, s->cfg.k_spring, s->G, s->st);
-    }
-    TRY(bin_markers(s, s->X));
-    TRY(spread_forces(s, vol, s->f[0], s->f[1], s->f[2]));
+    springs(s->X);
+    TRY(bin_markers(s, s->X, f32));
+    TRY(spread());
     TRY(substep(s));
     // velocity at t+dt/2: at X^n for the half-step, then at X^{n+1/2}
-    TRY(interp_markers(s, s->u, s->v, s->w, s->U1));
+    TRY(interp_markers(s, s->u, s->v, s->w, s->U1, f32));
     {
         ProfScope ps(s, P_MARKER, mbytes);
         launch_marker_axpy(M, s->Xh, s->X, s->U1, dt / 2, s->st);
     }
-    TRY(bin_markers(s, s->Xh));
-    TRY(interp_markers(s, s->u, s->v, s->w, s->U2));
+    TRY(bin_markers(s, s->Xh, f32));
+    TRY(interp_markers(s, s->u, s->v, s->w, s->U2, f32));
     // CN step with forces at X^{n+1/2}
-    {
-        ProfScope ps(s, P_SPRINGS, mbytes);
-        launch_springs<double>(M, s->Xh, s->nstart, s->nidx, s->cfg.k_spring, s->G, s->st);
-    }
+    springs(s->Xh);
     CKL();
-    TRY(spread_forces(s, vol, s->f[0], s->f[1], s->f[2]));
+    TRY(spread());
     TRY(substep(s));
     {
         ProfScope ps(s, P_MARKER, mbytes);
@@ -615,7 +807,8 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (g.inner_tol <= 0) g.inner_tol = 1e-5;
     if (g.nx < 2 || g.ny < 2 || g.nz < 2) return s->fail(AFMIB_ERR_ARG, "every extent must be at least 2 cells");
     if (g.bc != AFMIB_BC_PERIODIC && g.bc != AFMIB_BC_CHANNEL) return s->fail(AFMIB_ERR_ARG, "bc must be periodic or channel");
-    if (g.precision != AFMIB_FP64) return s->fail(AFMIB_ERR_ARG, "only the FP64 form is available in this build");
+    if (g.precision != AFMIB_FP64 && g.precision != AFMIB_MIXED) return s->fail(AFMIB_ERR_ARG, "precision");
+    s->mixed = g.precision == AFMIB_MIXED;
     if (!(g.rho > 0) || !(g.dt > 0) || !(g.mu >= 0) || !(g.tol > 0)) return s->fail(AFMIB_ERR_ARG, "mu, rho, dt, tol");
     s->d = Dims{g.nx, g.ny, g.nz, g.n, g.bc == AFMIB_BC_CHANNEL ? 1 : 0};
     if (stream) {
@@ -689,6 +882,28 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     const long long nc = s->lv.back().d.ncell();
     TRY(dalloc(s, &s->cw_p, nc));
     TRY(dalloc(s, &s->cw_q, nc));
+    if (s->mixed) {
+        for (int k = 0; k < 3; ++k) {
+            TRY(dalloc(s, &s->adv32[k], N));
+            TRY(dalloc(s, &s->f32[k], N));
+            CK(cudaMemsetAsync(s->f32[k], 0, N * sizeof(float), s->st));
+        }
+        TRY(dalloc(s, &s->d32, N));
+        TRY(dalloc(s, &s->e32, N));
+        TRY(dalloc(s, &s->cg32_r, N));
+        TRY(dalloc(s, &s->cg32_p, N));
+        TRY(dalloc(s, &s->cg32_q, N));
+        for (const MGLevel& L : s->lv) {
+            MGLevelT<float> F{L.d, nullptr, nullptr, nullptr};
+            TRY(dalloc(s, &F.x, L.d.ncell()));
+            TRY(dalloc(s, &F.b, L.d.ncell()));
+            TRY(dalloc(s, &F.r, L.d.ncell()));
+            s->lv32.push_back(F);
+        }
+        TRY(dalloc(s, &s->cx64, nc));
+        TRY(dalloc(s, &s->cb64, nc));
+        TRY(dalloc(s, &s->cr64, nc));
+    }
     CK(cudaStreamSynchronize(s->st));
     return AFMIB_OK;
 }
@@ -806,6 +1021,9 @@ int afmib_ns_step(afmib_solver* s, const double* fx, const double* fy, const dou
     if (fy) TRY(v_in(s, s->f[1], fy));
     else CK(cudaMemsetAsync(s->f[1], 0, s->N() * sizeof(double), s->st));
     TRY(copy_in(s, s->f[2], fz, s->N()));
+    if (s->mixed)
+        for (int c = 0; c < 3; ++c) launch_convert<float, double>(s->N(), s->f32[c], s->f[c], s->st);
+    CKL();
     TRY(substep(s));
     return sync(s);
 }
@@ -901,7 +1119,7 @@ int afmib_advection(afmib_solver* s, double* ua, double* va, double* wa, const d
     TRY(copy_in(s, s->tmp[0], u, N));
     TRY(v_in(s, s->tmp[1], v));
     TRY(copy_in(s, s->tmp[2], w, N));
-    launch_advect<double>(s->d, s->rhs[0], s->rhs[1], s->rhs[2], s->tmp[0], s->tmp[1], s->tmp[2], s->st);
+    launch_advect<double, double>(s->d, s->rhs[0], s->rhs[1], s->rhs[2], s->tmp[0], s->tmp[1], s->tmp[2], s->st);
     CKL();
     TRY(copy_out(s, ua, s->rhs[0], N));
     TRY(v_out(s, va, s->rhs[1]));
