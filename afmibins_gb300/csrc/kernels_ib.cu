@@ -259,6 +259,17 @@ __global__ void __launch_bounds__(512) k_spread_gather(Dims d, int TS, int M, co
             if (d.channel && (yy < 0 || yy >= nty)) continue;
             yy = wrapi(yy, nty);
             const int n = wrapi(tx + dx, ntx) + ntx * (yy + nty * wrapi(tz + dz, ntz));
+            // with fewer than three tiles along an axis the -1 and +1
+            // neighbours coincide: visit every tile once
+            bool seen = false;
+            for (int pb = 0; pb < nb && !seen; ++pb) {
+                const int px = pb % 3 - 1, py = (pb / 3) % 3 - 1, pz = pb / 9 - 1;
+                int qy = ty + py;
+                if (d.channel && (qy < 0 || qy >= nty)) continue;
+                qy = wrapi(qy, nty);
+                seen = (wrapi(tx + px, ntx) + ntx * (qy + nty * wrapi(tz + pz, ntz))) == n;
+            }
+            if (seen) continue;
             const int a = tstart[n], b = tend[n];
             for (int r0 = a; r0 < b; r0 += blockDim.x) {
                 const int p = r0 + tid;

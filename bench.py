@@ -274,20 +274,24 @@ def main():
                "steps": ke}
 
     # ---- per-kernel durations over profiled steps (events on the solver's stream)
-    sv.profile(True)
-    sv.profile_reset()
-    for _ in range(args.profile_steps):
-        sv.ib_step(1)
-    table = sv.profile_table()
-    sv.profile(False)
     peak, peak_kind = measured_peaks()
-    total_ms = sum(v[1] for v in table.values())
-    dom = max(table.items(), key=lambda kv: kv[1][1])
-    name, (nl, kms, kbytes) = dom
-    achieved = (kbytes / nl) / ((kms / nl) * 1e-3) / 1e9
-    kernels = {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / total_ms, 4),
-                   "GB_s": round(v[2] / (v[1] * 1e-3) / 1e9, 1) if v[1] > 0 else None}
-               for k, v in sorted(table.items(), key=lambda kv: -kv[1][1])}
+    roofline, kernels = None, None
+    if args.profile_steps > 0:
+        sv.profile(True)
+        sv.profile_reset()
+        for _ in range(args.profile_steps):
+            sv.ib_step(1)
+        table = sv.profile_table()
+        sv.profile(False)
+        total_ms = sum(v[1] for v in table.values())
+        name, (nl, kms, kbytes) = max(table.items(), key=lambda kv: kv[1][1])
+        achieved = (kbytes / nl) / ((kms / nl) * 1e-3) / 1e9
+        roofline = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
+                    "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                    "bytes_per_launch": kbytes / nl, "ms_per_launch": kms / nl}
+        kernels = {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / total_ms, 4),
+                       "GB_s": round(v[2] / (v[1] * 1e-3) / 1e9, 1) if v[1] > 0 else None}
+                   for k, v in sorted(table.items(), key=lambda kv: -kv[1][1])}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -300,9 +304,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic (seeded shells and solenoidal field)", "config": config_dict(args),
-            "roofline": {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                         "traffic": None, "bytes_per_launch": kbytes / nl, "ms_per_launch": kms / nl},
+            "roofline": roofline,
             "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clk.summary(),
             "solver": {"cg_iters_per_step": st["cg_iters"] / max(1, st["ib_steps"]),
                        "mg_cycles_per_step": st["mg_cycles"] / max(1, st["ib_steps"]),

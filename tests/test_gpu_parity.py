@@ -146,7 +146,7 @@ def test_ns_substeps_periodic(n):
     g, u, v, w, _, _, _ = _periodic_case(n)
     rng = np.random.default_rng(11)
     f = [rng.standard_normal(g.ncell) for _ in range(3)]
-    mu, rho, dt, tol = 0.01, 1.0, 1e-3, 1e-10
+    mu, rho, dt, tol = 0.01, 1.0, 1e-3, 1e-12
     ref = po.NSSolver(g, mu, rho, dt, tol, u, v, w)
     for _ in range(4):
         assert ref.step(*f) == 0
@@ -165,7 +165,7 @@ def test_ns_substeps_periodic(n):
 def test_ib_steps_periodic():
     n = 32
     g, u, v, w, X, nstart, nidx = _periodic_case(n, M=2000)
-    mu, rho, dt, tol, k = 0.01, 1.0, 5e-4, 1e-10, 0.5
+    mu, rho, dt, tol, k = 0.01, 1.0, 5e-4, 1e-12, 0.5
     ref = po.NSSolver(g, mu, rho, dt, tol, u, v, w)
     Xr = X.copy()
     for _ in range(3):
@@ -255,7 +255,7 @@ def test_mixed_ns_substeps(bc):
     rng = np.random.default_rng(21)
     u, v, w = 0.1 * rng.standard_normal(g.ncell), 0.1 * rng.standard_normal(g.nv), 0.1 * rng.standard_normal(g.ncell)
     f = [rng.standard_normal(g.ncell), rng.standard_normal(g.nv), rng.standard_normal(g.ncell)]
-    mu, rho, dt, tol = 0.01, 1.0, 1e-3, 1e-10
+    mu, rho, dt, tol = 0.01, 1.0, 1e-3, 1e-12
     ref = po.NSSolver(g, mu, rho, dt, tol, u, v, w)
     for _ in range(4):
         assert ref.step(*f) == 0
@@ -274,9 +274,11 @@ def test_mixed_ns_substeps(bc):
 
 
 def test_mixed_ib_steps_periodic():
+    # dt of the 256^3 benchmark configuration: the FP32 spreading error enters
+    # the velocity as dt * (FP32 rounding of the force density)
     n = 32
     g, u, v, w, X, nstart, nidx = _periodic_case(n, M=2000)
-    mu, rho, dt, tol, k = 0.01, 1.0, 5e-4, 1e-10, 0.5
+    mu, rho, dt, tol, k = 0.005, 1.0, 2e-5, 1e-12, 0.5
     ref = po.NSSolver(g, mu, rho, dt, tol, u, v, w)
     Xr = X.copy()
     for _ in range(3):
@@ -291,4 +293,4 @@ def test_mixed_ib_steps_periodic():
         Xg = sv.get_markers()
     assert rel(gu, ru) < MIXED_TOL and rel(gv, rv) < MIXED_TOL and rel(gw, rw) < MIXED_TOL
     assert rel(Xg - X, Xr - X) < 1e-6
-    assert np.max(np.abs(Xg - Xr)) < 1e-10
+    assert np.max(np.abs(Xg - Xr)) < 1e-12
