@@ -66,12 +66,17 @@ __device__ __forceinline__ void warp_sum(double (&v)[NV]) {
         for (int k = 0; k < NV; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
 }
 
-// Block-wide sum of NV values (blockDim.x == kRedBlock); result valid in thread 0.
+// linear thread / block indices for 1-D, 2-D and 3-D launches
+__device__ __forceinline__ int tid_lin() { return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z); }
+__device__ __forceinline__ int bid_lin() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
+__device__ __forceinline__ int nblk_lin() { return gridDim.x * gridDim.y * gridDim.z; }
+
+// Block-wide sum of NV values (kRedBlock threads per block); result valid in thread 0.
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV]) {
     __shared__ double s[kRedBlock / 32][NV];
     warp_sum<NV>(v);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const int w = tid_lin() >> 5, l = tid_lin() & 31;
     if (l == 0)
 #pragma unroll
         for (int k = 0; k < NV; ++k) s[w][k] = v[k];
@@ -92,12 +97,13 @@ template <int NV>
 __device__ __forceinline__ bool grid_sum(double (&v)[NV], RedScratch sc, double* out) {
     __shared__ bool last;
     block_sum<NV>(v);
-    if (threadIdx.x == 0) {
+    const int tid = tid_lin(), nb = nblk_lin();
+    if (tid == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) sc.partial[(size_t)k * kMaxRedBlocks + blockIdx.x] = v[k];
+        for (int k = 0; k < NV; ++k) sc.partial[(size_t)k * kMaxRedBlocks + bid_lin()] = v[k];
         __threadfence();
         unsigned t = atomicAdd(sc.ticket, 1u);
-        last = (t == gridDim.x - 1);
+        last = (t == (unsigned)nb - 1);
     }
     __syncthreads();
     if (last) {
@@ -105,11 +111,11 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], RedScratch sc, double*
         double a[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) a[k] = 0.0;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+        for (int b = tid; b < nb; b += kRedBlock)
 #pragma unroll
             for (int k = 0; k < NV; ++k) a[k] += __ldcg(&sc.partial[(size_t)k * kMaxRedBlocks + b]);
         block_sum<NV>(a);
-        if (threadIdx.x == 0) {
+        if (tid == 0) {
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
                 out[k] = a[k];
@@ -121,6 +127,26 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], RedScratch sc, double*
     }
     return false;
 }
+
+// Stencil reductions run on (32 x 8)-thread blocks over (x, y) tiles with
+// each thread walking z in steps of grid.z, so that no linear index is ever
+// divided; grid.z is chosen to keep the block count within kMaxRedBlocks.
+constexpr int kRBX = 32, kRBY = 8;
+inline dim3 red_grid3(int nx, int ny, int nz) {
+    const int gx = (nx + kRBX - 1) / kRBX, gy = (ny + kRBY - 1) / kRBY;
+    int gz = kMaxRedBlocks / (gx * gy);
+    if (gz > nz) gz = nz;
+    if (gz < 1) gz = 1;
+    return dim3(gx, gy, gz);
+}
+
+// Per-thread partial sums stay in the arithmetic type (one FP64 conversion
+// per thread, not per element: on GB300 conversions run on the FP64 pipe).
+template <typename T>
+struct Acc {
+    T v = T(0);
+    __device__ void add(T x) { v += x; }
+};
 
 inline int red_blocks(long long n) {
     long long b = (n + kRedBlock - 1) / kRedBlock;

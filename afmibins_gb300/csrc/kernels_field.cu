@@ -113,15 +113,26 @@ __global__ void k_grad(Dims d, T* __restrict__ px, T* __restrict__ py, T* __rest
 // the next wall update reads (src/ns/projection.h:91-94).
 template <typename T>
 __global__ void k_grad_sub(Dims d, T* __restrict__ u, T* __restrict__ v, T* __restrict__ w, const T* __restrict__ p,
-                           T* __restrict__ wg) {
+                           T* __restrict__ wg, float* __restrict__ u32, float* __restrict__ v32,
+                           float* __restrict__ w32) {
     AFMIB_XYZ
     const long long i = lin(d, x, y, z);
     const T n = T(d.n), p0 = p[i];
     const T gx = n * (p0 - p[lin(d, xm1(d, x), y, z)]);
     const T gz = n * (p0 - p[lin(d, x, y, zm1(d, z))]);
-    u[i] = u[i] - gx;
-    w[i] = w[i] - gz;
-    if (!d.channel || y > 0) v[i] = v[i] - n * (p0 - p[lin(d, x, ym1(d, y), z)]);
+    const T un = u[i] - gx, wn = w[i] - gz;
+    u[i] = un;
+    w[i] = wn;
+    T vn = v[i];
+    if (!d.channel || y > 0) {
+        vn = vn - n * (p0 - p[lin(d, x, ym1(d, y), z)]);
+        v[i] = vn;
+    }
+    if (u32) {  // FP32 shadow of the velocity for the mixed form's FP32 stencils
+        u32[i] = float(un);
+        v32[i] = float(vn);
+        w32[i] = float(wn);
+    }
     if (d.channel && wg) {
         const long long nxz = (long long)d.nx * d.nz, ixz = x + (long long)d.nx * z;
         if (y == 0) { wg[0 * nxz + ixz] = gx; wg[4 * nxz + ixz] = gz; }
@@ -216,30 +227,34 @@ template <typename T>
 __global__ void __launch_bounds__(kRedBlock) k_cg_init(Dims d, int comp, T s, const T* __restrict__ x,
                                                       const T* __restrict__ b, T* __restrict__ r, T* __restrict__ p,
                                                       RedScratch sc, double* cgs) {
-    const long long N = d.ncell(), sxy = d.sxy();
-    double acc[1] = {0.0};
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
-        const int xi = (int)(i % d.nx), yi = (int)((i % sxy) / d.nx), zi = (int)(i / sxy);
-        const T ri = b[i] - helm_point(d, comp, s, x, xi, yi, zi);
-        r[i] = ri;
-        p[i] = ri;
-        acc[0] += (double)ri * (double)ri;
-    }
-    grid_sum<1>(acc, sc, cgs + 0);
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+    T acc = T(0);
+    if (xi < d.nx && yi < d.ny)
+        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
+            const long long i = lin(d, xi, yi, zi);
+            const T ri = b[i] - helm_point(d, comp, s, x, xi, yi, zi);
+            r[i] = ri;
+            p[i] = ri;
+            acc += ri * ri;
+        }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, cgs + 0);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kRedBlock) k_cg_apply(Dims d, int comp, T s, const T* __restrict__ p,
                                                        T* __restrict__ q, RedScratch sc, double* cgs) {
-    const long long N = d.ncell(), sxy = d.sxy();
-    double acc[1] = {0.0};
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
-        const int xi = (int)(i % d.nx), yi = (int)((i % sxy) / d.nx), zi = (int)(i / sxy);
-        const T qi = helm_point(d, comp, s, p, xi, yi, zi);
-        q[i] = qi;
-        acc[0] += (double)p[i] * (double)qi;
-    }
-    if (grid_sum<1>(acc, sc, cgs + 1)) cgs[4] = cgs[0] / acc[0];  // alpha = n0 / (p.Ap)
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+    T acc = T(0);
+    if (xi < d.nx && yi < d.ny)
+        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
+            const long long i = lin(d, xi, yi, zi);
+            const T qi = helm_point(d, comp, s, p, xi, yi, zi);
+            q[i] = qi;
+            acc += p[i] * qi;
+        }
+    double a[1] = {(double)acc};
+    if (grid_sum<1>(a, sc, cgs + 1)) cgs[4] = cgs[0] / a[0];  // alpha = n0 / (p.Ap)
 }
 
 template <typename T>
@@ -247,13 +262,14 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update(long long N, T* __restr
                                                         const T* __restrict__ p, const T* __restrict__ q,
                                                         RedScratch sc, double* cgs) {
     const T alpha = T(cgs[4]);
-    double acc[1] = {0.0};
+    T part = T(0);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
         x[i] = x[i] + alpha * p[i];
         const T ri = r[i] - q[i] * alpha;
         r[i] = ri;
-        acc[0] += (double)ri * (double)ri;
+        part += ri * ri;
     }
+    double acc[1] = {(double)part};
     if (grid_sum<1>(acc, sc, cgs + 2)) {
         cgs[3] = acc[0] / cgs[0];  // beta = n1 / n0
         cgs[0] = acc[0];
@@ -276,15 +292,17 @@ template <typename TD>
 __global__ void __launch_bounds__(kRedBlock) k_helm_defect(Dims d, int comp, double s, const double* __restrict__ x,
                                                           const double* __restrict__ b, TD* __restrict__ r,
                                                           RedScratch sc, double* out) {
-    const long long N = d.ncell(), sxy = d.sxy();
-    double acc[1] = {0.0};
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
-        const int xi = (int)(i % d.nx), yi = (int)((i % sxy) / d.nx), zi = (int)(i / sxy);
-        const double ri = b[i] - helm_point(d, comp, s, x, xi, yi, zi);
-        r[i] = TD(ri);
-        acc[0] += ri * ri;
-    }
-    grid_sum<1>(acc, sc, out);
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+    TD acc = TD(0);
+    if (xi < d.nx && yi < d.ny)
+        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
+            const long long i = lin(d, xi, yi, zi);
+            const TD ri = TD(b[i] - helm_point(d, comp, s, x, xi, yi, zi));
+            r[i] = ri;
+            acc += ri * ri;
+        }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, out);
 }
 
 // CG started from zero: r = p = b, n0 = b.b
@@ -292,14 +310,15 @@ template <typename T>
 __global__ void __launch_bounds__(kRedBlock) k_cg_init_zero(long long N, const T* __restrict__ b, T* __restrict__ x,
                                                            T* __restrict__ r, T* __restrict__ p, RedScratch sc,
                                                            double* cgs) {
-    double acc[1] = {0.0};
+    T part = T(0);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
         const T bi = b[i];
         x[i] = T(0);
         r[i] = bi;
         p[i] = bi;
-        acc[0] += (double)bi * (double)bi;
+        part += bi * bi;
     }
+    double acc[1] = {(double)part};
     grid_sum<1>(acc, sc, cgs + 0);
 }
 
@@ -314,11 +333,12 @@ __global__ void k_add_correction(long long N, double* __restrict__ x, const TE* 
 // ---------------------------------------------------------------------------
 template <typename T, bool SQ>
 __global__ void __launch_bounds__(kRedBlock) k_sum(long long N, const T* __restrict__ x, RedScratch sc, double* out) {
-    double acc[1] = {0.0};
+    T part = T(0);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
-        const double e = (double)x[i];
-        acc[0] += SQ ? e * e : e;
+        const T e = x[i];
+        part += SQ ? e * e : e;
     }
+    double acc[1] = {(double)part};
     grid_sum<1>(acc, sc, out);
 }
 
@@ -368,8 +388,9 @@ void launch_grad(const Dims& d, T* px, T* py, T* pz, const T* p, cudaStream_t s)
     k_grad<T><<<grid3(d), block3(), 0, s>>>(d, px, py, pz, p);
 }
 template <typename T>
-void launch_grad_sub(const Dims& d, T* u, T* v, T* w, const T* phi, T* wallgrad, cudaStream_t s) {
-    k_grad_sub<T><<<grid3(d), block3(), 0, s>>>(d, u, v, w, phi, wallgrad);
+void launch_grad_sub(const Dims& d, T* u, T* v, T* w, const T* phi, T* wallgrad, cudaStream_t s, float* u32,
+                     float* v32, float* w32) {
+    k_grad_sub<T><<<grid3(d), block3(), 0, s>>>(d, u, v, w, phi, wallgrad, u32, v32, w32);
 }
 void launch_wall_update(const Dims& d, double* walls, const double* wallgrad, cudaStream_t s) {
     k_wall_update<<<ew_blocks((long long)d.nx * d.nz), 256, 0, s>>>(d, walls, wallgrad);
@@ -383,7 +404,7 @@ void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const
 template <typename TD>
 void launch_helm_defect(const Dims& d, int comp, double scale, const double* x, const double* b, TD* r, RedScratch sc,
                         double* out, cudaStream_t s) {
-    k_helm_defect<TD><<<red_blocks(d.ncell()), kRedBlock, 0, s>>>(d, comp, scale, x, b, r, sc, out);
+    k_helm_defect<TD><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, scale, x, b, r, sc, out);
 }
 template <typename T>
 void launch_cg_init_zero(long long n, const T* b, T* x, T* r, T* p, RedScratch sc, double* cgs, cudaStream_t s) {
@@ -400,11 +421,11 @@ void launch_helm_apply(const Dims& d, int comp, double scale, T* y, const T* x, 
 template <typename T>
 void launch_cg_init(const Dims& d, int comp, double scale, const T* x, const T* b, T* r, T* p, RedScratch sc,
                     double* cgs, cudaStream_t s) {
-    k_cg_init<T><<<red_blocks(d.ncell()), kRedBlock, 0, s>>>(d, comp, T(scale), x, b, r, p, sc, cgs);
+    k_cg_init<T><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, T(scale), x, b, r, p, sc, cgs);
 }
 template <typename T>
 void launch_cg_apply(const Dims& d, int comp, double scale, const T* p, T* q, RedScratch sc, double* cgs, cudaStream_t s) {
-    k_cg_apply<T><<<red_blocks(d.ncell()), kRedBlock, 0, s>>>(d, comp, T(scale), p, q, sc, cgs);
+    k_cg_apply<T><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, T(scale), p, q, sc, cgs);
 }
 template <typename T>
 void launch_cg_update(long long n, T* x, T* r, const T* p, const T* q, RedScratch sc, double* cgs, cudaStream_t s) {
@@ -442,7 +463,7 @@ void launch_convert(long long n, TO* out, const TI* in, cudaStream_t s) {
 #define AFMIB_INST(T)                                                                                          \
     template void launch_div<T>(const Dims&, T*, const T*, const T*, const T*, const T*, const T*, cudaStream_t); \
     template void launch_grad<T>(const Dims&, T*, T*, T*, const T*, cudaStream_t);                             \
-    template void launch_grad_sub<T>(const Dims&, T*, T*, T*, const T*, T*, cudaStream_t);                     \
+    template void launch_grad_sub<T>(const Dims&, T*, T*, T*, const T*, T*, cudaStream_t, float*, float*, float*); \
     template void launch_helm_apply<T>(const Dims&, int, double, T*, const T*, cudaStream_t);                  \
     template void launch_cg_init<T>(const Dims&, int, double, const T*, const T*, T*, T*, RedScratch, double*, \
                                     cudaStream_t);                                                             \
@@ -461,6 +482,8 @@ template void launch_advect<double, double>(const Dims&, double*, double*, doubl
                                             const double*, cudaStream_t);
 template void launch_advect<double, float>(const Dims&, float*, float*, float*, const double*, const double*,
                                            const double*, cudaStream_t);
+template void launch_advect<float, float>(const Dims&, float*, float*, float*, const float*, const float*,
+                                          const float*, cudaStream_t);
 template void launch_helm_rhs<double, double>(const Dims&, int, int, double*, const double*, const double*,
                                               const double*, const double*, const double*, double, double, double,
                                               double, cudaStream_t);

@@ -191,11 +191,21 @@ __global__ void k_tile_ranges(const unsigned* __restrict__ keys, int M, int cell
     if (p == M - 1 || keys[p + 1] / (unsigned)cells_per_tile != t) tend[t] = p + 1;
 }
 
-// output tiles whose (TS+4)^3 neighbourhood holds a marker
+// Per tile: slot of each occupied tile (or -1) and the list of output tiles
+// whose (TS+4)^3 neighbourhood holds a marker. Slots are handed out by an
+// atomic counter; a slot only names storage, so its value never reaches a result.
 __global__ void k_active_tiles(int ntx, int nty, int ntz, int channel, const int* __restrict__ tstart,
-                               const int* __restrict__ tend, int* __restrict__ list, int* __restrict__ count) {
+                               const int* __restrict__ tend, int* __restrict__ list, int* __restrict__ count,
+                               int* __restrict__ slot, int* __restrict__ occ, int* __restrict__ occ_count) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntx * nty * ntz) return;
+    if (tend[t] > tstart[t]) {
+        const int sl = atomicAdd(occ_count, 1);
+        slot[t] = sl;
+        occ[sl] = t;
+    } else {
+        slot[t] = -1;
+    }
     const int tx = t % ntx, ty = (t / ntx) % nty, tz = t / (ntx * nty);
     bool any = false;
     for (int dz = -1; dz <= 1 && !any; ++dz)
@@ -211,147 +221,157 @@ __global__ void k_active_tiles(int ntx, int nty, int ntz, int channel, const int
     if (any) list[atomicAdd(count, 1)] = t;
 }
 
+// Cell-start table of every occupied tile: ctab[slot][c] = first sorted
+// position of local cell c (c = TS^3 holds the tile's end), by binary search
+// in the tile's sorted key range.
+template <int TS>
+__global__ void __launch_bounds__(TS * TS * TS) k_cell_table(const unsigned* __restrict__ keys,
+                                                            const int* __restrict__ tstart, const int* __restrict__ tend,
+                                                            const int* __restrict__ occ, const int* __restrict__ occ_count,
+                                                            int* __restrict__ ctab) {
+    constexpr int C = TS * TS * TS;
+    const int nocc = *occ_count;
+    for (int li = blockIdx.x; li < nocc; li += gridDim.x) {
+        const int t = occ[li];
+        const int a = tstart[t], b = tend[t];
+        const unsigned key = (unsigned)t * C + threadIdx.x;
+        int lo = a, hi = b;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (keys[mid] < key) lo = mid + 1; else hi = mid;
+        }
+        int* row = ctab + (size_t)li * (C + 1);
+        row[threadIdx.x] = lo;
+        if (threadIdx.x == 0) row[C] = b;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Gather spreading. One block (TS^3 threads, one face per component each) per
-// active output tile. Candidates: markers of the 27 neighbour tiles whose
-// cell lies in E = tile grown by 2 cells per side, compacted in a fixed order
-// and counting-sorted by E-cell (x fastest) so that every row of cells is one
-// contiguous run. A face at E-local coordinate J along an axis with offset
-// off gathers cells [J-2, J+1] (off 0) or [J-2, J+2] (off 1/2).
+// active output tile. The markers binned in E = the tile grown by two cells
+// per side are staged in shared memory in E-cell order (x fastest): every E
+// row (ey, ez) is cut into at most three tile segments, each a contiguous run
+// of the sorted markers, and one block scan of the segment lengths places the
+// runs. A face at E-local J gathers cells [J-2, J+1] along its own axis and
+// [J-2, J+2] along the other two, i.e. at most 25 contiguous runs, in a fixed
+// order: no float atomics, bitwise repeatable.
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(512) k_spread_gather(Dims d, int TS, int M, const int* __restrict__ perm,
-                                                       MarkerW<T> mw, const T* __restrict__ G,
-                                                       const double* __restrict__ vol, double scale,
-                                                       const int* __restrict__ tstart, const int* __restrict__ tend,
-                                                       const int* __restrict__ list, const int* __restrict__ count,
-                                                       int cap, T* __restrict__ fu, T* __restrict__ fv,
-                                                       T* __restrict__ fw, int* __restrict__ flag) {
+template <typename T, int TS>
+__global__ void __launch_bounds__(TS * TS * TS) k_spread_gather(Dims d, int M, const int* __restrict__ perm,
+                                                                MarkerW<T> mw, const T* __restrict__ G,
+                                                                const double* __restrict__ vol, double scale,
+                                                                const int* __restrict__ slot, const int* __restrict__ ctab,
+                                                                const int* __restrict__ list, const int* __restrict__ count,
+                                                                int cap, T* __restrict__ fu, T* __restrict__ fv,
+                                                                T* __restrict__ fw, int* __restrict__ flag) {
+    constexpr int NT = TS * TS * TS, E = TS + 4, E2 = E * E, E3 = E2 * E, C = TS * TS * TS;
+    constexpr int NSEG = E2 * 3;  // (row, tile segment) pairs
     extern __shared__ __align__(16) unsigned char smem[];
-    const int E = TS + 4, E3 = E * E * E;
-    const int ntx = d.nx / TS, nty = d.ny / TS, ntz = d.nz / TS;
-    // carve shared memory
-    int* s_start = (int*)smem;                 // E3 + 1
-    int* s_first = s_start + (E3 + 1);         // E3
-    int* s_pos = s_first + E3;                 // cap: sorted position p of each compacted candidate
-    int* s_ecell = s_pos + cap;                // cap
-    int* s_order = s_ecell + cap;              // cap: slot -> compacted index
-    int* s_base = s_order + cap;               // cap: packed E-local bases (3 x 8 bit, biased by 8)
-    int* s_scan = s_base + cap;                // blockDim.x scan workspace + 2
-    T* s_w = (T*)(((uintptr_t)(s_scan + blockDim.x + 2) + 15) & ~(uintptr_t)15);  // cap * 12
-    T* s_g = s_w + (size_t)cap * 12;           // cap
-    __shared__ int s_nc;
+    int* s_estart = (int*)smem;          // E3 + 1: first staged slot of each E cell
+    int* s_seg = s_estart + (E3 + 1);    // NSEG: staged offset of each segment
+    int* s_scan = s_seg + NSEG;          // NT
+    int* s_k = s_scan + NT;              // cap: marker index of each staged slot
+    int* s_base = s_k + cap;             // cap: packed E-local first faces
+    T* s_w = (T*)(((uintptr_t)(s_base + cap) + 15) & ~(uintptr_t)15);  // cap * 12
+    T* s_g = s_w + (size_t)cap * 12;     // cap
 
+    const int ntx = d.nx / TS, nty = d.ny / TS, ntz = d.nz / TS;
     const int ncount = *count;
     const int tid = threadIdx.x;
     const int lx = tid % TS, ly = (tid / TS) % TS, lz = tid / (TS * TS);
     for (int li = blockIdx.x; li < ncount; li += gridDim.x) {
         const int t = list[li];
         const int tx = t % ntx, ty = (t / ntx) % nty, tz = t / (ntx * nty);
-        const int ox = tx * TS - 2, oy = ty * TS - 2, oz = tz * TS - 2;  // E origin (unwrapped)
-        for (int e = tid; e < E3; e += blockDim.x) { s_start[e] = 0; s_first[e] = 0x7fffffff; }
-        if (tid == 0) s_nc = 0;
-        __syncthreads();
-        // ---- ordered compaction of the candidates over the 27 neighbour tiles
-        for (int nb = 0; nb < 27; ++nb) {
-            const int dx = nb % 3 - 1, dy = (nb / 3) % 3 - 1, dz = nb / 9 - 1;
-            int yy = ty + dy;
-            if (d.channel && (yy < 0 || yy >= nty)) continue;
-            yy = wrapi(yy, nty);
-            const int n = wrapi(tx + dx, ntx) + ntx * (yy + nty * wrapi(tz + dz, ntz));
-            // with fewer than three tiles along an axis the -1 and +1
-            // neighbours coincide: visit every tile once
-            bool seen = false;
-            for (int pb = 0; pb < nb && !seen; ++pb) {
-                const int px = pb % 3 - 1, py = (pb / 3) % 3 - 1, pz = pb / 9 - 1;
-                int qy = ty + py;
-                if (d.channel && (qy < 0 || qy >= nty)) continue;
-                qy = wrapi(qy, nty);
-                seen = (wrapi(tx + px, ntx) + ntx * (qy + nty * wrapi(tz + pz, ntz))) == n;
+        const int ox = tx * TS - 2, oy = ty * TS - 2, oz = tz * TS - 2;  // E origin (unwrapped cells)
+        // ---- segment ranges: segment q = (row r, part j): cells ex in
+        //      [0, 2), [2, TS+2), [TS+2, E) of row r, i.e. tiles tx-1, tx, tx+1
+        int my_len[(NSEG + NT - 1) / NT], my_p0[(NSEG + NT - 1) / NT];
+        int tot = 0;
+#pragma unroll
+        for (int k = 0; k < (NSEG + NT - 1) / NT; ++k) {
+            const int q = tid * ((NSEG + NT - 1) / NT) + k;
+            my_len[k] = 0;
+            my_p0[k] = 0;
+            if (q < NSEG) {
+                const int r = q / 3, j = q % 3;
+                const int ey = r % E, ez = r / E;
+                int gy = oy + ey;
+                const bool ok = !(d.channel && (gy < 0 || gy >= d.ny));
+                if (ok) {
+                    gy = wrapi(gy, d.ny);
+                    const int gz = wrapi(oz + ez, d.nz);
+                    const int ex0 = j == 0 ? 0 : (j == 1 ? 2 : TS + 2);
+                    const int ex1 = j == 0 ? 2 : (j == 1 ? TS + 2 : E);  // exclusive
+                    const int gx0 = wrapi(ox + ex0, d.nx);
+                    const int tt = gx0 / TS + ntx * (gy / TS + nty * (gz / TS));
+                    const int sl = slot[tt];
+                    if (sl >= 0) {
+                        const int lc0 = (gx0 % TS) + TS * ((gy % TS) + TS * (gz % TS));
+                        const int* row = ctab + (size_t)sl * (C + 1);
+                        my_p0[k] = row[lc0];
+                        my_len[k] = row[lc0 + (ex1 - ex0)] - my_p0[k];
+                    }
+                }
             }
-            if (seen) continue;
-            const int a = tstart[n], b = tend[n];
-            for (int r0 = a; r0 < b; r0 += blockDim.x) {
-                const int p = r0 + tid;
-                int ecell = -1;
-                if (p < b) {
-                    const int k = perm[p];
-                    const int ex = wrapi(mw.cell[3 * k] - ox, d.nx), ez = wrapi(mw.cell[3 * k + 2] - oz, d.nz);
-                    const int ey = d.channel ? mw.cell[3 * k + 1] - oy : wrapi(mw.cell[3 * k + 1] - oy, d.ny);
-                    if (ex < E && ey >= 0 && ey < E && ez < E) ecell = ex + E * (ey + E * ez);
-                }
-                // block-wide exclusive scan of the flags (fixed order)
-                const int f = ecell >= 0;
-                s_scan[tid] = f;
-                __syncthreads();
-                for (int o = 1; o < (int)blockDim.x; o <<= 1) {
-                    const int v = tid >= o ? s_scan[tid - o] : 0;
-                    __syncthreads();
-                    s_scan[tid] += v;
-                    __syncthreads();
-                }
-                const int slot = s_nc + s_scan[tid] - f;
-                if (f && slot < cap) {
-                    s_pos[slot] = p;
-                    s_ecell[slot] = ecell;
-                }
-                __syncthreads();
-                if (tid == blockDim.x - 1) s_nc += s_scan[tid];
-                __syncthreads();
-            }
+            tot += my_len[k];
         }
-        int nc = s_nc;
-        if (nc > cap) {
-            if (tid == 0) atomicExch(flag, 3);
-            nc = cap;
-        }
-        // ---- counting sort by E-cell; within a cell, sorted position order
-        for (int c = tid; c < nc; c += blockDim.x) {
-            atomicAdd(&s_start[s_ecell[c]], 1);
-            atomicMin(&s_first[s_ecell[c]], s_pos[c]);
-        }
+        // block exclusive scan of the per-thread totals (fixed order)
+        s_scan[tid] = tot;
         __syncthreads();
-        {
-            // parallel exclusive scan of the E3 counts: each thread owns a
-            // contiguous run, then a block scan of the run totals
-            const int per = (E3 + blockDim.x - 1) / blockDim.x;
-            const int e0 = tid * per, e1 = min(e0 + per, E3);
-            int tot = 0;
-            for (int e = e0; e < e1; ++e) tot += s_start[e];
-            s_scan[tid] = tot;
+        for (int o = 1; o < NT; o <<= 1) {
+            const int v = tid >= o ? s_scan[tid - o] : 0;
             __syncthreads();
-            for (int o = 1; o < (int)blockDim.x; o <<= 1) {
-                const int v = tid >= o ? s_scan[tid - o] : 0;
-                __syncthreads();
-                s_scan[tid] += v;
-                __syncthreads();
-            }
-            int run = s_scan[tid] - tot;
-            for (int e = e0; e < e1; ++e) {
-                const int c = s_start[e];
-                s_start[e] = run;
-                run += c;
-            }
-            if (tid == blockDim.x - 1) s_start[E3] = s_scan[tid];
+            s_scan[tid] += v;
+            __syncthreads();
         }
-        __syncthreads();
-        for (int c = tid; c < nc; c += blockDim.x) {
-            const int e = s_ecell[c];
-            s_order[s_start[e] + (s_pos[c] - s_first[e])] = c;
+        const int nc_all = s_scan[NT - 1];
+        int off = s_scan[tid] - tot;
+#pragma unroll
+        for (int k = 0; k < (NSEG + NT - 1) / NT; ++k) {
+            const int q = tid * ((NSEG + NT - 1) / NT) + k;
+            if (q < NSEG) {
+                s_seg[q] = off;
+                for (int m = 0; m < my_len[k]; ++m)
+                    if (off + m < cap) s_k[off + m] = perm[my_p0[k] + m];
+                // E-cell starts of this segment's cells
+                const int r = q / 3, j = q % 3;
+                const int ex0 = j == 0 ? 0 : (j == 1 ? 2 : TS + 2);
+                const int ex1 = j == 0 ? 2 : (j == 1 ? TS + 2 : E);
+                int gy = oy + r % E;
+                const bool ok = !(d.channel && (gy < 0 || gy >= d.ny));
+                for (int ex = ex0; ex < ex1; ++ex) {
+                    int st = off;
+                    if (ok && my_len[k] > 0) {
+                        gy = wrapi(gy, d.ny);
+                        const int gz = wrapi(oz + r / E, d.nz);
+                        const int gx = wrapi(ox + ex, d.nx);
+                        const int tt = gx / TS + ntx * (gy / TS + nty * (gz / TS));
+                        const int lc = (gx % TS) + TS * ((gy % TS) + TS * (gz % TS));
+                        st = off + (ctab[(size_t)slot[tt] * (C + 1) + lc] - my_p0[k]);
+                    }
+                    s_estart[ex + E * r] = st;
+                }
+                off += my_len[k];
+            }
         }
+        if (tid == NT - 1) s_estart[E3] = nc_all;
+        if (nc_all > cap && tid == 0) atomicExch(flag, 3);
         __syncthreads();
+        const int nc = nc_all < cap ? nc_all : cap;
         // ---- one component at a time
         for (int comp = 0; comp < 3; ++comp) {
-            for (int sl = tid; sl < nc; sl += blockDim.x) {
-                const int c = s_order[sl];
-                const int k = perm[s_pos[c]];
-                const int e = s_ecell[c];
-                const int ec[3] = {e % E, (e / E) % E, e / (E * E)};
+            for (int sl = tid; sl < nc; sl += NT) {
+                const int k = s_k[sl];
                 int packed = 0;
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
                     const int v = (a == comp) ? 0 : 1;
-                    const int b = ec[a] + mw.dbase[(k * 3 + a) * 2 + v];  // E-local first face
+                    const int o = a == 0 ? ox : (a == 1 ? oy : oz);
+                    const int n_a = a == 0 ? d.nx : (a == 1 ? d.ny : d.nz);
+                    // E-local first face: cell relative to the E origin + offset
+                    int ec = mw.cell[3 * k + a] - o;
+                    if (!(a == 1 && d.channel)) ec = wrapi(ec, n_a);
+                    const int b = ec + mw.dbase[(k * 3 + a) * 2 + v];
                     packed |= (b + 8) << (8 * a);
                     const T* w = mw.w + (((size_t)k * 3 + a) * 2 + v) * 4;
 #pragma unroll
@@ -363,18 +383,15 @@ __global__ void __launch_bounds__(512) k_spread_gather(Dims d, int TS, int M, co
             __syncthreads();
             T* f = comp == 0 ? fu : (comp == 1 ? fv : fw);
             const int J[3] = {lx + 2, ly + 2, lz + 2};
-            int lo[3], hi[3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                lo[a] = J[a] - 2;
-                hi[a] = (a == comp) ? J[a] + 1 : J[a] + 2;
-            }
+            const int hx = (comp == 0) ? J[0] + 1 : J[0] + 2;
+            const int hy = (comp == 1) ? J[1] + 1 : J[1] + 2;
+            const int hz = (comp == 2) ? J[2] + 1 : J[2] + 2;
             T acc = T(0);
-            for (int ez = lo[2]; ez <= hi[2]; ++ez)
-                for (int ey = lo[1]; ey <= hi[1]; ++ey) {
+            for (int ez = J[2] - 2; ez <= hz; ++ez)
+                for (int ey = J[1] - 2; ey <= hy; ++ey) {
                     const int row = E * (ey + E * ez);
-                    const int s0 = s_start[row + lo[0]], s1 = s_start[row + hi[0] + 1];
-                    for (int sl = s0; sl < s1; ++sl) {
+                    const int s0 = s_estart[row + J[0] - 2], s1 = s_estart[row + hx + 1];
+                    for (int sl = s0; sl < s1 && sl < nc; ++sl) {
                         const int pk = s_base[sl];
                         const int mx = J[0] - ((pk & 255) - 8);
                         const int my = J[1] - (((pk >> 8) & 255) - 8);
@@ -480,39 +497,58 @@ void launch_tile_ranges(const unsigned* keys, int M, int cells_per_tile, int* ts
 }
 
 void launch_active_tiles(int ntx, int nty, int ntz, int channel, const int* tstart, const int* tend, int* list,
-                         int* count, cudaStream_t s) {
+                         int* count, int* slot, int* occ, int* occ_count, cudaStream_t s) {
     const int nt = ntx * nty * ntz;
-    k_active_tiles<<<(nt + 255) / 256, 256, 0, s>>>(ntx, nty, ntz, channel, tstart, tend, list, count);
+    k_active_tiles<<<(nt + 255) / 256, 256, 0, s>>>(ntx, nty, ntz, channel, tstart, tend, list, count, slot, occ,
+                                                    occ_count);
+}
+
+void launch_cell_table(int TS, const unsigned* keys, const int* tstart, const int* tend, const int* occ,
+                       const int* occ_count, int max_occ, int* ctab, cudaStream_t s) {
+    int blocks = max_occ < 152 * 8 ? max_occ : 152 * 8;
+    if (blocks < 1) blocks = 1;
+    if (TS == 8) k_cell_table<8><<<blocks, 512, 0, s>>>(keys, tstart, tend, occ, occ_count, ctab);
+    else k_cell_table<4><<<blocks, 64, 0, s>>>(keys, tstart, tend, occ, occ_count, ctab);
 }
 
 template <typename T>
 size_t spread_smem_bytes(int TS, int cap) {
-    const int E = TS + 4, E3 = E * E * E;
-    size_t ints = (size_t)(E3 + 1) + E3 + 5 * (size_t)cap + TS * TS * TS + 2;
+    const int E = TS + 4, E3 = E * E * E, NT = TS * TS * TS;
+    size_t ints = (size_t)(E3 + 1) + 3 * E * E + NT + 2 * (size_t)cap;
     size_t bytes = ints * sizeof(int);
     bytes = (bytes + 15) & ~(size_t)15;
     bytes += (size_t)cap * 13 * sizeof(T);
     return bytes;
 }
 
-template <typename T>
-void launch_spread_gather(const Dims& d, int TS, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
-                          double scale, const int* tstart, const int* tend, const int* list, const int* count,
+template <typename T, int TS>
+static void spread_launch(const Dims& d, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
+                          double scale, const int* slot, const int* ctab, const int* list, const int* count,
                           int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, cudaStream_t s) {
     const size_t smem = spread_smem_bytes<T>(TS, cap);
     // opt in to exactly the dynamic shared memory this launch uses (the
     // kernel's static shared memory counts against the same 227 KB)
-    static size_t configured[2] = {0, 0};
-    const int slot = sizeof(T) == 8 ? 0 : 1;
-    if (configured[slot] < smem) {
-        if (cudaFuncSetAttribute(k_spread_gather<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    static size_t configured = 0;
+    if (configured < smem) {
+        if (cudaFuncSetAttribute(k_spread_gather<T, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
             return;  // the launch error is reported by the caller's cudaGetLastError
-        configured[slot] = smem;
+        configured = smem;
     }
-    int blocks = max_tiles < 152 * 2 ? max_tiles : 152 * 2;
+    int blocks = max_tiles < 152 * 4 ? max_tiles : 152 * 4;
     if (blocks < 1) blocks = 1;
-    k_spread_gather<T><<<blocks, TS * TS * TS, smem, s>>>(d, TS, M, perm, mw, G, vol, scale, tstart, tend, list,
-                                                          count, cap, fu, fv, fw, flag);
+    k_spread_gather<T, TS><<<blocks, TS * TS * TS, smem, s>>>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count,
+                                                              cap, fu, fv, fw, flag);
+}
+
+template <typename T>
+void launch_spread_gather(const Dims& d, int TS, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
+                          double scale, const int* slot, const int* ctab, const int* list, const int* count,
+                          int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, cudaStream_t s) {
+    if (TS == 8)
+        spread_launch<T, 8>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, flag, s);
+    else
+        spread_launch<T, 4>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, flag, s);
 }
 
 template <typename T, typename TF>
@@ -534,7 +570,9 @@ void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, do
                                           double, const int*, const int*, const int*, const int*, int, int, T*,  \
                                           T*, T*, int*, cudaStream_t);                                          \
     template void launch_interp<T, double>(const Dims&, int, const int*, MarkerW<T>, const double*, const double*, \
-                                           const double*, double*, cudaStream_t);
+                                           const double*, double*, cudaStream_t);                               \
+    template void launch_interp<T, float>(const Dims&, int, const int*, MarkerW<T>, const float*, const float*,  \
+                                          const float*, double*, cudaStream_t);
 
 AFMIB_IB_INST(double)
 AFMIB_IB_INST(float)

@@ -31,8 +31,13 @@ void radix_sort_pairs(unsigned* keys, int* vals, unsigned* keys_alt, int* vals_a
                       unsigned** keys_out, int** vals_out, cudaStream_t s);
 
 void launch_tile_ranges(const unsigned* keys, int M, int cells_per_tile, int* tstart, int* tend, cudaStream_t s);
+// slot[t] = storage slot of occupied tile t (or -1), occ[slot] = t; list of
+// output tiles with a marker in their 3^3-tile neighbourhood.
 void launch_active_tiles(int ntx, int nty, int ntz, int channel, const int* tstart, const int* tend, int* list,
-                         int* count, cudaStream_t s);
+                         int* count, int* slot, int* occ, int* occ_count, cudaStream_t s);
+// ctab[slot][c]: first sorted position of local cell c of each occupied tile
+void launch_cell_table(int TS, const unsigned* keys, const int* tstart, const int* tend, const int* occ,
+                       const int* occ_count, int max_occ, int* ctab, cudaStream_t s);
 
 template <typename T>
 size_t spread_smem_bytes(int TS, int cap);
@@ -41,7 +46,7 @@ size_t spread_smem_bytes(int TS, int cap);
 // more than `cap` candidates.
 template <typename T>
 void launch_spread_gather(const Dims& d, int TS, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
-                          double scale, const int* tstart, const int* tend, const int* list, const int* count,
+                          double scale, const int* slot, const int* ctab, const int* list, const int* count,
                           int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, cudaStream_t s);
 
 // U[c*M + k] = sum (phi/n)^3 u_c(face); perm (may be null) orders the threads.

@@ -51,18 +51,20 @@ __global__ void k_residual(Dims d, T* __restrict__ r, const T* __restrict__ xv, 
 template <typename T>
 __global__ void __launch_bounds__(kRedBlock) k_residual_norm(Dims d, T* __restrict__ r, const T* __restrict__ xv,
                                                             const T* __restrict__ b, RedScratch sc, double* out) {
-    const long long N = d.ncell(), sxy = d.sxy();
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
     const T off = T(d.n) * T(d.n);
-    double acc[1] = {0.0};
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
-        const int xi = (int)(i % d.nx), yi = (int)((i % sxy) / d.nx), zi = (int)(i / sxy);
-        T S, c;
-        lap_row(d, xv, xi, yi, zi, S, c);
-        const T ri = b[i] - off * (S - c * xv[i]);
-        r[i] = ri;
-        acc[0] += (double)ri * (double)ri;
-    }
-    grid_sum<1>(acc, sc, out);
+    T acc = T(0);
+    if (xi < d.nx && yi < d.ny)
+        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
+            T S, c;
+            lap_row(d, xv, xi, yi, zi, S, c);
+            const long long i = lin(d, xi, yi, zi);
+            const T ri = b[i] - off * (S - c * xv[i]);
+            r[i] = ri;
+            acc += ri * ri;
+        }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, out);
 }
 
 // Mixed form: defect of the FP64 potential, r = b - L x evaluated in FP64 and
@@ -70,18 +72,20 @@ __global__ void __launch_bounds__(kRedBlock) k_residual_norm(Dims d, T* __restri
 template <typename TD>
 __global__ void __launch_bounds__(kRedBlock) k_lap_defect(Dims d, TD* __restrict__ r, const double* __restrict__ xv,
                                                          const double* __restrict__ b, RedScratch sc, double* out) {
-    const long long N = d.ncell(), sxy = d.sxy();
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
     const double off = double(d.n) * double(d.n);
-    double acc[1] = {0.0};
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
-        const int xi = (int)(i % d.nx), yi = (int)((i % sxy) / d.nx), zi = (int)(i / sxy);
-        double S, c;
-        lap_row(d, xv, xi, yi, zi, S, c);
-        const double ri = b[i] - off * (S - c * xv[i]);
-        r[i] = TD(ri);
-        acc[0] += ri * ri;
-    }
-    grid_sum<1>(acc, sc, out);
+    TD acc = TD(0);
+    if (xi < d.nx && yi < d.ny)
+        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
+            double S, c;
+            lap_row(d, xv, xi, yi, zi, S, c);
+            const long long i = lin(d, xi, yi, zi);
+            const TD ri = TD(b[i] - off * (S - c * xv[i]));
+            r[i] = ri;
+            acc += ri * ri;
+        }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, out);
 }
 
 // One colour of red-black Gauss–Seidel: x_i = (b_i - n^2 S) / (-c n^2).
@@ -255,7 +259,7 @@ void launch_lap_apply(const Dims& d, T* y, const T* x, cudaStream_t s) {
 template <typename T>
 void launch_residual(const Dims& d, T* r, const T* x, const T* b, RedScratch* sc, double* out, cudaStream_t s) {
     if (sc && out)
-        k_residual_norm<T><<<red_blocks(d.ncell()), kRedBlock, 0, s>>>(d, r, x, b, *sc, out);
+        k_residual_norm<T><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, r, x, b, *sc, out);
     else
         k_residual<T><<<grid3(d), dim3(BX, BY), 0, s>>>(d, r, x, b);
 }
@@ -281,7 +285,7 @@ void launch_prolong_assign(const Dims& d, T* fine, const T* coarse, cudaStream_t
 }
 template <typename TD>
 void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, RedScratch sc, double* out, cudaStream_t s) {
-    k_lap_defect<TD><<<red_blocks(d.ncell()), kRedBlock, 0, s>>>(d, r, x, b, sc, out);
+    k_lap_defect<TD><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, r, x, b, sc, out);
 }
 template void launch_lap_defect<float>(const Dims&, float*, const double*, const double*, RedScratch, double*,
                                        cudaStream_t);

@@ -6,6 +6,7 @@
 // enqueues every kernel on one CUDA stream. Iterative loops keep their
 // scalars on the device; the host reads one convergence scalar per
 // iteration, exactly where the reference tests its stopping criterion.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -48,6 +49,7 @@ struct afmib_solver {
     // the coarsest level, which is solved in FP64
     bool mixed = false;
     float *adv32[3] = {}, *f32[3] = {}, *d32 = nullptr, *e32 = nullptr;
+    float *u32 = nullptr, *v32 = nullptr, *w32 = nullptr;  // FP32 shadow of the velocity
     float *cg32_r = nullptr, *cg32_p = nullptr, *cg32_q = nullptr;
     std::vector<MGLevelT<float>> lv32;
     double *cx64 = nullptr, *cb64 = nullptr, *cr64 = nullptr;
@@ -68,6 +70,8 @@ struct afmib_solver {
     int *vals = nullptr, *vals2 = nullptr, *perm = nullptr;
     int TS = 0, ntx = 0, nty = 0, ntz = 0, ntiles = 0;
     int *tstart = nullptr, *tend = nullptr, *tlist = nullptr, *tcount = nullptr;
+    int *tslot = nullptr, *tocc = nullptr, *ctab = nullptr;
+    int ctab_cap = 0;  // occupied tiles the cell table can hold
     MarkerW<double> mw{};
     MarkerW<float> mw32{};
     float* G32 = nullptr;
@@ -529,7 +533,8 @@ int project(afmib_solver* s) {
     else TRY(mg_solve(s, nullptr));
     {
         ProfScope ps(s, P_GRAD_SUB, 7 * Ns);
-        launch_grad_sub<double>(s->d, s->u, s->v, s->w, s->lv[0].x, s->d.channel ? s->wallgrad : nullptr, s->st);
+        launch_grad_sub<double>(s->d, s->u, s->v, s->w, s->lv[0].x, s->d.channel ? s->wallgrad : nullptr, s->st,
+                                s->u32, s->v32, s->w32);
     }
     CKL();
     return AFMIB_OK;
@@ -542,8 +547,8 @@ int substep(afmib_solver* s) {
     const long long N = s->N();
     const double Ns = (double)N * sizeof(double);
     if (s->mixed) {
-        ProfScope ps(s, P_ADVECT, (double)N * (3 * 8 + 3 * 4));
-        launch_advect<double, float>(d, s->adv32[0], s->adv32[1], s->adv32[2], s->u, s->v, s->w, s->st);
+        ProfScope ps(s, P_ADVECT, (double)N * (3 * 4 + 3 * 4));
+        launch_advect<float, float>(d, s->adv32[0], s->adv32[1], s->adv32[2], s->u32, s->v32, s->w32, s->st);
     } else {
         ProfScope ps(s, P_ADVECT, 6 * Ns);
         launch_advect<double, double>(d, s->adv[0], s->adv[1], s->adv[2], s->u, s->v, s->w, s->st);
@@ -636,6 +641,13 @@ int marker_alloc(afmib_solver* s, int M, int nnz) {
         TRY(regrow(s, &s->G32, 3 * (size_t)M, 0));
         s->Mcap = M;
     }
+    {
+        const int need = std::min(s->ntiles, std::max(M, 1));
+        if (need > s->ctab_cap) {
+            TRY(regrow(s, &s->ctab, (size_t)need * (s->TS * s->TS * s->TS + 1), 0));
+            s->ctab_cap = need;
+        }
+    }
     if (nnz > s->nnz_cap) {
         TRY(regrow(s, &s->nidx, (size_t)nnz, 0));
         s->nnz_cap = nnz;
@@ -670,11 +682,14 @@ int bin_markers(afmib_solver* s, const double* P, bool fp32 = false) {
     s->perm = vo;
     CK(cudaMemsetAsync(s->tstart, 0, s->ntiles * sizeof(int), s->st));
     CK(cudaMemsetAsync(s->tend, 0, s->ntiles * sizeof(int), s->st));
-    CK(cudaMemsetAsync(s->tcount, 0, sizeof(int), s->st));
+    CK(cudaMemsetAsync(s->tcount, 0, 2 * sizeof(int), s->st));
     {
-        ProfScope ps(s, P_TILES, (double)M * 4 + 3.0 * s->ntiles * 4, 2);
-        launch_tile_ranges(ko, M, s->TS * s->TS * s->TS, s->tstart, s->tend, s->st);
-        launch_active_tiles(s->ntx, s->nty, s->ntz, s->d.channel, s->tstart, s->tend, s->tlist, s->tcount, s->st);
+        const int C = s->TS * s->TS * s->TS;
+        ProfScope ps(s, P_TILES, (double)M * 4 + 5.0 * s->ntiles * 4 + (double)std::min(M, s->ntiles) * (C + 1) * 4, 3);
+        launch_tile_ranges(ko, M, C, s->tstart, s->tend, s->st);
+        launch_active_tiles(s->ntx, s->nty, s->ntz, s->d.channel, s->tstart, s->tend, s->tlist, s->tcount, s->tslot,
+                            s->tocc, s->tcount + 1, s->st);
+        launch_cell_table(s->TS, ko, s->tstart, s->tend, s->tocc, s->tcount + 1, s->ctab_cap, s->ctab, s->st);
     }
     CKL();
     return AFMIB_OK;
@@ -693,7 +708,7 @@ int spread_forces(afmib_solver* s, const double* vol, double* fu, double* fv, do
     const double touched = (double)s->stats.spread_tiles * s->TS * s->TS * s->TS;
     {
         ProfScope ps(s, P_SPREAD, (double)s->M * (24 + 3 * 8 + 8 + 8) + 3 * touched * 8);
-        launch_spread_gather<double>(s->d, s->TS, s->M, s->perm, s->mw, s->G, vol, n3, s->tstart, s->tend, s->tlist,
+        launch_spread_gather<double>(s->d, s->TS, s->M, s->perm, s->mw, s->G, vol, n3, s->tslot, s->ctab, s->tlist,
                                      s->tcount, s->ntiles, cap, fu, fv, fw, s->dflag, s->st);
     }
     CKL();
@@ -704,11 +719,11 @@ int spread_forces32(afmib_solver* s, const double* vol) {
     const long long N = s->N();
     for (int c = 0; c < 3; ++c) CK(cudaMemsetAsync(s->f32[c], 0, N * sizeof(float), s->st));
     const double n3 = (double)s->d.n * s->d.n * s->d.n;
-    const int cap = 2560;
+    const int cap = 3072;
     const double touched = (double)s->stats.spread_tiles * s->TS * s->TS * s->TS;
     {
         ProfScope ps(s, P_SPREAD, (double)s->M * (24 + 3 * 4 + 8 + 8) + 3 * touched * 4);
-        launch_spread_gather<float>(s->d, s->TS, s->M, s->perm, s->mw32, s->G32, vol, n3, s->tstart, s->tend,
+        launch_spread_gather<float>(s->d, s->TS, s->M, s->perm, s->mw32, s->G32, vol, n3, s->tslot, s->ctab,
                                     s->tlist, s->tcount, s->ntiles, cap, s->f32[0], s->f32[1], s->f32[2], s->dflag,
                                     s->st);
     }
@@ -731,7 +746,7 @@ int check_marker_flag(afmib_solver* s) {
 int interp_markers(afmib_solver* s, const double* u, const double* v, const double* w, double* U, bool fp32 = false) {
     const double touched = (double)s->stats.spread_tiles * s->TS * s->TS * s->TS;
     ProfScope ps(s, P_INTERP, 3 * touched * 8 + (double)s->M * (24 + 3 * 8 + 8));
-    if (fp32) launch_interp<float, double>(s->d, s->M, s->perm, s->mw32, u, v, w, U, s->st);
+    if (fp32) launch_interp<float, float>(s->d, s->M, s->perm, s->mw32, s->u32, s->v32, s->w32, U, s->st);
     else launch_interp<double, double>(s->d, s->M, s->perm, s->mw, u, v, w, U, s->st);
     return AFMIB_OK;
 }
@@ -792,7 +807,9 @@ int setup_tiles(afmib_solver* s) {
     TRY(dalloc(s, &s->tstart, s->ntiles));
     TRY(dalloc(s, &s->tend, s->ntiles));
     TRY(dalloc(s, &s->tlist, s->ntiles));
-    TRY(dalloc(s, &s->tcount, 1));
+    TRY(dalloc(s, &s->tcount, 2));
+    TRY(dalloc(s, &s->tslot, s->ntiles));
+    TRY(dalloc(s, &s->tocc, s->ntiles));
     return AFMIB_OK;
 }
 
@@ -890,6 +907,12 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
         }
         TRY(dalloc(s, &s->d32, N));
         TRY(dalloc(s, &s->e32, N));
+        TRY(dalloc(s, &s->u32, N));
+        TRY(dalloc(s, &s->v32, N));
+        TRY(dalloc(s, &s->w32, N));
+        CK(cudaMemsetAsync(s->u32, 0, N * sizeof(float), s->st));
+        CK(cudaMemsetAsync(s->v32, 0, N * sizeof(float), s->st));
+        CK(cudaMemsetAsync(s->w32, 0, N * sizeof(float), s->st));
         TRY(dalloc(s, &s->cg32_r, N));
         TRY(dalloc(s, &s->cg32_p, N));
         TRY(dalloc(s, &s->cg32_q, N));
@@ -905,6 +928,16 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
         TRY(dalloc(s, &s->cr64, nc));
     }
     CK(cudaStreamSynchronize(s->st));
+    return AFMIB_OK;
+}
+
+// FP32 copy of the velocity for the mixed form's FP32 stencils
+int refresh_shadow(afmib_solver* s) {
+    if (!s->mixed) return AFMIB_OK;
+    launch_convert<float, double>(s->N(), s->u32, s->u, s->st);
+    launch_convert<float, double>(s->N(), s->v32, s->v, s->st);
+    launch_convert<float, double>(s->N(), s->w32, s->w, s->st);
+    CKL();
     return AFMIB_OK;
 }
 
@@ -970,6 +1003,7 @@ int afmib_set_velocity(afmib_solver* s, const double* u, const double* v, const 
     if (v) TRY(v_in(s, s->v, v));
     else CK(cudaMemsetAsync(s->v, 0, s->N() * sizeof(double), s->st));
     TRY(copy_in(s, s->w, w, s->N()));
+    TRY(refresh_shadow(s));
     return sync(s);
 }
 
