@@ -83,6 +83,10 @@ _SIGS = {
     "afmib_prolong": ([_vp, _vp, _vp], ctypes.c_int),
     "afmib_spread": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "afmib_interp": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "afmib_set_spring": ([_vp, ctypes.c_double], ctypes.c_int),
+    "afmib_trajectory_forward": ([_vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "afmib_trajectory_adjoint": ([_vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_double), _vp, _vp, _vp],
+                                 ctypes.c_int),
     "afmib_profile_enable": ([_vp, ctypes.c_int], ctypes.c_int),
     "afmib_profile_reset": ([_vp], ctypes.c_int),
     "afmib_profile_count": ([_vp], ctypes.c_int),
@@ -261,6 +265,23 @@ class Solver:
 
     def ib_step(self, nsteps=1):
         self._ck(self.lib.afmib_ib_step(self.h, nsteps))
+
+    # adjoint
+    def set_spring(self, k):
+        self._ck(self.lib.afmib_set_spring(self.h, float(k)))
+
+    def trajectory_forward(self, nsteps, ckpt_every):
+        self._ck(self.lib.afmib_trajectory_forward(self.h, nsteps, ckpt_every))
+
+    def trajectory_adjoint(self, lam_u=None, lam_v=None, lam_w=None, lam_X=None, want_u0=False, out_X=None):
+        """Gradients (dX0 [M,3], dk, (du0, dv0, dw0) or None) of a loss with the given final-state adjoints."""
+        gX = np.zeros((self.M, 3)) if out_X is None else out_X
+        gk = ctypes.c_double(0.0)
+        gu = [np.zeros(self.ncell) for _ in range(3)] if want_u0 else [None] * 3
+        self._ck(self.lib.afmib_trajectory_adjoint(self.h, ptr(_f64(lam_u)), ptr(_f64(lam_v)), ptr(_f64(lam_w)),
+                                                   ptr(_f64(lam_X)), ptr(gX), ctypes.byref(gk),
+                                                   *(ptr(a) for a in gu)))
+        return gX, gk.value, (gu if want_u0 else None)
 
     # per-kernel timing
     def profile(self, on=True):

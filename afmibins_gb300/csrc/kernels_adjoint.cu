@@ -180,3 +180,27 @@ void launch_springs_adjoint(int M, const double* X, const int* ns, const int* ni
 }
 
 }  // namespace afmib
+
+namespace afmib {
+namespace {
+// soa[c*M + k] = c0 * aos[3k + c]
+__global__ void k_aos_to_soa(int M, const double* __restrict__ aos, double* __restrict__ soa, double c0) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= M) return;
+    for (int c = 0; c < 3; ++c) soa[(size_t)c * M + k] = c0 * aos[3 * k + c];
+}
+// aos[3k + c] += c0 * soa[c*M + k]
+__global__ void k_soa_add_aos(int M, const double* __restrict__ soa, double* __restrict__ aos, double c0) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= M) return;
+    for (int c = 0; c < 3; ++c) aos[3 * k + c] += c0 * soa[(size_t)c * M + k];
+}
+}  // namespace
+
+void launch_aos_to_soa(int M, const double* aos, double* soa, double c0, cudaStream_t s) {
+    if (M > 0) k_aos_to_soa<<<(M + 255) / 256, 256, 0, s>>>(M, aos, soa, c0);
+}
+void launch_soa_add_aos(int M, const double* soa, double* aos, double c0, cudaStream_t s) {
+    if (M > 0) k_soa_add_aos<<<(M + 255) / 256, 256, 0, s>>>(M, soa, aos, c0);
+}
+}  // namespace afmib

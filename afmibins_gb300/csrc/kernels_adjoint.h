@@ -18,4 +18,8 @@ void launch_marker_grad(const Dims& d, int M, const double* X, const double* g, 
 void launch_springs_adjoint(int M, const double* X, const int* ns, const int* ni, double kspring, const double* lamG,
                             double* gX, double* dk_part, cudaStream_t s);
 
+// soa[c*M + k] = c0 * aos[3k + c]; aos[3k + c] += c0 * soa[c*M + k]
+void launch_aos_to_soa(int M, const double* aos, double* soa, double c0, cudaStream_t s);
+void launch_soa_add_aos(int M, const double* soa, double* aos, double c0, cudaStream_t s);
+
 }  // namespace afmib

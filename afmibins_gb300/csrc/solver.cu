@@ -16,6 +16,7 @@
 #include "afmib.h"
 #include "kernels.h"
 #include "kernels_ib.h"
+#include "kernels_adjoint.h"
 
 using namespace afmib;
 
@@ -75,6 +76,19 @@ struct afmib_solver {
     MarkerW<double> mw{};
     MarkerW<float> mw32{};
     float* G32 = nullptr;
+    bool nbr_symmetric = false;
+
+    // trajectory with checkpoints for the reverse (adjoint) pass
+    int traj_steps = 0, traj_every = 0;
+    std::vector<double*> ck_vel, ck_X;                     // checkpoints: [3N], [3M]
+    double *fin_vel = nullptr, *fin_X = nullptr;           // end state of the trajectory
+    std::vector<double*> rec_u0, rec_uh, rec_X0, rec_Xh;   // one segment's forward record
+    bool recording = false;
+    int rec_j = 0;
+    int traj_M = 0;
+    double* adj_f[4] = {};                                 // L, A, T, R: [3N] each
+    double *lamX = nullptr, *lamXh = nullptr, *mbar1 = nullptr, *mbar2 = nullptr, *lamG = nullptr, *Gtmp = nullptr,
+           *Ubuf = nullptr, *dkp = nullptr;
 
     // per-kernel event timing (afmib_profile_*): ranges recorded around each
     // launch while enabled, resolved at the next synchronisation
@@ -177,13 +191,15 @@ int sync(afmib_solver* s) {
 enum ProfId {
     P_ADVECT, P_HELM_RHS, P_CG_INIT, P_CG_APPLY, P_CG_UPDATE, P_CG_DIR, P_RBGS, P_RESID, P_RESID_NORM,
     P_RESTRICT, P_PROLONG, P_COARSE, P_DIV, P_GRAD_SUB, P_MEAN, P_WALL, P_SPRINGS, P_PREP, P_SORT,
-    P_TILES, P_SPREAD, P_INTERP, P_MARKER, P_HELM_DEFECT, P_LAP_DEFECT, P_CORRECT, P_COUNT
+    P_TILES, P_SPREAD, P_INTERP, P_MARKER, P_HELM_DEFECT, P_LAP_DEFECT, P_CORRECT, P_ADJ_ADVECT, P_ADJ_MARKER,
+    P_RBGS0, P_RESID0, P_RESTRICT0, P_PROLONG0, P_COUNT
 };
 const char* kProfNames[P_COUNT] = {
     "advect", "helm_rhs", "cg_init", "cg_apply", "cg_update", "cg_direction", "mg_rbgs", "mg_residual",
     "mg_residual_norm", "mg_restrict", "mg_prolong_add", "mg_coarse_cg", "div", "grad_sub", "mean_removal",
     "wall_update", "springs", "marker_prep", "radix_sort", "tile_bins", "spread_gather", "interp", "marker_update",
-    "helm_defect_fp64", "lap_defect_fp64", "add_correction_fp64"};
+    "helm_defect_fp64", "lap_defect_fp64", "add_correction_fp64", "advect_adjoint", "marker_adjoint",
+    "mg_rbgs_fine", "mg_residual_fine", "mg_restrict_fine", "mg_prolong_add_fine"};
 
 cudaEvent_t prof_event(afmib_solver* s) {
     if (!s->prof_pool.empty()) {
@@ -301,13 +317,14 @@ std::vector<MGLevelT<float>>& levels<float>(afmib_solver* s) { return s->lv32; }
 template <typename T>
 int smooth(afmib_solver* s, MGLevelT<T>& L, int sweeps) {
     const double Ns = (double)L.d.ncell() * sizeof(T);
+    const int id = L.d.nx == s->d.nx ? P_RBGS0 : P_RBGS;  // finest level kept apart in the profile
     for (int j = 0; j < sweeps; ++j) {
         {
-            ProfScope ps(s, P_RBGS, 1.5 * Ns);
+            ProfScope ps(s, id, 1.5 * Ns);
             launch_rbgs<T>(L.d, 0, L.x, L.b, s->st);
         }
         {
-            ProfScope ps(s, P_RBGS, 1.5 * Ns);
+            ProfScope ps(s, id, 1.5 * Ns);
             launch_rbgs<T>(L.d, 1, L.x, L.b, s->st);
         }
     }
@@ -342,21 +359,22 @@ int vcycle(afmib_solver* s, size_t l) {
         CKL();
         return AFMIB_OK;
     }
+    const bool fine = l == 0;
     TRY(smooth(s, L, s->cfg.nu1));
     {
-        ProfScope ps(s, P_RESID, 3 * Ns);
+        ProfScope ps(s, fine ? P_RESID0 : P_RESID, 3 * Ns);
         launch_residual<T>(L.d, L.r, L.x, L.b, nullptr, nullptr, s->st);
     }
     MGLevelT<T>& C = lv[l + 1];
     {
-        ProfScope ps(s, P_RESTRICT, Ns + Ns / 8);
+        ProfScope ps(s, fine ? P_RESTRICT0 : P_RESTRICT, Ns + Ns / 8);
         launch_restrict<T>(L.d, C.b, L.r, s->st);
     }
     CK(cudaMemsetAsync(C.x, 0, C.d.ncell() * sizeof(T), s->st));
     CKL();
     TRY(vcycle<T>(s, l + 1));
     {
-        ProfScope ps(s, P_PROLONG, 2 * Ns + Ns / 8);
+        ProfScope ps(s, fine ? P_PROLONG0 : P_PROLONG, 2 * Ns + Ns / 8);
         launch_prolong_add<T>(L.d, L.x, C.x, s->st);
     }
     TRY(smooth(s, L, s->cfg.nu2));
@@ -695,6 +713,23 @@ int bin_markers(afmib_solver* s, const double* P, bool fp32 = false) {
     return AFMIB_OK;
 }
 
+// f = scale * S(X) G with the FP64 bins and weights of the last bin_markers call
+int spread_generic(afmib_solver* s, const double* G, const double* vol, double scale, double* fu, double* fv,
+                   double* fw) {
+    const long long N = s->N();
+    CK(cudaMemsetAsync(fu, 0, N * sizeof(double), s->st));
+    CK(cudaMemsetAsync(fv, 0, N * sizeof(double), s->st));
+    CK(cudaMemsetAsync(fw, 0, N * sizeof(double), s->st));
+    const double touched = (double)s->stats.spread_tiles * s->TS * s->TS * s->TS;
+    {
+        ProfScope ps(s, P_SPREAD, (double)s->M * (24 + 3 * 8 + 8 + 8) + 3 * touched * 8);
+        launch_spread_gather<double>(s->d, s->TS, s->M, s->perm, s->mw, G, vol, scale, s->tslot, s->ctab, s->tlist,
+                                     s->tcount, s->ntiles, 1536, fu, fv, fw, s->dflag, s->st);
+    }
+    CKL();
+    return AFMIB_OK;
+}
+
 // f = spread(G) with the bins and weights of the last bin_markers call.
 // Algorithmic bytes: M (24 + 3s + 8 + 8) + 3 N_touched s with N_touched
 // taken as the faces of the active tiles (from the previous spreading).
@@ -764,17 +799,34 @@ int ib_one_step(afmib_solver* s) {
     };
     auto spread = [&]() { return f32 ? spread_forces32(s, vol) : spread_forces(s, vol, s->f[0], s->f[1], s->f[2]); };
     CK(cudaMemsetAsync(s->dflag, 0, sizeof(int), s->st));
+    const long long N = s->N();
+    if (s->recording) {
+        double* r = s->rec_u0[s->rec_j];
+        CK(cudaMemcpyAsync(r, s->u, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+        CK(cudaMemcpyAsync(r + N, s->v, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+        CK(cudaMemcpyAsync(r + 2 * N, s->w, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+        CK(cudaMemcpyAsync(s->rec_X0[s->rec_j], s->X, 3 * (size_t)M * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+    }
     // BE half: forces at X^n
     springs(s->X);
     TRY(bin_markers(s, s->X, f32));
     TRY(spread());
     TRY(substep(s));
+    if (s->recording) {
+        double* r = s->rec_uh[s->rec_j];
+        CK(cudaMemcpyAsync(r, s->u, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+        CK(cudaMemcpyAsync(r + N, s->v, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+        CK(cudaMemcpyAsync(r + 2 * N, s->w, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+    }
     // velocity at t+dt/2: at X^n for the half-step, then at X^{n+1/2}
     TRY(interp_markers(s, s->u, s->v, s->w, s->U1, f32));
     {
         ProfScope ps(s, P_MARKER, mbytes);
         launch_marker_axpy(M, s->Xh, s->X, s->U1, dt / 2, s->st);
     }
+    if (s->recording)
+        CK(cudaMemcpyAsync(s->rec_Xh[s->rec_j], s->Xh, 3 * (size_t)M * sizeof(double), cudaMemcpyDeviceToDevice,
+                           s->st));
     TRY(bin_markers(s, s->Xh, f32));
     TRY(interp_markers(s, s->u, s->v, s->w, s->U2, f32));
     // CN step with forces at X^{n+1/2}
@@ -789,6 +841,249 @@ int ib_one_step(afmib_solver* s) {
     CKL();
     TRY(check_marker_flag(s));
     s->stats.ib_steps++;
+    return AFMIB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Trajectory and adjoint. The forward trajectory stores the state (u, X) every
+// `every` steps; the reverse pass recomputes one segment at a time from its
+// checkpoint, recording u^n, u^{n+1/2}, X^n and X^{n+1/2} of each step, and
+// runs the reverse IB step over the records (periodic domain). In the
+// periodic domain the projection P and the Helmholtz operator H = I - s Delta
+// are symmetric, so their adjoints reuse the forward multigrid and CG solves.
+// ---------------------------------------------------------------------------
+int copy_vel_out(afmib_solver* s, double* dst) {
+    const long long N = s->N();
+    CK(cudaMemcpyAsync(dst, s->u, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+    CK(cudaMemcpyAsync(dst + N, s->v, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+    CK(cudaMemcpyAsync(dst + 2 * N, s->w, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+    return AFMIB_OK;
+}
+
+int refresh_shadow(afmib_solver* s);
+
+int copy_vel_in(afmib_solver* s, const double* src) {
+    const long long N = s->N();
+    CK(cudaMemcpyAsync(s->u, src, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+    CK(cudaMemcpyAsync(s->v, src + N, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+    CK(cudaMemcpyAsync(s->w, src + 2 * N, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+    return refresh_shadow(s);
+}
+
+// (u, v, w) <- P (u, v, w)
+int project_fields(afmib_solver* s, double* u, double* v, double* w) {
+    launch_div<double>(s->d, s->lv[0].b, u, v, w, nullptr, nullptr, s->st);
+    CKL();
+    if (s->mixed) TRY(mg_solve_mixed(s, nullptr));
+    else TRY(mg_solve(s, nullptr));
+    launch_grad_sub<double>(s->d, u, v, w, s->lv[0].x, nullptr, s->st);
+    CKL();
+    return AFMIB_OK;
+}
+
+// x <- H^{-1} b for each component, from a zero start
+int helm_inverse(afmib_solver* s, double* x, const double* b) {
+    const long long N = s->N();
+    CK(cudaMemsetAsync(x, 0, 3 * N * sizeof(double), s->st));
+    for (int c = 0; c < 3; ++c) {
+        if (s->mixed) TRY(helm_solve_mixed(s, c, s->s_minus(), x + c * N, b + c * N));
+        else TRY(cg_solve(s, c, s->s_minus(), x + c * N, b + c * N, nullptr));
+    }
+    return AFMIB_OK;
+}
+
+int traj_alloc(afmib_solver* s, int nsteps, int every) {
+    const long long N = s->N();
+    const int M = s->M;
+    const int nck = (nsteps + every - 1) / every;
+    auto grow = [&](std::vector<double*>& v, int count, size_t len) -> int {
+        while ((int)v.size() < count) {
+            double* p = nullptr;
+            TRY(dalloc(s, &p, len));
+            v.push_back(p);
+        }
+        return AFMIB_OK;
+    };
+    if (s->traj_M != M) {  // marker count changed: drop marker-sized buffers
+        s->ck_X.clear(); s->rec_X0.clear(); s->rec_Xh.clear();
+        s->fin_X = nullptr; s->lamX = nullptr;
+        s->traj_M = M;
+    }
+    TRY(grow(s->ck_vel, nck, 3 * N));
+    TRY(grow(s->ck_X, nck, 3 * (size_t)M));
+    TRY(grow(s->rec_u0, every, 3 * N));
+    TRY(grow(s->rec_uh, every, 3 * N));
+    TRY(grow(s->rec_X0, every, 3 * (size_t)M));
+    TRY(grow(s->rec_Xh, every, 3 * (size_t)M));
+    if (!s->fin_vel) TRY(dalloc(s, &s->fin_vel, 3 * N));
+    if (!s->adj_f[0])
+        for (int k = 0; k < 4; ++k) TRY(dalloc(s, &s->adj_f[k], 3 * N));
+    if (!s->fin_X || !s->lamX) {
+        TRY(dalloc(s, &s->fin_X, 3 * (size_t)M));
+        TRY(dalloc(s, &s->lamX, 3 * (size_t)M));
+        TRY(dalloc(s, &s->lamXh, 3 * (size_t)M));
+        TRY(dalloc(s, &s->mbar1, 3 * (size_t)M));
+        TRY(dalloc(s, &s->mbar2, 3 * (size_t)M));
+        TRY(dalloc(s, &s->lamG, 3 * (size_t)M));
+        TRY(dalloc(s, &s->Gtmp, 3 * (size_t)M));
+        TRY(dalloc(s, &s->Ubuf, 3 * (size_t)M));
+        TRY(dalloc(s, &s->dkp, (size_t)M));
+    }
+    return AFMIB_OK;
+}
+
+int traj_forward(afmib_solver* s, int nsteps, int every) {
+    if (s->d.channel) return s->fail(AFMIB_ERR_ARG, "the adjoint trajectory needs the periodic domain");
+    if (s->M <= 0) return s->fail(AFMIB_ERR_STATE, "no markers set");
+    if (!s->nbr_symmetric) return s->fail(AFMIB_ERR_ARG, "the adjoint needs symmetric spring neighbour lists");
+    if (s->has_vol) return s->fail(AFMIB_ERR_ARG, "the adjoint uses unit marker volumes");
+    if (nsteps < 1 || every < 1) return s->fail(AFMIB_ERR_ARG, "nsteps and every must be positive");
+    TRY(traj_alloc(s, nsteps, every));
+    const size_t mb = 3 * (size_t)s->M * sizeof(double);
+    for (int st = 0; st < nsteps; ++st) {
+        if (st % every == 0) {
+            TRY(copy_vel_out(s, s->ck_vel[st / every]));
+            CK(cudaMemcpyAsync(s->ck_X[st / every], s->X, mb, cudaMemcpyDeviceToDevice, s->st));
+        }
+        TRY(ib_one_step(s));
+    }
+    TRY(copy_vel_out(s, s->fin_vel));
+    CK(cudaMemcpyAsync(s->fin_X, s->X, mb, cudaMemcpyDeviceToDevice, s->st));
+    s->traj_steps = nsteps;
+    s->traj_every = every;
+    return sync(s);
+}
+
+// Reverse of one IB step over record j: (L = lam_u^{n+1}, lamX = lam_X^{n+1})
+// -> (lam_u^n, lam_X^n), lam_k accumulated in *lam_k.
+int adjoint_step(afmib_solver* s, int j, double* lam_k) {
+    const Dims& d = s->d;
+    const long long N = s->N();
+    const int M = s->M;
+    const double dt = s->cfg.dt, rho = s->cfg.rho, kk = s->cfg.k_spring;
+    const double n3 = (double)d.n * d.n * d.n;
+    double* L = s->adj_f[0];
+    double* A = s->adj_f[1];
+    double* T = s->adj_f[2];
+    double* R = s->adj_f[3];
+    const double* u0 = s->rec_u0[j];
+    const double* uh = s->rec_uh[j];
+    const double* X0 = s->rec_X0[j];
+    const double* Xh = s->rec_Xh[j];
+    auto F = [&](double* b, int c) { return b + c * N; };
+    auto cF = [&](const double* b, int c) { return b + c * N; };
+    // lam_U2 = dt lam_X1
+    launch_aos_to_soa(M, s->lamX, s->mbar2, dt, s->st);
+    // ---- CN: u1 = P H^{-1} (H+ u0 + dt (fh/rho - N(uh)))
+    CK(cudaMemcpyAsync(T, L, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+    TRY(project_fields(s, F(T, 0), F(T, 1), F(T, 2)));
+    TRY(helm_inverse(s, R, T));
+    for (int c = 0; c < 3; ++c) launch_helm_apply<double>(d, c, s->s_plus(), F(A, c), F(R, c), s->st);
+    // lam_uh = N'(uh)^T (-dt R)
+    CK(cudaMemsetAsync(T, 0, 3 * N * sizeof(double), s->st));
+    launch_axpy<double>(3 * N, T, R, -dt, s->st);
+    {
+        ProfScope ps(s, P_ADJ_ADVECT, 12.0 * N * 8);
+        launch_advect_adjoint(d, F(L, 0), F(L, 1), F(L, 2), cF(uh, 0), cF(uh, 1), cF(uh, 2), F(T, 0), F(T, 1),
+                              F(T, 2), 0, s->st);
+    }
+    CKL();
+    // fh = S(Xh) Gh with Gh = k K Xh; lam_fh = (dt/rho) R
+    TRY(bin_markers(s, Xh, false));
+    launch_springs<double>(M, Xh, s->nstart, s->nidx, kk, s->Gtmp, s->st);
+    TRY(interp_markers(s, F(R, 0), F(R, 1), F(R, 2), s->Ubuf, false));
+    CK(cudaMemsetAsync(s->lamG, 0, 3 * (size_t)M * sizeof(double), s->st));
+    launch_axpy<double>(3 * (long long)M, s->lamG, s->Ubuf, n3 * dt / rho, s->st);
+    CK(cudaMemsetAsync(s->lamXh, 0, 3 * (size_t)M * sizeof(double), s->st));
+    {
+        ProfScope ps(s, P_ADJ_MARKER, (double)M * 400, 2);
+        launch_marker_grad(d, M, Xh, s->Gtmp, F(R, 0), F(R, 1), F(R, 2), n3 * dt / rho, s->lamXh, s->st);
+        launch_springs_adjoint(M, Xh, s->nstart, s->nidx, kk, s->lamG, s->lamXh, s->dkp, s->st);
+    }
+    launch_sum<double>(M, s->dkp, s->red, s->scal + 11, s->st);
+    CKL();
+    TRY(read_scalars(s, 11, 1));
+    *lam_k += s->hscal[11];
+    // U2 = I(Xh) uh
+    TRY(spread_generic(s, s->mbar2, nullptr, 1.0, F(T, 0), F(T, 1), F(T, 2)));
+    launch_axpy<double>(3 * N, L, T, 1.0, s->st);
+    launch_marker_grad(d, M, Xh, s->mbar2, cF(uh, 0), cF(uh, 1), cF(uh, 2), 1.0, s->lamXh, s->st);
+    // Xh = X0 + dt/2 U1: lam_X0 += lam_Xh, lam_U1 = dt/2 lam_Xh
+    launch_axpy<double>(3 * (long long)M, s->lamX, s->lamXh, 1.0, s->st);
+    launch_aos_to_soa(M, s->lamXh, s->mbar1, dt / 2, s->st);
+    // U1 = I(X0) uh
+    TRY(bin_markers(s, X0, false));
+    TRY(spread_generic(s, s->mbar1, nullptr, 1.0, F(T, 0), F(T, 1), F(T, 2)));
+    launch_axpy<double>(3 * N, L, T, 1.0, s->st);
+    launch_marker_grad(d, M, X0, s->mbar1, cF(uh, 0), cF(uh, 1), cF(uh, 2), 1.0, s->lamX, s->st);
+    // ---- BE: uh = P H^{-1} (u0 + dt/2 (f0/rho - N(u0)))
+    CK(cudaMemcpyAsync(T, L, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+    TRY(project_fields(s, F(T, 0), F(T, 1), F(T, 2)));
+    TRY(helm_inverse(s, R, T));
+    launch_axpy<double>(3 * N, A, R, 1.0, s->st);
+    CK(cudaMemsetAsync(T, 0, 3 * N * sizeof(double), s->st));
+    launch_axpy<double>(3 * N, T, R, -dt / 2, s->st);
+    {
+        ProfScope ps(s, P_ADJ_ADVECT, 12.0 * N * 8);
+        launch_advect_adjoint(d, F(A, 0), F(A, 1), F(A, 2), cF(u0, 0), cF(u0, 1), cF(u0, 2), F(T, 0), F(T, 1),
+                              F(T, 2), 1, s->st);
+    }
+    // f0 = S(X0) G0, lam_f0 = dt/(2 rho) R (bins of X0 are current)
+    launch_springs<double>(M, X0, s->nstart, s->nidx, kk, s->Gtmp, s->st);
+    TRY(interp_markers(s, F(R, 0), F(R, 1), F(R, 2), s->Ubuf, false));
+    CK(cudaMemsetAsync(s->lamG, 0, 3 * (size_t)M * sizeof(double), s->st));
+    launch_axpy<double>(3 * (long long)M, s->lamG, s->Ubuf, n3 * dt / (2 * rho), s->st);
+    {
+        ProfScope ps(s, P_ADJ_MARKER, (double)M * 400, 2);
+        launch_marker_grad(d, M, X0, s->Gtmp, F(R, 0), F(R, 1), F(R, 2), n3 * dt / (2 * rho), s->lamX, s->st);
+        launch_springs_adjoint(M, X0, s->nstart, s->nidx, kk, s->lamG, s->lamX, s->dkp, s->st);
+    }
+    launch_sum<double>(M, s->dkp, s->red, s->scal + 11, s->st);
+    CKL();
+    TRY(read_scalars(s, 11, 1));
+    *lam_k += s->hscal[11];
+    CK(cudaMemcpyAsync(L, A, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+    return AFMIB_OK;
+}
+
+int traj_adjoint(afmib_solver* s, const double* lu, const double* lv, const double* lw, const double* lX,
+                 double* gX0, double* gk, double* gu0, double* gv0, double* gw0) {
+    if (s->traj_steps <= 0) return s->fail(AFMIB_ERR_STATE, "no trajectory: call afmib_trajectory_forward first");
+    const long long N = s->N();
+    const int M = s->M;
+    const size_t mb = 3 * (size_t)M * sizeof(double);
+    double* L = s->adj_f[0];
+    TRY(copy_in(s, L, lu, N));
+    TRY(copy_in(s, L + N, lv, N));
+    TRY(copy_in(s, L + 2 * N, lw, N));
+    TRY(copy_in(s, s->lamX, lX, 3 * (long long)M));
+    double lam_k = 0.0;
+    const int nseg = (s->traj_steps + s->traj_every - 1) / s->traj_every;
+    const bool half_saved = s->half;
+    for (int sg = nseg - 1; sg >= 0; --sg) {
+        const int first = sg * s->traj_every;
+        const int cnt = std::min(s->traj_every, s->traj_steps - first);
+        TRY(copy_vel_in(s, s->ck_vel[sg]));
+        CK(cudaMemcpyAsync(s->X, s->ck_X[sg], mb, cudaMemcpyDeviceToDevice, s->st));
+        s->recording = true;
+        for (int j = 0; j < cnt; ++j) {
+            s->rec_j = j;
+            const int rc = ib_one_step(s);
+            if (rc != AFMIB_OK) { s->recording = false; return rc; }
+        }
+        s->recording = false;
+        for (int j = cnt - 1; j >= 0; --j) TRY(adjoint_step(s, j, &lam_k));
+    }
+    // leave the solver at the end state of the trajectory
+    TRY(copy_vel_in(s, s->fin_vel));
+    CK(cudaMemcpyAsync(s->X, s->fin_X, mb, cudaMemcpyDeviceToDevice, s->st));
+    s->half = half_saved;
+    TRY(copy_out(s, gX0, s->lamX, 3 * (long long)M));
+    TRY(copy_out(s, gu0, L, N));
+    TRY(copy_out(s, gv0, L + N, N));
+    TRY(copy_out(s, gw0, L + 2 * N, N));
+    TRY(sync(s));
+    if (gk) *gk = lam_k;
     return AFMIB_OK;
 }
 
@@ -1080,6 +1375,18 @@ int afmib_set_markers(afmib_solver* s, int M, const double* X, const int* nstart
             CK(cudaMemcpy(hidx.data(), nidx, nnz * sizeof(int), cudaMemcpyDefault));
             for (int e = 0; e < nnz; ++e)
                 if (hidx[e] < 0 || hidx[e] >= M) return s->fail(AFMIB_ERR_ARG, "neighbour index out of range");
+            // symmetric lists (j in N(i) <=> i in N(j)) make K symmetric, which the adjoint relies on
+            std::vector<long long> pairs(nnz);
+            for (int i = 0; i < M; ++i)
+                for (int e = hstart[i]; e < hstart[i + 1]; ++e) pairs[e] = (long long)i * M + hidx[e];
+            std::sort(pairs.begin(), pairs.end());
+            bool sym = true;
+            for (int i = 0; i < M && sym; ++i)
+                for (int e = hstart[i]; e < hstart[i + 1] && sym; ++e)
+                    sym = std::binary_search(pairs.begin(), pairs.end(), (long long)hidx[e] * M + i);
+            s->nbr_symmetric = sym;
+        } else {
+            s->nbr_symmetric = true;
         }
     }
     TRY(marker_alloc(s, M, nnz));
@@ -1270,6 +1577,24 @@ int afmib_interp(afmib_solver* s, int M, const double* X, const double* u, const
     TRY(copy_out(s, U, s->U2, 3 * (long long)M));
     TRY(sync(s));
     return rc;
+}
+
+int afmib_set_spring(afmib_solver* s, double k) {
+    if (!s) return AFMIB_ERR_ARG;
+    s->cfg.k_spring = k;
+    return AFMIB_OK;
+}
+
+int afmib_trajectory_forward(afmib_solver* s, int nsteps, int ckpt_every) {
+    if (!s) return AFMIB_ERR_ARG;
+    return traj_forward(s, nsteps, ckpt_every);
+}
+
+int afmib_trajectory_adjoint(afmib_solver* s, const double* lam_u, const double* lam_v, const double* lam_w,
+                             const double* lam_X, double* grad_X0, double* grad_k, double* grad_u0, double* grad_v0,
+                             double* grad_w0) {
+    if (!s) return AFMIB_ERR_ARG;
+    return traj_adjoint(s, lam_u, lam_v, lam_w, lam_X, grad_X0, grad_k, grad_u0, grad_v0, grad_w0);
 }
 
 // ---- per-kernel profiling ----------------------------------------------------

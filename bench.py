@@ -9,9 +9,13 @@ initial velocity a seeded solenoidal random field (spectrum peaked at
 |k| = 4, RMS 0.1). Seeded synthetic inputs stand in for any dataset.
 
 One step = one IB step (BE and CN sub-steps, two spreads, two
-interpolations). `value` is measured with the state resident in HBM; `e2e`
-adds, every step, the upload of the state (u, v, w, X) from pinned host memory
-and the download of the new state through the C ABI.
+interpolations). The headline `value` is the mixed-precision form (FP32
+stencils, smoothing, spreading and interpolation inside FP64 defect
+correction); the FP64 form is run from the same initial state for the same
+steps, and the line carries its steps/s and the mixed form's error against it.
+`value` is measured with the state resident in HBM; `e2e` adds, every step,
+the upload of the state (u, v, w, X) from pinned host memory and the download
+of the new state through the C ABI.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -39,7 +43,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed",
+                    help="headline form; with mixed, the FP64 form is also run from the same state")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--shells", type=int, default=10)
     ap.add_argument("--per-shell", type=int, default=20000)
@@ -178,6 +184,47 @@ def config_dict(args):
             "l2": "inputs larger than L2 (each field 134 MB at 256^3 FP64, ~30 fields resident)"}
 
 
+def rel_err(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def pressure_err(p, pref, n, mu, dt):
+    """Pressure is fixed up to phi -> phi + c, i.e. p -> p + c (periodic)."""
+    dp = p - pref
+    return float(np.max(np.abs(dp - dp.mean())) / max(np.max(np.abs(pref - pref.mean())), 1e-300))
+
+
+def run_form(capi, torch, args, prec, state, dev, stream, timed=True):
+    """Create a solver of the given precision on the initial state, run the
+    warm-up and the timed steps; return (solver, ms, launches, clocks, wall)."""
+    X, nstart, nidx, u, v, w = state
+    sv = capi.Solver(args.n, mu=args.mu, rho=1.0, dt=args.dt, tol=args.tol, k_spring=0.5, precision=prec,
+                     stream=stream.cuda_stream)
+    ud, vd, wd = (torch.from_numpy(a).to(dev) for a in (u, v, w))
+    Xd = torch.from_numpy(X).to(dev)
+    torch.cuda.synchronize()
+    sv.set_velocity(ud, vd, wd)
+    sv.project()
+    sv.set_markers(Xd, nstart, nidx)
+    for _ in range(args.warmup):
+        sv.ib_step(1)
+    sv.synchronize()
+    l0 = sv.stats()["kernel_launches"]
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            sv.ib_step(1)
+        e1.record(stream)
+        stream.synchronize()
+        wall = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    return sv, e0.elapsed_time(e1), sv.stats()["kernel_launches"] - l0, clk.summary(), wall
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -195,55 +242,57 @@ def main():
         dist.init_process_group("nccl")
     from afmibins_gb300 import capi
 
-    X, nstart, nidx, u, v, w = workload(args.n, args.shells, args.per_shell, args.radius, args.min_sep,
-                                        seed_offset=rank)
+    # replicas: each rank runs its own seeded simulation (no data-path collective)
+    state = workload(args.n, args.shells, args.per_shell, args.radius, args.min_sep, seed_offset=rank)
+    X = state[0]
     M = X.shape[0]
-    stream = torch.cuda.Stream()
-    prec = capi.FP64 if args.precision == "fp64" else capi.MIXED
-    sv = capi.Solver(args.n, mu=args.mu, rho=1.0, dt=args.dt, tol=args.tol, k_spring=0.5, precision=prec,
-                     stream=stream.cuda_stream)
     dev = torch.device("cuda", local)
-    ud, vd, wd = (torch.from_numpy(a).to(dev) for a in (u, v, w))
-    Xd = torch.from_numpy(X).to(dev)
-    torch.cuda.synchronize()
-    sv.set_velocity(ud, vd, wd)
-    sv.project()
-    sv.set_markers(Xd, nstart, nidx)
+    stream = torch.cuda.Stream()
+    headline = capi.FP64 if args.precision == "fp64" else capi.MIXED
 
     def barrier():
         if dist is not None:
             dist.barrier()
 
-    for _ in range(args.warmup):
-        sv.ib_step(1)
-    sv.synchronize()
-
-    # ---- timed region: state resident in HBM
-    l0 = sv.stats()["kernel_launches"]
-    barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        with torch.cuda.stream(stream):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            t0 = time.perf_counter()
-            for _ in range(args.steps):
-                sv.ib_step(1)
-            e1.record(stream)
-        stream.synchronize()
-        wall = time.perf_counter() - t0
-    torch.cuda.synchronize()
-    barrier()
-    ms = e0.elapsed_time(e1)
-    launches = sv.stats()["kernel_launches"] - l0
-    ms_max = ms
-    if dist is not None:
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
+        return float(t.item())
+
+    # ---- the FP64 form (the drop-in) from the same initial state, for the
+    #      speed-up and the error of the mixed form
+    fp64 = None
+    if headline == capi.MIXED and not args.no_fp64:
+        barrier()
+        sv64, ms64, l64, clk64, _ = run_form(capi, torch, args, capi.FP64, state, dev, stream)
+        ms64 = max_over_ranks(ms64)
+        u64 = sv64.get_velocity()
+        p64 = sv64.get_pressure()
+        X64 = sv64.get_markers()
+        fp64 = {"value": world * args.steps / (ms64 / 1000.0), "ms_per_step": ms64 / args.steps,
+                "gpu_launches": int(l64)}
+        sv64.close()
+
+    # ---- headline form: timed region with the state resident in HBM
+    barrier()
+    sv, ms, launches, clocks, wall = run_form(capi, torch, args, headline, state, dev, stream)
+    barrier()
+    ms_max = max_over_ranks(ms)
     value = world * args.steps / (ms_max / 1000.0)
     st = sv.stats()
+    errors = None
+    if fp64 is not None:
+        uh = sv.get_velocity()
+        ph = sv.get_pressure()
+        Xh = sv.get_markers()
+        errors = {"velocity": max(rel_err(a, b) for a, b in zip(uh, u64)),
+                  "pressure": pressure_err(ph, p64, args.n, args.mu, args.dt),
+                  "marker_displacement": rel_err(Xh - X, X64 - X),
+                  "marker_position_max_abs": float(np.max(np.abs(Xh - X64))),
+                  "steps": args.warmup + args.steps}
+        fp64["speedup_of_headline"] = value / fp64["value"]
 
     # ---- e2e through the C ABI with host buffers
     e2e = None
@@ -264,11 +313,7 @@ def main():
             sv.get_velocity((hu, hv, hw))
             sv.get_markers(hX)
         torch.cuda.synchronize()
-        we = time.perf_counter() - t0
-        if dist is not None:
-            t = torch.tensor([we], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            we = float(t.item())
+        we = max_over_ranks(time.perf_counter() - t0)
         bio = 3 * N * 8 + M * 24
         e2e = {"value": world * ke / we, "unit": UNIT, "h2d_bytes_per_step": bio, "d2h_bytes_per_step": bio,
                "steps": ke}
@@ -288,7 +333,8 @@ def main():
         achieved = (kbytes / nl) / ((kms / nl) * 1e-3) / 1e9
         roofline = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
                     "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
-                    "bytes_per_launch": kbytes / nl, "ms_per_launch": kms / nl}
+                    "bytes_per_launch": kbytes / nl, "ms_per_launch": kms / nl,
+                    "note": "all launches of the family at every multigrid level, per-launch average"}
         kernels = {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / total_ms, 4),
                        "GB_s": round(v[2] / (v[1] * 1e-3) / 1e9, 1) if v[1] > 0 else None}
                    for k, v in sorted(table.items(), key=lambda kv: -kv[1][1])}
@@ -302,12 +348,13 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if headline == capi.FP64 else "f32+f64",
             "data": "synthetic (seeded shells and solenoidal field)", "config": config_dict(args),
-            "roofline": roofline,
-            "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clk.summary(),
+            "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clocks,
+            "fp64_form": fp64, "errors_vs_fp64": errors,
             "solver": {"cg_iters_per_step": st["cg_iters"] / max(1, st["ib_steps"]),
                        "mg_cycles_per_step": st["mg_cycles"] / max(1, st["ib_steps"]),
+                       "outer_iters_per_step": st["outer_iters"] / max(1, st["ib_steps"]),
                        "spread_tiles": st["spread_tiles"], "wall_s": wall},
             "kernels": kernels,
         }

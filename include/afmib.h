@@ -115,6 +115,23 @@ int afmib_set_marker_positions(afmib_solver* s, const double* X);
  * (the coupling left as comments in test/ib_ns_test.cc:73-96). */
 int afmib_ib_step(afmib_solver* s, int nsteps);
 
+/* Spring stiffness k of the membrane (G_i = k * sum_j (X_j - X_i)). */
+int afmib_set_spring(afmib_solver* s, double k);
+
+/* ---- adjoint (no reference counterpart: the reference has no adjoint) ----
+ * afmib_trajectory_forward runs nsteps IB steps from the current state and
+ * keeps the state (u, X) every ckpt_every steps in device memory.
+ * afmib_trajectory_adjoint takes the gradient of a loss with respect to the
+ * final velocity (lam_u, lam_v, lam_w; null -> 0) and final markers
+ * (lam_X[M][3]; null -> 0) and returns the gradients with respect to the
+ * initial markers (grad_X0[M][3]), the stiffness k (*grad_k) and optionally
+ * the initial velocity, recomputing each segment from its checkpoint.
+ * Periodic domain, unit marker volumes and symmetric neighbour lists. */
+int afmib_trajectory_forward(afmib_solver* s, int nsteps, int ckpt_every);
+int afmib_trajectory_adjoint(afmib_solver* s, const double* lam_u, const double* lam_v, const double* lam_w,
+                             const double* lam_X, double* grad_X0, double* grad_k, double* grad_u0, double* grad_v0,
+                             double* grad_w0);
+
 /* ---- single operators on caller buffers, on the solver's grid and stream ---- */
 /* alg::div<nx,ny,nz,n>(d, u, v, w, top, bottom), src/alg/div.h:29-60 (top/bottom may be null) */
 int afmib_div(afmib_solver* s, double* d, const double* u, const double* v, const double* w, const double* top,
