@@ -100,6 +100,11 @@ void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, R
 // One red (color 0) or black (color 1) Gauss-Seidel half sweep.
 template <typename T>
 void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s);
+// One full red+black sweep in a single tile-fused launch, out of place
+// (xin -> xout); identical cell for cell to the two per-colour launches.
+template <typename T>
+void launch_rbgs_fused(const Dims& d, const T* xin, T* xout, const T* b, cudaStream_t s);
+bool rbgs_fused_ok(const Dims& d);  // level large enough for the fused tiles
 // Full-weighting restriction, src/mg/solver.h:153-181 (d = fine dims).
 template <typename T>
 void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s);

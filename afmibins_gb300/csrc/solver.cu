@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -24,6 +25,7 @@ template <typename T>
 struct MGLevelT {
     Dims d;
     T *x, *b, *r;
+    T* x2;  // ping-pong partner of x for the tile-fused sweep (null on small levels)
 };
 typedef MGLevelT<double> MGLevel;
 
@@ -55,6 +57,7 @@ struct afmib_solver {
     std::vector<MGLevelT<float>> lv32;
     double *cx64 = nullptr, *cb64 = nullptr, *cr64 = nullptr;
     int inner_cycles = 3;
+    bool fused_smoother = true;
     RedScratch red{};
     double* scal = nullptr;   // device scalars: [0..4] CG, [8] sum, [9] sumsq
     double* hscal = nullptr;  // pinned mirror
@@ -318,7 +321,21 @@ template <typename T>
 int smooth(afmib_solver* s, MGLevelT<T>& L, int sweeps) {
     const double Ns = (double)L.d.ncell() * sizeof(T);
     const int id = L.d.nx == s->d.nx ? P_RBGS0 : P_RBGS;  // finest level kept apart in the profile
-    for (int j = 0; j < sweeps; ++j) {
+    int j = 0;
+    if (L.x2 && s->fused_smoother) {
+        // pairs of tile-fused sweeps, x -> x2 -> x
+        for (; j + 2 <= sweeps; j += 2) {
+            {
+                ProfScope ps(s, id, 3 * Ns);
+                launch_rbgs_fused<T>(L.d, L.x, L.x2, L.b, s->st);
+            }
+            {
+                ProfScope ps(s, id, 3 * Ns);
+                launch_rbgs_fused<T>(L.d, L.x2, L.x, L.b, s->st);
+            }
+        }
+    }
+    for (; j < sweeps; ++j) {
         {
             ProfScope ps(s, id, 1.5 * Ns);
             launch_rbgs<T>(L.d, 0, L.x, L.b, s->st);
@@ -1121,6 +1138,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (g.bc != AFMIB_BC_PERIODIC && g.bc != AFMIB_BC_CHANNEL) return s->fail(AFMIB_ERR_ARG, "bc must be periodic or channel");
     if (g.precision != AFMIB_FP64 && g.precision != AFMIB_MIXED) return s->fail(AFMIB_ERR_ARG, "precision");
     s->mixed = g.precision == AFMIB_MIXED;
+    if (const char* e = std::getenv("AFMIB_SMOOTHER")) s->fused_smoother = std::string(e) != "percolour";
     if (!(g.rho > 0) || !(g.dt > 0) || !(g.mu >= 0) || !(g.tol > 0)) return s->fail(AFMIB_ERR_ARG, "mu, rho, dt, tol");
     s->d = Dims{g.nx, g.ny, g.nz, g.n, g.bc == AFMIB_BC_CHANNEL ? 1 : 0};
     if (stream) {
@@ -1179,11 +1197,12 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
                 return s->fail(AFMIB_ERR_ARG, "mg_levels exceeds the number of halvings of the grid");
             t.nx /= 2; t.ny /= 2; t.nz /= 2; t.n = t.n / 2 > 0 ? t.n / 2 : 1;
         }
-        MGLevel L{t, nullptr, nullptr, nullptr};
+        MGLevel L{t, nullptr, nullptr, nullptr, nullptr};
         const long long n = t.ncell();
         TRY(dalloc(s, &L.x, n));
         TRY(dalloc(s, &L.b, n));
         TRY(dalloc(s, &L.r, n));
+        if (rbgs_fused_ok(t)) TRY(dalloc(s, &L.x2, n));
         s->lv.push_back(L);
     }
     // smoothed levels need even extents for the red-black colouring
@@ -1212,10 +1231,11 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
         TRY(dalloc(s, &s->cg32_p, N));
         TRY(dalloc(s, &s->cg32_q, N));
         for (const MGLevel& L : s->lv) {
-            MGLevelT<float> F{L.d, nullptr, nullptr, nullptr};
+            MGLevelT<float> F{L.d, nullptr, nullptr, nullptr, nullptr};
             TRY(dalloc(s, &F.x, L.d.ncell()));
             TRY(dalloc(s, &F.b, L.d.ncell()));
             TRY(dalloc(s, &F.r, L.d.ncell()));
+            if (rbgs_fused_ok(L.d)) TRY(dalloc(s, &F.x2, L.d.ncell()));
             s->lv32.push_back(F);
         }
         TRY(dalloc(s, &s->cx64, nc));
@@ -1577,6 +1597,24 @@ int afmib_interp(afmib_solver* s, int M, const double* X, const double* u, const
     TRY(copy_out(s, U, s->U2, 3 * (long long)M));
     TRY(sync(s));
     return rc;
+}
+
+int afmib_set_tolerance(afmib_solver* s, double tol) {
+    if (!s || !(tol > 0)) return AFMIB_ERR_ARG;
+    s->cfg.tol = tol;
+    return AFMIB_OK;
+}
+
+int afmib_smooth(afmib_solver* s, double* x, const double* b) {
+    if (!s || !x || !b) return AFMIB_ERR_ARG;
+    MGLevel& L = s->lv[0];
+    TRY(copy_in(s, L.x, x, s->N()));
+    TRY(copy_in(s, L.b, b, s->N()));
+    launch_rbgs<double>(L.d, 0, L.x, L.b, s->st);
+    launch_rbgs<double>(L.d, 1, L.x, L.b, s->st);
+    CKL();
+    TRY(copy_out(s, x, L.x, s->N()));
+    return sync(s);
 }
 
 int afmib_set_spring(afmib_solver* s, double k) {

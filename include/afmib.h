@@ -151,6 +151,11 @@ int afmib_lap_apply(afmib_solver* s, double* y, const double* x);
 int afmib_helm_apply(afmib_solver* s, int comp, double scale, double* y, const double* x);
 /* alg::conjugate_gradient(x, helmholtz(scale), b, tol), src/alg/cg.h:32-56 */
 int afmib_helmholtz_cg(afmib_solver* s, int comp, double scale, double* x, const double* b, int* iters);
+/* alg::smooth(x, L, b), src/alg/smooth.h:35-51: one Gauss-Seidel sweep of the
+ * pressure Laplacian on x, here in red-black order (red cells, then black) */
+int afmib_smooth(afmib_solver* s, double* x, const double* b);
+/* Solver tolerance (the tol of ns::solver, mg::solver and conjugate_gradient) */
+int afmib_set_tolerance(afmib_solver* s, double tol);
 /* mg::solver::restriction / interpolation (assigning), src/mg/solver.h:153-181, 71-151 */
 int afmib_restrict(afmib_solver* s, double* coarse, const double* fine);
 int afmib_prolong(afmib_solver* s, double* fine, const double* coarse);
