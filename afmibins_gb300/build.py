@@ -23,7 +23,7 @@ OUT_DIR = os.path.join(PKG, "_lib")
 OBJ_DIR = os.path.join(PKG, "_build")
 LIB_PATH = os.path.join(OUT_DIR, "libafmib.so")
 
-SOURCES = ["kernels_field.cu", "kernels_mg.cu", "kernels_ib.cu", "kernels_adjoint.cu", "solver.cu"]
+SOURCES = ["kernels_field.cu", "kernels_mg.cu", "kernels_ib.cu", "kernels_adjoint.cu", "solver.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-diag-suppress", "177",
          "-I", INCLUDE, "-I", CSRC]

@@ -86,6 +86,9 @@ _SIGS = {
     "afmib_set_spring": ([_vp, ctypes.c_double], ctypes.c_int),
     "afmib_set_tolerance": ([_vp, ctypes.c_double], ctypes.c_int),
     "afmib_smooth": ([_vp, _vp, _vp], ctypes.c_int),
+    "afmib_helmholtz_cg_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_double, ctypes.c_double, ctypes.c_int, _vp, _vp,
+                                    ctypes.POINTER(ctypes.c_int), _vp], ctypes.c_int),
     "afmib_trajectory_forward": ([_vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "afmib_trajectory_adjoint": ([_vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_double), _vp, _vp, _vp],
                                  ctypes.c_int),

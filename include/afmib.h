@@ -168,6 +168,20 @@ int afmib_spread(afmib_solver* s, int M, const double* X, const double* F, const
 int afmib_interp(afmib_solver* s, int M, const double* X, const double* u, const double* v, const double* w,
                  double* U);
 
+/* Helmholtz CG that allocates nothing (no reference counterpart). For callers
+ * that may not call cudaMalloc where they solve: code inside a memory pool or
+ * arena that owns the process's device allocations, code under a strict
+ * memory budget of its host framework, or inner loops that cannot take the
+ * implicit synchronisation of an allocation. Same solve and stopping rule as
+ * afmib_helmholtz_cg, on the caller's device buffers x (warm start, solution)
+ * and b; its working vectors live in an array the library reserves on every
+ * GPU (about 6.4 MB) for as long as it is loaded. Limit: nx*ny*nz <= 64^3
+ * (larger -> AFMIB_ERR_CAPACITY); periodic, or channel components 0 and 2.
+ * The first call on a device looks up the array's address: make it before any
+ * stream capture. Calls that overlap on the GPU share the array and race. */
+int afmib_helmholtz_cg_noalloc(int nx, int ny, int nz, int n, int bc, int comp, double scale, double tol,
+                               int max_iters, double* x, const double* b, int* iters, void* stream);
+
 /* ---- per-kernel timing (no reference counterpart; the reference has no
  * profiling): while enabled, every kernel launch is bracketed by CUDA events
  * on the solver's stream and accumulated per kernel family with its
