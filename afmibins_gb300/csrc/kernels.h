@@ -38,8 +38,9 @@ void launch_wall_update(const Dims& d, double* walls, const double* wallgrad, cu
 //   be=0: r = (I + s_plus*Delta) u_old + bdy(s_plus) - bdy(s_minus) + dt*(f/rho - adv)
 // src/ns/solver.h:105-135 with src/ns/helmholtz.h:177-196. walls: [top|bottom]
 // rows of this component (null in periodic mode or for v).
-template <typename T, typename TF>
-void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const TF* f, const TF* adv,
+// TF: force storage type, TA: advection storage type
+template <typename T, typename TF, typename TA>
+void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const TF* f, const TA* adv,
                      const double* top, const double* bottom, double s_plus, double s_minus, double dt,
                      double inv_rho, cudaStream_t s);
 // Mixed form: r = b - (I + s Delta) x in FP64, stored as TD, out[0] = ||r||^2.

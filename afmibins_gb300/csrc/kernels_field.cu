@@ -194,9 +194,9 @@ __global__ void k_helm_apply(Dims d, int comp, T s, T* __restrict__ out, const T
 }
 
 // Right-hand side of the viscous solve, src/ns/solver.h:105-135.
-template <typename T, typename TF>
+template <typename T, typename TF, typename TA>
 __global__ void k_helm_rhs(Dims d, int comp, int be, T* __restrict__ r, const T* __restrict__ uold,
-                           const TF* __restrict__ f, const TF* __restrict__ adv, const double* __restrict__ top,
+                           const TF* __restrict__ f, const TA* __restrict__ adv, const double* __restrict__ top,
                            const double* __restrict__ bottom, double s_plus, double s_minus, double hdt,
                            double inv_rho) {
     AFMIB_XYZ
@@ -395,11 +395,11 @@ void launch_grad_sub(const Dims& d, T* u, T* v, T* w, const T* phi, T* wallgrad,
 void launch_wall_update(const Dims& d, double* walls, const double* wallgrad, cudaStream_t s) {
     k_wall_update<<<ew_blocks((long long)d.nx * d.nz), 256, 0, s>>>(d, walls, wallgrad);
 }
-template <typename T, typename TF>
-void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const TF* f, const TF* adv, const double* top,
+template <typename T, typename TF, typename TA>
+void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const TF* f, const TA* adv, const double* top,
                      const double* bottom, double s_plus, double s_minus, double dt, double inv_rho, cudaStream_t s) {
-    k_helm_rhs<T, TF><<<grid3(d), block3(), 0, s>>>(d, comp, be, r, uold, f, adv, top, bottom, s_plus, s_minus,
-                                                    be ? dt / 2 : dt, inv_rho);
+    k_helm_rhs<T, TF, TA><<<grid3(d), block3(), 0, s>>>(d, comp, be, r, uold, f, adv, top, bottom, s_plus, s_minus,
+                                                        be ? dt / 2 : dt, inv_rho);
 }
 template <typename TD>
 void launch_helm_defect(const Dims& d, int comp, double scale, const double* x, const double* b, TD* r, RedScratch sc,
@@ -484,12 +484,15 @@ template void launch_advect<double, float>(const Dims&, float*, float*, float*, 
                                            const double*, cudaStream_t);
 template void launch_advect<float, float>(const Dims&, float*, float*, float*, const float*, const float*,
                                           const float*, cudaStream_t);
-template void launch_helm_rhs<double, double>(const Dims&, int, int, double*, const double*, const double*,
-                                              const double*, const double*, const double*, double, double, double,
-                                              double, cudaStream_t);
-template void launch_helm_rhs<double, float>(const Dims&, int, int, double*, const double*, const float*, const float*,
-                                             const double*, const double*, double, double, double, double,
-                                             cudaStream_t);
+template void launch_helm_rhs<double, double, double>(const Dims&, int, int, double*, const double*, const double*,
+                                                      const double*, const double*, const double*, double, double,
+                                                      double, double, cudaStream_t);
+template void launch_helm_rhs<double, float, float>(const Dims&, int, int, double*, const double*, const float*,
+                                                    const float*, const double*, const double*, double, double,
+                                                    double, double, cudaStream_t);
+template void launch_helm_rhs<double, double, float>(const Dims&, int, int, double*, const double*, const double*,
+                                                     const float*, const double*, const double*, double, double,
+                                                     double, double, cudaStream_t);
 template void launch_helm_defect<float>(const Dims&, int, double, const double*, const double*, float*, RedScratch,
                                         double*, cudaStream_t);
 template void launch_cg_init_zero<float>(long long, const float*, float*, float*, float*, RedScratch, double*,

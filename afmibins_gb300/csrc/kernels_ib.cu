@@ -91,8 +91,8 @@ __global__ void k_marker_prep(Dims d, int TS, int M, const double* __restrict__ 
     const int ntx = d.nx / TS, nty = d.ny / TS;
     const unsigned tile = (unsigned)(tx + ntx * (ty + nty * tz));
     const unsigned local = (unsigned)((cell[0] % TS) + TS * ((cell[1] % TS) + TS * (cell[2] % TS)));
-    keys[k] = tile * (unsigned)(TS * TS * TS) + local;
-    vals[k] = k;
+    if (keys) keys[k] = tile * (unsigned)(TS * TS * TS) + local;  // null: weights only
+    if (vals) vals[k] = k;
 }
 
 // ---------------------------------------------------------------------------

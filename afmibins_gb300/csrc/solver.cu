@@ -58,6 +58,7 @@ struct afmib_solver {
     double *cx64 = nullptr, *cb64 = nullptr, *cr64 = nullptr;
     int inner_cycles = 3;
     bool fused_smoother = true;
+    bool spread64 = false, interp64 = false;  // mixed form: IB transfers in FP64
     RedScratch red{};
     double* scal = nullptr;   // device scalars: [0..4] CG, [8] sum, [9] sumsq
     double* hscal = nullptr;  // pinned mirror
@@ -608,13 +609,17 @@ int substep(afmib_solver* s) {
     for (int c = 0; c < 3; ++c) {
         const double* top = (!d.channel || c == 1) ? nullptr : (c == 0 ? ut : wt);
         const double* bot = (!d.channel || c == 1) ? nullptr : (c == 0 ? ub : wb);
-        if (s->mixed) {
+        if (s->mixed && s->spread64) {
+            ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 4 + 8));
+            launch_helm_rhs<double, double, float>(d, c, be ? 1 : 0, s->rhs[c], s->uo[c], s->f[c], s->adv32[c], top,
+                                                   bot, s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
+        } else if (s->mixed) {
             ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 4 + 4 + 8));
-            launch_helm_rhs<double, float>(d, c, be ? 1 : 0, s->rhs[c], s->uo[c], s->f32[c], s->adv32[c], top, bot,
-                                           s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
+            launch_helm_rhs<double, float, float>(d, c, be ? 1 : 0, s->rhs[c], s->uo[c], s->f32[c], s->adv32[c], top,
+                                                  bot, s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
         } else {
             ProfScope ps(s, P_HELM_RHS, 4 * Ns);
-            launch_helm_rhs<double, double>(d, c, be ? 1 : 0, s->rhs[c], s->uo[c], s->f[c], s->adv[c], top, bot,
+            launch_helm_rhs<double, double, double>(d, c, be ? 1 : 0, s->rhs[c], s->uo[c], s->f[c], s->adv[c], top, bot,
                                             s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
         }
     }
@@ -808,13 +813,27 @@ int ib_one_step(afmib_solver* s) {
     const double dt = s->cfg.dt;
     const double* vol = s->has_vol ? s->mvol : nullptr;
     const double mbytes = (double)M * (24 + 24 + 24);
-    const bool f32 = s->mixed;
+    // precision of each transfer: FP64 form -> FP64; mixed -> FP32 unless ib_fp64 asks for FP64
+    const bool sp32 = s->mixed && !s->spread64;
+    const bool in32 = s->mixed && !s->interp64;
     auto springs = [&](const double* P) {
         ProfScope ps(s, P_SPRINGS, mbytes);
-        if (f32) launch_springs<float>(M, P, s->nstart, s->nidx, s->cfg.k_spring, s->G32, s->st);
+        if (sp32) launch_springs<float>(M, P, s->nstart, s->nidx, s->cfg.k_spring, s->G32, s->st);
         else launch_springs<double>(M, P, s->nstart, s->nidx, s->cfg.k_spring, s->G, s->st);
     };
-    auto spread = [&]() { return f32 ? spread_forces32(s, vol) : spread_forces(s, vol, s->f[0], s->f[1], s->f[2]); };
+    auto bin = [&](const double* P) -> int {
+        TRY(bin_markers(s, P, sp32));
+        if (sp32 != in32) {  // the other weight set for the other transfer (same bins)
+            ProfScope ps(s, P_PREP, (double)M * (24 + 4 + 4 + 12 + 6 + 24 * (in32 ? 4 : 8)));
+            if (in32) launch_marker_prep<float>(s->d, s->TS, M, P, nullptr, nullptr, s->mw32, s->dflag, s->st);
+            else launch_marker_prep<double>(s->d, s->TS, M, P, nullptr, nullptr, s->mw, s->dflag, s->st);
+        }
+        return AFMIB_OK;
+    };
+    auto spread = [&]() { return sp32 ? spread_forces32(s, vol) : spread_forces(s, vol, s->f[0], s->f[1], s->f[2]); };
+    auto interp = [&](double* U) {
+        return in32 ? interp_markers(s, s->u, s->v, s->w, U, true) : interp_markers(s, s->u, s->v, s->w, U, false);
+    };
     CK(cudaMemsetAsync(s->dflag, 0, sizeof(int), s->st));
     const long long N = s->N();
     if (s->recording) {
@@ -826,7 +845,7 @@ int ib_one_step(afmib_solver* s) {
     }
     // BE half: forces at X^n
     springs(s->X);
-    TRY(bin_markers(s, s->X, f32));
+    TRY(bin(s->X));
     TRY(spread());
     TRY(substep(s));
     if (s->recording) {
@@ -836,7 +855,7 @@ int ib_one_step(afmib_solver* s) {
         CK(cudaMemcpyAsync(r + 2 * N, s->w, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
     }
     // velocity at t+dt/2: at X^n for the half-step, then at X^{n+1/2}
-    TRY(interp_markers(s, s->u, s->v, s->w, s->U1, f32));
+    TRY(interp(s->U1));
     {
         ProfScope ps(s, P_MARKER, mbytes);
         launch_marker_axpy(M, s->Xh, s->X, s->U1, dt / 2, s->st);
@@ -844,8 +863,8 @@ int ib_one_step(afmib_solver* s) {
     if (s->recording)
         CK(cudaMemcpyAsync(s->rec_Xh[s->rec_j], s->Xh, 3 * (size_t)M * sizeof(double), cudaMemcpyDeviceToDevice,
                            s->st));
-    TRY(bin_markers(s, s->Xh, f32));
-    TRY(interp_markers(s, s->u, s->v, s->w, s->U2, f32));
+    TRY(bin(s->Xh));
+    TRY(interp(s->U2));
     // CN step with forces at X^{n+1/2}
     springs(s->Xh);
     CKL();
@@ -1138,6 +1157,8 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (g.bc != AFMIB_BC_PERIODIC && g.bc != AFMIB_BC_CHANNEL) return s->fail(AFMIB_ERR_ARG, "bc must be periodic or channel");
     if (g.precision != AFMIB_FP64 && g.precision != AFMIB_MIXED) return s->fail(AFMIB_ERR_ARG, "precision");
     s->mixed = g.precision == AFMIB_MIXED;
+    s->spread64 = s->mixed && (g.ib_fp64 & 1);
+    s->interp64 = s->mixed && (g.ib_fp64 & 2);
     if (const char* e = std::getenv("AFMIB_SMOOTHER")) s->fused_smoother = std::string(e) != "percolour";
     if (!(g.rho > 0) || !(g.dt > 0) || !(g.mu >= 0) || !(g.tol > 0)) return s->fail(AFMIB_ERR_ARG, "mu, rho, dt, tol");
     s->d = Dims{g.nx, g.ny, g.nz, g.n, g.bc == AFMIB_BC_CHANNEL ? 1 : 0};

@@ -27,8 +27,8 @@ def test_error_strings_without_gpu():
 
 
 def test_config_layout_matches_header():
-    # the ctypes mirror must agree with the C struct: 9 ints, 4 doubles, 2 ints, 2 doubles
-    assert ctypes.sizeof(capi.Config) == 9 * 4 + 4 + 4 * 8 + 2 * 4 + 2 * 8
+    # the ctypes mirror must agree with the C struct: 9 ints (+pad), 4 doubles, 2 ints, 2 doubles, 1 int (+pad)
+    assert ctypes.sizeof(capi.Config) == 9 * 4 + 4 + 4 * 8 + 2 * 4 + 2 * 8 + 8
 
 
 def test_build_is_in_tree():
