@@ -57,8 +57,19 @@ struct afmib_solver {
     std::vector<MGLevelT<float>> lv32;
     double *cx64 = nullptr, *cb64 = nullptr, *cr64 = nullptr;
     int inner_cycles = 3;
-    bool fused_smoother = true;
+    bool fused_smoother = false;  // tile-fused sweep: opt-in (AFMIB_SMOOTHER=fused) until its z-march is pipelined
+    // V-cycle blocks captured once into CUDA graphs and replayed (no host
+    // interaction inside a V-cycle); not used while per-kernel profiling is on
+    bool use_graphs = true;
+    cudaGraphExec_t vg64 = nullptr, vg32 = nullptr;
+    long long vg64_launches = 0, vg32_launches = 0;
     bool spread64 = false, interp64 = false;  // mixed form: IB transfers in FP64
+    // warm start of each projection from the potential of the previous
+    // projection of the same sub-step type (0: BE, 1: CN)
+    bool warm_start = true;
+    double* phi_prev[2] = {nullptr, nullptr};
+    bool phi_valid[2] = {false, false};
+    int proj_phase = -1;  // phase of the projection in progress (-1: none)
     RedScratch red{};
     double* scal = nullptr;   // device scalars: [0..4] CG, [8] sum, [9] sumsq
     double* hscal = nullptr;  // pinned mirror
@@ -399,6 +410,78 @@ int vcycle(afmib_solver* s, size_t l) {
     return AFMIB_OK;
 }
 
+// phi for the start of a projection: the previous potential of the same
+// sub-step type, or zero
+int initial_potential(afmib_solver* s) {
+    MGLevel& L = s->lv[0];
+    const long long N = L.d.ncell();
+    const int ph = s->proj_phase;
+    if (s->warm_start && ph >= 0 && s->phi_valid[ph])
+        CK(cudaMemcpyAsync(L.x, s->phi_prev[ph], N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+    else
+        CK(cudaMemsetAsync(L.x, 0, N * sizeof(double), s->st));
+    return AFMIB_OK;
+}
+
+// Capture `body` on the solver's stream into an executable graph.
+template <typename F>
+int capture_graph(afmib_solver* s, cudaGraphExec_t* exec, long long* launches, F body) {
+    const long long l0 = s->stats.kernel_launches;
+    CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+    const int rc = body();
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s->st, &g);
+    if (rc != AFMIB_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return s->fail(AFMIB_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    const cudaError_t e2 = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e2 != cudaSuccess) return s->fail(AFMIB_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e2));
+    *launches = s->stats.kernel_launches - l0;
+    s->stats.kernel_launches = l0;  // recorded, not run
+    return AFMIB_OK;
+}
+
+void drop_graphs(afmib_solver* s) {
+    if (s->vg64) cudaGraphExecDestroy(s->vg64);
+    if (s->vg32) cudaGraphExecDestroy(s->vg32);
+    s->vg64 = s->vg32 = nullptr;
+}
+
+// one FP64 V-cycle on level 0 (graph replay when possible)
+int vcycle64_top(afmib_solver* s) {
+    if (s->prof || !s->use_graphs) return vcycle<double>(s, 0);
+    if (!s->vg64) TRY(capture_graph(s, &s->vg64, &s->vg64_launches, [&]() { return vcycle<double>(s, 0); }));
+    CK(cudaGraphLaunch(s->vg64, s->st));
+    s->stats.kernel_launches += s->vg64_launches;
+    return AFMIB_OK;
+}
+
+// the FP32 inner solve of one defect-correction step: x32 = 0, inner_cycles
+// V-cycles on L e = r, phi += e (graph replay when possible)
+int inner_vcycles32(afmib_solver* s) {
+    MGLevel& L = s->lv[0];
+    MGLevelT<float>& L32 = s->lv32[0];
+    const long long N = L.d.ncell();
+    auto body = [&]() -> int {
+        CK(cudaMemsetAsync(L32.x, 0, N * sizeof(float), s->st));
+        for (int k = 0; k < s->inner_cycles; ++k) TRY(vcycle<float>(s, 0));
+        {
+            ProfScope ps(s, P_CORRECT, (double)N * (8 + 4 + 8));
+            launch_add_correction<float>(N, L.x, L32.x, s->st);
+        }
+        CKL();
+        return AFMIB_OK;
+    };
+    if (s->prof || !s->use_graphs) return body();
+    if (!s->vg32) TRY(capture_graph(s, &s->vg32, &s->vg32_launches, body));
+    CK(cudaGraphLaunch(s->vg32, s->st));
+    s->stats.kernel_launches += s->vg32_launches;
+    return AFMIB_OK;
+}
+
 // Solve L x = b on level 0 (b in lv[0].b, destroyed; x in lv[0].x), the
 // reference's solve loop: remove the mean of b, then cycle until
 // RMS(b - L x) <= tol (src/mg/solver.h:218-237).
@@ -411,7 +494,7 @@ int mg_solve(afmib_solver* s, int* cycles) {
         launch_sum<double>(N, L.b, s->red, s->scal + 8, s->st);
         launch_sub_scalar_scaled<double>(N, L.b, s->scal + 8, 1.0 / (double)N, s->st);
     }
-    CK(cudaMemsetAsync(L.x, 0, N * sizeof(double), s->st));
+    TRY(initial_potential(s));
     CK(cudaMemsetAsync(s->dflag + 1, 0, sizeof(int), s->st));
     int status = AFMIB_OK;
     int c = 0;
@@ -430,7 +513,7 @@ int mg_solve(afmib_solver* s, int* cycles) {
             if (!std::isfinite(rms)) { status = s->fail(AFMIB_ERR_NAN, "multigrid residual is not finite"); break; }
             if (rms <= s->cfg.tol) break;
             if (c >= s->cfg.max_mg_cycles) { status = s->fail(AFMIB_ERR_NOCONV, "multigrid cycle cap reached"); break; }
-            TRY(vcycle<double>(s, 0));
+            TRY(vcycle64_top(s));
             ++c;
         }
     }
@@ -522,7 +605,7 @@ int mg_solve_mixed(afmib_solver* s, int* cycles) {
         launch_sum<double>(N, L.b, s->red, s->scal + 8, s->st);
         launch_sub_scalar_scaled<double>(N, L.b, s->scal + 8, 1.0 / (double)N, s->st);
     }
-    CK(cudaMemsetAsync(L.x, 0, N * sizeof(double), s->st));
+    TRY(initial_potential(s));
     CK(cudaMemsetAsync(s->dflag + 1, 0, sizeof(int), s->st));
     int c = 0, outer = 0;
     int status = AFMIB_OK;
@@ -538,14 +621,8 @@ int mg_solve_mixed(afmib_solver* s, int* cycles) {
         if (!std::isfinite(rms)) { status = s->fail(AFMIB_ERR_NAN, "multigrid residual is not finite"); break; }
         if (rms <= s->cfg.tol) break;
         if (c >= s->cfg.max_mg_cycles) { status = s->fail(AFMIB_ERR_NOCONV, "multigrid cycle cap reached"); break; }
-        CK(cudaMemsetAsync(L32.x, 0, N * sizeof(float), s->st));
-        for (int k = 0; k < s->inner_cycles; ++k) TRY(vcycle<float>(s, 0));
+        TRY(inner_vcycles32(s));
         c += s->inner_cycles;
-        {
-            ProfScope ps(s, P_CORRECT, (double)N * (8 + 4 + 8));
-            launch_add_correction<float>(N, L.x, L32.x, s->st);
-        }
-        CKL();
         ++outer;
     }
     CK(cudaMemcpyAsync(s->hflag + 1, s->dflag + 1, sizeof(int), cudaMemcpyDeviceToHost, s->st));
@@ -567,6 +644,11 @@ int project(afmib_solver* s) {
     CKL();
     if (s->mixed) TRY(mg_solve_mixed(s, nullptr));
     else TRY(mg_solve(s, nullptr));
+    const int ph = s->proj_phase;
+    if (s->warm_start && ph >= 0) {
+        CK(cudaMemcpyAsync(s->phi_prev[ph], s->lv[0].x, s->N() * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
+        s->phi_valid[ph] = true;
+    }
     {
         ProfScope ps(s, P_GRAD_SUB, 7 * Ns);
         launch_grad_sub<double>(s->d, s->u, s->v, s->w, s->lv[0].x, s->d.channel ? s->wallgrad : nullptr, s->st,
@@ -629,7 +711,10 @@ int substep(afmib_solver* s) {
         if (s->mixed) TRY(helm_solve_mixed(s, c, s->s_minus(), vel[c], s->rhs[c]));
         else TRY(cg_solve(s, c, s->s_minus(), vel[c], s->rhs[c], nullptr));
     }
-    TRY(project(s));
+    s->proj_phase = be ? 0 : 1;
+    const int prc = project(s);
+    s->proj_phase = -1;
+    TRY(prc);
     s->half = !s->half;
     s->stats.half = s->half ? 1 : 0;
     s->stats.substeps++;
@@ -813,7 +898,7 @@ int ib_one_step(afmib_solver* s) {
     const double dt = s->cfg.dt;
     const double* vol = s->has_vol ? s->mvol : nullptr;
     const double mbytes = (double)M * (24 + 24 + 24);
-    // precision of each transfer: FP64 form -> FP64; mixed -> FP32 unless ib_fp64 asks for FP64
+    // precision of each transfer: FP64 form -> FP64; mixed -> FP64 unless ib_fp32 asks for FP32
     const bool sp32 = s->mixed && !s->spread64;
     const bool in32 = s->mixed && !s->interp64;
     auto springs = [&](const double* P) {
@@ -976,6 +1061,11 @@ int traj_forward(afmib_solver* s, int nsteps, int every) {
     if (nsteps < 1 || every < 1) return s->fail(AFMIB_ERR_ARG, "nsteps and every must be positive");
     TRY(traj_alloc(s, nsteps, every));
     const size_t mb = 3 * (size_t)s->M * sizeof(double);
+    // cold-started projections, so that the reverse pass recomputes every
+    // segment exactly from its checkpoint
+    const bool warm = s->warm_start;
+    s->warm_start = false;
+    struct Restore { afmib_solver* s; bool w; ~Restore() { s->warm_start = w; } } restore{s, warm};
     for (int st = 0; st < nsteps; ++st) {
         if (st % every == 0) {
             TRY(copy_vel_out(s, s->ck_vel[st / every]));
@@ -1094,6 +1184,9 @@ int traj_adjoint(afmib_solver* s, const double* lu, const double* lv, const doub
     TRY(copy_in(s, L + 2 * N, lw, N));
     TRY(copy_in(s, s->lamX, lX, 3 * (long long)M));
     double lam_k = 0.0;
+    const bool warm = s->warm_start;
+    s->warm_start = false;
+    struct Restore { afmib_solver* s; bool w; ~Restore() { s->warm_start = w; } } restore{s, warm};
     const int nseg = (s->traj_steps + s->traj_every - 1) / s->traj_every;
     const bool half_saved = s->half;
     for (int sg = nseg - 1; sg >= 0; --sg) {
@@ -1157,9 +1250,11 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (g.bc != AFMIB_BC_PERIODIC && g.bc != AFMIB_BC_CHANNEL) return s->fail(AFMIB_ERR_ARG, "bc must be periodic or channel");
     if (g.precision != AFMIB_FP64 && g.precision != AFMIB_MIXED) return s->fail(AFMIB_ERR_ARG, "precision");
     s->mixed = g.precision == AFMIB_MIXED;
-    s->spread64 = s->mixed && (g.ib_fp64 & 1);
-    s->interp64 = s->mixed && (g.ib_fp64 & 2);
-    if (const char* e = std::getenv("AFMIB_SMOOTHER")) s->fused_smoother = std::string(e) != "percolour";
+    s->spread64 = s->mixed && !(g.ib_fp32 & 1);
+    s->interp64 = s->mixed && !(g.ib_fp32 & 2);
+    if (const char* e = std::getenv("AFMIB_SMOOTHER")) s->fused_smoother = std::string(e) == "fused";
+    if (const char* e = std::getenv("AFMIB_GRAPHS")) s->use_graphs = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_WARM")) s->warm_start = std::string(e) != "0";
     if (!(g.rho > 0) || !(g.dt > 0) || !(g.mu >= 0) || !(g.tol > 0)) return s->fail(AFMIB_ERR_ARG, "mu, rho, dt, tol");
     s->d = Dims{g.nx, g.ny, g.nz, g.n, g.bc == AFMIB_BC_CHANNEL ? 1 : 0};
     if (stream) {
@@ -1180,6 +1275,8 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
         TRY(dalloc(s, &s->tmp[k], N));
     }
     TRY(dalloc(s, &s->divb, N));
+    TRY(dalloc(s, &s->phi_prev[0], N));
+    TRY(dalloc(s, &s->phi_prev[1], N));
     TRY(dalloc(s, &s->walls, 4 * s->nxz()));
     TRY(dalloc(s, &s->wallgrad, 6 * s->nxz()));
     TRY(dalloc(s, &s->cg_r, N));
@@ -1313,6 +1410,7 @@ int afmib_destroy(afmib_solver* s) {
     if (s->st) cudaStreamSynchronize(s->st);
     for (void* p : s->allocs)
         if (p) cudaFree(p);
+    drop_graphs(s);
     for (auto& p : s->prof_pend) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     for (auto e : s->prof_pool) cudaEventDestroy(e);
     if (s->hscal) cudaFreeHost(s->hscal);
@@ -1340,6 +1438,7 @@ int afmib_set_velocity(afmib_solver* s, const double* u, const double* v, const 
     else CK(cudaMemsetAsync(s->v, 0, s->N() * sizeof(double), s->st));
     TRY(copy_in(s, s->w, w, s->N()));
     TRY(refresh_shadow(s));
+    s->phi_valid[0] = s->phi_valid[1] = false;  // a new state: no warm start
     return sync(s);
 }
 
@@ -1622,6 +1721,7 @@ int afmib_interp(afmib_solver* s, int M, const double* X, const double* u, const
 
 int afmib_set_tolerance(afmib_solver* s, double tol) {
     if (!s || !(tol > 0)) return AFMIB_ERR_ARG;
+    if (tol != s->cfg.tol) drop_graphs(s);  // the coarsest solve's tolerance is baked into the graphs
     s->cfg.tol = tol;
     return AFMIB_OK;
 }

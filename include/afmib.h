@@ -59,7 +59,8 @@ typedef struct afmib_config {
     int max_mg_cycles;  /* 0 -> 200 */
     double k_spring;    /* linear spring stiffness of the membrane */
     double inner_tol;   /* mixed precision: relative reduction per FP32 inner solve, 0 -> 1e-5 */
-    int ib_fp64;        /* mixed precision: bit 0 spreads, bit 1 interpolates in FP64 (0: both FP32) */
+    int ib_fp32;        /* mixed precision: bit 0 spreads, bit 1 interpolates in FP32 (0: both FP64, the
+                           default, which keeps the velocity within 1e-8 of the FP64 form) */
 } afmib_config;
 
 typedef struct afmib_stats {

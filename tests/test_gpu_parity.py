@@ -297,3 +297,24 @@ def test_mixed_ib_steps_periodic():
     assert rel(gu, ru) < MIXED_TOL and rel(gv, rv) < MIXED_TOL and rel(gw, rw) < MIXED_TOL
     assert rel(Xg - X, Xr - X) < 1e-6
     assert np.max(np.abs(Xg - Xr)) < 1e-12
+
+
+def test_mixed_fp32_transfers_run():
+    """FP32 spreading and interpolation inside the mixed form (ib_fp32=3) run
+    and stay within 1e-6 of the FP64 oracle; the default FP64 transfers are
+    the ones held to 1e-8 above."""
+    n = 32
+    g, u, v, w, X, nstart, nidx = _periodic_case(n, M=2000)
+    mu, rho, dt, tol, k = 0.005, 1.0, 2e-5, 1e-12, 0.5
+    ref = po.NSSolver(g, mu, rho, dt, tol, u, v, w)
+    Xr = X.copy()
+    for _ in range(2):
+        Xr, st = ref.ib_step(Xr, nstart, nidx, k)
+    ru, rv, rw, _ = ref.get()
+    with capi.Solver(n, precision=capi.MIXED, mu=mu, rho=rho, dt=dt, tol=tol, k_spring=k, ib_fp32=3) as sv:
+        sv.set_velocity(u, v, w)
+        sv.project()
+        sv.set_markers(X, nstart, nidx)
+        sv.ib_step(2)
+        gu, gv, gw = sv.get_velocity()
+    assert rel(gu, ru) < 1e-6 and rel(gv, rv) < 1e-6 and rel(gw, rw) < 1e-6
