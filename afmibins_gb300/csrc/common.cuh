@@ -50,7 +50,7 @@ __device__ __forceinline__ int zp1(const Dims& d, int z) { return z == d.nz - 1 
 // ticket; the ticket is left at zero for the next launch.
 // ---------------------------------------------------------------------------
 constexpr int kRedBlock = 256;
-constexpr int kMaxRedBlocks = 2048;
+constexpr int kMaxRedBlocks = 8192;
 
 struct RedScratch {
     double* partial;     // [kMaxRedBlocks * kMaxRedVals]
@@ -130,11 +130,16 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], RedScratch sc, double*
 
 // Stencil reductions run on (32 x 8)-thread blocks over (x, y) tiles with
 // each thread walking z in steps of grid.z, so that no linear index is ever
-// divided; grid.z is chosen to keep the block count within kMaxRedBlocks.
+// divided; grid.z is chosen for about kRedWaveBlocks blocks, at most
+// kMaxRedBlocks.
 constexpr int kRBX = 32, kRBY = 8;
+// Blocks per grid: about four full waves of the 152 SMs at eight resident
+// 256-thread blocks each, so that the last wave is not a fraction.
+constexpr int kRedWaveBlocks = 152 * 8 * 4;
 inline dim3 red_grid3(int nx, int ny, int nz) {
     const int gx = (nx + kRBX - 1) / kRBX, gy = (ny + kRBY - 1) / kRBY;
-    int gz = kMaxRedBlocks / (gx * gy);
+    int gz = (kRedWaveBlocks + gx * gy - 1) / (gx * gy);
+    if (gz * gx * gy > kMaxRedBlocks) gz = kMaxRedBlocks / (gx * gy);
     if (gz > nz) gz = nz;
     if (gz < 1) gz = 1;
     return dim3(gx, gy, gz);
@@ -150,7 +155,7 @@ struct Acc {
 
 inline int red_blocks(long long n) {
     long long b = (n + kRedBlock - 1) / kRedBlock;
-    if (b > kMaxRedBlocks) b = kMaxRedBlocks;
+    if (b > kRedWaveBlocks) b = kRedWaveBlocks;
     if (b < 1) b = 1;
     return (int)b;
 }

@@ -161,30 +161,35 @@ __global__ void k_wall_update(Dims d, double* __restrict__ walls, const double* 
 // periodic mode) carry the one-sided Dirichlet closure at the channel walls,
 // src/ns/helmholtz.h:90-104; v rows in channel mode treat the walls as zero
 // neighbours (plane 0 and its periodic image), src/ns/helmholtz.h:247-248.
-template <typename T>
-__device__ __forceinline__ T helm_point(const Dims& d, int comp, T s, const T* __restrict__ x, int xi, int yi, int zi) {
+template <typename T, typename Get>
+__device__ __forceinline__ T helm_point_at(const Dims& d, int comp, T s, Get x, int xi, int yi, int zi) {
     const long long i = lin(d, xi, yi, zi);
     const T off = s * T(d.n) * T(d.n);
-    const T x0 = x[i];
-    const T sx = x[lin(d, xm1(d, xi), yi, zi)] + x[lin(d, xp1(d, xi), yi, zi)];
-    const T sz = x[lin(d, xi, yi, zm1(d, zi))] + x[lin(d, xi, yi, zp1(d, zi))];
+    const T x0 = x(i);
+    const T sx = x(lin(d, xm1(d, xi), yi, zi)) + x(lin(d, xp1(d, xi), yi, zi));
+    const T sz = x(lin(d, xi, yi, zm1(d, zi))) + x(lin(d, xi, yi, zp1(d, zi)));
     if (d.channel && comp != 1) {
         T diag = T(1) - T(6) * off;
         T sy;
         if (yi == 0) {
             diag -= T(2) * off;
-            sy = (off + off / T(3)) * x[lin(d, xi, 1, zi)];
+            sy = (off + off / T(3)) * x(lin(d, xi, 1, zi));
         } else if (yi == d.ny - 1) {
             diag -= T(2) * off;
-            sy = (off + off / T(3)) * x[lin(d, xi, yi - 1, zi)];
+            sy = (off + off / T(3)) * x(lin(d, xi, yi - 1, zi));
         } else {
-            sy = off * (x[lin(d, xi, yi - 1, zi)] + x[lin(d, xi, yi + 1, zi)]);
+            sy = off * (x(lin(d, xi, yi - 1, zi)) + x(lin(d, xi, yi + 1, zi)));
         }
         return diag * x0 + (off * (sx + sz) + sy);
     }
     if (d.channel && comp == 1 && yi == 0) return x0;
-    const T sy = x[lin(d, xi, ym1(d, yi), zi)] + x[lin(d, xi, yp1(d, yi), zi)];
+    const T sy = x(lin(d, xi, ym1(d, yi), zi)) + x(lin(d, xi, yp1(d, yi), zi));
     return (T(1) - T(6) * off) * x0 + off * (sx + sy + sz);
+}
+
+template <typename T>
+__device__ __forceinline__ T helm_point(const Dims& d, int comp, T s, const T* __restrict__ x, int xi, int yi, int zi) {
+    return helm_point_at(d, comp, s, [x](long long i) { return x[i]; }, xi, yi, zi);
 }
 
 template <typename T>
@@ -230,6 +235,7 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_init(Dims d, int comp, T s, co
     const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
     T acc = T(0);
     if (xi < d.nx && yi < d.ny)
+#pragma unroll 2
         for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
             const long long i = lin(d, xi, yi, zi);
             const T ri = b[i] - helm_point(d, comp, s, x, xi, yi, zi);
@@ -247,6 +253,7 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_apply(Dims d, int comp, T s, c
     const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
     T acc = T(0);
     if (xi < d.nx && yi < d.ny)
+#pragma unroll 2
         for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
             const long long i = lin(d, xi, yi, zi);
             const T qi = helm_point(d, comp, s, p, xi, yi, zi);
@@ -276,6 +283,31 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update(long long N, T* __restr
     }
 }
 
+// Direction update fused into the next operator apply (FP32 inner solves):
+// p' = beta p + r is formed on the fly at the seven stencil points, written
+// out of place to pn, and q = H p' with p'.q reduced; alpha in the finisher.
+template <typename T>
+__global__ void __launch_bounds__(kRedBlock) k_cg_dir_apply(Dims d, int comp, T s, const T* __restrict__ p,
+                                                           const T* __restrict__ r, T* __restrict__ pn,
+                                                           T* __restrict__ q, RedScratch sc, double* cgs) {
+    const T beta = T(cgs[3]);
+    auto P = [p, r, beta](long long i) { return p[i] * beta + r[i]; };
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+    T acc = T(0);
+    if (xi < d.nx && yi < d.ny)
+#pragma unroll 2
+        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
+            const long long i = lin(d, xi, yi, zi);
+            const T pi = P(i);
+            const T qi = helm_point_at(d, comp, s, P, xi, yi, zi);
+            pn[i] = pi;
+            q[i] = qi;
+            acc += pi * qi;
+        }
+    double a[1] = {(double)acc};
+    if (grid_sum<1>(a, sc, cgs + 1)) cgs[4] = cgs[0] / a[0];
+}
+
 template <typename T>
 __global__ void k_cg_direction(long long N, T* __restrict__ p, const T* __restrict__ r, const double* cgs) {
     const T beta = T(cgs[3]);
@@ -295,6 +327,7 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_defect(Dims d, int comp, dou
     const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
     TD acc = TD(0);
     if (xi < d.nx && yi < d.ny)
+#pragma unroll 2
         for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
             const long long i = lin(d, xi, yi, zi);
             const TD ri = TD(b[i] - helm_point(d, comp, s, x, xi, yi, zi));
@@ -428,6 +461,11 @@ void launch_cg_apply(const Dims& d, int comp, double scale, const T* p, T* q, Re
     k_cg_apply<T><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, T(scale), p, q, sc, cgs);
 }
 template <typename T>
+void launch_cg_dir_apply(const Dims& d, int comp, double scale, const T* p, const T* r, T* pn, T* q, RedScratch sc,
+                         double* cgs, cudaStream_t s) {
+    k_cg_dir_apply<T><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, T(scale), p, r, pn, q, sc, cgs);
+}
+template <typename T>
 void launch_cg_update(long long n, T* x, T* r, const T* p, const T* q, RedScratch sc, double* cgs, cudaStream_t s) {
     k_cg_update<T><<<red_blocks(n), kRedBlock, 0, s>>>(n, x, r, p, q, sc, cgs);
 }
@@ -495,6 +533,8 @@ template void launch_helm_rhs<double, double, float>(const Dims&, int, int, doub
                                                      double, double, cudaStream_t);
 template void launch_helm_defect<float>(const Dims&, int, double, const double*, const double*, float*, RedScratch,
                                         double*, cudaStream_t);
+template void launch_cg_dir_apply<float>(const Dims&, int, double, const float*, const float*, float*, float*,
+                                         RedScratch, double*, cudaStream_t);
 template void launch_cg_init_zero<float>(long long, const float*, float*, float*, float*, RedScratch, double*,
                                          cudaStream_t);
 template void launch_add_correction<float>(long long, double*, const float*, cudaStream_t);

@@ -272,8 +272,8 @@ __global__ void __launch_bounds__(TS * TS * TS) k_spread_gather(Dims d, int M, c
     int* s_scan = s_seg + NSEG;          // NT
     int* s_k = s_scan + NT;              // cap: marker index of each staged slot
     int* s_base = s_k + cap;             // cap: packed E-local first faces
-    T* s_w = (T*)(((uintptr_t)(s_base + cap) + 15) & ~(uintptr_t)15);  // cap * 12
-    T* s_g = s_w + (size_t)cap * 12;     // cap
+    // cap * 12: x weights, y weights, z weights times the marker's force
+    T* s_w = (T*)(((uintptr_t)(s_base + cap) + 15) & ~(uintptr_t)15);
 
     const int ntx = d.nx / TS, nty = d.ny / TS, ntz = d.nz / TS;
     const int ncount = *count;
@@ -362,6 +362,7 @@ __global__ void __launch_bounds__(TS * TS * TS) k_spread_gather(Dims d, int M, c
         for (int comp = 0; comp < 3; ++comp) {
             for (int sl = tid; sl < nc; sl += NT) {
                 const int k = s_k[sl];
+                const T g = T((double)G[(size_t)comp * M + k] * (vol ? vol[k] : 1.0) * scale);
                 int packed = 0;
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
@@ -375,10 +376,9 @@ __global__ void __launch_bounds__(TS * TS * TS) k_spread_gather(Dims d, int M, c
                     packed |= (b + 8) << (8 * a);
                     const T* w = mw.w + (((size_t)k * 3 + a) * 2 + v) * 4;
 #pragma unroll
-                    for (int m = 0; m < 4; ++m) s_w[(size_t)sl * 12 + a * 4 + m] = w[m];
+                    for (int m = 0; m < 4; ++m) s_w[(size_t)sl * 12 + a * 4 + m] = a == 2 ? w[m] * g : w[m];
                 }
                 s_base[sl] = packed;
-                s_g[sl] = T((double)G[(size_t)comp * M + k] * (vol ? vol[k] : 1.0) * scale);
             }
             __syncthreads();
             T* f = comp == 0 ? fu : (comp == 1 ? fv : fw);
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(TS * TS * TS) k_spread_gather(Dims d, int M, c
                         const int mz = J[2] - (((pk >> 16) & 255) - 8);
                         if ((unsigned)mx < 4u && (unsigned)my < 4u && (unsigned)mz < 4u) {
                             const T* w = s_w + (size_t)sl * 12;
-                            acc += w[mx] * w[4 + my] * w[8 + mz] * s_g[sl];
+                            acc += (w[mx] * w[4 + my]) * w[8 + mz];
                         }
                     }
                 }
@@ -517,7 +517,7 @@ size_t spread_smem_bytes(int TS, int cap) {
     size_t ints = (size_t)(E3 + 1) + 3 * E * E + NT + 2 * (size_t)cap;
     size_t bytes = ints * sizeof(int);
     bytes = (bytes + 15) & ~(size_t)15;
-    bytes += (size_t)cap * 13 * sizeof(T);
+    bytes += (size_t)cap * 12 * sizeof(T);
     return bytes;
 }
 

@@ -55,6 +55,7 @@ __global__ void __launch_bounds__(kRedBlock) k_residual_norm(Dims d, T* __restri
     const T off = T(d.n) * T(d.n);
     T acc = T(0);
     if (xi < d.nx && yi < d.ny)
+#pragma unroll 2
         for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
             T S, c;
             lap_row(d, xv, xi, yi, zi, S, c);
@@ -76,6 +77,7 @@ __global__ void __launch_bounds__(kRedBlock) k_lap_defect(Dims d, TD* __restrict
     const double off = double(d.n) * double(d.n);
     TD acc = TD(0);
     if (xi < d.nx && yi < d.ny)
+#pragma unroll 2
         for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
             double S, c;
             lap_row(d, xv, xi, yi, zi, S, c);

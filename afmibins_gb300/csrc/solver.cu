@@ -53,7 +53,7 @@ struct afmib_solver {
     bool mixed = false;
     float *adv32[3] = {}, *f32[3] = {}, *d32 = nullptr, *e32 = nullptr;
     float *u32 = nullptr, *v32 = nullptr, *w32 = nullptr;  // FP32 shadow of the velocity
-    float *cg32_r = nullptr, *cg32_p = nullptr, *cg32_q = nullptr;
+    float *cg32_r = nullptr, *cg32_p = nullptr, *cg32_q = nullptr, *cg32_p2 = nullptr;
     std::vector<MGLevelT<float>> lv32;
     double *cx64 = nullptr, *cb64 = nullptr, *cr64 = nullptr;
     int inner_cycles = 3;
@@ -65,8 +65,9 @@ struct afmib_solver {
     long long vg64_launches = 0, vg32_launches = 0;
     bool spread64 = false, interp64 = false;  // mixed form: IB transfers in FP64
     // warm start of each projection from the potential of the previous
-    // projection of the same sub-step type (0: BE, 1: CN)
-    bool warm_start = true;
+    // projection of the same sub-step type (0: BE, 1: CN); off in the FP64
+    // form unless asked for, which keeps the reference's start from zero
+    bool warm_start = false;
     double* phi_prev[2] = {nullptr, nullptr};
     bool phi_valid[2] = {false, false};
     int proj_phase = -1;  // phase of the projection in progress (-1: none)
@@ -207,14 +208,14 @@ enum ProfId {
     P_ADVECT, P_HELM_RHS, P_CG_INIT, P_CG_APPLY, P_CG_UPDATE, P_CG_DIR, P_RBGS, P_RESID, P_RESID_NORM,
     P_RESTRICT, P_PROLONG, P_COARSE, P_DIV, P_GRAD_SUB, P_MEAN, P_WALL, P_SPRINGS, P_PREP, P_SORT,
     P_TILES, P_SPREAD, P_INTERP, P_MARKER, P_HELM_DEFECT, P_LAP_DEFECT, P_CORRECT, P_ADJ_ADVECT, P_ADJ_MARKER,
-    P_RBGS0, P_RESID0, P_RESTRICT0, P_PROLONG0, P_COUNT
+    P_RBGS0, P_RESID0, P_RESTRICT0, P_PROLONG0, P_CG_DIRAPPLY, P_COUNT
 };
 const char* kProfNames[P_COUNT] = {
     "advect", "helm_rhs", "cg_init", "cg_apply", "cg_update", "cg_direction", "mg_rbgs", "mg_residual",
     "mg_residual_norm", "mg_restrict", "mg_prolong_add", "mg_coarse_cg", "div", "grad_sub", "mean_removal",
     "wall_update", "springs", "marker_prep", "radix_sort", "tile_bins", "spread_gather", "interp", "marker_update",
     "helm_defect_fp64", "lap_defect_fp64", "add_correction_fp64", "advect_adjoint", "marker_adjoint",
-    "mg_rbgs_fine", "mg_residual_fine", "mg_restrict_fine", "mg_prolong_add_fine"};
+    "mg_rbgs_fine", "mg_residual_fine", "mg_restrict_fine", "mg_prolong_add_fine", "cg_dir_apply"};
 
 cudaEvent_t prof_event(afmib_solver* s) {
     if (!s->prof_pool.empty()) {
@@ -544,21 +545,25 @@ int cg_inner32(afmib_solver* s, int comp, double scale, double rel_tol, int* ite
     TRY(read_scalars(s, 0, 1));
     const double stop = rel_tol * std::sqrt(s->hscal[0]);
     int it = 0;
+    // the direction update of iteration k is folded into the apply of k+1
+    // (p and cg32_p2 alternate)
+    float* p = s->cg32_p;
+    float* pn = s->cg32_p2;
     while (std::sqrt(s->hscal[0]) > stop && it < s->cfg.max_cg_iters) {
         if (!std::isfinite(s->hscal[0])) return s->fail(AFMIB_ERR_NAN, "inner CG residual is not finite");
-        {
+        if (it == 0) {
             ProfScope ps(s, P_CG_APPLY, 2 * Ns);
-            launch_cg_apply<float>(d, comp, scale, s->cg32_p, s->cg32_q, s->red, s->scal, s->st);
+            launch_cg_apply<float>(d, comp, scale, p, s->cg32_q, s->red, s->scal, s->st);
+        } else {
+            ProfScope ps(s, P_CG_DIRAPPLY, 4 * Ns);
+            launch_cg_dir_apply<float>(d, comp, scale, p, s->cg32_r, pn, s->cg32_q, s->red, s->scal, s->st);
+            std::swap(p, pn);
         }
         {
             ProfScope ps(s, P_CG_UPDATE, 6 * Ns);
-            launch_cg_update<float>(N, s->e32, s->cg32_r, s->cg32_p, s->cg32_q, s->red, s->scal, s->st);
+            launch_cg_update<float>(N, s->e32, s->cg32_r, p, s->cg32_q, s->red, s->scal, s->st);
         }
         CK(cudaMemcpyAsync(s->hscal, s->scal, sizeof(double), cudaMemcpyDeviceToHost, s->st));
-        {
-            ProfScope ps(s, P_CG_DIR, 3 * Ns);
-            launch_cg_direction<float>(N, s->cg32_p, s->cg32_r, s->scal, s->st);
-        }
         CKL();
         TRY(sync(s));
         ++it;
@@ -1254,7 +1259,9 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     s->interp64 = s->mixed && !(g.ib_fp32 & 2);
     if (const char* e = std::getenv("AFMIB_SMOOTHER")) s->fused_smoother = std::string(e) == "fused";
     if (const char* e = std::getenv("AFMIB_GRAPHS")) s->use_graphs = std::string(e) != "0";
-    if (const char* e = std::getenv("AFMIB_WARM")) s->warm_start = std::string(e) != "0";
+    if (g.proj_start < AFMIB_START_DEFAULT || g.proj_start > AFMIB_START_WARM)
+        return s->fail(AFMIB_ERR_ARG, "proj_start must be AFMIB_START_DEFAULT, _ZERO or _WARM");
+    s->warm_start = g.proj_start == AFMIB_START_WARM || (g.proj_start == AFMIB_START_DEFAULT && s->mixed);
     if (!(g.rho > 0) || !(g.dt > 0) || !(g.mu >= 0) || !(g.tol > 0)) return s->fail(AFMIB_ERR_ARG, "mu, rho, dt, tol");
     s->d = Dims{g.nx, g.ny, g.nz, g.n, g.bc == AFMIB_BC_CHANNEL ? 1 : 0};
     if (stream) {
@@ -1348,6 +1355,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
         TRY(dalloc(s, &s->cg32_r, N));
         TRY(dalloc(s, &s->cg32_p, N));
         TRY(dalloc(s, &s->cg32_q, N));
+        TRY(dalloc(s, &s->cg32_p2, N));
         for (const MGLevel& L : s->lv) {
             MGLevelT<float> F{L.d, nullptr, nullptr, nullptr, nullptr};
             TRY(dalloc(s, &F.x, L.d.ncell()));

@@ -194,12 +194,12 @@ def pressure_err(p, pref, n, mu, dt):
     return float(np.max(np.abs(dp - dp.mean())) / max(np.max(np.abs(pref - pref.mean())), 1e-300))
 
 
-def run_form(capi, torch, args, prec, state, dev, stream, timed=True):
+def run_form(capi, torch, args, prec, state, dev, stream, proj_start=0):
     """Create a solver of the given precision on the initial state, run the
     warm-up and the timed steps; return (solver, ms, launches, clocks, wall)."""
     X, nstart, nidx, u, v, w = state
     sv = capi.Solver(args.n, mu=args.mu, rho=1.0, dt=args.dt, tol=args.tol, k_spring=0.5, precision=prec,
-                     stream=stream.cuda_stream)
+                     proj_start=proj_start, stream=stream.cuda_stream)
     ud, vd, wd = (torch.from_numpy(a).to(dev) for a in (u, v, w))
     Xd = torch.from_numpy(X).to(dev)
     torch.cuda.synchronize()
@@ -262,17 +262,26 @@ def main():
         return float(t.item())
 
     # ---- the FP64 form (the drop-in) from the same initial state, for the
-    #      speed-up and the error of the mixed form
-    fp64 = None
+    #      speed-up and the error of the mixed form: once with the reference's
+    #      projections from zero (the parity configuration, the error
+    #      baseline), once warm-started like the mixed form (the speed-up is
+    #      quoted against the faster of the two)
+    fp64 = fp64w = None
     if headline == capi.MIXED and not args.no_fp64:
         barrier()
-        sv64, ms64, l64, clk64, _ = run_form(capi, torch, args, capi.FP64, state, dev, stream)
+        sv64, ms64, l64, clk64, _ = run_form(capi, torch, args, capi.FP64, state, dev, stream, capi.START_ZERO)
         ms64 = max_over_ranks(ms64)
         u64 = sv64.get_velocity()
         p64 = sv64.get_pressure()
         X64 = sv64.get_markers()
         fp64 = {"value": world * args.steps / (ms64 / 1000.0), "ms_per_step": ms64 / args.steps,
-                "gpu_launches": int(l64)}
+                "gpu_launches": int(l64), "proj_start": "zero (the reference's)"}
+        sv64.close()
+        barrier()
+        sv64, ms64w, l64w, _, _ = run_form(capi, torch, args, capi.FP64, state, dev, stream, capi.START_WARM)
+        ms64w = max_over_ranks(ms64w)
+        fp64w = {"value": world * args.steps / (ms64w / 1000.0), "ms_per_step": ms64w / args.steps,
+                 "gpu_launches": int(l64w), "proj_start": "warm"}
         sv64.close()
 
     # ---- headline form: timed region with the state resident in HBM
@@ -293,6 +302,7 @@ def main():
                   "marker_position_max_abs": float(np.max(np.abs(Xh - X64))),
                   "steps": args.warmup + args.steps}
         fp64["speedup_of_headline"] = value / fp64["value"]
+        fp64w["speedup_of_headline"] = value / fp64w["value"]
 
     # ---- e2e through the C ABI with host buffers
     e2e = None
@@ -351,7 +361,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if headline == capi.FP64 else "f32+f64",
             "data": "synthetic (seeded shells and solenoidal field)", "config": config_dict(args),
             "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clocks,
-            "fp64_form": fp64, "errors_vs_fp64": errors,
+            "fp64_form": fp64, "fp64_form_warm": fp64w, "errors_vs_fp64": errors,
             "solver": {"cg_iters_per_step": st["cg_iters"] / max(1, st["ib_steps"]),
                        "mg_cycles_per_step": st["mg_cycles"] / max(1, st["ib_steps"]),
                        "outer_iters_per_step": st["outer_iters"] / max(1, st["ib_steps"]),

@@ -61,7 +61,13 @@ typedef struct afmib_config {
     double inner_tol;   /* mixed precision: relative reduction per FP32 inner solve, 0 -> 1e-5 */
     int ib_fp32;        /* mixed precision: bit 0 spreads, bit 1 interpolates in FP32 (0: both FP64, the
                            default, which keeps the velocity within 1e-8 of the FP64 form) */
+    int proj_start;     /* initial pressure of each projection: AFMIB_START_DEFAULT (FP64: from zero, the
+                           reference's nested iteration, src/mg/solver.h:201-216; mixed: warm),
+                           AFMIB_START_ZERO, or AFMIB_START_WARM (the previous pressure of the same
+                           sub-step kind, BE or CN) */
 } afmib_config;
+
+enum { AFMIB_START_DEFAULT = 0, AFMIB_START_ZERO = 1, AFMIB_START_WARM = 2 };
 
 typedef struct afmib_stats {
     long long substeps;   /* ns sub-steps taken (BE and CN each count one) */
@@ -177,7 +183,7 @@ int afmib_interp(afmib_solver* s, int M, const double* X, const double* u, const
  * implicit synchronisation of an allocation. Same solve and stopping rule as
  * afmib_helmholtz_cg, on the caller's device buffers x (warm start, solution)
  * and b; its working vectors live in an array the library reserves on every
- * GPU (about 6.4 MB) for as long as it is loaded. Limit: nx*ny*nz <= 64^3
+ * GPU (about 6.5 MB) for as long as it is loaded. Limit: nx*ny*nz <= 64^3
  * (larger -> AFMIB_ERR_CAPACITY); periodic, or channel components 0 and 2.
  * The first call on a device looks up the array's address: make it before any
  * stream capture. Calls that overlap on the GPU share the array and race. */

@@ -1,6 +1,9 @@
 """CPU-side checks of the C-ABI boundary: the library builds, loads and
 exports every entry point that include/afmib.h declares. No compute calls."""
 import ctypes
+import os
+import shutil
+import subprocess
 
 import pytest
 
@@ -26,9 +29,22 @@ def test_error_strings_without_gpu():
     assert lib.afmib_error_string(99) == b"unknown status"
 
 
-def test_config_layout_matches_header():
-    # the ctypes mirror must agree with the C struct: 9 ints (+pad), 4 doubles, 2 ints, 2 doubles, 1 int (+pad)
-    assert ctypes.sizeof(capi.Config) == 9 * 4 + 4 + 4 * 8 + 2 * 4 + 2 * 8 + 8
+def test_config_layout_matches_header(tmp_path):
+    """The ctypes mirror agrees with the C struct field by field: a C program
+    compiled against include/afmib.h prints sizeof and every offsetof."""
+    fields = [f[0] for f in capi.Config._fields_]
+    src = tmp_path / "layout.c"
+    body = "".join(f'    printf("%zu\\n", offsetof(afmib_config, {f}));\n' for f in fields)
+    src.write_text("#include <stddef.h>\n#include <stdio.h>\n#include \"afmib.h\"\nint main(void) {\n"
+                   '    printf("%zu\\n", sizeof(afmib_config));\n' + body + "    return 0;\n}\n")
+    exe = tmp_path / "layout"
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(build.ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert out[0] == ctypes.sizeof(capi.Config)
+    assert out[1:] == [getattr(capi.Config, f).offset for f in fields]
 
 
 def test_build_is_in_tree():

@@ -104,6 +104,32 @@ def test_ns_substeps_channel(golden):
     assert rel(walls, d["walls"]) < TOL
 
 
+def test_ns_substeps_channel_warm_start(golden):
+    """FP64 form with warm-started projections (AFMIB_START_WARM): each
+    projection starts from the previous pressure of its sub-step kind instead
+    of the reference's nested iteration from zero, so the pressure converges
+    to another point inside the same RMS tolerance. Velocity stays within
+    1e-10 of the reference; pressure within 1e-9 (ten times the solver's
+    tolerance, relative)."""
+    d = golden("ns_16")
+    with capi.Solver(16, bc=capi.BC_CHANNEL, mu=float(d["mu"]), rho=float(d["rho"]), dt=float(d["dt"]),
+                     tol=float(d["tol"]), proj_start=capi.START_WARM) as sv:
+        sv.set_velocity(d["u0"], d["v0"], d["w0"])
+        sv.project()
+        for _ in range(int(d["substeps"])):
+            sv.ns_step(d["fx"], d["fy"], d["fz"])
+        u, v, w = sv.get_velocity()
+        p = sv.get_pressure()
+    assert rel(u, d["u"]) < TOL and rel(v, d["v"]) < TOL and rel(w, d["w"]) < TOL
+    g = po.Grid(16, 16, 16, 16, channel=True)
+    assert pressure_rel(p, d["p"], g, float(d["mu"]), float(d["rho"]), float(d["dt"])) < 1e-9
+
+
+def test_proj_start_rejected():
+    with pytest.raises(capi.AfmibError):
+        capi.Solver(8, proj_start=3)
+
+
 def test_spread_interp_channel(golden):
     d = golden("ib_16")
     with capi.Solver(16, bc=capi.BC_CHANNEL) as sv:
