@@ -351,7 +351,7 @@ class Solver:
         return x, it.value
 
     def restrict(self, fine):
-        c = np.zeros(self.ncell // 8)
+        c = np.zeros(self.ncell // (4 if self.nz == 1 else 8))
         self._ck(self.lib.afmib_restrict(self.h, ptr(c), ptr(_f64(fine))))
         return c
 

@@ -167,6 +167,12 @@ __device__ __forceinline__ T helm_point_at(const Dims& d, int comp, T s, Get x, 
     const T off = s * T(d.n) * T(d.n);
     const T x0 = x(i);
     const T sx = x(lin(d, xm1(d, xi), yi, zi)) + x(lin(d, xp1(d, xi), yi, zi));
+    if (d.nz == 1) {
+        // 2D (periodic): the one-cell z extent folds into the diagonal,
+        // src/ns/helmholtz.h:77-88
+        const T sy = x(lin(d, xi, ym1(d, yi), zi)) + x(lin(d, xi, yp1(d, yi), zi));
+        return (T(1) - T(4) * off) * x0 + off * (sx + sy);
+    }
     const T sz = x(lin(d, xi, yi, zm1(d, zi))) + x(lin(d, xi, yi, zp1(d, zi)));
     if (d.channel && comp != 1) {
         T diag = T(1) - T(6) * off;

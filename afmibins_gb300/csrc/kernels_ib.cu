@@ -61,6 +61,7 @@ __global__ void k_marker_prep(Dims d, int TS, int M, const double* __restrict__ 
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= M) return;
     const int ext[3] = {d.nx, d.ny, d.nz};
+    const int TZ = d.nz == 1 ? 1 : TS;  // 2D grids: tiles one cell deep
     int cell[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -69,6 +70,18 @@ __global__ void k_marker_prep(Dims d, int TS, int M, const double* __restrict__ 
         cell[a] = wrapi((int)fs, ext[a]);
         if (a == 1 && d.channel && (s < 2.5 || s > d.ny - 2.5)) atomicExch(flag, 1);
         if (!(s == s)) atomicExch(flag, 2);
+        if (a == 2 && d.nz == 1) {
+            // 2D: the z kernel is the single plane with weight one
+            cell[2] = 0;
+#pragma unroll
+            for (int v = 0; v < 2; ++v) {
+                mw.dbase[(k * 3 + a) * 2 + v] = 0;
+                T* w = mw.w + (((size_t)k * 3 + a) * 2 + v) * 4;
+                w[0] = T(1);
+                w[1] = w[2] = w[3] = T(0);
+            }
+            continue;
+        }
 #pragma unroll
         for (int v = 0; v < 2; ++v) {
             const double t = s - 0.5 * v;
@@ -87,11 +100,11 @@ __global__ void k_marker_prep(Dims d, int TS, int M, const double* __restrict__ 
     mw.cell[3 * k] = cell[0];
     mw.cell[3 * k + 1] = cell[1];
     mw.cell[3 * k + 2] = cell[2];
-    const int tx = cell[0] / TS, ty = cell[1] / TS, tz = cell[2] / TS;
+    const int tx = cell[0] / TS, ty = cell[1] / TS, tz = cell[2] / TZ;
     const int ntx = d.nx / TS, nty = d.ny / TS;
     const unsigned tile = (unsigned)(tx + ntx * (ty + nty * tz));
-    const unsigned local = (unsigned)((cell[0] % TS) + TS * ((cell[1] % TS) + TS * (cell[2] % TS)));
-    if (keys) keys[k] = tile * (unsigned)(TS * TS * TS) + local;  // null: weights only
+    const unsigned local = (unsigned)((cell[0] % TS) + TS * ((cell[1] % TS) + TS * (cell[2] % TZ)));
+    if (keys) keys[k] = tile * (unsigned)(TS * TS * TZ) + local;  // null: weights only
     if (vals) vals[k] = k;
 }
 
@@ -224,12 +237,12 @@ __global__ void k_active_tiles(int ntx, int nty, int ntz, int channel, const int
 // Cell-start table of every occupied tile: ctab[slot][c] = first sorted
 // position of local cell c (c = TS^3 holds the tile's end), by binary search
 // in the tile's sorted key range.
-template <int TS>
-__global__ void __launch_bounds__(TS * TS * TS) k_cell_table(const unsigned* __restrict__ keys,
+template <int TS, int TZ>
+__global__ void __launch_bounds__(TS * TS * TZ) k_cell_table(const unsigned* __restrict__ keys,
                                                             const int* __restrict__ tstart, const int* __restrict__ tend,
                                                             const int* __restrict__ occ, const int* __restrict__ occ_count,
                                                             int* __restrict__ ctab) {
-    constexpr int C = TS * TS * TS;
+    constexpr int C = TS * TS * TZ;
     const int nocc = *occ_count;
     for (int li = blockIdx.x; li < nocc; li += gridDim.x) {
         const int t = occ[li];
@@ -256,16 +269,19 @@ __global__ void __launch_bounds__(TS * TS * TS) k_cell_table(const unsigned* __r
 // [J-2, J+2] along the other two, i.e. at most 25 contiguous runs, in a fixed
 // order: no float atomics, bitwise repeatable.
 // ---------------------------------------------------------------------------
-template <typename T, int TS>
-__global__ void __launch_bounds__(TS * TS * TS) k_spread_gather(Dims d, int M, const int* __restrict__ perm,
+template <typename T, int TS, int TZ>
+__global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, const int* __restrict__ perm,
                                                                 MarkerW<T> mw, const T* __restrict__ G,
                                                                 const double* __restrict__ vol, double scale,
                                                                 const int* __restrict__ slot, const int* __restrict__ ctab,
                                                                 const int* __restrict__ list, const int* __restrict__ count,
                                                                 int cap, T* __restrict__ fu, T* __restrict__ fv,
                                                                 T* __restrict__ fw, int* __restrict__ flag) {
-    constexpr int NT = TS * TS * TS, E = TS + 4, E2 = E * E, E3 = E2 * E, C = TS * TS * TS;
-    constexpr int NSEG = E2 * 3;  // (row, tile segment) pairs
+    // 3D: TZ == TS, the neighbourhood grows by 2 cells per side along every
+    // axis. 2D (TZ == 1, nz == 1): one plane, no z halo.
+    constexpr int NT = TS * TS * TZ, E = TS + 4, EZ = TZ == 1 ? 1 : TS + 4, HZ = TZ == 1 ? 0 : 2;
+    constexpr int E2 = E * E, E3 = E2 * EZ, C = TS * TS * TZ;
+    constexpr int NSEG = E * EZ * 3;  // (row, tile segment) pairs
     extern __shared__ __align__(16) unsigned char smem[];
     int* s_estart = (int*)smem;          // E3 + 1: first staged slot of each E cell
     int* s_seg = s_estart + (E3 + 1);    // NSEG: staged offset of each segment
@@ -275,14 +291,14 @@ __global__ void __launch_bounds__(TS * TS * TS) k_spread_gather(Dims d, int M, c
     // cap * 12: x weights, y weights, z weights times the marker's force
     T* s_w = (T*)(((uintptr_t)(s_base + cap) + 15) & ~(uintptr_t)15);
 
-    const int ntx = d.nx / TS, nty = d.ny / TS, ntz = d.nz / TS;
+    const int ntx = d.nx / TS, nty = d.ny / TS, ntz = d.nz / TZ;
     const int ncount = *count;
     const int tid = threadIdx.x;
     const int lx = tid % TS, ly = (tid / TS) % TS, lz = tid / (TS * TS);
     for (int li = blockIdx.x; li < ncount; li += gridDim.x) {
         const int t = list[li];
         const int tx = t % ntx, ty = (t / ntx) % nty, tz = t / (ntx * nty);
-        const int ox = tx * TS - 2, oy = ty * TS - 2, oz = tz * TS - 2;  // E origin (unwrapped cells)
+        const int ox = tx * TS - 2, oy = ty * TS - 2, oz = tz * TZ - HZ;  // E origin (unwrapped cells)
         // ---- segment ranges: segment q = (row r, part j): cells ex in
         //      [0, 2), [2, TS+2), [TS+2, E) of row r, i.e. tiles tx-1, tx, tx+1
         int my_len[(NSEG + NT - 1) / NT], my_p0[(NSEG + NT - 1) / NT];
@@ -303,10 +319,10 @@ __global__ void __launch_bounds__(TS * TS * TS) k_spread_gather(Dims d, int M, c
                     const int ex0 = j == 0 ? 0 : (j == 1 ? 2 : TS + 2);
                     const int ex1 = j == 0 ? 2 : (j == 1 ? TS + 2 : E);  // exclusive
                     const int gx0 = wrapi(ox + ex0, d.nx);
-                    const int tt = gx0 / TS + ntx * (gy / TS + nty * (gz / TS));
+                    const int tt = gx0 / TS + ntx * (gy / TS + nty * (gz / TZ));
                     const int sl = slot[tt];
                     if (sl >= 0) {
-                        const int lc0 = (gx0 % TS) + TS * ((gy % TS) + TS * (gz % TS));
+                        const int lc0 = (gx0 % TS) + TS * ((gy % TS) + TS * (gz % TZ));
                         const int* row = ctab + (size_t)sl * (C + 1);
                         my_p0[k] = row[lc0];
                         my_len[k] = row[lc0 + (ex1 - ex0)] - my_p0[k];
@@ -345,8 +361,8 @@ __global__ void __launch_bounds__(TS * TS * TS) k_spread_gather(Dims d, int M, c
                         gy = wrapi(gy, d.ny);
                         const int gz = wrapi(oz + r / E, d.nz);
                         const int gx = wrapi(ox + ex, d.nx);
-                        const int tt = gx / TS + ntx * (gy / TS + nty * (gz / TS));
-                        const int lc = (gx % TS) + TS * ((gy % TS) + TS * (gz % TS));
+                        const int tt = gx / TS + ntx * (gy / TS + nty * (gz / TZ));
+                        const int lc = (gx % TS) + TS * ((gy % TS) + TS * (gz % TZ));
                         st = off + (ctab[(size_t)slot[tt] * (C + 1) + lc] - my_p0[k]);
                     }
                     s_estart[ex + E * r] = st;
@@ -382,12 +398,12 @@ __global__ void __launch_bounds__(TS * TS * TS) k_spread_gather(Dims d, int M, c
             }
             __syncthreads();
             T* f = comp == 0 ? fu : (comp == 1 ? fv : fw);
-            const int J[3] = {lx + 2, ly + 2, lz + 2};
+            const int J[3] = {lx + 2, ly + 2, lz + HZ};
             const int hx = (comp == 0) ? J[0] + 1 : J[0] + 2;
             const int hy = (comp == 1) ? J[1] + 1 : J[1] + 2;
-            const int hz = (comp == 2) ? J[2] + 1 : J[2] + 2;
+            const int hz = TZ == 1 ? J[2] : ((comp == 2) ? J[2] + 1 : J[2] + 2);
             T acc = T(0);
-            for (int ez = J[2] - 2; ez <= hz; ++ez)
+            for (int ez = J[2] - HZ; ez <= hz; ++ez)
                 for (int ey = J[1] - 2; ey <= hy; ++ey) {
                     const int row = E * (ey + E * ez);
                     const int s0 = s_estart[row + J[0] - 2], s1 = s_estart[row + hx + 1];
@@ -402,7 +418,7 @@ __global__ void __launch_bounds__(TS * TS * TS) k_spread_gather(Dims d, int M, c
                         }
                     }
                 }
-            const int gx = tx * TS + lx, gy = ty * TS + ly, gz = tz * TS + lz;
+            const int gx = tx * TS + lx, gy = ty * TS + ly, gz = tz * TZ + lz;
             if (!(d.channel && comp == 1 && gy == 0)) f[lin(d, gx, gy, gz)] = acc;
             __syncthreads();
         }
@@ -503,52 +519,59 @@ void launch_active_tiles(int ntx, int nty, int ntz, int channel, const int* tsta
                                                     occ_count);
 }
 
-void launch_cell_table(int TS, const unsigned* keys, const int* tstart, const int* tend, const int* occ,
+void launch_cell_table(int TS, int TZ, const unsigned* keys, const int* tstart, const int* tend, const int* occ,
                        const int* occ_count, int max_occ, int* ctab, cudaStream_t s) {
     int blocks = max_occ < 152 * 8 ? max_occ : 152 * 8;
     if (blocks < 1) blocks = 1;
-    if (TS == 8) k_cell_table<8><<<blocks, 512, 0, s>>>(keys, tstart, tend, occ, occ_count, ctab);
-    else k_cell_table<4><<<blocks, 64, 0, s>>>(keys, tstart, tend, occ, occ_count, ctab);
+    if (TS == 8 && TZ == 8) k_cell_table<8, 8><<<blocks, 512, 0, s>>>(keys, tstart, tend, occ, occ_count, ctab);
+    else if (TS == 4 && TZ == 4) k_cell_table<4, 4><<<blocks, 64, 0, s>>>(keys, tstart, tend, occ, occ_count, ctab);
+    else if (TS == 8) k_cell_table<8, 1><<<blocks, 64, 0, s>>>(keys, tstart, tend, occ, occ_count, ctab);
+    else k_cell_table<4, 1><<<blocks, 16, 0, s>>>(keys, tstart, tend, occ, occ_count, ctab);
 }
 
 template <typename T>
-size_t spread_smem_bytes(int TS, int cap) {
-    const int E = TS + 4, E3 = E * E * E, NT = TS * TS * TS;
-    size_t ints = (size_t)(E3 + 1) + 3 * E * E + NT + 2 * (size_t)cap;
+size_t spread_smem_bytes(int TS, int TZ, int cap) {
+    const int E = TS + 4, EZ = TZ == 1 ? 1 : TS + 4, E3 = E * E * EZ, NT = TS * TS * TZ;
+    size_t ints = (size_t)(E3 + 1) + 3 * E * EZ + NT + 2 * (size_t)cap;
     size_t bytes = ints * sizeof(int);
     bytes = (bytes + 15) & ~(size_t)15;
     bytes += (size_t)cap * 12 * sizeof(T);
     return bytes;
 }
 
-template <typename T, int TS>
+template <typename T, int TS, int TZ>
 static void spread_launch(const Dims& d, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
                           double scale, const int* slot, const int* ctab, const int* list, const int* count,
                           int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, cudaStream_t s) {
-    const size_t smem = spread_smem_bytes<T>(TS, cap);
+    const size_t smem = spread_smem_bytes<T>(TS, TZ, cap);
     // opt in to exactly the dynamic shared memory this launch uses (the
     // kernel's static shared memory counts against the same 227 KB)
     static size_t configured = 0;
     if (configured < smem) {
-        if (cudaFuncSetAttribute(k_spread_gather<T, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        if (cudaFuncSetAttribute(k_spread_gather<T, TS, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess)
             return;  // the launch error is reported by the caller's cudaGetLastError
         configured = smem;
     }
     int blocks = max_tiles < 152 * 4 ? max_tiles : 152 * 4;
     if (blocks < 1) blocks = 1;
-    k_spread_gather<T, TS><<<blocks, TS * TS * TS, smem, s>>>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count,
-                                                              cap, fu, fv, fw, flag);
+    k_spread_gather<T, TS, TZ><<<blocks, TS * TS * TZ, smem, s>>>(d, M, perm, mw, G, vol, scale, slot, ctab, list,
+                                                                  count, cap, fu, fv, fw, flag);
 }
 
 template <typename T>
 void launch_spread_gather(const Dims& d, int TS, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
                           double scale, const int* slot, const int* ctab, const int* list, const int* count,
                           int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, cudaStream_t s) {
-    if (TS == 8)
-        spread_launch<T, 8>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, flag, s);
+    const bool flat = d.nz == 1;
+    if (TS == 8 && !flat)
+        spread_launch<T, 8, 8>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, flag, s);
+    else if (TS == 4 && !flat)
+        spread_launch<T, 4, 4>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, flag, s);
+    else if (TS == 8)
+        spread_launch<T, 8, 1>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, flag, s);
     else
-        spread_launch<T, 4>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, flag, s);
+        spread_launch<T, 4, 1>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, flag, s);
 }
 
 template <typename T, typename TF>
@@ -565,7 +588,7 @@ void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, do
     template void launch_springs<T>(int, const double*, const int*, const int*, double, T*, cudaStream_t);       \
     template void launch_marker_prep<T>(const Dims&, int, int, const double*, unsigned*, int*, MarkerW<T>, int*, \
                                         cudaStream_t);                                                           \
-    template size_t spread_smem_bytes<T>(int, int);                                                             \
+    template size_t spread_smem_bytes<T>(int, int, int);                                                             \
     template void launch_spread_gather<T>(const Dims&, int, int, const int*, MarkerW<T>, const T*, const double*, \
                                           double, const int*, const int*, const int*, const int*, int, int, T*,  \
                                           T*, T*, int*, cudaStream_t);                                          \

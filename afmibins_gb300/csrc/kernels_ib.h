@@ -19,8 +19,9 @@ struct MarkerW {
 template <typename T>
 void launch_springs(int M, const double* X, const int* nstart, const int* nidx, double k, T* G, cudaStream_t s);
 
-// keys = tile * TS^3 + cell-in-tile, vals = marker index; flag set to 1 when a
-// marker is within 2.5h of a channel wall, 2 on a NaN position.
+// keys = tile * TS^2 TZ + cell-in-tile (TZ = TS, or 1 on a 2D grid), vals =
+// marker index; flag set to 1 when a marker is within 2.5h of a channel wall,
+// 2 on a NaN position.
 template <typename T>
 void launch_marker_prep(const Dims& d, int TS, int M, const double* X, unsigned* keys, int* vals, MarkerW<T> mw,
                         int* flag, cudaStream_t s);
@@ -36,11 +37,11 @@ void launch_tile_ranges(const unsigned* keys, int M, int cells_per_tile, int* ts
 void launch_active_tiles(int ntx, int nty, int ntz, int channel, const int* tstart, const int* tend, int* list,
                          int* count, int* slot, int* occ, int* occ_count, cudaStream_t s);
 // ctab[slot][c]: first sorted position of local cell c of each occupied tile
-void launch_cell_table(int TS, const unsigned* keys, const int* tstart, const int* tend, const int* occ,
+void launch_cell_table(int TS, int TZ, const unsigned* keys, const int* tstart, const int* tend, const int* occ,
                        const int* occ_count, int max_occ, int* ctab, cudaStream_t s);
 
 template <typename T>
-size_t spread_smem_bytes(int TS, int cap);
+size_t spread_smem_bytes(int TS, int TZ, int cap);
 // f_c(face) = scale * sum_k (phi/n)^3 * vol_k * G_c,k over the active tiles
 // (faces of the other tiles are left untouched). flag = 3 when a tile holds
 // more than `cap` candidates.

@@ -13,12 +13,18 @@ inline dim3 grid3(const Dims& d) { return dim3((d.nx + BX - 1) / BX, (d.ny + BY 
 
 // Neighbour sum and diagonal factor of the Laplacian row at (x, y, z):
 // L x = n^2 * (S - c * x_i), c = 6 in the interior and one less per channel
-// wall (Neumann, src/mg/laplacian.h:75-82).
+// wall (Neumann, src/mg/laplacian.h:75-82). A one-cell z extent (2D) folds
+// its two self-neighbours into the diagonal, src/mg/laplacian.h:62-73.
 template <typename T>
 __device__ __forceinline__ void lap_row(const Dims& d, const T* __restrict__ x, int xi, int yi, int zi, T& S, T& c) {
-    S = (x[lin(d, xm1(d, xi), yi, zi)] + x[lin(d, xp1(d, xi), yi, zi)]) +
-        (x[lin(d, xi, yi, zm1(d, zi))] + x[lin(d, xi, yi, zp1(d, zi))]);
-    c = T(6);
+    if (d.nz == 1) {
+        S = x[lin(d, xm1(d, xi), yi, zi)] + x[lin(d, xp1(d, xi), yi, zi)];
+        c = T(4);
+    } else {
+        S = (x[lin(d, xm1(d, xi), yi, zi)] + x[lin(d, xp1(d, xi), yi, zi)]) +
+            (x[lin(d, xi, yi, zm1(d, zi))] + x[lin(d, xi, yi, zp1(d, zi))]);
+        c = T(6);
+    }
     if (d.channel) {
         if (yi > 0) S += x[lin(d, xi, yi - 1, zi)]; else c -= T(1);
         if (yi < d.ny - 1) S += x[lin(d, xi, yi + 1, zi)]; else c -= T(1);
@@ -100,7 +106,7 @@ __global__ void k_rbgs(Dims d, int color, T* __restrict__ xv, const T* __restric
     lap_row(d, xv, x, y, z, S, c);
     const long long i = lin(d, x, y, z);
     const T inv = T(1) / (T(d.n) * T(d.n));
-    const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : T(1) / c);
+    const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
     xv[i] = (S - b[i] * inv) * rc;
 }
 
@@ -176,7 +182,7 @@ __global__ void __launch_bounds__(FX * FY) k_rbgs_fused(Dims d, const T* __restr
         } else {
             S += c0[hy - 1][hx] + c0[hy + 1][hx];
         }
-        const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : T(1) / c);
+        const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
         c0[hy][hx] = (S - bval * inv) * rc;
     };
     load_x(z0 - 2);
@@ -219,6 +225,19 @@ __global__ void k_restrict(Dims d, T* __restrict__ coarse, const T* __restrict__
     const int cx = d.nx / 2, cy = d.ny / 2, cz = d.nz / 2;
     const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
     if (xc >= cx || yc >= cy) return;
+    if (d.nz == 1) {
+        // 2D (periodic): (1,3,3,1)^2 / 64 over 16 taps
+        const T wgt[4] = {T(1), T(3), T(3), T(1)};
+        T acc = T(0);
+#pragma unroll
+        for (int ky = 0; ky < 4; ++ky)
+#pragma unroll
+            for (int kx = 0; kx < 4; ++kx)
+                acc += (wgt[kx] * wgt[ky] / T(64)) *
+                       fine[lin(d, wrapi(2 * xc + 1 + kx - 2, d.nx), wrapi(2 * yc + 1 + ky - 2, d.ny), 0)];
+        coarse[xc + (long long)cx * yc] = acc;
+        return;
+    }
     const int xcf = 2 * xc + 1, ycf = 2 * yc + 1, zcf = 2 * zc + 1;
     int xs[4], ys[4], zs[4];
 #pragma unroll
@@ -258,6 +277,19 @@ __global__ void k_prolong(Dims d, T* __restrict__ fine, const T* __restrict__ co
         const long long i = lin(d, a, b, c);
         if (ADD) fine[i] = fine[i] + val; else fine[i] = val;
     };
+    if (d.nz == 1) {
+        // 2D (periodic): bilinear (9,3,3,1)/16 onto the four fine cells
+        auto C2 = [&](int a, int b) { return coarse[a + (long long)cx * b]; };
+        const int xn = (xc + 1) % cx, yn = (yc + 1) % cy;
+        const int xcf = 2 * xc + 1, ycf = 2 * yc + 1, xnf = (xcf + 1) % d.nx, ynf = (ycf + 1) % d.ny;
+        const T bl = C2(xc, yc), br = C2(xn, yc), ul = C2(xc, yn), ur = C2(xn, yn);
+        const T a = T(9) / T(16), b = T(3) / T(16), e = T(1) / T(16);
+        put(xcf, ycf, 0, a * bl + b * (br + ul) + e * ur);
+        put(xnf, ycf, 0, a * br + b * (bl + ur) + e * ul);
+        put(xcf, ynf, 0, a * ul + b * (ur + bl) + e * br);
+        put(xnf, ynf, 0, a * ur + b * (ul + br) + e * bl);
+        return;
+    }
     const int xn = (xc + 1) % cx, zn = (zc + 1) % cz;
     const int xcf = 2 * xc + 1, zcf = 2 * zc + 1;
     const int xnf = (xcf + 1) % d.nx, znf = (zcf + 1) % d.nz;
@@ -387,17 +419,17 @@ bool rbgs_fused_ok(const Dims& d) { return d.nx >= FX && d.ny >= FY && d.nz >= F
 
 template <typename T>
 void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s) {
-    dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz / 2);
+    dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz == 1 ? 1 : d.nz / 2);
     k_restrict<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine);
 }
 template <typename T>
 void launch_prolong_add(const Dims& d, T* fine, const T* coarse, cudaStream_t s) {
-    dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz / 2);
+    dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz == 1 ? 1 : d.nz / 2);
     k_prolong<T, true><<<g, dim3(BX, BY), 0, s>>>(d, fine, coarse);
 }
 template <typename T>
 void launch_prolong_assign(const Dims& d, T* fine, const T* coarse, cudaStream_t s) {
-    dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz / 2);
+    dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz == 1 ? 1 : d.nz / 2);
     k_prolong<T, false><<<g, dim3(BX, BY), 0, s>>>(d, fine, coarse);
 }
 template <typename TD>

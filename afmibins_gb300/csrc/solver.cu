@@ -85,7 +85,8 @@ struct afmib_solver {
     bool has_vol = false;
     unsigned *keys = nullptr, *keys2 = nullptr, *hist = nullptr;
     int *vals = nullptr, *vals2 = nullptr, *perm = nullptr;
-    int TS = 0, ntx = 0, nty = 0, ntz = 0, ntiles = 0;
+    int TS = 0, TZ = 0, ntx = 0, nty = 0, ntz = 0, ntiles = 0;  // TZ: tile depth (TS; 1 on a 2D grid)
+    int tile_cells() const { return TS * TS * TZ; }
     int *tstart = nullptr, *tend = nullptr, *tlist = nullptr, *tcount = nullptr;
     int *tslot = nullptr, *tocc = nullptr, *ctab = nullptr;
     int ctab_cap = 0;  // occupied tiles the cell table can hold
@@ -774,7 +775,7 @@ int marker_alloc(afmib_solver* s, int M, int nnz) {
     {
         const int need = std::min(s->ntiles, std::max(M, 1));
         if (need > s->ctab_cap) {
-            TRY(regrow(s, &s->ctab, (size_t)need * (s->TS * s->TS * s->TS + 1), 0));
+            TRY(regrow(s, &s->ctab, (size_t)need * (s->tile_cells() + 1), 0));
             s->ctab_cap = need;
         }
     }
@@ -786,7 +787,7 @@ int marker_alloc(afmib_solver* s, int M, int nnz) {
 }
 
 int key_bits(afmib_solver* s) {
-    const unsigned long long top = (unsigned long long)s->ntiles * s->TS * s->TS * s->TS;
+    const unsigned long long top = (unsigned long long)s->ntiles * s->tile_cells();
     int b = 0;
     while ((1ull << b) < top) ++b;
     return b;
@@ -814,12 +815,12 @@ int bin_markers(afmib_solver* s, const double* P, bool fp32 = false) {
     CK(cudaMemsetAsync(s->tend, 0, s->ntiles * sizeof(int), s->st));
     CK(cudaMemsetAsync(s->tcount, 0, 2 * sizeof(int), s->st));
     {
-        const int C = s->TS * s->TS * s->TS;
+        const int C = s->tile_cells();
         ProfScope ps(s, P_TILES, (double)M * 4 + 5.0 * s->ntiles * 4 + (double)std::min(M, s->ntiles) * (C + 1) * 4, 3);
         launch_tile_ranges(ko, M, C, s->tstart, s->tend, s->st);
         launch_active_tiles(s->ntx, s->nty, s->ntz, s->d.channel, s->tstart, s->tend, s->tlist, s->tcount, s->tslot,
                             s->tocc, s->tcount + 1, s->st);
-        launch_cell_table(s->TS, ko, s->tstart, s->tend, s->tocc, s->tcount + 1, s->ctab_cap, s->ctab, s->st);
+        launch_cell_table(s->TS, s->TZ, ko, s->tstart, s->tend, s->tocc, s->tcount + 1, s->ctab_cap, s->ctab, s->st);
     }
     CKL();
     return AFMIB_OK;
@@ -832,7 +833,7 @@ int spread_generic(afmib_solver* s, const double* G, const double* vol, double s
     CK(cudaMemsetAsync(fu, 0, N * sizeof(double), s->st));
     CK(cudaMemsetAsync(fv, 0, N * sizeof(double), s->st));
     CK(cudaMemsetAsync(fw, 0, N * sizeof(double), s->st));
-    const double touched = (double)s->stats.spread_tiles * s->TS * s->TS * s->TS;
+    const double touched = (double)s->stats.spread_tiles * s->tile_cells();
     {
         ProfScope ps(s, P_SPREAD, (double)s->M * (24 + 3 * 8 + 8 + 8) + 3 * touched * 8);
         launch_spread_gather<double>(s->d, s->TS, s->M, s->perm, s->mw, G, vol, scale, s->tslot, s->ctab, s->tlist,
@@ -840,6 +841,12 @@ int spread_generic(afmib_solver* s, const double* G, const double* vol, double s
     }
     CKL();
     return AFMIB_OK;
+}
+
+// Spreading scale phi^3 / (phi/n)^3 = n^3; on a 2D grid the kernel is
+// phi^2 = n^2 (phi/n)^2 (a marker's volume is then its area measure).
+double spread_scale(const Dims& d) {
+    return d.nz == 1 ? (double)d.n * d.n : (double)d.n * d.n * d.n;
 }
 
 // f = spread(G) with the bins and weights of the last bin_markers call.
@@ -850,9 +857,9 @@ int spread_forces(afmib_solver* s, const double* vol, double* fu, double* fv, do
     CK(cudaMemsetAsync(fu, 0, N * sizeof(double), s->st));
     CK(cudaMemsetAsync(fv, 0, N * sizeof(double), s->st));
     CK(cudaMemsetAsync(fw, 0, N * sizeof(double), s->st));
-    const double n3 = (double)s->d.n * s->d.n * s->d.n;
+    const double n3 = spread_scale(s->d);
     const int cap = 1536;
-    const double touched = (double)s->stats.spread_tiles * s->TS * s->TS * s->TS;
+    const double touched = (double)s->stats.spread_tiles * s->tile_cells();
     {
         ProfScope ps(s, P_SPREAD, (double)s->M * (24 + 3 * 8 + 8 + 8) + 3 * touched * 8);
         launch_spread_gather<double>(s->d, s->TS, s->M, s->perm, s->mw, s->G, vol, n3, s->tslot, s->ctab, s->tlist,
@@ -865,9 +872,9 @@ int spread_forces(afmib_solver* s, const double* vol, double* fu, double* fv, do
 int spread_forces32(afmib_solver* s, const double* vol) {
     const long long N = s->N();
     for (int c = 0; c < 3; ++c) CK(cudaMemsetAsync(s->f32[c], 0, N * sizeof(float), s->st));
-    const double n3 = (double)s->d.n * s->d.n * s->d.n;
+    const double n3 = spread_scale(s->d);
     const int cap = 3072;
-    const double touched = (double)s->stats.spread_tiles * s->TS * s->TS * s->TS;
+    const double touched = (double)s->stats.spread_tiles * s->tile_cells();
     {
         ProfScope ps(s, P_SPREAD, (double)s->M * (24 + 3 * 4 + 8 + 8) + 3 * touched * 4);
         launch_spread_gather<float>(s->d, s->TS, s->M, s->perm, s->mw32, s->G32, vol, n3, s->tslot, s->ctab,
@@ -891,7 +898,7 @@ int check_marker_flag(afmib_solver* s) {
 }
 
 int interp_markers(afmib_solver* s, const double* u, const double* v, const double* w, double* U, bool fp32 = false) {
-    const double touched = (double)s->stats.spread_tiles * s->TS * s->TS * s->TS;
+    const double touched = (double)s->stats.spread_tiles * s->tile_cells();
     ProfScope ps(s, P_INTERP, 3 * touched * 8 + (double)s->M * (24 + 3 * 8 + 8));
     if (fp32) launch_interp<float, float>(s->d, s->M, s->perm, s->mw32, s->u32, s->v32, s->w32, U, s->st);
     else launch_interp<double, double>(s->d, s->M, s->perm, s->mw, u, v, w, U, s->st);
@@ -1060,6 +1067,7 @@ int traj_alloc(afmib_solver* s, int nsteps, int every) {
 
 int traj_forward(afmib_solver* s, int nsteps, int every) {
     if (s->d.channel) return s->fail(AFMIB_ERR_ARG, "the adjoint trajectory needs the periodic domain");
+    if (s->d.nz == 1) return s->fail(AFMIB_ERR_ARG, "the adjoint trajectory needs a 3D grid");
     if (s->M <= 0) return s->fail(AFMIB_ERR_STATE, "no markers set");
     if (!s->nbr_symmetric) return s->fail(AFMIB_ERR_ARG, "the adjoint needs symmetric spring neighbour lists");
     if (s->has_vol) return s->fail(AFMIB_ERR_ARG, "the adjoint uses unit marker volumes");
@@ -1223,15 +1231,19 @@ int traj_adjoint(afmib_solver* s, const double* lu, const double* lv, const doub
 
 int setup_tiles(afmib_solver* s) {
     const Dims& d = s->d;
+    // 2D grids (nz == 1) use tiles one cell deep
+    const bool flat = d.nz == 1;
     auto ok = [&](int ts) {
-        return d.nx % ts == 0 && d.ny % ts == 0 && d.nz % ts == 0 && d.nx >= ts + 4 && d.ny >= ts + 4 && d.nz >= ts + 4;
+        return d.nx % ts == 0 && d.ny % ts == 0 && d.nx >= ts + 4 && d.ny >= ts + 4 &&
+               (flat || (d.nz % ts == 0 && d.nz >= ts + 4));
     };
     if (ok(8)) s->TS = 8;
     else if (ok(4)) s->TS = 4;
     else return s->fail(AFMIB_ERR_ARG, "immersed boundary needs every extent a multiple of 4 and at least 8 cells");
+    s->TZ = flat ? 1 : s->TS;
     s->ntx = d.nx / s->TS;
     s->nty = d.ny / s->TS;
-    s->ntz = d.nz / s->TS;
+    s->ntz = d.nz / s->TZ;
     s->ntiles = s->ntx * s->nty * s->ntz;
     TRY(dalloc(s, &s->tstart, s->ntiles));
     TRY(dalloc(s, &s->tend, s->ntiles));
@@ -1251,7 +1263,8 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (g.max_cg_iters <= 0) g.max_cg_iters = 1000;
     if (g.max_mg_cycles <= 0) g.max_mg_cycles = 200;
     if (g.inner_tol <= 0) g.inner_tol = 1e-5;
-    if (g.nx < 2 || g.ny < 2 || g.nz < 2) return s->fail(AFMIB_ERR_ARG, "every extent must be at least 2 cells");
+    if (g.nx < 2 || g.ny < 2 || g.nz < 1 || (g.nz == 1 && g.bc != AFMIB_BC_PERIODIC))
+        return s->fail(AFMIB_ERR_ARG, "extents must be at least 2 cells (nz = 1, a 2D grid, only with periodic bc)");
     if (g.bc != AFMIB_BC_PERIODIC && g.bc != AFMIB_BC_CHANNEL) return s->fail(AFMIB_ERR_ARG, "bc must be periodic or channel");
     if (g.precision != AFMIB_FP64 && g.precision != AFMIB_MIXED) return s->fail(AFMIB_ERR_ARG, "precision");
     s->mixed = g.precision == AFMIB_MIXED;
@@ -1309,18 +1322,22 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (levels <= 0) {
         levels = 0;
         Dims t = s->d;
-        while (is_even(t.nx) && is_even(t.ny) && is_even(t.nz) && t.nx >= 2 && t.ny >= 2 && t.nz >= 2) {
-            t.nx /= 2; t.ny /= 2; t.nz /= 2; t.n /= 2;
+        // 2D grids (nz == 1) coarsen x and y only
+        const bool flat = t.nz == 1;
+        while (is_even(t.nx) && is_even(t.ny) && (flat || is_even(t.nz)) && t.nx >= 2 && t.ny >= 2 &&
+               (flat || t.nz >= 2)) {
+            t.nx /= 2; t.ny /= 2; if (!flat) t.nz /= 2; t.n /= 2;
             ++levels;
-            if (t.nx == 1 || t.ny == 1 || t.nz == 1) break;
+            if (t.nx == 1 || t.ny == 1 || (!flat && t.nz == 1)) break;
         }
     }
     Dims t = s->d;
     for (int l = 0; l <= levels; ++l) {
         if (l > 0) {
-            if (!is_even(t.nx) || !is_even(t.ny) || !is_even(t.nz))
+            const bool flat = t.nz == 1;
+            if (!is_even(t.nx) || !is_even(t.ny) || !(flat || is_even(t.nz)))
                 return s->fail(AFMIB_ERR_ARG, "mg_levels exceeds the number of halvings of the grid");
-            t.nx /= 2; t.ny /= 2; t.nz /= 2; t.n = t.n / 2 > 0 ? t.n / 2 : 1;
+            t.nx /= 2; t.ny /= 2; if (!flat) t.nz /= 2; t.n = t.n / 2 > 0 ? t.n / 2 : 1;
         }
         MGLevel L{t, nullptr, nullptr, nullptr, nullptr};
         const long long n = t.ncell();
@@ -1664,19 +1681,20 @@ int afmib_helmholtz_cg(afmib_solver* s, int comp, double scale, double* x, const
 int afmib_restrict(afmib_solver* s, double* coarse, const double* fine) {
     if (!s || !coarse || !fine) return AFMIB_ERR_ARG;
     const Dims& d = s->d;
-    if (!is_even(d.nx) || !is_even(d.ny) || !is_even(d.nz)) return s->fail(AFMIB_ERR_ARG, "odd extent");
+    if (!is_even(d.nx) || !is_even(d.ny) || !(d.nz == 1 || is_even(d.nz))) return s->fail(AFMIB_ERR_ARG, "odd extent");
+    const long long nc = s->N() / (d.nz == 1 ? 4 : 8);
     TRY(copy_in(s, s->tmp[0], fine, s->N()));
     launch_restrict<double>(d, s->tmp[1], s->tmp[0], s->st);
     CKL();
-    TRY(copy_out(s, coarse, s->tmp[1], s->N() / 8));
+    TRY(copy_out(s, coarse, s->tmp[1], nc));
     return sync(s);
 }
 
 int afmib_prolong(afmib_solver* s, double* fine, const double* coarse) {
     if (!s || !coarse || !fine) return AFMIB_ERR_ARG;
     const Dims& d = s->d;
-    if (!is_even(d.nx) || !is_even(d.ny) || !is_even(d.nz)) return s->fail(AFMIB_ERR_ARG, "odd extent");
-    TRY(copy_in(s, s->tmp[0], coarse, s->N() / 8));
+    if (!is_even(d.nx) || !is_even(d.ny) || !(d.nz == 1 || is_even(d.nz))) return s->fail(AFMIB_ERR_ARG, "odd extent");
+    TRY(copy_in(s, s->tmp[0], coarse, s->N() / (d.nz == 1 ? 4 : 8)));
     launch_prolong_assign<double>(d, s->tmp[1], s->tmp[0], s->st);
     CKL();
     TRY(copy_out(s, fine, s->tmp[1], s->N()));

@@ -15,6 +15,11 @@
  *    mode (interior y faces, src/ib/mac_grid.h:75-105) and nx*ny*nz in
  *    periodic mode.
  *  - Wall vectors (channel mode) have nx*nz entries.
+ *  - nz = 1 (periodic bc only) is a 2D grid in (x, y): the reference has no
+ *    2D mode; every operator is its 3D row with the one-cell z extent folded
+ *    into the diagonal (src/mg/laplacian.h:62-73), multigrid coarsens x and y,
+ *    w stays zero, and the marker kernel is phi_x phi_y (spreading scale n^2,
+ *    a marker's volume is its area measure; interpolation weight h^2).
  *  - Marker positions are X[M][3]; per-marker forces are F[3][M].
  *  - Pointers may be host or device memory (unified addressing); calls that
  *    return data to the host synchronise the solver's stream first.
@@ -47,7 +52,7 @@ enum { AFMIB_BC_PERIODIC = 0, AFMIB_BC_CHANNEL = 1 };
 enum { AFMIB_FP64 = 0, AFMIB_MIXED = 1 };
 
 typedef struct afmib_config {
-    int nx, ny, nz;     /* cells (the reference's geometry<L,W,H,D>::nx, ny, nz) */
+    int nx, ny, nz;     /* cells (the reference's geometry<L,W,H,D>::nx, ny, nz); nz = 1: 2D */
     int n;              /* cells per unit length, 0 -> nx (geometry::n) */
     int bc;             /* AFMIB_BC_CHANNEL: the reference's walls in y; AFMIB_BC_PERIODIC */
     int precision;      /* AFMIB_FP64 (drop-in) or AFMIB_MIXED (FP32 inner, FP64 outer) */

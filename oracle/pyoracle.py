@@ -101,7 +101,7 @@ class Grid:
 
     def levels(self):
         """Coarsening depth down to one cell along the shortest axis (src/mg/solver.h:239-271)."""
-        m = min(self.nx, self.ny, self.nz)
+        m = min(self.nx, self.ny) if self.nz == 1 else min(self.nx, self.ny, self.nz)
         return int(np.log2(m))
 
 
@@ -142,7 +142,7 @@ def gs_sweep(g, x, b):
 
 
 def restrict(g, fine):
-    c = np.zeros(g.ncell // 8)
+    c = np.zeros(g.ncell // (4 if g.nz == 1 else 8))
     lib().orc_restrict(g.dims, _p(c), _p(fine))
     return c
 

@@ -234,7 +234,29 @@ struct Level { int nx, ny, nz, n; };
 
 // Full-weighting restriction, 4^3 taps with weights (1,3,3,1)^3/512,
 // src/mg/solver.h:153-181. Walls clamp y in channel mode; periodic mode wraps.
+//
+// Two-dimensional problems (nz == 1, periodic): the reference has no 2D mode;
+// its own one-cell folding of periodic axes (src/mg/laplacian.h:62-73) makes
+// every operator on nz == 1 the 2D operator, and the transfers are the same
+// weights without the z factor: (1,3,3,1)^2/64 and the bilinear (9,3,3,1)/16
+// of the reference's wall rows (src/mg/solver.h:117-149). Levels coarsen x
+// and y only.
 void restrict_fw(const Level& f, bool channel, vec& out, const vec& in) {
+    if (f.nz == 1) {
+        const int cx = f.nx / 2, cy = f.ny / 2;
+        out.assign((long)cx * cy, 0.0);
+        for (int xcc = 0; xcc < cx; ++xcc)
+            for (int ycc = 0; ycc < cy; ++ycc) {
+                double& o = out[xcc + (long)cx * ycc];
+                for (int t = 0; t < 16; ++t) {
+                    const int dx = (t % 4) - 2, dy = t / 4 - 2;
+                    const int x = wrap(2 * xcc + 1 + dx, f.nx), y = wrap(2 * ycc + 1 + dy, f.ny);
+                    const int weight = (4 - std::abs(2 * dx + 1)) * (4 - std::abs(2 * dy + 1));
+                    o += weight / 64. * in[x + (long)f.nx * y];
+                }
+            }
+        return;
+    }
     const int cx = f.nx / 2, cy = f.ny / 2, cz = f.nz / 2;
     out.assign((long)cx * cy * cz, 0.0);
     for (int xcc = 0; xcc < cx; ++xcc)
@@ -259,6 +281,23 @@ void restrict_fw(const Level& f, bool channel, vec& out, const vec& in) {
 // indexes those rows with ny where nx is meant, src/mg/solver.h:136-139; the
 // two agree whenever nx == ny, the only shape the channel tests use.)
 void prolong_assign(const Level& f, bool channel, vec& out, const vec& in) {
+    if (f.nz == 1) {
+        const int cx = f.nx / 2, cy = f.ny / 2, nx = f.nx, ny = f.ny;
+        out.assign((long)nx * ny, 0.0);
+        auto C = [&](int x, int y) { return in[x + (long)cx * y]; };
+        auto F = [&](int x, int y) -> double& { return out[x + (long)nx * y]; };
+        for (int xcc = 0; xcc < cx; ++xcc)
+            for (int ycc = 0; ycc < cy; ++ycc) {
+                const int xnc = (xcc + 1) % cx, ync = (ycc + 1) % cy;
+                const int xcf = 2 * xcc + 1, ycf = 2 * ycc + 1, xnf = (xcf + 1) % nx, ynf = (ycf + 1) % ny;
+                const double bl = C(xcc, ycc), br = C(xnc, ycc), ul = C(xcc, ync), ur = C(xnc, ync);
+                F(xcf, ycf) = 9. / 16. * bl + 3. / 16. * (br + ul) + 1. / 16. * ur;
+                F(xnf, ycf) = 9. / 16. * br + 3. / 16. * (bl + ur) + 1. / 16. * ul;
+                F(xcf, ynf) = 9. / 16. * ul + 3. / 16. * (ur + bl) + 1. / 16. * br;
+                F(xnf, ynf) = 9. / 16. * ur + 3. / 16. * (ul + br) + 1. / 16. * bl;
+            }
+        return;
+    }
     const int cx = f.nx / 2, cy = f.ny / 2, cz = f.nz / 2;
     const int nx = f.nx, ny = f.ny, nz = f.nz;
     out.assign((long)nx * ny * nz, 0.0);
@@ -386,7 +425,7 @@ MG make_mg(const Grid& g, int levels, double tol, int nu1, int nu2, int maxit) {
     mg.nu2 = nu2;
     mg.maxit = maxit;
     for (int l = 0; l <= levels; ++l)
-        mg.lv.push_back(Level{g.nx >> l, g.ny >> l, g.nz >> l, g.n >> l});
+        mg.lv.push_back(Level{g.nx >> l, g.ny >> l, g.nz == 1 ? 1 : g.nz >> l, g.n >> l});
     return mg;
 }
 
@@ -681,6 +720,17 @@ inline long first_face(double s, double off) { return (long)std::floor(s - off) 
 
 struct Marker { double p[3]; };
 
+// Two-dimensional grids (nz == 1): the kernel is the 2D product phi_x phi_y
+// (the z factor is one on the single plane, zero on the other three taps),
+// spreading gives f = sum phi^2 vol F (vol: the marker's area measure) and
+// interpolation U = sum phi^2 h^2 u.
+inline void flat_z(const Grid& g, long* base, double (*wgt)[4]) {
+    if (g.nz != 1) return;
+    base[2] = 0;
+    wgt[2][0] = 1.0;
+    wgt[2][1] = wgt[2][2] = wgt[2][3] = 0.0;
+}
+
 // Spreading: f(face) = sum_k phi^3 * vol_k * F_k, the periodic-correct sum
 // (each marker's four nearest faces per axis, images taken along the periodic
 // axes). src/ib/grid.h:68-84 computes the same sum face by face through a
@@ -705,6 +755,7 @@ void spread(const Grid& g, int comp, double* f, long M, const double* X, const d
                 wgt[a][m] = delta1(xk[a] - pos, n);
             }
         }
+        flat_z(g, base, wgt);
         const double amp = (vol ? vol[k] : 1.0) * F[k];
         for (int mz = 0; mz < 4; ++mz)
             for (int my = 0; my < 4; ++my)
@@ -729,7 +780,7 @@ void interp(const Grid& g, int comp, double* U, long M, const double* X, const d
     int ext[3];
     face_dims(g, comp, ext);
     const int n = g.n;
-    const double vol = 1. / ((double)n * n * n);
+    const double vol = g.nz == 1 ? 1. / ((double)n * n) : 1. / ((double)n * n * n);
     for (long k = 0; k < M; ++k) {
         const double* xk = X + 3 * k;
         long base[3];
@@ -742,6 +793,7 @@ void interp(const Grid& g, int comp, double* U, long M, const double* X, const d
                 wgt[a][m] = delta1(pos - xk[a], n);
             }
         }
+        flat_z(g, base, wgt);
         double acc = 0.0;
         for (int mz = 0; mz < 4; ++mz)
             for (int my = 0; my < 4; ++my)
@@ -832,7 +884,7 @@ void orc_restrict(const int* dims, double* coarse, const double* fine) {
 
 void orc_prolong(const int* dims, double* fine, const double* coarse) {
     Grid g = make_grid(dims);
-    vec in(coarse, coarse + g.ncell() / 8), out;
+    vec in(coarse, coarse + g.ncell() / (g.nz == 1 ? 4 : 8)), out;
     prolong_assign(Level{g.nx, g.ny, g.nz, g.n}, g.channel, out, in);
     std::memcpy(fine, out.data(), out.size() * sizeof(double));
 }
