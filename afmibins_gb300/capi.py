@@ -333,6 +333,18 @@ class Solver:
         self._ck(self.lib.afmib_mg_solve(self.h, ptr(x), ctypes.byref(c)))
         return x, c.value
 
+    def smooth(self, x, b):
+        """One red-black Gauss-Seidel sweep on L x = b (alg::smooth)."""
+        x = np.array(x, dtype=np.float64, copy=True)
+        self._ck(self.lib.afmib_smooth(self.h, ptr(x), ptr(_f64(b))))
+        return x
+
+    def mg_solve_device(self, x):
+        """mg_solve in place on a device (or host) array; returns (x, cycles)."""
+        c = ctypes.c_int(0)
+        self._ck(self.lib.afmib_mg_solve(self.h, ptr(x), ctypes.byref(c)))
+        return x, c.value
+
     def lap_apply(self, x):
         y = np.zeros(self.ncell)
         self._ck(self.lib.afmib_lap_apply(self.h, ptr(y), ptr(_f64(x))))

@@ -105,11 +105,18 @@ void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, R
 // One red (color 0) or black (color 1) Gauss-Seidel half sweep.
 template <typename T>
 void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s);
-// One full red+black sweep in a single tile-fused launch, out of place
-// (xin -> xout); identical cell for cell to the two per-colour launches.
+// One full red+black sweep per launch, out of place (xin -> xout), z-marching
+// blocks fed by bulk asynchronous row copies; equals the two per-colour
+// launches cell for cell. FY == 0: level not eligible (small, 2D, or rows not
+// 16-byte multiples). err[0] |= 1 when a block gave up waiting for a copy.
+struct PipeCfg {
+    int FY = 0, ZC = 0, D = 0, grid = 0;
+    size_t smem = 0;
+};
 template <typename T>
-void launch_rbgs_fused(const Dims& d, const T* xin, T* xout, const T* b, cudaStream_t s);
-bool rbgs_fused_ok(const Dims& d);  // level large enough for the fused tiles
+PipeCfg rbgs_pipe_cfg(const Dims& d);
+template <typename T>
+void launch_rbgs_pipe(const Dims& d, const PipeCfg& c, const T* xin, T* xout, const T* b, int* err, cudaStream_t s);
 // Full-weighting restriction, src/mg/solver.h:153-181 (d = fine dims).
 template <typename T>
 void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s);

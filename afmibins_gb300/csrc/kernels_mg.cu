@@ -111,109 +111,192 @@ __global__ void k_rbgs(Dims d, int color, T* __restrict__ xv, const T* __restric
 }
 
 // ---------------------------------------------------------------------------
-// Tile-fused red-black sweep: one launch performs the red half sweep and the
-// black half sweep, reading x and b once and writing x once (3N words per full
-// sweep instead of the per-colour kernels' ~4.6N). A block owns an FX x FY
-// (x, y) tile and a chunk of FZ planes; it marches k along z with a ring of
-// four planes of x (tile + 2-cell halo) in shared memory: the red cells of
-// plane k are updated on the tile + 1-cell halo (they need the old black
-// values), then the black cells of plane k-1 on the tile (they need the new
-// red values of planes k-2, k-1, k), and plane k-1 is written out. The sweep
-// is out of place (xin -> xout): blocks read only old values, recompute the
-// red halo redundantly from them, and the result equals the two per-colour
-// launches cell for cell (same arithmetic, same summation order).
+// Pipelined red-black sweep: one full sweep (red, then black) per launch, out
+// of place (xin -> xout). A block owns FY full-width rows (every x of the row,
+// so there is no x halo: x wraps inside shared memory) and a chunk of ZC
+// planes, and marches along z. At step k it updates the red cells of plane k
+// on the rows tile +- 1, then the black cells of plane k-1 on the tile, then
+// writes plane k-1 of the tile. Rows of x (tile +- 2) and of b (tile +- 1)
+// arrive in a ring of R = D + 4 plane slots by bulk asynchronous copies
+// (cp.async.bulk, one per row, completing on one mbarrier per slot) that one
+// thread issues D planes ahead, so the march does not wait on DRAM. The
+// blocks are persistent and take (row strip, z chunk) items in order.
+// Every update is the per-colour kernel's arithmetic with the same terms in
+// the same order, so a pipelined sweep equals the two per-colour launches
+// cell for cell. Waits are bounded: a block that waits too long records
+// the failure in err[0], waits (bounded) for its copies and leaves.
 // ---------------------------------------------------------------------------
-constexpr int FX = 32, FY = 16, FZ = 16;
-constexpr int HX = FX + 4, HY = FY + 4;  // x ring planes with halo 2
+namespace pipe {
+__device__ __forceinline__ unsigned saddr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(saddr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: false after about `limit` SM clock cycles
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, long long limit) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > limit) return false;
+    return true;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     saddr(dst)),
+                 "l"(src), "r"(bytes), "r"(saddr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+constexpr long long kWaitCycles = 2000000000LL;  // about one second at 2 GHz
+}  // namespace pipe
 
 template <typename T>
-__global__ void __launch_bounds__(FX * FY) k_rbgs_fused(Dims d, const T* __restrict__ xin, T* __restrict__ xout,
-                                                        const T* __restrict__ b) {
-    __shared__ T ring[4][HY][HX];
-    __shared__ T bpl[2][FY + 2][FX + 2];
-    const int tid = threadIdx.x + FX * threadIdx.y;
-    const int x0 = blockIdx.x * FX, y0 = blockIdx.y * FY, z0 = blockIdx.z * FZ;
-    const int zend = min(z0 + FZ, d.nz);
+__global__ void __launch_bounds__(256) k_rbgs_pipe(Dims d, const T* __restrict__ xin, T* __restrict__ xout,
+                                                   const T* __restrict__ b, int FY, int ZC, int D, int* err) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int R = D + 4;
+    const int nx = d.nx, XR = FY + 4, BR = FY + 2;
+    const unsigned row_bytes = (unsigned)(nx * sizeof(T));
+    unsigned long long* bars = (unsigned long long*)smem;  // R <= 16 barriers in the first 128 bytes
+    T* xs = (T*)(smem + 128);                              // [R][XR][nx]
+    T* bs = xs + (size_t)R * XR * nx;                      // [R][BR][nx]
+    __shared__ int s_abort;
+    const int tid = threadIdx.x, NT = blockDim.x;
+    const int hx = nx >> 1;
     const T inv = T(1) / (T(d.n) * T(d.n));
-    // load plane z (wrapped) of x into ring slot: tile + halo 2
-    auto load_x = [&](int z) {
-        const int zz = wrapi(z, d.nz);
-        T(*pl)[HX] = ring[((z % 4) + 4) % 4];
-        for (int e = tid; e < HX * HY; e += FX * FY) {
-            const int hx = e % HX, hy = e / HX;
-            const int gx = wrapi(x0 + hx - 2, d.nx);
-            int gy = y0 + hy - 2;
-            T val = T(0);
-            if (d.channel) {
-                if (gy >= 0 && gy < d.ny) val = xin[lin(d, gx, gy, zz)];
-            } else {
-                val = xin[lin(d, gx, wrapi(gy, d.ny), zz)];
+    const int nstrip = d.ny / FY, nchunk = d.nz / ZC, items = nstrip * nchunk;
+    if (tid == 0) {
+        for (int q = 0; q < R; ++q) pipe::mbar_init(&bars[q], 1);
+        pipe::fence_mbar_init();
+        s_abort = 0;
+    }
+    __syncthreads();
+    long long base = 0;  // planes issued by this block before the current item
+    auto valid_row = [&](int gy) { return !(d.channel && (gy < 0 || gy >= d.ny)); };
+    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+        const int y0 = (item % nstrip) * FY, z0 = (item / nstrip) * ZC, zend = z0 + ZC;
+        const int pfirst = z0 - 2, plast = zend + 1;
+        auto seq = [&](int p) { return base + (p - pfirst); };
+        auto slot = [&](int p) { return (int)(seq(p) % R); };
+        auto parity = [&](int p) { return (unsigned)((seq(p) / R) & 1); };
+        auto xrow = [&](int p, int lr) { return xs + ((size_t)slot(p) * XR + lr) * nx; };
+        auto brow = [&](int p, int lb) { return bs + ((size_t)slot(p) * BR + lb) * nx; };
+        auto issue = [&](int p) {  // thread 0
+            const int q = slot(p), gz = wrapi(p, d.nz);
+            unsigned bytes = 0;
+            for (int r = 0; r < XR; ++r) bytes += valid_row(y0 - 2 + r) ? row_bytes : 0u;
+            for (int r = 0; r < BR; ++r) bytes += valid_row(y0 - 1 + r) ? row_bytes : 0u;
+            pipe::mbar_expect_tx(&bars[q], bytes);
+            for (int r = 0; r < XR; ++r) {
+                const int gy = y0 - 2 + r;
+                if (!valid_row(gy)) continue;
+                pipe::bulk_g2s(xs + ((size_t)q * XR + r) * nx, xin + lin(d, 0, wrapi(gy, d.ny), gz), row_bytes, &bars[q]);
             }
-            pl[hy][hx] = val;
-        }
-    };
-    auto load_b = [&](int z) {
-        const int zz = wrapi(z, d.nz);
-        T(*pl)[FX + 2] = bpl[((z % 2) + 2) % 2];
-        for (int e = tid; e < (FX + 2) * (FY + 2); e += FX * FY) {
-            const int hx = e % (FX + 2), hy = e / (FX + 2);
-            const int gx = wrapi(x0 + hx - 1, d.nx);
-            int gy = y0 + hy - 1;
-            T val = T(0);
-            if (d.channel) {
-                if (gy >= 0 && gy < d.ny) val = b[lin(d, gx, gy, zz)];
-            } else {
-                val = b[lin(d, gx, wrapi(gy, d.ny), zz)];
+            for (int r = 0; r < BR; ++r) {
+                const int gy = y0 - 1 + r;
+                if (!valid_row(gy)) continue;
+                pipe::bulk_g2s(bs + ((size_t)q * BR + r) * nx, b + lin(d, 0, wrapi(gy, d.ny), gz), row_bytes, &bars[q]);
             }
-            pl[hy][hx] = val;
+        };
+        // prefetch: planes pfirst .. pfirst + R - 2 (the last slot fills at the end of the first step)
+        int next = pfirst;
+        if (tid == 0) {
+            pipe::fence_proxy_async();
+            for (; next <= plast && next <= pfirst + R - 2; ++next) issue(next);
         }
-    };
-    // Gauss-Seidel update of the cell at ring coordinates (hx, hy) of plane z
-    auto update = [&](int z, int hx, int hy, T bval) {
-        T(*c0)[HX] = ring[((z % 4) + 4) % 4];
-        T(*cm)[HX] = ring[(((z - 1) % 4) + 4) % 4];
-        T(*cp)[HX] = ring[(((z + 1) % 4) + 4) % 4];
-        T S = (c0[hy][hx - 1] + c0[hy][hx + 1]) + (cm[hy][hx] + cp[hy][hx]);
-        T c = T(6);
-        if (d.channel) {
-            const int gy = y0 + hy - 2;
-            if (gy > 0) S += c0[hy - 1][hx]; else c -= T(1);
-            if (gy < d.ny - 1) S += c0[hy + 1][hx]; else c -= T(1);
-        } else {
-            S += c0[hy - 1][hx] + c0[hy + 1][hx];
-        }
-        const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
-        c0[hy][hx] = (S - bval * inv) * rc;
-    };
-    load_x(z0 - 2);
-    load_x(z0 - 1);
-    load_x(z0);
-    for (int k = z0 - 1; k <= zend; ++k) {
-        load_x(k + 1);
-        load_b(k);
-        __syncthreads();
-        // red cells of plane k on the tile + 1-cell halo
-        {
-            T(*bk)[FX + 2] = bpl[((k % 2) + 2) % 2];
-            for (int e = tid; e < (FX + 2) * (FY + 2); e += FX * FY) {
-                const int ex = e % (FX + 2), ey = e / (FX + 2);
-                const int gx = x0 + ex - 1, gy = y0 + ey - 1;
-                if (d.channel && (gy < 0 || gy >= d.ny)) continue;
-                if (((wrapi(gx, d.nx) + wrapi(gy, d.ny) + wrapi(k, d.nz)) & 1) != 0) continue;
-                update(k, ex + 1, ey + 1, bk[ey][ex]);
-            }
-        }
-        __syncthreads();
-        // black cells of plane k-1 on the tile, then write plane k-1
-        if (k - 1 >= z0 && k - 1 < zend) {
-            const int zb = k - 1;
-            T(*bk)[FX + 2] = bpl[((zb % 2) + 2) % 2];
-            const int lx = threadIdx.x, ly = threadIdx.y;
-            const int gx = x0 + lx, gy = y0 + ly;
-            if (gx < d.nx && gy < d.ny && (((gx + gy + zb) & 1) != 0)) update(zb, lx + 2, ly + 2, bk[ly + 1][lx + 1]);
+        bool ok = true;
+        // planes k-1 and k of the first step
+        ok = pipe::mbar_wait(&bars[slot(pfirst)], parity(pfirst), pipe::kWaitCycles) &&
+             pipe::mbar_wait(&bars[slot(pfirst + 1)], parity(pfirst + 1), pipe::kWaitCycles);
+        for (int k = z0 - 1; k <= zend; ++k) {
+            if (ok) ok = pipe::mbar_wait(&bars[slot(k + 1)], parity(k + 1), pipe::kWaitCycles);
+            if (!ok) s_abort = 1;
             __syncthreads();
-            if (gx < d.nx && gy < d.ny) xout[lin(d, gx, gy, zb)] = ring[((zb % 4) + 4) % 4][ly + 2][lx + 2];
+            if (s_abort) break;
+            // red cells of plane k, rows tile +- 1
+            {
+                const int gz = wrapi(k, d.nz);
+                for (int e = tid; e < (FY + 2) * hx; e += NT) {
+                    const int rr = e / hx, gy = y0 - 1 + rr;
+                    if (!valid_row(gy)) continue;
+                    const int wy = wrapi(gy, d.ny);
+                    const int xi = 2 * (e - rr * hx) + ((wy + gz) & 1);
+                    const int lr = rr + 1;
+                    T* c0 = xrow(k, lr);
+                    const int xm = xi == 0 ? nx - 1 : xi - 1, xp = xi == nx - 1 ? 0 : xi + 1;
+                    T S = (c0[xm] + c0[xp]) + (xrow(k - 1, lr)[xi] + xrow(k + 1, lr)[xi]);
+                    T c = T(6);
+                    if (d.channel) {
+                        if (gy > 0) S += xrow(k, lr - 1)[xi]; else c -= T(1);
+                        if (gy < d.ny - 1) S += xrow(k, lr + 1)[xi]; else c -= T(1);
+                    } else {
+                        S += xrow(k, lr - 1)[xi] + xrow(k, lr + 1)[xi];
+                    }
+                    const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
+                    c0[xi] = (S - brow(k, rr)[xi] * inv) * rc;
+                }
+            }
+            __syncthreads();
+            const int kb = k - 1;
+            if (kb >= z0) {
+                // black cells of plane k-1 on the tile
+                const int gz = wrapi(kb, d.nz);
+                for (int e = tid; e < FY * hx; e += NT) {
+                    const int rr = e / hx, gy = y0 + rr;
+                    const int xi = 2 * (e - rr * hx) + ((gy + gz + 1) & 1);
+                    const int lr = rr + 2;
+                    T* c0 = xrow(kb, lr);
+                    const int xm = xi == 0 ? nx - 1 : xi - 1, xp = xi == nx - 1 ? 0 : xi + 1;
+                    T S = (c0[xm] + c0[xp]) + (xrow(kb - 1, lr)[xi] + xrow(kb + 1, lr)[xi]);
+                    T c = T(6);
+                    if (d.channel) {
+                        if (gy > 0) S += xrow(kb, lr - 1)[xi]; else c -= T(1);
+                        if (gy < d.ny - 1) S += xrow(kb, lr + 1)[xi]; else c -= T(1);
+                    } else {
+                        S += xrow(kb, lr - 1)[xi] + xrow(kb, lr + 1)[xi];
+                    }
+                    const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
+                    c0[xi] = (S - brow(kb, rr + 1)[xi] * inv) * rc;
+                }
+            }
+            // order this step's shared-memory accesses before the bulk copy that refills a slot
+            pipe::fence_proxy_async();
+            __syncthreads();
+            if (kb >= z0) {
+                // plane k-1 of the tile is final
+                for (int e = tid; e < FY * nx; e += NT) {
+                    const int rr = e / nx, xi = e - rr * nx;
+                    xout[lin(d, xi, y0 + rr, kb)] = xrow(kb, rr + 2)[xi];
+                }
+            }
+            // the slot of plane k-2 is free (its last reader, the black update, is behind the barrier)
+            if (tid == 0 && next <= plast) {
+                pipe::fence_proxy_async();
+                issue(next);
+                ++next;
+            }
         }
+        if (s_abort) {
+            // leave no copy in flight: wait (bounded) for every plane issued so far
+            if (tid == 0) {
+                atomicOr(err, 1);
+                for (int p = pfirst; p < next; ++p) pipe::mbar_wait(&bars[slot(p)], parity(p), pipe::kWaitCycles);
+            }
+            return;
+        }
+        base += plast - pfirst + 1;
         __syncthreads();
     }
 }
@@ -411,11 +494,60 @@ void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s) {
     k_rbgs<T><<<g, dim3(BX, BY), 0, s>>>(d, color, x, b);
 }
 template <typename T>
-void launch_rbgs_fused(const Dims& d, const T* xin, T* xout, const T* b, cudaStream_t s) {
-    dim3 g((d.nx + FX - 1) / FX, (d.ny + FY - 1) / FY, (d.nz + FZ - 1) / FZ);
-    k_rbgs_fused<T><<<g, dim3(FX, FY), 0, s>>>(d, xin, xout, b);
+PipeCfg rbgs_pipe_cfg(const Dims& d) {
+    PipeCfg c;
+    const size_t row = (size_t)d.nx * sizeof(T);
+    if (d.nz < 2 || d.nx < 32 || (d.nx & 1) || row % 16 != 0) return c;
+    constexpr size_t kMaxSmem = 200 * 1024;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_rbgs_pipe<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem) !=
+            cudaSuccess)
+            return c;
+        attr = true;
+    }
+    for (int fy : {4, 2, 1}) {
+        if (d.ny % fy) continue;
+        for (int dd = 4; dd >= 2; --dd) {
+            const size_t smem = 128 + (size_t)(dd + 4) * (2 * fy + 6) * row;
+            if (smem <= kMaxSmem) {
+                c.FY = fy;
+                c.D = dd;
+                c.smem = smem;
+                break;
+            }
+        }
+        if (c.FY) break;
+    }
+    if (!c.FY) return c;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_pipe<T>, 256, c.smem);
+    if (sms <= 0 || per_sm <= 0) {
+        c.FY = 0;
+        return c;
+    }
+    const int resident = sms * per_sm;
+    // z chunk: the longest (least redundant halo) that still gives each
+    // resident block three or more items
+    const int strips = d.ny / c.FY;
+    c.ZC = 0;
+    for (int zc : {32, 16, 8}) {  // largest first; the smallest dividing one if none reaches 3 items
+        if (d.nz % zc) continue;
+        c.ZC = zc;
+        if ((long long)strips * (d.nz / zc) >= 3LL * resident) break;
+    }
+    if (!c.ZC) c.ZC = d.nz;  // short z extents: one chunk
+    const int items = strips * (d.nz / c.ZC);
+    c.grid = items < resident ? items : resident;
+    return c;
 }
-bool rbgs_fused_ok(const Dims& d) { return d.nx >= FX && d.ny >= FY && d.nz >= FZ; }
+
+template <typename T>
+void launch_rbgs_pipe(const Dims& d, const PipeCfg& c, const T* xin, T* xout, const T* b, int* err, cudaStream_t s) {
+    k_rbgs_pipe<T><<<c.grid, 256, c.smem, s>>>(d, xin, xout, b, c.FY, c.ZC, c.D, err);
+}
 
 template <typename T>
 void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s) {
@@ -448,7 +580,8 @@ void launch_coarse_solve(const Dims& d, T* x, T* b, T* r, T* p, T* q, double tol
     template void launch_lap_apply<T>(const Dims&, T*, const T*, cudaStream_t);                          \
     template void launch_residual<T>(const Dims&, T*, const T*, const T*, RedScratch*, double*, cudaStream_t); \
     template void launch_rbgs<T>(const Dims&, int, T*, const T*, cudaStream_t);                          \
-    template void launch_rbgs_fused<T>(const Dims&, const T*, T*, const T*, cudaStream_t);               \
+    template PipeCfg rbgs_pipe_cfg<T>(const Dims&);                                                      \
+    template void launch_rbgs_pipe<T>(const Dims&, const PipeCfg&, const T*, T*, const T*, int*, cudaStream_t); \
     template void launch_restrict<T>(const Dims&, T*, const T*, cudaStream_t);                           \
     template void launch_prolong_add<T>(const Dims&, T*, const T*, cudaStream_t);                        \
     template void launch_prolong_assign<T>(const Dims&, T*, const T*, cudaStream_t);                     \

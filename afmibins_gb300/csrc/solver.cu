@@ -25,7 +25,8 @@ template <typename T>
 struct MGLevelT {
     Dims d;
     T *x, *b, *r;
-    T* x2;  // ping-pong partner of x for the tile-fused sweep (null on small levels)
+    T* x2;       // ping-pong partner of x for the pipelined sweep (null where it does not apply)
+    PipeCfg pc;  // pipelined-sweep launch shape (pc.FY == 0: per-colour launches)
 };
 typedef MGLevelT<double> MGLevel;
 
@@ -57,7 +58,8 @@ struct afmib_solver {
     std::vector<MGLevelT<float>> lv32;
     double *cx64 = nullptr, *cb64 = nullptr, *cr64 = nullptr;
     int inner_cycles = 3;
-    bool fused_smoother = false;  // tile-fused sweep: opt-in (AFMIB_SMOOTHER=fused) until its z-march is pipelined
+    bool pipe_smoother = true;  // pipelined red-black sweeps where a level allows (AFMIB_SMOOTHER=percolour: off)
+    int pipe_min_nx = 64;       // smaller levels keep the per-colour launches (AFMIB_PIPE_MIN_NX)
     // V-cycle blocks captured once into CUDA graphs and replayed (no host
     // interaction inside a V-cycle); not used while per-kernel profiling is on
     bool use_graphs = true;
@@ -336,16 +338,16 @@ int smooth(afmib_solver* s, MGLevelT<T>& L, int sweeps) {
     const double Ns = (double)L.d.ncell() * sizeof(T);
     const int id = L.d.nx == s->d.nx ? P_RBGS0 : P_RBGS;  // finest level kept apart in the profile
     int j = 0;
-    if (L.x2 && s->fused_smoother) {
-        // pairs of tile-fused sweeps, x -> x2 -> x
+    if (L.x2 && s->pipe_smoother && L.pc.FY) {
+        // pairs of pipelined sweeps, x -> x2 -> x
         for (; j + 2 <= sweeps; j += 2) {
             {
                 ProfScope ps(s, id, 3 * Ns);
-                launch_rbgs_fused<T>(L.d, L.x, L.x2, L.b, s->st);
+                launch_rbgs_pipe<T>(L.d, L.pc, L.x, L.x2, L.b, s->dflag + 3, s->st);
             }
             {
                 ProfScope ps(s, id, 3 * Ns);
-                launch_rbgs_fused<T>(L.d, L.x2, L.x, L.b, s->st);
+                launch_rbgs_pipe<T>(L.d, L.pc, L.x2, L.x, L.b, s->dflag + 3, s->st);
             }
         }
     }
@@ -520,7 +522,9 @@ int mg_solve(afmib_solver* s, int* cycles) {
         }
     }
     CK(cudaMemcpyAsync(s->hflag + 1, s->dflag + 1, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaMemcpyAsync(s->hflag + 3, s->dflag + 3, sizeof(int), cudaMemcpyDeviceToHost, s->st));
     TRY(sync(s));
+    if (s->hflag[3] != 0) return s->fail(AFMIB_ERR_CUDA, "pipelined smoother: a row copy did not complete in time");
     if (status == AFMIB_OK && s->hflag[1] != 0) status = s->fail(AFMIB_ERR_NOCONV, "coarsest-level CG did not converge");
     s->stats.mg_cycles += c;
     if (cycles) *cycles = c;
@@ -632,7 +636,9 @@ int mg_solve_mixed(afmib_solver* s, int* cycles) {
         ++outer;
     }
     CK(cudaMemcpyAsync(s->hflag + 1, s->dflag + 1, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaMemcpyAsync(s->hflag + 3, s->dflag + 3, sizeof(int), cudaMemcpyDeviceToHost, s->st));
     TRY(sync(s));
+    if (s->hflag[3] != 0) return s->fail(AFMIB_ERR_CUDA, "pipelined smoother: a row copy did not complete in time");
     if (status == AFMIB_OK && s->hflag[1] != 0) status = s->fail(AFMIB_ERR_NOCONV, "coarsest-level CG did not converge");
     s->stats.mg_cycles += c;
     s->stats.outer_iters += outer;
@@ -1270,7 +1276,8 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     s->mixed = g.precision == AFMIB_MIXED;
     s->spread64 = s->mixed && !(g.ib_fp32 & 1);
     s->interp64 = s->mixed && !(g.ib_fp32 & 2);
-    if (const char* e = std::getenv("AFMIB_SMOOTHER")) s->fused_smoother = std::string(e) == "fused";
+    if (const char* e = std::getenv("AFMIB_SMOOTHER")) s->pipe_smoother = std::string(e) != "percolour";
+    if (const char* e = std::getenv("AFMIB_PIPE_MIN_NX")) s->pipe_min_nx = std::atoi(e);
     if (const char* e = std::getenv("AFMIB_GRAPHS")) s->use_graphs = std::string(e) != "0";
     if (g.proj_start < AFMIB_START_DEFAULT || g.proj_start > AFMIB_START_WARM)
         return s->fail(AFMIB_ERR_ARG, "proj_start must be AFMIB_START_DEFAULT, _ZERO or _WARM");
@@ -1344,7 +1351,8 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
         TRY(dalloc(s, &L.x, n));
         TRY(dalloc(s, &L.b, n));
         TRY(dalloc(s, &L.r, n));
-        if (rbgs_fused_ok(t)) TRY(dalloc(s, &L.x2, n));
+        if (s->pipe_smoother && t.nx >= s->pipe_min_nx) L.pc = rbgs_pipe_cfg<double>(t);
+        if (L.pc.FY) TRY(dalloc(s, &L.x2, n));
         s->lv.push_back(L);
     }
     // smoothed levels need even extents for the red-black colouring
@@ -1378,7 +1386,8 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
             TRY(dalloc(s, &F.x, L.d.ncell()));
             TRY(dalloc(s, &F.b, L.d.ncell()));
             TRY(dalloc(s, &F.r, L.d.ncell()));
-            if (rbgs_fused_ok(L.d)) TRY(dalloc(s, &F.x2, L.d.ncell()));
+            if (s->pipe_smoother && L.d.nx >= s->pipe_min_nx) F.pc = rbgs_pipe_cfg<float>(L.d);
+            if (F.pc.FY) TRY(dalloc(s, &F.x2, L.d.ncell()));
             s->lv32.push_back(F);
         }
         TRY(dalloc(s, &s->cx64, nc));
@@ -1396,6 +1405,13 @@ int refresh_shadow(afmib_solver* s) {
     launch_convert<float, double>(s->N(), s->v32, s->v, s->st);
     launch_convert<float, double>(s->N(), s->w32, s->w, s->st);
     CKL();
+    return AFMIB_OK;
+}
+
+int check_smoother_flag(afmib_solver* s) {
+    CK(cudaMemcpyAsync(s->hflag + 3, s->dflag + 3, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    TRY(sync(s));
+    if (s->hflag[3] != 0) return s->fail(AFMIB_ERR_CUDA, "pipelined smoother: a row copy did not complete in time");
     return AFMIB_OK;
 }
 
@@ -1636,7 +1652,7 @@ int afmib_advection(afmib_solver* s, double* ua, double* va, double* wa, const d
 int afmib_mg_solve(afmib_solver* s, double* rhs, int* cycles) {
     if (!s || !rhs) return AFMIB_ERR_ARG;
     TRY(copy_in(s, s->lv[0].b, rhs, s->N()));
-    const int rc = mg_solve(s, cycles);
+    const int rc = s->mixed ? mg_solve_mixed(s, cycles) : mg_solve(s, cycles);
     TRY(copy_out(s, rhs, s->lv[0].x, s->N()));
     TRY(sync(s));
     return rc;
@@ -1757,11 +1773,18 @@ int afmib_smooth(afmib_solver* s, double* x, const double* b) {
     MGLevel& L = s->lv[0];
     TRY(copy_in(s, L.x, x, s->N()));
     TRY(copy_in(s, L.b, b, s->N()));
-    launch_rbgs<double>(L.d, 0, L.x, L.b, s->st);
-    launch_rbgs<double>(L.d, 1, L.x, L.b, s->st);
+    double* out = L.x;
+    if (L.x2 && s->pipe_smoother && L.pc.FY) {
+        launch_rbgs_pipe<double>(L.d, L.pc, L.x, L.x2, L.b, s->dflag + 3, s->st);
+        out = L.x2;
+    } else {
+        launch_rbgs<double>(L.d, 0, L.x, L.b, s->st);
+        launch_rbgs<double>(L.d, 1, L.x, L.b, s->st);
+    }
     CKL();
-    TRY(copy_out(s, x, L.x, s->N()));
-    return sync(s);
+    TRY(copy_out(s, x, out, s->N()));
+    TRY(sync(s));
+    return check_smoother_flag(s);
 }
 
 int afmib_set_spring(afmib_solver* s, double k) {

@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--profile-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--case", choices=["ib", "mg"], default="ib",
+                    help="ib: the IB step (the headline); mg: pressure multigrid solves alone on a seeded right-hand "
+                         "side (a small, single-kernel-family target for profilers)")
     ap.add_argument("--cpu-sample-n", type=int, default=64,
                     help="grid of the CPU sample (the workload at reduced resolution, scaled by the cell count)")
     return ap.parse_args()
@@ -225,6 +228,40 @@ def run_form(capi, torch, args, prec, state, dev, stream, proj_start=0):
     return sv, e0.elapsed_time(e1), sv.stats()["kernel_launches"] - l0, clk.summary(), wall
 
 
+def run_mg_case(args, torch, local):
+    """Pressure multigrid solves L x = b - mean(b) to the tolerance from zero,
+    on a seeded right-hand side, in the chosen precision; one JSON line."""
+    from afmibins_gb300 import capi
+    n = args.n
+    prec = capi.FP64 if args.precision == "fp64" else capi.MIXED
+    rhs = np.random.default_rng(20261203).standard_normal(n ** 3)
+    rhs -= rhs.mean()
+    stream = torch.cuda.Stream()
+    dev = torch.device("cuda", local)
+    bd = torch.from_numpy(rhs).to(dev)
+    xd = torch.empty_like(bd)
+    with capi.Solver(n, precision=prec, tol=args.tol, stream=stream.cuda_stream) as sv:
+        cycles = 0
+        for _ in range(args.warmup):
+            xd.copy_(bd)
+            torch.cuda.synchronize()
+            _, cycles = sv.mg_solve_device(xd)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ms = 0.0
+        for _ in range(args.steps):
+            xd.copy_(bd)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            _, cycles = sv.mg_solve_device(xd)
+            e1.record(stream)
+            stream.synchronize()
+            ms += e0.elapsed_time(e1)
+    print(json.dumps({"metric": "multigrid pressure solves/s", "case": "mg", "value": args.steps / (ms / 1000.0),
+                      "unit": "solves/s", "ms_per_solve": ms / args.steps, "cycles_per_solve": cycles,
+                      "precision": args.precision, "config": {"grid": n, "tol": args.tol}}))
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -236,6 +273,9 @@ def main():
 
     import torch
     torch.cuda.set_device(local)
+    if args.case == "mg":
+        run_mg_case(args, torch, local)
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist

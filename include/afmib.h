@@ -155,7 +155,8 @@ int afmib_grad(afmib_solver* s, double* px, double* py, double* pz, const double
 int afmib_advection(afmib_solver* s, double* ua, double* va, double* wa, const double* u, const double* v,
                     const double* w);
 /* mg::solver<G>::solve(rhs): rhs is overwritten by the solution, returns the
- * V-cycle count in *cycles, src/mg/solver.h:218-237 */
+ * V-cycle count in *cycles, src/mg/solver.h:218-237. A mixed-precision solver
+ * solves by FP64 defect correction around FP32 V-cycles to the same RMS stop. */
 int afmib_mg_solve(afmib_solver* s, double* rhs, int* cycles);
 /* mg::solver::L * x, src/mg/laplacian.h:46-153 */
 int afmib_lap_apply(afmib_solver* s, double* y, const double* x);
