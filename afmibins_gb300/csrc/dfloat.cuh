@@ -13,7 +13,23 @@
 // rounding four or more orders below the solver tolerances (1e-10).
 #pragma once
 
+#include <cstdint>
+#include <cstring>
+
 namespace afmib {
+
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ long long dbits(double d) { return __double_as_longlong(d); }
+__device__ __forceinline__ float fbits(unsigned u) { return __int_as_float((int)u); }
+__device__ __forceinline__ unsigned fword(float f) { return (unsigned)__float_as_int(f); }
+__device__ __forceinline__ int clz64(unsigned long long v) { return __clzll((long long)v); }
+#else
+inline long long dbits(double d) { long long u; std::memcpy(&u, &d, 8); return u; }
+inline float fbits(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
+inline unsigned fword(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
+inline int clz64(unsigned long long v) { return v ? __builtin_clzll(v) : 64; }
+#endif
+#define AFMIB_HD __host__ __device__ __forceinline__
 
 struct df2 {
     float hi, lo;
@@ -22,8 +38,8 @@ struct df2 {
 // hi = the top 24 significant bits of d (truncated), lo = the next 23, both
 // with d's sign; |d| < 2^-126 (float subnormal range and zero) gives 0, and
 // lo is dropped below 2^-80. No FP64 instruction is issued.
-__device__ __forceinline__ df2 df_split(double d) {
-    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+AFMIB_HD df2 df_split(double d) {
+    const unsigned long long u = (unsigned long long)dbits(d);
     const unsigned hw = (unsigned)(u >> 32), lw = (unsigned)u;
     const unsigned sign = hw & 0x80000000u;
     const int e = (int)((hw >> 20) & 0x7ffu) - 1023;
@@ -36,24 +52,24 @@ __device__ __forceinline__ df2 df_split(double d) {
         return r;
     }
     if (e > 127) {  // beyond the float range (and inf / nan): keep inf or nan
-        r.hi = __int_as_float(sign | 0x7f800000u | (mh ? 0x400000u : 0u));
+        r.hi = fbits(sign | 0x7f800000u | (mh ? 0x400000u : 0u));
         r.lo = 0.f;
         return r;
     }
-    r.hi = __int_as_float(sign | ((unsigned)(e + 127) << 23) | mh);
+    r.hi = fbits(sign | ((unsigned)(e + 127) << 23) | mh);
     const int el = e - 46;  // lo = ml * 2^(e - 46)
     if (el < -126 || ml == 0u) {
         r.lo = 0.f;
         return r;
     }
-    const float m = __int_as_float(0x4B000000u | ml) - 8388608.0f;  // ml as a float, exactly
-    const float sc = __int_as_float((unsigned)(el + 127) << 23);     // 2^el
-    r.lo = __int_as_float(__float_as_int(m * sc) | sign);
+    const float m = fbits(0x4B000000u | ml) - 8388608.0f;  // ml as a float, exactly
+    const float sc = fbits((unsigned)(el + 127) << 23);     // 2^el
+    r.lo = fbits(fword(m * sc) | sign);
     return r;
 }
 
 // a + b with both pairs' rounding errors carried (accurate under cancellation)
-__device__ __forceinline__ df2 df_add(df2 a, df2 b) {
+AFMIB_HD df2 df_add(df2 a, df2 b) {
     float s = a.hi + b.hi;
     float v = s - a.hi;
     float e = (a.hi - (s - v)) + (b.hi - v);
@@ -70,13 +86,13 @@ __device__ __forceinline__ df2 df_add(df2 a, df2 b) {
     return r;
 }
 
-__device__ __forceinline__ df2 df_neg(df2 a) {
+AFMIB_HD df2 df_neg(df2 a) {
     a.hi = -a.hi;
     a.lo = -a.lo;
     return a;
 }
 
-__device__ __forceinline__ df2 df_mul(df2 a, df2 b) {
+AFMIB_HD df2 df_mul(df2 a, df2 b) {
     const float p = a.hi * b.hi;
     float e = fmaf(a.hi, b.hi, -p);
     e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
@@ -86,6 +102,105 @@ __device__ __forceinline__ df2 df_mul(df2 a, df2 b) {
     return r;
 }
 
-__device__ __forceinline__ float df_to_float(df2 a) { return a.hi + a.lo; }
+AFMIB_HD float df_to_float(df2 a) { return a.hi + a.lo; }
+
+// ---------------------------------------------------------------------------
+// Per-cell block floating point. The FP64 values of one stencil are taken to
+// int64 at a common scale set by the largest exponent E among them (biased):
+// value = q * 2^(E - 1078), so |q| < 2^56 and sums of up to 64 such terms
+// cannot overflow. Sums and differences are then exact; a value smaller than
+// the largest by more than 2^56 loses its bits below that resolution, which
+// is 2^-55 of the largest value. Results go back to df pairs (48 bits).
+// Zero and FP64 subnormals read as zero. No FP64 instruction is issued.
+// ---------------------------------------------------------------------------
+AFMIB_HD int bexp(double v) { return (int)(((unsigned long long)dbits(v) >> 52) & 0x7ffu); }
+
+AFMIB_HD long long to_fixed(double v, int E) {
+    const unsigned long long u = (unsigned long long)dbits(v);
+    const int e = (int)((u >> 52) & 0x7ffu);
+    if (e == 0) return 0;
+    const unsigned long long m = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = e - E + 3;  // <= 3
+    unsigned long long q;
+    if (sh >= 0) q = m << sh;
+    else if (sh > -64) q = m >> (-sh);
+    else q = 0;
+    return (u >> 63) ? -(long long)q : (long long)q;
+}
+
+// a float with the 24 leading bits of a (a > 0, top bit at position p) times 2^x
+AFMIB_HD float lead24(unsigned long long a, int p, int x) {
+    const unsigned long long h = p >= 23 ? (a >> (p - 23)) : (a << (23 - p));
+    const int fe = p + x + 127;
+    if (fe < 1) return 0.f;  // below the float normal range: negligible here
+    if (fe > 254) return fbits(0x7f800000u);
+    return fbits(((unsigned)fe << 23) | ((unsigned)h & 0x7fffffu));
+}
+
+// q * 2^(E - 1078) as a df pair (hi: 24 leading bits, lo: the next 24)
+AFMIB_HD df2 from_fixed(long long q, int E) {
+    df2 r;
+    r.hi = 0.f;
+    r.lo = 0.f;
+    if (q == 0) return r;
+    const bool neg = q < 0;
+    const unsigned long long a = neg ? (unsigned long long)(-q) : (unsigned long long)q;
+    const int x = E - 1078;
+    const int p = 63 - clz64(a);
+    r.hi = lead24(a, p, x);
+    if (p > 23) {
+        const unsigned long long rem = a & ((1ull << (p - 23)) - 1ull);
+        if (rem) r.lo = lead24(rem, 63 - clz64(rem), x);
+    }
+    if (neg) {
+        r.hi = -r.hi;
+        r.lo = -r.lo;
+    }
+    return r;
+}
+
+// v * 2^-k by exponent arithmetic (exact; 0 below the FP64 normal range)
+AFMIB_HD double scale_pow2_down(double v, int k) {
+    long long u = dbits(v);
+    const int e = (int)(((unsigned long long)u >> 52) & 0x7ffu);
+    if (e == 0 || k == 0) return v;
+    if (e - k < 1) return 0.0 * v;
+    u -= (long long)k << 52;
+    double r;
+#if defined(__CUDA_ARCH__)
+    r = __longlong_as_double(u);
+#else
+    std::memcpy(&r, &u, 8);
+#endif
+    return r;
+}
+
+// Mixed-form residual at one cell, r = b - (x0 + f * Q), Q an exact integer
+// combination of the stencil values: Q = sum_i cnb[i] * nb[i] + coef0 * x0,
+// f the operator's scale as a df pair. Returns r rounded to float.
+AFMIB_HD float helm_residual_bfp(double b, double x0, const double* nb, const int* cnb, int nnb, int coef0, df2 f) {
+    int E = bexp(b) > bexp(x0) ? bexp(b) : bexp(x0);
+    for (int i = 0; i < nnb; ++i) E = bexp(nb[i]) > E ? bexp(nb[i]) : E;
+    const long long q0 = to_fixed(x0, E);
+    long long Q = (long long)coef0 * q0;
+    for (int i = 0; i < nnb; ++i) Q += (long long)cnb[i] * to_fixed(nb[i], E);
+    const long long Db = to_fixed(b, E) - q0;
+    const df2 r = df_add(from_fixed(Db, E), df_neg(df_mul(f, from_fixed(Q, E))));
+    return df_to_float(r);
+}
+
+// Laplacian residual r = b - n^2 (sum(nb) - c x0) with n^2 = 2^k2: b is
+// brought to the stencil's scale exactly (b 2^-k2), the whole combination
+// Q = b 2^-k2 - sum(nb) + c x0 is exact, and r = 2^k2 Q.
+AFMIB_HD float lap_residual_bfp(double b, double x0, const double* nb, int nnb, int c, int k2) {
+    const double bs = scale_pow2_down(b, k2);
+    int E = bexp(bs) > bexp(x0) ? bexp(bs) : bexp(x0);
+    for (int i = 0; i < nnb; ++i) E = bexp(nb[i]) > E ? bexp(nb[i]) : E;
+    long long Q = to_fixed(bs, E) + (long long)c * to_fixed(x0, E);
+    for (int i = 0; i < nnb; ++i) Q -= to_fixed(nb[i], E);
+    const df2 q = from_fixed(Q, E);
+    const float sc = fbits((unsigned)(k2 + 127) << 23);  // 2^k2, k2 <= 126
+    return (q.hi + q.lo) * sc;
+}
 
 }  // namespace afmib

@@ -169,9 +169,10 @@ __global__ void __launch_bounds__(256) k_rbgs_pipe(Dims d, const T* __restrict__
     const int R = D + 4;
     const int nx = d.nx, XR = FY + 4, BR = FY + 2;
     const unsigned row_bytes = (unsigned)(nx * sizeof(T));
+    const int xplane = XR * nx, bplane = BR * nx;
     unsigned long long* bars = (unsigned long long*)smem;  // R <= 16 barriers in the first 128 bytes
     T* xs = (T*)(smem + 128);                              // [R][XR][nx]
-    T* bs = xs + (size_t)R * XR * nx;                      // [R][BR][nx]
+    T* bs = xs + (size_t)R * xplane;                       // [R][BR][nx]
     __shared__ int s_abort;
     const int tid = threadIdx.x, NT = blockDim.x;
     const int hx = nx >> 1;
@@ -183,92 +184,112 @@ __global__ void __launch_bounds__(256) k_rbgs_pipe(Dims d, const T* __restrict__
         s_abort = 0;
     }
     __syncthreads();
-    long long base = 0;  // planes issued by this block before the current item
+    // Slots are used round-robin in issue order and every thread waits on the
+    // planes in that same order, so a per-thread bit per slot tracks the
+    // barrier phase to wait for.
+    unsigned phase = 0u;
+    unsigned pending = 0u;  // thread 0: slots with a copy issued and not yet waited for
+    int s_first = 0;        // slot of the first plane of the current item
     auto valid_row = [&](int gy) { return !(d.channel && (gy < 0 || gy >= d.ny)); };
+    auto next_slot = [&](int q) { return q + 1 == R ? 0 : q + 1; };
+    auto prev_slot = [&](int q) { return q == 0 ? R - 1 : q - 1; };
+    auto wait_slot = [&](int q) {
+        const bool ok = pipe::mbar_wait(&bars[q], (phase >> q) & 1u, pipe::kWaitCycles);
+        if (ok) {
+            phase ^= 1u << q;
+            pending &= ~(1u << q);
+        }
+        return ok;
+    };
     for (int item = blockIdx.x; item < items; item += gridDim.x) {
         const int y0 = (item % nstrip) * FY, z0 = (item / nstrip) * ZC, zend = z0 + ZC;
         const int pfirst = z0 - 2, plast = zend + 1;
-        auto seq = [&](int p) { return base + (p - pfirst); };
-        auto slot = [&](int p) { return (int)(seq(p) % R); };
-        auto parity = [&](int p) { return (unsigned)((seq(p) / R) & 1); };
-        auto xrow = [&](int p, int lr) { return xs + ((size_t)slot(p) * XR + lr) * nx; };
-        auto brow = [&](int p, int lb) { return bs + ((size_t)slot(p) * BR + lb) * nx; };
-        auto issue = [&](int p) {  // thread 0
-            const int q = slot(p), gz = wrapi(p, d.nz);
+        auto issue = [&](int p, int q) {  // thread 0: plane p into slot q
+            const int gz = wrapi(p, d.nz);
             unsigned bytes = 0;
             for (int r = 0; r < XR; ++r) bytes += valid_row(y0 - 2 + r) ? row_bytes : 0u;
             for (int r = 0; r < BR; ++r) bytes += valid_row(y0 - 1 + r) ? row_bytes : 0u;
             pipe::mbar_expect_tx(&bars[q], bytes);
+            pending |= 1u << q;
             for (int r = 0; r < XR; ++r) {
                 const int gy = y0 - 2 + r;
                 if (!valid_row(gy)) continue;
-                pipe::bulk_g2s(xs + ((size_t)q * XR + r) * nx, xin + lin(d, 0, wrapi(gy, d.ny), gz), row_bytes, &bars[q]);
+                pipe::bulk_g2s(xs + (size_t)q * xplane + r * nx, xin + lin(d, 0, wrapi(gy, d.ny), gz), row_bytes,
+                               &bars[q]);
             }
             for (int r = 0; r < BR; ++r) {
                 const int gy = y0 - 1 + r;
                 if (!valid_row(gy)) continue;
-                pipe::bulk_g2s(bs + ((size_t)q * BR + r) * nx, b + lin(d, 0, wrapi(gy, d.ny), gz), row_bytes, &bars[q]);
+                pipe::bulk_g2s(bs + (size_t)q * bplane + r * nx, b + lin(d, 0, wrapi(gy, d.ny), gz), row_bytes,
+                               &bars[q]);
             }
         };
-        // prefetch: planes pfirst .. pfirst + R - 2 (the last slot fills at the end of the first step)
-        int next = pfirst;
+        // prefetch planes pfirst .. pfirst + R - 2; the last slot fills at the end of the first step
+        int next = pfirst, snext = s_first;
         if (tid == 0) {
             pipe::fence_proxy_async();
-            for (; next <= plast && next <= pfirst + R - 2; ++next) issue(next);
+            for (; next <= plast && next <= pfirst + R - 2; ++next, snext = next_slot(snext)) issue(next, snext);
         }
-        bool ok = true;
-        // planes k-1 and k of the first step
-        ok = pipe::mbar_wait(&bars[slot(pfirst)], parity(pfirst), pipe::kWaitCycles) &&
-             pipe::mbar_wait(&bars[slot(pfirst + 1)], parity(pfirst + 1), pipe::kWaitCycles);
+        // slots of planes k-1, k for the first step k = z0 - 1
+        int skm1 = s_first, sk = next_slot(s_first);
+        bool ok = wait_slot(skm1);
+        if (ok) ok = wait_slot(sk);
         for (int k = z0 - 1; k <= zend; ++k) {
-            if (ok) ok = pipe::mbar_wait(&bars[slot(k + 1)], parity(k + 1), pipe::kWaitCycles);
+            const int skp1 = next_slot(sk), skm2 = prev_slot(skm1);
+            if (ok) ok = wait_slot(skp1);
             if (!ok) s_abort = 1;
             __syncthreads();
             if (s_abort) break;
+            T* const Xm = xs + (size_t)skm1 * xplane;
+            T* const X0 = xs + (size_t)sk * xplane;
+            T* const Xp = xs + (size_t)skp1 * xplane;
             // red cells of plane k, rows tile +- 1
             {
                 const int gz = wrapi(k, d.nz);
+                const T* B0 = bs + (size_t)sk * bplane;
                 for (int e = tid; e < (FY + 2) * hx; e += NT) {
                     const int rr = e / hx, gy = y0 - 1 + rr;
                     if (!valid_row(gy)) continue;
                     const int wy = wrapi(gy, d.ny);
                     const int xi = 2 * (e - rr * hx) + ((wy + gz) & 1);
-                    const int lr = rr + 1;
-                    T* c0 = xrow(k, lr);
+                    const int o = (rr + 1) * nx;
+                    T* c0 = X0 + o;
                     const int xm = xi == 0 ? nx - 1 : xi - 1, xp = xi == nx - 1 ? 0 : xi + 1;
-                    T S = (c0[xm] + c0[xp]) + (xrow(k - 1, lr)[xi] + xrow(k + 1, lr)[xi]);
+                    T S = (c0[xm] + c0[xp]) + (Xm[o + xi] + Xp[o + xi]);
                     T c = T(6);
                     if (d.channel) {
-                        if (gy > 0) S += xrow(k, lr - 1)[xi]; else c -= T(1);
-                        if (gy < d.ny - 1) S += xrow(k, lr + 1)[xi]; else c -= T(1);
+                        if (gy > 0) S += c0[xi - nx]; else c -= T(1);
+                        if (gy < d.ny - 1) S += c0[xi + nx]; else c -= T(1);
                     } else {
-                        S += xrow(k, lr - 1)[xi] + xrow(k, lr + 1)[xi];
+                        S += c0[xi - nx] + c0[xi + nx];
                     }
                     const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
-                    c0[xi] = (S - brow(k, rr)[xi] * inv) * rc;
+                    c0[xi] = (S - B0[rr * nx + xi] * inv) * rc;
                 }
             }
             __syncthreads();
             const int kb = k - 1;
             if (kb >= z0) {
-                // black cells of plane k-1 on the tile
+                // black cells of plane k-1 on the tile (z neighbours: k-2 and k)
                 const int gz = wrapi(kb, d.nz);
+                T* const Ym = xs + (size_t)skm2 * xplane;
+                const T* B1 = bs + (size_t)skm1 * bplane;
                 for (int e = tid; e < FY * hx; e += NT) {
                     const int rr = e / hx, gy = y0 + rr;
                     const int xi = 2 * (e - rr * hx) + ((gy + gz + 1) & 1);
-                    const int lr = rr + 2;
-                    T* c0 = xrow(kb, lr);
+                    const int o = (rr + 2) * nx;
+                    T* c0 = Xm + o;
                     const int xm = xi == 0 ? nx - 1 : xi - 1, xp = xi == nx - 1 ? 0 : xi + 1;
-                    T S = (c0[xm] + c0[xp]) + (xrow(kb - 1, lr)[xi] + xrow(kb + 1, lr)[xi]);
+                    T S = (c0[xm] + c0[xp]) + (Ym[o + xi] + X0[o + xi]);
                     T c = T(6);
                     if (d.channel) {
-                        if (gy > 0) S += xrow(kb, lr - 1)[xi]; else c -= T(1);
-                        if (gy < d.ny - 1) S += xrow(kb, lr + 1)[xi]; else c -= T(1);
+                        if (gy > 0) S += c0[xi - nx]; else c -= T(1);
+                        if (gy < d.ny - 1) S += c0[xi + nx]; else c -= T(1);
                     } else {
-                        S += xrow(kb, lr - 1)[xi] + xrow(kb, lr + 1)[xi];
+                        S += c0[xi - nx] + c0[xi + nx];
                     }
                     const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
-                    c0[xi] = (S - brow(kb, rr + 1)[xi] * inv) * rc;
+                    c0[xi] = (S - B1[(rr + 1) * nx + xi] * inv) * rc;
                 }
             }
             // order this step's shared-memory accesses before the bulk copy that refills a slot
@@ -276,27 +297,32 @@ __global__ void __launch_bounds__(256) k_rbgs_pipe(Dims d, const T* __restrict__
             __syncthreads();
             if (kb >= z0) {
                 // plane k-1 of the tile is final
-                for (int e = tid; e < FY * nx; e += NT) {
-                    const int rr = e / nx, xi = e - rr * nx;
-                    xout[lin(d, xi, y0 + rr, kb)] = xrow(kb, rr + 2)[xi];
-                }
+                T* dst = xout + lin(d, 0, y0, kb);
+                const T* src = Xm + 2 * nx;
+                for (int e = tid; e < FY * nx; e += NT) dst[e] = src[e];
             }
             // the slot of plane k-2 is free (its last reader, the black update, is behind the barrier)
             if (tid == 0 && next <= plast) {
                 pipe::fence_proxy_async();
-                issue(next);
+                issue(next, snext);
                 ++next;
+                snext = next_slot(snext);
             }
+            skm1 = sk;
+            sk = skp1;
         }
         if (s_abort) {
-            // leave no copy in flight: wait (bounded) for every plane issued so far
+            // leave no copy in flight: wait (bounded) for every plane still outstanding
             if (tid == 0) {
                 atomicOr(err, 1);
-                for (int p = pfirst; p < next; ++p) pipe::mbar_wait(&bars[slot(p)], parity(p), pipe::kWaitCycles);
+                for (int q = 0; q < R; ++q)
+                    if ((pending >> q) & 1u) pipe::mbar_wait(&bars[q], (phase >> q) & 1u, pipe::kWaitCycles);
             }
             return;
         }
-        base += plast - pfirst + 1;
+        // the item used planes pfirst .. plast: the next item starts after them
+        const int used = plast - pfirst + 1;
+        s_first = (s_first + used) % R;
         __syncthreads();
     }
 }

@@ -1,0 +1,128 @@
+"""Host build of the block-floating-point residuals (afmibins_gb300/csrc/
+dfloat.cuh, the FP64-state residuals of the mixed form evaluated without FP64
+instructions) against exact rational arithmetic."""
+import ctypes
+import os
+import shutil
+import subprocess
+from fractions import Fraction as Fr
+
+import numpy as np
+import pytest
+
+from afmibins_gb300 import build
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    out = tmp_path_factory.mktemp("dfloat") / "libdfloat.so"
+    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-ffp-contract=off",
+                    "-I", os.path.join(build.PKG, "csrc"), os.path.join(HERE, "cpp", "dfloat_host.cc"),
+                    "-o", str(out)], check=True)
+    L = ctypes.CDLL(str(out))
+    dp, ip, fp = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)
+    L.afmib_test_helm_residual.argtypes = [ctypes.c_double, ctypes.c_double, dp, ip, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_double]
+    L.afmib_test_helm_residual.restype = ctypes.c_float
+    L.afmib_test_lap_residual.argtypes = [ctypes.c_double, ctypes.c_double, dp, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int]
+    L.afmib_test_lap_residual.restype = ctypes.c_float
+    L.afmib_test_split.argtypes = [ctypes.c_double, fp, fp]
+    L.afmib_test_fixed.argtypes = [ctypes.c_longlong, ctypes.c_int, fp, fp]
+    return L
+
+
+def _arr(a, t):
+    return (t * len(a))(*a)
+
+
+def test_split_keeps_47_bits(lib):
+    rng = np.random.default_rng(1)
+    hi, lo = ctypes.c_float(), ctypes.c_float()
+    for _ in range(3000):
+        d = float(rng.standard_normal() * 10.0 ** rng.uniform(-20, 20))
+        lib.afmib_test_split(d, ctypes.byref(hi), ctypes.byref(lo))
+        assert abs((Fr(hi.value) + Fr(lo.value)) - Fr(d)) <= abs(Fr(d)) * Fr(2) ** -46
+    lib.afmib_test_split(0.0, ctypes.byref(hi), ctypes.byref(lo))
+    assert hi.value == 0.0 and lo.value == 0.0
+
+
+def test_fixed_to_pair(lib):
+    rng = np.random.default_rng(2)
+    hi, lo = ctypes.c_float(), ctypes.c_float()
+    for _ in range(3000):
+        q = int(rng.integers(-(2 ** 61), 2 ** 61))
+        E = int(rng.integers(1000, 1100))
+        lib.afmib_test_fixed(q, E, ctypes.byref(hi), ctypes.byref(lo))
+        exact = Fr(q) * Fr(2) ** (E - 1078)
+        assert abs(Fr(hi.value) + Fr(lo.value) - exact) <= abs(exact) * Fr(2) ** -47
+
+
+def _helm_cases(rng, n):
+    for _ in range(n):
+        off = float(0.0066 * rng.uniform(0.2, 3.0))
+        x0 = float(0.3 + 0.1 * rng.standard_normal())
+        nb = [float(x0 + 1e-3 * rng.standard_normal()) for _ in range(6)]
+        exact_hx = Fr(x0) + Fr(off) * (sum(Fr(v) for v in nb) - 6 * Fr(x0))
+        b = float(exact_hx + Fr(float(10.0 ** rng.uniform(-16, -9) * rng.choice([-1, 1]))))
+        yield off, x0, nb, b
+
+
+def test_helm_residual_beats_fp64_formula(lib):
+    """Near convergence (|r| ~ 1e-16 .. 1e-9 against |x| ~ 0.3) the residual
+    from the block arithmetic carries only the float rounding of r itself,
+    below the rounding of the FP64 formula it replaces."""
+    rng = np.random.default_rng(3)
+    cnb = _arr([1] * 6, ctypes.c_int)
+    for off, x0, nb, b in _helm_cases(rng, 2000):
+        r = lib.afmib_test_helm_residual(b, x0, _arr(nb, ctypes.c_double), cnb, 6, -6, off)
+        exact = Fr(b) - (Fr(x0) + Fr(off) * (sum(Fr(v) for v in nb) - 6 * Fr(x0)))
+        err = abs(Fr(r) - exact)
+        M = max(abs(Fr(v)) for v in [b, x0] + nb)
+        # float rounding of r plus a few FP64 units of the largest value (each
+        # value truncates by at most 2^-55 of it at the block's scale; the FP64
+        # formula itself rounds at that order)
+        assert err <= abs(exact) * Fr(2) ** -23 + M * Fr(2) ** -50, (float(err), float(exact))
+
+
+def test_helm_residual_channel_wall_row(lib):
+    """Wall rows of the u/w Helmholtz operator: H x = x0 + (off/3)(3 sx + 3 sz + 4 x1 - 24 x0)."""
+    rng = np.random.default_rng(4)
+    cnb = _arr([3, 3, 3, 3, 4], ctypes.c_int)
+    for _ in range(1000):
+        off = float(0.0066 * rng.uniform(0.2, 3.0))
+        x0 = float(0.2 + 0.1 * rng.standard_normal())
+        nb = [float(x0 + 1e-3 * rng.standard_normal()) for _ in range(5)]
+        f = off / 3
+        exact_hx = Fr(x0) + Fr(f) * (sum(c * Fr(v) for c, v in zip([3, 3, 3, 3, 4], nb)) - 24 * Fr(x0))
+        b = float(exact_hx + Fr(1e-12))
+        r = lib.afmib_test_helm_residual(b, x0, _arr(nb, ctypes.c_double), cnb, 5, -24, f)
+        exact = Fr(b) - (Fr(x0) + Fr(f) * (sum(c * Fr(v) for c, v in zip([3, 3, 3, 3, 4], nb)) - 24 * Fr(x0)))
+        # the wall row does not annihilate constants (row sum 1 - 8 off / 3),
+        # so f Q is as large as x and carries f's pair rounding (2^-46)
+        fq = abs(Fr(f) * (sum(c * Fr(v) for c, v in zip([3, 3, 3, 3, 4], nb)) - 24 * Fr(x0)))
+        M = max(abs(Fr(v)) for v in [b, x0] + nb)
+        bound = abs(exact) * Fr(2) ** -23 + fq * Fr(2) ** -44 + M * Fr(2) ** -50
+        assert abs(Fr(r) - exact) <= bound
+
+
+def test_lap_residual(lib):
+    rng = np.random.default_rng(5)
+    n = 256
+    k2 = 16
+    for _ in range(2000):
+        x0 = float(1e-4 * rng.standard_normal())
+        nb = [float(x0 + 1e-6 * rng.standard_normal()) for _ in range(6)]
+        c = int(rng.choice([6, 5, 4]))
+        m = 6 if c == 6 else c
+        exact_l = Fr(n * n) * (sum(Fr(v) for v in nb[:m]) - c * Fr(x0))
+        b = float(exact_l + Fr(float(rng.standard_normal() * 1e-11)))
+        r = lib.afmib_test_lap_residual(b, x0, _arr(nb[:m], ctypes.c_double), m, c, k2)
+        exact = Fr(b) - exact_l
+        M = max([abs(Fr(b)) / (n * n)] + [abs(Fr(v)) for v in [x0] + nb[:m]])
+        assert abs(Fr(r) - exact) <= abs(exact) * Fr(2) ** -23 + n * n * M * Fr(2) ** -50
