@@ -102,6 +102,13 @@ void launch_residual(const Dims& d, T* r, const T* x, const T* b, RedScratch* sc
 // Mixed form: r = b - L x evaluated in FP64 (x, b FP64), stored as TD; out[0] = r.r
 template <typename TD>
 void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, RedScratch sc, double* out, cudaStream_t s);
+// The mixed form's FP64-state defects evaluated with int64 block arithmetic
+// and float pairs (no FP64 instruction; see dfloat.cuh). The Laplacian form
+// needs n a power of two and returns false (nothing launched) otherwise.
+bool launch_lap_defect_bfp(const Dims& d, float* r, const double* x, const double* b, RedScratch sc, double* out,
+                           cudaStream_t s);
+void launch_helm_defect_bfp(const Dims& d, int comp, double scale, const double* x, const double* b, float* r,
+                            RedScratch sc, double* out, cudaStream_t s);
 // One red (color 0) or black (color 1) Gauss-Seidel half sweep.
 template <typename T>
 void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s);

@@ -3,6 +3,7 @@
 // output element is produced by one thread from neighbours that the L1/L2
 // caches supply, so DRAM traffic is one read per input array and one write per
 // output array.
+#include "dfloat.cuh"
 #include "kernels.h"
 
 namespace afmib {
@@ -344,6 +345,55 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_defect(Dims d, int comp, dou
     grid_sum<1>(a, sc, out);
 }
 
+// The same defect without FP64 instructions: the stencil's FP64 values are
+// combined exactly in int64 at the cell's largest exponent and the small
+// results are scaled in float pairs (helm_residual_bfp). Rows follow
+// helm_point: interior (and 2D, and the channel v faces) H x = x0 + off Q
+// with Q = sum(nb) - k x0; channel u/w wall rows H x = x0 + (off/3) Q with
+// Q = 3 (sx + sz) + 4 x(y+-1) - 24 x0 (src/ns/helmholtz.h:90-104); the
+// channel v wall plane is the identity.
+__global__ void __launch_bounds__(kRedBlock) k_helm_defect_bfp(Dims d, int comp, double s, const double* __restrict__ x,
+                                                              const double* __restrict__ b, float* __restrict__ r,
+                                                              RedScratch sc, double* out) {
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+    const double off = s * (double)d.n * (double)d.n;
+    const df2 f1 = df_split(off), f3 = df_split(off / 3.0);
+    const int ones[6] = {1, 1, 1, 1, 1, 1}, wallc[5] = {3, 3, 3, 3, 4};
+    float acc = 0.f;
+    if (xi < d.nx && yi < d.ny)
+#pragma unroll 2
+        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
+            const long long i = lin(d, xi, yi, zi);
+            const double x0 = x[i], bi = b[i];
+            double nb[6];
+            nb[0] = x[lin(d, xm1(d, xi), yi, zi)];
+            nb[1] = x[lin(d, xp1(d, xi), yi, zi)];
+            float ri;
+            if (d.nz == 1) {
+                nb[2] = x[lin(d, xi, ym1(d, yi), zi)];
+                nb[3] = x[lin(d, xi, yp1(d, yi), zi)];
+                ri = helm_residual_bfp(bi, x0, nb, ones, 4, -4, f1);
+            } else {
+                nb[2] = x[lin(d, xi, yi, zm1(d, zi))];
+                nb[3] = x[lin(d, xi, yi, zp1(d, zi))];
+                if (d.channel && comp != 1 && (yi == 0 || yi == d.ny - 1)) {
+                    nb[4] = x[lin(d, xi, yi == 0 ? 1 : yi - 1, zi)];
+                    ri = helm_residual_bfp(bi, x0, nb, wallc, 5, -24, f3);
+                } else if (d.channel && comp == 1 && yi == 0) {
+                    ri = helm_residual_bfp(bi, x0, nb, ones, 0, 0, f1);
+                } else {
+                    nb[4] = x[lin(d, xi, ym1(d, yi), zi)];
+                    nb[5] = x[lin(d, xi, yp1(d, yi), zi)];
+                    ri = helm_residual_bfp(bi, x0, nb, ones, 6, -6, f1);
+                }
+            }
+            r[i] = ri;
+            acc += ri * ri;
+        }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, out);
+}
+
 // CG started from zero: r = p = b, n0 = b.b
 template <typename T>
 __global__ void __launch_bounds__(kRedBlock) k_cg_init_zero(long long N, const T* __restrict__ b, T* __restrict__ x,
@@ -537,6 +587,10 @@ template void launch_helm_rhs<double, float, float>(const Dims&, int, int, doubl
 template void launch_helm_rhs<double, double, float>(const Dims&, int, int, double*, const double*, const double*,
                                                      const float*, const double*, const double*, double, double,
                                                      double, double, cudaStream_t);
+void launch_helm_defect_bfp(const Dims& d, int comp, double scale, const double* x, const double* b, float* r,
+                            RedScratch sc, double* out, cudaStream_t s) {
+    k_helm_defect_bfp<<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, scale, x, b, r, sc, out);
+}
 template void launch_helm_defect<float>(const Dims&, int, double, const double*, const double*, float*, RedScratch,
                                         double*, cudaStream_t);
 template void launch_cg_dir_apply<float>(const Dims&, int, double, const float*, const float*, float*, float*,

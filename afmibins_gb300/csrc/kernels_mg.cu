@@ -2,6 +2,7 @@
 // src/mg/laplacian.h): red-black Gauss–Seidel in place of the reference's
 // lexicographic CSR sweep, the reference's full-weighting restriction and
 // trilinear prolongation, and a one-block CG for the coarsest level.
+#include "dfloat.cuh"
 #include "kernels.h"
 
 namespace afmib {
@@ -96,6 +97,43 @@ __global__ void __launch_bounds__(kRedBlock) k_lap_defect(Dims d, TD* __restrict
     grid_sum<1>(a, sc, out);
 }
 
+// The same defect without FP64 instructions (lap_residual_bfp): with
+// n^2 = 2^k2, b 2^-k2 - sum(nb) + c x0 is formed exactly in int64 at the
+// cell's largest exponent and scaled back by 2^k2.
+__global__ void __launch_bounds__(kRedBlock) k_lap_defect_bfp(Dims d, int k2, float* __restrict__ r,
+                                                             const double* __restrict__ xv, const double* __restrict__ b,
+                                                             RedScratch sc, double* out) {
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+    float acc = 0.f;
+    if (xi < d.nx && yi < d.ny)
+#pragma unroll 2
+        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
+            const long long i = lin(d, xi, yi, zi);
+            double nb[6];
+            int m = 0, c = 6;
+            nb[m++] = xv[lin(d, xm1(d, xi), yi, zi)];
+            nb[m++] = xv[lin(d, xp1(d, xi), yi, zi)];
+            if (d.nz == 1) {
+                c = 4;
+            } else {
+                nb[m++] = xv[lin(d, xi, yi, zm1(d, zi))];
+                nb[m++] = xv[lin(d, xi, yi, zp1(d, zi))];
+            }
+            if (d.channel) {
+                if (yi > 0) nb[m++] = xv[lin(d, xi, yi - 1, zi)]; else --c;
+                if (yi < d.ny - 1) nb[m++] = xv[lin(d, xi, yi + 1, zi)]; else --c;
+            } else {
+                nb[m++] = xv[lin(d, xi, ym1(d, yi), zi)];
+                nb[m++] = xv[lin(d, xi, yp1(d, yi), zi)];
+            }
+            const float ri = lap_residual_bfp(b[i], xv[i], nb, m, c, k2);
+            r[i] = ri;
+            acc += ri * ri;
+        }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, out);
+}
+
 // One colour of red-black Gauss–Seidel: x_i = (b_i - n^2 S) / (-c n^2).
 template <typename T>
 __global__ void k_rbgs(Dims d, int color, T* __restrict__ xv, const T* __restrict__ b) {
@@ -117,129 +155,71 @@ __global__ void k_rbgs(Dims d, int color, T* __restrict__ xv, const T* __restric
 // planes, and marches along z. At step k it updates the red cells of plane k
 // on the rows tile +- 1, then the black cells of plane k-1 on the tile, then
 // writes plane k-1 of the tile. Rows of x (tile +- 2) and of b (tile +- 1)
-// arrive in a ring of R = D + 4 plane slots by bulk asynchronous copies
-// (cp.async.bulk, one per row, completing on one mbarrier per slot) that one
-// thread issues D planes ahead, so the march does not wait on DRAM. The
-// blocks are persistent and take (row strip, z chunk) items in order.
-// Every update is the per-colour kernel's arithmetic with the same terms in
-// the same order, so a pipelined sweep equals the two per-colour launches
-// cell for cell. Waits are bounded: a block that waits too long records
-// the failure in err[0], waits (bounded) for its copies and leaves.
+// arrive in a ring of R = D + 4 plane slots by asynchronous 16-byte copies
+// (cp.async) that all threads issue D planes ahead, one commit group per
+// plane, so the march does not wait on DRAM. The blocks are persistent and
+// take (row strip, z chunk) items in order. Every update is the per-colour
+// kernel's arithmetic with the same terms in the same order, so a pipelined
+// sweep equals the two per-colour launches cell for cell.
 // ---------------------------------------------------------------------------
 namespace pipe {
 __device__ __forceinline__ unsigned saddr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count) : "memory");
+__device__ __forceinline__ void cp16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr(dst)), "l"(src) : "memory");
 }
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+__device__ __forceinline__ void commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void wait_pending() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(saddr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// bounded wait: false after about `limit` SM clock cycles
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, long long limit) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > limit) return false;
-    return true;
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     saddr(dst)),
-                 "l"(src), "r"(bytes), "r"(saddr(bar))
-                 : "memory");
-}
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-constexpr long long kWaitCycles = 2000000000LL;  // about one second at 2 GHz
 }  // namespace pipe
 
-template <typename T>
+template <typename T, int D>
 __global__ void __launch_bounds__(256) k_rbgs_pipe(Dims d, const T* __restrict__ xin, T* __restrict__ xout,
-                                                   const T* __restrict__ b, int FY, int ZC, int D, int* err) {
+                                                   const T* __restrict__ b, int FY, int ZC) {
     extern __shared__ __align__(128) unsigned char smem[];
-    const int R = D + 4;
+    constexpr int R = D + 4;
     const int nx = d.nx, XR = FY + 4, BR = FY + 2;
-    const unsigned row_bytes = (unsigned)(nx * sizeof(T));
     const int xplane = XR * nx, bplane = BR * nx;
-    unsigned long long* bars = (unsigned long long*)smem;  // R <= 16 barriers in the first 128 bytes
-    T* xs = (T*)(smem + 128);                              // [R][XR][nx]
-    T* bs = xs + (size_t)R * xplane;                       // [R][BR][nx]
-    __shared__ int s_abort;
+    T* xs = (T*)smem;                    // [R][XR][nx]
+    T* bs = xs + (size_t)R * xplane;     // [R][BR][nx]
     const int tid = threadIdx.x, NT = blockDim.x;
     const int hx = nx >> 1;
+    const int cpr = (int)(nx * sizeof(T) / 16);  // 16-byte chunks per row
     const T inv = T(1) / (T(d.n) * T(d.n));
     const int nstrip = d.ny / FY, nchunk = d.nz / ZC, items = nstrip * nchunk;
-    if (tid == 0) {
-        for (int q = 0; q < R; ++q) pipe::mbar_init(&bars[q], 1);
-        pipe::fence_mbar_init();
-        s_abort = 0;
-    }
-    __syncthreads();
-    // Slots are used round-robin in issue order and every thread waits on the
-    // planes in that same order, so a per-thread bit per slot tracks the
-    // barrier phase to wait for.
-    unsigned phase = 0u;
-    unsigned pending = 0u;  // thread 0: slots with a copy issued and not yet waited for
-    int s_first = 0;        // slot of the first plane of the current item
+    int s_first = 0;  // slot of the first plane of the current item
     auto valid_row = [&](int gy) { return !(d.channel && (gy < 0 || gy >= d.ny)); };
-    auto next_slot = [&](int q) { return q + 1 == R ? 0 : q + 1; };
-    auto prev_slot = [&](int q) { return q == 0 ? R - 1 : q - 1; };
-    auto wait_slot = [&](int q) {
-        const bool ok = pipe::mbar_wait(&bars[q], (phase >> q) & 1u, pipe::kWaitCycles);
-        if (ok) {
-            phase ^= 1u << q;
-            pending &= ~(1u << q);
-        }
-        return ok;
-    };
+    auto next_slot = [](int q) { return q + 1 == R ? 0 : q + 1; };
+    auto prev_slot = [](int q) { return q == 0 ? R - 1 : q - 1; };
     for (int item = blockIdx.x; item < items; item += gridDim.x) {
         const int y0 = (item % nstrip) * FY, z0 = (item / nstrip) * ZC, zend = z0 + ZC;
         const int pfirst = z0 - 2, plast = zend + 1;
-        auto issue = [&](int p, int q) {  // thread 0: plane p into slot q
-            const int gz = wrapi(p, d.nz);
-            unsigned bytes = 0;
-            for (int r = 0; r < XR; ++r) bytes += valid_row(y0 - 2 + r) ? row_bytes : 0u;
-            for (int r = 0; r < BR; ++r) bytes += valid_row(y0 - 1 + r) ? row_bytes : 0u;
-            pipe::mbar_expect_tx(&bars[q], bytes);
-            pending |= 1u << q;
-            for (int r = 0; r < XR; ++r) {
-                const int gy = y0 - 2 + r;
-                if (!valid_row(gy)) continue;
-                pipe::bulk_g2s(xs + (size_t)q * xplane + r * nx, xin + lin(d, 0, wrapi(gy, d.ny), gz), row_bytes,
-                               &bars[q]);
+        // every thread copies its share of plane p into slot q; one commit group
+        auto issue = [&](int p, int q) {
+            if (p <= plast) {
+                const int gz = wrapi(p, d.nz);
+                for (int c = tid; c < (XR + BR) * cpr; c += NT) {
+                    const int r = c / cpr, o = c - r * cpr;
+                    const bool isx = r < XR;
+                    const int gy = isx ? y0 - 2 + r : y0 - 1 + (r - XR);
+                    if (!valid_row(gy)) continue;
+                    const T* src = (isx ? xin : b) + lin(d, 0, wrapi(gy, d.ny), gz);
+                    T* dst = isx ? xs + (size_t)q * xplane + r * nx : bs + (size_t)q * bplane + (r - XR) * nx;
+                    pipe::cp16((char*)dst + 16 * o, (const char*)src + 16 * o);
+                }
             }
-            for (int r = 0; r < BR; ++r) {
-                const int gy = y0 - 1 + r;
-                if (!valid_row(gy)) continue;
-                pipe::bulk_g2s(bs + (size_t)q * bplane + r * nx, b + lin(d, 0, wrapi(gy, d.ny), gz), row_bytes,
-                               &bars[q]);
-            }
+            pipe::commit();  // empty groups past the last plane keep the group count uniform
         };
         // prefetch planes pfirst .. pfirst + R - 2; the last slot fills at the end of the first step
         int next = pfirst, snext = s_first;
-        if (tid == 0) {
-            pipe::fence_proxy_async();
-            for (; next <= plast && next <= pfirst + R - 2; ++next, snext = next_slot(snext)) issue(next, snext);
-        }
-        // slots of planes k-1, k for the first step k = z0 - 1
+        for (; next <= pfirst + R - 2; ++next, snext = next_slot(snext)) issue(next, snext);
         int skm1 = s_first, sk = next_slot(s_first);
-        bool ok = wait_slot(skm1);
-        if (ok) ok = wait_slot(sk);
         for (int k = z0 - 1; k <= zend; ++k) {
             const int skp1 = next_slot(sk), skm2 = prev_slot(skm1);
-            if (ok) ok = wait_slot(skp1);
-            if (!ok) s_abort = 1;
+            // planes up to k+1 complete: D groups (planes k+2 .. k+D+1) may stay in flight
+            pipe::wait_pending<D>();
             __syncthreads();
-            if (s_abort) break;
             T* const Xm = xs + (size_t)skm1 * xplane;
             T* const X0 = xs + (size_t)sk * xplane;
             T* const Xp = xs + (size_t)skp1 * xplane;
@@ -292,8 +272,6 @@ __global__ void __launch_bounds__(256) k_rbgs_pipe(Dims d, const T* __restrict__
                     c0[xi] = (S - B1[(rr + 1) * nx + xi] * inv) * rc;
                 }
             }
-            // order this step's shared-memory accesses before the bulk copy that refills a slot
-            pipe::fence_proxy_async();
             __syncthreads();
             if (kb >= z0) {
                 // plane k-1 of the tile is final
@@ -301,28 +279,16 @@ __global__ void __launch_bounds__(256) k_rbgs_pipe(Dims d, const T* __restrict__
                 const T* src = Xm + 2 * nx;
                 for (int e = tid; e < FY * nx; e += NT) dst[e] = src[e];
             }
-            // the slot of plane k-2 is free (its last reader, the black update, is behind the barrier)
-            if (tid == 0 && next <= plast) {
-                pipe::fence_proxy_async();
-                issue(next, snext);
-                ++next;
-                snext = next_slot(snext);
-            }
+            // the slot of plane k-2 is free: its last reader, the black update, is behind the barrier
+            issue(next, snext);
+            ++next;
+            snext = next_slot(snext);
             skm1 = sk;
             sk = skp1;
         }
-        if (s_abort) {
-            // leave no copy in flight: wait (bounded) for every plane still outstanding
-            if (tid == 0) {
-                atomicOr(err, 1);
-                for (int q = 0; q < R; ++q)
-                    if ((pending >> q) & 1u) pipe::mbar_wait(&bars[q], (phase >> q) & 1u, pipe::kWaitCycles);
-            }
-            return;
-        }
-        // the item used planes pfirst .. plast: the next item starts after them
-        const int used = plast - pfirst + 1;
-        s_first = (s_first + used) % R;
+        pipe::wait_pending<0>();
+        // the item used planes pfirst .. pfirst + ZC + 3 and issued (empty) groups up to next - 1
+        s_first = (s_first + (next - pfirst)) % R;
         __syncthreads();
     }
 }
@@ -527,15 +493,17 @@ PipeCfg rbgs_pipe_cfg(const Dims& d) {
     constexpr size_t kMaxSmem = 200 * 1024;
     static bool attr = false;
     if (!attr) {
-        if (cudaFuncSetAttribute(k_rbgs_pipe<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem) !=
-            cudaSuccess)
+        if (cudaFuncSetAttribute(k_rbgs_pipe<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(k_rbgs_pipe<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem) !=
+                cudaSuccess)
             return c;
         attr = true;
     }
     for (int fy : {4, 2, 1}) {
         if (d.ny % fy) continue;
-        for (int dd = 4; dd >= 2; --dd) {
-            const size_t smem = 128 + (size_t)(dd + 4) * (2 * fy + 6) * row;
+        for (int dd : {4, 2}) {
+            const size_t smem = (size_t)(dd + 4) * (2 * fy + 6) * row;
             if (smem <= kMaxSmem) {
                 c.FY = fy;
                 c.D = dd;
@@ -549,7 +517,8 @@ PipeCfg rbgs_pipe_cfg(const Dims& d) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_pipe<T>, 256, c.smem);
+    if (c.D == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_pipe<T, 4>, 256, c.smem);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_pipe<T, 2>, 256, c.smem);
     if (sms <= 0 || per_sm <= 0) {
         c.FY = 0;
         return c;
@@ -572,7 +541,9 @@ PipeCfg rbgs_pipe_cfg(const Dims& d) {
 
 template <typename T>
 void launch_rbgs_pipe(const Dims& d, const PipeCfg& c, const T* xin, T* xout, const T* b, int* err, cudaStream_t s) {
-    k_rbgs_pipe<T><<<c.grid, 256, c.smem, s>>>(d, xin, xout, b, c.FY, c.ZC, c.D, err);
+    (void)err;  // the copies are cp.async groups: no wait can time out
+    if (c.D == 4) k_rbgs_pipe<T, 4><<<c.grid, 256, c.smem, s>>>(d, xin, xout, b, c.FY, c.ZC);
+    else k_rbgs_pipe<T, 2><<<c.grid, 256, c.smem, s>>>(d, xin, xout, b, c.FY, c.ZC);
 }
 
 template <typename T>
@@ -593,6 +564,14 @@ void launch_prolong_assign(const Dims& d, T* fine, const T* coarse, cudaStream_t
 template <typename TD>
 void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, RedScratch sc, double* out, cudaStream_t s) {
     k_lap_defect<TD><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, r, x, b, sc, out);
+}
+bool launch_lap_defect_bfp(const Dims& d, float* r, const double* x, const double* b, RedScratch sc, double* out,
+                           cudaStream_t s) {
+    int k = 0;
+    while ((1 << k) < d.n) ++k;
+    if ((1 << k) != d.n || 2 * k > 126) return false;  // n must be a power of two
+    k_lap_defect_bfp<<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, 2 * k, r, x, b, sc, out);
+    return true;
 }
 template void launch_lap_defect<float>(const Dims&, float*, const double*, const double*, RedScratch, double*,
                                        cudaStream_t);

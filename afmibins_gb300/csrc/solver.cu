@@ -60,6 +60,8 @@ struct afmib_solver {
     int inner_cycles = 3;
     bool pipe_smoother = true;  // pipelined red-black sweeps where a level allows (AFMIB_SMOOTHER=percolour: off)
     int pipe_min_nx = 64;       // smaller levels keep the per-colour launches (AFMIB_PIPE_MIN_NX)
+    // mixed form: FP64-state defects by int64 block arithmetic (AFMIB_BFP=0: FP64 kernels)
+    bool bfp_defects = true;
     // V-cycle blocks captured once into CUDA graphs and replayed (no host
     // interaction inside a V-cycle); not used while per-kernel profiling is on
     bool use_graphs = true;
@@ -584,7 +586,10 @@ int helm_solve_mixed(afmib_solver* s, int comp, double scale, double* x, const d
     for (;;) {
         {
             ProfScope ps(s, P_HELM_DEFECT, (double)N * (8 + 8 + 4));
-            launch_helm_defect<float>(s->d, comp, scale, x, b, s->d32, s->red, s->scal + 10, s->st);
+            if (s->bfp_defects)
+                launch_helm_defect_bfp(s->d, comp, scale, x, b, s->d32, s->red, s->scal + 10, s->st);
+            else
+                launch_helm_defect<float>(s->d, comp, scale, x, b, s->d32, s->red, s->scal + 10, s->st);
         }
         CKL();
         TRY(read_scalars(s, 10, 1));
@@ -622,7 +627,8 @@ int mg_solve_mixed(afmib_solver* s, int* cycles) {
     for (;;) {
         {
             ProfScope ps(s, P_LAP_DEFECT, (double)N * (8 + 8 + 4));
-            launch_lap_defect<float>(L.d, L32.b, L.x, L.b, s->red, s->scal + 9, s->st);
+            if (!s->bfp_defects || !launch_lap_defect_bfp(L.d, L32.b, L.x, L.b, s->red, s->scal + 9, s->st))
+                launch_lap_defect<float>(L.d, L32.b, L.x, L.b, s->red, s->scal + 9, s->st);
         }
         CKL();
         TRY(read_scalars(s, 9, 1));
@@ -1278,6 +1284,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     s->interp64 = s->mixed && !(g.ib_fp32 & 2);
     if (const char* e = std::getenv("AFMIB_SMOOTHER")) s->pipe_smoother = std::string(e) != "percolour";
     if (const char* e = std::getenv("AFMIB_PIPE_MIN_NX")) s->pipe_min_nx = std::atoi(e);
+    if (const char* e = std::getenv("AFMIB_BFP")) s->bfp_defects = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_GRAPHS")) s->use_graphs = std::string(e) != "0";
     if (g.proj_start < AFMIB_START_DEFAULT || g.proj_start > AFMIB_START_WARM)
         return s->fail(AFMIB_ERR_ARG, "proj_start must be AFMIB_START_DEFAULT, _ZERO or _WARM");

@@ -364,3 +364,27 @@ def test_pipelined_smoother_equals_per_colour(monkeypatch, bc, shape):
             out[mode] = (sv.smooth(x0, b), sv.mg_solve(b)[0])
     assert np.array_equal(out["percolour"][0], out["pipe"][0])
     assert np.array_equal(out["percolour"][1], out["pipe"][1])
+
+
+@pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
+def test_block_arithmetic_defects_match_fp64_defects(monkeypatch, bc):
+    """The mixed form's FP64-state defects from int64 block arithmetic (no FP64
+    instruction) against the FP64 defect kernels: both stop on the same
+    residual tests, so four NS sub-steps agree to the solver tolerance."""
+    n = 32
+    channel = bc == capi.BC_CHANNEL
+    g = po.Grid(n, n, n, n, channel=channel)
+    rng = np.random.default_rng(22)
+    u, v, w = 0.1 * rng.standard_normal(g.ncell), 0.1 * rng.standard_normal(g.nv), 0.1 * rng.standard_normal(g.ncell)
+    f = [rng.standard_normal(g.ncell), rng.standard_normal(g.nv), rng.standard_normal(g.ncell)]
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("AFMIB_BFP", mode)
+        with capi.Solver(n, bc=bc, precision=capi.MIXED, mu=0.01, rho=1.0, dt=1e-3, tol=1e-12) as sv:
+            sv.set_velocity(u, v, w)
+            sv.project()
+            for _ in range(4):
+                sv.ns_step(*f)
+            out[mode] = sv.get_velocity()
+    for a, b in zip(out["0"], out["1"]):
+        assert rel(b, a) < 1e-10
