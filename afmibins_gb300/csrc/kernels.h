@@ -122,6 +122,26 @@ struct PipeCfg {
 };
 template <typename T>
 PipeCfg rbgs_pipe_cfg(const Dims& d);
+
+// The V-cycle from level 0 of these levels down (smooth nu1, residual,
+// restrict, ..., the one-block CG on the last level, prolong-add, smooth nu2)
+// in one block: for the coarse levels (a few thousand cells or fewer), where
+// launches cost more than work. Equals the launch-by-launch V-cycle bit for
+// bit. For T = float the last level is solved in FP64 through cx64/cb64/cr64.
+constexpr int kMaxTailLevels = 8;
+template <typename T>
+struct TailLevels {
+    int nlev, nu1, nu2, maxit;
+    Dims d[kMaxTailLevels];
+    T* x[kMaxTailLevels];
+    T* b[kMaxTailLevels];
+    T* r[kMaxTailLevels];
+    double *cx64, *cb64, *cr64, *cw_p, *cw_q;
+    double tol;
+    int* status;
+};
+template <typename T>
+void launch_vcycle_tail(const TailLevels<T>& a, cudaStream_t s);
 template <typename T>
 void launch_rbgs_pipe(const Dims& d, const PipeCfg& c, const T* xin, T* xout, const T* b, int* err, cudaStream_t s);
 // Full-weighting restriction, src/mg/solver.h:153-181 (d = fine dims).

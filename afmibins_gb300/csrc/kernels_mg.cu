@@ -44,15 +44,21 @@ __global__ void k_lap(Dims d, T* __restrict__ out, const T* __restrict__ in) {
     out[lin(d, x, y, z)] = off * (S - c * in[lin(d, x, y, z)]);
 }
 
+// r = b - L x at one cell
 template <typename T>
-__global__ void k_residual(Dims d, T* __restrict__ r, const T* __restrict__ xv, const T* __restrict__ b) {
-    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
-    if (x >= d.nx || y >= d.ny) return;
+__device__ __forceinline__ void residual_cell(const Dims& d, T* r, const T* xv, const T* b, int x, int y, int z) {
     T S, c;
     lap_row(d, xv, x, y, z, S, c);
     const long long i = lin(d, x, y, z);
     const T off = T(d.n) * T(d.n);
     r[i] = b[i] - off * (S - c * xv[i]);
+}
+
+template <typename T>
+__global__ void k_residual(Dims d, T* __restrict__ r, const T* __restrict__ xv, const T* __restrict__ b) {
+    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+    if (x >= d.nx || y >= d.ny) return;
+    residual_cell(d, r, xv, b, x, y, z);
 }
 
 template <typename T>
@@ -136,16 +142,21 @@ __global__ void __launch_bounds__(kRedBlock) k_lap_defect_bfp(Dims d, int k2, fl
 
 // One colour of red-black Gauss–Seidel: x_i = (b_i - n^2 S) / (-c n^2).
 template <typename T>
-__global__ void k_rbgs(Dims d, int color, T* __restrict__ xv, const T* __restrict__ b) {
-    const int y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
-    const int x = 2 * (blockIdx.x * BX + threadIdx.x) + ((y + z + color) & 1);
-    if (x >= d.nx || y >= d.ny) return;
+__device__ __forceinline__ void rbgs_cell(const Dims& d, T* xv, const T* b, int x, int y, int z) {
     T S, c;
     lap_row(d, xv, x, y, z, S, c);
     const long long i = lin(d, x, y, z);
     const T inv = T(1) / (T(d.n) * T(d.n));
     const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
     xv[i] = (S - b[i] * inv) * rc;
+}
+
+template <typename T>
+__global__ void k_rbgs(Dims d, int color, T* __restrict__ xv, const T* __restrict__ b) {
+    const int y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
+    const int x = 2 * (blockIdx.x * BX + threadIdx.x) + ((y + z + color) & 1);
+    if (x >= d.nx || y >= d.ny) return;
+    rbgs_cell(d, xv, b, x, y, z);
 }
 
 // ---------------------------------------------------------------------------
@@ -174,110 +185,109 @@ __device__ __forceinline__ void wait_pending() {
 }
 }  // namespace pipe
 
-template <typename T, int D>
-__global__ void __launch_bounds__(256) k_rbgs_pipe(Dims d, const T* __restrict__ xin, T* __restrict__ xout,
-                                                   const T* __restrict__ b, int FY, int ZC) {
+constexpr int kPipeThreads = 512;
+
+// Power-of-two extents only (every level the sweep serves): indices are
+// shifts and masks. CH: channel walls in y (Neumann rows, no wrap in y).
+template <typename T, int D, bool CH>
+__global__ void __launch_bounds__(kPipeThreads) k_rbgs_pipe(Dims d, const T* __restrict__ xin, T* __restrict__ xout,
+                                                            const T* __restrict__ b, int FY, int ZC, int lnx, int lny) {
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr int R = D + 4;
     const int nx = d.nx, XR = FY + 4, BR = FY + 2;
     const int xplane = XR * nx, bplane = BR * nx;
-    T* xs = (T*)smem;                    // [R][XR][nx]
-    T* bs = xs + (size_t)R * xplane;     // [R][BR][nx]
-    const int tid = threadIdx.x, NT = blockDim.x;
-    const int hx = nx >> 1;
-    const int cpr = (int)(nx * sizeof(T) / 16);  // 16-byte chunks per row
+    T* xs = (T*)smem;                 // [R][XR][nx]
+    T* bs = xs + (size_t)R * xplane;  // [R][BR][nx]
+    const int tid = threadIdx.x;
+    const int lhx = lnx - 1, xmask = nx - 1, hmask = (nx >> 1) - 1, ymask = d.ny - 1, zmask = d.nz - 1;
+    const int lcpr = lnx + (sizeof(T) == 8 ? 3 : 2) - 4;  // log2 of the 16-byte chunks per row
+    const int cmask = (1 << lcpr) - 1;
     const T inv = T(1) / (T(d.n) * T(d.n));
-    const int nstrip = d.ny / FY, nchunk = d.nz / ZC, items = nstrip * nchunk;
-    int s_first = 0;  // slot of the first plane of the current item
-    auto valid_row = [&](int gy) { return !(d.channel && (gy < 0 || gy >= d.ny)); };
+    const int nstrip = d.ny / FY, items = nstrip * (d.nz / ZC);
+    int s_first = 0;
     auto next_slot = [](int q) { return q + 1 == R ? 0 : q + 1; };
     auto prev_slot = [](int q) { return q == 0 ? R - 1 : q - 1; };
+    auto row_ok = [&](int gy) { return !CH || (gy >= 0 && gy < d.ny); };
     for (int item = blockIdx.x; item < items; item += gridDim.x) {
         const int y0 = (item % nstrip) * FY, z0 = (item / nstrip) * ZC, zend = z0 + ZC;
         const int pfirst = z0 - 2, plast = zend + 1;
-        // every thread copies its share of plane p into slot q; one commit group
         auto issue = [&](int p, int q) {
             if (p <= plast) {
-                const int gz = wrapi(p, d.nz);
-                for (int c = tid; c < (XR + BR) * cpr; c += NT) {
-                    const int r = c / cpr, o = c - r * cpr;
+                const long long zoff = (long long)(p & zmask) << lny;
+                for (int c = tid; c < ((XR + BR) << lcpr); c += kPipeThreads) {
+                    const int r = c >> lcpr, o = c & cmask;
                     const bool isx = r < XR;
                     const int gy = isx ? y0 - 2 + r : y0 - 1 + (r - XR);
-                    if (!valid_row(gy)) continue;
-                    const T* src = (isx ? xin : b) + lin(d, 0, wrapi(gy, d.ny), gz);
-                    T* dst = isx ? xs + (size_t)q * xplane + r * nx : bs + (size_t)q * bplane + (r - XR) * nx;
+                    if (!row_ok(gy)) continue;
+                    const T* src = (isx ? xin : b) + ((zoff + (gy & ymask)) << lnx);
+                    T* dst = isx ? xs + (size_t)q * xplane + (r << lnx) : bs + (size_t)q * bplane + ((r - XR) << lnx);
                     pipe::cp16((char*)dst + 16 * o, (const char*)src + 16 * o);
                 }
             }
-            pipe::commit();  // empty groups past the last plane keep the group count uniform
+            pipe::commit();
         };
-        // prefetch planes pfirst .. pfirst + R - 2; the last slot fills at the end of the first step
         int next = pfirst, snext = s_first;
         for (; next <= pfirst + R - 2; ++next, snext = next_slot(snext)) issue(next, snext);
         int skm1 = s_first, sk = next_slot(s_first);
         for (int k = z0 - 1; k <= zend; ++k) {
             const int skp1 = next_slot(sk), skm2 = prev_slot(skm1);
-            // planes up to k+1 complete: D groups (planes k+2 .. k+D+1) may stay in flight
             pipe::wait_pending<D>();
             __syncthreads();
             T* const Xm = xs + (size_t)skm1 * xplane;
             T* const X0 = xs + (size_t)sk * xplane;
             T* const Xp = xs + (size_t)skp1 * xplane;
-            // red cells of plane k, rows tile +- 1
             {
-                const int gz = wrapi(k, d.nz);
+                // red cells of plane k, rows tile +- 1
+                const int gz = k & zmask;
                 const T* B0 = bs + (size_t)sk * bplane;
-                for (int e = tid; e < (FY + 2) * hx; e += NT) {
-                    const int rr = e / hx, gy = y0 - 1 + rr;
-                    if (!valid_row(gy)) continue;
-                    const int wy = wrapi(gy, d.ny);
-                    const int xi = 2 * (e - rr * hx) + ((wy + gz) & 1);
-                    const int o = (rr + 1) * nx;
+                for (int e = tid; e < ((FY + 2) << lhx); e += kPipeThreads) {
+                    const int rr = e >> lhx, gy = y0 - 1 + rr;
+                    if (!row_ok(gy)) continue;
+                    const int xi = 2 * (e & hmask) + (((gy & ymask) + gz) & 1);
+                    const int o = (rr + 1) << lnx;
                     T* c0 = X0 + o;
-                    const int xm = xi == 0 ? nx - 1 : xi - 1, xp = xi == nx - 1 ? 0 : xi + 1;
-                    T S = (c0[xm] + c0[xp]) + (Xm[o + xi] + Xp[o + xi]);
+                    T S = (c0[(xi - 1) & xmask] + c0[(xi + 1) & xmask]) + (Xm[o + xi] + Xp[o + xi]);
                     T c = T(6);
-                    if (d.channel) {
+                    if (CH) {
                         if (gy > 0) S += c0[xi - nx]; else c -= T(1);
                         if (gy < d.ny - 1) S += c0[xi + nx]; else c -= T(1);
                     } else {
                         S += c0[xi - nx] + c0[xi + nx];
                     }
                     const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
-                    c0[xi] = (S - B0[rr * nx + xi] * inv) * rc;
+                    c0[xi] = (S - B0[(rr << lnx) + xi] * inv) * rc;
                 }
             }
             __syncthreads();
             const int kb = k - 1;
             if (kb >= z0) {
                 // black cells of plane k-1 on the tile (z neighbours: k-2 and k)
-                const int gz = wrapi(kb, d.nz);
+                const int gz = kb & zmask;
                 T* const Ym = xs + (size_t)skm2 * xplane;
                 const T* B1 = bs + (size_t)skm1 * bplane;
-                for (int e = tid; e < FY * hx; e += NT) {
-                    const int rr = e / hx, gy = y0 + rr;
-                    const int xi = 2 * (e - rr * hx) + ((gy + gz + 1) & 1);
-                    const int o = (rr + 2) * nx;
+                for (int e = tid; e < (FY << lhx); e += kPipeThreads) {
+                    const int rr = e >> lhx, gy = y0 + rr;
+                    const int xi = 2 * (e & hmask) + ((gy + gz + 1) & 1);
+                    const int o = (rr + 2) << lnx;
                     T* c0 = Xm + o;
-                    const int xm = xi == 0 ? nx - 1 : xi - 1, xp = xi == nx - 1 ? 0 : xi + 1;
-                    T S = (c0[xm] + c0[xp]) + (Ym[o + xi] + X0[o + xi]);
+                    T S = (c0[(xi - 1) & xmask] + c0[(xi + 1) & xmask]) + (Ym[o + xi] + X0[o + xi]);
                     T c = T(6);
-                    if (d.channel) {
+                    if (CH) {
                         if (gy > 0) S += c0[xi - nx]; else c -= T(1);
                         if (gy < d.ny - 1) S += c0[xi + nx]; else c -= T(1);
                     } else {
                         S += c0[xi - nx] + c0[xi + nx];
                     }
                     const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
-                    c0[xi] = (S - B1[(rr + 1) * nx + xi] * inv) * rc;
+                    c0[xi] = (S - B1[((rr + 1) << lnx) + xi] * inv) * rc;
                 }
             }
             __syncthreads();
             if (kb >= z0) {
                 // plane k-1 of the tile is final
-                T* dst = xout + lin(d, 0, y0, kb);
+                T* dst = xout + ((((long long)kb << lny) + y0) << lnx);
                 const T* src = Xm + 2 * nx;
-                for (int e = tid; e < FY * nx; e += NT) dst[e] = src[e];
+                for (int e = tid; e < (FY << lnx); e += kPipeThreads) dst[e] = src[e];
             }
             // the slot of plane k-2 is free: its last reader, the black update, is behind the barrier
             issue(next, snext);
@@ -287,7 +297,6 @@ __global__ void __launch_bounds__(256) k_rbgs_pipe(Dims d, const T* __restrict__
             sk = skp1;
         }
         pipe::wait_pending<0>();
-        // the item used planes pfirst .. pfirst + ZC + 3 and issued (empty) groups up to next - 1
         s_first = (s_first + (next - pfirst)) % R;
         __syncthreads();
     }
@@ -296,10 +305,8 @@ __global__ void __launch_bounds__(256) k_rbgs_pipe(Dims d, const T* __restrict__
 // Full weighting, src/mg/solver.h:153-181: 64 taps (1,3,3,1)^3/512 around the
 // coarse cell; y clamps at the channel walls, wraps in periodic mode.
 template <typename T>
-__global__ void k_restrict(Dims d, T* __restrict__ coarse, const T* __restrict__ fine) {
-    const int cx = d.nx / 2, cy = d.ny / 2, cz = d.nz / 2;
-    const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
-    if (xc >= cx || yc >= cy) return;
+__device__ __forceinline__ void restrict_cell(const Dims& d, T* coarse, const T* fine, int xc, int yc, int zc) {
+    const int cx = d.nx / 2, cy = d.ny / 2;
     if (d.nz == 1) {
         // 2D (periodic): (1,3,3,1)^2 / 64 over 16 taps
         const T wgt[4] = {T(1), T(3), T(3), T(1)};
@@ -339,14 +346,19 @@ __global__ void k_restrict(Dims d, T* __restrict__ coarse, const T* __restrict__
     coarse[xc + (long long)cx * (yc + (long long)cy * zc)] = acc;
 }
 
+template <typename T>
+__global__ void k_restrict(Dims d, T* __restrict__ coarse, const T* __restrict__ fine) {
+    const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
+    if (xc >= d.nx / 2 || yc >= d.ny / 2) return;
+    restrict_cell(d, coarse, fine, xc, yc, zc);
+}
+
 // Trilinear prolongation (27,9,3,1)/64, src/mg/solver.h:71-151. One thread per
 // coarse cell writes the eight fine cells between it and its +1 neighbours;
 // in channel mode the wall rows take the bilinear (9,3,1)/16 weights.
 template <typename T, bool ADD>
-__global__ void k_prolong(Dims d, T* __restrict__ fine, const T* __restrict__ coarse) {
+__device__ __forceinline__ void prolong_cell(const Dims& d, T* fine, const T* coarse, int xc, int yc, int zc) {
     const int cx = d.nx / 2, cy = d.ny / 2, cz = d.nz / 2;
-    const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
-    if (xc >= cx || yc >= cy) return;
     auto C = [&](int a, int b, int c) { return coarse[a + (long long)cx * (b + (long long)cy * c)]; };
     auto put = [&](int a, int b, int c, T val) {
         const long long i = lin(d, a, b, c);
@@ -400,13 +412,18 @@ __global__ void k_prolong(Dims d, T* __restrict__ fine, const T* __restrict__ co
     }
 }
 
+template <typename T, bool ADD>
+__global__ void k_prolong(Dims d, T* __restrict__ fine, const T* __restrict__ coarse) {
+    const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
+    if (xc >= d.nx / 2 || yc >= d.ny / 2) return;
+    prolong_cell<T, ADD>(d, fine, coarse, xc, yc, zc);
+}
+
 // Coarsest level, src/mg/solver.h:264-271: remove the mean of b, then CG
 // warm-started from b with the absolute 2-norm stop. One block; the level is
 // a handful of cells (one cell for a cube).
 template <typename T>
-__global__ void __launch_bounds__(kRedBlock) k_coarse_cg(Dims d, T* __restrict__ xv, T* __restrict__ b, T* __restrict__ r,
-                                                        T* __restrict__ p, T* __restrict__ q, double tol, int maxit,
-                                                        int* status) {
+__device__ void coarse_cg_block(const Dims& d, T* xv, T* b, T* r, T* p, T* q, double tol, int maxit, int* status) {
     const long long N = d.ncell(), sxy = d.sxy();
     const T off = T(d.n) * T(d.n);
     __shared__ double s_val;
@@ -467,6 +484,86 @@ __global__ void __launch_bounds__(kRedBlock) k_coarse_cg(Dims d, T* __restrict__
     }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(kRedBlock) k_coarse_cg(Dims d, T* __restrict__ xv, T* __restrict__ b, T* __restrict__ r,
+                                                        T* __restrict__ p, T* __restrict__ q, double tol, int maxit,
+                                                        int* status) {
+    coarse_cg_block(d, xv, b, r, p, q, tol, maxit, status);
+}
+
+// ---------------------------------------------------------------------------
+// Multigrid tail: the V-cycle below a level of at most 16^3 cells in one
+// block. The coarse levels are a few thousand cells or fewer, so launching
+// their ~12 kernels per level costs more than the work; here one block walks
+// the same sequence (smooth, residual, restrict, zero, ..., coarsest solve,
+// prolong-add, smooth) with block barriers between the phases. Every phase
+// runs the per-cell function of the corresponding kernel and the coarsest
+// solve is the same one-block CG, so the result equals the launch-by-launch
+// V-cycle bit for bit.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void tail_sweep(const Dims& d, T* x, const T* b, int color) {
+    const int hx = d.nx / 2;
+    const long long total = (long long)hx * d.ny * d.nz;
+    for (long long e = threadIdx.x; e < total; e += blockDim.x) {
+        const int t = (int)(e % hx);
+        const long long rest = e / hx;
+        const int y = (int)(rest % d.ny), z = (int)(rest / d.ny);
+        const int xx = 2 * t + ((y + z + color) & 1);
+        if (xx < d.nx) rbgs_cell(d, x, b, xx, y, z);
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRedBlock) k_vcycle_tail(TailLevels<T> a) {
+    for (int l = 0; l + 1 < a.nlev; ++l) {
+        const Dims& d = a.d[l];
+        for (int j = 0; j < a.nu1; ++j) {
+            tail_sweep(d, a.x[l], a.b[l], 0);
+            tail_sweep(d, a.x[l], a.b[l], 1);
+        }
+        const long long n = d.ncell();
+        for (long long i = threadIdx.x; i < n; i += blockDim.x)
+            residual_cell(d, a.r[l], a.x[l], a.b[l], (int)(i % d.nx), (int)((i / d.nx) % d.ny), (int)(i / d.sxy()));
+        __syncthreads();
+        const Dims& c = a.d[l + 1];
+        const long long nc = c.ncell();
+        for (long long i = threadIdx.x; i < nc; i += blockDim.x) {
+            restrict_cell(d, a.b[l + 1], a.r[l], (int)(i % c.nx), (int)((i / c.nx) % c.ny), (int)(i / c.sxy()));
+            a.x[l + 1][i] = T(0);
+        }
+        __syncthreads();
+    }
+    {
+        const int l = a.nlev - 1;
+        const Dims& d = a.d[l];
+        const long long n = d.ncell();
+        if constexpr (sizeof(T) == sizeof(double)) {
+            coarse_cg_block(d, a.x[l], a.b[l], a.r[l], a.cw_p, a.cw_q, a.tol, a.maxit, a.status);
+        } else {
+            for (long long i = threadIdx.x; i < n; i += blockDim.x) a.cb64[i] = (double)a.b[l][i];
+            __syncthreads();
+            coarse_cg_block(d, a.cx64, a.cb64, a.cr64, a.cw_p, a.cw_q, a.tol, a.maxit, a.status);
+            __syncthreads();
+            for (long long i = threadIdx.x; i < n; i += blockDim.x) a.x[l][i] = (T)a.cx64[i];
+        }
+        __syncthreads();
+    }
+    for (int l = a.nlev - 2; l >= 0; --l) {
+        const Dims& d = a.d[l];
+        const Dims& c = a.d[l + 1];
+        const long long nc = c.ncell();
+        for (long long i = threadIdx.x; i < nc; i += blockDim.x)
+            prolong_cell<T, true>(d, a.x[l], a.x[l + 1], (int)(i % c.nx), (int)((i / c.nx) % c.ny), (int)(i / c.sxy()));
+        __syncthreads();
+        for (int j = 0; j < a.nu2; ++j) {
+            tail_sweep(d, a.x[l], a.b[l], 0);
+            tail_sweep(d, a.x[l], a.b[l], 1);
+        }
+    }
+}
+
 }  // namespace
 
 template <typename T>
@@ -485,19 +582,33 @@ void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s) {
     dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz);
     k_rbgs<T><<<g, dim3(BX, BY), 0, s>>>(d, color, x, b);
 }
+namespace {
+int log2_exact(int v) {
+    int k = 0;
+    while ((1 << k) < v) ++k;
+    return (1 << k) == v ? k : -1;
+}
+template <typename T>
+void* pipe_kernel(int D, bool ch) {
+    if (D == 4) return ch ? (void*)k_rbgs_pipe<T, 4, true> : (void*)k_rbgs_pipe<T, 4, false>;
+    return ch ? (void*)k_rbgs_pipe<T, 2, true> : (void*)k_rbgs_pipe<T, 2, false>;
+}
+}  // namespace
+
 template <typename T>
 PipeCfg rbgs_pipe_cfg(const Dims& d) {
     PipeCfg c;
     const size_t row = (size_t)d.nx * sizeof(T);
-    if (d.nz < 2 || d.nx < 32 || (d.nx & 1) || row % 16 != 0) return c;
+    if (d.nz < 2 || d.nx < 32 || row % 16 != 0) return c;
+    if (log2_exact(d.nx) < 0 || log2_exact(d.ny) < 0 || log2_exact(d.nz) < 0) return c;
     constexpr size_t kMaxSmem = 200 * 1024;
     static bool attr = false;
     if (!attr) {
-        if (cudaFuncSetAttribute(k_rbgs_pipe<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem) !=
-                cudaSuccess ||
-            cudaFuncSetAttribute(k_rbgs_pipe<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem) !=
-                cudaSuccess)
-            return c;
+        for (int dd : {4, 2})
+            for (bool ch : {false, true})
+                if (cudaFuncSetAttribute(pipe_kernel<T>(dd, ch), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kMaxSmem) != cudaSuccess)
+                    return c;
         attr = true;
     }
     for (int fy : {4, 2, 1}) {
@@ -517,8 +628,7 @@ PipeCfg rbgs_pipe_cfg(const Dims& d) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (c.D == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_pipe<T, 4>, 256, c.smem);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_pipe<T, 2>, 256, c.smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pipe_kernel<T>(c.D, d.channel != 0), kPipeThreads, c.smem);
     if (sms <= 0 || per_sm <= 0) {
         c.FY = 0;
         return c;
@@ -542,8 +652,14 @@ PipeCfg rbgs_pipe_cfg(const Dims& d) {
 template <typename T>
 void launch_rbgs_pipe(const Dims& d, const PipeCfg& c, const T* xin, T* xout, const T* b, int* err, cudaStream_t s) {
     (void)err;  // the copies are cp.async groups: no wait can time out
-    if (c.D == 4) k_rbgs_pipe<T, 4><<<c.grid, 256, c.smem, s>>>(d, xin, xout, b, c.FY, c.ZC);
-    else k_rbgs_pipe<T, 2><<<c.grid, 256, c.smem, s>>>(d, xin, xout, b, c.FY, c.ZC);
+    const int lnx = log2_exact(d.nx), lny = log2_exact(d.ny);
+    if (c.D == 4) {
+        if (d.channel) k_rbgs_pipe<T, 4, true><<<c.grid, kPipeThreads, c.smem, s>>>(d, xin, xout, b, c.FY, c.ZC, lnx, lny);
+        else k_rbgs_pipe<T, 4, false><<<c.grid, kPipeThreads, c.smem, s>>>(d, xin, xout, b, c.FY, c.ZC, lnx, lny);
+    } else {
+        if (d.channel) k_rbgs_pipe<T, 2, true><<<c.grid, kPipeThreads, c.smem, s>>>(d, xin, xout, b, c.FY, c.ZC, lnx, lny);
+        else k_rbgs_pipe<T, 2, false><<<c.grid, kPipeThreads, c.smem, s>>>(d, xin, xout, b, c.FY, c.ZC, lnx, lny);
+    }
 }
 
 template <typename T>
@@ -577,6 +693,10 @@ template void launch_lap_defect<float>(const Dims&, float*, const double*, const
                                        cudaStream_t);
 
 template <typename T>
+void launch_vcycle_tail(const TailLevels<T>& a, cudaStream_t s) {
+    k_vcycle_tail<T><<<1, kRedBlock, 0, s>>>(a);
+}
+template <typename T>
 void launch_coarse_solve(const Dims& d, T* x, T* b, T* r, T* p, T* q, double tol, int maxit, int* status, cudaStream_t s) {
     k_coarse_cg<T><<<1, kRedBlock, 0, s>>>(d, x, b, r, p, q, tol, maxit, status);
 }
@@ -590,7 +710,8 @@ void launch_coarse_solve(const Dims& d, T* x, T* b, T* r, T* p, T* q, double tol
     template void launch_restrict<T>(const Dims&, T*, const T*, cudaStream_t);                           \
     template void launch_prolong_add<T>(const Dims&, T*, const T*, cudaStream_t);                        \
     template void launch_prolong_assign<T>(const Dims&, T*, const T*, cudaStream_t);                     \
-    template void launch_coarse_solve<T>(const Dims&, T*, T*, T*, T*, T*, double, int, int*, cudaStream_t);
+    template void launch_coarse_solve<T>(const Dims&, T*, T*, T*, T*, T*, double, int, int*, cudaStream_t);    \
+    template void launch_vcycle_tail<T>(const TailLevels<T>&, cudaStream_t);
 
 AFMIB_MG_INST(double)
 AFMIB_MG_INST(float)

@@ -60,8 +60,12 @@ struct afmib_solver {
     int inner_cycles = 3;
     bool pipe_smoother = true;  // pipelined red-black sweeps where a level allows (AFMIB_SMOOTHER=percolour: off)
     int pipe_min_nx = 64;       // smaller levels keep the per-colour launches (AFMIB_PIPE_MIN_NX)
-    // mixed form: FP64-state defects by int64 block arithmetic (AFMIB_BFP=0: FP64 kernels)
-    bool bfp_defects = true;
+    // mixed form: FP64-state defects by int64 block arithmetic instead of the
+    // FP64 kernels (opt-in, AFMIB_BFP=1: measured no faster on GB300, the
+    // integer form being instruction-bound at about the FP64 kernels' time)
+    bool bfp_defects = false;
+    // first multigrid level handled by the one-block V-cycle tail (-1: none; AFMIB_MG_TAIL=0)
+    int tail_level = -1;
     // V-cycle blocks captured once into CUDA graphs and replayed (no host
     // interaction inside a V-cycle); not used while per-kernel profiling is on
     bool use_graphs = true;
@@ -213,14 +217,14 @@ enum ProfId {
     P_ADVECT, P_HELM_RHS, P_CG_INIT, P_CG_APPLY, P_CG_UPDATE, P_CG_DIR, P_RBGS, P_RESID, P_RESID_NORM,
     P_RESTRICT, P_PROLONG, P_COARSE, P_DIV, P_GRAD_SUB, P_MEAN, P_WALL, P_SPRINGS, P_PREP, P_SORT,
     P_TILES, P_SPREAD, P_INTERP, P_MARKER, P_HELM_DEFECT, P_LAP_DEFECT, P_CORRECT, P_ADJ_ADVECT, P_ADJ_MARKER,
-    P_RBGS0, P_RESID0, P_RESTRICT0, P_PROLONG0, P_CG_DIRAPPLY, P_COUNT
+    P_RBGS0, P_RESID0, P_RESTRICT0, P_PROLONG0, P_CG_DIRAPPLY, P_TAIL, P_COUNT
 };
 const char* kProfNames[P_COUNT] = {
     "advect", "helm_rhs", "cg_init", "cg_apply", "cg_update", "cg_direction", "mg_rbgs", "mg_residual",
     "mg_residual_norm", "mg_restrict", "mg_prolong_add", "mg_coarse_cg", "div", "grad_sub", "mean_removal",
     "wall_update", "springs", "marker_prep", "radix_sort", "tile_bins", "spread_gather", "interp", "marker_update",
     "helm_defect_fp64", "lap_defect_fp64", "add_correction_fp64", "advect_adjoint", "marker_adjoint",
-    "mg_rbgs_fine", "mg_residual_fine", "mg_restrict_fine", "mg_prolong_add_fine", "cg_dir_apply"};
+    "mg_rbgs_fine", "mg_residual_fine", "mg_restrict_fine", "mg_prolong_add_fine", "cg_dir_apply", "mg_coarse_tail"};
 
 cudaEvent_t prof_event(afmib_solver* s) {
     if (!s->prof_pool.empty()) {
@@ -384,11 +388,40 @@ int coarse(afmib_solver* s, MGLevelT<float>& L) {
     return AFMIB_OK;
 }
 
+// the coarse V-cycle below level l in one block (see k_vcycle_tail)
+template <typename T>
+int vcycle_tail(afmib_solver* s, size_t l) {
+    auto& lv = levels<T>(s);
+    TailLevels<T> a{};
+    a.nlev = (int)(lv.size() - l);
+    a.nu1 = s->cfg.nu1;
+    a.nu2 = s->cfg.nu2;
+    a.maxit = s->cfg.max_cg_iters;
+    a.tol = s->cfg.tol;
+    for (int k = 0; k < a.nlev; ++k) {
+        a.d[k] = lv[l + k].d;
+        a.x[k] = lv[l + k].x;
+        a.b[k] = lv[l + k].b;
+        a.r[k] = lv[l + k].r;
+    }
+    a.cx64 = s->cx64;
+    a.cb64 = s->cb64;
+    a.cr64 = s->cr64;
+    a.cw_p = s->cw_p;
+    a.cw_q = s->cw_q;
+    a.status = s->dflag + 1;
+    ProfScope ps(s, P_TAIL, 0.0);
+    launch_vcycle_tail<T>(a, s->st);
+    CKL();
+    return AFMIB_OK;
+}
+
 template <typename T>
 int vcycle(afmib_solver* s, size_t l) {
     auto& lv = levels<T>(s);
     MGLevelT<T>& L = lv[l];
     const double Ns = (double)L.d.ncell() * sizeof(T);
+    if (s->tail_level >= 0 && l == (size_t)s->tail_level) return vcycle_tail<T>(s, l);
     if (l + 1 == lv.size()) {
         TRY(coarse(s, L));
         CKL();
@@ -1284,7 +1317,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     s->interp64 = s->mixed && !(g.ib_fp32 & 2);
     if (const char* e = std::getenv("AFMIB_SMOOTHER")) s->pipe_smoother = std::string(e) != "percolour";
     if (const char* e = std::getenv("AFMIB_PIPE_MIN_NX")) s->pipe_min_nx = std::atoi(e);
-    if (const char* e = std::getenv("AFMIB_BFP")) s->bfp_defects = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_BFP")) s->bfp_defects = std::string(e) == "1";
     if (const char* e = std::getenv("AFMIB_GRAPHS")) s->use_graphs = std::string(e) != "0";
     if (g.proj_start < AFMIB_START_DEFAULT || g.proj_start > AFMIB_START_WARM)
         return s->fail(AFMIB_ERR_ARG, "proj_start must be AFMIB_START_DEFAULT, _ZERO or _WARM");
@@ -1400,6 +1433,17 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
         TRY(dalloc(s, &s->cx64, nc));
         TRY(dalloc(s, &s->cb64, nc));
         TRY(dalloc(s, &s->cr64, nc));
+    }
+    // one-block V-cycle tail from the first level of at most 16^3 cells, when
+    // it leaves at least one smoothed level above the coarsest
+    {
+        bool tail = true;
+        if (const char* e = std::getenv("AFMIB_MG_TAIL")) tail = std::string(e) != "0";
+        for (size_t l = 0; tail && l + 1 < s->lv.size(); ++l)
+            if (s->lv[l].d.ncell() <= 4096 && s->lv.size() - l <= (size_t)kMaxTailLevels) {
+                s->tail_level = (int)l;
+                break;
+            }
     }
     CK(cudaStreamSynchronize(s->st));
     return AFMIB_OK;
