@@ -1318,6 +1318,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_SMOOTHER")) s->pipe_smoother = std::string(e) != "percolour";
     if (const char* e = std::getenv("AFMIB_PIPE_MIN_NX")) s->pipe_min_nx = std::atoi(e);
     if (const char* e = std::getenv("AFMIB_BFP")) s->bfp_defects = std::string(e) == "1";
+    if (const char* e = std::getenv("AFMIB_INNER_CYCLES")) s->inner_cycles = std::max(1, std::atoi(e));
     if (const char* e = std::getenv("AFMIB_GRAPHS")) s->use_graphs = std::string(e) != "0";
     if (g.proj_start < AFMIB_START_DEFAULT || g.proj_start > AFMIB_START_WARM)
         return s->fail(AFMIB_ERR_ARG, "proj_start must be AFMIB_START_DEFAULT, _ZERO or _WARM");

@@ -55,11 +55,22 @@ def parse():
     ap.add_argument("--dt", type=float, default=2e-5)
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--profile-steps", type=int, default=2)
+    ap.add_argument("--inner-tol", type=float, default=0.0,
+                    help="mixed form: relative reduction of each FP32 inner Helmholtz solve (0: the library default)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--case", choices=["ib", "mg"], default="ib",
+    ap.add_argument("--case", choices=["ib", "mg", "adjoint", "large"], default="ib",
                     help="ib: the IB step (the headline); mg: pressure multigrid solves alone on a seeded right-hand "
-                         "side (a small, single-kernel-family target for profilers)")
+                         "side (a small, single-kernel-family target for profilers); adjoint: gradient of the "
+                         "membrane loss through the hand-written adjoint, checked against central differences "
+                         "(128^3, 20,480-marker icosphere shell, 50 steps, checkpoints every 10, 16 directions); "
+                         "large: 512^3 with 1,000,000 markers (40 shells), the mixed forward against the FP64 "
+                         "forward and the adjoint with checkpoints every 5 steps, peak device memory")
+    ap.add_argument("--large-steps", type=int, default=50)
+    ap.add_argument("--adj-steps", type=int, default=50)
+    ap.add_argument("--adj-every", type=int, default=10)
+    ap.add_argument("--adj-dirs", type=int, default=16)
+    ap.add_argument("--adj-tol", type=float, default=1e-12)
     ap.add_argument("--cpu-sample-n", type=int, default=64,
                     help="grid of the CPU sample (the workload at reduced resolution, scaled by the cell count)")
     return ap.parse_args()
@@ -202,7 +213,7 @@ def run_form(capi, torch, args, prec, state, dev, stream, proj_start=0):
     warm-up and the timed steps; return (solver, ms, launches, clocks, wall)."""
     X, nstart, nidx, u, v, w = state
     sv = capi.Solver(args.n, mu=args.mu, rho=1.0, dt=args.dt, tol=args.tol, k_spring=0.5, precision=prec,
-                     proj_start=proj_start, stream=stream.cuda_stream)
+                     proj_start=proj_start, inner_tol=args.inner_tol, stream=stream.cuda_stream)
     ud, vd, wd = (torch.from_numpy(a).to(dev) for a in (u, v, w))
     Xd = torch.from_numpy(X).to(dev)
     torch.cuda.synchronize()
@@ -262,6 +273,152 @@ def run_mg_case(args, torch, local):
                       "precision": args.precision, "config": {"grid": n, "tol": args.tol}}))
 
 
+def run_adjoint_case(args, torch, local):
+    """The adjoint configuration: periodic 128^3 (--n), mu 0.01, dt 5e-5, an
+    icosphere face-centroid shell (20,480 markers, radius 0.2, 0.02 Y_2^0),
+    k = 0.5, a seeded solenoidal initial velocity (RMS 0.1, peak wavenumber 4);
+    loss = sum |X - c - (X0 - c0)|^2 + KE/2 after --adj-steps steps with
+    checkpoints every --adj-every. Gradients in k and X0 from the FP64 and the
+    mixed forward, each against central differences (h = 1e-6) of the FP64
+    forward on --adj-dirs seeded directions. One JSON line."""
+    from afmibins_gb300 import capi, markers as mk
+    from afmibins_gb300.autograd import ib_trajectory, membrane_loss
+    n = args.n if args.n != 256 else 128
+    dev = torch.device("cuda", local)
+    X, nstart, nidx = mk.icoshell(5, (0.5, 0.5, 0.5), 0.2, 0.02)
+    vel = mk.random_solenoidal_velocity(n, n, n, rms=0.1, k_peak=4.0, seed=mk.SEED + 4)
+    h3 = 1.0 / n ** 3
+
+    def solver(prec):
+        sv = capi.Solver(n, mu=0.01, rho=1.0, dt=5e-5, tol=args.adj_tol, k_spring=0.5, precision=prec,
+                         max_cg_iters=5000, max_mg_cycles=500)
+        sv.set_velocity(*vel)
+        sv.project()
+        v0 = tuple(torch.from_numpy(a).to(dev) for a in sv.get_velocity())
+        sv.set_markers(X, nstart, nidx)
+        return sv, v0
+
+    fd_sv, vel0 = solver(capi.FP64)
+
+    def loss(kv, Xv):
+        with torch.no_grad():
+            Xt = torch.tensor(Xv, device=dev)
+            uN, XN = ib_trajectory(torch.tensor(kv, dtype=torch.float64, device=dev), Xt, fd_sv, vel0,
+                                   args.adj_steps, args.adj_every)
+            return float(membrane_loss(uN, XN, Xt, h3))
+
+    results = {}
+    for name, prec in (("fp64", capi.FP64), ("mixed", capi.MIXED)):
+        sv, v0 = (fd_sv, vel0) if prec == capi.FP64 else solver(prec)
+        X0 = torch.tensor(X, device=dev, requires_grad=True)
+        k = torch.tensor(0.5, dtype=torch.float64, device=dev, requires_grad=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        uN, XN = ib_trajectory(k, X0, sv, v0, args.adj_steps, args.adj_every)
+        L = membrane_loss(uN, XN, X0, h3)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        L.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        results[name] = {"loss": float(L), "forward_s": t1 - t0, "adjoint_s": t2 - t1,
+                         "gk": float(k.grad), "gX": X0.grad.cpu().numpy()}
+        if prec != capi.FP64:
+            sv.close()
+    rng = np.random.default_rng(17)
+    h = 1e-6
+    worst = {"fp64": 0.0, "mixed": 0.0}
+    for _ in range(args.adj_dirs):
+        dX = rng.standard_normal(X.shape)
+        dX /= np.linalg.norm(dX)
+        dk = rng.standard_normal()
+        fd = (loss(0.5 + h * dk, X + h * dX) - loss(0.5 - h * dk, X - h * dX)) / (2 * h)
+        for name, r in results.items():
+            ad = r["gk"] * dk + float((r["gX"] * dX).sum())
+            worst[name] = max(worst[name], abs(fd - ad) / max(abs(fd), 1e-30))
+    fd_sv.close()
+    print(json.dumps({
+        "metric": "adjoint gradient vs central differences (max relative error over directions)", "case": "adjoint",
+        "config": {"grid": n, "markers": int(X.shape[0]), "steps": args.adj_steps, "checkpoint_every": args.adj_every,
+                   "directions": args.adj_dirs, "h": h, "tol": args.adj_tol, "dt": 5e-5, "mu": 0.01, "k": 0.5},
+        "fd_rel_error": worst,
+        "forward_steps_per_s": {k_: args.adj_steps / r["forward_s"] for k_, r in results.items()},
+        "adjoint_steps_per_s": {k_: args.adj_steps / r["adjoint_s"] for k_, r in results.items()},
+        "loss": {k_: r["loss"] for k_, r in results.items()},
+        "dL_dk": {k_: r["gk"] for k_, r in results.items()}}))
+
+
+def run_large_case(args, torch, local):
+    """512^3 periodic (--n 512 by default here), mu 0.002, dt 1e-5, 40 shells
+    of 25,000 markers (radius 0.05, minimum separation 0.12, 0.01 Y_2^m), k =
+    0.5, seeded solenoidal initial velocity: the FP64 forward and the mixed
+    forward over --large-steps IB steps from the same state (throughput and
+    the mixed form's error), then the adjoint of the mixed trajectory with
+    checkpoints every 5 steps (throughput). Peak device memory in use is
+    sampled after each phase. One JSON line."""
+    from afmibins_gb300 import capi, markers as mk
+    from afmibins_gb300.autograd import ib_trajectory, membrane_loss
+    n = args.n if args.n != 256 else 512
+    steps = args.large_steps
+    dev = torch.device("cuda", local)
+    X, nstart, nidx = mk.multi_shell(40, 25000, 0.05, 0.12, 0.01, seed=mk.SEED + 5)
+    vel = mk.random_solenoidal_velocity(n, n, n, rms=0.1, k_peak=4.0, seed=mk.SEED + 5)
+    free0, total = torch.cuda.mem_get_info()
+    peak = [0]
+
+    def sample():
+        f, _ = torch.cuda.mem_get_info()
+        peak[0] = max(peak[0], free0 - f)
+
+    out = {}
+    for name, prec in (("fp64", capi.FP64), ("mixed", capi.MIXED)):
+        with capi.Solver(n, mu=0.002, rho=1.0, dt=1e-5, tol=args.tol, k_spring=0.5, precision=prec) as sv:
+            sv.set_velocity(*vel)
+            sv.project()
+            sv.set_markers(X, nstart, nidx)
+            sample()
+            sv.synchronize()
+            t0 = time.perf_counter()
+            sv.ib_step(steps)
+            sv.synchronize()
+            dt_s = time.perf_counter() - t0
+            sample()
+            u = sv.get_velocity()
+            out[name] = {"steps_per_s": steps / dt_s, "u": u, "p": sv.get_pressure(), "X": sv.get_markers(),
+                         "stats": sv.stats()}
+    err = {"velocity": max(rel_err(a, b) for a, b in zip(out["mixed"]["u"], out["fp64"]["u"])),
+           "pressure": pressure_err(out["mixed"]["p"], out["fp64"]["p"], n, 0.002, 1e-5),
+           "marker_displacement": rel_err(out["mixed"]["X"] - X, out["fp64"]["X"] - X)}
+    # adjoint of the mixed trajectory, checkpoints every 5 steps
+    with capi.Solver(n, mu=0.002, rho=1.0, dt=1e-5, tol=args.tol, k_spring=0.5, precision=capi.MIXED) as sv:
+        sv.set_velocity(*vel)
+        sv.project()
+        v0 = tuple(torch.from_numpy(a).to(dev) for a in sv.get_velocity())
+        sv.set_markers(X, nstart, nidx)
+        X0 = torch.tensor(X, device=dev, requires_grad=True)
+        k = torch.tensor(0.5, dtype=torch.float64, device=dev, requires_grad=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        uN, XN = ib_trajectory(k, X0, sv, v0, steps, 5)
+        L = membrane_loss(uN, XN, X0, 1.0 / n ** 3)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        sample()
+        L.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        sample()
+        adj = {"forward_steps_per_s": steps / (t1 - t0), "adjoint_steps_per_s": steps / (t2 - t1),
+               "dL_dk": float(k.grad), "grad_X0_norm": float(X0.grad.norm())}
+    print(json.dumps({
+        "metric": "IB steps/s at 512^3 with 1,000,000 markers (mixed vs FP64) and adjoint throughput",
+        "case": "large", "config": {"grid": n, "markers": int(X.shape[0]), "steps": steps, "mu": 0.002, "dt": 1e-5,
+                                    "tol": args.tol, "checkpoint_every": 5},
+        "fp64_steps_per_s": out["fp64"]["steps_per_s"], "mixed_steps_per_s": out["mixed"]["steps_per_s"],
+        "speedup": out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"], "errors_vs_fp64": err,
+        "adjoint": adj, "peak_device_bytes": int(peak[0]), "device_bytes": int(total)}))
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -275,6 +432,12 @@ def main():
     torch.cuda.set_device(local)
     if args.case == "mg":
         run_mg_case(args, torch, local)
+        return
+    if args.case == "adjoint":
+        run_adjoint_case(args, torch, local)
+        return
+    if args.case == "large":
+        run_large_case(args, torch, local)
         return
     dist = None
     if world > 1:
