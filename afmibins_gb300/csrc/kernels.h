@@ -70,6 +70,9 @@ void launch_cg_apply(const Dims& d, int comp, double scale, const T* p, T* q, Re
 // update:    x += alpha p, r -= alpha q, n1 = r.r, beta = n1 / n0, n0 = n1
 template <typename T>
 void launch_cg_update(long long n, T* x, T* r, const T* p, const T* q, RedScratch sc, double* cgs, cudaStream_t s);
+// one Jacobi sweep x' = x + (b - H x) / diag(H) (x == nullptr: from zero)
+template <typename T>
+void launch_helm_jacobi(const Dims& d, int comp, double scale, const T* x, T* xo, const T* b, cudaStream_t s);
 // p' = beta p + r formed on the fly (out of place into pn), q = H p', p'.q and alpha
 template <typename T>
 void launch_cg_dir_apply(const Dims& d, int comp, double scale, const T* p, const T* r, T* pn, T* q, RedScratch sc,

@@ -394,6 +394,30 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_defect_bfp(Dims d, int comp,
     grid_sum<1>(a, sc, out);
 }
 
+// One Jacobi sweep on H x = b (the mixed form's FP32 inner Helmholtz solve):
+// x' = x + (b - H x) / diag, with H x from helm_point_at and diag its
+// diagonal (1 - 6 off in the interior, 1 - 4 off in 2D, 1 - 8 off on the
+// channel u/w wall rows, 1 on the channel v wall plane). x == nullptr starts
+// from zero: x' = b / diag.
+template <typename T>
+__global__ void k_helm_jacobi(Dims d, int comp, T s, const T* __restrict__ xv, T* __restrict__ xo,
+                              const T* __restrict__ b) {
+    AFMIB_XYZ
+    const long long i = lin(d, x, y, z);
+    const T off = s * T(d.n) * T(d.n);
+    T diag;
+    if (d.nz == 1) diag = T(1) - T(4) * off;
+    else if (d.channel && comp != 1 && (y == 0 || y == d.ny - 1)) diag = (T(1) - T(6) * off) - T(2) * off;
+    else if (d.channel && comp == 1 && y == 0) diag = T(1);
+    else diag = T(1) - T(6) * off;
+    if (!xv) {
+        xo[i] = b[i] / diag;
+        return;
+    }
+    const T hx = helm_point_at(d, comp, s, [xv](long long j) { return xv[j]; }, x, y, z);
+    xo[i] = xv[i] + (b[i] - hx) / diag;
+}
+
 // CG started from zero: r = p = b, n0 = b.b
 template <typename T>
 __global__ void __launch_bounds__(kRedBlock) k_cg_init_zero(long long N, const T* __restrict__ b, T* __restrict__ x,
@@ -516,6 +540,12 @@ template <typename T>
 void launch_cg_apply(const Dims& d, int comp, double scale, const T* p, T* q, RedScratch sc, double* cgs, cudaStream_t s) {
     k_cg_apply<T><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, T(scale), p, q, sc, cgs);
 }
+template <typename T>
+void launch_helm_jacobi(const Dims& d, int comp, double scale, const T* x, T* xo, const T* b, cudaStream_t s) {
+    k_helm_jacobi<T><<<grid3(d), dim3(BX, BY), 0, s>>>(d, comp, T(scale), x, xo, b);
+}
+template void launch_helm_jacobi<float>(const Dims&, int, double, const float*, float*, const float*, cudaStream_t);
+
 template <typename T>
 void launch_cg_dir_apply(const Dims& d, int comp, double scale, const T* p, const T* r, T* pn, T* q, RedScratch sc,
                          double* cgs, cudaStream_t s) {

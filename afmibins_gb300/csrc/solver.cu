@@ -66,6 +66,9 @@ struct afmib_solver {
     bool bfp_defects = false;
     // first multigrid level handled by the one-block V-cycle tail (-1: none; AFMIB_MG_TAIL=0)
     int tail_level = -1;
+    // mixed form: inner Helmholtz solves by fixed Jacobi sweeps where the
+    // operator's diagonal dominance bounds them (AFMIB_INNER_SOLVER=cg: CG)
+    bool jacobi_inner = true;
     // V-cycle blocks captured once into CUDA graphs and replayed (no host
     // interaction inside a V-cycle); not used while per-kernel profiling is on
     bool use_graphs = true;
@@ -217,14 +220,14 @@ enum ProfId {
     P_ADVECT, P_HELM_RHS, P_CG_INIT, P_CG_APPLY, P_CG_UPDATE, P_CG_DIR, P_RBGS, P_RESID, P_RESID_NORM,
     P_RESTRICT, P_PROLONG, P_COARSE, P_DIV, P_GRAD_SUB, P_MEAN, P_WALL, P_SPRINGS, P_PREP, P_SORT,
     P_TILES, P_SPREAD, P_INTERP, P_MARKER, P_HELM_DEFECT, P_LAP_DEFECT, P_CORRECT, P_ADJ_ADVECT, P_ADJ_MARKER,
-    P_RBGS0, P_RESID0, P_RESTRICT0, P_PROLONG0, P_CG_DIRAPPLY, P_TAIL, P_COUNT
+    P_RBGS0, P_RESID0, P_RESTRICT0, P_PROLONG0, P_CG_DIRAPPLY, P_TAIL, P_JACOBI, P_COUNT
 };
 const char* kProfNames[P_COUNT] = {
     "advect", "helm_rhs", "cg_init", "cg_apply", "cg_update", "cg_direction", "mg_rbgs", "mg_residual",
     "mg_residual_norm", "mg_restrict", "mg_prolong_add", "mg_coarse_cg", "div", "grad_sub", "mean_removal",
     "wall_update", "springs", "marker_prep", "radix_sort", "tile_bins", "spread_gather", "interp", "marker_update",
     "helm_defect_fp64", "lap_defect_fp64", "add_correction_fp64", "advect_adjoint", "marker_adjoint",
-    "mg_rbgs_fine", "mg_residual_fine", "mg_restrict_fine", "mg_prolong_add_fine", "cg_dir_apply", "mg_coarse_tail"};
+    "mg_rbgs_fine", "mg_residual_fine", "mg_restrict_fine", "mg_prolong_add_fine", "cg_dir_apply", "mg_coarse_tail", "helm_jacobi_fp32"};
 
 cudaEvent_t prof_event(afmib_solver* s) {
     if (!s->prof_pool.empty()) {
@@ -613,6 +616,35 @@ int cg_inner32(afmib_solver* s, int comp, double scale, double rel_tol, int* ite
     return AFMIB_OK;
 }
 
+// Jacobi sweeps for a relative reduction rel_tol of the inner Helmholtz
+// solve, or -1 when CG should be used. For the implicit operator (scale < 0)
+// H is strictly diagonally dominant: the Jacobi iteration contracts the
+// max-norm error by rho = k|off| / (1 + k|off|) per sweep (k = 6, 4 in 2D;
+// the channel wall rows contract faster), so ceil(log(rel_tol) / log(rho))
+// sweeps from zero reach rel_tol.
+int jacobi_sweeps(const Dims& d, double scale, double rel_tol) {
+    if (!(scale < 0)) return -1;
+    const double off = -scale * (double)d.n * (double)d.n, k = d.nz == 1 ? 4.0 : 6.0;
+    const double rho = k * off / (1.0 + k * off);
+    if (!(rho > 0) || !(rho < 1)) return -1;
+    const int sweeps = (int)std::ceil(std::log(rel_tol) / std::log(rho));
+    return sweeps >= 1 && sweeps <= 8 ? sweeps : -1;
+}
+
+// FP32 inner solve by fixed Jacobi sweeps: e32 = H^-1 d32 to rel_tol
+int jacobi_inner32(afmib_solver* s, int comp, double scale, int sweeps) {
+    const long long N = s->N();
+    float* bufs[2] = {s->e32, s->cg32_p};
+    for (int j = 0; j < sweeps; ++j) {
+        ProfScope ps(s, P_JACOBI, (double)N * 4 * (j == 0 ? 2 : 3));
+        float* out = bufs[(sweeps - 1 - j) % 2];
+        const float* in = j == 0 ? nullptr : bufs[(sweeps - j) % 2];
+        launch_helm_jacobi<float>(s->d, comp, scale, in, out, s->d32, s->st);
+    }
+    CKL();
+    return AFMIB_OK;
+}
+
 int helm_solve_mixed(afmib_solver* s, int comp, double scale, double* x, const double* b) {
     const long long N = s->N();
     int outer = 0;
@@ -631,7 +663,9 @@ int helm_solve_mixed(afmib_solver* s, int comp, double scale, double* x, const d
         if (!std::isfinite(nr)) return s->fail(AFMIB_ERR_NAN, "Helmholtz residual is not finite");
         if (nr <= s->cfg.tol) break;
         if (outer >= s->cfg.max_mg_cycles) return s->fail(AFMIB_ERR_NOCONV, "defect-correction cap reached (Helmholtz)");
-        TRY(cg_inner32(s, comp, scale, s->cfg.inner_tol, nullptr));
+        const int sweeps = s->jacobi_inner ? jacobi_sweeps(s->d, scale, s->cfg.inner_tol) : -1;
+        if (sweeps > 0) TRY(jacobi_inner32(s, comp, scale, sweeps));
+        else TRY(cg_inner32(s, comp, scale, s->cfg.inner_tol, nullptr));
         {
             ProfScope ps(s, P_CORRECT, (double)N * (8 + 4 + 8));
             launch_add_correction<float>(N, x, s->e32, s->st);
@@ -1319,6 +1353,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_PIPE_MIN_NX")) s->pipe_min_nx = std::atoi(e);
     if (const char* e = std::getenv("AFMIB_BFP")) s->bfp_defects = std::string(e) == "1";
     if (const char* e = std::getenv("AFMIB_INNER_CYCLES")) s->inner_cycles = std::max(1, std::atoi(e));
+    if (const char* e = std::getenv("AFMIB_INNER_SOLVER")) s->jacobi_inner = std::string(e) != "cg";
     if (const char* e = std::getenv("AFMIB_GRAPHS")) s->use_graphs = std::string(e) != "0";
     if (g.proj_start < AFMIB_START_DEFAULT || g.proj_start > AFMIB_START_WARM)
         return s->fail(AFMIB_ERR_ARG, "proj_start must be AFMIB_START_DEFAULT, _ZERO or _WARM");

@@ -405,3 +405,28 @@ def test_multigrid_tail_equals_level_launches(monkeypatch, bc, precision, n):
             out[mode] = sv.mg_solve(b)
     assert out["0"][1] == out["1"][1]
     assert np.array_equal(out["0"][0], out["1"][0])
+
+
+@pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
+def test_inner_jacobi_matches_inner_cg(monkeypatch, bc):
+    """Mixed form: the FP32 inner Helmholtz solves by a fixed number of Jacobi
+    sweeps (bounded by the operator's diagonal dominance) or by CG; the FP64
+    outer loop stops on the same residual test, so the sub-steps agree to the
+    solver tolerance."""
+    n = 32
+    channel = bc == capi.BC_CHANNEL
+    g = po.Grid(n, n, n, n, channel=channel)
+    rng = np.random.default_rng(24)
+    u, v, w = 0.1 * rng.standard_normal(g.ncell), 0.1 * rng.standard_normal(g.nv), 0.1 * rng.standard_normal(g.ncell)
+    f = [rng.standard_normal(g.ncell), rng.standard_normal(g.nv), rng.standard_normal(g.ncell)]
+    out = {}
+    for mode in ("cg", "jacobi"):
+        monkeypatch.setenv("AFMIB_INNER_SOLVER", mode)
+        with capi.Solver(n, bc=bc, precision=capi.MIXED, mu=0.01, rho=1.0, dt=1e-3, tol=1e-12) as sv:
+            sv.set_velocity(u, v, w)
+            sv.project()
+            for _ in range(4):
+                sv.ns_step(*f)
+            out[mode] = sv.get_velocity()
+    for a, b in zip(out["cg"], out["jacobi"]):
+        assert rel(b, a) < 1e-10
