@@ -185,21 +185,72 @@ __device__ __forceinline__ void wait_pending() {
 }
 }  // namespace pipe
 
-constexpr int kPipeThreads = 512;
+constexpr int kPipeThreads = 256;
+
+// Gauss-Seidel value of one cell from its six neighbours and b, the
+// per-colour kernel's arithmetic (rbgs_cell) in the same order.
+template <typename T, bool CH>
+__device__ __forceinline__ T gs_value(T xm, T xp, T zm, T zp, T ym, T yp, T bv, T inv, int gy, int ny) {
+    T S = (xm + xp) + (zm + zp);
+    T c = T(6);
+    if (CH) {
+        if (gy > 0) S += ym; else c -= T(1);
+        if (gy < ny - 1) S += yp; else c -= T(1);
+    } else {
+        S += ym + yp;
+    }
+    const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
+    return (S - bv * inv) * rc;
+}
+
+template <typename T>
+struct Vec4;
+template <>
+struct Vec4<float> {
+    typedef float4 type;
+};
+template <>
+struct Vec4<double> {
+    typedef double4 type;
+};
+
+// One colour of one plane row segment by quads: the quad of four cells at
+// x = 4q .. 4q+3 holds two cells of the colour, at offsets par and par + 2.
+template <typename T, bool CH>
+__device__ __forceinline__ void gs_quad(T* row, const T* rowm, const T* rowp, const T* zmr, const T* zpr, const T* br,
+                                        int q, int nq, int par, T inv, int gy, int ny) {
+    typedef typename Vec4<T>::type V;
+    V c = reinterpret_cast<V*>(row)[q];
+    const V n = reinterpret_cast<const V*>(rowm)[q], s = reinterpret_cast<const V*>(rowp)[q];
+    const V a = reinterpret_cast<const V*>(zmr)[q], e = reinterpret_cast<const V*>(zpr)[q];
+    const V bb = reinterpret_cast<const V*>(br)[q];
+    if (par == 0) {
+        const T left = row[4 * (q == 0 ? nq : q) - 1];
+        c.x = gs_value<T, CH>(left, c.y, a.x, e.x, n.x, s.x, bb.x, inv, gy, ny);
+        c.z = gs_value<T, CH>(c.y, c.w, a.z, e.z, n.z, s.z, bb.z, inv, gy, ny);
+    } else {
+        const T right = row[q + 1 == nq ? 0 : 4 * (q + 1)];
+        c.y = gs_value<T, CH>(c.x, c.z, a.y, e.y, n.y, s.y, bb.y, inv, gy, ny);
+        c.w = gs_value<T, CH>(c.z, right, a.w, e.w, n.w, s.w, bb.w, inv, gy, ny);
+    }
+    reinterpret_cast<V*>(row)[q] = c;
+}
 
 // Power-of-two extents only (every level the sweep serves): indices are
 // shifts and masks. CH: channel walls in y (Neumann rows, no wrap in y).
 template <typename T, int D, bool CH>
-__global__ void __launch_bounds__(kPipeThreads) k_rbgs_pipe(Dims d, const T* __restrict__ xin, T* __restrict__ xout,
+__global__ void __launch_bounds__(kPipeThreads, 1) k_rbgs_pipe(Dims d, const T* __restrict__ xin, T* __restrict__ xout,
                                                             const T* __restrict__ b, int FY, int ZC, int lnx, int lny) {
     extern __shared__ __align__(128) unsigned char smem[];
+    typedef typename Vec4<T>::type V;
     constexpr int R = D + 4;
     const int nx = d.nx, XR = FY + 4, BR = FY + 2;
     const int xplane = XR * nx, bplane = BR * nx;
     T* xs = (T*)smem;                 // [R][XR][nx]
     T* bs = xs + (size_t)R * xplane;  // [R][BR][nx]
     const int tid = threadIdx.x;
-    const int lhx = lnx - 1, xmask = nx - 1, hmask = (nx >> 1) - 1, ymask = d.ny - 1, zmask = d.nz - 1;
+    const int lq = lnx - 2, nq = nx >> 2, qmask = nq - 1;  // quads per row
+    const int ymask = d.ny - 1, zmask = d.nz - 1;
     const int lcpr = lnx + (sizeof(T) == 8 ? 3 : 2) - 4;  // log2 of the 16-byte chunks per row
     const int cmask = (1 << lcpr) - 1;
     const T inv = T(1) / (T(d.n) * T(d.n));
@@ -240,22 +291,12 @@ __global__ void __launch_bounds__(kPipeThreads) k_rbgs_pipe(Dims d, const T* __r
                 // red cells of plane k, rows tile +- 1
                 const int gz = k & zmask;
                 const T* B0 = bs + (size_t)sk * bplane;
-                for (int e = tid; e < ((FY + 2) << lhx); e += kPipeThreads) {
-                    const int rr = e >> lhx, gy = y0 - 1 + rr;
+                for (int e = tid; e < ((FY + 2) << lq); e += kPipeThreads) {
+                    const int rr = e >> lq, gy = y0 - 1 + rr;
                     if (!row_ok(gy)) continue;
-                    const int xi = 2 * (e & hmask) + (((gy & ymask) + gz) & 1);
                     const int o = (rr + 1) << lnx;
-                    T* c0 = X0 + o;
-                    T S = (c0[(xi - 1) & xmask] + c0[(xi + 1) & xmask]) + (Xm[o + xi] + Xp[o + xi]);
-                    T c = T(6);
-                    if (CH) {
-                        if (gy > 0) S += c0[xi - nx]; else c -= T(1);
-                        if (gy < d.ny - 1) S += c0[xi + nx]; else c -= T(1);
-                    } else {
-                        S += c0[xi - nx] + c0[xi + nx];
-                    }
-                    const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
-                    c0[xi] = (S - B0[(rr << lnx) + xi] * inv) * rc;
+                    gs_quad<T, CH>(X0 + o, X0 + o - nx, X0 + o + nx, Xm + o, Xp + o, B0 + (rr << lnx), e & qmask, nq,
+                                   ((gy & ymask) + gz) & 1, inv, gy, d.ny);
                 }
             }
             __syncthreads();
@@ -265,29 +306,19 @@ __global__ void __launch_bounds__(kPipeThreads) k_rbgs_pipe(Dims d, const T* __r
                 const int gz = kb & zmask;
                 T* const Ym = xs + (size_t)skm2 * xplane;
                 const T* B1 = bs + (size_t)skm1 * bplane;
-                for (int e = tid; e < (FY << lhx); e += kPipeThreads) {
-                    const int rr = e >> lhx, gy = y0 + rr;
-                    const int xi = 2 * (e & hmask) + ((gy + gz + 1) & 1);
+                for (int e = tid; e < (FY << lq); e += kPipeThreads) {
+                    const int rr = e >> lq, gy = y0 + rr;
                     const int o = (rr + 2) << lnx;
-                    T* c0 = Xm + o;
-                    T S = (c0[(xi - 1) & xmask] + c0[(xi + 1) & xmask]) + (Ym[o + xi] + X0[o + xi]);
-                    T c = T(6);
-                    if (CH) {
-                        if (gy > 0) S += c0[xi - nx]; else c -= T(1);
-                        if (gy < d.ny - 1) S += c0[xi + nx]; else c -= T(1);
-                    } else {
-                        S += c0[xi - nx] + c0[xi + nx];
-                    }
-                    const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
-                    c0[xi] = (S - B1[((rr + 1) << lnx) + xi] * inv) * rc;
+                    gs_quad<T, CH>(Xm + o, Xm + o - nx, Xm + o + nx, Ym + o, X0 + o, B1 + ((rr + 1) << lnx), e & qmask,
+                                   nq, (gy + gz + 1) & 1, inv, gy, d.ny);
                 }
             }
             __syncthreads();
             if (kb >= z0) {
                 // plane k-1 of the tile is final
-                T* dst = xout + ((((long long)kb << lny) + y0) << lnx);
-                const T* src = Xm + 2 * nx;
-                for (int e = tid; e < (FY << lnx); e += kPipeThreads) dst[e] = src[e];
+                V* dst = reinterpret_cast<V*>(xout + ((((long long)kb << lny) + y0) << lnx));
+                const V* src = reinterpret_cast<const V*>(Xm + 2 * nx);
+                for (int e = tid; e < (FY << lq); e += kPipeThreads) dst[e] = src[e];
             }
             // the slot of plane k-2 is free: its last reader, the black update, is behind the barrier
             issue(next, snext);
