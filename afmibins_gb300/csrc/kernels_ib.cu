@@ -276,7 +276,8 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
                                                                 const int* __restrict__ slot, const int* __restrict__ ctab,
                                                                 const int* __restrict__ list, const int* __restrict__ count,
                                                                 int cap, T* __restrict__ fu, T* __restrict__ fv,
-                                                                T* __restrict__ fw, int* __restrict__ flag) {
+                                                                T* __restrict__ fw, int* __restrict__ flag,
+                                                                int* __restrict__ ovf_list, int* __restrict__ ovf_count) {
     // 3D: TZ == TS, the neighbourhood grows by 2 cells per side along every
     // axis. 2D (TZ == 1, nz == 1): one plane, no z halo.
     constexpr int NT = TS * TS * TZ, E = TS + 4, EZ = TZ == 1 ? 1 : TS + 4, HZ = TZ == 1 ? 0 : 2;
@@ -371,8 +372,12 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
             }
         }
         if (tid == NT - 1) s_estart[E3] = nc_all;
-        if (nc_all > cap && tid == 0) atomicExch(flag, 3);
+        if (nc_all > cap && tid == 0) {
+            if (ovf_list) ovf_list[atomicAdd(ovf_count, 1)] = t;  // left to the large-capacity pass
+            else atomicExch(flag, 3);
+        }
         __syncthreads();
+        if (nc_all > cap && ovf_list) continue;  // block-uniform
         const int nc = nc_all < cap ? nc_all : cap;
         // ---- one component at a time
         for (int comp = 0; comp < 3; ++comp) {
@@ -542,11 +547,12 @@ size_t spread_smem_bytes(int TS, int TZ, int cap) {
 template <typename T, int TS, int TZ>
 static void spread_launch(const Dims& d, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
                           double scale, const int* slot, const int* ctab, const int* list, const int* count,
-                          int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, cudaStream_t s) {
+                          int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, int* ovf_list, int* ovf_count,
+                          cudaStream_t s) {
     const size_t smem = spread_smem_bytes<T>(TS, TZ, cap);
     // opt in to exactly the dynamic shared memory this launch uses (the
     // kernel's static shared memory counts against the same 227 KB)
-    static size_t configured = 0;
+    static size_t configured = 0;  // the largest capacity asked for so far
     if (configured < smem) {
         if (cudaFuncSetAttribute(k_spread_gather<T, TS, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess)
@@ -556,22 +562,23 @@ static void spread_launch(const Dims& d, int M, const int* perm, MarkerW<T> mw, 
     int blocks = max_tiles < 152 * 4 ? max_tiles : 152 * 4;
     if (blocks < 1) blocks = 1;
     k_spread_gather<T, TS, TZ><<<blocks, TS * TS * TZ, smem, s>>>(d, M, perm, mw, G, vol, scale, slot, ctab, list,
-                                                                  count, cap, fu, fv, fw, flag);
+                                                                  count, cap, fu, fv, fw, flag, ovf_list, ovf_count);
 }
 
 template <typename T>
 void launch_spread_gather(const Dims& d, int TS, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
                           double scale, const int* slot, const int* ctab, const int* list, const int* count,
-                          int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, cudaStream_t s) {
+                          int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, int* ovf_list, int* ovf_count,
+                          cudaStream_t s) {
     const bool flat = d.nz == 1;
-    if (TS == 8 && !flat)
-        spread_launch<T, 8, 8>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, flag, s);
-    else if (TS == 4 && !flat)
-        spread_launch<T, 4, 4>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, flag, s);
-    else if (TS == 8)
-        spread_launch<T, 8, 1>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, flag, s);
-    else
-        spread_launch<T, 4, 1>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, flag, s);
+#define AFMIB_SPREAD(TSV, TZV)                                                                                    \
+    spread_launch<T, TSV, TZV>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, \
+                               flag, ovf_list, ovf_count, s)
+    if (TS == 8 && !flat) AFMIB_SPREAD(8, 8);
+    else if (TS == 4 && !flat) AFMIB_SPREAD(4, 4);
+    else if (TS == 8) AFMIB_SPREAD(8, 1);
+    else AFMIB_SPREAD(4, 1);
+#undef AFMIB_SPREAD
 }
 
 template <typename T, typename TF>
@@ -591,7 +598,7 @@ void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, do
     template size_t spread_smem_bytes<T>(int, int, int);                                                             \
     template void launch_spread_gather<T>(const Dims&, int, int, const int*, MarkerW<T>, const T*, const double*, \
                                           double, const int*, const int*, const int*, const int*, int, int, T*,  \
-                                          T*, T*, int*, cudaStream_t);                                          \
+                                          T*, T*, int*, int*, int*, cudaStream_t);                              \
     template void launch_interp<T, double>(const Dims&, int, const int*, MarkerW<T>, const double*, const double*, \
                                            const double*, double*, cudaStream_t);                               \
     template void launch_interp<T, float>(const Dims&, int, const int*, MarkerW<T>, const float*, const float*,  \

@@ -546,8 +546,39 @@ __device__ __forceinline__ void tail_sweep(const Dims& d, T* x, const T* b, int 
     __syncthreads();
 }
 
+// With `staged`, the levels' x, b, r (and the FP64 coarsest-level vectors)
+// live in shared memory for the whole V-cycle: the top level's x and b are
+// read in, the top level's x is written back (the only result the level
+// above uses). Without it the phases work on the global arrays.
 template <typename T>
-__global__ void __launch_bounds__(kRedBlock) k_vcycle_tail(TailLevels<T> a) {
+__global__ void __launch_bounds__(kRedBlock) k_vcycle_tail(TailLevels<T> g, int staged) {
+    extern __shared__ __align__(16) unsigned char tsm[];
+    TailLevels<T> a = g;
+    if (staged) {
+        // layout: per level x, b, r (T), then cx64, cb64, cr64, cw_p, cw_q (double)
+        size_t off = 0;
+        for (int l = 0; l < a.nlev; ++l) {
+            const long long n = a.d[l].ncell();
+            a.x[l] = (T*)(tsm + off);
+            a.b[l] = a.x[l] + n;
+            a.r[l] = a.b[l] + n;
+            off += (size_t)3 * n * sizeof(T);
+            off = (off + 15) & ~(size_t)15;
+        }
+        const long long nc = a.d[a.nlev - 1].ncell();
+        double* dp = (double*)(tsm + off);
+        a.cx64 = dp;
+        a.cb64 = dp + nc;
+        a.cr64 = dp + 2 * nc;
+        a.cw_p = dp + 3 * nc;
+        a.cw_q = dp + 4 * nc;
+        const long long n0 = a.d[0].ncell();
+        for (long long i = threadIdx.x; i < n0; i += blockDim.x) {
+            a.x[0][i] = g.x[0][i];
+            a.b[0][i] = g.b[0][i];
+        }
+        __syncthreads();
+    }
     for (int l = 0; l + 1 < a.nlev; ++l) {
         const Dims& d = a.d[l];
         for (int j = 0; j < a.nu1; ++j) {
@@ -592,6 +623,10 @@ __global__ void __launch_bounds__(kRedBlock) k_vcycle_tail(TailLevels<T> a) {
             tail_sweep(d, a.x[l], a.b[l], 0);
             tail_sweep(d, a.x[l], a.b[l], 1);
         }
+    }
+    if (staged) {
+        const long long n0 = a.d[0].ncell();
+        for (long long i = threadIdx.x; i < n0; i += blockDim.x) g.x[0][i] = a.x[0][i];
     }
 }
 
@@ -725,7 +760,19 @@ template void launch_lap_defect<float>(const Dims&, float*, const double*, const
 
 template <typename T>
 void launch_vcycle_tail(const TailLevels<T>& a, cudaStream_t s) {
-    k_vcycle_tail<T><<<1, kRedBlock, 0, s>>>(a);
+    // shared-memory staging when the levels fit
+    size_t bytes = 0;
+    for (int l = 0; l < a.nlev; ++l) {
+        bytes += (size_t)3 * a.d[l].ncell() * sizeof(T);
+        bytes = (bytes + 15) & ~(size_t)15;
+    }
+    bytes += (size_t)5 * a.d[a.nlev - 1].ncell() * sizeof(double);
+    constexpr size_t kMax = 160 * 1024;
+    static bool attr = false;
+    if (!attr) attr = cudaFuncSetAttribute(k_vcycle_tail<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMax) ==
+                      cudaSuccess;
+    if (attr && bytes <= kMax) k_vcycle_tail<T><<<1, kRedBlock, bytes, s>>>(a, 1);
+    else k_vcycle_tail<T><<<1, kRedBlock, 0, s>>>(a, 0);
 }
 template <typename T>
 void launch_coarse_solve(const Dims& d, T* x, T* b, T* r, T* p, T* q, double tol, int maxit, int* status, cudaStream_t s) {

@@ -98,7 +98,8 @@ struct afmib_solver {
     int *vals = nullptr, *vals2 = nullptr, *perm = nullptr;
     int TS = 0, TZ = 0, ntx = 0, nty = 0, ntz = 0, ntiles = 0;  // TZ: tile depth (TS; 1 on a 2D grid)
     int tile_cells() const { return TS * TS * TZ; }
-    int *tstart = nullptr, *tend = nullptr, *tlist = nullptr, *tcount = nullptr;
+    // tcount: [0] active output tiles, [1] occupied tiles, [2] tiles left to the large-capacity spreading pass
+    int *tstart = nullptr, *tend = nullptr, *tlist = nullptr, *tcount = nullptr, *tovf = nullptr;
     int *tslot = nullptr, *tocc = nullptr, *ctab = nullptr;
     int ctab_cap = 0;  // occupied tiles the cell table can hold
     MarkerW<double> mw{};
@@ -905,6 +906,21 @@ int bin_markers(afmib_solver* s, const double* P, bool fp32 = false) {
     return AFMIB_OK;
 }
 
+// Spreading in two passes: blocks sized for `cap_small` neighbourhood markers
+// (two blocks per SM) take every active tile whose neighbourhood fits and list
+// the others, which a second pass with `cap_large` handles. Each tile is
+// computed once, by one of the passes, with the same arithmetic.
+template <typename T>
+int spread_two_pass(afmib_solver* s, MarkerW<T> mw, const T* G, const double* vol, double scale, T* fu, T* fv, T* fw,
+                    int cap_small, int cap_large) {
+    CK(cudaMemsetAsync(s->tcount + 2, 0, sizeof(int), s->st));
+    launch_spread_gather<T>(s->d, s->TS, s->M, s->perm, mw, G, vol, scale, s->tslot, s->ctab, s->tlist, s->tcount,
+                            s->ntiles, cap_small, fu, fv, fw, s->dflag, s->tovf, s->tcount + 2, s->st);
+    launch_spread_gather<T>(s->d, s->TS, s->M, s->perm, mw, G, vol, scale, s->tslot, s->ctab, s->tovf, s->tcount + 2,
+                            s->ntiles, cap_large, fu, fv, fw, s->dflag, nullptr, nullptr, s->st);
+    return AFMIB_OK;
+}
+
 // f = scale * S(X) G with the FP64 bins and weights of the last bin_markers call
 int spread_generic(afmib_solver* s, const double* G, const double* vol, double scale, double* fu, double* fv,
                    double* fw) {
@@ -915,8 +931,7 @@ int spread_generic(afmib_solver* s, const double* G, const double* vol, double s
     const double touched = (double)s->stats.spread_tiles * s->tile_cells();
     {
         ProfScope ps(s, P_SPREAD, (double)s->M * (24 + 3 * 8 + 8 + 8) + 3 * touched * 8);
-        launch_spread_gather<double>(s->d, s->TS, s->M, s->perm, s->mw, G, vol, scale, s->tslot, s->ctab, s->tlist,
-                                     s->tcount, s->ntiles, 1536, fu, fv, fw, s->dflag, s->st);
+        TRY(spread_two_pass<double>(s, s->mw, G, vol, scale, fu, fv, fw, 896, 1536));
     }
     CKL();
     return AFMIB_OK;
@@ -941,8 +956,7 @@ int spread_forces(afmib_solver* s, const double* vol, double* fu, double* fv, do
     const double touched = (double)s->stats.spread_tiles * s->tile_cells();
     {
         ProfScope ps(s, P_SPREAD, (double)s->M * (24 + 3 * 8 + 8 + 8) + 3 * touched * 8);
-        launch_spread_gather<double>(s->d, s->TS, s->M, s->perm, s->mw, s->G, vol, n3, s->tslot, s->ctab, s->tlist,
-                                     s->tcount, s->ntiles, cap, fu, fv, fw, s->dflag, s->st);
+        TRY(spread_two_pass<double>(s, s->mw, s->G, vol, n3, fu, fv, fw, 896, cap));
     }
     CKL();
     return AFMIB_OK;
@@ -956,9 +970,7 @@ int spread_forces32(afmib_solver* s, const double* vol) {
     const double touched = (double)s->stats.spread_tiles * s->tile_cells();
     {
         ProfScope ps(s, P_SPREAD, (double)s->M * (24 + 3 * 4 + 8 + 8) + 3 * touched * 4);
-        launch_spread_gather<float>(s->d, s->TS, s->M, s->perm, s->mw32, s->G32, vol, n3, s->tslot, s->ctab,
-                                    s->tlist, s->tcount, s->ntiles, cap, s->f32[0], s->f32[1], s->f32[2], s->dflag,
-                                    s->st);
+        TRY(spread_two_pass<float>(s, s->mw32, s->G32, vol, n3, s->f32[0], s->f32[1], s->f32[2], 1792, cap));
     }
     CKL();
     return AFMIB_OK;
@@ -1327,7 +1339,8 @@ int setup_tiles(afmib_solver* s) {
     TRY(dalloc(s, &s->tstart, s->ntiles));
     TRY(dalloc(s, &s->tend, s->ntiles));
     TRY(dalloc(s, &s->tlist, s->ntiles));
-    TRY(dalloc(s, &s->tcount, 2));
+    TRY(dalloc(s, &s->tcount, 3));
+    TRY(dalloc(s, &s->tovf, s->ntiles));
     TRY(dalloc(s, &s->tslot, s->ntiles));
     TRY(dalloc(s, &s->tocc, s->ntiles));
     return AFMIB_OK;

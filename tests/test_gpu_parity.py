@@ -260,6 +260,13 @@ def test_failure_statuses_are_reported():
         with pytest.raises(capi.AfmibError) as e:
             sv.mg_solve(b)
         assert e.value.status == capi.AFMIB_ERR_NAN
+    # more markers near one tile than the spreading capacity: a status, no fault
+    with capi.Solver(32) as sv:
+        rng = np.random.default_rng(26)
+        X = 0.5 + rng.uniform(-1.0, 1.0, (2000, 3)) / 32
+        with pytest.raises(capi.AfmibError) as e:
+            sv.spread(X, rng.standard_normal((3, 2000)))
+        assert e.value.status == capi.AFMIB_ERR_CAPACITY
     # bad configuration
     with pytest.raises(capi.AfmibError) as e:
         capi.Solver(16, mu=0.01, rho=-1.0)
@@ -430,3 +437,18 @@ def test_inner_jacobi_matches_inner_cg(monkeypatch, bc):
             out[mode] = sv.get_velocity()
     for a, b in zip(out["cg"], out["jacobi"]):
         assert rel(b, a) < 1e-10
+
+
+def test_spread_dense_cluster_takes_large_capacity_pass():
+    """1,200 markers inside two cells: their tiles' neighbourhoods exceed the
+    first pass's capacity and are spread by the large-capacity pass, with the
+    same result as the oracle."""
+    n = 32
+    g = po.Grid(n, n, n, n, channel=False)
+    rng = np.random.default_rng(25)
+    X = 0.5 + rng.uniform(-1.0, 1.0, (1200, 3)) / n
+    F = rng.standard_normal((3, 1200))
+    with capi.Solver(n) as sv:
+        fx, fy, fz = sv.spread(X, F)
+    for comp, f in enumerate((fx, fy, fz)):
+        assert rel(f, po.spread(g, comp, X, F[comp])) < OPS_TOL
