@@ -400,22 +400,35 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_defect_bfp(Dims d, int comp,
 // channel u/w wall rows, 1 on the channel v wall plane). x == nullptr starts
 // from zero: x' = b / diag.
 template <typename T>
+__device__ __forceinline__ T helm_diag(const Dims& d, int comp, T off, int y) {
+    if (d.nz == 1) return T(1) - T(4) * off;
+    if (d.channel && comp != 1 && (y == 0 || y == d.ny - 1)) return (T(1) - T(6) * off) - T(2) * off;
+    if (d.channel && comp == 1 && y == 0) return T(1);
+    return T(1) - T(6) * off;
+}
+
+// ZU cells along z per thread, all computed before any is stored (the
+// sweep is out of place, so this only puts ZU cells' loads in flight at once)
+template <typename T, int ZU>
 __global__ void k_helm_jacobi(Dims d, int comp, T s, const T* __restrict__ xv, T* __restrict__ xo,
                               const T* __restrict__ b) {
-    AFMIB_XYZ
-    const long long i = lin(d, x, y, z);
+    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z0 = blockIdx.z * ZU;
+    if (x >= d.nx || y >= d.ny) return;
     const T off = s * T(d.n) * T(d.n);
-    T diag;
-    if (d.nz == 1) diag = T(1) - T(4) * off;
-    else if (d.channel && comp != 1 && (y == 0 || y == d.ny - 1)) diag = (T(1) - T(6) * off) - T(2) * off;
-    else if (d.channel && comp == 1 && y == 0) diag = T(1);
-    else diag = T(1) - T(6) * off;
-    if (!xv) {
-        xo[i] = b[i] / diag;
-        return;
+    const T diag = helm_diag(d, comp, off, y);
+    T val[ZU];
+#pragma unroll
+    for (int u = 0; u < ZU; ++u) {
+        const long long i = lin(d, x, y, z0 + u);
+        if (!xv) {
+            val[u] = b[i] / diag;
+        } else {
+            const T hx = helm_point_at(d, comp, s, [xv](long long j) { return xv[j]; }, x, y, z0 + u);
+            val[u] = xv[i] + (b[i] - hx) / diag;
+        }
     }
-    const T hx = helm_point_at(d, comp, s, [xv](long long j) { return xv[j]; }, x, y, z);
-    xo[i] = xv[i] + (b[i] - hx) / diag;
+#pragma unroll
+    for (int u = 0; u < ZU; ++u) xo[lin(d, x, y, z0 + u)] = val[u];
 }
 
 // CG started from zero: r = p = b, n0 = b.b
@@ -542,7 +555,12 @@ void launch_cg_apply(const Dims& d, int comp, double scale, const T* p, T* q, Re
 }
 template <typename T>
 void launch_helm_jacobi(const Dims& d, int comp, double scale, const T* x, T* xo, const T* b, cudaStream_t s) {
-    k_helm_jacobi<T><<<grid3(d), dim3(BX, BY), 0, s>>>(d, comp, T(scale), x, xo, b);
+    const dim3 blk(BX, BY);
+    if (d.nz % 8 == 0)
+        k_helm_jacobi<T, 8><<<dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / 8), blk, 0, s>>>(d, comp, T(scale), x,
+                                                                                                  xo, b);
+    else
+        k_helm_jacobi<T, 1><<<grid3(d), blk, 0, s>>>(d, comp, T(scale), x, xo, b);
 }
 template void launch_helm_jacobi<float>(const Dims&, int, double, const float*, float*, const float*, cudaStream_t);
 

@@ -621,15 +621,18 @@ int cg_inner32(afmib_solver* s, int comp, double scale, double rel_tol, int* ite
 // solve, or -1 when CG should be used. For the implicit operator (scale < 0)
 // H is strictly diagonally dominant: the Jacobi iteration contracts the
 // max-norm error by rho = k|off| / (1 + k|off|) per sweep (k = 6, 4 in 2D;
-// the channel wall rows contract faster), so ceil(log(rel_tol) / log(rho))
-// sweeps from zero reach rel_tol.
+// the channel wall rows contract faster). The outer loop measures the 2-norm
+// of the residual, and the defects concentrate near the membrane (their
+// max/RMS ratio is large), so the sweeps aim at rel_tol / 100 in the max
+// norm: ceil(log(rel_tol / 100) / log(rho)) sweeps from zero.
 int jacobi_sweeps(const Dims& d, double scale, double rel_tol) {
     if (!(scale < 0)) return -1;
     const double off = -scale * (double)d.n * (double)d.n, k = d.nz == 1 ? 4.0 : 6.0;
     const double rho = k * off / (1.0 + k * off);
     if (!(rho > 0) || !(rho < 1)) return -1;
-    const int sweeps = (int)std::ceil(std::log(rel_tol) / std::log(rho));
-    return sweeps >= 1 && sweeps <= 8 ? sweeps : -1;
+    int sweeps = (int)std::ceil(std::log(rel_tol * 1e-2) / std::log(rho));
+    if (const char* e = std::getenv("AFMIB_JACOBI_SWEEPS")) sweeps = std::atoi(e);
+    return sweeps >= 1 && sweeps <= 10 ? sweeps : -1;
 }
 
 // FP32 inner solve by fixed Jacobi sweeps: e32 = H^-1 d32 to rel_tol
