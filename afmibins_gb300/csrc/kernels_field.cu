@@ -395,7 +395,8 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_defect_bfp(Dims d, int comp,
 }
 
 // One Jacobi sweep on H x = b (the mixed form's FP32 inner Helmholtz solve):
-// x' = x + (b - H x) / diag, with H x from helm_point_at and diag its
+// x' = x + (b - H x) / diag (as a product with the row's reciprocal), with
+// H x from helm_point_at and diag its
 // diagonal (1 - 6 off in the interior, 1 - 4 off in 2D, 1 - 8 off on the
 // channel u/w wall rows, 1 on the channel v wall plane). x == nullptr starts
 // from zero: x' = b / diag.
@@ -415,16 +416,16 @@ __global__ void k_helm_jacobi(Dims d, int comp, T s, const T* __restrict__ xv, T
     const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z0 = blockIdx.z * ZU;
     if (x >= d.nx || y >= d.ny) return;
     const T off = s * T(d.n) * T(d.n);
-    const T diag = helm_diag(d, comp, off, y);
+    const T rdiag = T(1) / helm_diag(d, comp, off, y);
     T val[ZU];
 #pragma unroll
     for (int u = 0; u < ZU; ++u) {
         const long long i = lin(d, x, y, z0 + u);
         if (!xv) {
-            val[u] = b[i] / diag;
+            val[u] = b[i] * rdiag;
         } else {
             const T hx = helm_point_at(d, comp, s, [xv](long long j) { return xv[j]; }, x, y, z0 + u);
-            val[u] = xv[i] + (b[i] - hx) / diag;
+            val[u] = xv[i] + (b[i] - hx) * rdiag;
         }
     }
 #pragma unroll

@@ -582,14 +582,21 @@ __global__ void __launch_bounds__(kRedBlock) k_coarse_cg(Dims d, T* __restrict__
 // solve is the same one-block CG, so the result equals the launch-by-launch
 // V-cycle bit for bit.
 // ---------------------------------------------------------------------------
+// cell index -> (x, y, z) for the tail's small levels (32-bit arithmetic)
+__device__ __forceinline__ void tail_xyz(const Dims& d, int i, int& x, int& y, int& z) {
+    const int sxy = d.nx * d.ny;
+    z = i / sxy;
+    const int rem = i - z * sxy;
+    y = rem / d.nx;
+    x = rem - y * d.nx;
+}
+
 template <typename T>
 __device__ __forceinline__ void tail_sweep(const Dims& d, T* x, const T* b, int color) {
-    const int hx = d.nx / 2;
-    const long long total = (long long)hx * d.ny * d.nz;
-    for (long long e = threadIdx.x; e < total; e += blockDim.x) {
-        const int t = (int)(e % hx);
-        const long long rest = e / hx;
-        const int y = (int)(rest % d.ny), z = (int)(rest / d.ny);
+    const int hx = d.nx / 2, total = hx * d.ny * d.nz;
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int row = e / hx, t = e - row * hx;
+        const int z = row / d.ny, y = row - z * d.ny;
         const int xx = 2 * t + ((y + z + color) & 1);
         if (xx < d.nx) rbgs_cell(d, x, b, xx, y, z);
     }
@@ -635,14 +642,19 @@ __global__ void __launch_bounds__(kRedBlock) k_vcycle_tail(TailLevels<T> g, int 
             tail_sweep(d, a.x[l], a.b[l], 0);
             tail_sweep(d, a.x[l], a.b[l], 1);
         }
-        const long long n = d.ncell();
-        for (long long i = threadIdx.x; i < n; i += blockDim.x)
-            residual_cell(d, a.r[l], a.x[l], a.b[l], (int)(i % d.nx), (int)((i / d.nx) % d.ny), (int)(i / d.sxy()));
+        const int n = (int)d.ncell();
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            int xx, yy, zz;
+            tail_xyz(d, i, xx, yy, zz);
+            residual_cell(d, a.r[l], a.x[l], a.b[l], xx, yy, zz);
+        }
         __syncthreads();
         const Dims& c = a.d[l + 1];
-        const long long nc = c.ncell();
-        for (long long i = threadIdx.x; i < nc; i += blockDim.x) {
-            restrict_cell(d, a.b[l + 1], a.r[l], (int)(i % c.nx), (int)((i / c.nx) % c.ny), (int)(i / c.sxy()));
+        const int nc = (int)c.ncell();
+        for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+            int xx, yy, zz;
+            tail_xyz(c, i, xx, yy, zz);
+            restrict_cell(d, a.b[l + 1], a.r[l], xx, yy, zz);
             a.x[l + 1][i] = T(0);
         }
         __syncthreads();
@@ -665,9 +677,12 @@ __global__ void __launch_bounds__(kRedBlock) k_vcycle_tail(TailLevels<T> g, int 
     for (int l = a.nlev - 2; l >= 0; --l) {
         const Dims& d = a.d[l];
         const Dims& c = a.d[l + 1];
-        const long long nc = c.ncell();
-        for (long long i = threadIdx.x; i < nc; i += blockDim.x)
-            prolong_cell<T, true>(d, a.x[l], a.x[l + 1], (int)(i % c.nx), (int)((i / c.nx) % c.ny), (int)(i / c.sxy()));
+        const int nc = (int)c.ncell();
+        for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+            int xx, yy, zz;
+            tail_xyz(c, i, xx, yy, zz);
+            prolong_cell<T, true>(d, a.x[l], a.x[l + 1], xx, yy, zz);
+        }
         __syncthreads();
         for (int j = 0; j < a.nu2; ++j) {
             tail_sweep(d, a.x[l], a.b[l], 0);

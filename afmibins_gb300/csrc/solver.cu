@@ -58,7 +58,9 @@ struct afmib_solver {
     std::vector<MGLevelT<float>> lv32;
     double *cx64 = nullptr, *cb64 = nullptr, *cr64 = nullptr;
     int inner_cycles = 3;
-    bool pipe_smoother = true;  // pipelined red-black sweeps where a level allows (AFMIB_SMOOTHER=percolour: off)
+    // pipelined red-black sweeps (AFMIB_SMOOTHER=pipe); the default is the
+    // batched per-colour launches, measured faster at 256^3
+    bool pipe_smoother = false;
     int pipe_min_nx = 64;       // smaller levels keep the per-colour launches (AFMIB_PIPE_MIN_NX)
     // mixed form: FP64-state defects by int64 block arithmetic instead of the
     // FP64 kernels (opt-in, AFMIB_BFP=1: measured no faster on GB300, the
@@ -623,14 +625,16 @@ int cg_inner32(afmib_solver* s, int comp, double scale, double rel_tol, int* ite
 // max-norm error by rho = k|off| / (1 + k|off|) per sweep (k = 6, 4 in 2D;
 // the channel wall rows contract faster). The outer loop measures the 2-norm
 // of the residual, and the defects concentrate near the membrane (their
-// max/RMS ratio is large), so the sweeps aim at rel_tol / 100 in the max
-// norm: ceil(log(rel_tol / 100) / log(rho)) sweeps from zero.
+// max/RMS ratio is large), so the sweeps aim at rel_tol / 10 in the max
+// norm: ceil(log(rel_tol / 10) / log(rho)) sweeps from zero (measured at
+// 256^3: one sweep fewer costs a third defect-correction step per solve,
+// one more costs a sweep per solve for nothing).
 int jacobi_sweeps(const Dims& d, double scale, double rel_tol) {
     if (!(scale < 0)) return -1;
     const double off = -scale * (double)d.n * (double)d.n, k = d.nz == 1 ? 4.0 : 6.0;
     const double rho = k * off / (1.0 + k * off);
     if (!(rho > 0) || !(rho < 1)) return -1;
-    int sweeps = (int)std::ceil(std::log(rel_tol * 1e-2) / std::log(rho));
+    int sweeps = (int)std::ceil(std::log(rel_tol * 1e-1) / std::log(rho));
     if (const char* e = std::getenv("AFMIB_JACOBI_SWEEPS")) sweeps = std::atoi(e);
     return sweeps >= 1 && sweeps <= 10 ? sweeps : -1;
 }
@@ -1365,7 +1369,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     s->mixed = g.precision == AFMIB_MIXED;
     s->spread64 = s->mixed && !(g.ib_fp32 & 1);
     s->interp64 = s->mixed && !(g.ib_fp32 & 2);
-    if (const char* e = std::getenv("AFMIB_SMOOTHER")) s->pipe_smoother = std::string(e) != "percolour";
+    if (const char* e = std::getenv("AFMIB_SMOOTHER")) s->pipe_smoother = std::string(e) == "pipe";
     if (const char* e = std::getenv("AFMIB_PIPE_MIN_NX")) s->pipe_min_nx = std::atoi(e);
     if (const char* e = std::getenv("AFMIB_BFP")) s->bfp_defects = std::string(e) == "1";
     if (const char* e = std::getenv("AFMIB_INNER_CYCLES")) s->inner_cycles = std::max(1, std::atoi(e));
