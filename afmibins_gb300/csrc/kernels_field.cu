@@ -400,6 +400,37 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_defect_bfp(Dims d, int comp,
 // diagonal (1 - 6 off in the interior, 1 - 4 off in 2D, 1 - 8 off on the
 // channel u/w wall rows, 1 on the channel v wall plane). x == nullptr starts
 // from zero: x' = b / diag.
+// helm_point_at with Ix2 indexing (power-of-two extents): same terms, same order
+template <typename T>
+__device__ __forceinline__ T helm_point2(const Dims& d, const Ix2& I, int comp, T s, const T* __restrict__ x, int xi,
+                                         int yi, int zi) {
+    const T off = s * T(d.n) * T(d.n);
+    const T x0 = x[I.at(xi, yi, zi)];
+    const T sx = x[I.at(I.xm(xi), yi, zi)] + x[I.at(I.xp(xi), yi, zi)];
+    if (d.nz == 1) {
+        const T sy = x[I.at(xi, I.ym(yi), zi)] + x[I.at(xi, I.yp(yi), zi)];
+        return (T(1) - T(4) * off) * x0 + off * (sx + sy);
+    }
+    const T sz = x[I.at(xi, yi, I.zm(zi))] + x[I.at(xi, yi, I.zp(zi))];
+    if (d.channel && comp != 1) {
+        T diag = T(1) - T(6) * off;
+        T sy;
+        if (yi == 0) {
+            diag -= T(2) * off;
+            sy = (off + off / T(3)) * x[I.at(xi, 1, zi)];
+        } else if (yi == d.ny - 1) {
+            diag -= T(2) * off;
+            sy = (off + off / T(3)) * x[I.at(xi, yi - 1, zi)];
+        } else {
+            sy = off * (x[I.at(xi, yi - 1, zi)] + x[I.at(xi, yi + 1, zi)]);
+        }
+        return diag * x0 + (off * (sx + sz) + sy);
+    }
+    if (d.channel && comp == 1 && yi == 0) return x0;
+    const T sy = x[I.at(xi, I.ym(yi), zi)] + x[I.at(xi, I.yp(yi), zi)];
+    return (T(1) - T(6) * off) * x0 + off * (sx + sy + sz);
+}
+
 template <typename T>
 __device__ __forceinline__ T helm_diag(const Dims& d, int comp, T off, int y) {
     if (d.nz == 1) return T(1) - T(4) * off;
@@ -554,10 +585,31 @@ template <typename T>
 void launch_cg_apply(const Dims& d, int comp, double scale, const T* p, T* q, RedScratch sc, double* cgs, cudaStream_t s) {
     k_cg_apply<T><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, T(scale), p, q, sc, cgs);
 }
+template <typename T, int ZU>
+__global__ void k_helm_jacobi2(Dims d, int comp, T s, const T* __restrict__ xv, T* __restrict__ xo,
+                               const T* __restrict__ b) {
+    const Ix2 I(d);
+    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z0 = blockIdx.z * ZU;
+    if (x >= d.nx || y >= d.ny) return;
+    const T off = s * T(d.n) * T(d.n);
+    const T rdiag = T(1) / helm_diag(d, comp, off, y);
+    T val[ZU];
+#pragma unroll
+    for (int u = 0; u < ZU; ++u) {
+        const int i = I.at(x, y, z0 + u);
+        val[u] = xv ? xv[i] + (b[i] - helm_point2(d, I, comp, s, xv, x, y, z0 + u)) * rdiag : b[i] * rdiag;
+    }
+#pragma unroll
+    for (int u = 0; u < ZU; ++u) xo[I.at(x, y, z0 + u)] = val[u];
+}
+
 template <typename T>
 void launch_helm_jacobi(const Dims& d, int comp, double scale, const T* x, T* xo, const T* b, cudaStream_t s) {
     const dim3 blk(BX, BY);
-    if (d.nz % 8 == 0)
+    if (d.nz % 8 == 0 && ix2_ok(d))
+        k_helm_jacobi2<T, 8><<<dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / 8), blk, 0, s>>>(d, comp, T(scale),
+                                                                                                   x, xo, b);
+    else if (d.nz % 8 == 0)
         k_helm_jacobi<T, 8><<<dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / 8), blk, 0, s>>>(d, comp, T(scale), x,
                                                                                                   xo, b);
     else

@@ -192,6 +192,66 @@ __global__ void k_rbgs_z(Dims d, int color, T* __restrict__ xv, const T* __restr
         if (at[u] >= 0) xv[at[u]] = val[u];
 }
 
+// Neighbour sum and diagonal factor of lap_row with Ix2 indexing (same terms,
+// same order).
+template <typename T>
+__device__ __forceinline__ void lap_row2(const Dims& d, const Ix2& I, const T* __restrict__ x, int xi, int yi, int zi,
+                                         T& S, T& c) {
+    if (d.nz == 1) {
+        S = x[I.at(I.xm(xi), yi, zi)] + x[I.at(I.xp(xi), yi, zi)];
+        c = T(4);
+    } else {
+        S = (x[I.at(I.xm(xi), yi, zi)] + x[I.at(I.xp(xi), yi, zi)]) + (x[I.at(xi, yi, I.zm(zi))] + x[I.at(xi, yi, I.zp(zi))]);
+        c = T(6);
+    }
+    if (d.channel) {
+        if (yi > 0) S += x[I.at(xi, yi - 1, zi)]; else c -= T(1);
+        if (yi < d.ny - 1) S += x[I.at(xi, yi + 1, zi)]; else c -= T(1);
+    } else {
+        S += x[I.at(xi, I.ym(yi), zi)] + x[I.at(xi, I.yp(yi), zi)];
+    }
+}
+
+template <typename T, int ZU>
+__global__ void k_rbgs_z2(Dims d, int color, T* __restrict__ xv, const T* __restrict__ b) {
+    const Ix2 I(d);
+    const int y = blockIdx.y * BY + threadIdx.y, t = blockIdx.x * BX + threadIdx.x, z0 = blockIdx.z * ZU;
+    if (y >= d.ny || 2 * t >= d.nx) return;
+    T val[ZU];
+    int at[ZU];
+    const T inv = T(1) / (T(d.n) * T(d.n));
+#pragma unroll
+    for (int u = 0; u < ZU; ++u) {
+        const int z = z0 + u, x = 2 * t + ((y + z + color) & 1);
+        T S, c;
+        lap_row2(d, I, xv, x, y, z, S, c);
+        const int i = I.at(x, y, z);
+        const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
+        val[u] = (S - b[i] * inv) * rc;
+        at[u] = i;
+    }
+#pragma unroll
+    for (int u = 0; u < ZU; ++u) xv[at[u]] = val[u];
+}
+
+template <typename T, int ZU>
+__global__ void k_residual_z2(Dims d, T* __restrict__ r, const T* __restrict__ xv, const T* __restrict__ b) {
+    const Ix2 I(d);
+    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z0 = blockIdx.z * ZU;
+    if (x >= d.nx || y >= d.ny) return;
+    const T off = T(d.n) * T(d.n);
+    T val[ZU];
+#pragma unroll
+    for (int u = 0; u < ZU; ++u) {
+        T S, c;
+        lap_row2(d, I, xv, x, y, z0 + u, S, c);
+        const int i = I.at(x, y, z0 + u);
+        val[u] = b[i] - off * (S - c * xv[i]);
+    }
+#pragma unroll
+    for (int u = 0; u < ZU; ++u) r[I.at(x, y, z0 + u)] = val[u];
+}
+
 template <typename T, int ZU>
 __global__ void k_residual_z(Dims d, T* __restrict__ r, const T* __restrict__ xv, const T* __restrict__ b) {
     const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z0 = blockIdx.z * ZU;
@@ -705,6 +765,8 @@ template <typename T>
 void launch_residual(const Dims& d, T* r, const T* x, const T* b, RedScratch* sc, double* out, cudaStream_t s) {
     if (sc && out)
         k_residual_norm<T><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, r, x, b, *sc, out);
+    else if (d.nz % kZU == 0 && d.nx >= 64 && ix2_ok(d))
+        k_residual_z2<T, kZU><<<dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / kZU), dim3(BX, BY), 0, s>>>(d, r, x, b);
     else if (d.nz % kZU == 0 && d.nx >= 64)
         k_residual_z<T, kZU><<<dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / kZU), dim3(BX, BY), 0, s>>>(d, r, x, b);
     else
@@ -714,7 +776,8 @@ template <typename T>
 void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s) {
     if (d.nz % kZU == 0 && d.nx >= 64) {
         dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / kZU);
-        k_rbgs_z<T, kZU><<<g, dim3(BX, BY), 0, s>>>(d, color, x, b);
+        if (ix2_ok(d)) k_rbgs_z2<T, kZU><<<g, dim3(BX, BY), 0, s>>>(d, color, x, b);
+        else k_rbgs_z<T, kZU><<<g, dim3(BX, BY), 0, s>>>(d, color, x, b);
         return;
     }
     dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz);
