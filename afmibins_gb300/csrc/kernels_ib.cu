@@ -282,96 +282,87 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
     // axis. 2D (TZ == 1, nz == 1): one plane, no z halo.
     constexpr int NT = TS * TS * TZ, E = TS + 4, EZ = TZ == 1 ? 1 : TS + 4, HZ = TZ == 1 ? 0 : 2;
     constexpr int E2 = E * E, E3 = E2 * EZ, C = TS * TS * TZ;
-    constexpr int NSEG = E * EZ * 3;  // (row, tile segment) pairs
+    constexpr int CPT = (E3 + NT - 1) / NT;  // consecutive E cells per thread
     extern __shared__ __align__(16) unsigned char smem[];
     int* s_estart = (int*)smem;          // E3 + 1: first staged slot of each E cell
-    int* s_seg = s_estart + (E3 + 1);    // NSEG: staged offset of each segment
-    int* s_scan = s_seg + NSEG;          // NT
+    int* s_scan = s_estart + (E3 + 1);   // NT / 32: warp totals of the block scan
     int* s_k = s_scan + NT;              // cap: marker index of each staged slot
     int* s_base = s_k + cap;             // cap: packed E-local first faces
     // cap * 12: x weights, y weights, z weights times the marker's force
     T* s_w = (T*)(((uintptr_t)(s_base + cap) + 15) & ~(uintptr_t)15);
 
-    const int ntx = d.nx / TS, nty = d.ny / TS, ntz = d.nz / TZ;
+    const int ntx = d.nx / TS, nty = d.ny / TS;
     const int ncount = *count;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int lx = tid % TS, ly = (tid / TS) % TS, lz = tid / (TS * TS);
+    auto wrap1 = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };
     for (int li = blockIdx.x; li < ncount; li += gridDim.x) {
         const int t = list[li];
         const int tx = t % ntx, ty = (t / ntx) % nty, tz = t / (ntx * nty);
         const int ox = tx * TS - 2, oy = ty * TS - 2, oz = tz * TZ - HZ;  // E origin (unwrapped cells)
-        // ---- segment ranges: segment q = (row r, part j): cells ex in
-        //      [0, 2), [2, TS+2), [TS+2, E) of row r, i.e. tiles tx-1, tx, tx+1
-        int my_len[(NSEG + NT - 1) / NT], my_p0[(NSEG + NT - 1) / NT];
+        // ---- markers of each E cell (E-linear order e = ex + E (ey + E ez)):
+        //      thread tid takes cells [tid * CPT, tid * CPT + CPT), whose
+        //      cell-table loads are independent of one another
+        int cnt[CPT], p0[CPT];
         int tot = 0;
 #pragma unroll
-        for (int k = 0; k < (NSEG + NT - 1) / NT; ++k) {
-            const int q = tid * ((NSEG + NT - 1) / NT) + k;
-            my_len[k] = 0;
-            my_p0[k] = 0;
-            if (q < NSEG) {
-                const int r = q / 3, j = q % 3;
-                const int ey = r % E, ez = r / E;
-                int gy = oy + ey;
-                const bool ok = !(d.channel && (gy < 0 || gy >= d.ny));
-                if (ok) {
-                    gy = wrapi(gy, d.ny);
-                    const int gz = wrapi(oz + ez, d.nz);
-                    const int ex0 = j == 0 ? 0 : (j == 1 ? 2 : TS + 2);
-                    const int ex1 = j == 0 ? 2 : (j == 1 ? TS + 2 : E);  // exclusive
-                    const int gx0 = wrapi(ox + ex0, d.nx);
-                    const int tt = gx0 / TS + ntx * (gy / TS + nty * (gz / TZ));
-                    const int sl = slot[tt];
+        for (int k = 0; k < CPT; ++k) {
+            const int e = tid * CPT + k;
+            cnt[k] = 0;
+            p0[k] = 0;
+            if (e < E3) {
+                const int ex = e % E, ey = (e / E) % E, ez = e / E2;
+                const int gy = oy + ey;
+                if (!(d.channel && (gy < 0 || gy >= d.ny))) {
+                    const int gx = wrap1(ox + ex, d.nx), gyw = wrap1(gy, d.ny), gz = wrap1(oz + ez, d.nz);
+                    const int sl = slot[gx / TS + ntx * (gyw / TS + nty * (gz / TZ))];
                     if (sl >= 0) {
-                        const int lc0 = (gx0 % TS) + TS * ((gy % TS) + TS * (gz % TZ));
-                        const int* row = ctab + (size_t)sl * (C + 1);
-                        my_p0[k] = row[lc0];
-                        my_len[k] = row[lc0 + (ex1 - ex0)] - my_p0[k];
+                        const int lc = (gx % TS) + TS * ((gyw % TS) + TS * (gz % TZ));
+                        const int* row = ctab + (size_t)sl * (C + 1) + lc;
+                        p0[k] = row[0];
+                        cnt[k] = row[1] - p0[k];
                     }
                 }
             }
-            tot += my_len[k];
+            tot += cnt[k];
         }
-        // block exclusive scan of the per-thread totals (fixed order)
-        s_scan[tid] = tot;
-        __syncthreads();
-        for (int o = 1; o < NT; o <<= 1) {
-            const int v = tid >= o ? s_scan[tid - o] : 0;
-            __syncthreads();
-            s_scan[tid] += v;
-            __syncthreads();
-        }
-        const int nc_all = s_scan[NT - 1];
-        int off = s_scan[tid] - tot;
+        // ---- block exclusive scan of the per-thread totals (thread order = E order);
+        //      NT < 32 (4 x 4 x 1 tiles) is one partial warp
+        constexpr int NW = (NT + 31) / 32;
+        constexpr unsigned WMASK = NT >= 32 ? 0xffffffffu : ((1u << NT) - 1u);
+        constexpr int WLAST = NT >= 32 ? 31 : NT - 1;
+        int inc = tot;
 #pragma unroll
-        for (int k = 0; k < (NSEG + NT - 1) / NT; ++k) {
-            const int q = tid * ((NSEG + NT - 1) / NT) + k;
-            if (q < NSEG) {
-                s_seg[q] = off;
-                for (int m = 0; m < my_len[k]; ++m)
-                    if (off + m < cap) s_k[off + m] = perm[my_p0[k] + m];
-                // E-cell starts of this segment's cells
-                const int r = q / 3, j = q % 3;
-                const int ex0 = j == 0 ? 0 : (j == 1 ? 2 : TS + 2);
-                const int ex1 = j == 0 ? 2 : (j == 1 ? TS + 2 : E);
-                int gy = oy + r % E;
-                const bool ok = !(d.channel && (gy < 0 || gy >= d.ny));
-                for (int ex = ex0; ex < ex1; ++ex) {
-                    int st = off;
-                    if (ok && my_len[k] > 0) {
-                        gy = wrapi(gy, d.ny);
-                        const int gz = wrapi(oz + r / E, d.nz);
-                        const int gx = wrapi(ox + ex, d.nx);
-                        const int tt = gx / TS + ntx * (gy / TS + nty * (gz / TZ));
-                        const int lc = (gx % TS) + TS * ((gy % TS) + TS * (gz % TZ));
-                        st = off + (ctab[(size_t)slot[tt] * (C + 1) + lc] - my_p0[k]);
-                    }
-                    s_estart[ex + E * r] = st;
-                }
-                off += my_len[k];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(WMASK, inc, o);
+            if (lane >= o) inc += v;
+        }
+        if (lane == WLAST) s_scan[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+            int w = lane < NW ? s_scan[lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(WMASK, w, o);
+                if (lane >= o) w += v;
+            }
+            if (lane < NW) s_scan[lane] = w;  // inclusive warp prefix
+        }
+        __syncthreads();
+        const int nc_all = s_scan[NW - 1];
+        int off = inc - tot + (warp > 0 ? s_scan[warp - 1] : 0);
+        // ---- E-cell starts and the staged marker indices
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) {
+            const int e = tid * CPT + k;
+            if (e < E3) {
+                s_estart[e] = off;
+                for (int m = 0; m < cnt[k]; ++m)
+                    if (off + m < cap) s_k[off + m] = perm[p0[k] + m];
+                off += cnt[k];
             }
         }
-        if (tid == NT - 1) s_estart[E3] = nc_all;
+        if (tid == 0) s_estart[E3] = nc_all;
         if (nc_all > cap && tid == 0) {
             if (ovf_list) ovf_list[atomicAdd(ovf_count, 1)] = t;  // left to the large-capacity pass
             else atomicExch(flag, 3);
@@ -537,7 +528,7 @@ void launch_cell_table(int TS, int TZ, const unsigned* keys, const int* tstart, 
 template <typename T>
 size_t spread_smem_bytes(int TS, int TZ, int cap) {
     const int E = TS + 4, EZ = TZ == 1 ? 1 : TS + 4, E3 = E * E * EZ, NT = TS * TS * TZ;
-    size_t ints = (size_t)(E3 + 1) + 3 * E * EZ + NT + 2 * (size_t)cap;
+    size_t ints = (size_t)(E3 + 1) + NT + 2 * (size_t)cap;
     size_t bytes = ints * sizeof(int);
     bytes = (bytes + 15) & ~(size_t)15;
     bytes += (size_t)cap * 12 * sizeof(T);

@@ -553,6 +553,85 @@ __device__ __forceinline__ void prolong_cell(const Dims& d, T* fine, const T* co
     }
 }
 
+// restrict_cell / prolong_cell for 3D power-of-two levels with Ix2 indexing
+// (same taps, same weights, same summation order)
+template <typename T>
+__global__ void k_restrict2(Dims d, T* __restrict__ coarse, const T* __restrict__ fine) {
+    const Ix2 I(d);
+    const int cx = d.nx / 2, cy = d.ny / 2;
+    const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
+    if (xc >= cx || yc >= cy) return;
+    const int xcf = 2 * xc + 1, ycf = 2 * yc + 1, zcf = 2 * zc + 1;
+    int xs[4], yo[4], zo[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int dd = k - 2;
+        xs[k] = (xcf + dd) & I.mx;
+        zo[k] = ((zcf + dd) & I.mz) << I.lxy;
+        if (d.channel) {
+            int yy = ycf + (dd > -ycf ? dd : -ycf);
+            yo[k] = (yy < d.ny - 1 ? yy : d.ny - 1) << I.lx;
+        } else {
+            yo[k] = ((ycf + dd) & I.my) << I.lx;
+        }
+    }
+    const T wgt[4] = {T(1), T(3), T(3), T(1)};
+    T acc = T(0);
+#pragma unroll
+    for (int kz = 0; kz < 4; ++kz)
+#pragma unroll
+        for (int ky = 0; ky < 4; ++ky)
+#pragma unroll
+            for (int kx = 0; kx < 4; ++kx)
+                acc += (wgt[kx] * wgt[ky] * wgt[kz] / T(512)) * fine[xs[kx] | yo[ky] | zo[kz]];
+    coarse[xc | (yc << (I.lx - 1)) | (zc << (I.lxy - 2))] = acc;
+}
+
+template <typename T, bool ADD>
+__global__ void k_prolong2(Dims d, T* __restrict__ fine, const T* __restrict__ coarse) {
+    const Ix2 I(d);
+    const int cx = d.nx / 2, cy = d.ny / 2, cz = d.nz / 2, lcx = I.lx - 1, lcxy = I.lxy - 2;
+    const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
+    if (xc >= cx || yc >= cy) return;
+    auto C = [&](int a, int b, int c) { return coarse[a | (b << lcx) | (c << lcxy)]; };
+    auto put = [&](int a, int b, int c, T val) {
+        const int i = I.at(a, b, c);
+        if (ADD) fine[i] = fine[i] + val; else fine[i] = val;
+    };
+    const int xn = (xc + 1) & (cx - 1), zn = (zc + 1) & (cz - 1);
+    const int xcf = 2 * xc + 1, zcf = 2 * zc + 1;
+    const int xnf = (xcf + 1) & I.mx, znf = (zcf + 1) & I.mz;
+    const bool interior = d.channel ? (yc < cy - 1) : true;
+    if (interior) {
+        const int yn = d.channel ? yc + 1 : (yc + 1) & (cy - 1);
+        const int ycf = 2 * yc + 1, ynf = d.channel ? ycf + 1 : (ycf + 1) & I.my;
+        const T blb = C(xc, yc, zc), brb = C(xn, yc, zc), ulb = C(xc, yn, zc), urb = C(xn, yn, zc);
+        const T blf = C(xc, yc, zn), brf = C(xn, yc, zn), ulf = C(xc, yn, zn), urf = C(xn, yn, zn);
+        const T a = T(27) / T(64), b = T(9) / T(64), c = T(3) / T(64), e = T(1) / T(64);
+        put(xcf, ycf, zcf, a * blb + b * (brb + ulb + blf) + c * (urb + ulf + brf) + e * urf);
+        put(xnf, ycf, zcf, a * brb + b * (urb + blb + brf) + c * (ulb + blf + urf) + e * ulf);
+        put(xcf, ynf, zcf, a * ulb + b * (urb + blb + ulf) + c * (brb + blf + urf) + e * brf);
+        put(xnf, ynf, zcf, a * urb + b * (brb + ulb + urf) + c * (blb + ulf + brf) + e * blf);
+        put(xcf, ycf, znf, a * blf + b * (brf + ulf + blb) + c * (urf + ulb + brb) + e * urb);
+        put(xnf, ycf, znf, a * brf + b * (urf + blf + brb) + c * (ulf + blb + urb) + e * ulb);
+        put(xcf, ynf, znf, a * ulf + b * (urf + blf + ulb) + c * (brf + blb + urb) + e * brb);
+        put(xnf, ynf, znf, a * urf + b * (brf + ulf + urb) + c * (blf + ulb + brb) + e * blb);
+    }
+    if (d.channel && (yc == 0 || yc == cy - 1)) {
+        const T a = T(9) / T(16), b = T(3) / T(16), e = T(1) / T(16);
+        for (int side = 0; side < 2; ++side) {
+            if (side == 0 && yc != 0) continue;
+            if (side == 1 && yc != cy - 1) continue;
+            const int ycs = side == 0 ? 0 : cy - 1, yf = side == 0 ? 0 : d.ny - 1;
+            const T bl = C(xc, ycs, zc), br = C(xn, ycs, zc), fl = C(xc, ycs, zn), fr = C(xn, ycs, zn);
+            put(xcf, yf, zcf, a * bl + b * (br + fl) + e * fr);
+            put(xnf, yf, zcf, a * br + b * (bl + fr) + e * fl);
+            put(xcf, yf, znf, a * fl + b * (fr + bl) + e * br);
+            put(xnf, yf, znf, a * fr + b * (fl + br) + e * bl);
+        }
+    }
+}
+
 template <typename T, bool ADD>
 __global__ void k_prolong(Dims d, T* __restrict__ fine, const T* __restrict__ coarse) {
     const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
@@ -866,12 +945,14 @@ void launch_rbgs_pipe(const Dims& d, const PipeCfg& c, const T* xin, T* xout, co
 template <typename T>
 void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s) {
     dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz == 1 ? 1 : d.nz / 2);
-    k_restrict<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine);
+    if (d.nz > 1 && d.nx >= 2 && d.ny >= 2 && ix2_ok(d)) k_restrict2<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine);
+    else k_restrict<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine);
 }
 template <typename T>
 void launch_prolong_add(const Dims& d, T* fine, const T* coarse, cudaStream_t s) {
     dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz == 1 ? 1 : d.nz / 2);
-    k_prolong<T, true><<<g, dim3(BX, BY), 0, s>>>(d, fine, coarse);
+    if (d.nz > 1 && d.nx >= 2 && d.ny >= 2 && ix2_ok(d)) k_prolong2<T, true><<<g, dim3(BX, BY), 0, s>>>(d, fine, coarse);
+    else k_prolong<T, true><<<g, dim3(BX, BY), 0, s>>>(d, fine, coarse);
 }
 template <typename T>
 void launch_prolong_assign(const Dims& d, T* fine, const T* coarse, cudaStream_t s) {
