@@ -277,7 +277,8 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
                                                                 const int* __restrict__ list, const int* __restrict__ count,
                                                                 int cap, T* __restrict__ fu, T* __restrict__ fv,
                                                                 T* __restrict__ fw, int* __restrict__ flag,
-                                                                int* __restrict__ ovf_list, int* __restrict__ ovf_count) {
+                                                                int* __restrict__ ovf_list, int* __restrict__ ovf_count,
+                                                                int* __restrict__ next_tile) {
     // 3D: TZ == TS, the neighbourhood grows by 2 cells per side along every
     // axis. 2D (TZ == 1, nz == 1): one plane, no z halo.
     constexpr int NT = TS * TS * TZ, E = TS + 4, EZ = TZ == 1 ? 1 : TS + 4, HZ = TZ == 1 ? 0 : 2;
@@ -296,7 +297,15 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int lx = tid % TS, ly = (tid / TS) % TS, lz = tid / (TS * TS);
     auto wrap1 = [](int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); };
-    for (int li = blockIdx.x; li < ncount; li += gridDim.x) {
+    // tiles are taken from a shared counter (their costs differ widely near a
+    // membrane); each tile is still computed by one block, in a fixed order
+    __shared__ int s_li;
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_li = atomicAdd(next_tile, 1);
+        __syncthreads();
+        const int li = s_li;
+        if (li >= ncount) break;
         const int t = list[li];
         const int tx = t % ntx, ty = (t / ntx) % nty, tz = t / (ntx * nty);
         const int ox = tx * TS - 2, oy = ty * TS - 2, oz = tz * TZ - HZ;  // E origin (unwrapped cells)
@@ -539,7 +548,7 @@ template <typename T, int TS, int TZ>
 static void spread_launch(const Dims& d, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
                           double scale, const int* slot, const int* ctab, const int* list, const int* count,
                           int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, int* ovf_list, int* ovf_count,
-                          cudaStream_t s) {
+                          int* next_tile, cudaStream_t s) {
     const size_t smem = spread_smem_bytes<T>(TS, TZ, cap);
     // opt in to exactly the dynamic shared memory this launch uses (the
     // kernel's static shared memory counts against the same 227 KB)
@@ -553,18 +562,19 @@ static void spread_launch(const Dims& d, int M, const int* perm, MarkerW<T> mw, 
     int blocks = max_tiles < 152 * 4 ? max_tiles : 152 * 4;
     if (blocks < 1) blocks = 1;
     k_spread_gather<T, TS, TZ><<<blocks, TS * TS * TZ, smem, s>>>(d, M, perm, mw, G, vol, scale, slot, ctab, list,
-                                                                  count, cap, fu, fv, fw, flag, ovf_list, ovf_count);
+                                                                  count, cap, fu, fv, fw, flag, ovf_list, ovf_count,
+                                                                  next_tile);
 }
 
 template <typename T>
 void launch_spread_gather(const Dims& d, int TS, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
                           double scale, const int* slot, const int* ctab, const int* list, const int* count,
                           int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, int* ovf_list, int* ovf_count,
-                          cudaStream_t s) {
+                          int* next_tile, cudaStream_t s) {
     const bool flat = d.nz == 1;
 #define AFMIB_SPREAD(TSV, TZV)                                                                                    \
     spread_launch<T, TSV, TZV>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, \
-                               flag, ovf_list, ovf_count, s)
+                               flag, ovf_list, ovf_count, next_tile, s)
     if (TS == 8 && !flat) AFMIB_SPREAD(8, 8);
     else if (TS == 4 && !flat) AFMIB_SPREAD(4, 4);
     else if (TS == 8) AFMIB_SPREAD(8, 1);
@@ -589,7 +599,7 @@ void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, do
     template size_t spread_smem_bytes<T>(int, int, int);                                                             \
     template void launch_spread_gather<T>(const Dims&, int, int, const int*, MarkerW<T>, const T*, const double*, \
                                           double, const int*, const int*, const int*, const int*, int, int, T*,  \
-                                          T*, T*, int*, int*, int*, cudaStream_t);                              \
+                                          T*, T*, int*, int*, int*, int*, cudaStream_t);                        \
     template void launch_interp<T, double>(const Dims&, int, const int*, MarkerW<T>, const double*, const double*, \
                                            const double*, double*, cudaStream_t);                               \
     template void launch_interp<T, float>(const Dims&, int, const int*, MarkerW<T>, const float*, const float*,  \

@@ -100,7 +100,8 @@ struct afmib_solver {
     int *vals = nullptr, *vals2 = nullptr, *perm = nullptr;
     int TS = 0, TZ = 0, ntx = 0, nty = 0, ntz = 0, ntiles = 0;  // TZ: tile depth (TS; 1 on a 2D grid)
     int tile_cells() const { return TS * TS * TZ; }
-    // tcount: [0] active output tiles, [1] occupied tiles, [2] tiles left to the large-capacity spreading pass
+    // tcount: [0] active output tiles, [1] occupied tiles, [2] tiles left to the large-capacity spreading pass,
+    // [3], [4] the two passes' tile counters
     int *tstart = nullptr, *tend = nullptr, *tlist = nullptr, *tcount = nullptr, *tovf = nullptr;
     int *tslot = nullptr, *tocc = nullptr, *ctab = nullptr;
     int ctab_cap = 0;  // occupied tiles the cell table can hold
@@ -920,11 +921,11 @@ int bin_markers(afmib_solver* s, const double* P, bool fp32 = false) {
 template <typename T>
 int spread_two_pass(afmib_solver* s, MarkerW<T> mw, const T* G, const double* vol, double scale, T* fu, T* fv, T* fw,
                     int cap_small, int cap_large) {
-    CK(cudaMemsetAsync(s->tcount + 2, 0, sizeof(int), s->st));
+    CK(cudaMemsetAsync(s->tcount + 2, 0, 3 * sizeof(int), s->st));  // overflow count and the two tile counters
     launch_spread_gather<T>(s->d, s->TS, s->M, s->perm, mw, G, vol, scale, s->tslot, s->ctab, s->tlist, s->tcount,
-                            s->ntiles, cap_small, fu, fv, fw, s->dflag, s->tovf, s->tcount + 2, s->st);
+                            s->ntiles, cap_small, fu, fv, fw, s->dflag, s->tovf, s->tcount + 2, s->tcount + 3, s->st);
     launch_spread_gather<T>(s->d, s->TS, s->M, s->perm, mw, G, vol, scale, s->tslot, s->ctab, s->tovf, s->tcount + 2,
-                            s->ntiles, cap_large, fu, fv, fw, s->dflag, nullptr, nullptr, s->st);
+                            s->ntiles, cap_large, fu, fv, fw, s->dflag, nullptr, nullptr, s->tcount + 4, s->st);
     return AFMIB_OK;
 }
 
@@ -1346,7 +1347,7 @@ int setup_tiles(afmib_solver* s) {
     TRY(dalloc(s, &s->tstart, s->ntiles));
     TRY(dalloc(s, &s->tend, s->ntiles));
     TRY(dalloc(s, &s->tlist, s->ntiles));
-    TRY(dalloc(s, &s->tcount, 3));
+    TRY(dalloc(s, &s->tcount, 5));
     TRY(dalloc(s, &s->tovf, s->ntiles));
     TRY(dalloc(s, &s->tslot, s->ntiles));
     TRY(dalloc(s, &s->tocc, s->ntiles));
