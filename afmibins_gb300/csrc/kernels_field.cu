@@ -519,6 +519,12 @@ __global__ void k_axpy(long long N, T* __restrict__ y, const T* __restrict__ x, 
         y[i] = y[i] + a * x[i];
 }
 
+template <typename T>
+__global__ void k_lincomb(long long N, T* __restrict__ y, T a, const T* __restrict__ x, T b, const T* __restrict__ z) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
+        y[i] = a * x[i] + b * z[i];
+}
+
 template <typename TO, typename TI>
 __global__ void k_convert(long long N, TO* __restrict__ o, const TI* __restrict__ in) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
@@ -650,6 +656,10 @@ template <typename T>
 void launch_axpy(long long n, T* y, const T* x, T a, cudaStream_t s) {
     k_axpy<T><<<ew_blocks(n), 256, 0, s>>>(n, y, x, a);
 }
+template <typename T>
+void launch_lincomb(long long n, T* y, T a, const T* x, T b, const T* z, cudaStream_t s) {
+    k_lincomb<T><<<ew_blocks(n), 256, 0, s>>>(n, y, a, x, b, z);
+}
 template <typename TO, typename TI>
 void launch_convert(long long n, TO* out, const TI* in, cudaStream_t s) {
     k_convert<TO, TI><<<ew_blocks(n), 256, 0, s>>>(n, out, in);
@@ -669,7 +679,8 @@ void launch_convert(long long n, TO* out, const TI* in, cudaStream_t s) {
     template void launch_sumsq<T>(long long, const T*, RedScratch, double*, cudaStream_t);                     \
     template void launch_sub_scalar_scaled<T>(long long, T*, const double*, double, cudaStream_t);             \
     template void launch_fill<T>(long long, T*, T, cudaStream_t);                                              \
-    template void launch_axpy<T>(long long, T*, const T*, T, cudaStream_t);
+    template void launch_axpy<T>(long long, T*, const T*, T, cudaStream_t);                                    \
+    template void launch_lincomb<T>(long long, T*, T, const T*, T, const T*, cudaStream_t);
 
 AFMIB_INST(double)
 AFMIB_INST(float)

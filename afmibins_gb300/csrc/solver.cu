@@ -30,6 +30,8 @@ struct MGLevelT {
 };
 typedef MGLevelT<double> MGLevel;
 
+constexpr int kMaxInnerCycles = 8;  // longest FP32 inner V-cycle block of the mixed form
+
 struct afmib_solver {
     afmib_config cfg{};
     Dims d{};
@@ -57,7 +59,16 @@ struct afmib_solver {
     float *cg32_r = nullptr, *cg32_p = nullptr, *cg32_q = nullptr, *cg32_p2 = nullptr;
     std::vector<MGLevelT<float>> lv32;
     double *cx64 = nullptr, *cb64 = nullptr, *cr64 = nullptr;
-    int inner_cycles = 3;
+    // cap of V-cycles per FP32 inner solve, at most kMaxInnerCycles
+    // (AFMIB_INNER_CYCLES); with the adaptive sizing below a long cap costs
+    // nothing on the last correction (256^3 IB step: 3 -> 6 saved 2 FP64
+    // defects per step)
+    int inner_cycles = 6;
+    // size each correction's inner solve from the per-cycle contraction seen
+    // in the previous one: only the cycles that bring the defect below
+    // tol / 2 (AFMIB_INNER_ADAPT=0: always inner_cycles)
+    bool adapt_cycles = true;
+    double mg_rho = 0.0;        // measured per-cycle contraction (0: none yet)
     // pipelined red-black sweeps (AFMIB_SMOOTHER=pipe); the default is the
     // batched per-colour launches, measured faster at 256^3
     bool pipe_smoother = false;
@@ -74,8 +85,8 @@ struct afmib_solver {
     // V-cycle blocks captured once into CUDA graphs and replayed (no host
     // interaction inside a V-cycle); not used while per-kernel profiling is on
     bool use_graphs = true;
-    cudaGraphExec_t vg64 = nullptr, vg32 = nullptr;
-    long long vg64_launches = 0, vg32_launches = 0;
+    cudaGraphExec_t vg64 = nullptr, vg32[kMaxInnerCycles + 1] = {};
+    long long vg64_launches = 0, vg32_launches[kMaxInnerCycles + 1] = {};
     bool spread64 = false, interp64 = false;  // mixed form: IB transfers in FP64
     // warm start of each projection from the potential of the previous
     // projection of the same sub-step type (0: BE, 1: CN); off in the FP64
@@ -83,6 +94,10 @@ struct afmib_solver {
     bool warm_start = false;
     double* phi_prev[2] = {nullptr, nullptr};
     bool phi_valid[2] = {false, false};
+    // second-order start (AFMIB_WARM_EXTRAP=1): 2 phi_prev - phi_prev2
+    bool warm_extrap = false;
+    double* phi_prev2[2] = {nullptr, nullptr};
+    bool phi_valid2[2] = {false, false};
     int proj_phase = -1;  // phase of the projection in progress (-1: none)
     RedScratch red{};
     double* scal = nullptr;   // device scalars: [0..4] CG, [8] sum, [9] sumsq
@@ -462,7 +477,9 @@ int initial_potential(afmib_solver* s) {
     MGLevel& L = s->lv[0];
     const long long N = L.d.ncell();
     const int ph = s->proj_phase;
-    if (s->warm_start && ph >= 0 && s->phi_valid[ph])
+    if (s->warm_start && ph >= 0 && s->phi_valid[ph] && s->warm_extrap && s->phi_valid2[ph])
+        launch_lincomb<double>(N, L.x, 2.0, s->phi_prev[ph], -1.0, s->phi_prev2[ph], s->st);
+    else if (s->warm_start && ph >= 0 && s->phi_valid[ph])
         CK(cudaMemcpyAsync(L.x, s->phi_prev[ph], N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
     else
         CK(cudaMemsetAsync(L.x, 0, N * sizeof(double), s->st));
@@ -492,8 +509,11 @@ int capture_graph(afmib_solver* s, cudaGraphExec_t* exec, long long* launches, F
 
 void drop_graphs(afmib_solver* s) {
     if (s->vg64) cudaGraphExecDestroy(s->vg64);
-    if (s->vg32) cudaGraphExecDestroy(s->vg32);
-    s->vg64 = s->vg32 = nullptr;
+    s->vg64 = nullptr;
+    for (auto& g : s->vg32) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
 }
 
 // one FP64 V-cycle on level 0 (graph replay when possible)
@@ -505,15 +525,16 @@ int vcycle64_top(afmib_solver* s) {
     return AFMIB_OK;
 }
 
-// the FP32 inner solve of one defect-correction step: x32 = 0, inner_cycles
-// V-cycles on L e = r, phi += e (graph replay when possible)
-int inner_vcycles32(afmib_solver* s) {
+// the FP32 inner solve of one defect-correction step: x32 = 0, ncyc
+// V-cycles on L e = r, phi += e (graph replay when possible, one graph per
+// cycle count)
+int inner_vcycles32(afmib_solver* s, int ncyc) {
     MGLevel& L = s->lv[0];
     MGLevelT<float>& L32 = s->lv32[0];
     const long long N = L.d.ncell();
     auto body = [&]() -> int {
         CK(cudaMemsetAsync(L32.x, 0, N * sizeof(float), s->st));
-        for (int k = 0; k < s->inner_cycles; ++k) TRY(vcycle<float>(s, 0));
+        for (int k = 0; k < ncyc; ++k) TRY(vcycle<float>(s, 0));
         {
             ProfScope ps(s, P_CORRECT, (double)N * (8 + 4 + 8));
             launch_add_correction<float>(N, L.x, L32.x, s->st);
@@ -522,9 +543,9 @@ int inner_vcycles32(afmib_solver* s) {
         return AFMIB_OK;
     };
     if (s->prof || !s->use_graphs) return body();
-    if (!s->vg32) TRY(capture_graph(s, &s->vg32, &s->vg32_launches, body));
-    CK(cudaGraphLaunch(s->vg32, s->st));
-    s->stats.kernel_launches += s->vg32_launches;
+    if (!s->vg32[ncyc]) TRY(capture_graph(s, &s->vg32[ncyc], &s->vg32_launches[ncyc], body));
+    CK(cudaGraphLaunch(s->vg32[ncyc], s->st));
+    s->stats.kernel_launches += s->vg32_launches[ncyc];
     return AFMIB_OK;
 }
 
@@ -698,7 +719,8 @@ int mg_solve_mixed(afmib_solver* s, int* cycles) {
     }
     TRY(initial_potential(s));
     CK(cudaMemsetAsync(s->dflag + 1, 0, sizeof(int), s->st));
-    int c = 0, outer = 0;
+    int c = 0, outer = 0, last_cyc = 0;
+    double last_rms = 0.0;
     int status = AFMIB_OK;
     for (;;) {
         {
@@ -711,11 +733,19 @@ int mg_solve_mixed(afmib_solver* s, int* cycles) {
         const double rms = std::sqrt(s->hscal[9]) / std::sqrt((double)N);
         s->stats.last_mg_rms = rms;
         if (!std::isfinite(rms)) { status = s->fail(AFMIB_ERR_NAN, "multigrid residual is not finite"); break; }
+        if (last_cyc > 0 && rms > 0.0 && rms < last_rms) s->mg_rho = std::pow(rms / last_rms, 1.0 / last_cyc);
         if (rms <= s->cfg.tol) break;
         if (c >= s->cfg.max_mg_cycles) { status = s->fail(AFMIB_ERR_NOCONV, "multigrid cycle cap reached"); break; }
-        TRY(inner_vcycles32(s));
-        c += s->inner_cycles;
+        int cyc = s->inner_cycles;
+        if (s->adapt_cycles && s->mg_rho > 0.0) {
+            const double need = std::log(0.5 * s->cfg.tol / rms) / std::log(s->mg_rho);
+            if (need < cyc) cyc = std::max(1, (int)std::ceil(need));
+        }
+        TRY(inner_vcycles32(s, cyc));
+        c += cyc;
         ++outer;
+        last_rms = rms;
+        last_cyc = cyc;
     }
     CK(cudaMemcpyAsync(s->hflag + 1, s->dflag + 1, sizeof(int), cudaMemcpyDeviceToHost, s->st));
     CK(cudaMemcpyAsync(s->hflag + 3, s->dflag + 3, sizeof(int), cudaMemcpyDeviceToHost, s->st));
@@ -740,6 +770,10 @@ int project(afmib_solver* s) {
     else TRY(mg_solve(s, nullptr));
     const int ph = s->proj_phase;
     if (s->warm_start && ph >= 0) {
+        if (s->warm_extrap) {
+            std::swap(s->phi_prev[ph], s->phi_prev2[ph]);
+            s->phi_valid2[ph] = s->phi_valid[ph];
+        }
         CK(cudaMemcpyAsync(s->phi_prev[ph], s->lv[0].x, s->N() * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
         s->phi_valid[ph] = true;
     }
@@ -1373,8 +1407,11 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_SMOOTHER")) s->pipe_smoother = std::string(e) == "pipe";
     if (const char* e = std::getenv("AFMIB_PIPE_MIN_NX")) s->pipe_min_nx = std::atoi(e);
     if (const char* e = std::getenv("AFMIB_BFP")) s->bfp_defects = std::string(e) == "1";
-    if (const char* e = std::getenv("AFMIB_INNER_CYCLES")) s->inner_cycles = std::max(1, std::atoi(e));
+    if (const char* e = std::getenv("AFMIB_INNER_CYCLES"))
+        s->inner_cycles = std::min(kMaxInnerCycles, std::max(1, std::atoi(e)));
+    if (const char* e = std::getenv("AFMIB_INNER_ADAPT")) s->adapt_cycles = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_INNER_SOLVER")) s->jacobi_inner = std::string(e) != "cg";
+    if (const char* e = std::getenv("AFMIB_WARM_EXTRAP")) s->warm_extrap = std::string(e) == "1";
     if (const char* e = std::getenv("AFMIB_GRAPHS")) s->use_graphs = std::string(e) != "0";
     if (g.proj_start < AFMIB_START_DEFAULT || g.proj_start > AFMIB_START_WARM)
         return s->fail(AFMIB_ERR_ARG, "proj_start must be AFMIB_START_DEFAULT, _ZERO or _WARM");
@@ -1401,6 +1438,10 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     TRY(dalloc(s, &s->divb, N));
     TRY(dalloc(s, &s->phi_prev[0], N));
     TRY(dalloc(s, &s->phi_prev[1], N));
+    if (s->warm_extrap) {
+        TRY(dalloc(s, &s->phi_prev2[0], N));
+        TRY(dalloc(s, &s->phi_prev2[1], N));
+    }
     TRY(dalloc(s, &s->walls, 4 * s->nxz()));
     TRY(dalloc(s, &s->wallgrad, 6 * s->nxz()));
     TRY(dalloc(s, &s->cg_r, N));
@@ -1588,6 +1629,7 @@ int afmib_set_velocity(afmib_solver* s, const double* u, const double* v, const 
     TRY(copy_in(s, s->w, w, s->N()));
     TRY(refresh_shadow(s));
     s->phi_valid[0] = s->phi_valid[1] = false;  // a new state: no warm start
+    s->phi_valid2[0] = s->phi_valid2[1] = false;
     return sync(s);
 }
 

@@ -125,6 +125,30 @@ def test_ns_substeps_channel_warm_start(golden):
     assert pressure_rel(p, d["p"], g, float(d["mu"]), float(d["rho"]), float(d["dt"])) < 1e-9
 
 
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
+def test_ns_substeps_channel_extrapolated_start(golden, monkeypatch, precision):
+    """Warm start extrapolated from the two previous potentials of the same
+    sub-step kind (AFMIB_WARM_EXTRAP=1, phi0 = 2 phi_{n-1} - phi_{n-2}): the
+    same fixed point inside the same RMS tolerance, so the bars are those of
+    the plain warm start (mixed form: the mixed-form bars, 1e-8 on velocity
+    and 1e-6 on pressure, as in the mixed sub-step test below)."""
+    monkeypatch.setenv("AFMIB_WARM_EXTRAP", "1")
+    d = golden("ns_16")
+    with capi.Solver(16, bc=capi.BC_CHANNEL, mu=float(d["mu"]), rho=float(d["rho"]), dt=float(d["dt"]),
+                     tol=float(d["tol"]), precision=precision, proj_start=capi.START_WARM) as sv:
+        sv.set_velocity(d["u0"], d["v0"], d["w0"])
+        sv.project()
+        for _ in range(int(d["substeps"])):
+            sv.ns_step(d["fx"], d["fy"], d["fz"])
+        u, v, w = sv.get_velocity()
+        p = sv.get_pressure()
+    vt = TOL if precision == capi.FP64 else 1e-8
+    assert rel(u, d["u"]) < vt and rel(v, d["v"]) < vt and rel(w, d["w"]) < vt
+    g = po.Grid(16, 16, 16, 16, channel=True)
+    pt = 1e-9 if precision == capi.FP64 else 1e-6
+    assert pressure_rel(p, d["p"], g, float(d["mu"]), float(d["rho"]), float(d["dt"])) < pt
+
+
 def test_proj_start_rejected():
     with pytest.raises(capi.AfmibError):
         capi.Solver(8, proj_start=3)
