@@ -12,6 +12,8 @@
 // need channel-specific code.
 #pragma once
 
+#include <cstdlib>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -63,8 +65,12 @@ struct Ix2 {
     __device__ __forceinline__ int zm(int z) const { return (z - 1) & mz; }
     __device__ __forceinline__ int zp(int z) const { return (z + 1) & mz; }
 };
+// Power-of-two kernels apply; AFMIB_IX2=0 keeps the general kernels (read at
+// every launch, so a test can compare both in one process).
 inline bool ix2_ok(const Dims& d) {
     auto p2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
+    if (const char* e = std::getenv("AFMIB_IX2"))
+        if (e[0] == '0') return false;
     return p2(d.nx) && p2(d.ny) && p2(d.nz) && d.ncell() < (1ll << 31);
 }
 

@@ -114,9 +114,10 @@ bool launch_lap_defect_bfp(const Dims& d, float* r, const double* x, const doubl
                            cudaStream_t s);
 void launch_helm_defect_bfp(const Dims& d, int comp, double scale, const double* x, const double* b, float* r,
                             RedScratch sc, double* out, cudaStream_t s);
-// One red (color 0) or black (color 1) Gauss-Seidel half sweep.
+// One red (color 0) or black (color 1) Gauss-Seidel half sweep; omega:
+// over-relaxation x + omega (gs - x) on levels with nx >= 64 (1 below).
 template <typename T>
-void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s);
+void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s, double omega = 1.0);
 // One full red+black sweep per launch, out of place (xin -> xout), z-marching
 // blocks fed by bulk asynchronous row copies; equals the two per-colour
 // launches cell for cell. FY == 0: level not eligible (small, 2D, or rows not

@@ -268,6 +268,12 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_cell_table(const unsigned* __r
 // runs. A face at E-local J gathers cells [J-2, J+1] along its own axis and
 // [J-2, J+2] along the other two, i.e. at most 25 contiguous runs, in a fixed
 // order: no float atomics, bitwise repeatable.
+// A tile whose neighbourhood holds more than `cap` markers is either left to
+// a second, larger-capacity launch (ovf_list given) or, in that launch,
+// spread in chunks of `cap` staged markers. A face visits its runs in
+// increasing staged order (rows ascend in E-linear order), so cutting that
+// order into chunks leaves every face's summation order, and its result bits,
+// unchanged: there is no marker-density limit.
 // ---------------------------------------------------------------------------
 template <typename T, int TS, int TZ>
 __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, const int* __restrict__ perm,
@@ -276,7 +282,7 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
                                                                 const int* __restrict__ slot, const int* __restrict__ ctab,
                                                                 const int* __restrict__ list, const int* __restrict__ count,
                                                                 int cap, T* __restrict__ fu, T* __restrict__ fv,
-                                                                T* __restrict__ fw, int* __restrict__ flag,
+                                                                T* __restrict__ fw,
                                                                 int* __restrict__ ovf_list, int* __restrict__ ovf_count,
                                                                 int* __restrict__ next_tile) {
     // 3D: TZ == TS, the neighbourhood grows by 2 cells per side along every
@@ -309,6 +315,21 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
         const int t = list[li];
         const int tx = t % ntx, ty = (t / ntx) % nty, tz = t / (ntx * nty);
         const int ox = tx * TS - 2, oy = ty * TS - 2, oz = tz * TZ - HZ;  // E origin (unwrapped cells)
+        // sorted run [p0, p0 + cnt) of the markers binned in E cell e
+        auto run_of = [&](int e, int& p0, int& cnt) {
+            p0 = 0;
+            cnt = 0;
+            const int ex = e % E, ey = (e / E) % E, ez = e / E2;
+            const int gy = oy + ey;
+            if (d.channel && (gy < 0 || gy >= d.ny)) return;
+            const int gx = wrap1(ox + ex, d.nx), gyw = wrap1(gy, d.ny), gz = wrap1(oz + ez, d.nz);
+            const int sl = slot[gx / TS + ntx * (gyw / TS + nty * (gz / TZ))];
+            if (sl < 0) return;
+            const int lc = (gx % TS) + TS * ((gyw % TS) + TS * (gz % TZ));
+            const int* row = ctab + (size_t)sl * (C + 1) + lc;
+            p0 = row[0];
+            cnt = row[1] - p0;
+        };
         // ---- markers of each E cell (E-linear order e = ex + E (ey + E ez)):
         //      thread tid takes cells [tid * CPT, tid * CPT + CPT), whose
         //      cell-table loads are independent of one another
@@ -319,20 +340,7 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
             const int e = tid * CPT + k;
             cnt[k] = 0;
             p0[k] = 0;
-            if (e < E3) {
-                const int ex = e % E, ey = (e / E) % E, ez = e / E2;
-                const int gy = oy + ey;
-                if (!(d.channel && (gy < 0 || gy >= d.ny))) {
-                    const int gx = wrap1(ox + ex, d.nx), gyw = wrap1(gy, d.ny), gz = wrap1(oz + ez, d.nz);
-                    const int sl = slot[gx / TS + ntx * (gyw / TS + nty * (gz / TZ))];
-                    if (sl >= 0) {
-                        const int lc = (gx % TS) + TS * ((gyw % TS) + TS * (gz % TZ));
-                        const int* row = ctab + (size_t)sl * (C + 1) + lc;
-                        p0[k] = row[0];
-                        cnt[k] = row[1] - p0[k];
-                    }
-                }
-            }
+            if (e < E3) run_of(e, p0[k], cnt[k]);
             tot += cnt[k];
         }
         // ---- block exclusive scan of the per-thread totals (thread order = E order);
@@ -360,69 +368,93 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
         __syncthreads();
         const int nc_all = s_scan[NW - 1];
         int off = inc - tot + (warp > 0 ? s_scan[warp - 1] : 0);
-        // ---- E-cell starts and the staged marker indices
+        const bool chunked = nc_all > cap;  // block-uniform
+        if (chunked && ovf_list) {           // left to the large-capacity pass
+            if (tid == 0) ovf_list[atomicAdd(ovf_count, 1)] = t;
+            continue;
+        }
+        // ---- E-cell starts and, in one pass, the staged marker indices
 #pragma unroll
         for (int k = 0; k < CPT; ++k) {
             const int e = tid * CPT + k;
             if (e < E3) {
                 s_estart[e] = off;
-                for (int m = 0; m < cnt[k]; ++m)
-                    if (off + m < cap) s_k[off + m] = perm[p0[k] + m];
+                if (!chunked)
+                    for (int m = 0; m < cnt[k]; ++m) s_k[off + m] = perm[p0[k] + m];
                 off += cnt[k];
             }
         }
         if (tid == 0) s_estart[E3] = nc_all;
-        if (nc_all > cap && tid == 0) {
-            if (ovf_list) ovf_list[atomicAdd(ovf_count, 1)] = t;  // left to the large-capacity pass
-            else atomicExch(flag, 3);
-        }
-        __syncthreads();
-        if (nc_all > cap && ovf_list) continue;  // block-uniform
-        const int nc = nc_all < cap ? nc_all : cap;
-        // ---- one component at a time
-        for (int comp = 0; comp < 3; ++comp) {
-            for (int sl = tid; sl < nc; sl += NT) {
-                const int k = s_k[sl];
-                const T g = T((double)G[(size_t)comp * M + k] * (vol ? vol[k] : 1.0) * scale);
-                int packed = 0;
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    const int v = (a == comp) ? 0 : 1;
-                    const int o = a == 0 ? ox : (a == 1 ? oy : oz);
-                    const int n_a = a == 0 ? d.nx : (a == 1 ? d.ny : d.nz);
-                    // E-local first face: cell relative to the E origin + offset
-                    int ec = mw.cell[3 * k + a] - o;
-                    if (!(a == 1 && d.channel)) ec = wrapi(ec, n_a);
-                    const int b = ec + mw.dbase[(k * 3 + a) * 2 + v];
-                    packed |= (b + 8) << (8 * a);
-                    const T* w = mw.w + (((size_t)k * 3 + a) * 2 + v) * 4;
-#pragma unroll
-                    for (int m = 0; m < 4; ++m) s_w[(size_t)sl * 12 + a * 4 + m] = a == 2 ? w[m] * g : w[m];
-                }
-                s_base[sl] = packed;
+        const int nchunk = chunked ? (nc_all + cap - 1) / cap : 1;
+        // chunked: marker indices of staged slots [lo, lo + cap) from this
+        // thread's E cells (runs looked up again: nothing held across chunks)
+        auto stage_ids = [&](int lo) {
+            for (int k = 0; k < CPT; ++k) {
+                const int e = tid * CPT + k;
+                if (e >= E3) break;
+                const int o = s_estart[e], n = s_estart[e + 1] - o;
+                if (n == 0 || o + n <= lo || o >= lo + cap) continue;
+                int q0, qn;
+                run_of(e, q0, qn);
+                const int a = lo - o > 0 ? lo - o : 0, b = lo + cap - o < n ? lo + cap - o : n;
+                for (int m = a; m < b; ++m) s_k[o + m - lo] = perm[q0 + m];
             }
-            __syncthreads();
-            T* f = comp == 0 ? fu : (comp == 1 ? fv : fw);
-            const int J[3] = {lx + 2, ly + 2, lz + HZ};
+        };
+        __syncthreads();
+        // ---- one component at a time (and, past the capacity, one chunk at a time)
+        const int J[3] = {lx + 2, ly + 2, lz + HZ};
+        for (int comp = 0; comp < 3; ++comp) {
+            T acc = T(0);
             const int hx = (comp == 0) ? J[0] + 1 : J[0] + 2;
             const int hy = (comp == 1) ? J[1] + 1 : J[1] + 2;
             const int hz = TZ == 1 ? J[2] : ((comp == 2) ? J[2] + 1 : J[2] + 2);
-            T acc = T(0);
-            for (int ez = J[2] - HZ; ez <= hz; ++ez)
-                for (int ey = J[1] - 2; ey <= hy; ++ey) {
-                    const int row = E * (ey + E * ez);
-                    const int s0 = s_estart[row + J[0] - 2], s1 = s_estart[row + hx + 1];
-                    for (int sl = s0; sl < s1 && sl < nc; ++sl) {
-                        const int pk = s_base[sl];
-                        const int mx = J[0] - ((pk & 255) - 8);
-                        const int my = J[1] - (((pk >> 8) & 255) - 8);
-                        const int mz = J[2] - (((pk >> 16) & 255) - 8);
-                        if ((unsigned)mx < 4u && (unsigned)my < 4u && (unsigned)mz < 4u) {
-                            const T* w = s_w + (size_t)sl * 12;
-                            acc += (w[mx] * w[4 + my]) * w[8 + mz];
+            for (int ch = 0; ch < nchunk; ++ch) {
+                const int lo = ch * cap, nc = nc_all - lo < cap ? nc_all - lo : cap;
+                if (chunked) {
+                    __syncthreads();  // the previous chunk's gather is done with s_k, s_base, s_w
+                    stage_ids(lo);
+                    __syncthreads();
+                }
+                for (int sl = tid; sl < nc; sl += NT) {
+                    const int k = s_k[sl];
+                    const T g = T((double)G[(size_t)comp * M + k] * (vol ? vol[k] : 1.0) * scale);
+                    int packed = 0;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const int v = (a == comp) ? 0 : 1;
+                        const int o = a == 0 ? ox : (a == 1 ? oy : oz);
+                        const int n_a = a == 0 ? d.nx : (a == 1 ? d.ny : d.nz);
+                        // E-local first face: cell relative to the E origin + offset
+                        int ec = mw.cell[3 * k + a] - o;
+                        if (!(a == 1 && d.channel)) ec = wrapi(ec, n_a);
+                        const int b = ec + mw.dbase[(k * 3 + a) * 2 + v];
+                        packed |= (b + 8) << (8 * a);
+                        const T* w = mw.w + (((size_t)k * 3 + a) * 2 + v) * 4;
+#pragma unroll
+                        for (int m = 0; m < 4; ++m) s_w[(size_t)sl * 12 + a * 4 + m] = a == 2 ? w[m] * g : w[m];
+                    }
+                    s_base[sl] = packed;
+                }
+                __syncthreads();
+                for (int ez = J[2] - HZ; ez <= hz; ++ez)
+                    for (int ey = J[1] - 2; ey <= hy; ++ey) {
+                        const int row = E * (ey + E * ez);
+                        int s0 = s_estart[row + J[0] - 2] - lo, s1 = s_estart[row + hx + 1] - lo;
+                        s0 = s0 > 0 ? s0 : 0;
+                        s1 = s1 < nc ? s1 : nc;
+                        for (int sl = s0; sl < s1; ++sl) {
+                            const int pk = s_base[sl];
+                            const int mx = J[0] - ((pk & 255) - 8);
+                            const int my = J[1] - (((pk >> 8) & 255) - 8);
+                            const int mz = J[2] - (((pk >> 16) & 255) - 8);
+                            if ((unsigned)mx < 4u && (unsigned)my < 4u && (unsigned)mz < 4u) {
+                                const T* w = s_w + (size_t)sl * 12;
+                                acc += (w[mx] * w[4 + my]) * w[8 + mz];
+                            }
                         }
                     }
-                }
+            }
+            T* f = comp == 0 ? fu : (comp == 1 ? fv : fw);
             const int gx = tx * TS + lx, gy = ty * TS + ly, gz = tz * TZ + lz;
             if (!(d.channel && comp == 1 && gy == 0)) f[lin(d, gx, gy, gz)] = acc;
             __syncthreads();
@@ -547,7 +579,7 @@ size_t spread_smem_bytes(int TS, int TZ, int cap) {
 template <typename T, int TS, int TZ>
 static void spread_launch(const Dims& d, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
                           double scale, const int* slot, const int* ctab, const int* list, const int* count,
-                          int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, int* ovf_list, int* ovf_count,
+                          int max_tiles, int cap, T* fu, T* fv, T* fw, int* ovf_list, int* ovf_count,
                           int* next_tile, cudaStream_t s) {
     const size_t smem = spread_smem_bytes<T>(TS, TZ, cap);
     // opt in to exactly the dynamic shared memory this launch uses (the
@@ -562,19 +594,19 @@ static void spread_launch(const Dims& d, int M, const int* perm, MarkerW<T> mw, 
     int blocks = max_tiles < 152 * 4 ? max_tiles : 152 * 4;
     if (blocks < 1) blocks = 1;
     k_spread_gather<T, TS, TZ><<<blocks, TS * TS * TZ, smem, s>>>(d, M, perm, mw, G, vol, scale, slot, ctab, list,
-                                                                  count, cap, fu, fv, fw, flag, ovf_list, ovf_count,
+                                                                  count, cap, fu, fv, fw, ovf_list, ovf_count,
                                                                   next_tile);
 }
 
 template <typename T>
 void launch_spread_gather(const Dims& d, int TS, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
                           double scale, const int* slot, const int* ctab, const int* list, const int* count,
-                          int max_tiles, int cap, T* fu, T* fv, T* fw, int* flag, int* ovf_list, int* ovf_count,
+                          int max_tiles, int cap, T* fu, T* fv, T* fw, int* ovf_list, int* ovf_count,
                           int* next_tile, cudaStream_t s) {
     const bool flat = d.nz == 1;
 #define AFMIB_SPREAD(TSV, TZV)                                                                                    \
     spread_launch<T, TSV, TZV>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, \
-                               flag, ovf_list, ovf_count, next_tile, s)
+                               ovf_list, ovf_count, next_tile, s)
     if (TS == 8 && !flat) AFMIB_SPREAD(8, 8);
     else if (TS == 4 && !flat) AFMIB_SPREAD(4, 4);
     else if (TS == 8) AFMIB_SPREAD(8, 1);
@@ -599,7 +631,7 @@ void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, do
     template size_t spread_smem_bytes<T>(int, int, int);                                                             \
     template void launch_spread_gather<T>(const Dims&, int, int, const int*, MarkerW<T>, const T*, const double*, \
                                           double, const int*, const int*, const int*, const int*, int, int, T*,  \
-                                          T*, T*, int*, int*, int*, int*, cudaStream_t);                        \
+                                          T*, T*, int*, int*, int*, cudaStream_t);                              \
     template void launch_interp<T, double>(const Dims&, int, const int*, MarkerW<T>, const double*, const double*, \
                                            const double*, double*, cudaStream_t);                               \
     template void launch_interp<T, float>(const Dims&, int, const int*, MarkerW<T>, const float*, const float*,  \

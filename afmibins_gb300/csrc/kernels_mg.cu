@@ -142,21 +142,25 @@ __global__ void __launch_bounds__(kRedBlock) k_lap_defect_bfp(Dims d, int k2, fl
 
 // One colour of red-black Gauss–Seidel: x_i = (b_i - n^2 S) / (-c n^2).
 template <typename T>
-__device__ __forceinline__ void rbgs_cell(const Dims& d, T* xv, const T* b, int x, int y, int z) {
+__device__ __forceinline__ void rbgs_cell(const Dims& d, T* xv, const T* b, int x, int y, int z, T omega = T(1)) {
     T S, c;
     lap_row(d, xv, x, y, z, S, c);
     const long long i = lin(d, x, y, z);
     const T inv = T(1) / (T(d.n) * T(d.n));
     const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
-    xv[i] = (S - b[i] * inv) * rc;
+    T v = (S - b[i] * inv) * rc;
+    if (omega != T(1)) v = v + (omega - T(1)) * (v - xv[i]);
+    xv[i] = v;
 }
 
+// omega != 1: over-relaxed update x + omega (gs - x); omega == 1 is plain
+// Gauss-Seidel, bit for bit
 template <typename T>
-__global__ void k_rbgs(Dims d, int color, T* __restrict__ xv, const T* __restrict__ b) {
+__global__ void k_rbgs(Dims d, int color, T omega, T* __restrict__ xv, const T* __restrict__ b) {
     const int y = blockIdx.y * BY + threadIdx.y, z = blockIdx.z;
     const int x = 2 * (blockIdx.x * BX + threadIdx.x) + ((y + z + color) & 1);
     if (x >= d.nx || y >= d.ny) return;
-    rbgs_cell(d, xv, b, x, y, z);
+    rbgs_cell(d, xv, b, x, y, z, omega);
 }
 
 // Batched forms: each thread takes ZU cells along z of its (x, y) column and
@@ -166,9 +170,12 @@ __global__ void k_rbgs(Dims d, int color, T* __restrict__ xv, const T* __restric
 // black ones, so the delayed stores change nothing: same values as the
 // one-cell kernels.
 constexpr int kZU = 8;  // z cells per thread of the batched stencil kernels
+// smallest level (x extent) on which a requested over-relaxation applies;
+// the coarser levels, the one-block tail among them, stay Gauss-Seidel
+constexpr int kOmegaMinNx = 64;
 
 template <typename T, int ZU>
-__global__ void k_rbgs_z(Dims d, int color, T* __restrict__ xv, const T* __restrict__ b) {
+__global__ void k_rbgs_z(Dims d, int color, T omega, T* __restrict__ xv, const T* __restrict__ b) {
     const int y = blockIdx.y * BY + threadIdx.y, t = blockIdx.x * BX + threadIdx.x, z0 = blockIdx.z * ZU;
     if (y >= d.ny) return;
     T val[ZU];
@@ -184,6 +191,7 @@ __global__ void k_rbgs_z(Dims d, int color, T* __restrict__ xv, const T* __restr
             const long long i = lin(d, x, y, z);
             const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
             val[u] = (S - b[i] * inv) * rc;
+            if (omega != T(1)) val[u] = val[u] + (omega - T(1)) * (val[u] - xv[i]);
             at[u] = i;
         }
     }
@@ -213,7 +221,7 @@ __device__ __forceinline__ void lap_row2(const Dims& d, const Ix2& I, const T* _
 }
 
 template <typename T, int ZU>
-__global__ void k_rbgs_z2(Dims d, int color, T* __restrict__ xv, const T* __restrict__ b) {
+__global__ void k_rbgs_z2(Dims d, int color, T omega, T* __restrict__ xv, const T* __restrict__ b) {
     const Ix2 I(d);
     const int y = blockIdx.y * BY + threadIdx.y, t = blockIdx.x * BX + threadIdx.x, z0 = blockIdx.z * ZU;
     if (y >= d.ny || 2 * t >= d.nx) return;
@@ -228,6 +236,7 @@ __global__ void k_rbgs_z2(Dims d, int color, T* __restrict__ xv, const T* __rest
         const int i = I.at(x, y, z);
         const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
         val[u] = (S - b[i] * inv) * rc;
+        if (omega != T(1)) val[u] = val[u] + (omega - T(1)) * (val[u] - xv[i]);
         at[u] = i;
     }
 #pragma unroll
@@ -852,15 +861,16 @@ void launch_residual(const Dims& d, T* r, const T* x, const T* b, RedScratch* sc
         k_residual<T><<<grid3(d), dim3(BX, BY), 0, s>>>(d, r, x, b);
 }
 template <typename T>
-void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s) {
+void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s, double omega) {
+    if (d.nx < kOmegaMinNx) omega = 1.0;
     if (d.nz % kZU == 0 && d.nx >= 64) {
         dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / kZU);
-        if (ix2_ok(d)) k_rbgs_z2<T, kZU><<<g, dim3(BX, BY), 0, s>>>(d, color, x, b);
-        else k_rbgs_z<T, kZU><<<g, dim3(BX, BY), 0, s>>>(d, color, x, b);
+        if (ix2_ok(d)) k_rbgs_z2<T, kZU><<<g, dim3(BX, BY), 0, s>>>(d, color, T(omega), x, b);
+        else k_rbgs_z<T, kZU><<<g, dim3(BX, BY), 0, s>>>(d, color, T(omega), x, b);
         return;
     }
     dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz);
-    k_rbgs<T><<<g, dim3(BX, BY), 0, s>>>(d, color, x, b);
+    k_rbgs<T><<<g, dim3(BX, BY), 0, s>>>(d, color, T(omega), x, b);
 }
 namespace {
 int log2_exact(int v) {
@@ -998,7 +1008,7 @@ void launch_coarse_solve(const Dims& d, T* x, T* b, T* r, T* p, T* q, double tol
 #define AFMIB_MG_INST(T)                                                                                 \
     template void launch_lap_apply<T>(const Dims&, T*, const T*, cudaStream_t);                          \
     template void launch_residual<T>(const Dims&, T*, const T*, const T*, RedScratch*, double*, cudaStream_t); \
-    template void launch_rbgs<T>(const Dims&, int, T*, const T*, cudaStream_t);                          \
+    template void launch_rbgs<T>(const Dims&, int, T*, const T*, cudaStream_t, double);                        \
     template PipeCfg rbgs_pipe_cfg<T>(const Dims&);                                                      \
     template void launch_rbgs_pipe<T>(const Dims&, const PipeCfg&, const T*, T*, const T*, int*, cudaStream_t); \
     template void launch_restrict<T>(const Dims&, T*, const T*, cudaStream_t);                           \

@@ -68,6 +68,15 @@ struct afmib_solver {
     // in the previous one: only the cycles that bring the defect below
     // tol / 2 (AFMIB_INNER_ADAPT=0: always inner_cycles)
     bool adapt_cycles = true;
+    // The FP32 inner cycles only precondition the FP64 defect correction, so
+    // they keep their own schedule: red-black sweeps over-relaxed by omega on
+    // levels with nx >= 64 (AFMIB_INNER_OMEGA; 1: Gauss-Seidel) and (nu1, nu2)
+    // sweeps around the coarse correction (AFMIB_INNER_NU=a,b). V(2,1) with
+    // omega = 1.25 measured fastest at 256^3 (36.4 steps/s against 33.8 for
+    // the FP64 cycles' V(2,2) Gauss-Seidel). The FP64 cycles keep the
+    // configuration's nu1, nu2 and plain Gauss-Seidel.
+    double inner_omega = 1.25;
+    int inner_nu1 = 2, inner_nu2 = 1;
     double mg_rho = 0.0;        // measured per-cycle contraction (0: none yet)
     // pipelined red-black sweeps (AFMIB_SMOOTHER=pipe); the default is the
     // batched per-colour launches, measured faster at 256^3
@@ -365,8 +374,9 @@ template <typename T>
 int smooth(afmib_solver* s, MGLevelT<T>& L, int sweeps) {
     const double Ns = (double)L.d.ncell() * sizeof(T);
     const int id = L.d.nx == s->d.nx ? P_RBGS0 : P_RBGS;  // finest level kept apart in the profile
+    const double omega = sizeof(T) == sizeof(float) ? s->inner_omega : 1.0;
     int j = 0;
-    if (L.x2 && s->pipe_smoother && L.pc.FY) {
+    if (L.x2 && s->pipe_smoother && L.pc.FY && omega == 1.0) {
         // pairs of pipelined sweeps, x -> x2 -> x
         for (; j + 2 <= sweeps; j += 2) {
             {
@@ -382,11 +392,11 @@ int smooth(afmib_solver* s, MGLevelT<T>& L, int sweeps) {
     for (; j < sweeps; ++j) {
         {
             ProfScope ps(s, id, 1.5 * Ns);
-            launch_rbgs<T>(L.d, 0, L.x, L.b, s->st);
+            launch_rbgs<T>(L.d, 0, L.x, L.b, s->st, omega);
         }
         {
             ProfScope ps(s, id, 1.5 * Ns);
-            launch_rbgs<T>(L.d, 1, L.x, L.b, s->st);
+            launch_rbgs<T>(L.d, 1, L.x, L.b, s->st, omega);
         }
     }
     CKL();
@@ -416,8 +426,8 @@ int vcycle_tail(afmib_solver* s, size_t l) {
     auto& lv = levels<T>(s);
     TailLevels<T> a{};
     a.nlev = (int)(lv.size() - l);
-    a.nu1 = s->cfg.nu1;
-    a.nu2 = s->cfg.nu2;
+    a.nu1 = sizeof(T) == sizeof(float) ? s->inner_nu1 : s->cfg.nu1;
+    a.nu2 = sizeof(T) == sizeof(float) ? s->inner_nu2 : s->cfg.nu2;
     a.maxit = s->cfg.max_cg_iters;
     a.tol = s->cfg.tol;
     for (int k = 0; k < a.nlev; ++k) {
@@ -450,7 +460,7 @@ int vcycle(afmib_solver* s, size_t l) {
         return AFMIB_OK;
     }
     const bool fine = l == 0;
-    TRY(smooth(s, L, s->cfg.nu1));
+    TRY(smooth(s, L, sizeof(T) == sizeof(float) ? s->inner_nu1 : s->cfg.nu1));
     {
         ProfScope ps(s, fine ? P_RESID0 : P_RESID, 3 * Ns);
         launch_residual<T>(L.d, L.r, L.x, L.b, nullptr, nullptr, s->st);
@@ -467,7 +477,7 @@ int vcycle(afmib_solver* s, size_t l) {
         ProfScope ps(s, fine ? P_PROLONG0 : P_PROLONG, 2 * Ns + Ns / 8);
         launch_prolong_add<T>(L.d, L.x, C.x, s->st);
     }
-    TRY(smooth(s, L, s->cfg.nu2));
+    TRY(smooth(s, L, sizeof(T) == sizeof(float) ? s->inner_nu2 : s->cfg.nu2));
     return AFMIB_OK;
 }
 
@@ -957,9 +967,9 @@ int spread_two_pass(afmib_solver* s, MarkerW<T> mw, const T* G, const double* vo
                     int cap_small, int cap_large) {
     CK(cudaMemsetAsync(s->tcount + 2, 0, 3 * sizeof(int), s->st));  // overflow count and the two tile counters
     launch_spread_gather<T>(s->d, s->TS, s->M, s->perm, mw, G, vol, scale, s->tslot, s->ctab, s->tlist, s->tcount,
-                            s->ntiles, cap_small, fu, fv, fw, s->dflag, s->tovf, s->tcount + 2, s->tcount + 3, s->st);
+                            s->ntiles, cap_small, fu, fv, fw, s->tovf, s->tcount + 2, s->tcount + 3, s->st);
     launch_spread_gather<T>(s->d, s->TS, s->M, s->perm, mw, G, vol, scale, s->tslot, s->ctab, s->tovf, s->tcount + 2,
-                            s->ntiles, cap_large, fu, fv, fw, s->dflag, nullptr, nullptr, s->tcount + 4, s->st);
+                            s->ntiles, cap_large, fu, fv, fw, nullptr, nullptr, s->tcount + 4, s->st);
     return AFMIB_OK;
 }
 
@@ -1026,7 +1036,6 @@ int check_marker_flag(afmib_solver* s) {
     const int f = s->hflag[0];
     if (f == 1) return s->fail(AFMIB_ERR_BOUNDS, "a marker came within 2.5h of a channel wall");
     if (f == 2) return s->fail(AFMIB_ERR_NAN, "a marker position is not finite");
-    if (f == 3) return s->fail(AFMIB_ERR_CAPACITY, "too many markers near one spreading tile");
     return AFMIB_OK;
 }
 
@@ -1399,6 +1408,9 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (g.inner_tol <= 0) g.inner_tol = 1e-5;
     if (g.nx < 2 || g.ny < 2 || g.nz < 1 || (g.nz == 1 && g.bc != AFMIB_BC_PERIODIC))
         return s->fail(AFMIB_ERR_ARG, "extents must be at least 2 cells (nz = 1, a 2D grid, only with periodic bc)");
+    // the grid-wide sums keep one partial per block of (32 x 8)-cell tiles
+    if ((long long)((g.nx + kRBX - 1) / kRBX) * ((g.ny + kRBY - 1) / kRBY) > kMaxRedBlocks)
+        return s->fail(AFMIB_ERR_ARG, "an (x, y) plane of more than 8192 tiles of 32 x 8 cells");
     if (g.bc != AFMIB_BC_PERIODIC && g.bc != AFMIB_BC_CHANNEL) return s->fail(AFMIB_ERR_ARG, "bc must be periodic or channel");
     if (g.precision != AFMIB_FP64 && g.precision != AFMIB_MIXED) return s->fail(AFMIB_ERR_ARG, "precision");
     s->mixed = g.precision == AFMIB_MIXED;
@@ -1410,6 +1422,14 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_INNER_CYCLES"))
         s->inner_cycles = std::min(kMaxInnerCycles, std::max(1, std::atoi(e)));
     if (const char* e = std::getenv("AFMIB_INNER_ADAPT")) s->adapt_cycles = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_INNER_OMEGA")) s->inner_omega = std::atof(e);
+    if (const char* e = std::getenv("AFMIB_INNER_NU")) {
+        int a = 0, b = 0;
+        if (std::sscanf(e, "%d,%d", &a, &b) == 2 && a >= 0 && b >= 0 && a + b > 0) {
+            s->inner_nu1 = a;
+            s->inner_nu2 = b;
+        }
+    }
     if (const char* e = std::getenv("AFMIB_INNER_SOLVER")) s->jacobi_inner = std::string(e) != "cg";
     if (const char* e = std::getenv("AFMIB_WARM_EXTRAP")) s->warm_extrap = std::string(e) == "1";
     if (const char* e = std::getenv("AFMIB_GRAPHS")) s->use_graphs = std::string(e) != "0";
@@ -1580,7 +1600,7 @@ const char* afmib_error_string(int status) {
         case AFMIB_ERR_BOUNDS: return "marker too close to a wall";
         case AFMIB_ERR_NAN: return "non-finite value";
         case AFMIB_ERR_STATE: return "call out of order";
-        case AFMIB_ERR_CAPACITY: return "too many markers near one tile";
+        case AFMIB_ERR_CAPACITY: return "a fixed capacity exceeded";
         default: return "unknown status";
     }
 }

@@ -106,54 +106,92 @@ def measured_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled during the timed region.
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    nvidia-smi is started, and its first sample awaited, before the region
+    opens: its start-up (library load, device attach) stalled CUDA calls of
+    this process when it fell inside the region. Each sample carries
+    nvidia-smi's own timestamp; the summary keeps the samples taken inside
+    the region, or the nearest ones when the region is shorter than the
+    sampling period."""
+
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 50
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.p = None
+        self.rows = []
+        self.t0 = self.t1 = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            if line.strip():
+                self.rows.append(line)
 
     def __enter__(self):
+        import threading
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
-                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                                       "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, bufsize=1)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+            t = time.time()
+            while not self.rows and time.time() - t < 5.0 and self.p.poll() is None:
+                time.sleep(0.01)
         except Exception:
             self.p = None
+        self.t0 = time.time()
         return self
 
     def __exit__(self, *a):
-        self.lines = []
+        self.t1 = time.time()
         if self.p is not None:
+            time.sleep(2 * self.PERIOD_MS / 1000.0)  # the sample after the region
             self.p.terminate()
             try:
-                out, _ = self.p.communicate(timeout=5)
+                self.p.wait(timeout=5)
             except Exception:
                 self.p.kill()
-                out, _ = self.p.communicate()
-            self.lines = [l for l in out.splitlines() if l.strip()]
+                self.p.wait()
+            self.th.join(timeout=5)
 
-    def summary(self):
-        sm, smax, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in getattr(self, "lines", []):
+    def _parsed(self):
+        import datetime
+        out = []
+        for l in self.rows:
             c = [x.strip() for x in l.split(",")]
-            if len(c) < 9:
+            if len(c) < 10:
                 continue
             try:
-                sm.append(float(c[1]))
-                smax = float(c[2])
+                ts = datetime.datetime.strptime(c[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                sm, smax = float(c[2]), float(c[3])
             except ValueError:
                 continue
-            for k, nm in enumerate(names):
-                if c[5 + k].lower() in ("active", "1"):
-                    reasons.add(nm)
-        if not sm:
+            out.append((ts, sm, smax, c[6:10]))
+        return out
+
+    def summary(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = self._parsed()
+        inside = [r for r in rows if self.t0 <= r[0] <= self.t1]
+        use = inside
+        if not use and rows:  # region shorter than the period: the nearest samples on either side
+            before = [r for r in rows if r[0] < self.t0]
+            after = [r for r in rows if r[0] > self.t1]
+            use = before[-1:] + after[:1]
+        if not use:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+        reasons = set()
+        for r in use:
+            for k, nm in enumerate(names):
+                if r[3][k].lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median([r[1] for r in use])), "sm_max_mhz": use[-1][2],
+                "reasons": sorted(reasons), "samples": len(use), "samples_in_region": len(inside)}
 
 
 def cpu_sample(args, kind_note=""):

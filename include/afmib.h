@@ -45,7 +45,7 @@ enum afmib_status {
     AFMIB_ERR_BOUNDS = 4,   /* a marker within 2.5h of a channel wall */
     AFMIB_ERR_NAN = 5,      /* non-finite residual or marker position */
     AFMIB_ERR_STATE = 6,    /* call out of order (e.g. no markers set) */
-    AFMIB_ERR_CAPACITY = 7  /* too many markers near one tile */
+    AFMIB_ERR_CAPACITY = 7  /* a fixed capacity exceeded (the no-allocation solve's array) */
 };
 
 enum { AFMIB_BC_PERIODIC = 0, AFMIB_BC_CHANNEL = 1 };
@@ -57,7 +57,9 @@ typedef struct afmib_config {
     int bc;             /* AFMIB_BC_CHANNEL: the reference's walls in y; AFMIB_BC_PERIODIC */
     int precision;      /* AFMIB_FP64 (drop-in) or AFMIB_MIXED (FP32 inner, FP64 outer) */
     int mg_levels;      /* coarsenings of the pressure multigrid; 0 -> until a dimension is odd */
-    int nu1, nu2;       /* smoothing sweeps, 0 -> 2 (src/ns/projection.h:44) */
+    int nu1, nu2;       /* smoothing sweeps of the FP64 V-cycles, 0 -> 2 (src/ns/projection.h:44);
+                           the mixed form's FP32 inner cycles run their own V(2,1)
+                           with red-black over-relaxation 1.25 on levels >= 64 */
     double mu, rho, dt; /* ns::solver(mu, rho, k, tol, ...), src/ns/solver.h:61-72 */
     double tol;         /* CG stops at ||r||_2 <= tol, MG at RMS(r) <= tol */
     int max_cg_iters;   /* 0 -> 1000 */

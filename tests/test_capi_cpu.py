@@ -49,3 +49,20 @@ def test_config_layout_matches_header(tmp_path):
 
 def test_build_is_in_tree():
     assert capi.library_path().startswith(build.PKG)
+
+
+@pytest.mark.parametrize("kwargs, words", [
+    (dict(nx=8, bc=7), "bc must be"),
+    (dict(nx=8, proj_start=3), "proj_start"),
+    (dict(nx=8, ny=8, nz=1, bc=capi.BC_CHANNEL), "2D grid"),
+    (dict(nx=4096, ny=4096, nz=1), "8192 tiles"),
+    (dict(nx=8, dt=0.0), "dt"),
+])
+def test_create_rejects_bad_configurations_without_gpu(kwargs, words):
+    """Configuration checks run before any CUDA call: a bad configuration
+    returns AFMIB_ERR_ARG with its reason, and nothing is allocated."""
+    nx = kwargs.pop("nx")
+    with pytest.raises(capi.AfmibError) as e:
+        capi.Solver(nx, **kwargs)
+    assert e.value.status == capi.AFMIB_ERR_ARG
+    assert words in str(e.value)

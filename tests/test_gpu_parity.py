@@ -284,13 +284,6 @@ def test_failure_statuses_are_reported():
         with pytest.raises(capi.AfmibError) as e:
             sv.mg_solve(b)
         assert e.value.status == capi.AFMIB_ERR_NAN
-    # more markers near one tile than the spreading capacity: a status, no fault
-    with capi.Solver(32) as sv:
-        rng = np.random.default_rng(26)
-        X = 0.5 + rng.uniform(-1.0, 1.0, (2000, 3)) / 32
-        with pytest.raises(capi.AfmibError) as e:
-            sv.spread(X, rng.standard_normal((3, 2000)))
-        assert e.value.status == capi.AFMIB_ERR_CAPACITY
     # bad configuration
     with pytest.raises(capi.AfmibError) as e:
         capi.Solver(16, mu=0.01, rho=-1.0)
@@ -463,16 +456,88 @@ def test_inner_jacobi_matches_inner_cg(monkeypatch, bc):
         assert rel(b, a) < 1e-10
 
 
-def test_spread_dense_cluster_takes_large_capacity_pass():
-    """1,200 markers inside two cells: their tiles' neighbourhoods exceed the
-    first pass's capacity and are spread by the large-capacity pass, with the
-    same result as the oracle."""
+@pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
+def test_power_of_two_kernels_match_general_kernels(monkeypatch, bc):
+    """The power-of-two kernels (32-bit shift-composed indices, several planes
+    per thread: smoother, residual, transfers, Jacobi sweeps) evaluate the
+    same terms in the same order as the general kernels (AFMIB_IX2=0): an
+    FP64 multigrid solve agrees bit for bit, mixed-form sub-steps to the
+    solver tolerance."""
+    n = 64
+    channel = bc == capi.BC_CHANNEL
+    g = po.Grid(n, n, n, n, channel=channel)
+    rng = np.random.default_rng(25)
+    b = rng.standard_normal(g.ncell)
+    u, v, w = 0.1 * rng.standard_normal(g.ncell), 0.1 * rng.standard_normal(g.nv), 0.1 * rng.standard_normal(g.ncell)
+    f = [rng.standard_normal(g.ncell), rng.standard_normal(g.nv), rng.standard_normal(g.ncell)]
+    mg, ns = {}, {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("AFMIB_IX2", mode)
+        with capi.Solver(n, bc=bc, precision=capi.FP64, tol=1e-10) as sv:
+            mg[mode] = sv.mg_solve(b)
+        with capi.Solver(n, bc=bc, precision=capi.MIXED, mu=0.01, rho=1.0, dt=1e-3, tol=1e-12) as sv:
+            sv.set_velocity(u, v, w)
+            sv.project()
+            for _ in range(2):
+                sv.ns_step(*f)
+            ns[mode] = sv.get_velocity()
+    assert mg["0"][1] == mg["1"][1]
+    assert np.array_equal(mg["0"][0], mg["1"][0])
+    for a, c in zip(ns["0"], ns["1"]):
+        assert rel(c, a) < 1e-10
+
+
+@pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
+def test_inner_cycle_schedule_matches_plain_gauss_seidel(monkeypatch, bc):
+    """Mixed form: the FP32 inner V-cycles' own schedule (V(2,1), red-black
+    over-relaxation 1.25 on levels >= 64) against V(2,2) plain Gauss-Seidel
+    (AFMIB_INNER_OMEGA=1, AFMIB_INNER_NU=2,2): both are preconditioners of the
+    same FP64 defect correction and stop on the same residual test, so the
+    sub-steps agree to the solver tolerance: RMS(r) <= 1e-12 leaves the
+    velocities 1e-10 to 1e-9 apart (max-norm, relative), and each solve's own
+    residual is checked against the oracle's Laplacian."""
+    n = 64
+    channel = bc == capi.BC_CHANNEL
+    g = po.Grid(n, n, n, n, channel=channel)
+    rng = np.random.default_rng(26)
+    u, v, w = 0.1 * rng.standard_normal(g.ncell), 0.1 * rng.standard_normal(g.nv), 0.1 * rng.standard_normal(g.ncell)
+    f = [rng.standard_normal(g.ncell), rng.standard_normal(g.nv), rng.standard_normal(g.ncell)]
+    out = {}
+    for mode, env in (("plain", ("1", "2,2")), ("default", None)):
+        if env:
+            monkeypatch.setenv("AFMIB_INNER_OMEGA", env[0])
+            monkeypatch.setenv("AFMIB_INNER_NU", env[1])
+        else:
+            monkeypatch.delenv("AFMIB_INNER_OMEGA", raising=False)
+            monkeypatch.delenv("AFMIB_INNER_NU", raising=False)
+        with capi.Solver(n, bc=bc, precision=capi.MIXED, mu=0.01, rho=1.0, dt=1e-3, tol=1e-12) as sv:
+            sv.set_velocity(u, v, w)
+            sv.project()
+            for _ in range(2):
+                sv.ns_step(*f)
+            out[mode] = sv.get_velocity()
+            b = rng.standard_normal(g.ncell)
+            x, cycles = sv.mg_solve(b)
+        r = (b - b.mean()) - po.lap_apply(g, x)
+        assert np.sqrt(np.mean(r ** 2)) <= 2e-12
+    for a, c in zip(out["plain"], out["default"]):
+        assert rel(c, a) < 1e-9
+
+
+@pytest.mark.parametrize("m", [1200, 5000, 20000])
+def test_spread_dense_cluster_takes_large_capacity_pass(m):
+    """m markers inside two cells: 1,200 exceed the first pass's capacity and
+    are spread by the large-capacity pass; 5,000 and 20,000 exceed that one
+    too and are spread in chunks of its capacity. Same result as the oracle
+    in every case, and the same bits on a repeat."""
     n = 32
     g = po.Grid(n, n, n, n, channel=False)
     rng = np.random.default_rng(25)
-    X = 0.5 + rng.uniform(-1.0, 1.0, (1200, 3)) / n
-    F = rng.standard_normal((3, 1200))
+    X = 0.5 + rng.uniform(-1.0, 1.0, (m, 3)) / n
+    F = rng.standard_normal((3, m))
     with capi.Solver(n) as sv:
         fx, fy, fz = sv.spread(X, F)
+        again = sv.spread(X, F)
     for comp, f in enumerate((fx, fy, fz)):
         assert rel(f, po.spread(g, comp, X, F[comp])) < OPS_TOL
+        assert np.array_equal(f, again[comp])
