@@ -20,16 +20,42 @@ namespace afmib {
 
 #if defined(__CUDA_ARCH__)
 __device__ __forceinline__ long long dbits(double d) { return __double_as_longlong(d); }
+__device__ __forceinline__ double dfrom(unsigned long long u) { return __longlong_as_double((long long)u); }
 __device__ __forceinline__ float fbits(unsigned u) { return __int_as_float((int)u); }
 __device__ __forceinline__ unsigned fword(float f) { return (unsigned)__float_as_int(f); }
 __device__ __forceinline__ int clz64(unsigned long long v) { return __clzll((long long)v); }
 #else
 inline long long dbits(double d) { long long u; std::memcpy(&u, &d, 8); return u; }
+inline double dfrom(unsigned long long u) { double d; std::memcpy(&d, &u, 8); return d; }
 inline float fbits(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline unsigned fword(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
 inline int clz64(unsigned long long v) { return v ? __builtin_clzll(v) : 64; }
 #endif
 #define AFMIB_HD __host__ __device__ __forceinline__
+
+// ---------------------------------------------------------------------------
+// FP32 -> FP64 by integer operations (exact, as the IEEE conversion). In the
+// mixed form's FP64 kernels that widen FP32 operands (the viscous right-hand
+// side, the FP64 += FP32 correction) this measured faster on GB300 than the
+// hardware conversion (right-hand side 4.27 -> 4.10 ms per two 256^3 steps);
+// the narrowing direction did not (an integer FP64 -> FP32 rounding made the
+// FP64 defect kernels 9% slower), so it stays the hardware conversion.
+// Zero takes the sign path; subnormal, inf and nan the plain conversion.
+// ---------------------------------------------------------------------------
+AFMIB_HD double f32_to_f64(float f) {
+    const unsigned u = fword(f);
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    if ((u & 0x7fffffffu) == 0u) return dfrom(sign);  // +-0
+    const unsigned ex = (u >> 23) & 0xffu;
+    if (ex == 0u || ex == 255u) return (double)f;  // subnormal, inf, nan
+    return dfrom(sign | ((unsigned long long)(ex + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29));
+}
+
+// TI -> TO, FP32 -> FP64 by f32_to_f64
+template <typename TO, typename TI>
+AFMIB_HD TO cvt(TI v) { return TO(v); }
+template <>
+AFMIB_HD double cvt<double, float>(float v) { return f32_to_f64(v); }
 
 struct df2 {
     float hi, lo;

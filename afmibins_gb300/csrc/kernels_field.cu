@@ -222,7 +222,7 @@ __global__ void k_helm_rhs(Dims d, int comp, int be, T* __restrict__ r, const T*
         bm = T(8. / 3. * s_minus * d.n * d.n * wv);
         bp = T(8. / 3. * s_plus * d.n * d.n * wv);
     }
-    const T src = T(hdt) * (T(inv_rho) * T(f[i]) - T(adv[i]));
+    const T src = T(hdt) * (T(inv_rho) * cvt<T, TF>(f[i]) - cvt<T, TA>(adv[i]));
     if (be) {
         r[i] = (uold[i] + T(-1) * bm) + src;
     } else {
@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_init_zero(long long N, const T
 template <typename TE>
 __global__ void k_add_correction(long long N, double* __restrict__ x, const TE* __restrict__ e) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
-        x[i] = x[i] + (double)e[i];
+        x[i] = x[i] + cvt<double, TE>(e[i]);
 }
 
 // ---------------------------------------------------------------------------

@@ -5,6 +5,7 @@
 #define __device__
 #define __forceinline__ inline
 #include <cmath>
+#include <cstring>
 using std::fmaf;
 #include "dfloat.cuh"
 
@@ -19,6 +20,41 @@ void afmib_test_split(double d, float* hi, float* lo) {
     const afmib::df2 r = afmib::df_split(d);
     *hi = r.hi;
     *lo = r.lo;
+}
+// count of inputs (out of n, from a small LCG over raw bit patterns plus the
+// edge cases) where the integer FP32 -> FP64 conversion differs from the C cast
+long long afmib_test_convert_mismatches(long long n, unsigned long long seed) {
+    long long bad = 0;
+    unsigned long long st = seed;
+    auto next = [&]() {
+        st = st * 6364136223846793005ull + 1442695040888963407ull;
+        return st;
+    };
+    auto same32 = [](float a, float b) { return std::memcmp(&a, &b, 4) == 0 || (a != a && b != b); };
+    auto same64 = [](double a, double b) { return std::memcmp(&a, &b, 8) == 0 || (a != a && b != b); };
+    auto check = [&](double v) {
+        const float f = (float)v;
+        if (!same64(afmib::f32_to_f64(f), (double)f)) ++bad;
+        float g;
+        const unsigned w = (unsigned)(v == v ? afmib::dbits(v) >> 16 : 0x7fc00001u);  // raw float bit patterns too
+        std::memcpy(&g, &w, 4);
+        if (!same64(afmib::f32_to_f64(g), (double)g)) ++bad;
+    };
+    (void)same32;
+    const double edges[] = {0.0, -0.0, 1.0, -1.0, 3.4028234663852886e38, 3.4028235677973366e38, 3.40282357e38,
+                            1.1754943508222875e-38, 1.1754942807573643e-38, 1.1754943e-38 * 0.5, 1e-300, -1e300,
+                            1.0 + 1.0 / (1 << 24), 1.0 + 3.0 / (1 << 24), 1.0 - 1.0 / (1 << 25), 0.1, -2.5e-10};
+    for (double v : edges) check(v);
+    for (long long i = 0; i < n; ++i) {
+        const unsigned long long r = next();
+        switch (i % 4) {
+            case 0: check(afmib::dfrom(r)); break;                              // any bit pattern
+            case 1: check(afmib::dfrom((r & ~(0x7ffull << 52)) | ((896ull + (r >> 56) % 260) << 52))); break;  // float range
+            case 2: check(afmib::dfrom((r & ~0x1FFFFFFFull) | 0x10000000ull)); break;  // exact ties
+            default: check(afmib::dfrom(r | 0x1FFFFFFFull)); break;            // carries
+        }
+    }
+    return bad;
 }
 void afmib_test_fixed(long long q, int E, float* hi, float* lo) {
     const afmib::df2 r = afmib::from_fixed(q, E);

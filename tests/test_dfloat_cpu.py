@@ -34,7 +34,16 @@ def lib(tmp_path_factory):
     L.afmib_test_lap_residual.restype = ctypes.c_float
     L.afmib_test_split.argtypes = [ctypes.c_double, fp, fp]
     L.afmib_test_fixed.argtypes = [ctypes.c_longlong, ctypes.c_int, fp, fp]
+    L.afmib_test_convert_mismatches.argtypes = [ctypes.c_longlong, ctypes.c_ulonglong]
+    L.afmib_test_convert_mismatches.restype = ctypes.c_longlong
     return L
+
+
+def test_integer_conversion_matches_ieee_cast(lib):
+    """f32_to_f64 (the integer-op widening used by the mixed form's FP64
+    kernels) agrees bit for bit with the C cast on zeros, subnormals, inf,
+    nan, normal values and raw bit patterns."""
+    assert lib.afmib_test_convert_mismatches(2_000_000, 12345) == 0
 
 
 def _arr(a, t):
