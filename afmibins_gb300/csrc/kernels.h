@@ -147,7 +147,10 @@ struct TailLevels {
     int* status;
 };
 template <typename T>
-void launch_vcycle_tail(const TailLevels<T>& a, cudaStream_t s);
+void launch_vcycle_tail(const TailLevels<T>& a, cudaStream_t s, int cluster = 1);
+// Largest thread-block cluster (16, 8 or 4 CTAs) the cluster form of the
+// V-cycle tail can be launched with on this device; 1: none.
+int vcycle_tail_cluster_max();
 template <typename T>
 void launch_rbgs_pipe(const Dims& d, const PipeCfg& c, const T* xin, T* xout, const T* b, int* err, cudaStream_t s);
 // Full-weighting restriction, src/mg/solver.h:153-181 (d = fine dims).

@@ -2,6 +2,8 @@
 // src/mg/laplacian.h): red-black Gauss–Seidel in place of the reference's
 // lexicographic CSR sweep, the reference's full-weighting restriction and
 // trilinear prolongation, and a one-block CG for the coarsest level.
+#include <cooperative_groups.h>
+
 #include "dfloat.cuh"
 #include "kernels.h"
 
@@ -17,7 +19,7 @@ inline dim3 grid3(const Dims& d) { return dim3((d.nx + BX - 1) / BX, (d.ny + BY 
 // wall (Neumann, src/mg/laplacian.h:75-82). A one-cell z extent (2D) folds
 // its two self-neighbours into the diagonal, src/mg/laplacian.h:62-73.
 template <typename T>
-__device__ __forceinline__ void lap_row(const Dims& d, const T* __restrict__ x, int xi, int yi, int zi, T& S, T& c) {
+__device__ __forceinline__ void lap_row(const Dims& d, const T* x, int xi, int yi, int zi, T& S, T& c) {
     if (d.nz == 1) {
         S = x[lin(d, xm1(d, xi), yi, zi)] + x[lin(d, xp1(d, xi), yi, zi)];
         c = T(4);
@@ -203,7 +205,7 @@ __global__ void k_rbgs_z(Dims d, int color, T omega, T* __restrict__ xv, const T
 // Neighbour sum and diagonal factor of lap_row with Ix2 indexing (same terms,
 // same order).
 template <typename T>
-__device__ __forceinline__ void lap_row2(const Dims& d, const Ix2& I, const T* __restrict__ x, int xi, int yi, int zi,
+__device__ __forceinline__ void lap_row2(const Dims& d, const Ix2& I, const T* x, int xi, int yi, int zi,
                                          T& S, T& c) {
     if (d.nz == 1) {
         S = x[I.at(I.xm(xi), yi, zi)] + x[I.at(I.xp(xi), yi, zi)];
@@ -565,11 +567,8 @@ __device__ __forceinline__ void prolong_cell(const Dims& d, T* fine, const T* co
 // restrict_cell / prolong_cell for 3D power-of-two levels with Ix2 indexing
 // (same taps, same weights, same summation order)
 template <typename T>
-__global__ void k_restrict2(Dims d, T* __restrict__ coarse, const T* __restrict__ fine) {
-    const Ix2 I(d);
-    const int cx = d.nx / 2, cy = d.ny / 2;
-    const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
-    if (xc >= cx || yc >= cy) return;
+__device__ __forceinline__ void restrict_cell2(const Dims& d, const Ix2& I, T* coarse, const T* fine, int xc, int yc,
+                                               int zc) {
     const int xcf = 2 * xc + 1, ycf = 2 * yc + 1, zcf = 2 * zc + 1;
     int xs[4], yo[4], zo[4];
 #pragma unroll
@@ -596,12 +595,18 @@ __global__ void k_restrict2(Dims d, T* __restrict__ coarse, const T* __restrict_
     coarse[xc | (yc << (I.lx - 1)) | (zc << (I.lxy - 2))] = acc;
 }
 
-template <typename T, bool ADD>
-__global__ void k_prolong2(Dims d, T* __restrict__ fine, const T* __restrict__ coarse) {
+template <typename T>
+__global__ void k_restrict2(Dims d, T* __restrict__ coarse, const T* __restrict__ fine) {
     const Ix2 I(d);
-    const int cx = d.nx / 2, cy = d.ny / 2, cz = d.nz / 2, lcx = I.lx - 1, lcxy = I.lxy - 2;
     const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
-    if (xc >= cx || yc >= cy) return;
+    if (xc >= d.nx / 2 || yc >= d.ny / 2) return;
+    restrict_cell2(d, I, coarse, fine, xc, yc, zc);
+}
+
+template <typename T, bool ADD>
+__device__ __forceinline__ void prolong_cell2(const Dims& d, const Ix2& I, T* fine, const T* coarse, int xc, int yc,
+                                              int zc) {
+    const int cx = d.nx / 2, cy = d.ny / 2, cz = d.nz / 2, lcx = I.lx - 1, lcxy = I.lxy - 2;
     auto C = [&](int a, int b, int c) { return coarse[a | (b << lcx) | (c << lcxy)]; };
     auto put = [&](int a, int b, int c, T val) {
         const int i = I.at(a, b, c);
@@ -639,6 +644,14 @@ __global__ void k_prolong2(Dims d, T* __restrict__ fine, const T* __restrict__ c
             put(xnf, yf, znf, a * fr + b * (fl + br) + e * bl);
         }
     }
+}
+
+template <typename T, bool ADD>
+__global__ void k_prolong2(Dims d, T* __restrict__ fine, const T* __restrict__ coarse) {
+    const Ix2 I(d);
+    const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
+    if (xc >= d.nx / 2 || yc >= d.ny / 2) return;
+    prolong_cell2<T, ADD>(d, I, fine, coarse, xc, yc, zc);
 }
 
 template <typename T, bool ADD>
@@ -740,26 +753,68 @@ __device__ __forceinline__ void tail_xyz(const Dims& d, int i, int& x, int& y, i
 }
 
 template <typename T>
-__device__ __forceinline__ void tail_sweep(const Dims& d, T* x, const T* b, int color) {
+__device__ __forceinline__ void tail_sweep(const Dims& d, T* x, const T* b, int color, int t0, int ts) {
     const int hx = d.nx / 2, total = hx * d.ny * d.nz;
-    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    for (int e = t0; e < total; e += ts) {
         const int row = e / hx, t = e - row * hx;
         const int z = row / d.ny, y = row - z * d.ny;
         const int xx = 2 * t + ((y + z + color) & 1);
         if (xx < d.nx) rbgs_cell(d, x, b, xx, y, z);
     }
-    __syncthreads();
+}
+
+// Power-of-two 3D levels take the shift-composed forms of the same per-cell
+// functions (lap_row2, restrict_cell2, prolong_cell2: same terms, same order)
+// and decode cell indices by shifts: the one-block tail is bound by the
+// integer work of its phases, not by their few thousand cells' bytes.
+__device__ __forceinline__ bool tail_p2(const Dims& d) {
+    auto p2 = [](int v) { return (v & (v - 1)) == 0; };
+    return d.nz > 1 && p2(d.nx) && p2(d.ny) && p2(d.nz);
+}
+
+template <typename T>
+__device__ __forceinline__ void tail_sweep2(const Dims& d, const Ix2& I, T* x, const T* b, int color, int t0, int ts) {
+    const int hx = d.nx >> 1, lhx = I.lx - 1, ly = I.lxy - I.lx, total = hx * d.ny * d.nz;
+    for (int e = t0; e < total; e += ts) {
+        const int t = e & (hx - 1), row = e >> lhx;
+        const int y = row & I.my, z = row >> ly;
+        const int xx = 2 * t + ((y + z + color) & 1);
+        T S, c;
+        lap_row2(d, I, x, xx, y, z, S, c);
+        const int i = I.at(xx, y, z);
+        const T inv = T(1) / (T(d.n) * T(d.n));
+        const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
+        x[i] = (S - b[i] * inv) * rc;
+    }
 }
 
 // With `staged`, the levels' x, b, r (and the FP64 coarsest-level vectors)
 // live in shared memory for the whole V-cycle: the top level's x and b are
 // read in, the top level's x is written back (the only result the level
 // above uses). Without it the phases work on the global arrays.
-template <typename T>
+// CL: the same phases spread over a thread-block cluster (every CTA takes a
+// share of each phase's cells; cluster barriers, whose arrive/wait release
+// and acquire the phase's global writes, separate the phases). The coarsest
+// solve runs in the cluster's first CTA, the same one-block CG, so the result
+// is the one-block tail's, bit for bit; the levels stay in global memory (L2).
+template <typename T, bool CL>
 __global__ void __launch_bounds__(kRedBlock) k_vcycle_tail(TailLevels<T> g, int staged) {
     extern __shared__ __align__(16) unsigned char tsm[];
     TailLevels<T> a = g;
-    if (staged) {
+    int t0 = threadIdx.x, ts = blockDim.x;
+    bool lead = true;
+    if constexpr (CL) {
+        namespace cg = cooperative_groups;
+        const cg::cluster_group cl = cg::this_cluster();
+        t0 = (int)cl.block_rank() * blockDim.x + threadIdx.x;
+        ts = (int)cl.num_blocks() * blockDim.x;
+        lead = cl.block_rank() == 0;
+    }
+    auto sync = [&]() {
+        if constexpr (CL) cooperative_groups::this_cluster().sync();
+        else __syncthreads();
+    };
+    if (!CL && staged) {
         // layout: per level x, b, r (T), then cx64, cb64, cr64, cw_p, cw_q (double)
         size_t off = 0;
         for (int l = 0; l < a.nlev; ++l) {
@@ -786,28 +841,51 @@ __global__ void __launch_bounds__(kRedBlock) k_vcycle_tail(TailLevels<T> g, int 
     }
     for (int l = 0; l + 1 < a.nlev; ++l) {
         const Dims& d = a.d[l];
+        const bool p2 = tail_p2(d);
+        const Ix2 I(d);
         for (int j = 0; j < a.nu1; ++j) {
-            tail_sweep(d, a.x[l], a.b[l], 0);
-            tail_sweep(d, a.x[l], a.b[l], 1);
+            for (int color = 0; color < 2; ++color) {
+                if (p2) tail_sweep2(d, I, a.x[l], a.b[l], color, t0, ts);
+                else tail_sweep(d, a.x[l], a.b[l], color, t0, ts);
+                sync();
+            }
         }
         const int n = (int)d.ncell();
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            int xx, yy, zz;
-            tail_xyz(d, i, xx, yy, zz);
-            residual_cell(d, a.r[l], a.x[l], a.b[l], xx, yy, zz);
+        if (p2) {
+            const T off = T(d.n) * T(d.n);
+            for (int i = t0; i < n; i += ts) {
+                const int xx = i & I.mx, yy = (i >> I.lx) & I.my, zz = i >> I.lxy;
+                T S, c;
+                lap_row2(d, I, a.x[l], xx, yy, zz, S, c);
+                a.r[l][i] = a.b[l][i] - off * (S - c * a.x[l][i]);
+            }
+        } else {
+            for (int i = t0; i < n; i += ts) {
+                int xx, yy, zz;
+                tail_xyz(d, i, xx, yy, zz);
+                residual_cell(d, a.r[l], a.x[l], a.b[l], xx, yy, zz);
+            }
         }
-        __syncthreads();
+        sync();
         const Dims& c = a.d[l + 1];
         const int nc = (int)c.ncell();
-        for (int i = threadIdx.x; i < nc; i += blockDim.x) {
-            int xx, yy, zz;
-            tail_xyz(c, i, xx, yy, zz);
-            restrict_cell(d, a.b[l + 1], a.r[l], xx, yy, zz);
-            a.x[l + 1][i] = T(0);
+        if (p2) {
+            const int lcx = I.lx - 1, lcxy = I.lxy - 2, mcx = (d.nx >> 1) - 1, mcy = (d.ny >> 1) - 1;
+            for (int i = t0; i < nc; i += ts) {
+                restrict_cell2(d, I, a.b[l + 1], a.r[l], i & mcx, (i >> lcx) & mcy, i >> lcxy);
+                a.x[l + 1][i] = T(0);
+            }
+        } else {
+            for (int i = t0; i < nc; i += ts) {
+                int xx, yy, zz;
+                tail_xyz(c, i, xx, yy, zz);
+                restrict_cell(d, a.b[l + 1], a.r[l], xx, yy, zz);
+                a.x[l + 1][i] = T(0);
+            }
         }
-        __syncthreads();
+        sync();
     }
-    {
+    if (lead) {  // block-uniform: the whole first CTA (or the one block)
         const int l = a.nlev - 1;
         const Dims& d = a.d[l];
         const long long n = d.ncell();
@@ -820,24 +898,35 @@ __global__ void __launch_bounds__(kRedBlock) k_vcycle_tail(TailLevels<T> g, int 
             __syncthreads();
             for (long long i = threadIdx.x; i < n; i += blockDim.x) a.x[l][i] = (T)a.cx64[i];
         }
-        __syncthreads();
     }
+    sync();
     for (int l = a.nlev - 2; l >= 0; --l) {
         const Dims& d = a.d[l];
         const Dims& c = a.d[l + 1];
+        const bool p2 = tail_p2(d);
+        const Ix2 I(d);
         const int nc = (int)c.ncell();
-        for (int i = threadIdx.x; i < nc; i += blockDim.x) {
-            int xx, yy, zz;
-            tail_xyz(c, i, xx, yy, zz);
-            prolong_cell<T, true>(d, a.x[l], a.x[l + 1], xx, yy, zz);
+        if (p2) {
+            const int lcx = I.lx - 1, lcxy = I.lxy - 2, mcx = (d.nx >> 1) - 1, mcy = (d.ny >> 1) - 1;
+            for (int i = t0; i < nc; i += ts)
+                prolong_cell2<T, true>(d, I, a.x[l], a.x[l + 1], i & mcx, (i >> lcx) & mcy, i >> lcxy);
+        } else {
+            for (int i = t0; i < nc; i += ts) {
+                int xx, yy, zz;
+                tail_xyz(c, i, xx, yy, zz);
+                prolong_cell<T, true>(d, a.x[l], a.x[l + 1], xx, yy, zz);
+            }
         }
-        __syncthreads();
+        sync();
         for (int j = 0; j < a.nu2; ++j) {
-            tail_sweep(d, a.x[l], a.b[l], 0);
-            tail_sweep(d, a.x[l], a.b[l], 1);
+            for (int color = 0; color < 2; ++color) {
+                if (p2) tail_sweep2(d, I, a.x[l], a.b[l], color, t0, ts);
+                else tail_sweep(d, a.x[l], a.b[l], color, t0, ts);
+                sync();
+            }
         }
     }
-    if (staged) {
+    if (!CL && staged) {
         const long long n0 = a.d[0].ncell();
         for (long long i = threadIdx.x; i < n0; i += blockDim.x) g.x[0][i] = a.x[0][i];
     }
@@ -985,7 +1074,29 @@ template void launch_lap_defect<float>(const Dims&, float*, const double*, const
                                        cudaStream_t);
 
 template <typename T>
-void launch_vcycle_tail(const TailLevels<T>& a, cudaStream_t s) {
+void launch_vcycle_tail(const TailLevels<T>& a, cudaStream_t s, int cluster) {
+    if (cluster > 1) {
+        if (cluster > 8) {
+            static bool np = false;
+            if (!np)
+                np = cudaFuncSetAttribute(k_vcycle_tail<T, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                     cudaSuccess;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cluster);
+        cfg.blockDim = dim3(kRedBlock);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cluster;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k_vcycle_tail<T, true>, a, 0);  // errors reach the caller's cudaGetLastError
+        return;
+    }
     // shared-memory staging when the levels fit
     size_t bytes = 0;
     for (int l = 0; l < a.nlev; ++l) {
@@ -995,10 +1106,35 @@ void launch_vcycle_tail(const TailLevels<T>& a, cudaStream_t s) {
     bytes += (size_t)5 * a.d[a.nlev - 1].ncell() * sizeof(double);
     constexpr size_t kMax = 160 * 1024;
     static bool attr = false;
-    if (!attr) attr = cudaFuncSetAttribute(k_vcycle_tail<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMax) ==
-                      cudaSuccess;
-    if (attr && bytes <= kMax) k_vcycle_tail<T><<<1, kRedBlock, bytes, s>>>(a, 1);
-    else k_vcycle_tail<T><<<1, kRedBlock, 0, s>>>(a, 0);
+    if (!attr)
+        attr = cudaFuncSetAttribute(k_vcycle_tail<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMax) ==
+               cudaSuccess;
+    if (attr && bytes <= kMax) k_vcycle_tail<T, false><<<1, kRedBlock, bytes, s>>>(a, 1);
+    else k_vcycle_tail<T, false><<<1, kRedBlock, 0, s>>>(a, 0);
+}
+
+int vcycle_tail_cluster_max() {
+    for (int cs : {16, 8, 4}) {
+        if (cs > 8 && cudaFuncSetAttribute(k_vcycle_tail<float, true>, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                                           1) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cs);
+        cfg.blockDim = dim3(kRedBlock);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, k_vcycle_tail<float, true>, &cfg) == cudaSuccess && n > 0) return cs;
+        cudaGetLastError();
+    }
+    return 1;
 }
 template <typename T>
 void launch_coarse_solve(const Dims& d, T* x, T* b, T* r, T* p, T* q, double tol, int maxit, int* status, cudaStream_t s) {
@@ -1015,7 +1151,7 @@ void launch_coarse_solve(const Dims& d, T* x, T* b, T* r, T* p, T* q, double tol
     template void launch_prolong_add<T>(const Dims&, T*, const T*, cudaStream_t);                        \
     template void launch_prolong_assign<T>(const Dims&, T*, const T*, cudaStream_t);                     \
     template void launch_coarse_solve<T>(const Dims&, T*, T*, T*, T*, T*, double, int, int*, cudaStream_t);    \
-    template void launch_vcycle_tail<T>(const TailLevels<T>&, cudaStream_t);
+    template void launch_vcycle_tail<T>(const TailLevels<T>&, cudaStream_t, int);
 
 AFMIB_MG_INST(double)
 AFMIB_MG_INST(float)

@@ -86,8 +86,11 @@ struct afmib_solver {
     // FP64 kernels (opt-in, AFMIB_BFP=1: measured no faster on GB300, the
     // integer form being instruction-bound at about the FP64 kernels' time)
     bool bfp_defects = false;
-    // first multigrid level handled by the one-block V-cycle tail (-1: none; AFMIB_MG_TAIL=0)
+    // first multigrid level handled by the V-cycle tail (-1: none;
+    // AFMIB_MG_TAIL=0), and the thread-block cluster it runs on (1: one
+    // block)
     int tail_level = -1;
+    int tail_cluster = 1;
     // mixed form: inner Helmholtz solves by fixed Jacobi sweeps where the
     // operator's diagonal dominance bounds them (AFMIB_INNER_SOLVER=cg: CG)
     bool jacobi_inner = true;
@@ -420,7 +423,7 @@ int coarse(afmib_solver* s, MGLevelT<float>& L) {
     return AFMIB_OK;
 }
 
-// the coarse V-cycle below level l in one block (see k_vcycle_tail)
+// the coarse V-cycle below level l in one block or one cluster (k_vcycle_tail)
 template <typename T>
 int vcycle_tail(afmib_solver* s, size_t l) {
     auto& lv = levels<T>(s);
@@ -443,7 +446,7 @@ int vcycle_tail(afmib_solver* s, size_t l) {
     a.cw_q = s->cw_q;
     a.status = s->dflag + 1;
     ProfScope ps(s, P_TAIL, 0.0);
-    launch_vcycle_tail<T>(a, s->st);
+    launch_vcycle_tail<T>(a, s->st, s->tail_cluster);
     CKL();
     return AFMIB_OK;
 }
@@ -1552,14 +1555,26 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
         TRY(dalloc(s, &s->cb64, nc));
         TRY(dalloc(s, &s->cr64, nc));
     }
-    // one-block V-cycle tail from the first level of at most 16^3 cells, when
-    // it leaves at least one smoothed level above the coarsest
+    // V-cycle tail, when it leaves at least one smoothed level above the
+    // coarsest: in one block from the first level of at most 16^3 cells, or
+    // (AFMIB_MG_TAIL_CLUSTER=n) on a cluster of n CTAs from the first level of
+    // at most 32^3
     {
         bool tail = true;
         if (const char* e = std::getenv("AFMIB_MG_TAIL")) tail = std::string(e) != "0";
+        // the cluster form is opt-in: at 256^3 it measured 114 us per V-cycle
+        // for the levels 32^3..1 on 16 CTAs against 80 us for 16^3..1 in one
+        // block plus the 32^3 level launches, 36.2 against 36.45 IB steps/s
+        int cs = 1;
+        if (const char* e = std::getenv("AFMIB_MG_TAIL_CLUSTER")) {
+            cs = std::min(vcycle_tail_cluster_max(), std::max(1, std::atoi(e)));
+            cudaGetLastError();
+        }
+        const long long cells = cs > 1 ? 32768 : 4096;
         for (size_t l = 0; tail && l + 1 < s->lv.size(); ++l)
-            if (s->lv[l].d.ncell() <= 4096 && s->lv.size() - l <= (size_t)kMaxTailLevels) {
+            if (s->lv[l].d.ncell() <= cells && s->lv.size() - l <= (size_t)kMaxTailLevels) {
                 s->tail_level = (int)l;
+                s->tail_cluster = cs;
                 break;
             }
     }

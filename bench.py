@@ -261,7 +261,8 @@ def pressure_err(p, pref, n, mu, dt):
 
 def run_form(capi, torch, args, prec, state, dev, stream, proj_start=0):
     """Create a solver of the given precision on the initial state, run the
-    warm-up and the timed steps; return (solver, ms, launches, clocks, wall)."""
+    warm-up and the timed steps; return (solver, ms, launches, clocks, timing)
+    with timing = {"wall_s", "host_ms_per_step"}."""
     X, nstart, nidx, u, v, w = state
     sv = capi.Solver(args.n, mu=args.mu, rho=1.0, dt=args.dt, tol=args.tol, k_spring=0.5, precision=prec,
                      proj_start=proj_start, inner_tol=args.inner_tol, stream=stream.cuda_stream)
@@ -281,13 +282,17 @@ def run_form(capi, torch, args, prec, state, dev, stream, proj_start=0):
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         t0 = time.perf_counter()
+        marks = []
         for _ in range(args.steps):
             sv.ib_step(1)
+            marks.append(time.perf_counter())
         e1.record(stream)
         stream.synchronize()
         wall = time.perf_counter() - t0
     torch.cuda.synchronize()
-    return sv, e0.elapsed_time(e1), sv.stats()["kernel_launches"] - l0, clk.summary(), wall
+    steps_ms = [round(1000.0 * (b - a), 2) for a, b in zip([t0] + marks[:-1], marks)]
+    return sv, e0.elapsed_time(e1), sv.stats()["kernel_launches"] - l0, clk.summary(), {"wall_s": wall,
+                                                                                       "host_ms_per_step": steps_ms}
 
 
 def run_mg_case(args, torch, local):
@@ -540,7 +545,7 @@ def main():
 
     # ---- headline form: timed region with the state resident in HBM
     barrier()
-    sv, ms, launches, clocks, wall = run_form(capi, torch, args, headline, state, dev, stream)
+    sv, ms, launches, clocks, timing = run_form(capi, torch, args, headline, state, dev, stream)
     barrier()
     ms_max = max_over_ranks(ms)
     value = world * args.steps / (ms_max / 1000.0)
@@ -626,7 +631,8 @@ def main():
             "solver": {"cg_iters_per_step": st["cg_iters"] / max(1, st["ib_steps"]),
                        "mg_cycles_per_step": st["mg_cycles"] / max(1, st["ib_steps"]),
                        "outer_iters_per_step": st["outer_iters"] / max(1, st["ib_steps"]),
-                       "spread_tiles": st["spread_tiles"], "wall_s": wall},
+                       "spread_tiles": st["spread_tiles"], "wall_s": timing["wall_s"],
+                       "host_ms_per_step": timing["host_ms_per_step"]},
             "kernels": kernels,
         }
         print(json.dumps(line), flush=True)

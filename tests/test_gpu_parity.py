@@ -418,17 +418,24 @@ def test_block_arithmetic_defects_match_fp64_defects(monkeypatch, bc):
 @pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
 @pytest.mark.parametrize("n", [16, 32, 64])
 def test_multigrid_tail_equals_level_launches(monkeypatch, bc, precision, n):
-    """The one-block V-cycle below 16^3 runs the per-cell functions of the
+    """The V-cycle tail (in one block from 16^3, or on a thread-block cluster
+    from 32^3 with AFMIB_MG_TAIL_CLUSTER=16) runs the per-cell functions of the
     level kernels and the same coarsest-level CG: multigrid solves agree bit
-    for bit with the launch-by-launch V-cycle."""
+    for bit with the launch-by-launch V-cycle, and repeat bit for bit."""
     b = np.random.default_rng(23).standard_normal(n ** 3)
     out = {}
-    for mode in ("0", "1"):
-        monkeypatch.setenv("AFMIB_MG_TAIL", mode)
+    for mode, tail, cluster in (("levels", "0", None), ("cluster", "1", "16"), ("cluster2", "1", "16"),
+                                ("block", "1", None)):
+        monkeypatch.setenv("AFMIB_MG_TAIL", tail)
+        if cluster:
+            monkeypatch.setenv("AFMIB_MG_TAIL_CLUSTER", cluster)
+        else:
+            monkeypatch.delenv("AFMIB_MG_TAIL_CLUSTER", raising=False)
         with capi.Solver(n, bc=bc, precision=precision, tol=1e-10) as sv:
             out[mode] = sv.mg_solve(b)
-    assert out["0"][1] == out["1"][1]
-    assert np.array_equal(out["0"][0], out["1"][0])
+    for mode in ("cluster", "cluster2", "block"):
+        assert out[mode][1] == out["levels"][1]
+        assert np.array_equal(out[mode][0], out["levels"][0])
 
 
 @pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
