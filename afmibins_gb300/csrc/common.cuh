@@ -65,6 +65,16 @@ struct Ix2 {
     __device__ __forceinline__ int zm(int z) const { return (z - 1) & mz; }
     __device__ __forceinline__ int zp(int z) const { return (z + 1) & mz; }
 };
+// Block coordinates, walked from the grid's far end when rev. Blocks are
+// dispatched roughly in index order, so a pass over a field larger than L2
+// that runs opposite to the pass before it starts on the rows that pass
+// left in L2 (results are unchanged: the kernels that take it are pointwise
+// or update one red-black colour).
+__device__ __forceinline__ uint3 block_at(int rev) {
+    return rev ? make_uint3(gridDim.x - 1 - blockIdx.x, gridDim.y - 1 - blockIdx.y, gridDim.z - 1 - blockIdx.z)
+               : blockIdx;
+}
+
 // Power-of-two kernels apply; AFMIB_IX2=0 keeps the general kernels (read at
 // every launch, so a test can compare both in one process).
 inline bool ix2_ok(const Dims& d) {

@@ -72,7 +72,8 @@ template <typename T>
 void launch_cg_update(long long n, T* x, T* r, const T* p, const T* q, RedScratch sc, double* cgs, cudaStream_t s);
 // one Jacobi sweep x' = x + (b - H x) / diag(H) (x == nullptr: from zero)
 template <typename T>
-void launch_helm_jacobi(const Dims& d, int comp, double scale, const T* x, T* xo, const T* b, cudaStream_t s);
+void launch_helm_jacobi(const Dims& d, int comp, double scale, const T* x, T* xo, const T* b, cudaStream_t s,
+                        int rev = 0);
 // p' = beta p + r formed on the fly (out of place into pn), q = H p', p'.q and alpha
 template <typename T>
 void launch_cg_dir_apply(const Dims& d, int comp, double scale, const T* p, const T* r, T* pn, T* q, RedScratch sc,
@@ -103,7 +104,8 @@ template <typename T>
 void launch_lap_apply(const Dims& d, T* y, const T* x, cudaStream_t s);
 // r = b - L x, optionally out[0] = r.r
 template <typename T>
-void launch_residual(const Dims& d, T* r, const T* x, const T* b, RedScratch* sc, double* out, cudaStream_t s);
+void launch_residual(const Dims& d, T* r, const T* x, const T* b, RedScratch* sc, double* out, cudaStream_t s,
+                     int rev = 0);
 // Mixed form: r = b - L x evaluated in FP64 (x, b FP64), stored as TD; out[0] = r.r
 template <typename TD>
 void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, RedScratch sc, double* out, cudaStream_t s);
@@ -116,8 +118,10 @@ void launch_helm_defect_bfp(const Dims& d, int comp, double scale, const double*
                             RedScratch sc, double* out, cudaStream_t s);
 // One red (color 0) or black (color 1) Gauss-Seidel half sweep; omega:
 // over-relaxation x + omega (gs - x) on levels with nx >= 64 (1 below).
+// rev (here and in the residual, transfer and Jacobi launchers): blocks in
+// reverse order (block_at, common.cuh) on the batched power-of-two kernels.
 template <typename T>
-void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s, double omega = 1.0);
+void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s, double omega = 1.0, int rev = 0);
 // One full red+black sweep per launch, out of place (xin -> xout), z-marching
 // blocks fed by bulk asynchronous row copies; equals the two per-colour
 // launches cell for cell. FY == 0: level not eligible (small, 2D, or rows not
@@ -155,10 +159,10 @@ template <typename T>
 void launch_rbgs_pipe(const Dims& d, const PipeCfg& c, const T* xin, T* xout, const T* b, int* err, cudaStream_t s);
 // Full-weighting restriction, src/mg/solver.h:153-181 (d = fine dims).
 template <typename T>
-void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s);
+void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s, int rev = 0);
 // fine += P coarse (trilinear), src/mg/solver.h:71-151 and :211-212.
 template <typename T>
-void launch_prolong_add(const Dims& d, T* fine, const T* coarse, cudaStream_t s);
+void launch_prolong_add(const Dims& d, T* fine, const T* coarse, cudaStream_t s, int rev = 0);
 // Prolongation that assigns (for the op-level API).
 template <typename T>
 void launch_prolong_assign(const Dims& d, T* fine, const T* coarse, cudaStream_t s);

@@ -593,9 +593,10 @@ void launch_cg_apply(const Dims& d, int comp, double scale, const T* p, T* q, Re
 }
 template <typename T, int ZU>
 __global__ void k_helm_jacobi2(Dims d, int comp, T s, const T* __restrict__ xv, T* __restrict__ xo,
-                               const T* __restrict__ b) {
+                               const T* __restrict__ b, int rev) {
     const Ix2 I(d);
-    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z0 = blockIdx.z * ZU;
+    const uint3 B = block_at(rev);
+    const int x = B.x * BX + threadIdx.x, y = B.y * BY + threadIdx.y, z0 = B.z * ZU;
     if (x >= d.nx || y >= d.ny) return;
     const T off = s * T(d.n) * T(d.n);
     const T rdiag = T(1) / helm_diag(d, comp, off, y);
@@ -610,18 +611,20 @@ __global__ void k_helm_jacobi2(Dims d, int comp, T s, const T* __restrict__ xv, 
 }
 
 template <typename T>
-void launch_helm_jacobi(const Dims& d, int comp, double scale, const T* x, T* xo, const T* b, cudaStream_t s) {
+void launch_helm_jacobi(const Dims& d, int comp, double scale, const T* x, T* xo, const T* b, cudaStream_t s,
+                        int rev) {
     const dim3 blk(BX, BY);
     if (d.nz % 8 == 0 && ix2_ok(d))
         k_helm_jacobi2<T, 8><<<dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / 8), blk, 0, s>>>(d, comp, T(scale),
-                                                                                                   x, xo, b);
+                                                                                                   x, xo, b, rev);
     else if (d.nz % 8 == 0)
         k_helm_jacobi<T, 8><<<dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / 8), blk, 0, s>>>(d, comp, T(scale), x,
                                                                                                   xo, b);
     else
         k_helm_jacobi<T, 1><<<grid3(d), blk, 0, s>>>(d, comp, T(scale), x, xo, b);
 }
-template void launch_helm_jacobi<float>(const Dims&, int, double, const float*, float*, const float*, cudaStream_t);
+template void launch_helm_jacobi<float>(const Dims&, int, double, const float*, float*, const float*, cudaStream_t,
+                                        int);
 
 template <typename T>
 void launch_cg_dir_apply(const Dims& d, int comp, double scale, const T* p, const T* r, T* pn, T* q, RedScratch sc,

@@ -223,9 +223,10 @@ __device__ __forceinline__ void lap_row2(const Dims& d, const Ix2& I, const T* x
 }
 
 template <typename T, int ZU>
-__global__ void k_rbgs_z2(Dims d, int color, T omega, T* __restrict__ xv, const T* __restrict__ b) {
+__global__ void k_rbgs_z2(Dims d, int color, T omega, T* __restrict__ xv, const T* __restrict__ b, int rev) {
     const Ix2 I(d);
-    const int y = blockIdx.y * BY + threadIdx.y, t = blockIdx.x * BX + threadIdx.x, z0 = blockIdx.z * ZU;
+    const uint3 B = block_at(rev);
+    const int y = B.y * BY + threadIdx.y, t = B.x * BX + threadIdx.x, z0 = B.z * ZU;
     if (y >= d.ny || 2 * t >= d.nx) return;
     T val[ZU];
     int at[ZU];
@@ -246,9 +247,10 @@ __global__ void k_rbgs_z2(Dims d, int color, T omega, T* __restrict__ xv, const 
 }
 
 template <typename T, int ZU>
-__global__ void k_residual_z2(Dims d, T* __restrict__ r, const T* __restrict__ xv, const T* __restrict__ b) {
+__global__ void k_residual_z2(Dims d, T* __restrict__ r, const T* __restrict__ xv, const T* __restrict__ b, int rev) {
     const Ix2 I(d);
-    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y, z0 = blockIdx.z * ZU;
+    const uint3 B = block_at(rev);
+    const int x = B.x * BX + threadIdx.x, y = B.y * BY + threadIdx.y, z0 = B.z * ZU;
     if (x >= d.nx || y >= d.ny) return;
     const T off = T(d.n) * T(d.n);
     T val[ZU];
@@ -596,9 +598,10 @@ __device__ __forceinline__ void restrict_cell2(const Dims& d, const Ix2& I, T* c
 }
 
 template <typename T>
-__global__ void k_restrict2(Dims d, T* __restrict__ coarse, const T* __restrict__ fine) {
+__global__ void k_restrict2(Dims d, T* __restrict__ coarse, const T* __restrict__ fine, int rev) {
     const Ix2 I(d);
-    const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
+    const uint3 B = block_at(rev);
+    const int xc = B.x * BX + threadIdx.x, yc = B.y * BY + threadIdx.y, zc = B.z;
     if (xc >= d.nx / 2 || yc >= d.ny / 2) return;
     restrict_cell2(d, I, coarse, fine, xc, yc, zc);
 }
@@ -647,9 +650,10 @@ __device__ __forceinline__ void prolong_cell2(const Dims& d, const Ix2& I, T* fi
 }
 
 template <typename T, bool ADD>
-__global__ void k_prolong2(Dims d, T* __restrict__ fine, const T* __restrict__ coarse) {
+__global__ void k_prolong2(Dims d, T* __restrict__ fine, const T* __restrict__ coarse, int rev) {
     const Ix2 I(d);
-    const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
+    const uint3 B = block_at(rev);
+    const int xc = B.x * BX + threadIdx.x, yc = B.y * BY + threadIdx.y, zc = B.z;
     if (xc >= d.nx / 2 || yc >= d.ny / 2) return;
     prolong_cell2<T, ADD>(d, I, fine, coarse, xc, yc, zc);
 }
@@ -934,27 +938,40 @@ __global__ void __launch_bounds__(kRedBlock) k_vcycle_tail(TailLevels<T> g, int 
 
 }  // namespace
 
+// smallest level (x extent) on which the smoother and residual take the
+// batched z-column kernels (AFMIB_BATCH_MIN_NX; one cell per thread below:
+// at 64^3 the batched grid is 64 blocks, and the one-cell kernels measured
+// 5% faster over the coarse levels of a 256^3 V-cycle)
+int batch_min_nx() {
+    static const int v = [] {
+        const char* e = std::getenv("AFMIB_BATCH_MIN_NX");
+        return e ? std::atoi(e) : 128;
+    }();
+    return v;
+}
+
 template <typename T>
 void launch_lap_apply(const Dims& d, T* y, const T* x, cudaStream_t s) {
     k_lap<T><<<grid3(d), dim3(BX, BY), 0, s>>>(d, y, x);
 }
 template <typename T>
-void launch_residual(const Dims& d, T* r, const T* x, const T* b, RedScratch* sc, double* out, cudaStream_t s) {
+void launch_residual(const Dims& d, T* r, const T* x, const T* b, RedScratch* sc, double* out, cudaStream_t s, int rev) {
     if (sc && out)
         k_residual_norm<T><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, r, x, b, *sc, out);
-    else if (d.nz % kZU == 0 && d.nx >= 64 && ix2_ok(d))
-        k_residual_z2<T, kZU><<<dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / kZU), dim3(BX, BY), 0, s>>>(d, r, x, b);
-    else if (d.nz % kZU == 0 && d.nx >= 64)
+    else if (d.nz % kZU == 0 && d.nx >= batch_min_nx() && ix2_ok(d))
+        k_residual_z2<T, kZU><<<dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / kZU), dim3(BX, BY), 0, s>>>(d, r, x, b,
+                                                                                                          rev);
+    else if (d.nz % kZU == 0 && d.nx >= batch_min_nx())
         k_residual_z<T, kZU><<<dim3((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / kZU), dim3(BX, BY), 0, s>>>(d, r, x, b);
     else
         k_residual<T><<<grid3(d), dim3(BX, BY), 0, s>>>(d, r, x, b);
 }
 template <typename T>
-void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s, double omega) {
+void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s, double omega, int rev) {
     if (d.nx < kOmegaMinNx) omega = 1.0;
-    if (d.nz % kZU == 0 && d.nx >= 64) {
+    if (d.nz % kZU == 0 && d.nx >= batch_min_nx()) {
         dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / kZU);
-        if (ix2_ok(d)) k_rbgs_z2<T, kZU><<<g, dim3(BX, BY), 0, s>>>(d, color, T(omega), x, b);
+        if (ix2_ok(d)) k_rbgs_z2<T, kZU><<<g, dim3(BX, BY), 0, s>>>(d, color, T(omega), x, b, rev);
         else k_rbgs_z<T, kZU><<<g, dim3(BX, BY), 0, s>>>(d, color, T(omega), x, b);
         return;
     }
@@ -1042,15 +1059,16 @@ void launch_rbgs_pipe(const Dims& d, const PipeCfg& c, const T* xin, T* xout, co
 }
 
 template <typename T>
-void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s) {
+void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s, int rev) {
     dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz == 1 ? 1 : d.nz / 2);
-    if (d.nz > 1 && d.nx >= 2 && d.ny >= 2 && ix2_ok(d)) k_restrict2<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine);
+    if (d.nz > 1 && d.nx >= 2 && d.ny >= 2 && ix2_ok(d)) k_restrict2<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine, rev);
     else k_restrict<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine);
 }
 template <typename T>
-void launch_prolong_add(const Dims& d, T* fine, const T* coarse, cudaStream_t s) {
+void launch_prolong_add(const Dims& d, T* fine, const T* coarse, cudaStream_t s, int rev) {
     dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz == 1 ? 1 : d.nz / 2);
-    if (d.nz > 1 && d.nx >= 2 && d.ny >= 2 && ix2_ok(d)) k_prolong2<T, true><<<g, dim3(BX, BY), 0, s>>>(d, fine, coarse);
+    if (d.nz > 1 && d.nx >= 2 && d.ny >= 2 && ix2_ok(d))
+        k_prolong2<T, true><<<g, dim3(BX, BY), 0, s>>>(d, fine, coarse, rev);
     else k_prolong<T, true><<<g, dim3(BX, BY), 0, s>>>(d, fine, coarse);
 }
 template <typename T>
@@ -1143,12 +1161,12 @@ void launch_coarse_solve(const Dims& d, T* x, T* b, T* r, T* p, T* q, double tol
 
 #define AFMIB_MG_INST(T)                                                                                 \
     template void launch_lap_apply<T>(const Dims&, T*, const T*, cudaStream_t);                          \
-    template void launch_residual<T>(const Dims&, T*, const T*, const T*, RedScratch*, double*, cudaStream_t); \
-    template void launch_rbgs<T>(const Dims&, int, T*, const T*, cudaStream_t, double);                        \
+    template void launch_residual<T>(const Dims&, T*, const T*, const T*, RedScratch*, double*, cudaStream_t, int); \
+    template void launch_rbgs<T>(const Dims&, int, T*, const T*, cudaStream_t, double, int);                        \
     template PipeCfg rbgs_pipe_cfg<T>(const Dims&);                                                      \
     template void launch_rbgs_pipe<T>(const Dims&, const PipeCfg&, const T*, T*, const T*, int*, cudaStream_t); \
-    template void launch_restrict<T>(const Dims&, T*, const T*, cudaStream_t);                           \
-    template void launch_prolong_add<T>(const Dims&, T*, const T*, cudaStream_t);                        \
+    template void launch_restrict<T>(const Dims&, T*, const T*, cudaStream_t, int);                         \
+    template void launch_prolong_add<T>(const Dims&, T*, const T*, cudaStream_t, int);                      \
     template void launch_prolong_assign<T>(const Dims&, T*, const T*, cudaStream_t);                     \
     template void launch_coarse_solve<T>(const Dims&, T*, T*, T*, T*, T*, double, int, int*, cudaStream_t);    \
     template void launch_vcycle_tail<T>(const TailLevels<T>&, cudaStream_t, int);

@@ -97,6 +97,10 @@ struct afmib_solver {
     // V-cycle blocks captured once into CUDA graphs and replayed (no host
     // interaction inside a V-cycle); not used while per-kernel profiling is on
     bool use_graphs = true;
+    // passes over fields larger than L2 alternate their block order
+    // (AFMIB_ALTERNATE=0: always index order); pass_rev is the last direction
+    bool alternate = true;
+    int pass_rev = 0;
     cudaGraphExec_t vg64 = nullptr, vg32[kMaxInnerCycles + 1] = {};
     long long vg64_launches = 0, vg32_launches[kMaxInnerCycles + 1] = {};
     bool spread64 = false, interp64 = false;  // mixed form: IB transfers in FP64
@@ -373,6 +377,17 @@ std::vector<MGLevelT<double>>& levels<double>(afmib_solver* s) { return s->lv; }
 template <>
 std::vector<MGLevelT<float>>& levels<float>(afmib_solver* s) { return s->lv32; }
 
+// Block order of the next pass over a field of level d (block_at): passes
+// over arrays of more than 32 MB (the 126 MB L2 holds about two of them)
+// alternate, so that each starts on the rows the previous one left in L2.
+// Measured at 256^3: fine-level red-black sweeps 7.11 -> 6.04 ms per two IB
+// steps with the black sweeps reversed.
+int pass_dir(afmib_solver* s, const Dims& d, size_t elem) {
+    if (!s->alternate || (double)d.ncell() * (double)elem < 32.0 * (1 << 20)) return 0;
+    s->pass_rev ^= 1;
+    return s->pass_rev;
+}
+
 template <typename T>
 int smooth(afmib_solver* s, MGLevelT<T>& L, int sweeps) {
     const double Ns = (double)L.d.ncell() * sizeof(T);
@@ -395,11 +410,11 @@ int smooth(afmib_solver* s, MGLevelT<T>& L, int sweeps) {
     for (; j < sweeps; ++j) {
         {
             ProfScope ps(s, id, 1.5 * Ns);
-            launch_rbgs<T>(L.d, 0, L.x, L.b, s->st, omega);
+            launch_rbgs<T>(L.d, 0, L.x, L.b, s->st, omega, pass_dir(s, L.d, sizeof(T)));
         }
         {
             ProfScope ps(s, id, 1.5 * Ns);
-            launch_rbgs<T>(L.d, 1, L.x, L.b, s->st, omega);
+            launch_rbgs<T>(L.d, 1, L.x, L.b, s->st, omega, pass_dir(s, L.d, sizeof(T)));
         }
     }
     CKL();
@@ -466,19 +481,19 @@ int vcycle(afmib_solver* s, size_t l) {
     TRY(smooth(s, L, sizeof(T) == sizeof(float) ? s->inner_nu1 : s->cfg.nu1));
     {
         ProfScope ps(s, fine ? P_RESID0 : P_RESID, 3 * Ns);
-        launch_residual<T>(L.d, L.r, L.x, L.b, nullptr, nullptr, s->st);
+        launch_residual<T>(L.d, L.r, L.x, L.b, nullptr, nullptr, s->st, pass_dir(s, L.d, sizeof(T)));
     }
     MGLevelT<T>& C = lv[l + 1];
     {
         ProfScope ps(s, fine ? P_RESTRICT0 : P_RESTRICT, Ns + Ns / 8);
-        launch_restrict<T>(L.d, C.b, L.r, s->st);
+        launch_restrict<T>(L.d, C.b, L.r, s->st, pass_dir(s, L.d, sizeof(T)));
     }
     CK(cudaMemsetAsync(C.x, 0, C.d.ncell() * sizeof(T), s->st));
     CKL();
     TRY(vcycle<T>(s, l + 1));
     {
         ProfScope ps(s, fine ? P_PROLONG0 : P_PROLONG, 2 * Ns + Ns / 8);
-        launch_prolong_add<T>(L.d, L.x, C.x, s->st);
+        launch_prolong_add<T>(L.d, L.x, C.x, s->st, pass_dir(s, L.d, sizeof(T)));
     }
     TRY(smooth(s, L, sizeof(T) == sizeof(float) ? s->inner_nu2 : s->cfg.nu2));
     return AFMIB_OK;
@@ -682,7 +697,7 @@ int jacobi_inner32(afmib_solver* s, int comp, double scale, int sweeps) {
         ProfScope ps(s, P_JACOBI, (double)N * 4 * (j == 0 ? 2 : 3));
         float* out = bufs[(sweeps - 1 - j) % 2];
         const float* in = j == 0 ? nullptr : bufs[(sweeps - j) % 2];
-        launch_helm_jacobi<float>(s->d, comp, scale, in, out, s->d32, s->st);
+        launch_helm_jacobi<float>(s->d, comp, scale, in, out, s->d32, s->st, pass_dir(s, s->d, sizeof(float)));
     }
     CKL();
     return AFMIB_OK;
@@ -1436,6 +1451,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_INNER_SOLVER")) s->jacobi_inner = std::string(e) != "cg";
     if (const char* e = std::getenv("AFMIB_WARM_EXTRAP")) s->warm_extrap = std::string(e) == "1";
     if (const char* e = std::getenv("AFMIB_GRAPHS")) s->use_graphs = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_ALTERNATE")) s->alternate = std::string(e) != "0";
     if (g.proj_start < AFMIB_START_DEFAULT || g.proj_start > AFMIB_START_WARM)
         return s->fail(AFMIB_ERR_ARG, "proj_start must be AFMIB_START_DEFAULT, _ZERO or _WARM");
     s->warm_start = g.proj_start == AFMIB_START_WARM || (g.proj_start == AFMIB_START_DEFAULT && s->mixed);

@@ -531,6 +531,23 @@ def test_inner_cycle_schedule_matches_plain_gauss_seidel(monkeypatch, bc):
         assert rel(c, a) < 1e-9
 
 
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
+def test_alternating_block_order_keeps_bits(monkeypatch, precision):
+    """Passes over fields larger than L2 (256^3) alternate their block order;
+    the kernels that take it are pointwise or update one red-black colour, so
+    a multigrid solve is bit for bit the one in index order
+    (AFMIB_ALTERNATE=0)."""
+    n = 256
+    b = np.random.default_rng(27).standard_normal(n ** 3)
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("AFMIB_ALTERNATE", mode)
+        with capi.Solver(n, precision=precision, tol=1e-8) as sv:
+            out[mode] = sv.mg_solve(b)
+    assert out["0"][1] == out["1"][1]
+    assert np.array_equal(out["0"][0], out["1"][0])
+
+
 @pytest.mark.parametrize("m", [1200, 5000, 20000])
 def test_spread_dense_cluster_takes_large_capacity_pass(m):
     """m markers inside two cells: 1,200 exceed the first pass's capacity and
