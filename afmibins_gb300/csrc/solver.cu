@@ -560,18 +560,25 @@ int inner_vcycles32(afmib_solver* s, int ncyc) {
     MGLevel& L = s->lv[0];
     MGLevelT<float>& L32 = s->lv32[0];
     const long long N = L.d.ncell();
-    auto body = [&]() -> int {
-        CK(cudaMemsetAsync(L32.x, 0, N * sizeof(float), s->st));
-        for (int k = 0; k < ncyc; ++k) TRY(vcycle<float>(s, 0));
-        {
-            ProfScope ps(s, P_CORRECT, (double)N * (8 + 4 + 8));
-            launch_add_correction<float>(N, L.x, L32.x, s->st);
-        }
-        CKL();
-        return AFMIB_OK;
+    auto body = [&](int nc) {
+        return [&, nc]() -> int {
+            CK(cudaMemsetAsync(L32.x, 0, N * sizeof(float), s->st));
+            for (int k = 0; k < nc; ++k) TRY(vcycle<float>(s, 0));
+            {
+                ProfScope ps(s, P_CORRECT, (double)N * (8 + 4 + 8));
+                launch_add_correction<float>(N, L.x, L32.x, s->st);
+            }
+            CKL();
+            return AFMIB_OK;
+        };
     };
-    if (s->prof || !s->use_graphs) return body();
-    if (!s->vg32[ncyc]) TRY(capture_graph(s, &s->vg32[ncyc], &s->vg32_launches[ncyc], body));
+    if (s->prof || !s->use_graphs) return body(ncyc)();
+    // every block length is captured at the first use of any: a length first
+    // needed later (the adaptive sizing picks them as the residuals go) would
+    // pay for its capture and instantiation inside a running time step
+    if (!s->vg32[ncyc])
+        for (int k = 1; k <= s->inner_cycles; ++k)
+            if (!s->vg32[k]) TRY(capture_graph(s, &s->vg32[k], &s->vg32_launches[k], body(k)));
     CK(cudaGraphLaunch(s->vg32[ncyc], s->st));
     s->stats.kernel_launches += s->vg32_launches[ncyc];
     return AFMIB_OK;
