@@ -90,9 +90,11 @@ NOT_HBM_BOUND = {"helm_defect_fp64", "lap_defect_fp64", "helm_rhs", "spread_gath
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) measured
 # by ncu for the fine-level kernel of a family, by (family, grid, precision).
 NCU_TRAFFIC = {
-    # k_rbgs_z2<float>, one colour of the 256^3 level in the mixed form:
-    # 134.69 MB read + 18.05 MB written, and 134.68 + 14.91 MB on the next launch
-    ("mg_rbgs_fine", 256, "mixed"): 151.2e6,
+    # k_rbgs_z2<float>, one colour of the 256^3 level in the mixed form, in
+    # sequence inside a multigrid solve (ncu --cache-control none): mean DRAM
+    # read + write over ten launches; the alternating block order keeps part
+    # of x and b in L2 between passes (151 MB with cold caches)
+    ("mg_rbgs_fine", 256, "mixed"): 78.7e6,
 }
 
 
@@ -608,8 +610,8 @@ def main():
         roofline = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
                     "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                     "traffic": traffic, "bytes_per_launch": kbytes / nl, "ms_per_launch": kms / nl,
-                    "note": "dominant HBM-bound family: all its launches at every multigrid level, per-launch "
-                            "average; traffic = ncu dram bytes per launch of its fine-level kernel",
+                    "note": "dominant HBM-bound family, per-launch average over its launches; traffic = ncu "
+                            "dram bytes per launch of the same kernel in sequence",
                     "not_hbm_bound": {k: round(v[1] / total_ms, 4) for k, v in table.items() if k in NOT_HBM_BOUND}}
         kernels = {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / total_ms, 4),
                        "GB_s": round(v[2] / (v[1] * 1e-3) / 1e9, 1) if v[1] > 0 else None}
