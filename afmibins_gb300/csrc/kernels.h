@@ -74,6 +74,12 @@ void launch_cg_update(long long n, T* x, T* r, const T* p, const T* q, RedScratc
 template <typename T>
 void launch_helm_jacobi(const Dims& d, int comp, double scale, const T* x, T* xo, const T* b, cudaStream_t s,
                         int rev = 0);
+// One colour of a red-black Gauss-Seidel sweep of (I + scale*Delta) x = b in
+// place (init: from x = 0). Power-of-two extents, nz a multiple of 8;
+// returns false (nothing launched) otherwise.
+template <typename T>
+bool launch_helm_rbgs(const Dims& d, int comp, double scale, int color, int init, T* x, const T* b, cudaStream_t s,
+                      int rev = 0);
 // p' = beta p + r formed on the fly (out of place into pn), q = H p', p'.q and alpha
 template <typename T>
 void launch_cg_dir_apply(const Dims& d, int comp, double scale, const T* p, const T* r, T* pn, T* q, RedScratch sc,

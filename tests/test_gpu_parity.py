@@ -441,9 +441,9 @@ def test_multigrid_tail_equals_level_launches(monkeypatch, bc, precision, n):
 @pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
 def test_inner_jacobi_matches_inner_cg(monkeypatch, bc):
     """Mixed form: the FP32 inner Helmholtz solves by a fixed number of Jacobi
-    sweeps (bounded by the operator's diagonal dominance) or by CG; the FP64
-    outer loop stops on the same residual test, so the sub-steps agree to the
-    solver tolerance."""
+    sweeps (bounded by the operator's diagonal dominance), of red-black
+    Gauss-Seidel sweeps, or by CG; the FP64 outer loop stops on the same
+    residual test, so the sub-steps agree to the solver tolerance."""
     n = 32
     channel = bc == capi.BC_CHANNEL
     g = po.Grid(n, n, n, n, channel=channel)
@@ -451,7 +451,7 @@ def test_inner_jacobi_matches_inner_cg(monkeypatch, bc):
     u, v, w = 0.1 * rng.standard_normal(g.ncell), 0.1 * rng.standard_normal(g.nv), 0.1 * rng.standard_normal(g.ncell)
     f = [rng.standard_normal(g.ncell), rng.standard_normal(g.nv), rng.standard_normal(g.ncell)]
     out = {}
-    for mode in ("cg", "jacobi"):
+    for mode in ("cg", "jacobi", "gs"):
         monkeypatch.setenv("AFMIB_INNER_SOLVER", mode)
         with capi.Solver(n, bc=bc, precision=capi.MIXED, mu=0.01, rho=1.0, dt=1e-3, tol=1e-12) as sv:
             sv.set_velocity(u, v, w)
@@ -459,8 +459,9 @@ def test_inner_jacobi_matches_inner_cg(monkeypatch, bc):
             for _ in range(4):
                 sv.ns_step(*f)
             out[mode] = sv.get_velocity()
-    for a, b in zip(out["cg"], out["jacobi"]):
-        assert rel(b, a) < 1e-10
+    for mode in ("jacobi", "gs"):
+        for a, b in zip(out["cg"], out[mode]):
+            assert rel(b, a) < 1e-10
 
 
 @pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
