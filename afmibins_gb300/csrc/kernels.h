@@ -43,6 +43,19 @@ template <typename T, typename TF, typename TA>
 void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const TF* f, const TA* adv,
                      const double* top, const double* bottom, double s_plus, double s_minus, double dt,
                      double inv_rho, cudaStream_t s);
+// Mixed form, backward-Euler sub-step: b (as launch_helm_rhs), the first FP64
+// defect r = b - H uold as FP32 with out[0] = r.r (H = I + s_minus Delta), and
+// q = Q(uold), the off-diagonal term of the Helmholtz rows, in one pass.
+template <typename TF, typename TA>
+void launch_helm_rhs_be_defect(const Dims& d, int comp, double* b, float* r, double* q, const double* uold,
+                               const TF* f, const TA* adv, const double* top, const double* bottom, double s_minus,
+                               double dt, double inv_rho, RedScratch sc, double* out, cudaStream_t s);
+// Mixed form, Crank-Nicolson sub-step: b from q = Q(uold) kept by the
+// backward-Euler sub-step (pointwise).
+template <typename TF, typename TA>
+void launch_helm_rhs_cn_q(const Dims& d, int comp, double* r, const double* uold, const double* q, const TF* f,
+                          const TA* adv, const double* top, const double* bottom, double s_plus, double s_minus,
+                          double dt, double inv_rho, cudaStream_t s);
 // Mixed form: r = b - (I + s Delta) x in FP64, stored as TD, out[0] = ||r||^2.
 template <typename TD>
 void launch_helm_defect(const Dims& d, int comp, double scale, const double* x, const double* b, TD* r, RedScratch sc,

@@ -230,6 +230,111 @@ __global__ void k_helm_rhs(Dims d, int comp, int be, T* __restrict__ r, const T*
     }
 }
 
+// Off-diagonal term of the Helmholtz row: helm_point(x) = x0 + off * Q(x) in
+// exact arithmetic, with Q = sum(nb) - k x0 (interior, 2D, channel v faces),
+// Q = (sx + sz) + 4/3 x(y+-1) - 8 x0 (channel u/w wall rows) and Q = 0 on the
+// channel v wall plane (src/ns/helmholtz.h:61-175).
+// helm_point (the same expressions, so the same bits) and Q of one cell from
+// one set of neighbour loads and partial sums
+template <typename T>
+__device__ __forceinline__ void helm_point_q(const Dims& d, int comp, T s, const T* __restrict__ x, int xi, int yi,
+                                             int zi, T& hx, T& q) {
+    const T off = s * T(d.n) * T(d.n);
+    const T x0 = x[lin(d, xi, yi, zi)];
+    const T sx = x[lin(d, xm1(d, xi), yi, zi)] + x[lin(d, xp1(d, xi), yi, zi)];
+    if (d.nz == 1) {
+        const T sy = x[lin(d, xi, ym1(d, yi), zi)] + x[lin(d, xi, yp1(d, yi), zi)];
+        hx = (T(1) - T(4) * off) * x0 + off * (sx + sy);
+        q = (sx + sy) - T(4) * x0;
+        return;
+    }
+    const T sz = x[lin(d, xi, yi, zm1(d, zi))] + x[lin(d, xi, yi, zp1(d, zi))];
+    if (d.channel && comp != 1) {
+        T diag = T(1) - T(6) * off;
+        if (yi == 0 || yi == d.ny - 1) {
+            diag -= T(2) * off;
+            const T xa = x[lin(d, xi, yi == 0 ? 1 : yi - 1, zi)];
+            hx = diag * x0 + (off * (sx + sz) + (off + off / T(3)) * xa);
+            q = (sx + sz) + (T(4) / T(3)) * xa - T(8) * x0;
+        } else {
+            const T sy = x[lin(d, xi, yi - 1, zi)] + x[lin(d, xi, yi + 1, zi)];
+            hx = diag * x0 + (off * (sx + sz) + off * sy);
+            q = (sx + sz) + sy - T(6) * x0;
+        }
+        return;
+    }
+    if (d.channel && comp == 1 && yi == 0) {
+        hx = x0;
+        q = T(0);
+        return;
+    }
+    const T sy = x[lin(d, xi, ym1(d, yi), zi)] + x[lin(d, xi, yp1(d, yi), zi)];
+    const T sum = sx + sy + sz;
+    hx = (T(1) - T(6) * off) * x0 + off * sum;
+    q = sum - T(6) * x0;
+}
+
+// Mixed form, backward-Euler sub-step: the right-hand side b (as k_helm_rhs),
+// the first FP64 defect of the viscous solve started from x = uold
+// (r = b - H uold, as k_helm_defect, with its squared norm) and Q(uold) for
+// the Crank-Nicolson right-hand side of the next sub-step, in one pass.
+template <typename TF, typename TA>
+__global__ void __launch_bounds__(kRedBlock) k_helm_rhs_be_defect(Dims d, int comp, double* __restrict__ b_out,
+                                                                 float* __restrict__ r_out, double* __restrict__ q_out,
+                                                                 const double* __restrict__ uold, const TF* __restrict__ f,
+                                                                 const TA* __restrict__ adv, const double* __restrict__ top,
+                                                                 const double* __restrict__ bottom, double s_minus,
+                                                                 double hdt, double inv_rho, RedScratch sc, double* out) {
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+    float acc = 0.f;
+    if (xi < d.nx && yi < d.ny)
+        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
+            const long long i = lin(d, xi, yi, zi);
+            double b = 0.0;
+            if (!(d.channel && comp == 1 && yi == 0)) {
+                double bm = 0.0;
+                if (d.channel && comp != 1 && (yi == 0 || yi == d.ny - 1) && top) {
+                    const long long ixz = xi + (long long)d.nx * zi;
+                    bm = 8. / 3. * s_minus * d.n * d.n * ((yi == 0) ? bottom[ixz] : top[ixz]);
+                }
+                const double src = hdt * (inv_rho * cvt<double, TF>(f[i]) - cvt<double, TA>(adv[i]));
+                b = (uold[i] + -1.0 * bm) + src;
+            }
+            double hx, q;
+            helm_point_q(d, comp, s_minus, uold, xi, yi, zi, hx, q);
+            b_out[i] = b;
+            q_out[i] = q;
+            const float ri = float(b - hx);
+            r_out[i] = ri;
+            acc += ri * ri;
+        }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, out);
+}
+
+// Mixed form, Crank-Nicolson sub-step: the right-hand side from Q(uold) kept
+// by the backward-Euler sub-step, b = (uold + off+ Q + (bp - bm)) + src, a
+// pointwise pass instead of the FP64 stencil.
+template <typename TF, typename TA>
+__global__ void k_helm_rhs_cn_q(Dims d, int comp, double* __restrict__ r, const double* __restrict__ uold,
+                                const double* __restrict__ q, const TF* __restrict__ f, const TA* __restrict__ adv,
+                                const double* __restrict__ top, const double* __restrict__ bottom, double s_plus,
+                                double s_minus, double hdt, double inv_rho) {
+    AFMIB_XYZ
+    const long long i = lin(d, x, y, z);
+    if (d.channel && comp == 1 && y == 0) { r[i] = 0.0; return; }
+    double bm = 0.0, bp = 0.0;
+    if (d.channel && comp != 1 && (y == 0 || y == d.ny - 1) && top) {
+        const long long ixz = x + (long long)d.nx * z;
+        const double wv = (y == 0) ? bottom[ixz] : top[ixz];
+        bm = 8. / 3. * s_minus * d.n * d.n * wv;
+        bp = 8. / 3. * s_plus * d.n * d.n * wv;
+    }
+    const double src = hdt * (inv_rho * cvt<double, TF>(f[i]) - cvt<double, TA>(adv[i]));
+    const double off = s_plus * double(d.n) * double(d.n);
+    r[i] = ((uold[i] + off * q[i]) + (bp - bm)) + src;
+}
+
 // ---------------------------------------------------------------------------
 // CG pieces. Scalars live on the device in cgs[] = {n0, pq, n1, beta, alpha}
 // so that no host round trip sits inside an iteration except the convergence
@@ -565,6 +670,33 @@ void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const
     k_helm_rhs<T, TF, TA><<<grid3(d), block3(), 0, s>>>(d, comp, be, r, uold, f, adv, top, bottom, s_plus, s_minus,
                                                         be ? dt / 2 : dt, inv_rho);
 }
+template <typename TF, typename TA>
+void launch_helm_rhs_be_defect(const Dims& d, int comp, double* b, float* r, double* q, const double* uold,
+                               const TF* f, const TA* adv, const double* top, const double* bottom, double s_minus,
+                               double dt, double inv_rho, RedScratch sc, double* out, cudaStream_t s) {
+    k_helm_rhs_be_defect<TF, TA><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(
+        d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out);
+}
+template <typename TF, typename TA>
+void launch_helm_rhs_cn_q(const Dims& d, int comp, double* r, const double* uold, const double* q, const TF* f,
+                          const TA* adv, const double* top, const double* bottom, double s_plus, double s_minus,
+                          double dt, double inv_rho, cudaStream_t s) {
+    k_helm_rhs_cn_q<TF, TA><<<grid3(d), block3(), 0, s>>>(d, comp, r, uold, q, f, adv, top, bottom, s_plus, s_minus, dt,
+                                                          inv_rho);
+}
+template void launch_helm_rhs_be_defect<double, float>(const Dims&, int, double*, float*, double*, const double*,
+                                                       const double*, const float*, const double*, const double*,
+                                                       double, double, double, RedScratch, double*, cudaStream_t);
+template void launch_helm_rhs_be_defect<float, float>(const Dims&, int, double*, float*, double*, const double*,
+                                                      const float*, const float*, const double*, const double*, double,
+                                                      double, double, RedScratch, double*, cudaStream_t);
+template void launch_helm_rhs_cn_q<double, float>(const Dims&, int, double*, const double*, const double*,
+                                                  const double*, const float*, const double*, const double*, double,
+                                                  double, double, double, cudaStream_t);
+template void launch_helm_rhs_cn_q<float, float>(const Dims&, int, double*, const double*, const double*, const float*,
+                                                 const float*, const double*, const double*, double, double, double,
+                                                 double, cudaStream_t);
+
 template <typename TD>
 void launch_helm_defect(const Dims& d, int comp, double scale, const double* x, const double* b, TD* r, RedScratch sc,
                         double* out, cudaStream_t s) {

@@ -44,6 +44,12 @@ struct afmib_solver {
     // FP64 state on MAC faces (v padded to ny planes in channel mode)
     double *u = nullptr, *v = nullptr, *w = nullptr;
     double *uo[3] = {}, *adv[3] = {}, *rhs[3] = {}, *f[3] = {};
+    // mixed form: Q(uold), the off-diagonal term of the viscous rows, kept by
+    // the backward-Euler sub-step for the Crank-Nicolson right-hand side
+    // (AFMIB_FUSED_RHS=0: each right-hand side and first defect apart)
+    double* qo[3] = {};
+    bool qo_valid = false;
+    bool fused_rhs = true;
     double *divb = nullptr, *walls = nullptr, *wallgrad = nullptr;
     double *cg_r = nullptr, *cg_p = nullptr, *cg_q = nullptr;
     double *tmp[3] = {};
@@ -740,11 +746,13 @@ int jacobi_inner32(afmib_solver* s, int comp, double scale, int sweeps) {
     return AFMIB_OK;
 }
 
-int helm_solve_mixed(afmib_solver* s, int comp, double scale, double* x, const double* b) {
+// r0_ready: the first defect (d32, its squared norm in scal[10]) is already
+// computed for this x and b
+int helm_solve_mixed(afmib_solver* s, int comp, double scale, double* x, const double* b, bool r0_ready = false) {
     const long long N = s->N();
     int outer = 0;
     for (;;) {
-        {
+        if (!(r0_ready && outer == 0)) {
             ProfScope ps(s, P_HELM_DEFECT, (double)N * (8 + 8 + 4));
             if (s->bfp_defects)
                 launch_helm_defect_bfp(s->d, comp, scale, x, b, s->d32, s->red, s->scal + 10, s->st);
@@ -887,6 +895,61 @@ int substep(afmib_solver* s) {
     const double* wt = s->walls + 2 * nxz;
     const double* wb = s->walls + 3 * nxz;
     const double inv_rho = 1 / s->cfg.rho;
+    double* vel[3] = {s->u, s->v, s->w};
+    if (s->mixed && s->fused_rhs && s->qo[0] && !s->bfp_defects) {
+        // backward Euler: right-hand side, first defect (x starts at uold)
+        // and Q(uold) in one pass, component by component; Crank-Nicolson:
+        // right-hand sides from Q(uold), then the solves
+        for (int c = 0; c < 3; ++c) {
+            const double* top = (!d.channel || c == 1) ? nullptr : (c == 0 ? ut : wt);
+            const double* bot = (!d.channel || c == 1) ? nullptr : (c == 0 ? ub : wb);
+            if (be) {
+                {
+                    ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 4 + 8 + 8 + 4));
+                    if (s->spread64)
+                        launch_helm_rhs_be_defect<double, float>(d, c, s->rhs[c], s->d32, s->qo[c], s->uo[c], s->f[c],
+                                                                 s->adv32[c], top, bot, s->s_minus(), s->cfg.dt, inv_rho,
+                                                                 s->red, s->scal + 10, s->st);
+                    else
+                        launch_helm_rhs_be_defect<float, float>(d, c, s->rhs[c], s->d32, s->qo[c], s->uo[c],
+                                                                s->f32[c], s->adv32[c], top, bot, s->s_minus(),
+                                                                s->cfg.dt, inv_rho, s->red, s->scal + 10, s->st);
+                }
+                CKL();
+                TRY(helm_solve_mixed(s, c, s->s_minus(), vel[c], s->rhs[c], true));
+            } else if (s->qo_valid) {
+                ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 8 + 4 + 8));
+                if (s->spread64)
+                    launch_helm_rhs_cn_q<double, float>(d, c, s->rhs[c], s->uo[c], s->qo[c], s->f[c], s->adv32[c], top,
+                                                        bot, s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
+                else
+                    launch_helm_rhs_cn_q<float, float>(d, c, s->rhs[c], s->uo[c], s->qo[c], s->f32[c], s->adv32[c], top,
+                                                       bot, s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
+            } else if (s->spread64) {
+                ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 4 + 8));
+                launch_helm_rhs<double, double, float>(d, c, 0, s->rhs[c], s->uo[c], s->f[c], s->adv32[c], top, bot,
+                                                       s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
+            } else {
+                ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 4 + 4 + 8));
+                launch_helm_rhs<double, float, float>(d, c, 0, s->rhs[c], s->uo[c], s->f32[c], s->adv32[c], top, bot,
+                                                      s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
+            }
+        }
+        CKL();
+        if (be) {
+            s->qo_valid = true;
+        } else {
+            for (int c = 0; c < 3; ++c) TRY(helm_solve_mixed(s, c, s->s_minus(), vel[c], s->rhs[c]));
+        }
+        s->proj_phase = be ? 0 : 1;
+        const int prc = project(s);
+        s->proj_phase = -1;
+        TRY(prc);
+        s->half = !s->half;
+        s->stats.half = s->half ? 1 : 0;
+        s->stats.substeps++;
+        return AFMIB_OK;
+    }
     for (int c = 0; c < 3; ++c) {
         const double* top = (!d.channel || c == 1) ? nullptr : (c == 0 ? ut : wt);
         const double* bot = (!d.channel || c == 1) ? nullptr : (c == 0 ? ub : wb);
@@ -905,7 +968,6 @@ int substep(afmib_solver* s) {
         }
     }
     CKL();
-    double* vel[3] = {s->u, s->v, s->w};
     for (int c = 0; c < 3; ++c) {
         if (s->mixed) TRY(helm_solve_mixed(s, c, s->s_minus(), vel[c], s->rhs[c]));
         else TRY(cg_solve(s, c, s->s_minus(), vel[c], s->rhs[c], nullptr));
@@ -1521,6 +1583,9 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
         TRY(dalloc(s, &s->tmp[k], N));
     }
     TRY(dalloc(s, &s->divb, N));
+    if (const char* e = std::getenv("AFMIB_FUSED_RHS")) s->fused_rhs = std::string(e) != "0";
+    if (s->mixed && s->fused_rhs)
+        for (auto& q : s->qo) TRY(dalloc(s, &q, N));
     TRY(dalloc(s, &s->phi_prev[0], N));
     TRY(dalloc(s, &s->phi_prev[1], N));
     if (s->warm_extrap) {
@@ -1727,6 +1792,7 @@ int afmib_set_velocity(afmib_solver* s, const double* u, const double* v, const 
     TRY(refresh_shadow(s));
     s->phi_valid[0] = s->phi_valid[1] = false;  // a new state: no warm start
     s->phi_valid2[0] = s->phi_valid2[1] = false;
+    s->qo_valid = false;
     return sync(s);
 }
 
