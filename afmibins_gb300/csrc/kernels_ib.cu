@@ -405,6 +405,8 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
         const int J[3] = {lx + 2, ly + 2, lz + HZ};
         for (int comp = 0; comp < 3; ++comp) {
             T acc = T(0);
+            const unsigned jp = 0x00808080u | (unsigned)(J[0] + 8) | ((unsigned)(J[1] + 8) << 8) |
+                                ((unsigned)(J[2] + 8) << 16);
             const int hx = (comp == 0) ? J[0] + 1 : J[0] + 2;
             const int hy = (comp == 1) ? J[1] + 1 : J[1] + 2;
             const int hz = TZ == 1 ? J[2] : ((comp == 2) ? J[2] + 1 : J[2] + 2);
@@ -443,13 +445,13 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
                         s0 = s0 > 0 ? s0 : 0;
                         s1 = s1 < nc ? s1 : nc;
                         for (int sl = s0; sl < s1; ++sl) {
-                            const int pk = s_base[sl];
-                            const int mx = J[0] - ((pk & 255) - 8);
-                            const int my = J[1] - (((pk >> 8) & 255) - 8);
-                            const int mz = J[2] - (((pk >> 16) & 255) - 8);
-                            if ((unsigned)mx < 4u && (unsigned)my < 4u && (unsigned)mz < 4u) {
+                            // per byte (0x80 + J + 8) - (b + 8): no borrow crosses a
+                            // byte (all fields < 0x80); the face is in the marker's
+                            // support iff every byte is 0x80 + {0..3}
+                            const unsigned t = jp - (unsigned)s_base[sl];
+                            if ((t & 0x00FCFCFCu) == 0x00808080u) {
                                 const T* w = s_w + (size_t)sl * 12;
-                                acc += (w[mx] * w[4 + my]) * w[8 + mz];
+                                acc += (w[t & 3u] * w[4 + ((t >> 8) & 3u)]) * w[8 + ((t >> 16) & 3u)];
                             }
                         }
                     }
