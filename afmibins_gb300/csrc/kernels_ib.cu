@@ -368,6 +368,10 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
         __syncthreads();
         const int nc_all = s_scan[NW - 1];
         int off = inc - tot + (warp > 0 ? s_scan[warp - 1] : 0);
+        // an active tile whose neighbourhood holds no marker (its occupied
+        // neighbour tiles' markers lie beyond the 2-cell halo) adds nothing:
+        // its faces keep the zeros the callers wrote (block-uniform)
+        if (nc_all == 0) continue;
         const bool chunked = nc_all > cap;  // block-uniform
         if (chunked && ovf_list) {           // left to the large-capacity pass
             if (tid == 0) ovf_list[atomicAdd(ovf_count, 1)] = t;

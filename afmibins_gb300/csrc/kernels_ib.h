@@ -43,7 +43,8 @@ void launch_cell_table(int TS, int TZ, const unsigned* keys, const int* tstart, 
 template <typename T>
 size_t spread_smem_bytes(int TS, int TZ, int cap);
 // f_c(face) = scale * sum_k (phi/n)^3 * vol_k * G_c,k over the active tiles
-// (faces of the other tiles are left untouched). A tile whose neighbourhood
+// (faces of the other tiles, and of active tiles whose neighbourhood holds no
+// marker, are left untouched: the callers zero the fields first). A tile whose neighbourhood
 // holds more than `cap` markers is appended to ovf_list (and left untouched)
 // when ovf_list is given, else spread in chunks of `cap` markers (same
 // result bits as one pass). Blocks take tiles from *next_tile, which must be
