@@ -74,6 +74,8 @@ _SIGS = {
     "afmib_ns_step": ([_vp, _vp, _vp, _vp], ctypes.c_int),
     "afmib_set_markers": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     "afmib_get_markers": ([_vp, _vp], ctypes.c_int),
+    "afmib_save": ([_vp, ctypes.c_char_p], ctypes.c_int),
+    "afmib_load": ([_vp, ctypes.c_char_p], ctypes.c_int),
     "afmib_set_marker_positions": ([_vp, _vp], ctypes.c_int),
     "afmib_ib_step": ([_vp, ctypes.c_int], ctypes.c_int),
     "afmib_div": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
@@ -274,6 +276,16 @@ class Solver:
 
     def ib_step(self, nsteps=1):
         self._ck(self.lib.afmib_ib_step(self.h, nsteps))
+
+    # snapshots (afmibins_gb300/snapshot.py reads the files without a GPU)
+    def save(self, path):
+        self._ck(self.lib.afmib_save(self.h, os.fsencode(path)))
+
+    def load(self, path):
+        from . import snapshot
+        self._ck(self.lib.afmib_load(self.h, os.fsencode(path)))
+        counts = snapshot.sections(path)
+        self.M = counts["X"][1] // 3 if "X" in counts else 0
 
     # adjoint
     def set_spring(self, k):

@@ -18,6 +18,7 @@
 #include "kernels.h"
 #include "kernels_ib.h"
 #include "kernels_adjoint.h"
+#include "snapshot_io.h"
 
 using namespace afmib;
 
@@ -1731,6 +1732,14 @@ int check_smoother_flag(afmib_solver* s) {
 // ===========================================================================
 // C ABI
 // ===========================================================================
+// device -> host copy on the solver's stream (the caller synchronises)
+template <typename T>
+int to_host(afmib_solver* s, std::vector<T>& h, const T* d, long long n) {
+    h.resize((size_t)n);
+    if (n > 0) CK(cudaMemcpyAsync(h.data(), d, (size_t)n * sizeof(T), cudaMemcpyDeviceToHost, s->st));
+    return AFMIB_OK;
+}
+
 extern "C" {
 
 const char* afmib_error_string(int status) {
@@ -1908,6 +1917,139 @@ int afmib_get_markers(afmib_solver* s, double* X) {
     if (!s || !X) return AFMIB_ERR_ARG;
     TRY(copy_out(s, X, s->X, 3 * (long long)s->M));
     return sync(s);
+}
+
+// ---------------------------------------------------------------------------
+// Snapshots (snapshot_io.h): everything a run needs to continue bit for bit.
+// ---------------------------------------------------------------------------
+int afmib_save(afmib_solver* s, const char* path) {
+    if (!s || !path) return AFMIB_ERR_ARG;
+    const long long N = s->N(), nxz = s->nxz(), M = s->M;
+    std::vector<double> u, v, w, phi, pp0, pp1, walls, wallgrad, X, vol, uo[3], qo[3];
+    std::vector<int> nstart, nidx;
+    TRY(to_host(s, u, s->u, N));
+    // mid-step (a Crank-Nicolson sub-step next): its right-hand side needs the
+    // velocity at the start of the step and, in the mixed form, Q of it
+    for (int c = 0; c < 3 && s->half; ++c) {
+        TRY(to_host(s, uo[c], s->uo[c], N));
+        if (s->qo_valid) TRY(to_host(s, qo[c], s->qo[c], N));
+    }
+    TRY(to_host(s, v, s->v, N));
+    TRY(to_host(s, w, s->w, N));
+    TRY(to_host(s, phi, s->lv[0].x, N));
+    if (s->phi_valid[0]) TRY(to_host(s, pp0, s->phi_prev[0], N));
+    if (s->phi_valid[1]) TRY(to_host(s, pp1, s->phi_prev[1], N));
+    TRY(to_host(s, walls, s->walls, 4 * nxz));
+    // the wall rows of the last projection's gradient, which the next
+    // sub-step's wall update uses (channel)
+    TRY(to_host(s, wallgrad, s->wallgrad, 6 * nxz));
+    if (M > 0) {
+        TRY(to_host(s, X, s->X, 3 * M));
+        TRY(to_host(s, nstart, s->nstart, M + 1));
+        if (s->has_vol) TRY(to_host(s, vol, s->mvol, M));
+    }
+    TRY(sync(s));
+    if (M > 0 && nstart[M] > 0) {
+        TRY(to_host(s, nidx, s->nidx, nstart[M]));
+        TRY(sync(s));
+    }
+    snap::Writer wr;
+    wr.h.nx = s->d.nx;
+    wr.h.ny = s->d.ny;
+    wr.h.nz = s->d.nz;
+    wr.h.n = s->d.n;
+    wr.h.bc = s->cfg.bc;
+    wr.h.precision = s->cfg.precision;
+    wr.h.half = s->half ? 1 : 0;
+    wr.h.substeps = s->stats.substeps;
+    wr.h.mg_rho = s->mg_rho;
+    wr.add("u", snap::kF64, u.data(), u.size());
+    wr.add("v", snap::kF64, v.data(), v.size());
+    wr.add("w", snap::kF64, w.data(), w.size());
+    wr.add("phi", snap::kF64, phi.data(), phi.size());
+    if (!pp0.empty()) wr.add("phi_prev0", snap::kF64, pp0.data(), pp0.size());
+    if (!pp1.empty()) wr.add("phi_prev1", snap::kF64, pp1.data(), pp1.size());
+    wr.add("walls", snap::kF64, walls.data(), walls.size());
+    wr.add("wallgrad", snap::kF64, wallgrad.data(), wallgrad.size());
+    const char* uo_name[3] = {"uo0", "uo1", "uo2"};
+    const char* qo_name[3] = {"qo0", "qo1", "qo2"};
+    for (int c = 0; c < 3; ++c) {
+        if (!uo[c].empty()) wr.add(uo_name[c], snap::kF64, uo[c].data(), uo[c].size());
+        if (!qo[c].empty()) wr.add(qo_name[c], snap::kF64, qo[c].data(), qo[c].size());
+    }
+    if (M > 0) {
+        wr.add("X", snap::kF64, X.data(), X.size());
+        wr.add("nstart", snap::kI32, nstart.data(), nstart.size());
+        wr.add("nidx", snap::kI32, nidx.data(), nidx.size());
+        if (s->has_vol) wr.add("vol", snap::kF64, vol.data(), vol.size());
+    }
+    if (!wr.write(path)) return s->fail(AFMIB_ERR_ARG, "cannot write the snapshot file");
+    return AFMIB_OK;
+}
+
+int afmib_load(afmib_solver* s, const char* path) {
+    if (!s || !path) return AFMIB_ERR_ARG;
+    snap::Header h{};
+    std::map<std::string, snap::Section> sec;
+    const std::string err = snap::read(path, &h, &sec);
+    if (!err.empty()) return s->fail(AFMIB_ERR_ARG, err);
+    if (h.nx != s->d.nx || h.ny != s->d.ny || h.nz != s->d.nz || h.n != s->d.n || h.bc != s->cfg.bc)
+        return s->fail(AFMIB_ERR_ARG, "the snapshot's grid or boundary conditions differ from the solver's");
+    const long long N = s->N(), nxz = s->nxz();
+    auto f64 = [&](const char* name, long long count) -> const double* {
+        auto it = sec.find(name);
+        if (it == sec.end() || it->second.dtype != snap::kF64 || (long long)it->second.count() != count) return nullptr;
+        return it->second.f64();
+    };
+    const double *u = f64("u", N), *v = f64("v", N), *w = f64("w", N), *phi = f64("phi", N),
+                 *walls = f64("walls", 4 * nxz), *wallgrad = f64("wallgrad", 6 * nxz);
+    if (!u || !v || !w || !phi || !walls || !wallgrad)
+        return s->fail(AFMIB_ERR_ARG, "snapshot sections missing or of the wrong size");
+    CK(cudaMemcpyAsync(s->u, u, N * sizeof(double), cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(s->v, v, N * sizeof(double), cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(s->w, w, N * sizeof(double), cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(s->lv[0].x, phi, N * sizeof(double), cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(s->walls, walls, 4 * nxz * sizeof(double), cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(s->wallgrad, wallgrad, 6 * nxz * sizeof(double), cudaMemcpyHostToDevice, s->st));
+    TRY(refresh_shadow(s));
+    for (int k = 0; k < 2; ++k) {
+        const double* pp = f64(k == 0 ? "phi_prev0" : "phi_prev1", N);
+        s->phi_valid[k] = pp != nullptr;
+        if (pp) CK(cudaMemcpyAsync(s->phi_prev[k], pp, N * sizeof(double), cudaMemcpyHostToDevice, s->st));
+    }
+    s->phi_valid2[0] = s->phi_valid2[1] = false;
+    s->qo_valid = false;
+    if (h.half) {
+        const char* uo_name[3] = {"uo0", "uo1", "uo2"};
+        const char* qo_name[3] = {"qo0", "qo1", "qo2"};
+        bool q_all = s->qo[0] != nullptr;
+        for (int c = 0; c < 3; ++c) {
+            const double* uo = f64(uo_name[c], N);
+            if (!uo) return s->fail(AFMIB_ERR_ARG, "a mid-step snapshot without the step's start velocity");
+            CK(cudaMemcpyAsync(s->uo[c], uo, N * sizeof(double), cudaMemcpyHostToDevice, s->st));
+            const double* q = f64(qo_name[c], N);
+            if (q && s->qo[c]) CK(cudaMemcpyAsync(s->qo[c], q, N * sizeof(double), cudaMemcpyHostToDevice, s->st));
+            q_all = q_all && q;
+        }
+        s->qo_valid = q_all;
+    }
+    s->half = h.half != 0;
+    s->stats.half = h.half;
+    s->stats.substeps = h.substeps;
+    s->mg_rho = h.mg_rho;
+    TRY(sync(s));
+    auto xs = sec.find("X");
+    if (xs != sec.end()) {
+        const long long M = (long long)xs->second.count() / 3;
+        auto ns = sec.find("nstart");
+        auto ni = sec.find("nidx");
+        if (xs->second.dtype != snap::kF64 || ns == sec.end() || ns->second.dtype != snap::kI32 ||
+            (long long)ns->second.count() != M + 1 || ni == sec.end() || ni->second.dtype != snap::kI32)
+            return s->fail(AFMIB_ERR_ARG, "snapshot marker sections inconsistent");
+        const double* vol = f64("vol", M);
+        TRY(afmib_set_markers(s, (int)M, xs->second.f64(), ns->second.i32(), ni->second.i32(), vol));
+    }
+    return AFMIB_OK;
 }
 
 int afmib_ib_step(afmib_solver* s, int nsteps) {

@@ -130,6 +130,18 @@ int afmib_set_marker_positions(afmib_solver* s, const double* X);
  * (the coupling left as comments in test/ib_ns_test.cc:73-96). */
 int afmib_ib_step(afmib_solver* s, int nsteps);
 
+/* Snapshot of the solver state to a binary file (layout documented in
+ * afmibins_gb300/csrc/snapshot_io.h; afmibins_gb300/snapshot.py reads it):
+ * velocity (device layout, v with its wall plane), wall velocities and the
+ * wall rows of the last pressure gradient, the pressure potential and its
+ * warm-start copies, markers, springs and volumes,
+ * the sub-step phase and the multigrid contraction estimate. Loading it into
+ * a solver of the same grid and boundary conditions continues the run bit for
+ * bit. The reference has no format (it prints with operator<<,
+ * src/dt/vector.h:153-165). */
+int afmib_save(afmib_solver* s, const char* path);
+int afmib_load(afmib_solver* s, const char* path);
+
 /* Spring stiffness k of the membrane (G_i = k * sum_j (X_j - X_i)). */
 int afmib_set_spring(afmib_solver* s, double k);
 
