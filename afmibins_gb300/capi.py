@@ -44,7 +44,7 @@ class Config(ctypes.Structure):
                 ("nu1", ctypes.c_int), ("nu2", ctypes.c_int), ("mu", ctypes.c_double), ("rho", ctypes.c_double),
                 ("dt", ctypes.c_double), ("tol", ctypes.c_double), ("max_cg_iters", ctypes.c_int),
                 ("max_mg_cycles", ctypes.c_int), ("k_spring", ctypes.c_double), ("inner_tol", ctypes.c_double),
-                ("ib_fp32", ctypes.c_int), ("proj_start", ctypes.c_int)]
+                ("ib_fp32", ctypes.c_int), ("proj_start", ctypes.c_int), ("walls_corrected", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -169,12 +169,12 @@ class Solver:
 
     def __init__(self, nx, ny=None, nz=None, *, n=None, bc=BC_PERIODIC, precision=FP64, mu=0.01, rho=1.0, dt=1e-4,
                  tol=1e-10, mg_levels=0, nu1=2, nu2=2, max_cg_iters=1000, max_mg_cycles=200, k_spring=0.0,
-                 inner_tol=0.0, ib_fp32=0, proj_start=0, stream=None):
+                 inner_tol=0.0, ib_fp32=0, proj_start=0, walls_corrected=0, stream=None):
         self.lib = load()
         ny = nx if ny is None else ny
         nz = nx if nz is None else nz
         self.cfg = Config(nx, ny, nz, n or nx, bc, precision, mg_levels, nu1, nu2, mu, rho, dt, tol, max_cg_iters,
-                          max_mg_cycles, k_spring, inner_tol, ib_fp32, proj_start)
+                          max_mg_cycles, k_spring, inner_tol, ib_fp32, proj_start, walls_corrected)
         self.nx, self.ny, self.nz = nx, ny, nz
         self.channel = bc == BC_CHANNEL
         h = _vp()

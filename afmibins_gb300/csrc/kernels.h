@@ -24,14 +24,15 @@ template <typename T>
 void launch_grad(const Dims& d, T* px, T* py, T* pz, const T* p, cudaStream_t s);
 // Projection update u -= grad(phi), src/ns/projection.h:60-73. In channel
 // mode the wall-adjacent gradient rows needed by the next wall update are
-// saved into wallgrad[6][nx*nz] (may be null).
+// saved into wallgrad[8][nx*nz] (may be null): x-gradient at y = 0, 1,
+// ny-1, ny-2, z-gradient at y = 0, ny-1, 1, ny-2.
 // u32/v32/w32 (optional): FP32 shadow of the updated velocity.
 template <typename T>
 void launch_grad_sub(const Dims& d, T* u, T* v, T* w, const T* phi, T* wallgrad, cudaStream_t s, float* u32 = nullptr,
                      float* v32 = nullptr, float* w32 = nullptr);
 // Wall-velocity correction of src/ns/projection.h:75-122 (channel only).
 // walls = [ut | ub | wt | wb], nx*nz each.
-void launch_wall_update(const Dims& d, double* walls, const double* wallgrad, cudaStream_t s);
+void launch_wall_update(const Dims& d, double* walls, const double* wallgrad, cudaStream_t s, int corrected = 0);
 
 // Helmholtz right-hand side for one component.
 //   be=1: r = u_old - bdy(s_minus) + dt/2 * (f/rho - adv)

@@ -137,24 +137,27 @@ __global__ void k_grad_sub(Dims d, T* __restrict__ u, T* __restrict__ v, T* __re
     if (d.channel && wg) {
         const long long nxz = (long long)d.nx * d.nz, ixz = x + (long long)d.nx * z;
         if (y == 0) { wg[0 * nxz + ixz] = gx; wg[4 * nxz + ixz] = gz; }
-        if (y == 1) wg[1 * nxz + ixz] = gx;
+        if (y == 1) { wg[1 * nxz + ixz] = gx; wg[6 * nxz + ixz] = gz; }
         if (y == d.ny - 1) { wg[2 * nxz + ixz] = gx; wg[5 * nxz + ixz] = gz; }
-        if (y == d.ny - 2) wg[3 * nxz + ixz] = gx;
+        if (y == d.ny - 2) { wg[3 * nxz + ixz] = gx; wg[7 * nxz + ixz] = gz; }
     }
 }
 
 // src/ns/projection.h:86-104, including its slips: the loop covers
 // nx*min(ny, nz) wall entries and the w corrections read the x-gradient rows.
-__global__ void k_wall_update(Dims d, double* __restrict__ walls, const double* __restrict__ wg) {
+// corrected: every nx*nz entry, the w corrections from the z-gradient rows.
+__global__ void k_wall_update(Dims d, double* __restrict__ walls, const double* __restrict__ wg, int corrected) {
     const long long nxz = (long long)d.nx * d.nz;
-    const long long cnt = (long long)d.nx * (d.ny < d.nz ? d.ny : d.nz);
+    const long long cnt = corrected ? nxz : (long long)d.nx * (d.ny < d.nz ? d.ny : d.nz);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cnt; i += (long long)gridDim.x * blockDim.x) {
         const double pxb1 = wg[0 * nxz + i], pxb2 = wg[1 * nxz + i], pxt1 = wg[2 * nxz + i], pxt2 = wg[3 * nxz + i];
         const double pzb1 = wg[4 * nxz + i], pzt1 = wg[5 * nxz + i];
         walls[0 * nxz + i] += (9 * pxt1 - pxt2) / 8;   // ut
         walls[1 * nxz + i] += (9 * pxb1 - pxb2) / 8;   // ub
-        walls[2 * nxz + i] += (9 * pzt1 - pxt2) / 8;   // wt (pzt2 = phidtx[...])
-        walls[3 * nxz + i] += (9 * pzb1 - pxb2) / 8;   // wb (pzb2 = phidtx[...])
+        const double pzt2 = corrected ? wg[7 * nxz + i] : pxt2;  // the reference reads phidtx here
+        const double pzb2 = corrected ? wg[6 * nxz + i] : pxb2;
+        walls[2 * nxz + i] += (9 * pzt1 - pzt2) / 8;   // wt
+        walls[3 * nxz + i] += (9 * pzb1 - pzb2) / 8;   // wb
     }
 }
 
@@ -661,8 +664,8 @@ void launch_grad_sub(const Dims& d, T* u, T* v, T* w, const T* phi, T* wallgrad,
                      float* v32, float* w32) {
     k_grad_sub<T><<<grid3(d), block3(), 0, s>>>(d, u, v, w, phi, wallgrad, u32, v32, w32);
 }
-void launch_wall_update(const Dims& d, double* walls, const double* wallgrad, cudaStream_t s) {
-    k_wall_update<<<ew_blocks((long long)d.nx * d.nz), 256, 0, s>>>(d, walls, wallgrad);
+void launch_wall_update(const Dims& d, double* walls, const double* wallgrad, cudaStream_t s, int corrected) {
+    k_wall_update<<<ew_blocks((long long)d.nx * d.nz), 256, 0, s>>>(d, walls, wallgrad, corrected);
 }
 template <typename T, typename TF, typename TA>
 void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const TF* f, const TA* adv, const double* top,

@@ -888,7 +888,7 @@ int substep(afmib_solver* s) {
     }
     if (d.channel) {
         ProfScope ps(s, P_WALL, 10.0 * s->nxz() * sizeof(double));
-        launch_wall_update(d, s->walls, s->wallgrad, s->st);
+        launch_wall_update(d, s->walls, s->wallgrad, s->st, s->cfg.walls_corrected);
     }
     const long long nxz = s->nxz();
     const double* ut = s->walls;
@@ -1561,6 +1561,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_WARM_EXTRAP")) s->warm_extrap = std::string(e) == "1";
     if (const char* e = std::getenv("AFMIB_GRAPHS")) s->use_graphs = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_ALTERNATE")) s->alternate = std::string(e) != "0";
+    if (g.walls_corrected != 0 && g.walls_corrected != 1) return s->fail(AFMIB_ERR_ARG, "walls_corrected must be 0 or 1");
     if (g.proj_start < AFMIB_START_DEFAULT || g.proj_start > AFMIB_START_WARM)
         return s->fail(AFMIB_ERR_ARG, "proj_start must be AFMIB_START_DEFAULT, _ZERO or _WARM");
     s->warm_start = g.proj_start == AFMIB_START_WARM || (g.proj_start == AFMIB_START_DEFAULT && s->mixed);
@@ -1594,7 +1595,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
         TRY(dalloc(s, &s->phi_prev2[1], N));
     }
     TRY(dalloc(s, &s->walls, 4 * s->nxz()));
-    TRY(dalloc(s, &s->wallgrad, 6 * s->nxz()));
+    TRY(dalloc(s, &s->wallgrad, 8 * s->nxz()));
     TRY(dalloc(s, &s->cg_r, N));
     TRY(dalloc(s, &s->cg_p, N));
     TRY(dalloc(s, &s->cg_q, N));
@@ -1607,7 +1608,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     CK(cudaMemsetAsync(s->red.ticket, 0, sizeof(unsigned), s->st));
     CK(cudaMemsetAsync(s->dflag, 0, 4 * sizeof(int), s->st));
     CK(cudaMemsetAsync(s->walls, 0, 4 * s->nxz() * sizeof(double), s->st));
-    CK(cudaMemsetAsync(s->wallgrad, 0, 6 * s->nxz() * sizeof(double), s->st));
+    CK(cudaMemsetAsync(s->wallgrad, 0, 8 * s->nxz() * sizeof(double), s->st));
     CK(cudaMemsetAsync(s->u, 0, N * sizeof(double), s->st));
     CK(cudaMemsetAsync(s->v, 0, N * sizeof(double), s->st));
     CK(cudaMemsetAsync(s->w, 0, N * sizeof(double), s->st));
@@ -1942,7 +1943,7 @@ int afmib_save(afmib_solver* s, const char* path) {
     TRY(to_host(s, walls, s->walls, 4 * nxz));
     // the wall rows of the last projection's gradient, which the next
     // sub-step's wall update uses (channel)
-    TRY(to_host(s, wallgrad, s->wallgrad, 6 * nxz));
+    TRY(to_host(s, wallgrad, s->wallgrad, 8 * nxz));
     if (M > 0) {
         TRY(to_host(s, X, s->X, 3 * M));
         TRY(to_host(s, nstart, s->nstart, M + 1));
@@ -2002,7 +2003,7 @@ int afmib_load(afmib_solver* s, const char* path) {
         return it->second.f64();
     };
     const double *u = f64("u", N), *v = f64("v", N), *w = f64("w", N), *phi = f64("phi", N),
-                 *walls = f64("walls", 4 * nxz), *wallgrad = f64("wallgrad", 6 * nxz);
+                 *walls = f64("walls", 4 * nxz), *wallgrad = f64("wallgrad", 8 * nxz);
     if (!u || !v || !w || !phi || !walls || !wallgrad)
         return s->fail(AFMIB_ERR_ARG, "snapshot sections missing or of the wrong size");
     CK(cudaMemcpyAsync(s->u, u, N * sizeof(double), cudaMemcpyHostToDevice, s->st));
@@ -2010,7 +2011,7 @@ int afmib_load(afmib_solver* s, const char* path) {
     CK(cudaMemcpyAsync(s->w, w, N * sizeof(double), cudaMemcpyHostToDevice, s->st));
     CK(cudaMemcpyAsync(s->lv[0].x, phi, N * sizeof(double), cudaMemcpyHostToDevice, s->st));
     CK(cudaMemcpyAsync(s->walls, walls, 4 * nxz * sizeof(double), cudaMemcpyHostToDevice, s->st));
-    CK(cudaMemcpyAsync(s->wallgrad, wallgrad, 6 * nxz * sizeof(double), cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(s->wallgrad, wallgrad, 8 * nxz * sizeof(double), cudaMemcpyHostToDevice, s->st));
     TRY(refresh_shadow(s));
     for (int k = 0; k < 2; ++k) {
         const double* pp = f64(k == 0 ? "phi_prev0" : "phi_prev1", N);

@@ -72,6 +72,10 @@ typedef struct afmib_config {
                            reference's nested iteration, src/mg/solver.h:201-216; mixed: warm),
                            AFMIB_START_ZERO, or AFMIB_START_WARM (the previous pressure of the same
                            sub-step kind, BE or CN) */
+    int walls_corrected; /* channel wall-velocity update after each projection: 0 the reference's
+                           (src/ns/projection.h:86-104, its loop over nx*ny entries and its w rows
+                           reading the x-gradient), 1 corrected (all nx*nz entries, w rows from the
+                           z-gradient) */
 } afmib_config;
 
 enum { AFMIB_START_DEFAULT = 0, AFMIB_START_ZERO = 1, AFMIB_START_WARM = 2 };

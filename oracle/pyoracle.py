@@ -47,6 +47,7 @@ def lib():
         L.orc_ns_create.argtypes = [_ip, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_int, _dp, _dp, _dp]
         L.orc_ns_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_ns_set_walls_corrected.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_ns_step.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_ns_get.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp]
         L.orc_ns_set.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
@@ -171,7 +172,7 @@ def mg_solve(g, rhs, tol, nu1=2, nu2=2, maxit=1000, levels=None):
 class NSSolver:
     """ns::solver restated (src/ns/solver.h:61-140); projects the initial field on construction."""
 
-    def __init__(self, g, mu, rho, dt, tol, u0, v0, w0, maxit=10000, levels=None):
+    def __init__(self, g, mu, rho, dt, tol, u0, v0, w0, maxit=10000, levels=None, walls_corrected=False):
         self.g = g
         self.dt = dt
         lv = g.levels() if levels is None else levels
@@ -181,6 +182,7 @@ class NSSolver:
                                      _p(np.ascontiguousarray(w0, dtype=np.float64)))
         nxz = g.nx * g.nz
         self.walls = np.zeros(4 * nxz)
+        lib().orc_ns_set_walls_corrected(self.h, 1 if walls_corrected else 0)
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -574,6 +574,7 @@ struct NS {
     vec u_old, v_old, w_old, ua, va, wa;
     vec phidt, phx, phy, phz;    // projection state
     bool half = false;
+    bool walls_corrected = false;  // all nx*nz entries, w rows from the z-gradient
     int status = 0;
     long cg_iters = 0, mg_cycles = 0;
 
@@ -595,16 +596,19 @@ struct NS {
     }
 
     // src/ns/projection.h:75-122 — including its two index slips (loop bound
-    // nx*ny, and pzb2/pzt2 read phidtx); channel mode only.
+    // nx*ny, and pzb2/pzt2 read phidtx); channel mode only. walls_corrected:
+    // the loop covers nx*nz and pzb2/pzt2 read phidtz.
     void wall_boundary(double* ut, double* ub, double* wt, double* wb) {
         if (!g.channel) return;
         const int nx = g.nx, ny = g.ny;
         if (ny > 1) {
-            for (long i = 0; i < (long)nx * ny; ++i) {
+            const long cnt = walls_corrected ? (long)nx * g.nz : (long)nx * ny;
+            const vec& pz2 = walls_corrected ? phz : phx;
+            for (long i = 0; i < cnt; ++i) {
                 const long x = i % nx, z = i / nx;
                 const long ixzb = x + (long)nx * ny * z, ixzt = x + (long)nx * ((long)ny * (z + 1) - 1);
                 const double pxb1 = phx[ixzb], pxb2 = phx[ixzb + nx], pxt1 = phx[ixzt], pxt2 = phx[ixzt - nx],
-                             pzb1 = phz[ixzb], pzb2 = phx[ixzb + nx], pzt1 = phz[ixzt], pzt2 = phx[ixzt - nx];
+                             pzb1 = phz[ixzb], pzb2 = pz2[ixzb + nx], pzt1 = phz[ixzt], pzt2 = pz2[ixzt - nx];
                 ut[i] += (9 * pxt1 - pxt2) / 8;
                 ub[i] += (9 * pxb1 - pxb2) / 8;
                 wt[i] += (9 * pzt1 - pzt2) / 8;
@@ -907,6 +911,8 @@ int orc_mg_solve(const int* dims, int levels, double* rhs, double tol, int nu1, 
     std::memcpy(rhs, r.data(), r.size() * sizeof(double));
     return st;
 }
+
+void orc_ns_set_walls_corrected(void* h, int corrected) { static_cast<NS*>(h)->walls_corrected = corrected != 0; }
 
 void* orc_ns_create(const int* dims, int levels, double mu, double rho, double dt, double tol, int maxit,
                     const double* u0, const double* v0, const double* w0) {

@@ -566,3 +566,34 @@ def test_spread_dense_cluster_takes_large_capacity_pass(m):
     for comp, f in enumerate((fx, fy, fz)):
         assert rel(f, po.spread(g, comp, X, F[comp])) < OPS_TOL
         assert np.array_equal(f, again[comp])
+
+
+@pytest.mark.parametrize("dims", [(16, 8, 16), (16, 16, 8)])
+@pytest.mark.parametrize("corrected", [0, 1])
+def test_channel_walls_noncubic(dims, corrected):
+    """Channel sub-steps on non-cubic grids, the wall-velocity update in the
+    reference's form (its loop over nx*ny entries; only grids with ny <= nz,
+    where that loop stays inside the arrays) or corrected (every nx*nz entry,
+    w rows from the z-gradient), against the oracle in the same mode."""
+    nx, ny, nz = dims
+    if not corrected and ny > nz:
+        pytest.skip("the reference's loop reads past the gradient arrays when ny > nz")
+    g = po.Grid(nx, ny, nz, nx, channel=True)
+    rng = np.random.default_rng(42)
+    u, v, w = 0.1 * rng.standard_normal(g.ncell), 0.1 * rng.standard_normal(g.nv), 0.1 * rng.standard_normal(g.ncell)
+    f = [rng.standard_normal(g.ncell), rng.standard_normal(g.nv), rng.standard_normal(g.ncell)]
+    mu, rho, dt, tol = 0.01, 1.0, 1e-3, 1e-12
+    ref = po.NSSolver(g, mu, rho, dt, tol, u, v, w, walls_corrected=bool(corrected))
+    for _ in range(4):
+        assert ref.step(*f) == 0
+    ru, rv, rw, _ = ref.get()
+    with capi.Solver(nx, ny, nz, n=nx, bc=capi.BC_CHANNEL, mu=mu, rho=rho, dt=dt, tol=tol,
+                     walls_corrected=corrected) as sv:
+        sv.set_velocity(u, v, w)
+        sv.project()
+        for _ in range(4):
+            sv.ns_step(*f)
+        gu, gv, gw = sv.get_velocity()
+        walls = np.concatenate(sv.get_walls())
+    assert rel(gu, ru) < TOL and rel(gv, rv) < TOL and rel(gw, rw) < TOL
+    assert rel(walls, ref.walls) < TOL
