@@ -44,7 +44,8 @@ class Config(ctypes.Structure):
                 ("nu1", ctypes.c_int), ("nu2", ctypes.c_int), ("mu", ctypes.c_double), ("rho", ctypes.c_double),
                 ("dt", ctypes.c_double), ("tol", ctypes.c_double), ("max_cg_iters", ctypes.c_int),
                 ("max_mg_cycles", ctypes.c_int), ("k_spring", ctypes.c_double), ("inner_tol", ctypes.c_double),
-                ("ib_fp32", ctypes.c_int), ("proj_start", ctypes.c_int), ("walls_corrected", ctypes.c_int)]
+                ("ib_fp32", ctypes.c_int), ("proj_start", ctypes.c_int), ("walls_corrected", ctypes.c_int),
+                ("k_bend", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -90,6 +91,7 @@ _SIGS = {
     "afmib_spread": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "afmib_interp": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "afmib_set_spring": ([_vp, ctypes.c_double], ctypes.c_int),
+    "afmib_set_bending": ([_vp, ctypes.c_double], ctypes.c_int),
     "afmib_set_tolerance": ([_vp, ctypes.c_double], ctypes.c_int),
     "afmib_smooth": ([_vp, _vp, _vp], ctypes.c_int),
     "afmib_helmholtz_cg_noalloc": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -169,12 +171,12 @@ class Solver:
 
     def __init__(self, nx, ny=None, nz=None, *, n=None, bc=BC_PERIODIC, precision=FP64, mu=0.01, rho=1.0, dt=1e-4,
                  tol=1e-10, mg_levels=0, nu1=2, nu2=2, max_cg_iters=1000, max_mg_cycles=200, k_spring=0.0,
-                 inner_tol=0.0, ib_fp32=0, proj_start=0, walls_corrected=0, stream=None):
+                 inner_tol=0.0, ib_fp32=0, proj_start=0, walls_corrected=0, k_bend=0.0, stream=None):
         self.lib = load()
         ny = nx if ny is None else ny
         nz = nx if nz is None else nz
         self.cfg = Config(nx, ny, nz, n or nx, bc, precision, mg_levels, nu1, nu2, mu, rho, dt, tol, max_cg_iters,
-                          max_mg_cycles, k_spring, inner_tol, ib_fp32, proj_start, walls_corrected)
+                          max_mg_cycles, k_spring, inner_tol, ib_fp32, proj_start, walls_corrected, k_bend)
         self.nx, self.ny, self.nz = nx, ny, nz
         self.channel = bc == BC_CHANNEL
         h = _vp()
@@ -290,6 +292,9 @@ class Solver:
     # adjoint
     def set_spring(self, k):
         self._ck(self.lib.afmib_set_spring(self.h, float(k)))
+
+    def set_bending(self, kb):
+        self._ck(self.lib.afmib_set_bending(self.h, float(kb)))
 
     def trajectory_forward(self, nsteps, ckpt_every):
         self._ck(self.lib.afmib_trajectory_forward(self.h, nsteps, ckpt_every))

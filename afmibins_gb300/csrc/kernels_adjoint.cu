@@ -161,7 +161,39 @@ __global__ void k_springs_adjoint(int M, const double* __restrict__ X, const int
     dk_part[i] = li[0] * kx[0] + li[1] * kx[1] + li[2] * kx[2];
 }
 
+// Bending part of the marker-force adjoint: gX += -kb L (L lamG) (L
+// symmetric), in two passes through Z = L lamG (stored like lamG).
+__global__ void k_lap_soa(int M, const double* __restrict__ lam, const int* __restrict__ ns,
+                          const int* __restrict__ ni, double* __restrict__ Z) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    for (int a = 0; a < 3; ++a) {
+        const double li = lam[(size_t)a * M + i];
+        double z = 0;
+        for (int e = ns[i]; e < ns[i + 1]; ++e) z += lam[(size_t)a * M + ni[e]] - li;
+        Z[(size_t)a * M + i] = z;
+    }
+}
+__global__ void k_bend_adjoint(int M, const double* __restrict__ Z, const int* __restrict__ ns,
+                               const int* __restrict__ ni, double kb, double* __restrict__ gX) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    for (int a = 0; a < 3; ++a) {
+        const double zi = Z[(size_t)a * M + i];
+        double b = 0;
+        for (int e = ns[i]; e < ns[i + 1]; ++e) b += Z[(size_t)a * M + ni[e]] - zi;
+        gX[3 * i + a] += -kb * b;
+    }
+}
+
 }  // namespace
+
+void launch_bending_adjoint(int M, const int* ns, const int* ni, double kb, const double* lamG, double* Z, double* gX,
+                            cudaStream_t s) {
+    if (M <= 0) return;
+    k_lap_soa<<<(M + 255) / 256, 256, 0, s>>>(M, lamG, ns, ni, Z);
+    k_bend_adjoint<<<(M + 255) / 256, 256, 0, s>>>(M, Z, ns, ni, kb, gX);
+}
 
 void launch_advect_adjoint(const Dims& d, double* ou, double* ov, double* ow, const double* u, const double* v,
                            const double* w, const double* lu, const double* lv, const double* lw, int acc,

@@ -15,6 +15,10 @@ void launch_marker_grad(const Dims& d, int M, const double* X, const double* g, 
                         const double* Fw, double scale, double* gX, cudaStream_t s);
 
 // gX += k K^T lamG (symmetric lists); dk_part[i] = lamG_i . (K X)_i
+// gX += -kb L (L lamG): the bending term of the marker-force adjoint
+// (lamG per component, gX like X; Z: 3M doubles of workspace)
+void launch_bending_adjoint(int M, const int* ns, const int* ni, double kb, const double* lamG, double* Z, double* gX,
+                            cudaStream_t s);
 void launch_springs_adjoint(int M, const double* X, const int* ns, const int* ni, double kspring, const double* lamG,
                             double* gX, double* dk_part, cudaStream_t s);
 

@@ -52,6 +52,42 @@ __global__ void k_springs(int M, const double* __restrict__ X, const int* __rest
     G[2 * M + i] = T(k * sz);
 }
 
+// Y = L X per marker (L the graph Laplacian of the spring lists), stored
+// like X: Y_i = sum_{j in N(i)} (X_j - X_i)
+__global__ void k_lap_aos(int M, const double* __restrict__ X, const int* __restrict__ ns, const int* __restrict__ ni,
+                          double* __restrict__ Y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    const double xi = X[3 * i], yi = X[3 * i + 1], zi = X[3 * i + 2];
+    double sx = 0, sy = 0, sz = 0;
+    for (int e = ns[i]; e < ns[i + 1]; ++e) {
+        const int j = ni[e];
+        sx += X[3 * j] - xi;
+        sy += X[3 * j + 1] - yi;
+        sz += X[3 * j + 2] - zi;
+    }
+    Y[3 * i] = sx;
+    Y[3 * i + 1] = sy;
+    Y[3 * i + 2] = sz;
+}
+
+// Springs plus bending from Y = L X: G_i = ks Y_i - kb (L Y)_i. The bending
+// term is the force of the discrete energy kb/2 sum_i |(L X)_i|^2 (with
+// symmetric lists L is symmetric, so the gradient is kb L L X).
+template <typename T>
+__global__ void k_spring_bend(int M, const double* __restrict__ Y, const int* __restrict__ ns,
+                              const int* __restrict__ ni, double ks, double kb, T* __restrict__ G) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    const double yi[3] = {Y[3 * i], Y[3 * i + 1], Y[3 * i + 2]};
+    double b[3] = {0, 0, 0};
+    for (int e = ns[i]; e < ns[i + 1]; ++e) {
+        const int j = ni[e];
+        for (int a = 0; a < 3; ++a) b[a] += Y[3 * j + a] - yi[a];
+    }
+    for (int a = 0; a < 3; ++a) G[(size_t)a * M + i] = T(ks * yi[a] - kb * b[a]);
+}
+
 // Per marker: bin key, wrapped cell, and for each axis and offset variant
 // (0: faces on integer positions, 1: on half-integers) the base offset
 // (first face - cell) and the four weights phi/n.
@@ -518,6 +554,13 @@ __global__ void k_marker_axpy(int M, double* __restrict__ Xo, const double* __re
 }  // namespace
 
 template <typename T>
+void launch_springs_bending(int M, const double* X, const int* nstart, const int* nidx, double ks, double kb,
+                            double* Y, T* G, cudaStream_t s) {
+    if (M <= 0) return;
+    k_lap_aos<<<(M + 255) / 256, 256, 0, s>>>(M, X, nstart, nidx, Y);
+    k_spring_bend<T><<<(M + 255) / 256, 256, 0, s>>>(M, Y, nstart, nidx, ks, kb, G);
+}
+template <typename T>
 void launch_springs(int M, const double* X, const int* nstart, const int* nidx, double k, T* G, cudaStream_t s) {
     if (M > 0) k_springs<T><<<(M + 255) / 256, 256, 0, s>>>(M, X, nstart, nidx, k, G);
 }
@@ -632,6 +675,8 @@ void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, do
 
 #define AFMIB_IB_INST(T)                                                                                        \
     template void launch_springs<T>(int, const double*, const int*, const int*, double, T*, cudaStream_t);       \
+    template void launch_springs_bending<T>(int, const double*, const int*, const int*, double, double, double*, T*, \
+                                            cudaStream_t);                                                         \
     template void launch_marker_prep<T>(const Dims&, int, int, const double*, unsigned*, int*, MarkerW<T>, int*, \
                                         cudaStream_t);                                                           \
     template size_t spread_smem_bytes<T>(int, int, int);                                                             \

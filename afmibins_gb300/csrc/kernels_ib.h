@@ -18,6 +18,12 @@ struct MarkerW {
 
 template <typename T>
 void launch_springs(int M, const double* X, const int* nstart, const int* nidx, double k, T* G, cudaStream_t s);
+// Springs plus bending: G = ks L X - kb L (L X), with Y (3M doubles) the
+// workspace that receives L X; the bending term is the force of the discrete
+// membrane energy kb/2 sum_i |(L X)_i|^2.
+template <typename T>
+void launch_springs_bending(int M, const double* X, const int* nstart, const int* nidx, double ks, double kb,
+                            double* Y, T* G, cudaStream_t s);
 
 // keys = tile * TS^2 TZ + cell-in-tile (TZ = TS, or 1 on a 2D grid), vals =
 // marker index; flag set to 1 when a marker is within 2.5h of a channel wall,

@@ -137,6 +137,7 @@ struct afmib_solver {
     // markers
     int M = 0, Mcap = 0, nnz_cap = 0;
     double *X = nullptr, *Xh = nullptr, *U1 = nullptr, *U2 = nullptr, *G = nullptr, *mvol = nullptr;
+    double* Ybend = nullptr;  // L X (or L lamG in the adjoint) for the bending force
     int *nstart = nullptr, *nidx = nullptr;
     bool has_vol = false;
     unsigned *keys = nullptr, *keys2 = nullptr, *hist = nullptr;
@@ -1011,6 +1012,7 @@ int marker_alloc(afmib_solver* s, int M, int nnz) {
         TRY(regrow(s, &s->nstart, (size_t)M + 1, keep ? keep + 1 : 0));
         TRY(regrow(s, &s->mvol, (size_t)M, keep));
         TRY(regrow(s, &s->Xh, 3 * (size_t)M, 0));
+        TRY(regrow(s, &s->Ybend, 3 * (size_t)M, 0));
         TRY(regrow(s, &s->U1, 3 * (size_t)M, 0));
         TRY(regrow(s, &s->U2, 3 * (size_t)M, 0));
         TRY(regrow(s, &s->G, 3 * (size_t)M, 0));
@@ -1181,8 +1183,15 @@ int ib_one_step(afmib_solver* s) {
     const bool in32 = s->mixed && !s->interp64;
     auto springs = [&](const double* P) {
         ProfScope ps(s, P_SPRINGS, mbytes);
-        if (sp32) launch_springs<float>(M, P, s->nstart, s->nidx, s->cfg.k_spring, s->G32, s->st);
-        else launch_springs<double>(M, P, s->nstart, s->nidx, s->cfg.k_spring, s->G, s->st);
+        const double ks = s->cfg.k_spring, kb = s->cfg.k_bend;
+        if (kb != 0.0) {
+            if (sp32) launch_springs_bending<float>(M, P, s->nstart, s->nidx, ks, kb, s->Ybend, s->G32, s->st);
+            else launch_springs_bending<double>(M, P, s->nstart, s->nidx, ks, kb, s->Ybend, s->G, s->st);
+        } else if (sp32) {
+            launch_springs<float>(M, P, s->nstart, s->nidx, ks, s->G32, s->st);
+        } else {
+            launch_springs<double>(M, P, s->nstart, s->nidx, ks, s->G, s->st);
+        }
     };
     auto bin = [&](const double* P) -> int {
         TRY(bin_markers(s, P, sp32));
@@ -1359,6 +1368,15 @@ int traj_forward(afmib_solver* s, int nsteps, int every) {
     return sync(s);
 }
 
+// FP64 marker forces G (per component) at positions P: springs, plus bending
+// when the configuration has it
+void marker_forces(afmib_solver* s, const double* P, double* G) {
+    if (s->cfg.k_bend != 0.0)
+        launch_springs_bending<double>(s->M, P, s->nstart, s->nidx, s->cfg.k_spring, s->cfg.k_bend, s->Ybend, G, s->st);
+    else
+        launch_springs<double>(s->M, P, s->nstart, s->nidx, s->cfg.k_spring, G, s->st);
+}
+
 // Reverse of one IB step over record j: (L = lam_u^{n+1}, lamX = lam_X^{n+1})
 // -> (lam_u^n, lam_X^n), lam_k accumulated in *lam_k.
 int adjoint_step(afmib_solver* s, int j, double* lam_k) {
@@ -1395,7 +1413,7 @@ int adjoint_step(afmib_solver* s, int j, double* lam_k) {
     CKL();
     // fh = S(Xh) Gh with Gh = k K Xh; lam_fh = (dt/rho) R
     TRY(bin_markers(s, Xh, false));
-    launch_springs<double>(M, Xh, s->nstart, s->nidx, kk, s->Gtmp, s->st);
+    marker_forces(s, Xh, s->Gtmp);
     TRY(interp_markers(s, F(R, 0), F(R, 1), F(R, 2), s->Ubuf, false));
     CK(cudaMemsetAsync(s->lamG, 0, 3 * (size_t)M * sizeof(double), s->st));
     launch_axpy<double>(3 * (long long)M, s->lamG, s->Ubuf, n3 * dt / rho, s->st);
@@ -1404,6 +1422,8 @@ int adjoint_step(afmib_solver* s, int j, double* lam_k) {
         ProfScope ps(s, P_ADJ_MARKER, (double)M * 400, 2);
         launch_marker_grad(d, M, Xh, s->Gtmp, F(R, 0), F(R, 1), F(R, 2), n3 * dt / rho, s->lamXh, s->st);
         launch_springs_adjoint(M, Xh, s->nstart, s->nidx, kk, s->lamG, s->lamXh, s->dkp, s->st);
+        if (s->cfg.k_bend != 0.0)
+            launch_bending_adjoint(M, s->nstart, s->nidx, s->cfg.k_bend, s->lamG, s->Ybend, s->lamXh, s->st);
     }
     launch_sum<double>(M, s->dkp, s->red, s->scal + 11, s->st);
     CKL();
@@ -1434,7 +1454,7 @@ int adjoint_step(afmib_solver* s, int j, double* lam_k) {
                               F(T, 2), 1, s->st);
     }
     // f0 = S(X0) G0, lam_f0 = dt/(2 rho) R (bins of X0 are current)
-    launch_springs<double>(M, X0, s->nstart, s->nidx, kk, s->Gtmp, s->st);
+    marker_forces(s, X0, s->Gtmp);
     TRY(interp_markers(s, F(R, 0), F(R, 1), F(R, 2), s->Ubuf, false));
     CK(cudaMemsetAsync(s->lamG, 0, 3 * (size_t)M * sizeof(double), s->st));
     launch_axpy<double>(3 * (long long)M, s->lamG, s->Ubuf, n3 * dt / (2 * rho), s->st);
@@ -1442,6 +1462,8 @@ int adjoint_step(afmib_solver* s, int j, double* lam_k) {
         ProfScope ps(s, P_ADJ_MARKER, (double)M * 400, 2);
         launch_marker_grad(d, M, X0, s->Gtmp, F(R, 0), F(R, 1), F(R, 2), n3 * dt / (2 * rho), s->lamX, s->st);
         launch_springs_adjoint(M, X0, s->nstart, s->nidx, kk, s->lamG, s->lamX, s->dkp, s->st);
+        if (s->cfg.k_bend != 0.0)
+            launch_bending_adjoint(M, s->nstart, s->nidx, s->cfg.k_bend, s->lamG, s->Ybend, s->lamX, s->st);
     }
     launch_sum<double>(M, s->dkp, s->red, s->scal + 11, s->st);
     CKL();
@@ -2246,6 +2268,12 @@ int afmib_smooth(afmib_solver* s, double* x, const double* b) {
 int afmib_set_spring(afmib_solver* s, double k) {
     if (!s) return AFMIB_ERR_ARG;
     s->cfg.k_spring = k;
+    return AFMIB_OK;
+}
+
+int afmib_set_bending(afmib_solver* s, double kb) {
+    if (!s) return AFMIB_ERR_ARG;
+    s->cfg.k_bend = kb;
     return AFMIB_OK;
 }
 

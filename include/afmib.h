@@ -76,6 +76,9 @@ typedef struct afmib_config {
                            (src/ns/projection.h:86-104, its loop over nx*ny entries and its w rows
                            reading the x-gradient), 1 corrected (all nx*nz entries, w rows from the
                            z-gradient) */
+    double k_bend;      /* bending stiffness of the membrane: force -k_bend L (L X) of the energy
+                           k_bend/2 sum_i |(L X)_i|^2, L the graph Laplacian of the spring lists
+                           (0: springs only; the reference has no membrane mechanics) */
 } afmib_config;
 
 enum { AFMIB_START_DEFAULT = 0, AFMIB_START_ZERO = 1, AFMIB_START_WARM = 2 };
@@ -148,6 +151,8 @@ int afmib_load(afmib_solver* s, const char* path);
 
 /* Spring stiffness k of the membrane (G_i = k * sum_j (X_j - X_i)). */
 int afmib_set_spring(afmib_solver* s, double k);
+/* Bending stiffness of the membrane (afmib_config.k_bend). */
+int afmib_set_bending(afmib_solver* s, double kb);
 
 /* ---- adjoint (no reference counterpart: the reference has no adjoint) ----
  * afmib_trajectory_forward runs nsteps IB steps from the current state and

@@ -48,6 +48,8 @@ def lib():
                                     ctypes.c_double, ctypes.c_int, _dp, _dp, _dp]
         L.orc_ns_destroy.argtypes = [ctypes.c_void_p]
         L.orc_ns_set_walls_corrected.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_ns_set_bending.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.orc_membrane_forces.argtypes = [ctypes.c_long, _dp, _ip, _ip, ctypes.c_double, ctypes.c_double, _dp]
         L.orc_ns_step.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_ns_get.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp]
         L.orc_ns_set.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
@@ -206,8 +208,9 @@ class NSSolver:
         lib().orc_ns_counters(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
         return a.value, b.value, c.value
 
-    def ib_step(self, X, nstart, nidx, k):
+    def ib_step(self, X, nstart, nidx, k, kb=0.0):
         X = np.ascontiguousarray(X, dtype=np.float64)
+        lib().orc_ns_set_bending(self.h, kb)
         st = lib().orc_ib_step(self.h, X.shape[0], _p(X), _pi(nstart), _pi(nidx), k, _p(self.walls))
         return X, st
 
@@ -262,3 +265,12 @@ def run_ref(cmd, arrays, L, M=256, W=1, H=1, D=1, timeout=3600):
         flat.tofile(fi)
         subprocess.run([exe, cmd, fi, fo], check=True, timeout=timeout)
         return np.fromfile(fo, dtype=np.float64)
+
+
+def membrane_forces(X, nstart, nidx, k, kb):
+    """G (3, M): springs k L X plus bending -kb L (L X)."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    M = X.shape[0]
+    G = np.zeros(3 * M)
+    lib().orc_membrane_forces(M, _p(X), _pi(nstart), _pi(nidx), k, kb, _p(G))
+    return G.reshape(3, M)

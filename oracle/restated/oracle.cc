@@ -575,6 +575,7 @@ struct NS {
     vec phidt, phx, phy, phz;    // projection state
     bool half = false;
     bool walls_corrected = false;  // all nx*nz entries, w rows from the z-gradient
+    double k_bend = 0.0;           // membrane bending stiffness (IB steps)
     int status = 0;
     long cg_iters = 0, mg_cycles = 0;
 
@@ -913,6 +914,27 @@ int orc_mg_solve(const int* dims, int levels, double* rhs, double tol, int nu1, 
 }
 
 void orc_ns_set_walls_corrected(void* h, int corrected) { static_cast<NS*>(h)->walls_corrected = corrected != 0; }
+void orc_ns_set_bending(void* h, double kb) { static_cast<NS*>(h)->k_bend = kb; }
+
+// Membrane forces with bending, G = k L X - kb L (L X) (per component): the
+// springs plus the force of the energy kb/2 sum_i |(L X)_i|^2, L the graph
+// Laplacian of the (symmetric) neighbour lists. The reference has no
+// membrane mechanics (test/ib_ns_test.cc:80-90 leaves them to the user).
+void orc_membrane_forces(long M, const double* X, const int* nstart, const int* nidx, double k, double kb, double* G) {
+    vec Y(3 * M);
+    for (long i = 0; i < M; ++i) {
+        double acc[3] = {0, 0, 0};
+        for (int e = nstart[i]; e < nstart[i + 1]; ++e)
+            for (int a = 0; a < 3; ++a) acc[a] += X[3 * (long)nidx[e] + a] - X[3 * i + a];
+        for (int a = 0; a < 3; ++a) Y[3 * i + a] = acc[a];
+    }
+    for (long i = 0; i < M; ++i) {
+        double b[3] = {0, 0, 0};
+        for (int e = nstart[i]; e < nstart[i + 1]; ++e)
+            for (int a = 0; a < 3; ++a) b[a] += Y[3 * (long)nidx[e] + a] - Y[3 * i + a];
+        for (int a = 0; a < 3; ++a) G[a * M + i] = k * Y[3 * i + a] - kb * b[a];
+    }
+}
 
 void* orc_ns_create(const int* dims, int levels, double mu, double rho, double dt, double tol, int maxit,
                     const double* u0, const double* v0, const double* w0) {
@@ -991,7 +1013,8 @@ int orc_ib_step(void* h, long M, double* X, const int* nstart, const int* nidx, 
     vec z4(4 * nxz, 0.0);
     double* wl = walls ? walls : z4.data();
     auto force = [&](const vec& P) {
-        springs(M, P.data(), nstart, nidx, k, G.data());
+        if (s->k_bend != 0.0) orc_membrane_forces(M, P.data(), nstart, nidx, k, s->k_bend, G.data());
+        else springs(M, P.data(), nstart, nidx, k, G.data());
         spread(g, 0, fx.data(), M, P.data(), G.data(), nullptr);
         spread(g, 1, fy.data(), M, P.data(), G.data() + M, nullptr);
         spread(g, 2, fz.data(), M, P.data(), G.data() + 2 * M, nullptr);

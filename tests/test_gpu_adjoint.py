@@ -99,3 +99,42 @@ def test_dk_against_oracle_reference():
     h = 1e-6
     ref = (oracle_loss(0.5 + h) - oracle_loss(0.5 - h)) / (2 * h)
     assert abs(gk - ref) / abs(ref) < 1e-6, (gk, ref)
+
+
+def test_adjoint_with_bending_matches_finite_differences():
+    """With membrane bending (k_bend = 0.05: force -k_bend L (L X)) the
+    adjoint carries the bending term's transpose; the gradient agrees with
+    central differences of the forward, 1e-6 relative."""
+    from afmibins_gb300.autograd import ib_trajectory, membrane_loss
+    n, nsteps, every = 16, 4, 2
+    X, nstart, nidx, vel = _case(n, M=200, seed=13)
+    sv = capi.Solver(n, mu=0.01, rho=1.0, dt=2e-3, tol=1e-13, k_spring=0.5, k_bend=0.05, max_cg_iters=2000)
+    sv.set_velocity(*vel)
+    sv.project()
+    vel0 = sv.get_velocity()
+    sv.set_markers(X, nstart, nidx)
+    dev = torch.device("cuda")
+    h3 = 1.0 / n ** 3
+    X0 = torch.tensor(X, device=dev, requires_grad=True)
+    k = torch.tensor(0.5, dtype=torch.float64, device=dev, requires_grad=True)
+    uN, XN = ib_trajectory(k, X0, sv, vel0, nsteps, every)
+    membrane_loss(uN, XN, X0, h3).backward()
+    gk, gX = float(k.grad), X0.grad.cpu().numpy()
+
+    def loss(kv, Xv):
+        with torch.no_grad():
+            Xt = torch.tensor(Xv, device=dev)
+            uN, XN = ib_trajectory(torch.tensor(kv, dtype=torch.float64), Xt, sv, vel0, nsteps, every)
+            return float(membrane_loss(uN, XN, Xt, h3))
+
+    rng = np.random.default_rng(19)
+    h, worst = 1e-6, 0.0
+    for _ in range(8):
+        dX = rng.standard_normal(X.shape)
+        dX /= np.linalg.norm(dX)
+        dk = rng.standard_normal()
+        fd = (loss(0.5 + h * dk, X + h * dX) - loss(0.5 - h * dk, X - h * dX)) / (2 * h)
+        ad = gk * dk + float((gX * dX).sum())
+        worst = max(worst, abs(fd - ad) / max(abs(fd), 1e-30))
+    sv.close()
+    assert worst < 1e-6, worst

@@ -597,3 +597,28 @@ def test_channel_walls_noncubic(dims, corrected):
         walls = np.concatenate(sv.get_walls())
     assert rel(gu, ru) < TOL and rel(gv, rv) < TOL and rel(gw, rw) < TOL
     assert rel(walls, ref.walls) < TOL
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
+def test_ib_steps_with_bending_periodic(precision):
+    """IB steps with membrane bending (k_bend: force -k_bend L (L X)) against
+    the oracle: FP64 to 1e-10, the mixed form to its 1e-8 bar."""
+    n = 16
+    g, u, v, w, X, nstart, nidx = _periodic_case(n, M=400, seed=23)
+    mu, rho, dt, tol, k, kb = 0.01, 1.0, 1e-3, 1e-12, 0.5, 0.05
+    ref = po.NSSolver(g, mu, rho, dt, tol, u, v, w)
+    Xr = X.copy()
+    for _ in range(3):
+        Xr, st = ref.ib_step(Xr, nstart, nidx, k, kb)
+        assert st == 0
+    ru, rv, rw, _ = ref.get()
+    with capi.Solver(n, precision=precision, mu=mu, rho=rho, dt=dt, tol=tol, k_spring=k, k_bend=kb) as sv:
+        sv.set_velocity(u, v, w)
+        sv.project()
+        sv.set_markers(X, nstart, nidx)
+        sv.ib_step(3)
+        gu, gv, gw = sv.get_velocity()
+        gX = sv.get_markers()
+    bar = TOL if precision == capi.FP64 else MIXED_TOL
+    assert rel(gu, ru) < bar and rel(gv, rv) < bar and rel(gw, rw) < bar
+    assert rel(gX, Xr) < bar
