@@ -84,6 +84,8 @@ struct afmib_solver {
     // configuration's nu1, nu2 and plain Gauss-Seidel.
     double inner_omega = 1.25;
     int inner_nu1 = 2, inner_nu2 = 1;
+    // the same below the finest level (AFMIB_INNER_NU_COARSE=a,b)
+    int inner_nu1c = 2, inner_nu2c = 1;
     double mg_rho = 0.0;        // measured per-cycle contraction (0: none yet)
     // pipelined red-black sweeps (AFMIB_SMOOTHER=pipe); the default is the
     // batched per-colour launches, measured faster at 256^3
@@ -457,8 +459,8 @@ int vcycle_tail(afmib_solver* s, size_t l) {
     auto& lv = levels<T>(s);
     TailLevels<T> a{};
     a.nlev = (int)(lv.size() - l);
-    a.nu1 = sizeof(T) == sizeof(float) ? s->inner_nu1 : s->cfg.nu1;
-    a.nu2 = sizeof(T) == sizeof(float) ? s->inner_nu2 : s->cfg.nu2;
+    a.nu1 = sizeof(T) == sizeof(float) ? s->inner_nu1c : s->cfg.nu1;
+    a.nu2 = sizeof(T) == sizeof(float) ? s->inner_nu2c : s->cfg.nu2;
     a.maxit = s->cfg.max_cg_iters;
     a.tol = s->cfg.tol;
     for (int k = 0; k < a.nlev; ++k) {
@@ -491,7 +493,7 @@ int vcycle(afmib_solver* s, size_t l) {
         return AFMIB_OK;
     }
     const bool fine = l == 0;
-    TRY(smooth(s, L, sizeof(T) == sizeof(float) ? s->inner_nu1 : s->cfg.nu1));
+    TRY(smooth(s, L, sizeof(T) == sizeof(float) ? (fine ? s->inner_nu1 : s->inner_nu1c) : s->cfg.nu1));
     {
         ProfScope ps(s, fine ? P_RESID0 : P_RESID, 3 * Ns);
         launch_residual<T>(L.d, L.r, L.x, L.b, nullptr, nullptr, s->st, pass_dir(s, L.d, sizeof(T)));
@@ -508,7 +510,7 @@ int vcycle(afmib_solver* s, size_t l) {
         ProfScope ps(s, fine ? P_PROLONG0 : P_PROLONG, 2 * Ns + Ns / 8);
         launch_prolong_add<T>(L.d, L.x, C.x, s->st, pass_dir(s, L.d, sizeof(T)));
     }
-    TRY(smooth(s, L, sizeof(T) == sizeof(float) ? s->inner_nu2 : s->cfg.nu2));
+    TRY(smooth(s, L, sizeof(T) == sizeof(float) ? (fine ? s->inner_nu2 : s->inner_nu2c) : s->cfg.nu2));
     return AFMIB_OK;
 }
 
@@ -1572,8 +1574,15 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_INNER_NU")) {
         int a = 0, b = 0;
         if (std::sscanf(e, "%d,%d", &a, &b) == 2 && a >= 0 && b >= 0 && a + b > 0) {
-            s->inner_nu1 = a;
-            s->inner_nu2 = b;
+            s->inner_nu1 = s->inner_nu1c = a;
+            s->inner_nu2 = s->inner_nu2c = b;
+        }
+    }
+    if (const char* e = std::getenv("AFMIB_INNER_NU_COARSE")) {
+        int a = 0, b = 0;
+        if (std::sscanf(e, "%d,%d", &a, &b) == 2 && a >= 0 && b >= 0 && a + b > 0) {
+            s->inner_nu1c = a;
+            s->inner_nu2c = b;
         }
     }
     if (const char* e = std::getenv("AFMIB_INNER_SOLVER")) {
