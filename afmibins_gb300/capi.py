@@ -76,6 +76,7 @@ _SIGS = {
     "afmib_set_markers": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     "afmib_get_markers": ([_vp, _vp], ctypes.c_int),
     "afmib_save": ([_vp, ctypes.c_char_p], ctypes.c_int),
+    "afmib_reset_warm_start": ([_vp], ctypes.c_int),
     "afmib_load": ([_vp, ctypes.c_char_p], ctypes.c_int),
     "afmib_set_marker_positions": ([_vp, _vp], ctypes.c_int),
     "afmib_ib_step": ([_vp, ctypes.c_int], ctypes.c_int),
@@ -280,6 +281,9 @@ class Solver:
         self._ck(self.lib.afmib_ib_step(self.h, nsteps))
 
     # snapshots (afmibins_gb300/snapshot.py reads the files without a GPU)
+    def reset_warm_start(self):
+        self._ck(self.lib.afmib_reset_warm_start(self.h))
+
     def save(self, path):
         self._ck(self.lib.afmib_save(self.h, os.fsencode(path)))
 

@@ -1831,10 +1831,22 @@ int afmib_set_velocity(afmib_solver* s, const double* u, const double* v, const 
     else CK(cudaMemsetAsync(s->v, 0, s->N() * sizeof(double), s->st));
     TRY(copy_in(s, s->w, w, s->N()));
     TRY(refresh_shadow(s));
-    s->phi_valid[0] = s->phi_valid[1] = false;  // a new state: no warm start
+    // The warm-start potentials stay: they are only the projections' first
+    // guess (the stopping rule is unchanged), and a caller that feeds the
+    // velocity back every step (a host-coupled loop) keeps its warm starts.
+    // afmib_reset_warm_start drops them for runs that must not depend on the
+    // solver's history.
     s->phi_valid2[0] = s->phi_valid2[1] = false;
     s->qo_valid = false;
     return sync(s);
+}
+
+int afmib_reset_warm_start(afmib_solver* s) {
+    if (!s) return AFMIB_ERR_ARG;
+    s->phi_valid[0] = s->phi_valid[1] = false;
+    s->phi_valid2[0] = s->phi_valid2[1] = false;
+    s->mg_rho = 0.0;
+    return AFMIB_OK;
 }
 
 int afmib_get_velocity(afmib_solver* s, double* u, double* v, double* w) {

@@ -109,6 +109,11 @@ int afmib_synchronize(afmib_solver* s);
 /* Velocity state: the reference keeps references to the caller's u0, v0, w0
  * (src/ns/solver.h:54-56, 83-85). */
 int afmib_set_velocity(afmib_solver* s, const double* u, const double* v, const double* w);
+/* Drop the projections' warm-start potentials (and the multigrid contraction
+ * estimate): the next projections start as on a new solver. afmib_set_velocity
+ * keeps them (they are only a first guess), so that a loop feeding the
+ * velocity back every step keeps its warm starts. */
+int afmib_reset_warm_start(afmib_solver* s);
 int afmib_get_velocity(afmib_solver* s, double* u, double* v, double* w);
 /* p = (I - s*Delta) phi, ns::solver::get_p, src/ns/solver.h:86 */
 int afmib_get_pressure(afmib_solver* s, double* p);
