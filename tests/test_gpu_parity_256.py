@@ -1,0 +1,52 @@
+"""FP64 parity with the compiled reference at 256^3 (channel): one BE/CN pair
+of NS sub-steps from seeded fields against the digest of the reference's run
+(tests/golden/make_golden_256.py). The inputs are regenerated from the seed;
+velocity and wall velocities are compared at 4096 seeded cells each and by
+their sums, the pressure at the same cells after fitting the null-space
+constant on them. Bar: 1e-10 relative to each field's largest magnitude."""
+import os
+
+import numpy as np
+import pytest
+
+from afmibins_gb300 import capi
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIXTURE = os.path.join(HERE, "golden", "ns_channel_256_digest.npz")
+
+
+def _inputs(seed, n=256):
+    N, NV = n ** 3, n * (n - 1) * n
+    rng = np.random.default_rng(seed)
+    u, v, w = 0.1 * rng.standard_normal(N), 0.1 * rng.standard_normal(NV), 0.1 * rng.standard_normal(N)
+    fx, fy, fz = rng.standard_normal(N), rng.standard_normal(NV), rng.standard_normal(N)
+    return u, v, w, fx, fy, fz
+
+
+@pytest.mark.skipif(not os.path.exists(FIXTURE), reason="no 256^3 digest fixture")
+def test_ns_substeps_channel_256_against_reference_digest():
+    d = np.load(FIXTURE)
+    n = 256
+    u, v, w, fx, fy, fz = _inputs(int(d["seed"]), n)
+    mu, rho, dt, tol = float(d["mu"]), float(d["rho"]), float(d["dt"]), float(d["tol"])
+    with capi.Solver(n, bc=capi.BC_CHANNEL, mu=mu, rho=rho, dt=dt, tol=tol, max_cg_iters=5000,
+                     max_mg_cycles=500) as sv:
+        sv.set_velocity(u, v, w)
+        sv.project()
+        for _ in range(int(d["substeps"])):
+            sv.ns_step(fx, fy, fz)
+        gu, gv, gw = sv.get_velocity()
+        gp = sv.get_pressure()
+        walls = np.concatenate(sv.get_walls())
+        h1 = sv.helm_apply(0, -mu * dt / (2 * rho), np.ones(n ** 3))
+    for name, a in (("u", gu), ("v", gv), ("w", gw), ("walls", walls)):
+        scale = float(d[name + "_max"])
+        err = np.max(np.abs(a[d[name + "_idx"]] - d[name + "_val"])) / scale
+        assert err < 1e-10, (name, err)
+        assert abs(a.sum() - float(d[name + "_sum"])) < 1e-10 * scale * a.size ** 0.5, name
+    idx = d["p_idx"]
+    dlt = gp[idx] - d["p_val"]
+    c = float(dlt @ h1[idx] / (h1[idx] @ h1[idx]))
+    assert np.max(np.abs(gp[idx] - c * h1[idx] - d["p_val"])) / float(d["p_max"]) < 1e-10
