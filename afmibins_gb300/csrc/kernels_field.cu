@@ -219,17 +219,21 @@ __global__ void k_helm_rhs(Dims d, int comp, int be, T* __restrict__ r, const T*
     if (d.channel && comp == 1 && y == 0) { r[i] = T(0); return; }
     // wall term of helmholtz_periodic::boundary (u, w rows next to the walls)
     T bm = T(0), bp = T(0);
-    if (d.channel && comp != 1 && (y == 0 || y == d.ny - 1) && top) {
+    const bool wall = d.channel && comp != 1 && (y == 0 || y == d.ny - 1) && top;
+    if (wall) {
         const long long ixz = x + (long long)d.nx * z;
         const double wv = (y == 0) ? bottom[ixz] : top[ixz];
         bm = T(8. / 3. * s_minus * d.n * d.n * wv);
         bp = T(8. / 3. * s_plus * d.n * d.n * wv);
     }
     const T src = T(hdt) * (T(inv_rho) * cvt<T, TF>(f[i]) - cvt<T, TA>(adv[i]));
+    // away from the wall rows the wall terms are zero and their additions are
+    // exact, so they are skipped
     if (be) {
-        r[i] = (uold[i] + T(-1) * bm) + src;
+        r[i] = wall ? (uold[i] + T(-1) * bm) + src : uold[i] + src;
     } else {
-        r[i] = (helm_point(d, comp, T(s_plus), uold, x, y, z) + (bp - bm)) + src;
+        const T hp = helm_point(d, comp, T(s_plus), uold, x, y, z);
+        r[i] = wall ? (hp + (bp - bm)) + src : hp + src;
     }
 }
 
@@ -295,13 +299,14 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_rhs_be_defect(Dims d, int co
             const long long i = lin(d, xi, yi, zi);
             double b = 0.0;
             if (!(d.channel && comp == 1 && yi == 0)) {
-                double bm = 0.0;
+                const double src = hdt * (inv_rho * cvt<double, TF>(f[i]) - cvt<double, TA>(adv[i]));
                 if (d.channel && comp != 1 && (yi == 0 || yi == d.ny - 1) && top) {
                     const long long ixz = xi + (long long)d.nx * zi;
-                    bm = 8. / 3. * s_minus * d.n * d.n * ((yi == 0) ? bottom[ixz] : top[ixz]);
+                    const double bm = 8. / 3. * s_minus * d.n * d.n * ((yi == 0) ? bottom[ixz] : top[ixz]);
+                    b = (uold[i] + -1.0 * bm) + src;
+                } else {
+                    b = uold[i] + src;
                 }
-                const double src = hdt * (inv_rho * cvt<double, TF>(f[i]) - cvt<double, TA>(adv[i]));
-                b = (uold[i] + -1.0 * bm) + src;
             }
             double hx, q;
             helm_point_q(d, comp, s_minus, uold, xi, yi, zi, hx, q);
@@ -326,16 +331,16 @@ __global__ void k_helm_rhs_cn_q(Dims d, int comp, double* __restrict__ r, const 
     AFMIB_XYZ
     const long long i = lin(d, x, y, z);
     if (d.channel && comp == 1 && y == 0) { r[i] = 0.0; return; }
-    double bm = 0.0, bp = 0.0;
+    const double src = hdt * (inv_rho * cvt<double, TF>(f[i]) - cvt<double, TA>(adv[i]));
+    const double off = s_plus * double(d.n) * double(d.n);
     if (d.channel && comp != 1 && (y == 0 || y == d.ny - 1) && top) {
         const long long ixz = x + (long long)d.nx * z;
         const double wv = (y == 0) ? bottom[ixz] : top[ixz];
-        bm = 8. / 3. * s_minus * d.n * d.n * wv;
-        bp = 8. / 3. * s_plus * d.n * d.n * wv;
+        const double bm = 8. / 3. * s_minus * d.n * d.n * wv, bp = 8. / 3. * s_plus * d.n * d.n * wv;
+        r[i] = ((uold[i] + off * q[i]) + (bp - bm)) + src;
+    } else {
+        r[i] = (uold[i] + off * q[i]) + src;
     }
-    const double src = hdt * (inv_rho * cvt<double, TF>(f[i]) - cvt<double, TA>(adv[i]));
-    const double off = s_plus * double(d.n) * double(d.n);
-    r[i] = ((uold[i] + off * q[i]) + (bp - bm)) + src;
 }
 
 // ---------------------------------------------------------------------------
