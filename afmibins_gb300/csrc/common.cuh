@@ -187,6 +187,32 @@ inline dim3 red_grid3(int nx, int ny, int nz) {
     return dim3(gx, gy, gz);
 }
 
+// Persistent form of the same walk, for a stencil reduction that runs beside
+// kernels on another stream: a 1-D grid of a few blocks per SM (so that the
+// other stream's blocks find free SM slots) strides over (tile, z) items in
+// z-major order. The cells each thread visits and their values are those of
+// the red_grid3 form; only the order of the reduction's partial sums differs.
+inline dim3 walk_grid(const Dims& d, int blocks) {
+    const long long items =
+        (long long)((d.nx + kRBX - 1) / kRBX) * ((d.ny + kRBY - 1) / kRBY) * d.nz;
+    long long b = blocks;
+    if (b > items) b = items;
+    if (b > kMaxRedBlocks) b = kMaxRedBlocks;
+    if (b < 1) b = 1;
+    return dim3((unsigned)b);
+}
+template <typename F>
+__device__ __forceinline__ void tile_walk(const Dims& d, F&& body) {
+    const int gx = (d.nx + kRBX - 1) / kRBX, gxy = gx * ((d.ny + kRBY - 1) / kRBY);
+    const long long items = (long long)gxy * d.nz;
+#pragma unroll 2
+    for (long long it = blockIdx.x; it < items; it += gridDim.x) {
+        const int t = (int)(it % gxy), zi = (int)(it / gxy);
+        const int xi = (t % gx) * kRBX + threadIdx.x, yi = (t / gx) * kRBY + threadIdx.y;
+        if (xi < d.nx && yi < d.ny) body(xi, yi, zi);
+    }
+}
+
 // Per-thread partial sums stay in the arithmetic type (one FP64 conversion
 // per thread, not per element: on GB300 conversions run on the FP64 pipe).
 template <typename T>

@@ -47,20 +47,23 @@ void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const
 // Mixed form, backward-Euler sub-step: b (as launch_helm_rhs), the first FP64
 // defect r = b - H uold as FP32 with out[0] = r.r (H = I + s_minus Delta), and
 // q = Q(uold), the off-diagonal term of the Helmholtz rows, in one pass.
+// walk_blocks > 0: the persistent form on that many blocks (tile_walk).
 template <typename TF, typename TA>
 void launch_helm_rhs_be_defect(const Dims& d, int comp, double* b, float* r, double* q, const double* uold,
                                const TF* f, const TA* adv, const double* top, const double* bottom, double s_minus,
-                               double dt, double inv_rho, RedScratch sc, double* out, cudaStream_t s);
+                               double dt, double inv_rho, RedScratch sc, double* out, cudaStream_t s,
+                               int walk_blocks = 0);
 // Mixed form, Crank-Nicolson sub-step: b from q = Q(uold) kept by the
 // backward-Euler sub-step (pointwise).
 template <typename TF, typename TA>
 void launch_helm_rhs_cn_q(const Dims& d, int comp, double* r, const double* uold, const double* q, const TF* f,
                           const TA* adv, const double* top, const double* bottom, double s_plus, double s_minus,
                           double dt, double inv_rho, cudaStream_t s);
-// Mixed form: r = b - (I + s Delta) x in FP64, stored as TD, out[0] = ||r||^2.
+// Mixed form: r = b - (I + s Delta) x in FP64, stored as TD, out[0] = ||r||^2;
+// walk_blocks > 0: the persistent form on that many blocks (tile_walk).
 template <typename TD>
 void launch_helm_defect(const Dims& d, int comp, double scale, const double* x, const double* b, TD* r, RedScratch sc,
-                        double* out, cudaStream_t s);
+                        double* out, cudaStream_t s, int walk_blocks = 0);
 // x = 0, r = p = b, cgs[0] = b.b
 template <typename T>
 void launch_cg_init_zero(long long n, const T* b, T* x, T* r, T* p, RedScratch sc, double* cgs, cudaStream_t s);

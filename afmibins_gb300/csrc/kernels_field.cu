@@ -285,37 +285,42 @@ __device__ __forceinline__ void helm_point_q(const Dims& d, int comp, T s, const
 // the first FP64 defect of the viscous solve started from x = uold
 // (r = b - H uold, as k_helm_defect, with its squared norm) and Q(uold) for
 // the Crank-Nicolson right-hand side of the next sub-step, in one pass.
-template <typename TF, typename TA>
+template <typename TF, typename TA, bool WALK>
 __global__ void __launch_bounds__(kRedBlock) k_helm_rhs_be_defect(Dims d, int comp, double* __restrict__ b_out,
                                                                  float* __restrict__ r_out, double* __restrict__ q_out,
                                                                  const double* __restrict__ uold, const TF* __restrict__ f,
                                                                  const TA* __restrict__ adv, const double* __restrict__ top,
                                                                  const double* __restrict__ bottom, double s_minus,
                                                                  double hdt, double inv_rho, RedScratch sc, double* out) {
-    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
     float acc = 0.f;
-    if (xi < d.nx && yi < d.ny)
-        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
-            const long long i = lin(d, xi, yi, zi);
-            double b = 0.0;
-            if (!(d.channel && comp == 1 && yi == 0)) {
-                const double src = hdt * (inv_rho * cvt<double, TF>(f[i]) - cvt<double, TA>(adv[i]));
-                if (d.channel && comp != 1 && (yi == 0 || yi == d.ny - 1) && top) {
-                    const long long ixz = xi + (long long)d.nx * zi;
-                    const double bm = 8. / 3. * s_minus * d.n * d.n * ((yi == 0) ? bottom[ixz] : top[ixz]);
-                    b = (uold[i] + -1.0 * bm) + src;
-                } else {
-                    b = uold[i] + src;
-                }
+    auto body = [&](int xi, int yi, int zi) {
+        const long long i = lin(d, xi, yi, zi);
+        double b = 0.0;
+        if (!(d.channel && comp == 1 && yi == 0)) {
+            const double src = hdt * (inv_rho * cvt<double, TF>(f[i]) - cvt<double, TA>(adv[i]));
+            if (d.channel && comp != 1 && (yi == 0 || yi == d.ny - 1) && top) {
+                const long long ixz = xi + (long long)d.nx * zi;
+                const double bm = 8. / 3. * s_minus * d.n * d.n * ((yi == 0) ? bottom[ixz] : top[ixz]);
+                b = (uold[i] + -1.0 * bm) + src;
+            } else {
+                b = uold[i] + src;
             }
-            double hx, q;
-            helm_point_q(d, comp, s_minus, uold, xi, yi, zi, hx, q);
-            b_out[i] = b;
-            q_out[i] = q;
-            const float ri = float(b - hx);
-            r_out[i] = ri;
-            acc += ri * ri;
         }
+        double hx, q;
+        helm_point_q(d, comp, s_minus, uold, xi, yi, zi, hx, q);
+        b_out[i] = b;
+        q_out[i] = q;
+        const float ri = float(b - hx);
+        r_out[i] = ri;
+        acc += ri * ri;
+    };
+    if (WALK) {
+        tile_walk(d, body);
+    } else {
+        const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+        if (xi < d.nx && yi < d.ny)
+            for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) body(xi, yi, zi);
+    }
     double a[1] = {(double)acc};
     grid_sum<1>(a, sc, out);
 }
@@ -440,20 +445,25 @@ __global__ void k_cg_direction(long long N, T* __restrict__ p, const T* __restri
 // evaluated in FP64 and handed to the FP32 inner solve as an FP32 defect, and
 // the FP64 update x += e with the FP32 correction.
 // ---------------------------------------------------------------------------
-template <typename TD>
+template <typename TD, bool WALK>
 __global__ void __launch_bounds__(kRedBlock) k_helm_defect(Dims d, int comp, double s, const double* __restrict__ x,
                                                           const double* __restrict__ b, TD* __restrict__ r,
                                                           RedScratch sc, double* out) {
-    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
     TD acc = TD(0);
-    if (xi < d.nx && yi < d.ny)
+    auto body = [&](int xi, int yi, int zi) {
+        const long long i = lin(d, xi, yi, zi);
+        const TD ri = TD(b[i] - helm_point(d, comp, s, x, xi, yi, zi));
+        r[i] = ri;
+        acc += ri * ri;
+    };
+    if (WALK) {
+        tile_walk(d, body);
+    } else {
+        const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+        if (xi < d.nx && yi < d.ny)
 #pragma unroll 2
-        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
-            const long long i = lin(d, xi, yi, zi);
-            const TD ri = TD(b[i] - helm_point(d, comp, s, x, xi, yi, zi));
-            r[i] = ri;
-            acc += ri * ri;
-        }
+            for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) body(xi, yi, zi);
+    }
     double a[1] = {(double)acc};
     grid_sum<1>(a, sc, out);
 }
@@ -696,9 +706,13 @@ void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const
 template <typename TF, typename TA>
 void launch_helm_rhs_be_defect(const Dims& d, int comp, double* b, float* r, double* q, const double* uold,
                                const TF* f, const TA* adv, const double* top, const double* bottom, double s_minus,
-                               double dt, double inv_rho, RedScratch sc, double* out, cudaStream_t s) {
-    k_helm_rhs_be_defect<TF, TA><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(
-        d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out);
+                               double dt, double inv_rho, RedScratch sc, double* out, cudaStream_t s, int walk_blocks) {
+    if (walk_blocks > 0)
+        k_helm_rhs_be_defect<TF, TA, true><<<walk_grid(d, walk_blocks), dim3(kRBX, kRBY), 0, s>>>(
+            d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out);
+    else
+        k_helm_rhs_be_defect<TF, TA, false><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(
+            d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out);
 }
 template <typename TF, typename TA>
 void launch_helm_rhs_cn_q(const Dims& d, int comp, double* r, const double* uold, const double* q, const TF* f,
@@ -709,10 +723,10 @@ void launch_helm_rhs_cn_q(const Dims& d, int comp, double* r, const double* uold
 }
 template void launch_helm_rhs_be_defect<double, float>(const Dims&, int, double*, float*, double*, const double*,
                                                        const double*, const float*, const double*, const double*,
-                                                       double, double, double, RedScratch, double*, cudaStream_t);
+                                                       double, double, double, RedScratch, double*, cudaStream_t, int);
 template void launch_helm_rhs_be_defect<float, float>(const Dims&, int, double*, float*, double*, const double*,
                                                       const float*, const float*, const double*, const double*, double,
-                                                      double, double, RedScratch, double*, cudaStream_t);
+                                                      double, double, RedScratch, double*, cudaStream_t, int);
 template void launch_helm_rhs_cn_q<double, float>(const Dims&, int, double*, const double*, const double*,
                                                   const double*, const float*, const double*, const double*, double,
                                                   double, double, double, cudaStream_t);
@@ -722,8 +736,12 @@ template void launch_helm_rhs_cn_q<float, float>(const Dims&, int, double*, cons
 
 template <typename TD>
 void launch_helm_defect(const Dims& d, int comp, double scale, const double* x, const double* b, TD* r, RedScratch sc,
-                        double* out, cudaStream_t s) {
-    k_helm_defect<TD><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, scale, x, b, r, sc, out);
+                        double* out, cudaStream_t s, int walk_blocks) {
+    if (walk_blocks > 0)
+        k_helm_defect<TD, true><<<walk_grid(d, walk_blocks), dim3(kRBX, kRBY), 0, s>>>(d, comp, scale, x, b, r, sc, out);
+    else
+        k_helm_defect<TD, false><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, scale, x, b, r, sc,
+                                                                                            out);
 }
 template <typename T>
 void launch_cg_init_zero(long long n, const T* b, T* x, T* r, T* p, RedScratch sc, double* cgs, cudaStream_t s) {
@@ -908,7 +926,7 @@ void launch_helm_defect_bfp(const Dims& d, int comp, double scale, const double*
     k_helm_defect_bfp<<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, scale, x, b, r, sc, out);
 }
 template void launch_helm_defect<float>(const Dims&, int, double, const double*, const double*, float*, RedScratch,
-                                        double*, cudaStream_t);
+                                        double*, cudaStream_t, int);
 template void launch_cg_dir_apply<float>(const Dims&, int, double, const float*, const float*, float*, float*,
                                          RedScratch, double*, cudaStream_t);
 template void launch_cg_init_zero<float>(long long, const float*, float*, float*, float*, RedScratch, double*,

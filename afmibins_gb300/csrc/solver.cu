@@ -51,6 +51,20 @@ struct afmib_solver {
     double* qo[3] = {};
     bool qo_valid = false;
     bool fused_rhs = true;
+    // mixed form: the three viscous solves of a sub-step interleaved on two
+    // streams, one component's FP32 correction beside the next component's
+    // FP64 defect (AFMIB_HELM_OVERLAP=0: one solve after another). The
+    // defects then run on a persistent grid of walk_blocks blocks (3 per SM,
+    // AFMIB_HELM_WALK_BLOCKS) so that the corrections find free SM slots.
+    bool helm_overlap = true;
+    int walk_blocks = 0, walk_blocks_be = 0;  // the backward-Euler fused first defects (AFMIB_HELM_WALK_BLOCKS_BE)
+    // the defects run on a stream of the device's highest priority (hi), so
+    // that their persistent blocks take free SM slots before pending blocks
+    // of the corrections on aux (measured no faster or slower than default
+    // priority at 256^3: the defects are queued ahead of the corrections)
+    cudaStream_t aux = nullptr, hi = nullptr;
+    cudaEvent_t ev_def[3] = {}, ev_cor[3] = {}, ev_join = nullptr;
+    float* d32c[3] = {};  // per-component defects; d32c[0] is d32
     double *divb = nullptr, *walls = nullptr, *wallgrad = nullptr;
     double *cg_r = nullptr, *cg_p = nullptr, *cg_q = nullptr;
     double *tmp[3] = {};
@@ -132,7 +146,7 @@ struct afmib_solver {
     RedScratch red{};
     double* scal = nullptr;   // device scalars: [0..4] CG, [8] sum, [9] sumsq
     double* hscal = nullptr;  // pinned mirror
-    int* dflag = nullptr;     // device status flags [0] markers, [1] coarse solve
+    int* dflag = nullptr;     // device status flags [0] markers, [1] coarse solve, [3] pipelined smoother
     int* hflag = nullptr;
     bool half = false;
 
@@ -790,6 +804,100 @@ int helm_solve_mixed(afmib_solver* s, int comp, double scale, double* x, const d
     return AFMIB_OK;
 }
 
+// The three viscous solves of a mixed-form sub-step interleaved on two
+// streams. The FP64 defects (FP64-pipe bound, on the persistent grid) stay on
+// the solver's stream; as soon as a component's defect norm reaches the host
+// and asks for a correction, that correction (Gauss-Seidel sweeps on e32 from
+// d32c[c], then x += e) goes to the auxiliary stream, where it runs beside
+// the next component's defect, and the component's next defect is queued
+// behind it. Components are served in the order their defects were queued.
+// Each component goes through exactly the steps of helm_solve_mixed (same
+// defects, corrections and stopping test, bit for bit); only the order of
+// the norms' partial sums differs. first(c) launches component c's first
+// defect into d32c[c] with its squared norm in scal[12 + c]. Needs the
+// Gauss-Seidel inner solve (helm_overlap_ok).
+bool helm_overlap_ok(afmib_solver* s, double scale) {
+    const Dims& d = s->d;
+    return s->helm_overlap && s->aux && s->hi && !s->prof && s->gs_inner && !s->bfp_defects &&
+           gs_sweeps(d, scale, s->cfg.inner_tol) > 0 && d.nz % 8 == 0 && d.nx % 2 == 0 && ix2_ok(d);
+}
+
+template <typename F>
+int helm_solve3_mixed(afmib_solver* s, double scale, double* const x[3], const double* const b[3], F first) {
+    const Dims& d = s->d;
+    const long long N = s->N();
+    const int gsw = gs_sweeps(d, scale, s->cfg.inner_tol);
+    const bool big = s->alternate && (double)N * sizeof(float) >= 32.0 * (1 << 20);
+    cudaStream_t hs = s->hi;
+    auto post = [&](int c) -> int {
+        CK(cudaMemcpyAsync(s->hscal + 12 + c, s->scal + 12 + c, sizeof(double), cudaMemcpyDeviceToHost, hs));
+        CK(cudaEventRecord(s->ev_def[c], hs));
+        return AFMIB_OK;
+    };
+    CK(cudaEventRecord(s->ev_join, s->st));
+    CK(cudaStreamWaitEvent(hs, s->ev_join, 0));
+    int ring[3], head = 0, count = 0, outer[3] = {0, 0, 0};
+    for (int c = 0; c < 3; ++c) {
+        first(c, hs);
+        CKL();
+        TRY(post(c));
+        ring[count++] = c;
+    }
+    int status = AFMIB_OK;
+    while (count > 0) {
+        const int c = ring[head];
+        head = (head + 1) % 3;
+        --count;
+        CK(cudaEventSynchronize(s->ev_def[c]));
+        const double nr = std::sqrt(s->hscal[12 + c]);
+        s->stats.last_cg_norm = nr;
+        if (!std::isfinite(nr)) { status = s->fail(AFMIB_ERR_NAN, "Helmholtz residual is not finite"); break; }
+        if (nr <= s->cfg.tol) {
+            s->stats.outer_iters += outer[c];
+            continue;
+        }
+        if (outer[c] >= s->cfg.max_mg_cycles) {
+            status = s->fail(AFMIB_ERR_NOCONV, "defect-correction cap reached (Helmholtz)");
+            break;
+        }
+        CK(cudaStreamWaitEvent(s->aux, s->ev_def[c], 0));
+        int rev = 1;  // the defect's walk ended at the last z planes
+        for (int j = 0; j < gsw; ++j)
+            for (int color = 0; color < 2; ++color) {
+                ProfScope ps(s, P_JACOBI, (double)N * 4 * 1.5);
+                launch_helm_rbgs<float>(d, c, scale, color, j == 0 && color == 0, s->e32, s->d32c[c], s->aux,
+                                        big ? rev : 0);
+                rev ^= 1;
+            }
+        {
+            ProfScope ps(s, P_CORRECT, (double)N * (8 + 4 + 8));
+            launch_add_correction<float>(N, x[c], s->e32, s->aux);
+        }
+        CKL();
+        CK(cudaEventRecord(s->ev_cor[c], s->aux));
+        CK(cudaStreamWaitEvent(hs, s->ev_cor[c], 0));
+        {
+            ProfScope ps(s, P_HELM_DEFECT, (double)N * (8 + 8 + 4));
+            launch_helm_defect<float>(d, c, scale, x[c], b[c], s->d32c[c], s->red, s->scal + 12 + c, hs,
+                                      s->walk_blocks);
+        }
+        CKL();
+        TRY(post(c));
+        ring[(head + count++) % 3] = c;
+        ++outer[c];
+    }
+    if (status != AFMIB_OK) {
+        cudaStreamSynchronize(s->aux);
+        cudaStreamSynchronize(hs);
+        cudaStreamSynchronize(s->st);
+        return status;
+    }
+    // every correction was followed by a defect on hs: joining hs joins both
+    CK(cudaEventRecord(s->ev_join, hs));
+    CK(cudaStreamWaitEvent(s->st, s->ev_join, 0));
+    return AFMIB_OK;
+}
+
 int mg_solve_mixed(afmib_solver* s, int* cycles) {
     MGLevel& L = s->lv[0];
     MGLevelT<float>& L32 = s->lv32[0];
@@ -902,48 +1010,73 @@ int substep(afmib_solver* s) {
     double* vel[3] = {s->u, s->v, s->w};
     if (s->mixed && s->fused_rhs && s->qo[0] && !s->bfp_defects) {
         // backward Euler: right-hand side, first defect (x starts at uold)
-        // and Q(uold) in one pass, component by component; Crank-Nicolson:
-        // right-hand sides from Q(uold), then the solves
-        for (int c = 0; c < 3; ++c) {
-            const double* top = (!d.channel || c == 1) ? nullptr : (c == 0 ? ut : wt);
-            const double* bot = (!d.channel || c == 1) ? nullptr : (c == 0 ? ub : wb);
-            if (be) {
-                {
-                    ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 4 + 8 + 8 + 4));
-                    if (s->spread64)
-                        launch_helm_rhs_be_defect<double, float>(d, c, s->rhs[c], s->d32, s->qo[c], s->uo[c], s->f[c],
-                                                                 s->adv32[c], top, bot, s->s_minus(), s->cfg.dt, inv_rho,
-                                                                 s->red, s->scal + 10, s->st);
-                    else
-                        launch_helm_rhs_be_defect<float, float>(d, c, s->rhs[c], s->d32, s->qo[c], s->uo[c],
-                                                                s->f32[c], s->adv32[c], top, bot, s->s_minus(),
-                                                                s->cfg.dt, inv_rho, s->red, s->scal + 10, s->st);
-                }
-                CKL();
-                TRY(helm_solve_mixed(s, c, s->s_minus(), vel[c], s->rhs[c], true));
-            } else if (s->qo_valid) {
-                ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 8 + 4 + 8));
-                if (s->spread64)
-                    launch_helm_rhs_cn_q<double, float>(d, c, s->rhs[c], s->uo[c], s->qo[c], s->f[c], s->adv32[c], top,
-                                                        bot, s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
-                else
-                    launch_helm_rhs_cn_q<float, float>(d, c, s->rhs[c], s->uo[c], s->qo[c], s->f32[c], s->adv32[c], top,
-                                                       bot, s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
-            } else if (s->spread64) {
-                ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 4 + 8));
-                launch_helm_rhs<double, double, float>(d, c, 0, s->rhs[c], s->uo[c], s->f[c], s->adv32[c], top, bot,
-                                                       s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
-            } else {
-                ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 4 + 4 + 8));
-                launch_helm_rhs<double, float, float>(d, c, 0, s->rhs[c], s->uo[c], s->f32[c], s->adv32[c], top, bot,
-                                                      s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
-            }
-        }
-        CKL();
+        // and Q(uold) in one pass per component; Crank-Nicolson: right-hand
+        // sides from Q(uold), then the solves
+        const bool ovl = helm_overlap_ok(s, s->s_minus());
+        auto walls_of = [&](int c, const double** top, const double** bot) {
+            *top = (!d.channel || c == 1) ? nullptr : (c == 0 ? ut : wt);
+            *bot = (!d.channel || c == 1) ? nullptr : (c == 0 ? ub : wb);
+        };
+        auto be_first = [&](int c, float* r, double* out, int wblocks, cudaStream_t q) {
+            const double *top, *bot;
+            walls_of(c, &top, &bot);
+            ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 4 + 8 + 8 + 4));
+            if (s->spread64)
+                launch_helm_rhs_be_defect<double, float>(d, c, s->rhs[c], r, s->qo[c], s->uo[c], s->f[c], s->adv32[c],
+                                                         top, bot, s->s_minus(), s->cfg.dt, inv_rho, s->red, out, q,
+                                                         wblocks);
+            else
+                launch_helm_rhs_be_defect<float, float>(d, c, s->rhs[c], r, s->qo[c], s->uo[c], s->f32[c],
+                                                        s->adv32[c], top, bot, s->s_minus(), s->cfg.dt, inv_rho,
+                                                        s->red, out, q, wblocks);
+        };
         if (be) {
+            if (ovl) {
+                TRY(helm_solve3_mixed(s, s->s_minus(), vel, s->rhs, [&](int c, cudaStream_t hs) {
+                    be_first(c, s->d32c[c], s->scal + 12 + c, s->walk_blocks_be, hs);
+                }));
+            } else {
+                for (int c = 0; c < 3; ++c) {
+                    be_first(c, s->d32, s->scal + 10, 0, s->st);
+                    CKL();
+                    TRY(helm_solve_mixed(s, c, s->s_minus(), vel[c], s->rhs[c], true));
+                }
+            }
             s->qo_valid = true;
         } else {
-            for (int c = 0; c < 3; ++c) TRY(helm_solve_mixed(s, c, s->s_minus(), vel[c], s->rhs[c]));
+            for (int c = 0; c < 3; ++c) {
+                const double *top, *bot;
+                walls_of(c, &top, &bot);
+                if (s->qo_valid) {
+                    ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 8 + 4 + 8));
+                    if (s->spread64)
+                        launch_helm_rhs_cn_q<double, float>(d, c, s->rhs[c], s->uo[c], s->qo[c], s->f[c], s->adv32[c],
+                                                            top, bot, s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho,
+                                                            s->st);
+                    else
+                        launch_helm_rhs_cn_q<float, float>(d, c, s->rhs[c], s->uo[c], s->qo[c], s->f32[c],
+                                                           s->adv32[c], top, bot, s->s_plus(), s->s_minus(),
+                                                           s->cfg.dt, inv_rho, s->st);
+                } else if (s->spread64) {
+                    ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 4 + 8));
+                    launch_helm_rhs<double, double, float>(d, c, 0, s->rhs[c], s->uo[c], s->f[c], s->adv32[c], top,
+                                                           bot, s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
+                } else {
+                    ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 4 + 4 + 8));
+                    launch_helm_rhs<double, float, float>(d, c, 0, s->rhs[c], s->uo[c], s->f32[c], s->adv32[c], top,
+                                                          bot, s->s_plus(), s->s_minus(), s->cfg.dt, inv_rho, s->st);
+                }
+            }
+            CKL();
+            if (ovl) {
+                TRY(helm_solve3_mixed(s, s->s_minus(), vel, s->rhs, [&](int c, cudaStream_t hs) {
+                    ProfScope ps(s, P_HELM_DEFECT, (double)N * (8 + 8 + 4));
+                    launch_helm_defect<float>(d, c, s->s_minus(), vel[c], s->rhs[c], s->d32c[c], s->red,
+                                              s->scal + 12 + c, hs, s->walk_blocks);
+                }));
+            } else {
+                for (int c = 0; c < 3; ++c) TRY(helm_solve_mixed(s, c, s->s_minus(), vel[c], s->rhs[c]));
+            }
         }
         s->proj_phase = be ? 0 : 1;
         const int prc = project(s);
@@ -1617,6 +1750,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     }
     TRY(dalloc(s, &s->divb, N));
     if (const char* e = std::getenv("AFMIB_FUSED_RHS")) s->fused_rhs = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_HELM_OVERLAP")) s->helm_overlap = std::string(e) != "0";
     if (s->mixed && s->fused_rhs)
         for (auto& q : s->qo) TRY(dalloc(s, &q, N));
     TRY(dalloc(s, &s->phi_prev[0], N));
@@ -1692,6 +1826,29 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
         }
         TRY(dalloc(s, &s->d32, N));
         TRY(dalloc(s, &s->e32, N));
+        s->d32c[0] = s->d32;
+        if (s->helm_overlap) {
+            TRY(dalloc(s, &s->d32c[1], N));
+            TRY(dalloc(s, &s->d32c[2], N));
+            CK(cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking));
+            int least = 0, greatest = 0;
+            CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+            CK(cudaStreamCreateWithPriority(&s->hi, cudaStreamNonBlocking, greatest));
+            CK(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+            for (int k = 0; k < 3; ++k) {
+                CK(cudaEventCreateWithFlags(&s->ev_def[k], cudaEventDisableTiming));
+                CK(cudaEventCreateWithFlags(&s->ev_cor[k], cudaEventDisableTiming));
+            }
+            int dev = 0, sms = 0;
+            CK(cudaGetDevice(&dev));
+            CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            int per_sm = 3;
+            if (const char* e = std::getenv("AFMIB_HELM_WALK_BLOCKS")) per_sm = std::max(1, std::min(8, std::atoi(e)));
+            s->walk_blocks = per_sm * sms;
+            int per_sm_be = per_sm;
+            if (const char* e = std::getenv("AFMIB_HELM_WALK_BLOCKS_BE")) per_sm_be = std::max(1, std::min(8, std::atoi(e)));
+            s->walk_blocks_be = per_sm_be * sms;
+        }
         TRY(dalloc(s, &s->u32, N));
         TRY(dalloc(s, &s->v32, N));
         TRY(dalloc(s, &s->w32, N));
@@ -1808,6 +1965,16 @@ int afmib_destroy(afmib_solver* s) {
     for (auto e : s->prof_pool) cudaEventDestroy(e);
     if (s->hscal) cudaFreeHost(s->hscal);
     if (s->hflag) cudaFreeHost(s->hflag);
+    for (cudaStream_t q : {s->aux, s->hi})
+        if (q) {
+            cudaStreamSynchronize(q);
+            cudaStreamDestroy(q);
+        }
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
+    for (int k = 0; k < 3; ++k) {
+        if (s->ev_def[k]) cudaEventDestroy(s->ev_def[k]);
+        if (s->ev_cor[k]) cudaEventDestroy(s->ev_cor[k]);
+    }
     if (s->own_stream && s->st) cudaStreamDestroy(s->st);
     delete s;
     return AFMIB_OK;

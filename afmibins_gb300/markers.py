@@ -185,7 +185,7 @@ def random_solenoidal_velocity(nx, ny, nz, rms=0.1, k_peak=4.0, seed=SEED):
     K = np.stack([KX, KY, KZ])
     kdot = (A * K).sum(0) / np.maximum(kk ** 2, 1e-12)
     A = A - K * kdot
-    fields = [np.fft.irfftn(a, s=(nx, ny, nz)) for a in A]
+    fields = [np.fft.irfftn(a, s=(nx, ny, nz), axes=(0, 1, 2)) for a in A]
     r = np.sqrt(sum((f ** 2).mean() for f in fields) / 3.0)
     # indexing='ij' gives [x, y, z]; flatten x-fastest -> transpose to [z, y, x]
     return [np.ascontiguousarray((f * (rms / r)).transpose(2, 1, 0)).ravel() for f in fields]

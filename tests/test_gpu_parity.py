@@ -549,6 +549,52 @@ def test_alternating_block_order_keeps_bits(monkeypatch, precision):
     assert np.array_equal(out["0"][0], out["1"][0])
 
 
+@pytest.mark.parametrize("n,bc,markers", [(64, capi.BC_PERIODIC, True), (64, capi.BC_CHANNEL, False),
+                                          (256, capi.BC_PERIODIC, False)])
+def test_interleaved_viscous_solves_keep_bits(monkeypatch, n, bc, markers):
+    """Mixed form: the three viscous solves of a sub-step interleaved on two
+    streams (one component's FP32 correction beside the next component's FP64
+    defect, the defects on a persistent grid of 2 or 8 blocks per SM) go
+    through the same defects, corrections and stopping tests as the solves one
+    after another (AFMIB_HELM_OVERLAP=0): the same velocity, pressure and
+    markers bit for bit, and the same number of defect-correction steps."""
+    channel = bc == capi.BC_CHANNEL
+    g = po.Grid(n, n, n, n, channel=channel)
+    rng = np.random.default_rng(28)
+    u, v, w = 0.1 * rng.standard_normal(g.ncell), 0.1 * rng.standard_normal(g.nv), 0.1 * rng.standard_normal(g.ncell)
+    f = [rng.standard_normal(g.ncell), rng.standard_normal(g.nv), rng.standard_normal(g.ncell)]
+    out = {}
+    for mode, blocks in (("0", None), ("1", None), ("1", "8")):
+        monkeypatch.setenv("AFMIB_HELM_OVERLAP", mode)
+        if blocks:
+            monkeypatch.setenv("AFMIB_HELM_WALK_BLOCKS", blocks)
+        else:
+            monkeypatch.delenv("AFMIB_HELM_WALK_BLOCKS", raising=False)
+        with capi.Solver(n, bc=bc, precision=capi.MIXED, mu=0.01, rho=1.0, dt=1e-3, tol=1e-10,
+                         k_spring=0.5) as sv:
+            sv.set_velocity(u, v, w)
+            sv.project()
+            if markers:
+                _, _, _, _, X, nstart, nidx = _periodic_case(n, M=2000, seed=29)
+                sv.set_markers(X, nstart, nidx)
+                sv.ib_step(3)
+                gX = sv.get_markers()
+            else:
+                for _ in range(4):
+                    sv.ns_step(*f)
+                gX = None
+            out[(mode, blocks)] = (sv.get_velocity(), sv.get_pressure(), gX, sv.stats()["outer_iters"])
+    ref = out[("0", None)]
+    for key in (("1", None), ("1", "8")):
+        got = out[key]
+        for a, b in zip(ref[0], got[0]):
+            assert np.array_equal(a, b)
+        assert np.array_equal(ref[1], got[1])
+        if markers:
+            assert np.array_equal(ref[2], got[2])
+        assert ref[3] == got[3]
+
+
 @pytest.mark.parametrize("m", [1200, 5000, 20000])
 def test_spread_dense_cluster_takes_large_capacity_pass(m):
     """m markers inside two cells: 1,200 exceed the first pass's capacity and
