@@ -130,6 +130,54 @@ AFMIB_HD df2 df_mul(df2 a, df2 b) {
 
 AFMIB_HD float df_to_float(df2 a) { return a.hi + a.lo; }
 
+// a + b as an exact pair (Knuth's two-sum)
+AFMIB_HD df2 two_sum_f(float a, float b) {
+    df2 r;
+    r.hi = a + b;
+    const float v = r.hi - a;
+    r.lo = (a - (r.hi - v)) + (b - v);
+    return r;
+}
+
+// a + b for a pair and a float, renormalised
+AFMIB_HD df2 df_add_f(df2 a, float b) {
+    df2 s = two_sum_f(a.hi, b);
+    s.lo += a.lo;
+    df2 r;
+    r.hi = s.hi + s.lo;
+    r.lo = s.lo - (r.hi - s.hi);
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// One row of the viscous operator applied to an FP32 correction e, in
+// double-float: H e = e0 + off Q(e), Q = sum(nb) - k e0, plus cxa * xa for
+// the channel u/w wall rows (there nb are the x and z neighbours, k = 8, xa
+// the neighbour away from the wall and cxa = off + off/3; the FP64 rows are
+// helm_point's). The neighbour sum, k e0 (an exact product by fma) and the
+// two coefficient products are carried as pairs, so H e has a relative error
+// of a few units of 2^-46 of its largest term: the mixed form subtracts it
+// from the outer residual instead of re-evaluating b - H x in FP64.
+// ---------------------------------------------------------------------------
+AFMIB_HD df2 df_helm_row(float e0, const float* nb, int nnb, float k, df2 off, float xa, df2 cxa, bool wall) {
+    df2 q;
+    q.hi = nb[0];
+    q.lo = 0.f;
+    for (int j = 1; j < nnb; ++j) q = df_add_f(q, nb[j]);
+    df2 ke;
+    ke.hi = k * e0;
+    ke.lo = fmaf(k, e0, -ke.hi);
+    q = df_add(q, df_neg(ke));
+    df2 h = df_mul(off, q);
+    if (wall) {
+        df2 a;
+        a.hi = xa;
+        a.lo = 0.f;
+        h = df_add(h, df_mul(cxa, a));
+    }
+    return df_add_f(h, e0);
+}
+
 // ---------------------------------------------------------------------------
 // Per-cell block floating point. The FP64 values of one stencil are taken to
 // int64 at a common scale set by the largest exponent E among them (biased):

@@ -52,7 +52,7 @@ template <typename TF, typename TA>
 void launch_helm_rhs_be_defect(const Dims& d, int comp, double* b, float* r, double* q, const double* uold,
                                const TF* f, const TA* adv, const double* top, const double* bottom, double s_minus,
                                double dt, double inv_rho, RedScratch sc, double* out, cudaStream_t s,
-                               int walk_blocks = 0);
+                               int walk_blocks = 0, float* r_lo = nullptr);
 // Mixed form, Crank-Nicolson sub-step: b from q = Q(uold) kept by the
 // backward-Euler sub-step (pointwise).
 template <typename TF, typename TA>
@@ -63,7 +63,12 @@ void launch_helm_rhs_cn_q(const Dims& d, int comp, double* r, const double* uold
 // walk_blocks > 0: the persistent form on that many blocks (tile_walk).
 template <typename TD>
 void launch_helm_defect(const Dims& d, int comp, double scale, const double* x, const double* b, TD* r, RedScratch sc,
-                        double* out, cudaStream_t s, int walk_blocks = 0);
+                        double* out, cudaStream_t s, int walk_blocks = 0, float* r_lo = nullptr);
+// r_lo (both defects): also the rest of the FP64 residual, float(r - r_float),
+// the second word of the double-float pair that launch_helm_update_df updates
+// Mixed form: x += e, (rh, rl) -= H e in double-float, out[0] = rh.rh
+void launch_helm_update_df(const Dims& d, int comp, double scale, double* x, const float* e, float* rh, float* rl,
+                           RedScratch sc, double* out, cudaStream_t s);
 // x = 0, r = p = b, cgs[0] = b.b
 template <typename T>
 void launch_cg_init_zero(long long n, const T* b, T* x, T* r, T* p, RedScratch sc, double* cgs, cudaStream_t s);

@@ -291,7 +291,8 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_rhs_be_defect(Dims d, int co
                                                                  const double* __restrict__ uold, const TF* __restrict__ f,
                                                                  const TA* __restrict__ adv, const double* __restrict__ top,
                                                                  const double* __restrict__ bottom, double s_minus,
-                                                                 double hdt, double inv_rho, RedScratch sc, double* out) {
+                                                                 double hdt, double inv_rho, RedScratch sc, double* out,
+                                                                 float* __restrict__ r_lo) {
     float acc = 0.f;
     auto body = [&](int xi, int yi, int zi) {
         const long long i = lin(d, xi, yi, zi);
@@ -310,8 +311,10 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_rhs_be_defect(Dims d, int co
         helm_point_q(d, comp, s_minus, uold, xi, yi, zi, hx, q);
         b_out[i] = b;
         q_out[i] = q;
-        const float ri = float(b - hx);
+        const double rd = b - hx;
+        const float ri = float(rd);
         r_out[i] = ri;
+        if (r_lo) r_lo[i] = float(rd - cvt<double, float>(ri));  // exact difference, rounded
         acc += ri * ri;
     };
     if (WALK) {
@@ -448,12 +451,14 @@ __global__ void k_cg_direction(long long N, T* __restrict__ p, const T* __restri
 template <typename TD, bool WALK>
 __global__ void __launch_bounds__(kRedBlock) k_helm_defect(Dims d, int comp, double s, const double* __restrict__ x,
                                                           const double* __restrict__ b, TD* __restrict__ r,
-                                                          RedScratch sc, double* out) {
+                                                          RedScratch sc, double* out, float* __restrict__ r_lo) {
     TD acc = TD(0);
     auto body = [&](int xi, int yi, int zi) {
         const long long i = lin(d, xi, yi, zi);
-        const TD ri = TD(b[i] - helm_point(d, comp, s, x, xi, yi, zi));
+        const double rd = b[i] - helm_point(d, comp, s, x, xi, yi, zi);
+        const TD ri = TD(rd);
         r[i] = ri;
+        if (r_lo) r_lo[i] = float(rd - cvt<double, TD>(ri));  // exact difference, rounded
         acc += ri * ri;
     };
     if (WALK) {
@@ -706,13 +711,14 @@ void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const
 template <typename TF, typename TA>
 void launch_helm_rhs_be_defect(const Dims& d, int comp, double* b, float* r, double* q, const double* uold,
                                const TF* f, const TA* adv, const double* top, const double* bottom, double s_minus,
-                               double dt, double inv_rho, RedScratch sc, double* out, cudaStream_t s, int walk_blocks) {
+                               double dt, double inv_rho, RedScratch sc, double* out, cudaStream_t s, int walk_blocks,
+                               float* r_lo) {
     if (walk_blocks > 0)
         k_helm_rhs_be_defect<TF, TA, true><<<walk_grid(d, walk_blocks), dim3(kRBX, kRBY), 0, s>>>(
-            d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out);
+            d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out, r_lo);
     else
         k_helm_rhs_be_defect<TF, TA, false><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(
-            d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out);
+            d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out, r_lo);
 }
 template <typename TF, typename TA>
 void launch_helm_rhs_cn_q(const Dims& d, int comp, double* r, const double* uold, const double* q, const TF* f,
@@ -723,10 +729,11 @@ void launch_helm_rhs_cn_q(const Dims& d, int comp, double* r, const double* uold
 }
 template void launch_helm_rhs_be_defect<double, float>(const Dims&, int, double*, float*, double*, const double*,
                                                        const double*, const float*, const double*, const double*,
-                                                       double, double, double, RedScratch, double*, cudaStream_t, int);
+                                                       double, double, double, RedScratch, double*, cudaStream_t, int,
+                                                       float*);
 template void launch_helm_rhs_be_defect<float, float>(const Dims&, int, double*, float*, double*, const double*,
                                                       const float*, const float*, const double*, const double*, double,
-                                                      double, double, RedScratch, double*, cudaStream_t, int);
+                                                      double, double, RedScratch, double*, cudaStream_t, int, float*);
 template void launch_helm_rhs_cn_q<double, float>(const Dims&, int, double*, const double*, const double*,
                                                   const double*, const float*, const double*, const double*, double,
                                                   double, double, double, cudaStream_t);
@@ -736,12 +743,73 @@ template void launch_helm_rhs_cn_q<float, float>(const Dims&, int, double*, cons
 
 template <typename TD>
 void launch_helm_defect(const Dims& d, int comp, double scale, const double* x, const double* b, TD* r, RedScratch sc,
-                        double* out, cudaStream_t s, int walk_blocks) {
+                        double* out, cudaStream_t s, int walk_blocks, float* r_lo) {
     if (walk_blocks > 0)
-        k_helm_defect<TD, true><<<walk_grid(d, walk_blocks), dim3(kRBX, kRBY), 0, s>>>(d, comp, scale, x, b, r, sc, out);
+        k_helm_defect<TD, true><<<walk_grid(d, walk_blocks), dim3(kRBX, kRBY), 0, s>>>(d, comp, scale, x, b, r, sc, out,
+                                                                                       r_lo);
     else
         k_helm_defect<TD, false><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, scale, x, b, r, sc,
-                                                                                            out);
+                                                                                            out, r_lo);
+}
+
+// Mixed form, recursive outer residual of a viscous solve: with the FP32
+// correction e of the last inner solve, x += e (FP64, as k_add_correction)
+// and the residual, kept as a double-float pair (rh: the FP32 residual the
+// inner solve reads, the float nearest to the pair; rl: the rest), loses
+// H e evaluated in double-float (df_helm_row); out[0] = rh.rh, as the FP64
+// defect's norm. HBM bound: 40 bytes per cell, no FP64 stencil.
+__global__ void __launch_bounds__(kRedBlock) k_helm_update_df(Dims d, int comp, df2 off, df2 cxa,
+                                                             double* __restrict__ x, const float* __restrict__ e,
+                                                             float* __restrict__ rh, float* __restrict__ rl,
+                                                             RedScratch sc, double* out) {
+    float acc = 0.f;
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+    if (xi < d.nx && yi < d.ny)
+        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
+            const long long i = lin(d, xi, yi, zi);
+            const float e0 = e[i];
+            float nb[6];
+            nb[0] = e[lin(d, xm1(d, xi), yi, zi)];
+            nb[1] = e[lin(d, xp1(d, xi), yi, zi)];
+            df2 he;
+            if (d.nz == 1) {
+                nb[2] = e[lin(d, xi, ym1(d, yi), zi)];
+                nb[3] = e[lin(d, xi, yp1(d, yi), zi)];
+                he = df_helm_row(e0, nb, 4, 4.f, off, 0.f, cxa, false);
+            } else if (d.channel && comp == 1 && yi == 0) {
+                he.hi = e0;  // the v wall plane: identity rows
+                he.lo = 0.f;
+            } else {
+                nb[2] = e[lin(d, xi, yi, zm1(d, zi))];
+                nb[3] = e[lin(d, xi, yi, zp1(d, zi))];
+                if (d.channel && comp != 1 && (yi == 0 || yi == d.ny - 1)) {
+                    const float xa = e[lin(d, xi, yi == 0 ? 1 : yi - 1, zi)];
+                    he = df_helm_row(e0, nb, 4, 8.f, off, xa, cxa, true);
+                } else {
+                    nb[4] = e[lin(d, xi, ym1(d, yi), zi)];
+                    nb[5] = e[lin(d, xi, yp1(d, yi), zi)];
+                    he = df_helm_row(e0, nb, 6, 6.f, off, 0.f, cxa, false);
+                }
+            }
+            df2 r;
+            r.hi = rh[i];
+            r.lo = rl[i];
+            r = df_add(r, df_neg(he));
+            rh[i] = r.hi;
+            rl[i] = r.lo;
+            x[i] = x[i] + cvt<double, float>(e0);
+            acc += r.hi * r.hi;
+        }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, out);
+}
+
+void launch_helm_update_df(const Dims& d, int comp, double scale, double* x, const float* e, float* rh, float* rl,
+                           RedScratch sc, double* out, cudaStream_t s) {
+    const double off = scale * double(d.n) * double(d.n);
+    k_helm_update_df<<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, df_split(off),
+                                                                               df_split(off + off / 3.0), x, e, rh, rl,
+                                                                               sc, out);
 }
 template <typename T>
 void launch_cg_init_zero(long long n, const T* b, T* x, T* r, T* p, RedScratch sc, double* cgs, cudaStream_t s) {
@@ -926,7 +994,7 @@ void launch_helm_defect_bfp(const Dims& d, int comp, double scale, const double*
     k_helm_defect_bfp<<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, scale, x, b, r, sc, out);
 }
 template void launch_helm_defect<float>(const Dims&, int, double, const double*, const double*, float*, RedScratch,
-                                        double*, cudaStream_t, int);
+                                        double*, cudaStream_t, int, float*);
 template void launch_cg_dir_apply<float>(const Dims&, int, double, const float*, const float*, float*, float*,
                                          RedScratch, double*, cudaStream_t);
 template void launch_cg_init_zero<float>(long long, const float*, float*, float*, float*, RedScratch, double*,

@@ -65,6 +65,15 @@ struct afmib_solver {
     cudaStream_t aux = nullptr, hi = nullptr;
     cudaEvent_t ev_def[3] = {}, ev_cor[3] = {}, ev_join = nullptr;
     float* d32c[3] = {};  // per-component defects; d32c[0] is d32
+    // interleaved solves: after the first FP64 defect, the outer residual of
+    // each viscous solve is kept as a double-float pair (d32c[c], rlo[c]) and
+    // updated by r -= H e in double-float on the correction stream (an
+    // HBM-bound pass fused with x += e) instead of re-evaluating b - H x with
+    // the FP64 stencil (AFMIB_HELM_DF=0: FP64 defects); red2 is that
+    // stream's reduction scratch
+    bool helm_df = true;
+    float* rlo[3] = {};
+    RedScratch red2{};
     double *divb = nullptr, *walls = nullptr, *wallgrad = nullptr;
     double *cg_r = nullptr, *cg_p = nullptr, *cg_q = nullptr;
     double *tmp[3] = {};
@@ -284,14 +293,15 @@ enum ProfId {
     P_ADVECT, P_HELM_RHS, P_CG_INIT, P_CG_APPLY, P_CG_UPDATE, P_CG_DIR, P_RBGS, P_RESID, P_RESID_NORM,
     P_RESTRICT, P_PROLONG, P_COARSE, P_DIV, P_GRAD_SUB, P_MEAN, P_WALL, P_SPRINGS, P_PREP, P_SORT,
     P_TILES, P_SPREAD, P_INTERP, P_MARKER, P_HELM_DEFECT, P_LAP_DEFECT, P_CORRECT, P_ADJ_ADVECT, P_ADJ_MARKER,
-    P_RBGS0, P_RESID0, P_RESTRICT0, P_PROLONG0, P_CG_DIRAPPLY, P_TAIL, P_JACOBI, P_COUNT
+    P_RBGS0, P_RESID0, P_RESTRICT0, P_PROLONG0, P_CG_DIRAPPLY, P_TAIL, P_JACOBI, P_HELM_UPDATE, P_COUNT
 };
 const char* kProfNames[P_COUNT] = {
     "advect", "helm_rhs", "cg_init", "cg_apply", "cg_update", "cg_direction", "mg_rbgs", "mg_residual",
     "mg_residual_norm", "mg_restrict", "mg_prolong_add", "mg_coarse_cg", "div", "grad_sub", "mean_removal",
     "wall_update", "springs", "marker_prep", "radix_sort", "tile_bins", "spread_gather", "interp", "marker_update",
     "helm_defect_fp64", "lap_defect_fp64", "add_correction_fp64", "advect_adjoint", "marker_adjoint",
-    "mg_rbgs_fine", "mg_residual_fine", "mg_restrict_fine", "mg_prolong_add_fine", "cg_dir_apply", "mg_coarse_tail", "helm_jacobi_fp32"};
+    "mg_rbgs_fine", "mg_residual_fine", "mg_restrict_fine", "mg_prolong_add_fine", "cg_dir_apply", "mg_coarse_tail", "helm_jacobi_fp32",
+    "helm_update_df"};
 
 cudaEvent_t prof_event(afmib_solver* s) {
     if (!s->prof_pool.empty()) {
@@ -321,22 +331,25 @@ void prof_flush(afmib_solver* s) {
 
 // Brackets one (or a fixed group of) kernel launch(es) with events when
 // profiling is on; counts the launches either way.
+// q: the stream the launches go to (default: the solver's stream).
 struct ProfScope {
     afmib_solver* s;
     int id;
     double bytes;
+    cudaStream_t q;
     cudaEvent_t a = nullptr;
-    ProfScope(afmib_solver* s_, int id_, double bytes_, int launches = 1) : s(s_), id(id_), bytes(bytes_) {
+    ProfScope(afmib_solver* s_, int id_, double bytes_, int launches = 1, cudaStream_t q_ = nullptr)
+        : s(s_), id(id_), bytes(bytes_), q(q_ ? q_ : s_->st) {
         s->stats.kernel_launches += launches;
         if (s->prof) {
             a = prof_event(s);
-            cudaEventRecord(a, s->st);
+            cudaEventRecord(a, q);
         }
     }
     ~ProfScope() {
         if (s->prof && a) {
             cudaEvent_t b = prof_event(s);
-            cudaEventRecord(b, s->st);
+            cudaEventRecord(b, q);
             s->prof_pend.push_back({id, a, b, bytes});
         }
     }
@@ -815,10 +828,12 @@ int helm_solve_mixed(afmib_solver* s, int comp, double scale, double* x, const d
 // defects, corrections and stopping test, bit for bit); only the order of
 // the norms' partial sums differs. first(c) launches component c's first
 // defect into d32c[c] with its squared norm in scal[12 + c]. Needs the
-// Gauss-Seidel inner solve (helm_overlap_ok).
+// Gauss-Seidel inner solve (helm_overlap_ok). With per-kernel profiling on,
+// each launch is timed by events on its own stream (durations of kernels
+// that ran side by side overlap).
 bool helm_overlap_ok(afmib_solver* s, double scale) {
     const Dims& d = s->d;
-    return s->helm_overlap && s->aux && s->hi && !s->prof && s->gs_inner && !s->bfp_defects &&
+    return s->helm_overlap && s->aux && s->hi && s->gs_inner && !s->bfp_defects &&
            gs_sweeps(d, scale, s->cfg.inner_tol) > 0 && d.nz % 8 == 0 && d.nx % 2 == 0 && ix2_ok(d);
 }
 
@@ -829,18 +844,19 @@ int helm_solve3_mixed(afmib_solver* s, double scale, double* const x[3], const d
     const int gsw = gs_sweeps(d, scale, s->cfg.inner_tol);
     const bool big = s->alternate && (double)N * sizeof(float) >= 32.0 * (1 << 20);
     cudaStream_t hs = s->hi;
-    auto post = [&](int c) -> int {
-        CK(cudaMemcpyAsync(s->hscal + 12 + c, s->scal + 12 + c, sizeof(double), cudaMemcpyDeviceToHost, hs));
-        CK(cudaEventRecord(s->ev_def[c], hs));
+    const bool df = s->helm_df && s->rlo[0];
+    auto post = [&](int c, cudaStream_t q) -> int {
+        CK(cudaMemcpyAsync(s->hscal + 12 + c, s->scal + 12 + c, sizeof(double), cudaMemcpyDeviceToHost, q));
+        CK(cudaEventRecord(s->ev_def[c], q));
         return AFMIB_OK;
     };
     CK(cudaEventRecord(s->ev_join, s->st));
     CK(cudaStreamWaitEvent(hs, s->ev_join, 0));
     int ring[3], head = 0, count = 0, outer[3] = {0, 0, 0};
     for (int c = 0; c < 3; ++c) {
-        first(c, hs);
+        first(c, hs, df ? s->rlo[c] : nullptr);
         CKL();
-        TRY(post(c));
+        TRY(post(c, hs));
         ring[count++] = c;
     }
     int status = AFMIB_OK;
@@ -864,25 +880,35 @@ int helm_solve3_mixed(afmib_solver* s, double scale, double* const x[3], const d
         int rev = 1;  // the defect's walk ended at the last z planes
         for (int j = 0; j < gsw; ++j)
             for (int color = 0; color < 2; ++color) {
-                ProfScope ps(s, P_JACOBI, (double)N * 4 * 1.5);
+                ProfScope ps(s, P_JACOBI, (double)N * 4 * 1.5, 1, s->aux);
                 launch_helm_rbgs<float>(d, c, scale, color, j == 0 && color == 0, s->e32, s->d32c[c], s->aux,
                                         big ? rev : 0);
                 rev ^= 1;
             }
+        if (df) {
+            ProfScope ps(s, P_HELM_UPDATE, (double)N * (8 + 4 + 8 + 8 + 8 + 4), 1, s->aux);
+            launch_helm_update_df(d, c, scale, x[c], s->e32, s->d32c[c], s->rlo[c], s->red2, s->scal + 12 + c,
+                                  s->aux);
+            CKL();
+            TRY(post(c, s->aux));
+            ring[(head + count++) % 3] = c;
+            ++outer[c];
+            continue;
+        }
         {
-            ProfScope ps(s, P_CORRECT, (double)N * (8 + 4 + 8));
+            ProfScope ps(s, P_CORRECT, (double)N * (8 + 4 + 8), 1, s->aux);
             launch_add_correction<float>(N, x[c], s->e32, s->aux);
         }
         CKL();
         CK(cudaEventRecord(s->ev_cor[c], s->aux));
         CK(cudaStreamWaitEvent(hs, s->ev_cor[c], 0));
         {
-            ProfScope ps(s, P_HELM_DEFECT, (double)N * (8 + 8 + 4));
+            ProfScope ps(s, P_HELM_DEFECT, (double)N * (8 + 8 + 4), 1, hs);
             launch_helm_defect<float>(d, c, scale, x[c], b[c], s->d32c[c], s->red, s->scal + 12 + c, hs,
                                       s->walk_blocks);
         }
         CKL();
-        TRY(post(c));
+        TRY(post(c, hs));
         ring[(head + count++) % 3] = c;
         ++outer[c];
     }
@@ -892,9 +918,14 @@ int helm_solve3_mixed(afmib_solver* s, double scale, double* const x[3], const d
         cudaStreamSynchronize(s->st);
         return status;
     }
-    // every correction was followed by a defect on hs: joining hs joins both
+    // FP64 defects: every correction was followed by a defect on hs, so
+    // joining hs joins both; double-float updates: join both streams
     CK(cudaEventRecord(s->ev_join, hs));
     CK(cudaStreamWaitEvent(s->st, s->ev_join, 0));
+    if (df) {
+        CK(cudaEventRecord(s->ev_cor[0], s->aux));
+        CK(cudaStreamWaitEvent(s->st, s->ev_cor[0], 0));
+    }
     return AFMIB_OK;
 }
 
@@ -1017,27 +1048,27 @@ int substep(afmib_solver* s) {
             *top = (!d.channel || c == 1) ? nullptr : (c == 0 ? ut : wt);
             *bot = (!d.channel || c == 1) ? nullptr : (c == 0 ? ub : wb);
         };
-        auto be_first = [&](int c, float* r, double* out, int wblocks, cudaStream_t q) {
+        auto be_first = [&](int c, float* r, double* out, int wblocks, cudaStream_t q, float* lo) {
             const double *top, *bot;
             walls_of(c, &top, &bot);
-            ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 4 + 8 + 8 + 4));
+            ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 4 + 8 + 8 + 4), 1, q);
             if (s->spread64)
                 launch_helm_rhs_be_defect<double, float>(d, c, s->rhs[c], r, s->qo[c], s->uo[c], s->f[c], s->adv32[c],
                                                          top, bot, s->s_minus(), s->cfg.dt, inv_rho, s->red, out, q,
-                                                         wblocks);
+                                                         wblocks, lo);
             else
                 launch_helm_rhs_be_defect<float, float>(d, c, s->rhs[c], r, s->qo[c], s->uo[c], s->f32[c],
                                                         s->adv32[c], top, bot, s->s_minus(), s->cfg.dt, inv_rho,
-                                                        s->red, out, q, wblocks);
+                                                        s->red, out, q, wblocks, lo);
         };
         if (be) {
             if (ovl) {
-                TRY(helm_solve3_mixed(s, s->s_minus(), vel, s->rhs, [&](int c, cudaStream_t hs) {
-                    be_first(c, s->d32c[c], s->scal + 12 + c, s->walk_blocks_be, hs);
+                TRY(helm_solve3_mixed(s, s->s_minus(), vel, s->rhs, [&](int c, cudaStream_t hs, float* lo) {
+                    be_first(c, s->d32c[c], s->scal + 12 + c, s->walk_blocks_be, hs, lo);
                 }));
             } else {
                 for (int c = 0; c < 3; ++c) {
-                    be_first(c, s->d32, s->scal + 10, 0, s->st);
+                    be_first(c, s->d32, s->scal + 10, 0, s->st, nullptr);
                     CKL();
                     TRY(helm_solve_mixed(s, c, s->s_minus(), vel[c], s->rhs[c], true));
                 }
@@ -1069,10 +1100,10 @@ int substep(afmib_solver* s) {
             }
             CKL();
             if (ovl) {
-                TRY(helm_solve3_mixed(s, s->s_minus(), vel, s->rhs, [&](int c, cudaStream_t hs) {
-                    ProfScope ps(s, P_HELM_DEFECT, (double)N * (8 + 8 + 4));
+                TRY(helm_solve3_mixed(s, s->s_minus(), vel, s->rhs, [&](int c, cudaStream_t hs, float* lo) {
+                    ProfScope ps(s, P_HELM_DEFECT, (double)N * (8 + 8 + 4), 1, hs);
                     launch_helm_defect<float>(d, c, s->s_minus(), vel[c], s->rhs[c], s->d32c[c], s->red,
-                                              s->scal + 12 + c, hs, s->walk_blocks);
+                                              s->scal + 12 + c, hs, s->walk_blocks, lo);
                 }));
             } else {
                 for (int c = 0; c < 3; ++c) TRY(helm_solve_mixed(s, c, s->s_minus(), vel[c], s->rhs[c]));
@@ -1751,6 +1782,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     TRY(dalloc(s, &s->divb, N));
     if (const char* e = std::getenv("AFMIB_FUSED_RHS")) s->fused_rhs = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_HELM_OVERLAP")) s->helm_overlap = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_HELM_DF")) s->helm_df = std::string(e) != "0";
     if (s->mixed && s->fused_rhs)
         for (auto& q : s->qo) TRY(dalloc(s, &q, N));
     TRY(dalloc(s, &s->phi_prev[0], N));
@@ -1830,6 +1862,12 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
         if (s->helm_overlap) {
             TRY(dalloc(s, &s->d32c[1], N));
             TRY(dalloc(s, &s->d32c[2], N));
+            if (s->helm_df) {
+                for (int k = 0; k < 3; ++k) TRY(dalloc(s, &s->rlo[k], N));
+                TRY(dalloc(s, &s->red2.partial, (size_t)kMaxRedBlocks * kMaxRedVals));
+                TRY(dalloc(s, &s->red2.ticket, 1));
+                CK(cudaMemsetAsync(s->red2.ticket, 0, sizeof(unsigned), s->st));
+            }
             CK(cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking));
             int least = 0, greatest = 0;
             CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));

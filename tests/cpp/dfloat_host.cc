@@ -62,3 +62,18 @@ void afmib_test_fixed(long long q, int E, float* hi, float* lo) {
     *lo = r.lo;
 }
 }
+
+extern "C" {
+// r - H e for an FP32 correction e in double-float (df_helm_row), the FP64
+// residual r given as its double-float pair (rh, rl); returns the new pair
+void afmib_test_helm_update_df(float rh, float rl, float e0, const float* nb, int nnb, float k, double off, float xa,
+                               double cxa, int wall, float* oh, float* ol) {
+    afmib::df2 r;
+    r.hi = rh;
+    r.lo = rl;
+    const afmib::df2 he = afmib::df_helm_row(e0, nb, nnb, k, afmib::df_split(off), xa, afmib::df_split(cxa), wall != 0);
+    r = afmib::df_add(r, afmib::df_neg(he));
+    *oh = r.hi;
+    *ol = r.lo;
+}
+}

@@ -554,15 +554,17 @@ def test_alternating_block_order_keeps_bits(monkeypatch, precision):
 def test_interleaved_viscous_solves_keep_bits(monkeypatch, n, bc, markers):
     """Mixed form: the three viscous solves of a sub-step interleaved on two
     streams (one component's FP32 correction beside the next component's FP64
-    defect, the defects on a persistent grid of 2 or 8 blocks per SM) go
-    through the same defects, corrections and stopping tests as the solves one
-    after another (AFMIB_HELM_OVERLAP=0): the same velocity, pressure and
-    markers bit for bit, and the same number of defect-correction steps."""
+    defect, the defects on a persistent grid of 3 or 8 blocks per SM; FP64
+    defects throughout, AFMIB_HELM_DF=0) go through the same defects,
+    corrections and stopping tests as the solves one after another
+    (AFMIB_HELM_OVERLAP=0): the same velocity, pressure and markers bit for
+    bit, and the same number of defect-correction steps."""
     channel = bc == capi.BC_CHANNEL
     g = po.Grid(n, n, n, n, channel=channel)
     rng = np.random.default_rng(28)
     u, v, w = 0.1 * rng.standard_normal(g.ncell), 0.1 * rng.standard_normal(g.nv), 0.1 * rng.standard_normal(g.ncell)
     f = [rng.standard_normal(g.ncell), rng.standard_normal(g.nv), rng.standard_normal(g.ncell)]
+    monkeypatch.setenv("AFMIB_HELM_DF", "0")
     out = {}
     for mode, blocks in (("0", None), ("1", None), ("1", "8")):
         monkeypatch.setenv("AFMIB_HELM_OVERLAP", mode)
@@ -593,6 +595,41 @@ def test_interleaved_viscous_solves_keep_bits(monkeypatch, n, bc, markers):
         if markers:
             assert np.array_equal(ref[2], got[2])
         assert ref[3] == got[3]
+
+
+@pytest.mark.parametrize("n,bc,markers", [(64, capi.BC_PERIODIC, True), (64, capi.BC_CHANNEL, False),
+                                          (32, capi.BC_CHANNEL, True), (256, capi.BC_PERIODIC, False)])
+def test_double_float_outer_residual(monkeypatch, n, bc, markers):
+    """Mixed form: after each viscous solve's first FP64 defect, its outer
+    residual is kept as a double-float pair and updated by r -= H e (the FP32
+    correction's row sums in double-float, 2^-46) instead of re-evaluating
+    b - H x with the FP64 stencil. The FP64 state x takes the same += e, the
+    stopping test the same norm, so the sub-steps agree with the FP64-defect
+    solves to the solver tolerance (1e-10 relative, as the inner-solver
+    variants) and with the FP64 form to the mixed form's 1e-8 bar."""
+    channel = bc == capi.BC_CHANNEL
+    g = po.Grid(n, n, n, n, channel=channel)
+    rng = np.random.default_rng(32)
+    u, v, w = 0.1 * rng.standard_normal(g.ncell), 0.1 * rng.standard_normal(g.nv), 0.1 * rng.standard_normal(g.ncell)
+    f = [rng.standard_normal(g.ncell), rng.standard_normal(g.nv), rng.standard_normal(g.ncell)]
+    _, _, _, _, X, nstart, nidx = _periodic_case(n, M=2000, seed=33)
+    out = {}
+    for key, prec, df in (("fp64", capi.FP64, "1"), ("defects", capi.MIXED, "0"), ("df", capi.MIXED, "1")):
+        monkeypatch.setenv("AFMIB_HELM_DF", df)
+        with capi.Solver(n, bc=bc, precision=prec, mu=0.01, rho=1.0, dt=1e-3, tol=1e-11, k_spring=0.5) as sv:
+            sv.set_velocity(u, v, w)
+            sv.project()
+            if markers:
+                sv.set_markers(X, nstart, nidx)
+                sv.ib_step(3)
+            else:
+                for _ in range(4):
+                    sv.ns_step(*f)
+            out[key] = sv.get_velocity()
+    for a, b in zip(out["defects"], out["df"]):
+        assert rel(b, a) < 1e-10
+    for a, b in zip(out["fp64"], out["df"]):
+        assert rel(b, a) < 1e-8
 
 
 @pytest.mark.parametrize("m", [1200, 5000, 20000])
