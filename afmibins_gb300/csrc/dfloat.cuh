@@ -149,6 +149,24 @@ AFMIB_HD df2 df_add_f(df2 a, float b) {
     return r;
 }
 
+// One row of the pressure Laplacian applied to an FP32 correction e, in
+// double-float: L e = off (sum(nb) - c e0), off = n^2 (exact as a float for
+// n < 4096; missing channel neighbours passed as 0).
+AFMIB_HD df2 df_lap_row(float e0, const float* nb, int nnb, float c, float off) {
+    df2 q;
+    q.hi = nb[0];
+    q.lo = 0.f;
+    for (int j = 1; j < nnb; ++j) q = df_add_f(q, nb[j]);
+    df2 ce;
+    ce.hi = c * e0;
+    ce.lo = fmaf(c, e0, -ce.hi);
+    q = df_add(q, df_neg(ce));
+    df2 o;
+    o.hi = off;
+    o.lo = 0.f;
+    return df_mul(q, o);
+}
+
 // ---------------------------------------------------------------------------
 // One row of the viscous operator applied to an FP32 correction e, in
 // double-float: H e = e0 + off Q(e), Q = sum(nb) - k e0, plus cxa * xa for

@@ -136,7 +136,12 @@ void launch_residual(const Dims& d, T* r, const T* x, const T* b, RedScratch* sc
                      int rev = 0);
 // Mixed form: r = b - L x evaluated in FP64 (x, b FP64), stored as TD; out[0] = r.r
 template <typename TD>
-void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, RedScratch sc, double* out, cudaStream_t s);
+void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, RedScratch sc, double* out, cudaStream_t s,
+                       float* r_lo = nullptr);
+// Mixed form: x += e, (rh, rl) -= L e in double-float, out[0] = rh.rh
+// (r_lo of launch_lap_defect starts the pair)
+void launch_lap_update_df(const Dims& d, double* x, const float* e, float* rh, float* rl, RedScratch sc, double* out,
+                          cudaStream_t s);
 // The mixed form's FP64-state defects evaluated with int64 block arithmetic
 // and float pairs (no FP64 instruction; see dfloat.cuh). The Laplacian form
 // needs n a power of two and returns false (nothing launched) otherwise.

@@ -5,6 +5,7 @@
 // output array.
 #include "dfloat.cuh"
 #include "kernels.h"
+#include <algorithm>
 
 namespace afmib {
 
@@ -804,12 +805,92 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_update_df(Dims d, int comp, 
     grid_sum<1>(a, sc, out);
 }
 
+// The same for power-of-two grids with nz % ZU == 0: each thread takes ZU
+// consecutive z cells of one (x, y) column (the column's e values reused from
+// registers, 32-bit shift-composed indices, every load of the batch issued
+// before the rows are evaluated), blocks walk z batches in steps of grid.z;
+// the same arithmetic per cell, so the same bits.
+template <int ZU>
+__global__ void __launch_bounds__(kRedBlock) k_helm_update_df2(Dims d, int comp, df2 off, df2 cxa,
+                                                              double* __restrict__ x, const float* __restrict__ e,
+                                                              float* __restrict__ rh, float* __restrict__ rl,
+                                                              RedScratch sc, double* out) {
+    const Ix2 I(d);
+    float acc = 0.f;
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+    const bool vwall = d.channel && comp == 1 && yi == 0;
+    const bool uwall = d.channel && comp != 1 && (yi == 0 || yi == d.ny - 1);
+    // in-plane neighbours: x -+ 1 and y -+ 1 (u/w wall rows: the row away from the wall)
+    const int ya = uwall ? (yi == 0 ? 1 : yi - 1) : I.ym(yi), yb = I.yp(yi);
+    if (xi < d.nx && yi < d.ny)
+        for (int zb = blockIdx.z; zb < d.nz / ZU; zb += gridDim.z) {
+            const int z0 = zb * ZU;
+            // every load of the batch first (independent, in flight together), then the rows
+            float col[ZU + 2], ex0[ZU], ex1[ZU], ey0[ZU], ey1[ZU], h[ZU], l[ZU];
+            double xv[ZU];
+#pragma unroll
+            for (int u = 0; u < ZU + 2; ++u) col[u] = e[I.at(xi, yi, (z0 + u - 1) & I.mz)];  // z0 - 1 .. z0 + ZU
+#pragma unroll
+            for (int u = 0; u < ZU; ++u) {
+                const int z = z0 + u, i = I.at(xi, yi, z);
+                ex0[u] = e[I.at(I.xm(xi), yi, z)];
+                ex1[u] = e[I.at(I.xp(xi), yi, z)];
+                ey0[u] = e[I.at(xi, ya, z)];
+                ey1[u] = uwall ? 0.f : e[I.at(xi, yb, z)];
+                h[u] = rh[i];
+                l[u] = rl[i];
+                xv[u] = x[i];
+            }
+#pragma unroll
+            for (int u = 0; u < ZU; ++u) {
+                const int i = I.at(xi, yi, z0 + u);
+                const float e0 = col[u + 1];
+                df2 he;
+                if (vwall) {
+                    he.hi = e0;
+                    he.lo = 0.f;
+                } else {
+                    float nb[6] = {ex0[u], ex1[u], col[u], col[u + 2], ey0[u], ey1[u]};
+                    he = uwall ? df_helm_row(e0, nb, 4, 8.f, off, ey0[u], cxa, true)
+                               : df_helm_row(e0, nb, 6, 6.f, off, 0.f, cxa, false);
+                }
+                df2 r;
+                r.hi = h[u];
+                r.lo = l[u];
+                r = df_add(r, df_neg(he));
+                rh[i] = r.hi;
+                rl[i] = r.lo;
+                x[i] = xv[u] + cvt<double, float>(e0);
+                acc += r.hi * r.hi;
+            }
+        }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, out);
+}
+
+// AFMIB_UPDATE_DF_GENERIC=1: the general kernel on power-of-two grids too
+// (read at every launch, so that a test compares both in one process)
+static bool update_df_generic() {
+    const char* e = std::getenv("AFMIB_UPDATE_DF_GENERIC");
+    return e && e[0] == '1';
+}
+
 void launch_helm_update_df(const Dims& d, int comp, double scale, double* x, const float* e, float* rh, float* rl,
                            RedScratch sc, double* out, cudaStream_t s) {
     const double off = scale * double(d.n) * double(d.n);
-    k_helm_update_df<<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, df_split(off),
-                                                                               df_split(off + off / 3.0), x, e, rh, rl,
-                                                                               sc, out);
+    const df2 o = df_split(off), c = df_split(off + off / 3.0);
+    // two z cells per thread: 46.4 IB steps/s at 256^3 against 46.3 for four
+    // and 45.5 for eight (more registers, fewer warps) and 45.5 for the
+    // general kernel
+    constexpr int ZU = 2;
+    if (d.nz > 1 && d.nz % ZU == 0 && ix2_ok(d) && !update_df_generic()) {
+        const int gx = (d.nx + kRBX - 1) / kRBX, gy = (d.ny + kRBY - 1) / kRBY;
+        int gz = d.nz / ZU;
+        if ((long long)gx * gy * gz > kMaxRedBlocks) gz = std::max(1, kMaxRedBlocks / (gx * gy));
+        k_helm_update_df2<ZU><<<dim3(gx, gy, gz), dim3(kRBX, kRBY), 0, s>>>(d, comp, o, c, x, e, rh, rl, sc, out);
+        return;
+    }
+    k_helm_update_df<<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, o, c, x, e, rh, rl, sc, out);
 }
 template <typename T>
 void launch_cg_init_zero(long long n, const T* b, T* x, T* r, T* p, RedScratch sc, double* cgs, cudaStream_t s) {

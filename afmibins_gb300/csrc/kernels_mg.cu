@@ -85,9 +85,12 @@ __global__ void __launch_bounds__(kRedBlock) k_residual_norm(Dims d, T* __restri
 
 // Mixed form: defect of the FP64 potential, r = b - L x evaluated in FP64 and
 // stored in TD for the FP32 inner V-cycles; out[0] = r.r.
+// r_lo: also the rest of the FP64 residual, float(r - r_float), the second
+// word of the double-float pair that k_lap_update_df updates.
 template <typename TD>
 __global__ void __launch_bounds__(kRedBlock) k_lap_defect(Dims d, TD* __restrict__ r, const double* __restrict__ xv,
-                                                         const double* __restrict__ b, RedScratch sc, double* out) {
+                                                         const double* __restrict__ b, RedScratch sc, double* out,
+                                                         float* __restrict__ r_lo) {
     const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
     const double off = double(d.n) * double(d.n);
     TD acc = TD(0);
@@ -97,9 +100,111 @@ __global__ void __launch_bounds__(kRedBlock) k_lap_defect(Dims d, TD* __restrict
             double S, c;
             lap_row(d, xv, xi, yi, zi, S, c);
             const long long i = lin(d, xi, yi, zi);
-            const TD ri = TD(b[i] - off * (S - c * xv[i]));
+            const double rd = b[i] - off * (S - c * xv[i]);
+            const TD ri = TD(rd);
             r[i] = ri;
+            if (r_lo) r_lo[i] = float(rd - cvt<double, TD>(ri));  // exact difference, rounded
             acc += ri * ri;
+        }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, out);
+}
+
+// Mixed form, recursive outer residual of the pressure solve: with the FP32
+// correction e of the inner V-cycles, x += e (FP64) and the residual, kept
+// as a double-float pair (rh: the FP32 right-hand side of the V-cycles, rl:
+// the rest), loses L e evaluated in double-float (df_lap_row); out[0] =
+// rh.rh, as the FP64 defect's norm.
+__global__ void __launch_bounds__(kRedBlock) k_lap_update_df(Dims d, double* __restrict__ x,
+                                                            const float* __restrict__ e, float* __restrict__ rh,
+                                                            float* __restrict__ rl, RedScratch sc, double* out) {
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+    const float off = float(d.n) * float(d.n);
+    float acc = 0.f;
+    if (xi < d.nx && yi < d.ny)
+        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
+            const long long i = lin(d, xi, yi, zi);
+            const float e0 = e[i];
+            float nb[6];
+            int m = 0;
+            nb[m++] = e[lin(d, xm1(d, xi), yi, zi)];
+            nb[m++] = e[lin(d, xp1(d, xi), yi, zi)];
+            if (d.nz > 1) {
+                nb[m++] = e[lin(d, xi, yi, zm1(d, zi))];
+                nb[m++] = e[lin(d, xi, yi, zp1(d, zi))];
+            }
+            float c = d.nz > 1 ? 6.f : 4.f;
+            if (d.channel) {
+                if (yi > 0) nb[m++] = e[lin(d, xi, yi - 1, zi)]; else c -= 1.f;
+                if (yi < d.ny - 1) nb[m++] = e[lin(d, xi, yi + 1, zi)]; else c -= 1.f;
+            } else {
+                nb[m++] = e[lin(d, xi, ym1(d, yi), zi)];
+                nb[m++] = e[lin(d, xi, yp1(d, yi), zi)];
+            }
+            for (int j = m; j < 6; ++j) nb[j] = 0.f;
+            const df2 le = df_lap_row(e0, nb, 6, c, off);
+            df2 r;
+            r.hi = rh[i];
+            r.lo = rl[i];
+            r = df_add(r, df_neg(le));
+            rh[i] = r.hi;
+            rl[i] = r.lo;
+            x[i] = x[i] + cvt<double, float>(e0);
+            acc += r.hi * r.hi;
+        }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, out);
+}
+
+// The same on power-of-two 3D grids, two z cells per thread with every load
+// of the pair issued first (as k_helm_update_df2); the same rows, so the
+// same bits.
+template <int ZU>
+__global__ void __launch_bounds__(kRedBlock) k_lap_update_df2(Dims d, double* __restrict__ x,
+                                                             const float* __restrict__ e, float* __restrict__ rh,
+                                                             float* __restrict__ rl, RedScratch sc, double* out) {
+    const Ix2 I(d);
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+    const float off = float(d.n) * float(d.n);
+    const bool has_ym = !d.channel || yi > 0, has_yp = !d.channel || yi < d.ny - 1;
+    const float c = 6.f - (has_ym ? 0.f : 1.f) - (has_yp ? 0.f : 1.f);
+    const int ym = I.ym(yi), yp = I.yp(yi);
+    float acc = 0.f;
+    if (xi < d.nx && yi < d.ny)
+        for (int zb = blockIdx.z; zb < d.nz / ZU; zb += gridDim.z) {
+            const int z0 = zb * ZU;
+            float col[ZU + 2], ex0[ZU], ex1[ZU], ey0[ZU], ey1[ZU], h[ZU], l[ZU];
+            double xv[ZU];
+#pragma unroll
+            for (int u = 0; u < ZU + 2; ++u) col[u] = e[I.at(xi, yi, (z0 + u - 1) & I.mz)];  // z0 - 1 .. z0 + ZU
+#pragma unroll
+            for (int u = 0; u < ZU; ++u) {
+                const int z = z0 + u, i = I.at(xi, yi, z);
+                ex0[u] = e[I.at(I.xm(xi), yi, z)];
+                ex1[u] = e[I.at(I.xp(xi), yi, z)];
+                ey0[u] = has_ym ? e[I.at(xi, ym, z)] : 0.f;
+                ey1[u] = has_yp ? e[I.at(xi, yp, z)] : 0.f;
+                h[u] = rh[i];
+                l[u] = rl[i];
+                xv[u] = x[i];
+            }
+#pragma unroll
+            for (int u = 0; u < ZU; ++u) {
+                const int i = I.at(xi, yi, z0 + u);
+                const float e0 = col[u + 1];
+                // the general kernel's neighbour order: x, z, then the y neighbours present
+                float nb[6] = {ex0[u], ex1[u], col[u], col[u + 2], has_ym ? ey0[u] : ey1[u], has_ym ? ey1[u] : 0.f};
+                if (!has_yp) nb[5] = 0.f;
+                const df2 le = df_lap_row(e0, nb, 6, c, off);
+                df2 r;
+                r.hi = h[u];
+                r.lo = l[u];
+                r = df_add(r, df_neg(le));
+                rh[i] = r.hi;
+                rl[i] = r.lo;
+                x[i] = xv[u] + cvt<double, float>(e0);
+                acc += r.hi * r.hi;
+            }
         }
     double a[1] = {(double)acc};
     grid_sum<1>(a, sc, out);
@@ -1077,8 +1182,22 @@ void launch_prolong_assign(const Dims& d, T* fine, const T* coarse, cudaStream_t
     k_prolong<T, false><<<g, dim3(BX, BY), 0, s>>>(d, fine, coarse);
 }
 template <typename TD>
-void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, RedScratch sc, double* out, cudaStream_t s) {
-    k_lap_defect<TD><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, r, x, b, sc, out);
+void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, RedScratch sc, double* out, cudaStream_t s,
+                       float* r_lo) {
+    k_lap_defect<TD><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, r, x, b, sc, out, r_lo);
+}
+void launch_lap_update_df(const Dims& d, double* x, const float* e, float* rh, float* rl, RedScratch sc, double* out,
+                          cudaStream_t s) {
+    constexpr int ZU = 2;
+    const char* g = std::getenv("AFMIB_UPDATE_DF_GENERIC");
+    if (d.nz > 1 && d.nz % ZU == 0 && ix2_ok(d) && !(g && g[0] == '1')) {
+        const int gx = (d.nx + kRBX - 1) / kRBX, gy = (d.ny + kRBY - 1) / kRBY;
+        int gz = d.nz / ZU;
+        if ((long long)gx * gy * gz > kMaxRedBlocks) gz = std::max(1, kMaxRedBlocks / (gx * gy));
+        k_lap_update_df2<ZU><<<dim3(gx, gy, gz), dim3(kRBX, kRBY), 0, s>>>(d, x, e, rh, rl, sc, out);
+        return;
+    }
+    k_lap_update_df<<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, x, e, rh, rl, sc, out);
 }
 bool launch_lap_defect_bfp(const Dims& d, float* r, const double* x, const double* b, RedScratch sc, double* out,
                            cudaStream_t s) {
@@ -1089,7 +1208,7 @@ bool launch_lap_defect_bfp(const Dims& d, float* r, const double* x, const doubl
     return true;
 }
 template void launch_lap_defect<float>(const Dims&, float*, const double*, const double*, RedScratch, double*,
-                                       cudaStream_t);
+                                       cudaStream_t, float*);
 
 template <typename T>
 void launch_vcycle_tail(const TailLevels<T>& a, cudaStream_t s, int cluster) {

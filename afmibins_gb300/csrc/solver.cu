@@ -74,6 +74,12 @@ struct afmib_solver {
     bool helm_df = true;
     float* rlo[3] = {};
     RedScratch red2{};
+    // the same for the pressure solve: after its first FP64 defect the
+    // residual is the pair (lv32[0].b, plo), updated by r -= L e in
+    // double-float at the end of each block of inner V-cycles, fused with
+    // x += e (AFMIB_LAP_DF=0: an FP64 defect per block)
+    bool lap_df = true;
+    float* plo = nullptr;
     double *divb = nullptr, *walls = nullptr, *wallgrad = nullptr;
     double *cg_r = nullptr, *cg_p = nullptr, *cg_q = nullptr;
     double *tmp[3] = {};
@@ -293,7 +299,7 @@ enum ProfId {
     P_ADVECT, P_HELM_RHS, P_CG_INIT, P_CG_APPLY, P_CG_UPDATE, P_CG_DIR, P_RBGS, P_RESID, P_RESID_NORM,
     P_RESTRICT, P_PROLONG, P_COARSE, P_DIV, P_GRAD_SUB, P_MEAN, P_WALL, P_SPRINGS, P_PREP, P_SORT,
     P_TILES, P_SPREAD, P_INTERP, P_MARKER, P_HELM_DEFECT, P_LAP_DEFECT, P_CORRECT, P_ADJ_ADVECT, P_ADJ_MARKER,
-    P_RBGS0, P_RESID0, P_RESTRICT0, P_PROLONG0, P_CG_DIRAPPLY, P_TAIL, P_JACOBI, P_HELM_UPDATE, P_COUNT
+    P_RBGS0, P_RESID0, P_RESTRICT0, P_PROLONG0, P_CG_DIRAPPLY, P_TAIL, P_JACOBI, P_HELM_UPDATE, P_LAP_UPDATE, P_COUNT
 };
 const char* kProfNames[P_COUNT] = {
     "advect", "helm_rhs", "cg_init", "cg_apply", "cg_update", "cg_direction", "mg_rbgs", "mg_residual",
@@ -301,7 +307,7 @@ const char* kProfNames[P_COUNT] = {
     "wall_update", "springs", "marker_prep", "radix_sort", "tile_bins", "spread_gather", "interp", "marker_update",
     "helm_defect_fp64", "lap_defect_fp64", "add_correction_fp64", "advect_adjoint", "marker_adjoint",
     "mg_rbgs_fine", "mg_residual_fine", "mg_restrict_fine", "mg_prolong_add_fine", "cg_dir_apply", "mg_coarse_tail", "helm_jacobi_fp32",
-    "helm_update_df"};
+    "helm_update_df", "lap_update_df"};
 
 cudaEvent_t prof_event(afmib_solver* s) {
     if (!s->prof_pool.empty()) {
@@ -598,6 +604,11 @@ int vcycle64_top(afmib_solver* s) {
 // the FP32 inner solve of one defect-correction step: x32 = 0, ncyc
 // V-cycles on L e = r, phi += e (graph replay when possible, one graph per
 // cycle count)
+// the pressure solve keeps its outer residual as a double-float pair
+bool lap_df_on(const afmib_solver* s) { return s->lap_df && s->plo && !s->bfp_defects; }
+
+// One block of ncyc FP32 V-cycles from zero on the residual in lv32[0].b,
+// then x += e, and with lap_df_on also r -= L e with its norm in scal[9].
 int inner_vcycles32(afmib_solver* s, int ncyc) {
     MGLevel& L = s->lv[0];
     MGLevelT<float>& L32 = s->lv32[0];
@@ -606,7 +617,10 @@ int inner_vcycles32(afmib_solver* s, int ncyc) {
         return [&, nc]() -> int {
             CK(cudaMemsetAsync(L32.x, 0, N * sizeof(float), s->st));
             for (int k = 0; k < nc; ++k) TRY(vcycle<float>(s, 0));
-            {
+            if (lap_df_on(s)) {
+                ProfScope ps(s, P_LAP_UPDATE, (double)N * (8 + 4 + 8 + 8 + 8 + 4));
+                launch_lap_update_df(L.d, L.x, L32.x, L32.b, s->plo, s->red, s->scal + 9, s->st);
+            } else {
                 ProfScope ps(s, P_CORRECT, (double)N * (8 + 4 + 8));
                 launch_add_correction<float>(N, L.x, L32.x, s->st);
             }
@@ -944,11 +958,12 @@ int mg_solve_mixed(afmib_solver* s, int* cycles) {
     int c = 0, outer = 0, last_cyc = 0;
     double last_rms = 0.0;
     int status = AFMIB_OK;
+    const bool df = lap_df_on(s);
     for (;;) {
-        {
+        if (!(df && outer > 0)) {  // double-float: the norm came with the last block's update
             ProfScope ps(s, P_LAP_DEFECT, (double)N * (8 + 8 + 4));
             if (!s->bfp_defects || !launch_lap_defect_bfp(L.d, L32.b, L.x, L.b, s->red, s->scal + 9, s->st))
-                launch_lap_defect<float>(L.d, L32.b, L.x, L.b, s->red, s->scal + 9, s->st);
+                launch_lap_defect<float>(L.d, L32.b, L.x, L.b, s->red, s->scal + 9, s->st, df ? s->plo : nullptr);
         }
         CKL();
         TRY(read_scalars(s, 9, 1));
@@ -1783,6 +1798,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_FUSED_RHS")) s->fused_rhs = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_HELM_OVERLAP")) s->helm_overlap = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_HELM_DF")) s->helm_df = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_LAP_DF")) s->lap_df = std::string(e) != "0";
     if (s->mixed && s->fused_rhs)
         for (auto& q : s->qo) TRY(dalloc(s, &q, N));
     TRY(dalloc(s, &s->phi_prev[0], N));
@@ -1859,6 +1875,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
         TRY(dalloc(s, &s->d32, N));
         TRY(dalloc(s, &s->e32, N));
         s->d32c[0] = s->d32;
+        if (s->lap_df) TRY(dalloc(s, &s->plo, N));
         if (s->helm_overlap) {
             TRY(dalloc(s, &s->d32c[1], N));
             TRY(dalloc(s, &s->d32c[2], N));

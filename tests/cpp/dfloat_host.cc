@@ -77,3 +77,16 @@ void afmib_test_helm_update_df(float rh, float rl, float e0, const float* nb, in
     *ol = r.lo;
 }
 }
+
+extern "C" {
+// r - L e for an FP32 correction e in double-float (df_lap_row)
+void afmib_test_lap_update_df(float rh, float rl, float e0, const float* nb, int nnb, float c, float off, float* oh,
+                              float* ol) {
+    afmib::df2 r;
+    r.hi = rh;
+    r.lo = rl;
+    r = afmib::df_add(r, afmib::df_neg(afmib::df_lap_row(e0, nb, nnb, c, off)));
+    *oh = r.hi;
+    *ol = r.lo;
+}
+}

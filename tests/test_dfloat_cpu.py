@@ -33,6 +33,8 @@ def lib(tmp_path_factory):
                                           ctypes.c_int]
     L.afmib_test_lap_residual.restype = ctypes.c_float
     L.afmib_test_split.argtypes = [ctypes.c_double, fp, fp]
+    L.afmib_test_lap_update_df.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float, fp, ctypes.c_int,
+                                           ctypes.c_float, ctypes.c_float, fp, fp]
     L.afmib_test_helm_update_df.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float, fp, ctypes.c_int,
                                             ctypes.c_float, ctypes.c_double, ctypes.c_float, ctypes.c_double,
                                             ctypes.c_int, fp, fp]
@@ -170,3 +172,31 @@ def test_helm_update_df(lib, kind):
         assert abs(Fr(oh.value) + Fr(ol.value) - exact) <= bound, (it, kind)
         # the pair is normalised: hi is the float nearest to the pair
         assert oh.value == f32(Fr(oh.value) + Fr(ol.value))
+
+
+@pytest.mark.parametrize("c", [6.0, 5.0, 4.0])
+def test_lap_update_df(lib, c):
+    """Outer residual update of the mixed pressure solve, r - L e for an FP32
+    correction in double-float (df_lap_row; c = 6 interior, 5 next to a
+    channel wall, 4 in 2D, missing neighbours as zeros), against exact
+    rational arithmetic."""
+    rng = np.random.default_rng(7)
+    f32 = lambda v: float(np.float32(v))
+    for it in range(3000):
+        n = int(rng.choice([16, 64, 256, 96, 4096]))
+        off = float(n * n)
+        e0 = f32(10.0 ** rng.uniform(-10, -2) * rng.standard_normal())
+        m = int(c)
+        nb = [f32(e0 * (1 + 10.0 ** rng.uniform(-6, 0) * rng.standard_normal())) for _ in range(m)]
+        nb += [0.0] * (6 - m)
+        le = Fr(off) * (sum(Fr(v) for v in nb) - Fr(c) * Fr(e0))
+        r = float(le) * (1 + 1e-5 * rng.standard_normal())
+        rh = f32(r)
+        rl = f32(r - rh)
+        oh, ol = ctypes.c_float(), ctypes.c_float()
+        lib.afmib_test_lap_update_df(rh, rl, e0, _arr(nb, ctypes.c_float), 6, c, off, ctypes.byref(oh),
+                                     ctypes.byref(ol))
+        exact = Fr(rh) + Fr(rl) - le
+        scale = Fr(off) * (sum(abs(Fr(v)) for v in nb) + Fr(c) * abs(Fr(e0)))
+        bound = scale * Fr(2) ** -44 + (abs(Fr(rh)) + abs(Fr(rl))) * Fr(2) ** -46
+        assert abs(Fr(oh.value) + Fr(ol.value) - exact) <= bound, it

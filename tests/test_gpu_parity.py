@@ -600,13 +600,14 @@ def test_interleaved_viscous_solves_keep_bits(monkeypatch, n, bc, markers):
 @pytest.mark.parametrize("n,bc,markers", [(64, capi.BC_PERIODIC, True), (64, capi.BC_CHANNEL, False),
                                           (32, capi.BC_CHANNEL, True), (256, capi.BC_PERIODIC, False)])
 def test_double_float_outer_residual(monkeypatch, n, bc, markers):
-    """Mixed form: after each viscous solve's first FP64 defect, its outer
-    residual is kept as a double-float pair and updated by r -= H e (the FP32
-    correction's row sums in double-float, 2^-46) instead of re-evaluating
-    b - H x with the FP64 stencil. The FP64 state x takes the same += e, the
-    stopping test the same norm, so the sub-steps agree with the FP64-defect
-    solves to the solver tolerance (1e-10 relative, as the inner-solver
-    variants) and with the FP64 form to the mixed form's 1e-8 bar."""
+    """Mixed form: after the first FP64 defect of each viscous and pressure
+    solve, the outer residual is kept as a double-float pair and updated by
+    r -= H e (r -= L e) with the FP32 correction's rows in double-float
+    (2^-46) instead of re-evaluating b - H x (b - L x) with the FP64 stencil.
+    The FP64 state x takes the same += e, the stopping tests the same norms,
+    so the sub-steps agree with the FP64-defect solves to the solver
+    tolerance (1e-10 relative, as the inner-solver variants) and with the
+    FP64 form to the mixed form's 1e-8 bar."""
     channel = bc == capi.BC_CHANNEL
     g = po.Grid(n, n, n, n, channel=channel)
     rng = np.random.default_rng(32)
@@ -616,6 +617,7 @@ def test_double_float_outer_residual(monkeypatch, n, bc, markers):
     out = {}
     for key, prec, df in (("fp64", capi.FP64, "1"), ("defects", capi.MIXED, "0"), ("df", capi.MIXED, "1")):
         monkeypatch.setenv("AFMIB_HELM_DF", df)
+        monkeypatch.setenv("AFMIB_LAP_DF", df)
         with capi.Solver(n, bc=bc, precision=prec, mu=0.01, rho=1.0, dt=1e-3, tol=1e-11, k_spring=0.5) as sv:
             sv.set_velocity(u, v, w)
             sv.project()
@@ -630,6 +632,55 @@ def test_double_float_outer_residual(monkeypatch, n, bc, markers):
         assert rel(b, a) < 1e-10
     for a, b in zip(out["fp64"], out["df"]):
         assert rel(b, a) < 1e-8
+
+
+@pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
+@pytest.mark.parametrize("n", [32, 128])
+def test_pressure_double_float_residual(monkeypatch, bc, n):
+    """Mixed pressure solves with the double-float recursive residual reach
+    the reference's stopping rule on the true FP64 residual: RMS(b - mean(b)
+    - L x) <= tol, L applied in FP64 through the C ABI, and agree with the
+    FP64-defect solves to that tolerance."""
+    b = np.random.default_rng(35).standard_normal(n ** 3)
+    tol = 1e-9
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("AFMIB_LAP_DF", mode)
+        with capi.Solver(n, bc=bc, precision=capi.MIXED, tol=tol) as sv:
+            x, cycles = sv.mg_solve(b)
+            r = (b - b.mean()) - sv.lap_apply(x)
+            out[mode] = x
+        assert np.sqrt(np.mean(r ** 2)) <= tol * (1 + 1e-6)
+    # both residuals within tol: the potentials differ by L^-1 of at most
+    # 2 tol, and L's smallest nonzero eigenvalue is pi^2 or more
+    d0, d1 = demean(out["0"]), demean(out["1"])
+    assert np.max(np.abs(d1 - d0)) <= 10 * tol
+
+
+@pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
+def test_double_float_update_kernels_agree(monkeypatch, bc):
+    """The residual update's power-of-two kernel (eight z cells per thread,
+    the column reused from registers) and its general kernel
+    (AFMIB_UPDATE_DF_GENERIC=1) evaluate the same double-float rows: the same
+    velocity bit for bit."""
+    n = 64
+    channel = bc == capi.BC_CHANNEL
+    g = po.Grid(n, n, n, n, channel=channel)
+    rng = np.random.default_rng(34)
+    u, v, w = 0.1 * rng.standard_normal(g.ncell), 0.1 * rng.standard_normal(g.nv), 0.1 * rng.standard_normal(g.ncell)
+    f = [rng.standard_normal(g.ncell), rng.standard_normal(g.nv), rng.standard_normal(g.ncell)]
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("AFMIB_UPDATE_DF_GENERIC", mode)
+        with capi.Solver(n, bc=bc, precision=capi.MIXED, mu=0.01, rho=1.0, dt=1e-3, tol=1e-11) as sv:
+            sv.set_velocity(u, v, w)
+            sv.project()
+            for _ in range(4):
+                sv.ns_step(*f)
+            out[mode] = (sv.get_velocity(), sv.stats()["outer_iters"])
+    for a, b in zip(out["0"][0], out["1"][0]):
+        assert np.array_equal(a, b)
+    assert out["0"][1] == out["1"][1]
 
 
 @pytest.mark.parametrize("m", [1200, 5000, 20000])
