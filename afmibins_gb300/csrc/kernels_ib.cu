@@ -16,6 +16,9 @@
 // and with t = frac(s - off), S = sin(pi t / 2), C = cos(pi t / 2):
 //   phi/n = (1 - S)/4, (1 + C)/4, (1 + S)/4, (1 - C)/4      (sum = 1)
 // (cos(pi r/2) at r = -1-t, -t, 1-t, 2-t). One sincospi per axis and offset.
+#include <type_traits>
+
+#include "dfloat.cuh"
 #include "kernels_ib.h"
 
 namespace afmib {
@@ -295,6 +298,28 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_cell_table(const unsigned* __r
     }
 }
 
+// Compute types of the gather: T itself (FP64, FP32) or, for FP64 inputs in
+// the mixed form, dfl: the weight products and the face sums carried as
+// double-float pairs (relative 2^-44) on the FP32 pipe, GB300's FP64 pipe
+// being 1/64 of it. Inputs are split exactly by integer operations
+// (df_split), the sum goes back to FP64 with one addition per face.
+struct dfl {
+    df2 v;
+};
+__device__ __forceinline__ dfl operator*(dfl a, dfl b) { return dfl{df_mul(a.v, b.v)}; }
+__device__ __forceinline__ dfl& operator+=(dfl& a, dfl b) {
+    a.v = df_add(a.v, b.v);
+    return a;
+}
+template <typename TC>
+__device__ __forceinline__ TC tc_from(double v) { return TC(v); }
+template <>
+__device__ __forceinline__ dfl tc_from<dfl>(double v) { return dfl{df_split(v)}; }
+template <typename T, typename TC>
+__device__ __forceinline__ T tc_to(TC v) { return T(v); }
+template <>
+__device__ __forceinline__ double tc_to<double, dfl>(dfl v) { return f32_to_f64(v.v.hi) + f32_to_f64(v.v.lo); }
+
 // ---------------------------------------------------------------------------
 // Gather spreading. One block (TS^3 threads, one face per component each) per
 // active output tile. The markers binned in E = the tile grown by two cells
@@ -311,7 +336,7 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_cell_table(const unsigned* __r
 // order into chunks leaves every face's summation order, and its result bits,
 // unchanged: there is no marker-density limit.
 // ---------------------------------------------------------------------------
-template <typename T, int TS, int TZ>
+template <typename T, int TS, int TZ, typename TC = T>
 __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, const int* __restrict__ perm,
                                                                 MarkerW<T> mw, const T* __restrict__ G,
                                                                 const double* __restrict__ vol, double scale,
@@ -332,7 +357,7 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
     int* s_k = s_scan + NT;              // cap: marker index of each staged slot
     int* s_base = s_k + cap;             // cap: packed E-local first faces
     // cap * 12: x weights, y weights, z weights times the marker's force
-    T* s_w = (T*)(((uintptr_t)(s_base + cap) + 15) & ~(uintptr_t)15);
+    TC* s_w = (TC*)(((uintptr_t)(s_base + cap) + 15) & ~(uintptr_t)15);
 
     const int ntx = d.nx / TS, nty = d.ny / TS;
     const int ncount = *count;
@@ -444,7 +469,7 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
         // ---- one component at a time (and, past the capacity, one chunk at a time)
         const int J[3] = {lx + 2, ly + 2, lz + HZ};
         for (int comp = 0; comp < 3; ++comp) {
-            T acc = T(0);
+            TC acc = tc_from<TC>(0.0);
             const unsigned jp = 0x00808080u | (unsigned)(J[0] + 8) | ((unsigned)(J[1] + 8) << 8) |
                                 ((unsigned)(J[2] + 8) << 16);
             const int hx = (comp == 0) ? J[0] + 1 : J[0] + 2;
@@ -459,7 +484,7 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
                 }
                 for (int sl = tid; sl < nc; sl += NT) {
                     const int k = s_k[sl];
-                    const T g = T((double)G[(size_t)comp * M + k] * (vol ? vol[k] : 1.0) * scale);
+                    const TC g = tc_from<TC>((double)G[(size_t)comp * M + k] * (vol ? vol[k] : 1.0) * scale);
                     int packed = 0;
 #pragma unroll
                     for (int a = 0; a < 3; ++a) {
@@ -473,7 +498,8 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
                         packed |= (b + 8) << (8 * a);
                         const T* w = mw.w + (((size_t)k * 3 + a) * 2 + v) * 4;
 #pragma unroll
-                        for (int m = 0; m < 4; ++m) s_w[(size_t)sl * 12 + a * 4 + m] = a == 2 ? w[m] * g : w[m];
+                        for (int m = 0; m < 4; ++m)
+                            s_w[(size_t)sl * 12 + a * 4 + m] = a == 2 ? tc_from<TC>(w[m]) * g : tc_from<TC>(w[m]);
                     }
                     s_base[sl] = packed;
                 }
@@ -490,7 +516,7 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
                             // support iff every byte is 0x80 + {0..3}
                             const unsigned t = jp - (unsigned)s_base[sl];
                             if ((t & 0x00FCFCFCu) == 0x00808080u) {
-                                const T* w = s_w + (size_t)sl * 12;
+                                const TC* w = s_w + (size_t)sl * 12;
                                 acc += (w[t & 3u] * w[4 + ((t >> 8) & 3u)]) * w[8 + ((t >> 16) & 3u)];
                             }
                         }
@@ -498,7 +524,7 @@ __global__ void __launch_bounds__(TS * TS * TZ) k_spread_gather(Dims d, int M, c
             }
             T* f = comp == 0 ? fu : (comp == 1 ? fv : fw);
             const int gx = tx * TS + lx, gy = ty * TS + ly, gz = tz * TZ + lz;
-            if (!(d.channel && comp == 1 && gy == 0)) f[lin(d, gx, gy, gz)] = acc;
+            if (!(d.channel && comp == 1 && gy == 0)) f[lin(d, gx, gy, gz)] = tc_to<T, TC>(acc);
             __syncthreads();
         }
     }
@@ -625,37 +651,45 @@ size_t spread_smem_bytes(int TS, int TZ, int cap) {
     return bytes;
 }
 
-template <typename T, int TS, int TZ>
+template <typename T, int TS, int TZ, typename TC>
 static void spread_launch(const Dims& d, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
                           double scale, const int* slot, const int* ctab, const int* list, const int* count,
                           int max_tiles, int cap, T* fu, T* fv, T* fw, int* ovf_list, int* ovf_count,
                           int* next_tile, cudaStream_t s) {
+    static_assert(sizeof(TC) == sizeof(T), "the staged weights take the input type's size");
     const size_t smem = spread_smem_bytes<T>(TS, TZ, cap);
     // opt in to exactly the dynamic shared memory this launch uses (the
     // kernel's static shared memory counts against the same 227 KB)
     static size_t configured = 0;  // the largest capacity asked for so far
     if (configured < smem) {
-        if (cudaFuncSetAttribute(k_spread_gather<T, TS, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
+        if (cudaFuncSetAttribute(k_spread_gather<T, TS, TZ, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
             return;  // the launch error is reported by the caller's cudaGetLastError
         configured = smem;
     }
     int blocks = max_tiles < 152 * 4 ? max_tiles : 152 * 4;
     if (blocks < 1) blocks = 1;
-    k_spread_gather<T, TS, TZ><<<blocks, TS * TS * TZ, smem, s>>>(d, M, perm, mw, G, vol, scale, slot, ctab, list,
-                                                                  count, cap, fu, fv, fw, ovf_list, ovf_count,
-                                                                  next_tile);
+    k_spread_gather<T, TS, TZ, TC><<<blocks, TS * TS * TZ, smem, s>>>(d, M, perm, mw, G, vol, scale, slot, ctab,
+                                                                      list, count, cap, fu, fv, fw, ovf_list,
+                                                                      ovf_count, next_tile);
 }
 
 template <typename T>
 void launch_spread_gather(const Dims& d, int TS, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
                           double scale, const int* slot, const int* ctab, const int* list, const int* count,
                           int max_tiles, int cap, T* fu, T* fv, T* fw, int* ovf_list, int* ovf_count,
-                          int* next_tile, cudaStream_t s) {
+                          int* next_tile, cudaStream_t s, bool dfloat) {
     const bool flat = d.nz == 1;
-#define AFMIB_SPREAD(TSV, TZV)                                                                                    \
-    spread_launch<T, TSV, TZV>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, \
-                               ovf_list, ovf_count, next_tile, s)
+#define AFMIB_SPREAD(TSV, TZV)                                                                                     \
+    do {                                                                                                           \
+        if (dfloat && sizeof(T) == sizeof(double))                                                                 \
+            spread_launch<T, TSV, TZV, std::conditional_t<sizeof(T) == sizeof(double), dfl, T>>(                   \
+                d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, fu, fv, fw, ovf_list,      \
+                ovf_count, next_tile, s);                                                                          \
+        else                                                                                                       \
+            spread_launch<T, TSV, TZV, T>(d, M, perm, mw, G, vol, scale, slot, ctab, list, count, max_tiles, cap, \
+                                          fu, fv, fw, ovf_list, ovf_count, next_tile, s);                         \
+    } while (0)
     if (TS == 8 && !flat) AFMIB_SPREAD(8, 8);
     else if (TS == 4 && !flat) AFMIB_SPREAD(4, 4);
     else if (TS == 8) AFMIB_SPREAD(8, 1);
@@ -682,7 +716,7 @@ void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, do
     template size_t spread_smem_bytes<T>(int, int, int);                                                             \
     template void launch_spread_gather<T>(const Dims&, int, int, const int*, MarkerW<T>, const T*, const double*, \
                                           double, const int*, const int*, const int*, const int*, int, int, T*,  \
-                                          T*, T*, int*, int*, int*, cudaStream_t);                              \
+                                          T*, T*, int*, int*, int*, cudaStream_t, bool);                        \
     template void launch_interp<T, double>(const Dims&, int, const int*, MarkerW<T>, const double*, const double*, \
                                            const double*, double*, cudaStream_t);                               \
     template void launch_interp<T, float>(const Dims&, int, const int*, MarkerW<T>, const float*, const float*,  \

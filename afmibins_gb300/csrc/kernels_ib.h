@@ -54,12 +54,13 @@ size_t spread_smem_bytes(int TS, int TZ, int cap);
 // holds more than `cap` markers is appended to ovf_list (and left untouched)
 // when ovf_list is given, else spread in chunks of `cap` markers (same
 // result bits as one pass). Blocks take tiles from *next_tile, which must be
-// zero at launch.
+// zero at launch. dfloat (FP64 inputs): weight products and face sums in
+// double-float on the FP32 pipe (relative 2^-44) instead of FP64.
 template <typename T>
 void launch_spread_gather(const Dims& d, int TS, int M, const int* perm, MarkerW<T> mw, const T* G, const double* vol,
                           double scale, const int* slot, const int* ctab, const int* list, const int* count,
                           int max_tiles, int cap, T* fu, T* fv, T* fw, int* ovf_list, int* ovf_count,
-                          int* next_tile, cudaStream_t s);
+                          int* next_tile, cudaStream_t s, bool dfloat = false);
 
 // U[c*M + k] = sum (phi/n)^3 u_c(face); perm (may be null) orders the threads.
 // T: weight and arithmetic type, TF: field storage type

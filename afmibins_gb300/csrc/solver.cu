@@ -80,6 +80,10 @@ struct afmib_solver {
     // x += e (AFMIB_LAP_DF=0: an FP64 defect per block)
     bool lap_df = true;
     float* plo = nullptr;
+    // mixed form: the FP64 spreading of the IB step computes its weight
+    // products and face sums in double-float (relative 2^-44; the FP64 form
+    // and the single-operator entry point stay FP64; AFMIB_SPREAD_DF=0: FP64)
+    bool spread_df = true;
     double *divb = nullptr, *walls = nullptr, *wallgrad = nullptr;
     double *cg_r = nullptr, *cg_p = nullptr, *cg_q = nullptr;
     double *tmp[3] = {};
@@ -1271,12 +1275,12 @@ int bin_markers(afmib_solver* s, const double* P, bool fp32 = false) {
 // computed once, by one of the passes, with the same arithmetic.
 template <typename T>
 int spread_two_pass(afmib_solver* s, MarkerW<T> mw, const T* G, const double* vol, double scale, T* fu, T* fv, T* fw,
-                    int cap_small, int cap_large) {
+                    int cap_small, int cap_large, bool dfloat = false) {
     CK(cudaMemsetAsync(s->tcount + 2, 0, 3 * sizeof(int), s->st));  // overflow count and the two tile counters
     launch_spread_gather<T>(s->d, s->TS, s->M, s->perm, mw, G, vol, scale, s->tslot, s->ctab, s->tlist, s->tcount,
-                            s->ntiles, cap_small, fu, fv, fw, s->tovf, s->tcount + 2, s->tcount + 3, s->st);
+                            s->ntiles, cap_small, fu, fv, fw, s->tovf, s->tcount + 2, s->tcount + 3, s->st, dfloat);
     launch_spread_gather<T>(s->d, s->TS, s->M, s->perm, mw, G, vol, scale, s->tslot, s->ctab, s->tovf, s->tcount + 2,
-                            s->ntiles, cap_large, fu, fv, fw, nullptr, nullptr, s->tcount + 4, s->st);
+                            s->ntiles, cap_large, fu, fv, fw, nullptr, nullptr, s->tcount + 4, s->st, dfloat);
     return AFMIB_OK;
 }
 
@@ -1305,7 +1309,7 @@ double spread_scale(const Dims& d) {
 // f = spread(G) with the bins and weights of the last bin_markers call.
 // Algorithmic bytes: M (24 + 3s + 8 + 8) + 3 N_touched s with N_touched
 // taken as the faces of the active tiles (from the previous spreading).
-int spread_forces(afmib_solver* s, const double* vol, double* fu, double* fv, double* fw) {
+int spread_forces(afmib_solver* s, const double* vol, double* fu, double* fv, double* fw, bool dfloat = false) {
     const long long N = s->N();
     CK(cudaMemsetAsync(fu, 0, N * sizeof(double), s->st));
     CK(cudaMemsetAsync(fv, 0, N * sizeof(double), s->st));
@@ -1315,7 +1319,7 @@ int spread_forces(afmib_solver* s, const double* vol, double* fu, double* fv, do
     const double touched = (double)s->stats.spread_tiles * s->tile_cells();
     {
         ProfScope ps(s, P_SPREAD, (double)s->M * (24 + 3 * 8 + 8 + 8) + 3 * touched * 8);
-        TRY(spread_two_pass<double>(s, s->mw, s->G, vol, n3, fu, fv, fw, 896, cap));
+        TRY(spread_two_pass<double>(s, s->mw, s->G, vol, n3, fu, fv, fw, 896, cap, dfloat));
     }
     CKL();
     return AFMIB_OK;
@@ -1383,7 +1387,10 @@ int ib_one_step(afmib_solver* s) {
         }
         return AFMIB_OK;
     };
-    auto spread = [&]() { return sp32 ? spread_forces32(s, vol) : spread_forces(s, vol, s->f[0], s->f[1], s->f[2]); };
+    auto spread = [&]() {
+        return sp32 ? spread_forces32(s, vol)
+                    : spread_forces(s, vol, s->f[0], s->f[1], s->f[2], s->mixed && s->spread_df);
+    };
     auto interp = [&](double* U) {
         return in32 ? interp_markers(s, s->u, s->v, s->w, U, true) : interp_markers(s, s->u, s->v, s->w, U, false);
     };
@@ -1799,6 +1806,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_HELM_OVERLAP")) s->helm_overlap = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_HELM_DF")) s->helm_df = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_LAP_DF")) s->lap_df = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_SPREAD_DF")) s->spread_df = std::string(e) != "0";
     if (s->mixed && s->fused_rhs)
         for (auto& q : s->qo) TRY(dalloc(s, &q, N));
     TRY(dalloc(s, &s->phi_prev[0], N));

@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--profile-steps", type=int, default=2)
     ap.add_argument("--inner-tol", type=float, default=0.0,
                     help="mixed form: relative reduction of each FP32 inner Helmholtz solve (0: the library default)")
+    ap.add_argument("--ib-fp32", type=int, default=0,
+                    help="mixed form: bit 0 FP32 spreading, bit 1 FP32 interpolation (0: both FP64, the default)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", choices=["ib", "mg", "adjoint", "large"], default="ib",
@@ -267,7 +269,8 @@ def run_form(capi, torch, args, prec, state, dev, stream, proj_start=0):
     with timing = {"wall_s", "host_ms_per_step"}."""
     X, nstart, nidx, u, v, w = state
     sv = capi.Solver(args.n, mu=args.mu, rho=1.0, dt=args.dt, tol=args.tol, k_spring=0.5, precision=prec,
-                     proj_start=proj_start, inner_tol=args.inner_tol, stream=stream.cuda_stream)
+                     proj_start=proj_start, inner_tol=args.inner_tol,
+                     ib_fp32=args.ib_fp32 if prec == capi.MIXED else 0, stream=stream.cuda_stream)
     ud, vd, wd = (torch.from_numpy(a).to(dev) for a in (u, v, w))
     Xd = torch.from_numpy(X).to(dev)
     torch.cuda.synchronize()

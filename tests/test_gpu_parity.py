@@ -607,7 +607,9 @@ def test_double_float_outer_residual(monkeypatch, n, bc, markers):
     The FP64 state x takes the same += e, the stopping tests the same norms,
     so the sub-steps agree with the FP64-defect solves to the solver
     tolerance (1e-10 relative, as the inner-solver variants) and with the
-    FP64 form to the mixed form's 1e-8 bar."""
+    FP64 form to the mixed form's 1e-8 bar. The IB cases also spread their
+    forces with double-float products and sums (2^-44) against FP64
+    spreading (AFMIB_SPREAD_DF)."""
     channel = bc == capi.BC_CHANNEL
     g = po.Grid(n, n, n, n, channel=channel)
     rng = np.random.default_rng(32)
@@ -618,6 +620,7 @@ def test_double_float_outer_residual(monkeypatch, n, bc, markers):
     for key, prec, df in (("fp64", capi.FP64, "1"), ("defects", capi.MIXED, "0"), ("df", capi.MIXED, "1")):
         monkeypatch.setenv("AFMIB_HELM_DF", df)
         monkeypatch.setenv("AFMIB_LAP_DF", df)
+        monkeypatch.setenv("AFMIB_SPREAD_DF", df)
         with capi.Solver(n, bc=bc, precision=prec, mu=0.01, rho=1.0, dt=1e-3, tol=1e-11, k_spring=0.5) as sv:
             sv.set_velocity(u, v, w)
             sv.project()
