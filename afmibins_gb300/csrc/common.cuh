@@ -213,6 +213,12 @@ __device__ __forceinline__ void tile_walk(const Dims& d, F&& body) {
     }
 }
 
+// Resident blocks per SM the double-float residual updates are compiled for
+// (registers capped at 40, a few bytes spilled): more loads in flight; at
+// 256^3 50.2 IB steps/s against 48.5 uncapped (66 registers) and 48.6 for 8
+// blocks (32 registers, heavy spills).
+constexpr int kUpdateMinBlocks = 6;
+
 // Per-thread partial sums stay in the arithmetic type (one FP64 conversion
 // per thread, not per element: on GB300 conversions run on the FP64 pipe).
 template <typename T>

@@ -810,8 +810,8 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_update_df(Dims d, int comp, 
 // registers, 32-bit shift-composed indices, every load of the batch issued
 // before the rows are evaluated), blocks walk z batches in steps of grid.z;
 // the same arithmetic per cell, so the same bits.
-template <int ZU>
-__global__ void __launch_bounds__(kRedBlock) k_helm_update_df2(Dims d, int comp, df2 off, df2 cxa,
+template <int ZU, int MINB>
+__global__ void __launch_bounds__(kRedBlock, MINB) k_helm_update_df2(Dims d, int comp, df2 off, df2 cxa,
                                                               double* __restrict__ x, const float* __restrict__ e,
                                                               float* __restrict__ rh, float* __restrict__ rl,
                                                               RedScratch sc, double* out) {
@@ -881,13 +881,14 @@ void launch_helm_update_df(const Dims& d, int comp, double scale, double* x, con
     const df2 o = df_split(off), c = df_split(off + off / 3.0);
     // two z cells per thread: 46.4 IB steps/s at 256^3 against 46.3 for four
     // and 45.5 for eight (more registers, fewer warps) and 45.5 for the
-    // general kernel
+    // general kernel; registers capped for kUpdateMinBlocks resident blocks
     constexpr int ZU = 2;
     if (d.nz > 1 && d.nz % ZU == 0 && ix2_ok(d) && !update_df_generic()) {
         const int gx = (d.nx + kRBX - 1) / kRBX, gy = (d.ny + kRBY - 1) / kRBY;
         int gz = d.nz / ZU;
         if ((long long)gx * gy * gz > kMaxRedBlocks) gz = std::max(1, kMaxRedBlocks / (gx * gy));
-        k_helm_update_df2<ZU><<<dim3(gx, gy, gz), dim3(kRBX, kRBY), 0, s>>>(d, comp, o, c, x, e, rh, rl, sc, out);
+        k_helm_update_df2<ZU, kUpdateMinBlocks><<<dim3(gx, gy, gz), dim3(kRBX, kRBY), 0, s>>>(d, comp, o, c, x, e, rh,
+                                                                                             rl, sc, out);
         return;
     }
     k_helm_update_df<<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, o, c, x, e, rh, rl, sc, out);

@@ -159,8 +159,8 @@ __global__ void __launch_bounds__(kRedBlock) k_lap_update_df(Dims d, double* __r
 // The same on power-of-two 3D grids, two z cells per thread with every load
 // of the pair issued first (as k_helm_update_df2); the same rows, so the
 // same bits.
-template <int ZU>
-__global__ void __launch_bounds__(kRedBlock) k_lap_update_df2(Dims d, double* __restrict__ x,
+template <int ZU, int MINB>
+__global__ void __launch_bounds__(kRedBlock, MINB) k_lap_update_df2(Dims d, double* __restrict__ x,
                                                              const float* __restrict__ e, float* __restrict__ rh,
                                                              float* __restrict__ rl, RedScratch sc, double* out) {
     const Ix2 I(d);
@@ -1194,7 +1194,7 @@ void launch_lap_update_df(const Dims& d, double* x, const float* e, float* rh, f
         const int gx = (d.nx + kRBX - 1) / kRBX, gy = (d.ny + kRBY - 1) / kRBY;
         int gz = d.nz / ZU;
         if ((long long)gx * gy * gz > kMaxRedBlocks) gz = std::max(1, kMaxRedBlocks / (gx * gy));
-        k_lap_update_df2<ZU><<<dim3(gx, gy, gz), dim3(kRBX, kRBY), 0, s>>>(d, x, e, rh, rl, sc, out);
+        k_lap_update_df2<ZU, kUpdateMinBlocks><<<dim3(gx, gy, gz), dim3(kRBX, kRBY), 0, s>>>(d, x, e, rh, rl, sc, out);
         return;
     }
     k_lap_update_df<<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, x, e, rh, rl, sc, out);
