@@ -945,8 +945,8 @@ __global__ void k_helm_jacobi2(Dims d, int comp, T s, const T* __restrict__ xv, 
 // the 7-point operator under red-black ordering the sweep contracts the
 // error as the square of the Jacobi rate.
 template <typename T, int ZU>
-__global__ void k_helm_rbgs2(Dims d, int comp, T s, int color, int init, T* __restrict__ xv, const T* __restrict__ b,
-                             int rev) {
+__device__ __forceinline__ void helm_rbgs2_body(Dims d, int comp, T s, int color, int init, T* __restrict__ xv,
+                                                const T* __restrict__ b, int rev) {
     const Ix2 I(d);
     const uint3 B = block_at(rev);
     const int y = B.y * BY + threadIdx.y, t = B.x * BX + threadIdx.x, z0 = B.z * ZU;
@@ -968,13 +968,20 @@ __global__ void k_helm_rbgs2(Dims d, int comp, T s, int color, int init, T* __re
         if (init) xv[I.at(2 * t + ((y + z0 + u + color + 1) & 1), y, z0 + u)] = T(0);
     }
 }
+template <typename T, int ZU, int MINB>
+__global__ void __launch_bounds__(BX * BY, MINB) k_helm_rbgs2b(Dims d, int comp, T s, int color, int init,
+                                                              T* __restrict__ xv, const T* __restrict__ b, int rev) {
+    helm_rbgs2_body<T, ZU>(d, comp, s, color, init, xv, b, rev);
+}
 
 template <typename T>
 bool launch_helm_rbgs(const Dims& d, int comp, double scale, int color, int init, T* x, const T* b, cudaStream_t s,
                       int rev) {
     if (!(d.nz % 8 == 0 && d.nx % 2 == 0 && ix2_ok(d))) return false;
-    k_helm_rbgs2<T, 8><<<dim3((d.nx / 2 + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / 8), dim3(BX, BY), 0, s>>>(
-        d, comp, T(scale), color, init, x, b, rev);
+    const dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / 8);
+    // registers capped for 6 resident blocks (40 against 48): measured with the
+    // multigrid smoother's cap, 50.5 against 50.0 IB steps/s at 256^3
+    k_helm_rbgs2b<T, 8, 6><<<g, dim3(BX, BY), 0, s>>>(d, comp, T(scale), color, init, x, b, rev);
     return true;
 }
 template bool launch_helm_rbgs<float>(const Dims&, int, double, int, int, float*, const float*, cudaStream_t, int);
