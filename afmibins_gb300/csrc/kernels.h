@@ -47,12 +47,13 @@ void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const
 // Mixed form, backward-Euler sub-step: b (as launch_helm_rhs), the first FP64
 // defect r = b - H uold as FP32 with out[0] = r.r (H = I + s_minus Delta), and
 // q = Q(uold), the off-diagonal term of the Helmholtz rows, in one pass.
-// walk_blocks > 0: the persistent form on that many blocks (tile_walk).
+// walk_blocks > 0: the persistent form on that many blocks (tile_walk);
+// uo_out: also a copy of uold there.
 template <typename TF, typename TA>
 void launch_helm_rhs_be_defect(const Dims& d, int comp, double* b, float* r, double* q, const double* uold,
                                const TF* f, const TA* adv, const double* top, const double* bottom, double s_minus,
                                double dt, double inv_rho, RedScratch sc, double* out, cudaStream_t s,
-                               int walk_blocks = 0, float* r_lo = nullptr);
+                               int walk_blocks = 0, float* r_lo = nullptr, double* uo_out = nullptr);
 // Mixed form, Crank-Nicolson sub-step: b from q = Q(uold) kept by the
 // backward-Euler sub-step (pointwise).
 template <typename TF, typename TA>

@@ -32,9 +32,13 @@ inline dim3 block3() { return dim3(BX, BY, 1); }
 // which makes every wall flux of the reference (uvt, uvb, vwt, vwb = 0; vvb,
 // vvt from the one interior face) come out of the same formulas.
 // ---------------------------------------------------------------------------
-template <typename TI, typename T>
-__global__ void k_advect(Dims d, T* __restrict__ ua, T* __restrict__ va, T* __restrict__ wa,
-                         const TI* __restrict__ ui, const TI* __restrict__ vi, const TI* __restrict__ wi) {
+// P2: power-of-two grids, 32-bit shift-composed indices and wraps by masks,
+// registers capped for 6 resident blocks (the same arithmetic, so the same
+// bits as the general form)
+template <typename TI, typename T, bool P2>
+__global__ void __launch_bounds__(BX * BY, P2 ? 6 : 4) k_advect(Dims d, T* __restrict__ ua, T* __restrict__ va,
+                                                                 T* __restrict__ wa, const TI* __restrict__ ui,
+                                                                 const TI* __restrict__ vi, const TI* __restrict__ wi) {
     AFMIB_XYZ
     // loads in the storage type TI, arithmetic in T (FP32 for the mixed form)
     struct Ld {
@@ -42,7 +46,12 @@ __global__ void k_advect(Dims d, T* __restrict__ ua, T* __restrict__ va, T* __re
         __device__ T operator[](long long k) const { return T(p[k]); }
     } u{ui}, v{vi}, w{wi};
     const T h = T(0.5), n = T(d.n);
-    const int xm = xm1(d, x), xp = xp1(d, x), ym = ym1(d, y), yp = yp1(d, y), zm = zm1(d, z), zp = zp1(d, z);
+    const Ix2 I(d);
+    auto lin = [&](const Dims& dd, int xx, int yy, int zz) -> long long {
+        return P2 ? (long long)I.at(xx, yy, zz) : afmib::lin(dd, xx, yy, zz);
+    };
+    const int xm = P2 ? I.xm(x) : xm1(d, x), xp = P2 ? I.xp(x) : xp1(d, x), ym = P2 ? I.ym(y) : ym1(d, y),
+              yp = P2 ? I.yp(y) : yp1(d, y), zm = P2 ? I.zm(z) : zm1(d, z), zp = P2 ? I.zp(z) : zp1(d, z);
     const long long i = lin(d, x, y, z);
     const long long ixm = lin(d, xm, y, z), ixp = lin(d, xp, y, z), iym = lin(d, x, ym, z), iyp = lin(d, x, yp, z),
                     izm = lin(d, x, y, zm), izp = lin(d, x, y, zp);
@@ -293,7 +302,7 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_rhs_be_defect(Dims d, int co
                                                                  const TA* __restrict__ adv, const double* __restrict__ top,
                                                                  const double* __restrict__ bottom, double s_minus,
                                                                  double hdt, double inv_rho, RedScratch sc, double* out,
-                                                                 float* __restrict__ r_lo) {
+                                                                 float* __restrict__ r_lo, double* __restrict__ uo_out) {
     float acc = 0.f;
     auto body = [&](int xi, int yi, int zi) {
         const long long i = lin(d, xi, yi, zi);
@@ -312,6 +321,7 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_rhs_be_defect(Dims d, int co
         helm_point_q(d, comp, s_minus, uold, xi, yi, zi, hx, q);
         b_out[i] = b;
         q_out[i] = q;
+        if (uo_out) uo_out[i] = uold[i];  // the step's start velocity, kept for the CN sub-step
         const double rd = b - hx;
         const float ri = float(rd);
         r_out[i] = ri;
@@ -685,7 +695,8 @@ inline int ew_blocks(long long n) {
 
 template <typename TI, typename T>
 void launch_advect(const Dims& d, T* ua, T* va, T* wa, const TI* u, const TI* v, const TI* w, cudaStream_t s) {
-    k_advect<TI, T><<<grid3(d), block3(), 0, s>>>(d, ua, va, wa, u, v, w);
+    if (ix2_ok(d)) k_advect<TI, T, true><<<grid3(d), block3(), 0, s>>>(d, ua, va, wa, u, v, w);
+    else k_advect<TI, T, false><<<grid3(d), block3(), 0, s>>>(d, ua, va, wa, u, v, w);
 }
 template <typename T>
 void launch_div(const Dims& d, T* out, const T* u, const T* v, const T* w, const T* top, const T* bottom, cudaStream_t s) {
@@ -713,13 +724,13 @@ template <typename TF, typename TA>
 void launch_helm_rhs_be_defect(const Dims& d, int comp, double* b, float* r, double* q, const double* uold,
                                const TF* f, const TA* adv, const double* top, const double* bottom, double s_minus,
                                double dt, double inv_rho, RedScratch sc, double* out, cudaStream_t s, int walk_blocks,
-                               float* r_lo) {
+                               float* r_lo, double* uo_out) {
     if (walk_blocks > 0)
         k_helm_rhs_be_defect<TF, TA, true><<<walk_grid(d, walk_blocks), dim3(kRBX, kRBY), 0, s>>>(
-            d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out, r_lo);
+            d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out, r_lo, uo_out);
     else
         k_helm_rhs_be_defect<TF, TA, false><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(
-            d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out, r_lo);
+            d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out, r_lo, uo_out);
 }
 template <typename TF, typename TA>
 void launch_helm_rhs_cn_q(const Dims& d, int comp, double* r, const double* uold, const double* q, const TF* f,
@@ -731,10 +742,11 @@ void launch_helm_rhs_cn_q(const Dims& d, int comp, double* r, const double* uold
 template void launch_helm_rhs_be_defect<double, float>(const Dims&, int, double*, float*, double*, const double*,
                                                        const double*, const float*, const double*, const double*,
                                                        double, double, double, RedScratch, double*, cudaStream_t, int,
-                                                       float*);
+                                                       float*, double*);
 template void launch_helm_rhs_be_defect<float, float>(const Dims&, int, double*, float*, double*, const double*,
                                                       const float*, const float*, const double*, const double*, double,
-                                                      double, double, RedScratch, double*, cudaStream_t, int, float*);
+                                                      double, double, RedScratch, double*, cudaStream_t, int, float*,
+                                                      double*);
 template void launch_helm_rhs_cn_q<double, float>(const Dims&, int, double*, const double*, const double*,
                                                   const double*, const float*, const double*, const double*, double,
                                                   double, double, double, cudaStream_t);

@@ -1042,7 +1042,9 @@ int substep(afmib_solver* s) {
     }
     CKL();
     const bool be = !s->half;
-    if (be) {
+    // the fused mixed-form path copies u into uo inside its first pass
+    const bool fused = s->mixed && s->fused_rhs && s->qo[0] && !s->bfp_defects;
+    if (be && !fused) {
         CK(cudaMemcpyAsync(s->uo[0], s->u, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
         CK(cudaMemcpyAsync(s->uo[1], s->v, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
         CK(cudaMemcpyAsync(s->uo[2], s->w, N * sizeof(double), cudaMemcpyDeviceToDevice, s->st));
@@ -1058,10 +1060,10 @@ int substep(afmib_solver* s) {
     const double* wb = s->walls + 3 * nxz;
     const double inv_rho = 1 / s->cfg.rho;
     double* vel[3] = {s->u, s->v, s->w};
-    if (s->mixed && s->fused_rhs && s->qo[0] && !s->bfp_defects) {
-        // backward Euler: right-hand side, first defect (x starts at uold)
-        // and Q(uold) in one pass per component; Crank-Nicolson: right-hand
-        // sides from Q(uold), then the solves
+    if (fused) {
+        // backward Euler: right-hand side, first defect (x starts at uold),
+        // Q(uold) and the copy of uold in one pass per component;
+        // Crank-Nicolson: right-hand sides from Q(uold), then the solves
         const bool ovl = helm_overlap_ok(s, s->s_minus());
         auto walls_of = [&](int c, const double** top, const double** bot) {
             *top = (!d.channel || c == 1) ? nullptr : (c == 0 ? ut : wt);
@@ -1072,13 +1074,13 @@ int substep(afmib_solver* s) {
             walls_of(c, &top, &bot);
             ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 4 + 8 + 8 + 4), 1, q);
             if (s->spread64)
-                launch_helm_rhs_be_defect<double, float>(d, c, s->rhs[c], r, s->qo[c], s->uo[c], s->f[c], s->adv32[c],
+                launch_helm_rhs_be_defect<double, float>(d, c, s->rhs[c], r, s->qo[c], vel[c], s->f[c], s->adv32[c],
                                                          top, bot, s->s_minus(), s->cfg.dt, inv_rho, s->red, out, q,
-                                                         wblocks, lo);
+                                                         wblocks, lo, s->uo[c]);
             else
-                launch_helm_rhs_be_defect<float, float>(d, c, s->rhs[c], r, s->qo[c], s->uo[c], s->f32[c],
+                launch_helm_rhs_be_defect<float, float>(d, c, s->rhs[c], r, s->qo[c], vel[c], s->f32[c],
                                                         s->adv32[c], top, bot, s->s_minus(), s->cfg.dt, inv_rho,
-                                                        s->red, out, q, wblocks, lo);
+                                                        s->red, out, q, wblocks, lo, s->uo[c]);
         };
         if (be) {
             if (ovl) {
