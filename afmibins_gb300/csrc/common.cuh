@@ -213,6 +213,13 @@ __device__ __forceinline__ void tile_walk(const Dims& d, F&& body) {
     }
 }
 
+// First FP64 defects of the mixed form: the double-float pair by integer
+// operations (AFMIB_LO_SPLIT=0: hardware rounding and an FP64 difference)
+inline bool lo_split() {
+    const char* e = std::getenv("AFMIB_LO_SPLIT");
+    return !(e && e[0] == '0');
+}
+
 // Resident blocks per SM the double-float residual updates are compiled for
 // (registers capped at 40, a few bytes spilled): more loads in flight; at
 // 256^3 50.2 IB steps/s against 48.5 uncapped (66 registers) and 48.6 for 8

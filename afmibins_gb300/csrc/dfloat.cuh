@@ -130,6 +130,22 @@ AFMIB_HD df2 df_mul(df2 a, df2 b) {
 
 AFMIB_HD float df_to_float(df2 a) { return a.hi + a.lo; }
 
+// An FP64 residual as the FP32 defect of the inner solves and, when rest is
+// given, the rest of its double-float pair. split: by integer operations
+// (df_split: the top 24 bits truncated, the next 23 bits), no FP64-pipe
+// instruction; else the hardware rounding and the rounded exact difference.
+AFMIB_HD float defect_words(double rd, float* rest, bool split) {
+    if (!rest) return (float)rd;
+    if (split) {
+        const df2 p = df_split(rd);
+        *rest = p.lo;
+        return p.hi;
+    }
+    const float h = (float)rd;
+    *rest = (float)(rd - f32_to_f64(h));
+    return h;
+}
+
 // a + b as an exact pair (Knuth's two-sum)
 AFMIB_HD df2 two_sum_f(float a, float b) {
     df2 r;

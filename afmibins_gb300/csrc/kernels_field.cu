@@ -302,7 +302,8 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_rhs_be_defect(Dims d, int co
                                                                  const TA* __restrict__ adv, const double* __restrict__ top,
                                                                  const double* __restrict__ bottom, double s_minus,
                                                                  double hdt, double inv_rho, RedScratch sc, double* out,
-                                                                 float* __restrict__ r_lo, double* __restrict__ uo_out) {
+                                                                 float* __restrict__ r_lo, double* __restrict__ uo_out,
+                                                                 bool lo_split) {
     float acc = 0.f;
     auto body = [&](int xi, int yi, int zi) {
         const long long i = lin(d, xi, yi, zi);
@@ -322,10 +323,10 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_rhs_be_defect(Dims d, int co
         b_out[i] = b;
         q_out[i] = q;
         if (uo_out) uo_out[i] = uold[i];  // the step's start velocity, kept for the CN sub-step
-        const double rd = b - hx;
-        const float ri = float(rd);
+        float lo;
+        const float ri = defect_words(b - hx, r_lo ? &lo : nullptr, lo_split);
         r_out[i] = ri;
-        if (r_lo) r_lo[i] = float(rd - cvt<double, float>(ri));  // exact difference, rounded
+        if (r_lo) r_lo[i] = lo;
         acc += ri * ri;
     };
     if (WALK) {
@@ -462,14 +463,15 @@ __global__ void k_cg_direction(long long N, T* __restrict__ p, const T* __restri
 template <typename TD, bool WALK>
 __global__ void __launch_bounds__(kRedBlock) k_helm_defect(Dims d, int comp, double s, const double* __restrict__ x,
                                                           const double* __restrict__ b, TD* __restrict__ r,
-                                                          RedScratch sc, double* out, float* __restrict__ r_lo) {
+                                                          RedScratch sc, double* out, float* __restrict__ r_lo,
+                                                          bool lo_split) {
     TD acc = TD(0);
     auto body = [&](int xi, int yi, int zi) {
         const long long i = lin(d, xi, yi, zi);
-        const double rd = b[i] - helm_point(d, comp, s, x, xi, yi, zi);
-        const TD ri = TD(rd);
+        float lo;
+        const TD ri = defect_words(b[i] - helm_point(d, comp, s, x, xi, yi, zi), r_lo ? &lo : nullptr, lo_split);
         r[i] = ri;
-        if (r_lo) r_lo[i] = float(rd - cvt<double, TD>(ri));  // exact difference, rounded
+        if (r_lo) r_lo[i] = lo;
         acc += ri * ri;
     };
     if (WALK) {
@@ -727,10 +729,10 @@ void launch_helm_rhs_be_defect(const Dims& d, int comp, double* b, float* r, dou
                                float* r_lo, double* uo_out) {
     if (walk_blocks > 0)
         k_helm_rhs_be_defect<TF, TA, true><<<walk_grid(d, walk_blocks), dim3(kRBX, kRBY), 0, s>>>(
-            d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out, r_lo, uo_out);
+            d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out, r_lo, uo_out, lo_split());
     else
         k_helm_rhs_be_defect<TF, TA, false><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(
-            d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out, r_lo, uo_out);
+            d, comp, b, r, q, uold, f, adv, top, bottom, s_minus, dt / 2, inv_rho, sc, out, r_lo, uo_out, lo_split());
 }
 template <typename TF, typename TA>
 void launch_helm_rhs_cn_q(const Dims& d, int comp, double* r, const double* uold, const double* q, const TF* f,
@@ -759,10 +761,10 @@ void launch_helm_defect(const Dims& d, int comp, double scale, const double* x, 
                         double* out, cudaStream_t s, int walk_blocks, float* r_lo) {
     if (walk_blocks > 0)
         k_helm_defect<TD, true><<<walk_grid(d, walk_blocks), dim3(kRBX, kRBY), 0, s>>>(d, comp, scale, x, b, r, sc, out,
-                                                                                       r_lo);
+                                                                                       r_lo, lo_split());
     else
         k_helm_defect<TD, false><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, scale, x, b, r, sc,
-                                                                                            out, r_lo);
+                                                                                            out, r_lo, lo_split());
 }
 
 // Mixed form, recursive outer residual of a viscous solve: with the FP32

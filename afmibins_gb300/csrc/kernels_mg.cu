@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(kRedBlock) k_residual_norm(Dims d, T* __restri
 template <typename TD>
 __global__ void __launch_bounds__(kRedBlock) k_lap_defect(Dims d, TD* __restrict__ r, const double* __restrict__ xv,
                                                          const double* __restrict__ b, RedScratch sc, double* out,
-                                                         float* __restrict__ r_lo) {
+                                                         float* __restrict__ r_lo, bool lo_split) {
     const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
     const double off = double(d.n) * double(d.n);
     TD acc = TD(0);
@@ -100,10 +100,10 @@ __global__ void __launch_bounds__(kRedBlock) k_lap_defect(Dims d, TD* __restrict
             double S, c;
             lap_row(d, xv, xi, yi, zi, S, c);
             const long long i = lin(d, xi, yi, zi);
-            const double rd = b[i] - off * (S - c * xv[i]);
-            const TD ri = TD(rd);
+            float lo;
+            const TD ri = defect_words(b[i] - off * (S - c * xv[i]), r_lo ? &lo : nullptr, lo_split);
             r[i] = ri;
-            if (r_lo) r_lo[i] = float(rd - cvt<double, TD>(ri));  // exact difference, rounded
+            if (r_lo) r_lo[i] = lo;
             acc += ri * ri;
         }
     double a[1] = {(double)acc};
@@ -1201,7 +1201,7 @@ void launch_prolong_assign(const Dims& d, T* fine, const T* coarse, cudaStream_t
 template <typename TD>
 void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, RedScratch sc, double* out, cudaStream_t s,
                        float* r_lo) {
-    k_lap_defect<TD><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, r, x, b, sc, out, r_lo);
+    k_lap_defect<TD><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, r, x, b, sc, out, r_lo, lo_split());
 }
 void launch_lap_update_df(const Dims& d, double* x, const float* e, float* rh, float* rl, RedScratch sc, double* out,
                           cudaStream_t s) {
