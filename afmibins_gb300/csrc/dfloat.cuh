@@ -94,6 +94,21 @@ AFMIB_HD df2 df_split(double d) {
     return r;
 }
 
+// The first word of df_split alone: the float of d's top 24 significant
+// bits (truncated toward zero), by integer operations; 0 below the float
+// normal range, inf or nan beyond it. On GB300 the hardware FP64 -> FP32
+// conversion takes an FP64-pipe slot.
+AFMIB_HD float df_hi(double d) {
+    const unsigned long long u = (unsigned long long)dbits(d);
+    const unsigned hw = (unsigned)(u >> 32), lw = (unsigned)u;
+    const unsigned sign = hw & 0x80000000u;
+    const int e = (int)((hw >> 20) & 0x7ffu) - 1023;
+    const unsigned mh = ((hw & 0xfffffu) << 3) | (lw >> 29);
+    if (e < -126) return fbits(sign);
+    if (e > 127) return fbits(sign | 0x7f800000u | (mh ? 0x400000u : 0u));
+    return fbits(sign | ((unsigned)(e + 127) << 23) | mh);
+}
+
 // a + b with both pairs' rounding errors carried (accurate under cancellation)
 AFMIB_HD df2 df_add(df2 a, df2 b) {
     float s = a.hi + b.hi;

@@ -124,6 +124,8 @@ template <typename T>
 void launch_axpy(long long n, T* y, const T* x, T a, cudaStream_t s);  // y += a x
 template <typename T>
 void launch_lincomb(long long n, T* y, T a, const T* x, T b, const T* z, cudaStream_t s);  // y = a x + b z
+// FP32 shadow of an FP64 field, truncated (df_hi), as the projection writes it
+void launch_shadow(long long n, float* out, const double* in, cudaStream_t s);
 template <typename TO, typename TI>
 void launch_convert(long long n, TO* out, const TI* in, cudaStream_t s);
 

@@ -140,9 +140,17 @@ __global__ void k_grad_sub(Dims d, T* __restrict__ u, T* __restrict__ v, T* __re
         v[i] = vn;
     }
     if (u32) {  // FP32 shadow of the velocity for the mixed form's FP32 stencils
-        u32[i] = float(un);
-        v32[i] = float(vn);
-        w32[i] = float(wn);
+        // truncated by integer operations (df_hi), not rounded by the FP64
+        // pipe: 2^-23 relative, below what the FP32 stencils resolve
+        if constexpr (sizeof(T) == sizeof(double)) {
+            u32[i] = df_hi(un);
+            v32[i] = df_hi(vn);
+            w32[i] = df_hi(wn);
+        } else {
+            u32[i] = float(un);
+            v32[i] = float(vn);
+            w32[i] = float(wn);
+        }
     }
     if (d.channel && wg) {
         const long long nxz = (long long)d.nx * d.nz, ixz = x + (long long)d.nx * z;
@@ -1056,6 +1064,15 @@ void launch_lincomb(long long n, T* y, T a, const T* x, T b, const T* z, cudaStr
 template <typename TO, typename TI>
 void launch_convert(long long n, TO* out, const TI* in, cudaStream_t s) {
     k_convert<TO, TI><<<ew_blocks(n), 256, 0, s>>>(n, out, in);
+}
+
+// FP32 shadow of an FP64 velocity field, truncated as k_grad_sub writes it
+__global__ void k_shadow(long long N, float* __restrict__ o, const double* __restrict__ in) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
+        o[i] = df_hi(in[i]);
+}
+void launch_shadow(long long n, float* out, const double* in, cudaStream_t s) {
+    k_shadow<<<ew_blocks(n), 256, 0, s>>>(n, out, in);
 }
 
 #define AFMIB_INST(T)                                                                                          \

@@ -1967,9 +1967,9 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
 // FP32 copy of the velocity for the mixed form's FP32 stencils
 int refresh_shadow(afmib_solver* s) {
     if (!s->mixed) return AFMIB_OK;
-    launch_convert<float, double>(s->N(), s->u32, s->u, s->st);
-    launch_convert<float, double>(s->N(), s->v32, s->v, s->st);
-    launch_convert<float, double>(s->N(), s->w32, s->w, s->st);
+    launch_shadow(s->N(), s->u32, s->u, s->st);
+    launch_shadow(s->N(), s->v32, s->v, s->st);
+    launch_shadow(s->N(), s->w32, s->w, s->st);
     CKL();
     return AFMIB_OK;
 }

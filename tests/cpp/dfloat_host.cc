@@ -90,3 +90,7 @@ void afmib_test_lap_update_df(float rh, float rl, float e0, const float* nb, int
     *ol = r.lo;
 }
 }
+
+extern "C" {
+float afmib_test_df_hi(double d) { return afmib::df_hi(d); }
+}

@@ -33,6 +33,8 @@ def lib(tmp_path_factory):
                                           ctypes.c_int]
     L.afmib_test_lap_residual.restype = ctypes.c_float
     L.afmib_test_split.argtypes = [ctypes.c_double, fp, fp]
+    L.afmib_test_df_hi.argtypes = [ctypes.c_double]
+    L.afmib_test_df_hi.restype = ctypes.c_float
     L.afmib_test_lap_update_df.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float, fp, ctypes.c_int,
                                            ctypes.c_float, ctypes.c_float, fp, fp]
     L.afmib_test_helm_update_df.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float, fp, ctypes.c_int,
@@ -200,3 +202,19 @@ def test_lap_update_df(lib, c):
         scale = Fr(off) * (sum(abs(Fr(v)) for v in nb) + Fr(c) * abs(Fr(e0)))
         bound = scale * Fr(2) ** -44 + (abs(Fr(rh)) + abs(Fr(rl))) * Fr(2) ** -46
         assert abs(Fr(oh.value) + Fr(ol.value) - exact) <= bound, it
+
+
+def test_df_hi_truncates(lib):
+    """df_hi (the FP32 shadow of the velocity, by integer operations): the
+    float of the double's leading 24 bits, truncated toward zero, over the
+    float normal range; zero below it."""
+    rng = np.random.default_rng(8)
+    for _ in range(20000):
+        d = float(rng.standard_normal() * 10.0 ** rng.uniform(-30, 30))
+        h = lib.afmib_test_df_hi(d)
+        f = float(np.float32(d))  # nearest
+        # truncation: |h| <= |d|, same sign, and h is f or the float next to f toward zero
+        assert abs(h) <= abs(d) and (h == 0.0 or np.sign(h) == np.sign(d))
+        assert h == f or h == float(np.nextafter(np.float32(f), np.float32(0.0)))
+    assert lib.afmib_test_df_hi(1e-45) == 0.0 and lib.afmib_test_df_hi(-0.0) == 0.0
+    assert lib.afmib_test_df_hi(0.1) == float(np.float32(0.1)) or lib.afmib_test_df_hi(0.1) < 0.1

@@ -606,8 +606,8 @@ def test_double_float_outer_residual(monkeypatch, n, bc, markers):
     (2^-46) instead of re-evaluating b - H x (b - L x) with the FP64 stencil.
     The FP64 state x takes the same += e, the stopping tests the same norms,
     so the sub-steps agree with the FP64-defect solves to the solver
-    tolerance (1e-10 relative, as the inner-solver variants) and with the
-    FP64 form to the mixed form's 1e-8 bar. The IB cases also spread their
+    tolerance (1e-10 relative, as the inner-solver variants; 1e-9 at 256^3)
+    and with the FP64 form to the mixed form's 1e-8 bar. The IB cases also spread their
     forces with double-float products and sums (2^-44) against FP64
     spreading (AFMIB_SPREAD_DF)."""
     channel = bc == capi.BC_CHANNEL
@@ -631,8 +631,12 @@ def test_double_float_outer_residual(monkeypatch, n, bc, markers):
                 for _ in range(4):
                     sv.ns_step(*f)
             out[key] = sv.get_velocity()
+    # both pressure solves stop at RMS(r) <= tol: at 256^3 the 2-norm of
+    # what each leaves is 4096 times that, and their velocities differ by
+    # more than at 32^3-64^3 (measured 1.7e-10 after 4 sub-steps)
+    bar = 1e-10 if n <= 64 else 1e-9
     for a, b in zip(out["defects"], out["df"]):
-        assert rel(b, a) < 1e-10
+        assert rel(b, a) < bar
     for a, b in zip(out["fp64"], out["df"]):
         assert rel(b, a) < 1e-8
 
