@@ -48,7 +48,8 @@ void launch_helm_rhs(const Dims& d, int comp, int be, T* r, const T* uold, const
 // defect r = b - H uold as FP32 with out[0] = r.r (H = I + s_minus Delta), and
 // q = Q(uold), the off-diagonal term of the Helmholtz rows, in one pass.
 // walk_blocks > 0: the persistent form on that many blocks (tile_walk);
-// uo_out: also a copy of uold there.
+// uo_out: also a copy of uold there; r_lo (the double-float residual): b is
+// not written and r is formed as src - bm - off Q.
 template <typename TF, typename TA>
 void launch_helm_rhs_be_defect(const Dims& d, int comp, double* b, float* r, double* q, const double* uold,
                                const TF* f, const TA* adv, const double* top, const double* bottom, double s_minus,
