@@ -61,6 +61,13 @@ template <typename TF, typename TA>
 void launch_helm_rhs_cn_q(const Dims& d, int comp, double* r, const double* uold, const double* q, const TF* f,
                           const TA* adv, const double* top, const double* bottom, double s_plus, double s_minus,
                           double dt, double inv_rho, cudaStream_t s);
+// Mixed form, Crank-Nicolson sub-step with the double-float residual: x =
+// uold and the first residual r = b - H uold from the kept Q (pointwise), as
+// its double-float pair (rh, rl), out[0] = rh.rh.
+template <typename TF, typename TA>
+void launch_helm_cn_first(const Dims& d, int comp, double* x, float* rh, float* rl, const double* uold, const double* q,
+                          const TF* f, const TA* adv, const double* top, const double* bottom, double s_plus,
+                          double s_minus, double dt, double inv_rho, RedScratch sc, double* out, cudaStream_t s);
 // Mixed form: r = b - (I + s Delta) x in FP64, stored as TD, out[0] = ||r||^2;
 // walk_blocks > 0: the persistent form on that many blocks (tile_walk).
 template <typename TD>

@@ -380,6 +380,53 @@ __global__ void k_helm_rhs_cn_q(Dims d, int comp, double* __restrict__ r, const 
     }
 }
 
+// Mixed form, Crank-Nicolson sub-step with the double-float residual: the
+// viscous solve starts from x = uold instead of the current velocity, so its
+// first residual needs no stencil. With b as k_helm_rhs_cn_q forms it and
+// H uold = uold + off- Q(uold) (Q kept by the backward-Euler pass),
+// r = b - H uold = (off+ - off-) Q + src (+ bp - bm on the channel u/w wall
+// rows; -uold on the v wall plane): one FP64 pass at HBM speed. Writes
+// x = uold, the residual's double-float pair and out[0] = rh.rh.
+template <typename TF, typename TA>
+__global__ void __launch_bounds__(kRedBlock) k_helm_cn_first(Dims d, int comp, double* __restrict__ xo,
+                                                            float* __restrict__ rh, float* __restrict__ rl,
+                                                            const double* __restrict__ uold, const double* __restrict__ q,
+                                                            const TF* __restrict__ f, const TA* __restrict__ adv,
+                                                            const double* __restrict__ top,
+                                                            const double* __restrict__ bottom, double s_plus,
+                                                            double s_minus, double hdt, double inv_rho, RedScratch sc,
+                                                            double* out) {
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+    const double offd = (s_plus - s_minus) * double(d.n) * double(d.n);
+    float acc = 0.f;
+    if (xi < d.nx && yi < d.ny)
+        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
+            const long long i = lin(d, xi, yi, zi);
+            const double u0 = uold[i];
+            double rd;
+            if (d.channel && comp == 1 && yi == 0) {
+                rd = -u0;
+            } else {
+                double s2 = hdt * (inv_rho * cvt<double, TF>(f[i]) - cvt<double, TA>(adv[i]));
+                if (d.channel && comp != 1 && (yi == 0 || yi == d.ny - 1) && top) {
+                    const long long ixz = xi + (long long)d.nx * zi;
+                    const double wv = (yi == 0) ? bottom[ixz] : top[ixz];
+                    const double bm = 8. / 3. * s_minus * d.n * d.n * wv, bp = 8. / 3. * s_plus * d.n * d.n * wv;
+                    s2 = s2 + (bp - bm);
+                }
+                rd = offd * q[i] + s2;
+            }
+            xo[i] = u0;
+            float lo;
+            const float hi = defect_words(rd, &lo, true);
+            rh[i] = hi;
+            rl[i] = lo;
+            acc += hi * hi;
+        }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, out);
+}
+
 // ---------------------------------------------------------------------------
 // CG pieces. Scalars live on the device in cgs[] = {n0, pq, n1, beta, alpha}
 // so that no host round trip sits inside an iteration except the convergence
@@ -763,6 +810,21 @@ void launch_helm_rhs_cn_q(const Dims& d, int comp, double* r, const double* uold
     k_helm_rhs_cn_q<TF, TA><<<grid3(d), block3(), 0, s>>>(d, comp, r, uold, q, f, adv, top, bottom, s_plus, s_minus, dt,
                                                           inv_rho);
 }
+template <typename TF, typename TA>
+void launch_helm_cn_first(const Dims& d, int comp, double* x, float* rh, float* rl, const double* uold, const double* q,
+                          const TF* f, const TA* adv, const double* top, const double* bottom, double s_plus,
+                          double s_minus, double dt, double inv_rho, RedScratch sc, double* out, cudaStream_t s) {
+    k_helm_cn_first<TF, TA><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(
+        d, comp, x, rh, rl, uold, q, f, adv, top, bottom, s_plus, s_minus, dt, inv_rho, sc, out);
+}
+template void launch_helm_cn_first<double, float>(const Dims&, int, double*, float*, float*, const double*,
+                                                  const double*, const double*, const float*, const double*,
+                                                  const double*, double, double, double, double, RedScratch, double*,
+                                                  cudaStream_t);
+template void launch_helm_cn_first<float, float>(const Dims&, int, double*, float*, float*, const double*,
+                                                 const double*, const float*, const float*, const double*,
+                                                 const double*, double, double, double, double, RedScratch, double*,
+                                                 cudaStream_t);
 template void launch_helm_rhs_be_defect<double, float>(const Dims&, int, double*, float*, double*, const double*,
                                                        const double*, const float*, const double*, const double*,
                                                        double, double, double, RedScratch, double*, cudaStream_t, int,

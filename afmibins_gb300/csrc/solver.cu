@@ -84,6 +84,11 @@ struct afmib_solver {
     // products and face sums in double-float (relative 2^-44; the FP64 form
     // and the single-operator entry point stay FP64; AFMIB_SPREAD_DF=0: FP64)
     bool spread_df = true;
+    // mixed form with the double-float residual: the Crank-Nicolson viscous
+    // solves start from uold (the step's start velocity), whose residual
+    // comes pointwise from the kept Q, instead of the current velocity
+    // (AFMIB_CN_START_OLD=0: the current velocity and an FP64 stencil)
+    bool cn_start_old = true;
     double *divb = nullptr, *walls = nullptr, *wallgrad = nullptr;
     double *cg_r = nullptr, *cg_p = nullptr, *cg_q = nullptr;
     double *tmp[3] = {};
@@ -1096,7 +1101,8 @@ int substep(afmib_solver* s) {
             }
             s->qo_valid = true;
         } else {
-            for (int c = 0; c < 3; ++c) {
+            const bool cn_first = ovl && s->helm_df && s->rlo[0] && s->qo_valid && s->cn_start_old;
+            for (int c = 0; c < 3 && !cn_first; ++c) {
                 const double *top, *bot;
                 walls_of(c, &top, &bot);
                 if (s->qo_valid) {
@@ -1122,6 +1128,22 @@ int substep(afmib_solver* s) {
             CKL();
             if (ovl) {
                 TRY(helm_solve3_mixed(s, s->s_minus(), vel, s->rhs, [&](int c, cudaStream_t hs, float* lo) {
+                    if (cn_first) {
+                        const double *top, *bot;
+                        walls_of(c, &top, &bot);
+                        ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 8 + 4 + 8 + 4 + 4), 1, hs);
+                        if (s->spread64)
+                            launch_helm_cn_first<double, float>(d, c, vel[c], s->d32c[c], lo, s->uo[c], s->qo[c],
+                                                                s->f[c], s->adv32[c], top, bot, s->s_plus(),
+                                                                s->s_minus(), s->cfg.dt, inv_rho, s->red,
+                                                                s->scal + 12 + c, hs);
+                        else
+                            launch_helm_cn_first<float, float>(d, c, vel[c], s->d32c[c], lo, s->uo[c], s->qo[c],
+                                                               s->f32[c], s->adv32[c], top, bot, s->s_plus(),
+                                                               s->s_minus(), s->cfg.dt, inv_rho, s->red,
+                                                               s->scal + 12 + c, hs);
+                        return;
+                    }
                     ProfScope ps(s, P_HELM_DEFECT, (double)N * (8 + 8 + 4), 1, hs);
                     launch_helm_defect<float>(d, c, s->s_minus(), vel[c], s->rhs[c], s->d32c[c], s->red,
                                               s->scal + 12 + c, hs, s->walk_blocks, lo);
@@ -1809,6 +1831,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_HELM_DF")) s->helm_df = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_LAP_DF")) s->lap_df = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_SPREAD_DF")) s->spread_df = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_CN_START_OLD")) s->cn_start_old = std::string(e) != "0";
     if (s->mixed && s->fused_rhs)
         for (auto& q : s->qo) TRY(dalloc(s, &q, N));
     TRY(dalloc(s, &s->phi_prev[0], N));
