@@ -22,7 +22,22 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liborc.so")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_SRC = os.environ.get("AFMIB_REFERENCE", "/root/reference")
+
+
+def _make_default_reference() -> str:
+    """The reference source tree named by the oracle's Makefile (REF ?= ...)."""
+    try:
+        with open(os.path.join(HERE, "Makefile")) as f:
+            for line in f:
+                if line.startswith("REF ?="):
+                    return line.split("?=", 1)[1].strip()
+    except OSError:
+        pass
+    return ""
+
+
+# AFMIB_REFERENCE overrides the Makefile's default location of the reference sources.
+REFERENCE_SRC = os.environ.get("AFMIB_REFERENCE") or _make_default_reference()
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -63,8 +78,24 @@ def lib():
         L.orc_mg_solve.argtypes = [_ip, ctypes.c_int, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                    ctypes.c_int, _ip]
         L.orc_helm_apply.argtypes = [_ip, ctypes.c_int, ctypes.c_double, _dp, _dp]
+        L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_set_fast_rows.argtypes = [ctypes.c_int]
         _lib = L
     return _lib
+
+
+def set_threads(n: int) -> None:
+    """Threads of the oracle's parallel passes; the results do not depend on it."""
+    lib().orc_set_threads(int(n))
+
+
+def get_threads() -> int:
+    return int(lib().orc_get_threads())
+
+
+def set_fast_rows(on: bool) -> None:
+    """False routes every operator row through the generic row builder."""
+    lib().orc_set_fast_rows(1 if on else 0)
 
 
 def _p(a):

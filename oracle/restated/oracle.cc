@@ -21,16 +21,52 @@
 //
 // Compile with -ffp-contract=off so that results are identical on x86-64 and
 // aarch64 (no fused multiply-adds).
+//
+// Threads (orc_set_threads, default 1). Every parallel pass gives the same
+// bits as the one-thread pass: each output element is computed by one thread
+// from the same operands in the same order. Stencil, transfer and vector
+// passes split the cells; spreading splits the faces by z slab and each slab
+// takes its markers in index order; the lexicographic Gauss–Seidel sweep
+// keeps its sequential semantics by a plane pipeline (plane z starts row y
+// only once plane z-1 has finished row y, so every cell reads exactly the
+// updated and not-yet-updated neighbours of the one-thread sweep); dot
+// products and norms stay one sequential sum. Interior rows of the 7-point
+// operators (every neighbour inside the box, extents >= 3) take a direct form
+// with the columns and values make_row produces there, in the same order.
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <tuple>
+#include <utility>
 #include <vector>
 
 namespace {
 
-typedef std::vector<double> vec;
+// Vectors whose size-only constructor and resize leave the new elements
+// uninitialised: every such vector below is written in full before it is
+// read (or filled by par_fill), so large arrays are first touched by the
+// threads of the pass that fills them rather than by one serial memset.
+template <class T>
+struct uninit_alloc : std::allocator<T> {
+    template <class U>
+    struct rebind { typedef uninit_alloc<U> other; };
+    uninit_alloc() = default;
+    template <class U>
+    uninit_alloc(const uninit_alloc<U>&) {}
+    template <class U>
+    void construct(U* p) { ::new ((void*)p) U; }
+    template <class U, class... A>
+    void construct(U* p, A&&... a) { ::new ((void*)p) U(std::forward<A>(a)...); }
+};
+typedef std::vector<double, uninit_alloc<double>> vec;
 
 // Grid description. dims[] from the C API = {nx, ny, nz, n, channel}.
 struct Grid {
@@ -46,6 +82,50 @@ struct Grid {
 Grid make_grid(const int* d) { return Grid{d[0], d[1], d[2], d[3], d[4] != 0}; }
 
 inline int wrap(int i, int m) { return ((i % m) + m) % m; }
+
+// ---------------------------------------------------------------------------
+// Threads
+// ---------------------------------------------------------------------------
+int g_threads = 1;
+bool g_fast_rows = true;
+
+// f(lo, hi) over [0, n) in contiguous chunks, one per thread; one call on the
+// calling thread when n is small or one thread is configured.
+template <class F>
+void par_range(long n, long min_chunk, F f) {
+    long T = g_threads;
+    if (min_chunk > 0) T = std::min(T, n / min_chunk);
+    if (T <= 1) {
+        f(0L, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve(T - 1);
+    for (long t = 1; t < T; ++t) th.emplace_back([&f, n, t, T] { f(n * t / T, n * (t + 1) / T); });
+    f(0L, n / T);
+    for (auto& x : th) x.join();
+}
+
+// Element-wise pass over [0, n).
+template <class F>
+void par_for(long n, F f) {
+    par_range(n, 1L << 15, [&f](long lo, long hi) {
+        for (long i = lo; i < hi; ++i) f(i);
+    });
+}
+
+inline void par_fill(vec& v, long n, double value) {
+    v.resize(n);
+    double* p = v.data();
+    par_for(n, [p, value](long i) { p[i] = value; });
+}
+
+inline void par_copy(vec& dst, const vec& src) {
+    dst.resize(src.size());
+    double* d = dst.data();
+    const double* s = src.data();
+    par_for((long)src.size(), [d, s](long i) { d[i] = s[i]; });
+}
 
 // ---------------------------------------------------------------------------
 // Sparse rows. The reference stores its operators as CSR whose rows are
@@ -158,32 +238,199 @@ void make_row(const Op& op, long i, Row& r) {
 
 long op_size(const Op& op) { return (long)op.nx * op.ny * op.nz; }
 
+// Coefficients of an interior row: off on the six neighbours, diag on the
+// centre, as the first lines of make_row compute them. ok is false where
+// make_row would drop a zero entry or an extent folds (below 3).
+struct Interior {
+    double off, diag;
+    bool ok;
+};
+
+Interior interior_coef(const Op& op) {
+    Interior c;
+    if (op.kind == OP_LAPLACIAN) {
+        c.off = (double)(op.n * op.n);
+        c.diag = -6.0 * c.off;
+    } else if (op.kind == OP_HELM_CELL) {
+        c.off = op.scale * op.n * op.n;
+        c.diag = 1. - 6. * c.off;
+    } else {
+        c.diag = 1. - op.scale * 6. * (double)(op.n * op.n);
+        c.off = op.scale * op.n * op.n;
+    }
+    c.ok = g_fast_rows && op.nx >= 3 && op.ny >= 3 && op.nz >= 3 && c.off != 0 && c.diag != 0;
+    return c;
+}
+
+// Rows of the cells that touch a face of the box, built once per operator by
+// make_row and kept in walk order: all nx cells of the rows with y or z on a
+// face, the cells x = 0 and x = nx-1 of the others. start[y + ny*z] is the
+// first cached row of grid row (y, z).
+struct FaceRows {
+    std::vector<Row> rows;
+    std::vector<long> start;
+};
+
+inline bool face_row(const Op& op, int y, int z) { return y < 1 || y > op.ny - 2 || z < 1 || z > op.nz - 2; }
+
+const FaceRows& face_rows(const Op& op) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int, int, int, int, uint64_t>, std::unique_ptr<FaceRows>> cache;
+    uint64_t sbits;
+    std::memcpy(&sbits, &op.scale, sizeof sbits);
+    const auto key = std::make_tuple((int)op.kind, op.nx, op.ny, op.nz, op.n, (int)op.channel, sbits);
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return *it->second;
+    std::unique_ptr<FaceRows> fr(new FaceRows);
+    const long rows = (long)op.ny * op.nz;
+    fr->start.resize(rows + 1);
+    long cnt = 0;
+    for (int z = 0; z < op.nz; ++z)
+        for (int y = 0; y < op.ny; ++y) {
+            fr->start[y + (long)op.ny * z] = cnt;
+            cnt += face_row(op, y, z) ? op.nx : 2;
+        }
+    fr->start[rows] = cnt;
+    fr->rows.resize(cnt);
+    FaceRows* f = fr.get();
+    par_range(op.nz, 1, [&](long z0, long z1) {
+        for (int z = (int)z0; z < (int)z1; ++z)
+            for (int y = 0; y < op.ny; ++y) {
+                const long base = (long)op.nx * (y + (long)op.ny * z), s0 = f->start[y + (long)op.ny * z];
+                if (face_row(op, y, z)) {
+                    for (int x = 0; x < op.nx; ++x) make_row(op, base + x, f->rows[s0 + x]);
+                } else {
+                    make_row(op, base, f->rows[s0]);
+                    make_row(op, base + op.nx - 1, f->rows[s0 + 1]);
+                }
+            }
+    });
+    return *(cache[key] = std::move(fr));
+}
+
+// Row (y, z) of the operator in increasing x: generic(i, row) on the cells
+// that touch a face of the box (rows from the cache, or from make_row when
+// the direct form is off), inner(i) on the interior cells, whose sorted
+// columns are i-nx*ny, i-nx, i-1, i, i+1, i+nx, i+nx*ny.
+template <class G, class F>
+inline void walk_row(const Op& op, const Interior& c, const FaceRows* fr, int y, int z, G&& generic, F&& inner) {
+    const int nx = op.nx;
+    const long base = (long)nx * (y + (long)op.ny * z);
+    if (!c.ok) {
+        Row r;
+        for (int x = 0; x < nx; ++x) {
+            make_row(op, base + x, r);
+            generic(base + x, r);
+        }
+        return;
+    }
+    const Row* rw = fr->rows.data() + fr->start[y + (long)op.ny * z];
+    if (face_row(op, y, z)) {
+        for (int x = 0; x < nx; ++x) generic(base + x, rw[x]);
+        return;
+    }
+    generic(base, rw[0]);
+    for (int x = 1; x < nx - 1; ++x) inner(base + x);
+    generic(base + nx - 1, rw[1]);
+}
+
 // y = A x, src/dt/matrix.h:81-94
 void spmv(const Op& op, vec& y, const vec& x) {
     const long N = op_size(op);
-    y.assign(N, 0.0);
-    Row r;
-    for (long i = 0; i < N; ++i) {
-        make_row(op, i, r);
+    y.resize(N);
+    const Interior c = interior_coef(op);
+    const long nx = op.nx, sxy = (long)op.nx * op.ny;
+    double* Y = y.data();
+    const double* X = x.data();
+    const FaceRows* fr = c.ok ? &face_rows(op) : nullptr;
+    auto generic = [&](long i, const Row& r) {
         double acc = 0.0;
-        for (int k = 0; k < r.cnt; ++k) acc += r.val[k] * x[r.col[k]];
-        y[i] = acc;
-    }
+        for (int k = 0; k < r.cnt; ++k) acc += r.val[k] * X[r.col[k]];
+        Y[i] = acc;
+    };
+    auto inner = [&](long i) {
+        double acc = 0.0;
+        acc += c.off * X[i - sxy];
+        acc += c.off * X[i - nx];
+        acc += c.off * X[i - 1];
+        acc += c.diag * X[i];
+        acc += c.off * X[i + 1];
+        acc += c.off * X[i + nx];
+        acc += c.off * X[i + sxy];
+        Y[i] = acc;
+    };
+    const long planes = op.nz, rows = op.ny;
+    par_range(planes, N >= (1L << 15) ? 1 : planes, [&](long z0, long z1) {
+        for (long z = z0; z < z1; ++z)
+            for (long yy = 0; yy < rows; ++yy) walk_row(op, c, fr, (int)yy, (int)z, generic, inner);
+    });
 }
 
-// One lexicographic Gauss–Seidel sweep, src/alg/smooth.h:35-51
+// One lexicographic Gauss–Seidel sweep, src/alg/smooth.h:35-51: cell i reads
+// the updated values of the cells before it and the old values of the cells
+// after it.
 void gs_sweep(const Op& op, vec& x, const vec& b) {
     const long N = op_size(op);
-    Row r;
-    for (long i = 0; i < N; ++i) {
-        make_row(op, i, r);
+    const Interior c = interior_coef(op);
+    const long nx = op.nx, sxy = (long)op.nx * op.ny;
+    double* X = x.data();
+    const double* B = b.data();
+    const FaceRows* fr = c.ok ? &face_rows(op) : nullptr;
+    auto generic = [&](long i, const Row& r) {
         double value = 0.0, diagonal = 0.0;
         for (int k = 0; k < r.cnt; ++k) {
             if (r.col[k] == i) { diagonal = r.val[k]; continue; }
-            value += r.val[k] * x[r.col[k]];
+            value += r.val[k] * X[r.col[k]];
         }
-        x[i] = (b[i] - value) / diagonal;
+        X[i] = (B[i] - value) / diagonal;
+    };
+    auto inner = [&](long i) {
+        double value = 0.0;
+        value += c.off * X[i - sxy];
+        value += c.off * X[i - nx];
+        value += c.off * X[i - 1];
+        value += c.off * X[i + 1];
+        value += c.off * X[i + nx];
+        value += c.off * X[i + sxy];
+        X[i] = (B[i] - value) / c.diag;
+    };
+    const int nz = op.nz, ny = op.ny;
+    const int T = (int)std::min<long>(g_threads, nz / 2);
+    if (T <= 1 || nz < 4 || N < (1L << 15)) {
+        for (int z = 0; z < nz; ++z)
+            for (int y = 0; y < ny; ++y) walk_row(op, c, fr, y, z, generic, inner);
+        return;
     }
+    // Plane pipeline: thread t sweeps planes t, t+T, ... in order; plane z
+    // starts row y once plane z-1 has finished row y. A 7-point row of plane
+    // z reads rows y of planes z-1 (final by then) and z+1 (not yet started,
+    // since plane z+1 waits for this row), and rows y-1, y+1 of its own plane
+    // in sweep order, which is what the one-thread sweep reads. The periodic
+    // images (plane 0 reads plane nz-1 before it is swept, plane nz-1 reads
+    // plane 0 after) follow from the same chain.
+    // Rows go in chunks of about 2k cells between synchronisations (a chunk
+    // of plane z waits until plane z-1 has finished the same rows); one
+    // cache line per plane counter.
+    struct alignas(64) Progress { std::atomic<int> rows; };
+    std::unique_ptr<Progress[]> done(new Progress[nz]);
+    for (int z = 0; z < nz; ++z) done[z].rows.store(0, std::memory_order_relaxed);
+    const int chunk = std::max(1, 2048 / op.nx);
+    auto work = [&](int t) {
+        for (int z = t; z < nz; z += T) {
+            for (int y0 = 0; y0 < ny; y0 += chunk) {
+                const int y1 = std::min(ny, y0 + chunk);
+                if (z > 0)
+                    while (done[z - 1].rows.load(std::memory_order_acquire) < y1) std::this_thread::yield();
+                for (int y = y0; y < y1; ++y) walk_row(op, c, fr, y, z, generic, inner);
+                done[z].rows.store(y1, std::memory_order_release);
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < T; ++t) th.emplace_back(work, t);
+    work(0);
+    for (auto& t : th) t.join();
 }
 
 double dot(const vec& a, const vec& b) {
@@ -205,22 +452,28 @@ int cg_solve(const Op& op, vec& x, const vec& b, double tol, int maxit, int* ite
     const long N = op_size(op);
     vec r(N), p(N), z(N);
     spmv(op, z, x);
-    for (long i = 0; i < N; ++i) r[i] = b[i] - z[i];
-    p = r;
+    double *X = x.data(), *R = r.data(), *P = p.data(), *Z = z.data();
+    const double* B = b.data();
+    par_for(N, [=](long i) { R[i] = B[i] - Z[i]; });
+    par_copy(p, r);
     double n0 = dot(r, r);
     int count = 0;
     while (std::sqrt(n0) > tol) {
         if (count >= maxit || !std::isfinite(n0)) { *iters = count; return 3; }
         spmv(op, z, p);
-        double nu = n0 / dot(p, z);
-        for (long i = 0; i < N; ++i) x[i] += nu * p[i];
-        for (long i = 0; i < N; ++i) z[i] *= nu;
-        for (long i = 0; i < N; ++i) r[i] -= z[i];
-        double n1 = dot(r, r);
-        double mu = n1 / n0;
+        const double nu = n0 / dot(p, z);
+        par_for(N, [=](long i) {
+            X[i] += nu * P[i];
+            Z[i] *= nu;
+            R[i] -= Z[i];
+        });
+        const double n1 = dot(r, r);
+        const double mu = n1 / n0;
         n0 = n1;
-        for (long i = 0; i < N; ++i) p[i] *= mu;
-        for (long i = 0; i < N; ++i) p[i] += r[i];
+        par_for(N, [=](long i) {
+            P[i] *= mu;
+            P[i] += R[i];
+        });
         ++count;
     }
     *iters = count;
@@ -258,21 +511,39 @@ void restrict_fw(const Level& f, bool channel, vec& out, const vec& in) {
         return;
     }
     const int cx = f.nx / 2, cy = f.ny / 2, cz = f.nz / 2;
-    out.assign((long)cx * cy * cz, 0.0);
-    for (int xcc = 0; xcc < cx; ++xcc)
-        for (int ycc = 0; ycc < cy; ++ycc)
-            for (int zcc = 0; zcc < cz; ++zcc) {
-                const int xcf = 2 * xcc + 1, ycf = 2 * ycc + 1, zcf = 2 * zcc + 1;
-                double& o = out[xcc + (long)cx * (ycc + (long)cy * zcc)];
-                for (int t = 0; t < 64; ++t) {
-                    const int dx = (t % 4) - 2, dy = (t % 16) / 4 - 2, dz = t / 16 - 2;
-                    const int x = wrap(xcf + dx, f.nx);
-                    const int y = channel ? std::min(ycf + std::max(dy, -ycf), f.ny - 1) : wrap(ycf + dy, f.ny);
-                    const int z = wrap(zcf + dz, f.nz);
-                    const int weight = (4 - std::abs(2 * dx + 1)) * (4 - std::abs(2 * dy + 1)) * (4 - std::abs(2 * dz + 1));
-                    o += weight / 512. * in[x + (long)f.nx * (y + (long)f.ny * z)];
+    par_fill(out, (long)cx * cy * cz, 0.0);
+    // every coarse cell sums its 64 taps in the same order whichever thread
+    // takes it
+    // tap t: dx = t%4 - 2, dy = (t%16)/4 - 2, dz = t/16 - 2, weight
+    // (4-|2dx+1|)(4-|2dy+1|)(4-|2dz+1|)/512; fine indices per axis and tap
+    // taken from tables (the same wraps and wall clamps)
+    double wt[64];
+    for (int t = 0; t < 64; ++t) {
+        const int dx = (t % 4) - 2, dy = (t % 16) / 4 - 2, dz = t / 16 - 2;
+        const int weight = (4 - std::abs(2 * dx + 1)) * (4 - std::abs(2 * dy + 1)) * (4 - std::abs(2 * dz + 1));
+        wt[t] = weight / 512.;
+    }
+    std::vector<long> tx(4L * cx), ty(4L * cy), tz(4L * cz);
+    for (int c = 0; c < cx; ++c)
+        for (int d = 0; d < 4; ++d) tx[4 * c + d] = wrap(2 * c + 1 + d - 2, f.nx);
+    for (int c = 0; c < cy; ++c)
+        for (int d = 0; d < 4; ++d) {
+            const int ycf = 2 * c + 1, dy = d - 2;
+            ty[4 * c + d] = (long)f.nx * (channel ? std::min(ycf + std::max(dy, -ycf), f.ny - 1) : wrap(ycf + dy, f.ny));
+        }
+    for (int c = 0; c < cz; ++c)
+        for (int d = 0; d < 4; ++d) tz[4 * c + d] = (long)f.nx * f.ny * wrap(2 * c + 1 + d - 2, f.nz);
+    par_range(cz, (long)cx * cy * cz >= 4096 ? 1 : cz, [&](long z0, long z1) {
+        for (int zcc = (int)z0; zcc < (int)z1; ++zcc)
+            for (int ycc = 0; ycc < cy; ++ycc)
+                for (int xcc = 0; xcc < cx; ++xcc) {
+                    double& o = out[xcc + (long)cx * (ycc + (long)cy * zcc)];
+                    const long* px = &tx[4 * xcc];
+                    const long* py = &ty[4 * ycc];
+                    const long* pz = &tz[4 * zcc];
+                    for (int t = 0; t < 64; ++t) o += wt[t] * in[px[t % 4] + py[(t % 16) / 4] + pz[t / 16]];
                 }
-            }
+    });
 }
 
 // Cell-centred trilinear prolongation (27,9,3,1)/64 that ASSIGNS the fine
@@ -300,46 +571,50 @@ void prolong_assign(const Level& f, bool channel, vec& out, const vec& in) {
     }
     const int cx = f.nx / 2, cy = f.ny / 2, cz = f.nz / 2;
     const int nx = f.nx, ny = f.ny, nz = f.nz;
-    out.assign((long)nx * ny * nz, 0.0);
+    par_fill(out, (long)nx * ny * nz, 0.0);
     auto C = [&](int x, int y, int z) { return in[x + (long)cx * (y + (long)cy * z)]; };
     auto F = [&](int x, int y, int z) -> double& { return out[x + (long)nx * (y + (long)ny * z)]; };
     const int ylim = channel ? cy - 1 : cy;
-    for (int xcc = 0; xcc < cx; ++xcc) {
-        for (int ycc = 0; ycc < ylim; ++ycc)
-            for (int zcc = 0; zcc < cz; ++zcc) {
-                const int xnc = (xcc + 1) % cx, ync = channel ? ycc + 1 : (ycc + 1) % cy, znc = (zcc + 1) % cz;
-                const int xcf = 2 * xcc + 1, ycf = 2 * ycc + 1, zcf = 2 * zcc + 1;
-                const int xnf = (xcf + 1) % nx, ynf = channel ? ycf + 1 : (ycf + 1) % ny, znf = (zcf + 1) % nz;
-                const double blbc = C(xcc, ycc, zcc), brbc = C(xnc, ycc, zcc), ulbc = C(xcc, ync, zcc),
-                             urbc = C(xnc, ync, zcc), blfc = C(xcc, ycc, znc), brfc = C(xnc, ycc, znc),
-                             ulfc = C(xcc, ync, znc), urfc = C(xnc, ync, znc);
-                F(xcf, ycf, zcf) = 27. / 64. * blbc + 9. / 64. * (brbc + ulbc + blfc) + 3. / 64. * (urbc + ulfc + brfc) + 1. / 64. * urfc;
-                F(xnf, ycf, zcf) = 27. / 64. * brbc + 9. / 64. * (urbc + blbc + brfc) + 3. / 64. * (ulbc + blfc + urfc) + 1. / 64. * ulfc;
-                F(xcf, ynf, zcf) = 27. / 64. * ulbc + 9. / 64. * (urbc + blbc + ulfc) + 3. / 64. * (brbc + blfc + urfc) + 1. / 64. * brfc;
-                F(xnf, ynf, zcf) = 27. / 64. * urbc + 9. / 64. * (brbc + ulbc + urfc) + 3. / 64. * (blbc + ulfc + brfc) + 1. / 64. * blfc;
-                F(xcf, ycf, znf) = 27. / 64. * blfc + 9. / 64. * (brfc + ulfc + blbc) + 3. / 64. * (urfc + ulbc + brbc) + 1. / 64. * urbc;
-                F(xnf, ycf, znf) = 27. / 64. * brfc + 9. / 64. * (urfc + blfc + brbc) + 3. / 64. * (ulfc + blbc + urbc) + 1. / 64. * ulbc;
-                F(xcf, ynf, znf) = 27. / 64. * ulfc + 9. / 64. * (urfc + blfc + ulbc) + 3. / 64. * (brfc + blbc + urbc) + 1. / 64. * brbc;
-                F(xnf, ynf, znf) = 27. / 64. * urfc + 9. / 64. * (brfc + ulfc + urbc) + 3. / 64. * (blfc + ulbc + brbc) + 1. / 64. * blbc;
+    // each coarse cell writes its own eight fine cells (and, in channel mode,
+    // each coarse wall column its own wall cells): disjoint across threads
+    par_range(cz, (long)nx * ny * nz >= (1L << 15) ? 1 : cz, [&](long z0, long z1) {
+        for (int zcc = (int)z0; zcc < (int)z1; ++zcc)
+            for (int ycc = 0; ycc < ylim; ++ycc)
+                for (int xcc = 0; xcc < cx; ++xcc) {
+                    const int xnc = (xcc + 1) % cx, ync = channel ? ycc + 1 : (ycc + 1) % cy, znc = (zcc + 1) % cz;
+                    const int xcf = 2 * xcc + 1, ycf = 2 * ycc + 1, zcf = 2 * zcc + 1;
+                    const int xnf = (xcf + 1) % nx, ynf = channel ? ycf + 1 : (ycf + 1) % ny, znf = (zcf + 1) % nz;
+                    const double blbc = C(xcc, ycc, zcc), brbc = C(xnc, ycc, zcc), ulbc = C(xcc, ync, zcc),
+                                 urbc = C(xnc, ync, zcc), blfc = C(xcc, ycc, znc), brfc = C(xnc, ycc, znc),
+                                 ulfc = C(xcc, ync, znc), urfc = C(xnc, ync, znc);
+                    F(xcf, ycf, zcf) = 27. / 64. * blbc + 9. / 64. * (brbc + ulbc + blfc) + 3. / 64. * (urbc + ulfc + brfc) + 1. / 64. * urfc;
+                    F(xnf, ycf, zcf) = 27. / 64. * brbc + 9. / 64. * (urbc + blbc + brfc) + 3. / 64. * (ulbc + blfc + urfc) + 1. / 64. * ulfc;
+                    F(xcf, ynf, zcf) = 27. / 64. * ulbc + 9. / 64. * (urbc + blbc + ulfc) + 3. / 64. * (brbc + blfc + urfc) + 1. / 64. * brfc;
+                    F(xnf, ynf, zcf) = 27. / 64. * urbc + 9. / 64. * (brbc + ulbc + urfc) + 3. / 64. * (blbc + ulfc + brfc) + 1. / 64. * blfc;
+                    F(xcf, ycf, znf) = 27. / 64. * blfc + 9. / 64. * (brfc + ulfc + blbc) + 3. / 64. * (urfc + ulbc + brbc) + 1. / 64. * urbc;
+                    F(xnf, ycf, znf) = 27. / 64. * brfc + 9. / 64. * (urfc + blfc + brbc) + 3. / 64. * (ulfc + blbc + urbc) + 1. / 64. * ulbc;
+                    F(xcf, ynf, znf) = 27. / 64. * ulfc + 9. / 64. * (urfc + blfc + ulbc) + 3. / 64. * (brfc + blbc + urbc) + 1. / 64. * brbc;
+                    F(xnf, ynf, znf) = 27. / 64. * urfc + 9. / 64. * (brfc + ulfc + urbc) + 3. / 64. * (blfc + ulbc + brbc) + 1. / 64. * blbc;
+                }
+        if (!channel) return;
+        for (int zcc = (int)z0; zcc < (int)z1; ++zcc)
+            for (int xcc = 0; xcc < cx; ++xcc) {
+                const int xnc = (xcc + 1) % cx, znc = (zcc + 1) % cz;
+                const int xcf = 2 * xcc + 1, zcf = 2 * zcc + 1;
+                const int xnf = (xcf + 1) % nx, znf = (zcf + 1) % nz;
+                const double blbc = C(xcc, 0, zcc), brbc = C(xnc, 0, zcc), blfc = C(xcc, 0, znc), brfc = C(xnc, 0, znc),
+                             ulbc = C(xcc, cy - 1, zcc), urbc = C(xnc, cy - 1, zcc), ulfc = C(xcc, cy - 1, znc),
+                             urfc = C(xnc, cy - 1, znc);
+                F(xcf, 0, zcf) = 9. / 16. * blbc + 3. / 16. * (brbc + blfc) + 1. / 16. * brfc;
+                F(xnf, 0, zcf) = 9. / 16. * brbc + 3. / 16. * (blbc + brfc) + 1. / 16. * blfc;
+                F(xcf, 0, znf) = 9. / 16. * blfc + 3. / 16. * (brfc + blbc) + 1. / 16. * brbc;
+                F(xnf, 0, znf) = 9. / 16. * brfc + 3. / 16. * (blfc + brbc) + 1. / 16. * blbc;
+                F(xcf, ny - 1, zcf) = 9. / 16. * ulbc + 3. / 16. * (urbc + ulfc) + 1. / 16. * urfc;
+                F(xnf, ny - 1, zcf) = 9. / 16. * urbc + 3. / 16. * (ulbc + urfc) + 1. / 16. * ulfc;
+                F(xcf, ny - 1, znf) = 9. / 16. * ulfc + 3. / 16. * (urfc + ulbc) + 1. / 16. * urbc;
+                F(xnf, ny - 1, znf) = 9. / 16. * urfc + 3. / 16. * (ulfc + urbc) + 1. / 16. * ulbc;
             }
-        if (!channel) continue;
-        for (int zcc = 0; zcc < cz; ++zcc) {
-            const int xnc = (xcc + 1) % cx, znc = (zcc + 1) % cz;
-            const int xcf = 2 * xcc + 1, zcf = 2 * zcc + 1;
-            const int xnf = (xcf + 1) % nx, znf = (zcf + 1) % nz;
-            const double blbc = C(xcc, 0, zcc), brbc = C(xnc, 0, zcc), blfc = C(xcc, 0, znc), brfc = C(xnc, 0, znc),
-                         ulbc = C(xcc, cy - 1, zcc), urbc = C(xnc, cy - 1, zcc), ulfc = C(xcc, cy - 1, znc),
-                         urfc = C(xnc, cy - 1, znc);
-            F(xcf, 0, zcf) = 9. / 16. * blbc + 3. / 16. * (brbc + blfc) + 1. / 16. * brfc;
-            F(xnf, 0, zcf) = 9. / 16. * brbc + 3. / 16. * (blbc + brfc) + 1. / 16. * blfc;
-            F(xcf, 0, znf) = 9. / 16. * blfc + 3. / 16. * (brfc + blbc) + 1. / 16. * brbc;
-            F(xnf, 0, znf) = 9. / 16. * brfc + 3. / 16. * (blfc + brbc) + 1. / 16. * blbc;
-            F(xcf, ny - 1, zcf) = 9. / 16. * ulbc + 3. / 16. * (urbc + ulfc) + 1. / 16. * urfc;
-            F(xnf, ny - 1, zcf) = 9. / 16. * urbc + 3. / 16. * (ulbc + urfc) + 1. / 16. * ulfc;
-            F(xcf, ny - 1, znf) = 9. / 16. * ulfc + 3. / 16. * (urfc + ulbc) + 1. / 16. * urbc;
-            F(xnf, ny - 1, znf) = 9. / 16. * urfc + 3. / 16. * (ulfc + urbc) + 1. / 16. * ulbc;
-        }
-    }
+    });
 }
 
 struct MG {
@@ -366,23 +641,34 @@ struct MG {
     void recurse(int l, vec& rhs) {
         if (coarsest(l)) { coarse_solve(l, rhs); return; }
         const Op A = lap(l);
-        vec x(rhs.size(), 0.0), Ax, rf, rc;
+        const long N = (long)rhs.size();
+        vec x, Ax, rf, rc;
+        par_fill(x, N, 0.0);
         for (int j = 0; j < nu1; ++j) gs_sweep(A, x, rhs);
         spmv(A, Ax, x);
-        rf.resize(rhs.size());
-        for (size_t i = 0; i < rhs.size(); ++i) rf[i] = rhs[i] - Ax[i];
+        rf.resize(N);
+        {
+            double* RF = rf.data();
+            const double *RH = rhs.data(), *AX = Ax.data();
+            par_for(N, [=](long i) { RF[i] = RH[i] - AX[i]; });
+        }
         restrict_fw(lv[l], channel, rc, rf);
         recurse(l + 1, rc);
         prolong_assign(lv[l], channel, rf, rc);
-        for (size_t i = 0; i < x.size(); ++i) x[i] += rf[i];
+        {
+            double* X = x.data();
+            const double* RF = rf.data();
+            par_for(N, [=](long i) { X[i] += RF[i]; });
+        }
         for (int j = 0; j < nu2; ++j) gs_sweep(A, x, rhs);
-        rhs = x;
+        par_copy(rhs, x);
     }
 
     // src/mg/solver.h:183-197 (turns an rhs into a starting iterate)
     void nested(int l, vec& input) {
         if (coarsest(l)) return;
-        vec copy = input, coarse;
+        vec copy, coarse;
+        par_copy(copy, input);
         restrict_fw(lv[l], channel, coarse, input);
         nested(l + 1, coarse);
         recurse(l + 1, coarse);
@@ -394,24 +680,32 @@ struct MG {
     int solve(vec& rhs, int* cycles) {
         status = 0;
         if (coarsest(0)) { coarse_solve(0, rhs); *cycles = 0; return status; }
-        vec x = rhs, Ax, res(rhs.size());
+        const long N = (long)rhs.size();
+        vec x, Ax, res(N);
+        par_copy(x, rhs);
         nested(0, x);
-        vec ones(rhs.size(), 1.0);
-        double m = dot(rhs, ones) / (double)rhs.size();
-        for (auto& e : rhs) e -= m * 1.0;
+        vec ones;
+        par_fill(ones, N, 1.0);
+        const double m = dot(rhs, ones) / (double)N;
+        double *RH = rhs.data(), *X = x.data(), *RS = res.data();
+        par_for(N, [=](long i) { RH[i] -= m * 1.0; });
         const Op A = lap(0);
         spmv(A, Ax, x);
-        for (size_t i = 0; i < rhs.size(); ++i) res[i] = rhs[i] - Ax[i];
+        const double* AX = Ax.data();
+        par_for(N, [=](long i) { RS[i] = RH[i] - AX[i]; });
         int count = 0;
-        while (rms(res) > tol) {
-            if (count >= maxit || !std::isfinite(rms(res))) { status = 3; break; }
+        double rr;
+        while ((rr = rms(res)) > tol) {
+            if (count >= maxit || !std::isfinite(rr)) { status = 3; break; }
             recurse(0, res);
-            for (size_t i = 0; i < x.size(); ++i) x[i] += res[i];
+            RS = res.data();
+            par_for(N, [=](long i) { X[i] += RS[i]; });
             spmv(A, Ax, x);
-            for (size_t i = 0; i < rhs.size(); ++i) res[i] = rhs[i] - Ax[i];
+            AX = Ax.data();
+            par_for(N, [=](long i) { RS[i] = RH[i] - AX[i]; });
             ++count;
         }
-        rhs = x;
+        par_copy(rhs, x);
         *cycles = count;
         return status;
     }
@@ -438,7 +732,7 @@ MG make_mg(const Grid& g, int levels, double tol, int nu1, int nu2, int maxit) {
 void divergence(int nx, int ny, int nz, int n, bool channel, double* d, const double* u, const double* v,
                 const double* w, const double* top, const double* bottom) {
     const long N = (long)nx * ny * nz, sxy = (long)nx * ny;
-    for (long i = 0; i < N; ++i) {
+    par_for(N, [=](long i) {
         const int x = (int)(i % nx), y = (int)((i % sxy) / nx), z = (int)(i / sxy);
         const long ixz = x + (long)nx * z;
         double dv;
@@ -454,23 +748,24 @@ void divergence(int nx, int ny, int nz, int n, bool channel, double* d, const do
             dv = v[i + (long)nx * (wrap(y + 1, ny) - y)] - v[i];
         }
         d[i] = n * ((u[i + (wrap(x + 1, nx) - x)] - u[i]) + dv + (w[i + sxy * (wrap(z + 1, nz) - z)] - w[i]));
-    }
+    });
 }
 
 // Gradient onto faces, src/alg/grad.h:29-44
 void gradient(const Grid& g, double* px, double* py, double* pz, const double* p) {
     const int nx = g.nx, ny = g.ny, nz = g.nz, n = g.n;
     const long N = g.ncell(), sxy = (long)nx * ny;
-    for (long i = 0; i < N; ++i) {
+    const bool channel = g.channel;
+    par_for(N, [=](long i) {
         const int x = (int)(i % nx), y = (int)((i % sxy) / nx), z = (int)(i / sxy);
         px[i] = n * (p[i] - p[i + (wrap(x - 1, nx) - x)]);
         pz[i] = n * (p[i] - p[i + sxy * (wrap(z - 1, nz) - z)]);
-        if (g.channel) {
+        if (channel) {
             if (y > 0) py[i - (long)nx * (z + 1)] = n * (p[i] - p[i - nx]);
         } else {
             py[i] = n * (p[i] - p[i + (long)nx * (wrap(y - 1, ny) - y)]);
         }
-    }
+    });
 }
 
 // Conservative centred advection, src/ns/solver.h:142-236 (channel mode,
@@ -483,56 +778,59 @@ void advection(const Grid& g, double* ua, double* va, double* wa, const double* 
     if (g.channel) {
         const long nv = (long)nx * (ny - 1) * nz, nxz = (long)nx * nz;
         vec uu(N), ww(N), uw(N), uv(nv), vw(nv), vv((long)nx * (ny - 2 > 0 ? ny - 2 : 0) * nz);
-        vec uvt(nxz), uvb(nxz), vvt(nxz), vvb(nxz), vwt(nxz), vwb(nxz);
-        double q, r;
-        for (long i = 0; i < N; ++i) {
+        vec uvt(nxz, 0.0), uvb(nxz, 0.0), vvt(nxz, 0.0), vvb(nxz, 0.0), vwt(nxz, 0.0), vwb(nxz, 0.0);
+        double *UU = uu.data(), *WW = ww.data(), *UW = uw.data(), *UV = uv.data(), *VW = vw.data(), *VV = vv.data();
+        double *VVT = vvt.data(), *VVB = vvb.data();
+        par_for(N, [=](long i) {
+            double q, r;
             const int x = (int)(i % nx), y = (int)((i % sxy) / nx), z = (int)(i / sxy);
             const long ixz = x + (long)nx * z;
             const long xm = wrap(x - 1, nx) - x;
             const long zm = sxy * (wrap(z - 1, nz) - z);
             q = 0.5 * (u[i] + u[i + xm]);
-            uu[i] = q * q;
+            UU[i] = q * q;
             if (y == 0) {
                 q = 0.5 * (v[i - (long)nx * z]);
-                vvb[ixz] = q * q;
+                VVB[ixz] = q * q;
             } else if (y == ny - 1) {
                 q = 0.5 * (v[i - (long)nx * (z + 1)]);
-                vvt[ixz] = q * q;
+                VVT[ixz] = q * q;
             } else {
                 q = 0.5 * (v[i - (long)nx * z] + v[i - (long)nx * (z + 1)]);
-                vv[i - (long)nx * (2 * z + 1)] = q * q;
+                VV[i - (long)nx * (2 * z + 1)] = q * q;
             }
             q = 0.5 * (w[i] + w[i + zm]);
-            ww[i] = q * q;
+            WW[i] = q * q;
             if (y < ny - 1) {
                 q = 0.5 * (u[i + nx] + u[i]);
                 r = 0.5 * (v[i - (long)nx * z + xm] + v[i - (long)nx * z]);
-                uv[i - (long)nx * z] = q * r;
+                UV[i - (long)nx * z] = q * r;
                 q = 0.5 * (v[i - (long)nx * z + (long)nx * (ny - 1) * (wrap(z - 1, nz) - z)] + v[i - (long)nx * z]);
                 r = 0.5 * (w[i + nx] + w[i]);
-                vw[i - (long)nx * z] = q * r;
+                VW[i - (long)nx * z] = q * r;
             }
             q = 0.5 * (u[i + zm] + u[i]);
             r = 0.5 * (w[i + xm] + w[i]);
-            uw[i] = q * r;
-        }
+            UW[i] = q * r;
+        });
         divergence(nx, ny, nz, n, true, ua, uu.data(), uv.data(), uw.data(), uvt.data(), uvb.data());
         divergence(nx, ny - 1, nz, n, true, va, uv.data(), vv.data(), vw.data(), vvt.data(), vvb.data());
         divergence(nx, ny, nz, n, true, wa, uw.data(), vw.data(), ww.data(), vwt.data(), vwb.data());
         return;
     }
     vec uu(N), vv(N), ww(N), uv(N), uw(N), vw(N);
-    for (long i = 0; i < N; ++i) {
+    double *UU = uu.data(), *VV = vv.data(), *WW = ww.data(), *UV = uv.data(), *UW = uw.data(), *VW = vw.data();
+    par_for(N, [=](long i) {
         const int x = (int)(i % nx), y = (int)((i % sxy) / nx), z = (int)(i / sxy);
         const long xm = wrap(x - 1, nx) - x, ym = (long)nx * (wrap(y - 1, ny) - y), zm = sxy * (wrap(z - 1, nz) - z);
         double q;
-        q = 0.5 * (u[i] + u[i + xm]); uu[i] = q * q;
-        q = 0.5 * (v[i] + v[i + ym]); vv[i] = q * q;
-        q = 0.5 * (w[i] + w[i + zm]); ww[i] = q * q;
-        uv[i] = (0.5 * (u[i] + u[i + ym])) * (0.5 * (v[i] + v[i + xm]));
-        uw[i] = (0.5 * (u[i] + u[i + zm])) * (0.5 * (w[i] + w[i + xm]));
-        vw[i] = (0.5 * (v[i] + v[i + zm])) * (0.5 * (w[i] + w[i + ym]));
-    }
+        q = 0.5 * (u[i] + u[i + xm]); UU[i] = q * q;
+        q = 0.5 * (v[i] + v[i + ym]); VV[i] = q * q;
+        q = 0.5 * (w[i] + w[i + zm]); WW[i] = q * q;
+        UV[i] = (0.5 * (u[i] + u[i + ym])) * (0.5 * (v[i] + v[i + xm]));
+        UW[i] = (0.5 * (u[i] + u[i + zm])) * (0.5 * (w[i] + w[i + xm]));
+        VW[i] = (0.5 * (v[i] + v[i + zm])) * (0.5 * (w[i] + w[i + ym]));
+    });
     // each adv = n * (F1[+x] - F1 + F2[+y] - F2 + F3[+z] - F3), the periodic div
     divergence(nx, ny, nz, n, false, ua, uu.data(), uv.data(), uw.data(), nullptr, nullptr);
     divergence(nx, ny, nz, n, false, va, uv.data(), vv.data(), vw.data(), nullptr, nullptr);
@@ -549,7 +847,7 @@ Op helm_op(const Grid& g, int comp, double s) {
 // Wall right-hand side of the u/w Helmholtz rows, src/ns/helmholtz.h:177-196
 void helm_boundary_cell(const Grid& g, double scale, vec& b, const double* top, const double* bottom) {
     const int nx = g.nx, ny = g.ny, nz = g.nz, n = g.n;
-    b.assign(g.ncell(), 0.0);
+    par_fill(b, g.ncell(), 0.0);
     for (long i = 0; i < (long)nx * nz; ++i) {
         const int x = (int)(i % nx), z = (int)(i / nx);
         if (ny > 1) {
@@ -582,18 +880,20 @@ struct NS {
     void project() {
         const long N = g.ncell(), nxz = (long)g.nx * g.nz;
         vec zero(nxz, 0.0);
-        phidt.assign(N, 0.0);
+        par_fill(phidt, N, 0.0);
         divergence(g.nx, g.ny, g.nz, g.n, g.channel, phidt.data(), u.data(), v.data(), w.data(), zero.data(), zero.data());
         int cyc = 0;
         if (mg.solve(phidt, &cyc) != 0) status = 3;
         mg_cycles += cyc;
-        phx.assign(N, 0.0);
-        phy.assign(g.nv(), 0.0);
-        phz.assign(N, 0.0);
+        par_fill(phx, N, 0.0);
+        par_fill(phy, g.nv(), 0.0);
+        par_fill(phz, N, 0.0);
         gradient(g, phx.data(), phy.data(), phz.data(), phidt.data());
-        for (long i = 0; i < N; ++i) u[i] -= phx[i];
-        for (long i = 0; i < g.nv(); ++i) v[i] -= phy[i];
-        for (long i = 0; i < N; ++i) w[i] -= phz[i];
+        double *U = u.data(), *V = v.data(), *W = w.data();
+        const double *PX = phx.data(), *PY = phy.data(), *PZ = phz.data();
+        par_for(N, [=](long i) { U[i] -= PX[i]; });
+        par_for(g.nv(), [=](long i) { V[i] -= PY[i]; });
+        par_for(N, [=](long i) { W[i] -= PZ[i]; });
     }
 
     // src/ns/projection.h:75-122 — including its two index slips (loop bound
@@ -635,27 +935,30 @@ struct NS {
     // src/ns/solver.h:90-140
     void step(double* ut, double* ub, double* wt, double* wb, const double* fx, const double* fy, const double* fz) {
         const long N = g.ncell(), NV = g.nv();
-        ua.assign(N, 0.0);
-        va.assign(NV, 0.0);
-        wa.assign(N, 0.0);
+        par_fill(ua, N, 0.0);
+        par_fill(va, NV, 0.0);
+        par_fill(wa, N, 0.0);
         advection(g, ua.data(), va.data(), wa.data(), u.data(), v.data(), w.data());
         const double sm = mu * dt / (2 * rho), ss = -mu * dt / (2 * rho);
         vec rx(N), ry(NV), rz(N);
         if (!half) {
-            u_old = u; v_old = v; w_old = w;
+            par_copy(u_old, u); par_copy(v_old, v); par_copy(w_old, w);
             wall_boundary(ut, ub, wt, wb);
             vec bu, bw;
             if (g.channel) {
                 helm_boundary_cell(g, ss, bu, ut, ub);
                 helm_boundary_cell(g, ss, bw, wt, wb);
             } else {
-                bu.assign(N, 0.0);
-                bw.assign(N, 0.0);
+                par_fill(bu, N, 0.0);
+                par_fill(bw, N, 0.0);
             }
-            const double h = dt / 2;
-            for (long i = 0; i < N; ++i) rx[i] = (u_old[i] + -1 * bu[i]) + h * (1 / rho * fx[i] - ua[i]);
-            for (long i = 0; i < NV; ++i) ry[i] = v_old[i] + +(h * (1 / rho * fy[i] - va[i]));
-            for (long i = 0; i < N; ++i) rz[i] = (w_old[i] + -1 * bw[i]) + h * (1 / rho * fz[i] - wa[i]);
+            const double h = dt / 2, rho_ = rho;
+            double *RX = rx.data(), *RY = ry.data(), *RZ = rz.data();
+            const double *UO = u_old.data(), *VO = v_old.data(), *WO = w_old.data(), *BU = bu.data(), *BW = bw.data();
+            const double *UA = ua.data(), *VA = va.data(), *WA = wa.data();
+            par_for(N, [=](long i) { RX[i] = (UO[i] + -1 * BU[i]) + h * (1 / rho_ * fx[i] - UA[i]); });
+            par_for(NV, [=](long i) { RY[i] = VO[i] + +(h * (1 / rho_ * fy[i] - VA[i])); });
+            par_for(N, [=](long i) { RZ[i] = (WO[i] + -1 * BW[i]) + h * (1 / rho_ * fz[i] - WA[i]); });
         } else {
             wall_boundary(ut, ub, wt, wb);
             vec bum, bus, bwm, bws, au, av, aw;
@@ -665,14 +968,19 @@ struct NS {
                 helm_boundary_cell(g, sm, bwm, wt, wb);
                 helm_boundary_cell(g, ss, bws, wt, wb);
             } else {
-                bum.assign(N, 0.0); bus.assign(N, 0.0); bwm.assign(N, 0.0); bws.assign(N, 0.0);
+                par_fill(bum, N, 0.0); par_fill(bus, N, 0.0); par_fill(bwm, N, 0.0); par_fill(bws, N, 0.0);
             }
             spmv(helm_op(g, 0, sm), au, u_old);
             spmv(helm_op(g, 1, sm), av, v_old);
             spmv(helm_op(g, 2, sm), aw, w_old);
-            for (long i = 0; i < N; ++i) rx[i] = (au[i] + (bum[i] - bus[i])) + dt * (1 / rho * fx[i] - ua[i]);
-            for (long i = 0; i < NV; ++i) ry[i] = av[i] + +(dt * (1 / rho * fy[i] - va[i]));
-            for (long i = 0; i < N; ++i) rz[i] = (aw[i] + (bwm[i] - bws[i])) + dt * (1 / rho * fz[i] - wa[i]);
+            const double dt_ = dt, rho_ = rho;
+            double *RX = rx.data(), *RY = ry.data(), *RZ = rz.data();
+            const double *AU = au.data(), *AV = av.data(), *AW = aw.data(), *BUM = bum.data(), *BUS = bus.data(),
+                         *BWM = bwm.data(), *BWS = bws.data();
+            const double *UA = ua.data(), *VA = va.data(), *WA = wa.data();
+            par_for(N, [=](long i) { RX[i] = (AU[i] + (BUM[i] - BUS[i])) + dt_ * (1 / rho_ * fx[i] - UA[i]); });
+            par_for(NV, [=](long i) { RY[i] = AV[i] + +(dt_ * (1 / rho_ * fy[i] - VA[i])); });
+            par_for(N, [=](long i) { RZ[i] = (AW[i] + (BWM[i] - BWS[i])) + dt_ * (1 / rho_ * fz[i] - WA[i]); });
         }
         helm_solve(0, u, rx);
         helm_solve(1, v, ry);
@@ -746,37 +1054,55 @@ void spread(const Grid& g, int comp, double* f, long M, const double* X, const d
     int ext[3];
     face_dims(g, comp, ext);
     const long NF = (long)ext[0] * ext[1] * ext[2];
-    for (long i = 0; i < NF; ++i) f[i] = 0.0;
+    const long plane = (long)ext[0] * ext[1];
     const int n = g.n;
-    for (long k = 0; k < M; ++k) {
-        const double* xk = X + 3 * k;
-        long base[3];
-        double wgt[3][4];
-        for (int a = 0; a < 3; ++a) {
-            const double off = face_offset(g, comp, a);
-            base[a] = first_face(xk[a] * n, off);
-            for (int m = 0; m < 4; ++m) {
-                const double pos = ((double)(base[a] + m) + off) / n;
-                wgt[a][m] = delta1(xk[a] - pos, n);
+    // Faces split by z slab; every slab walks the markers in index order, so
+    // each face receives its terms in the order of the one-thread loop.
+    par_range(ext[2], NF >= (1L << 15) ? 1 : ext[2], [&](long zlo, long zhi) {
+        for (long i = zlo * plane; i < zhi * plane; ++i) f[i] = 0.0;
+        for (long k = 0; k < M; ++k) {
+            const double* xk = X + 3 * k;
+            long base[3];
+            double wgt[3][4];
+            // z taps first: skip markers whose four z faces all lie outside the slab
+            {
+                const double offz = face_offset(g, comp, 2);
+                const long bz = g.nz == 1 ? 0 : first_face(xk[2] * n, offz);
+                bool any = false;
+                for (int mz = 0; mz < 4; ++mz) {
+                    const long iz = wrap((int)(bz + mz), ext[2]);
+                    any = any || (iz >= zlo && iz < zhi);
+                }
+                if (!any) continue;
+            }
+            for (int a = 0; a < 3; ++a) {
+                const double off = face_offset(g, comp, a);
+                base[a] = first_face(xk[a] * n, off);
+                for (int m = 0; m < 4; ++m) {
+                    const double pos = ((double)(base[a] + m) + off) / n;
+                    wgt[a][m] = delta1(xk[a] - pos, n);
+                }
+            }
+            flat_z(g, base, wgt);
+            const double amp = (vol ? vol[k] : 1.0) * F[k];
+            for (int mz = 0; mz < 4; ++mz) {
+                const long iz = wrap((int)(base[2] + mz), ext[2]);
+                if (iz < zlo || iz >= zhi) continue;
+                for (int my = 0; my < 4; ++my)
+                    for (int mx = 0; mx < 4; ++mx) {
+                        long ix = base[0] + mx, iy = base[1] + my;
+                        ix = wrap((int)ix, ext[0]);
+                        if (g.channel) {
+                            if (iy < 0 || iy >= ext[1]) continue;
+                        } else {
+                            iy = wrap((int)iy, ext[1]);
+                        }
+                        const double wgt3 = wgt[0][mx] * wgt[1][my] * wgt[2][mz];
+                        f[ix + (long)ext[0] * (iy + (long)ext[1] * iz)] += wgt3 * amp;
+                    }
             }
         }
-        flat_z(g, base, wgt);
-        const double amp = (vol ? vol[k] : 1.0) * F[k];
-        for (int mz = 0; mz < 4; ++mz)
-            for (int my = 0; my < 4; ++my)
-                for (int mx = 0; mx < 4; ++mx) {
-                    long ix = base[0] + mx, iy = base[1] + my, iz = base[2] + mz;
-                    ix = wrap((int)ix, ext[0]);
-                    iz = wrap((int)iz, ext[2]);
-                    if (g.channel) {
-                        if (iy < 0 || iy >= ext[1]) continue;
-                    } else {
-                        iy = wrap((int)iy, ext[1]);
-                    }
-                    const double wgt3 = wgt[0][mx] * wgt[1][my] * wgt[2][mz];
-                    f[ix + (long)ext[0] * (iy + (long)ext[1] * iz)] += wgt3 * amp;
-                }
-    }
+    });
 }
 
 // Interpolation: U_k = sum over 64 faces of phi^3 * h^3 * u(face),
@@ -786,7 +1112,8 @@ void interp(const Grid& g, int comp, double* U, long M, const double* X, const d
     face_dims(g, comp, ext);
     const int n = g.n;
     const double vol = g.nz == 1 ? 1. / ((double)n * n) : 1. / ((double)n * n * n);
-    for (long k = 0; k < M; ++k) {
+    par_range(M, 4096, [&](long k0, long k1) {
+    for (long k = k0; k < k1; ++k) {
         const double* xk = X + 3 * k;
         long base[3];
         double wgt[3][4];
@@ -814,6 +1141,7 @@ void interp(const Grid& g, int comp, double* U, long M, const double* X, const d
                 }
         U[k] = acc;
     }
+    });
 }
 
 // Linear zero-rest-length springs between listed neighbours (no reference
@@ -837,7 +1165,16 @@ void springs(long M, const double* X, const int* nstart, const int* nidx, double
 // ---------------------------------------------------------------------------
 extern "C" {
 
-int orc_version() { return 1; }
+int orc_version() { return 2; }
+
+// Threads of the parallel passes (1: one thread, the default). Results do not
+// depend on the count.
+void orc_set_threads(int t) { g_threads = t < 1 ? 1 : t; }
+int orc_get_threads() { return g_threads; }
+
+// 0 routes every operator row through the generic row builder (for checking
+// that the direct interior form gives the same bits).
+void orc_set_fast_rows(int on) { g_fast_rows = on != 0; }
 
 void orc_div(const int* dims, double* d, const double* u, const double* v, const double* w, const double* top,
              const double* bottom) {
