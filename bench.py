@@ -59,6 +59,8 @@ def parse():
                     help="mixed form: relative reduction of each FP32 inner Helmholtz solve (0: the library default)")
     ap.add_argument("--ib-fp32", type=int, default=0,
                     help="mixed form: bit 0 FP32 spreading, bit 1 FP32 interpolation (0: both FP64, the default)")
+    ap.add_argument("--err-steps", type=int, default=100,
+                    help="IB steps of the untimed mixed-vs-FP64 error run (the configuration's 100; 0 skips it)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", choices=["ib", "mg", "adjoint", "large"], default="ib",
@@ -73,8 +75,8 @@ def parse():
     ap.add_argument("--adj-every", type=int, default=10)
     ap.add_argument("--adj-dirs", type=int, default=16)
     ap.add_argument("--adj-tol", type=float, default=1e-12)
-    ap.add_argument("--cpu-sample-n", type=int, default=64,
-                    help="grid of the CPU sample (the workload at reduced resolution, scaled by the cell count)")
+    ap.add_argument("--ref-budget-s", type=float, default=200.0,
+                    help="reference arm: timed CPU steps stop once the next would pass this many seconds")
     return ap.parse_args()
 
 
@@ -198,50 +200,69 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(use), "samples_in_region": len(inside)}
 
 
-def cpu_sample(args, kind_note=""):
-    """One IB step of the workload at reduced resolution on the CPU oracle
-    (single thread), scaled to the full grid by the cell count. Returns
-    (steps_per_s_scaled, seconds, description)."""
+def host_cpu():
+    """(model name, logical cores) of the host."""
+    model = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    return model or "unknown", os.cpu_count() or 1
+
+
+def cpu_run(args, warmup, steps, budget_s=None):
+    """The reference path on the host cores at the full workload: the CPU
+    oracle (a restatement of the reference's algorithm in FP64; the reference
+    has no periodic mode and its headers are not present on the GPU host) on
+    all host threads. Its threaded passes give the one-thread bits. Runs
+    `warmup` untimed IB steps, then up to `steps` timed ones, stopping early
+    once the next step would overrun `budget_s` of timed work. Returns
+    (seconds per step, steps timed, warm-up steps, threads, description)."""
     from oracle import pyoracle as po
-    ns = args.cpu_sample_n
-    scale_cells = (args.n / ns) ** 3
-    per = max(200, int(args.per_shell * (ns / args.n) ** 2))
-    X, nstart, nidx, u, v, w = workload(ns, args.shells, per, args.radius, args.min_sep)
-    g = po.Grid(ns, ns, ns, ns, channel=False)
+    model, cores = host_cpu()
+    po.set_threads(cores)
+    X, nstart, nidx, u, v, w = workload(args.n, args.shells, args.per_shell, args.radius, args.min_sep)
+    g = po.Grid(args.n, args.n, args.n, args.n, channel=False)
     t0 = time.perf_counter()
     s = po.NSSolver(g, args.mu, 1.0, args.dt, args.tol, u, v, w)
-    t1 = time.perf_counter()
-    Xo, st = s.ib_step(X, nstart, nidx, 0.5)
-    t2 = time.perf_counter()
-    sec = t2 - t1
-    desc = (f"1 IB step of the workload at {ns}^3 with {args.shells}x{per} markers on 1 thread of the host CPU "
-            f"({sec:.2f} s), time scaled x{scale_cells:.0f} to {args.n}^3 cells")
-    return 1.0 / (sec * scale_cells), sec, desc
+    setup = time.perf_counter() - t0
+    for _ in range(warmup):
+        X, st = s.ib_step(X, nstart, nidx, 0.5)
+    times = []
+    while len(times) < steps:
+        if budget_s is not None and times and sum(times) + max(times) > budget_s:
+            break
+        t0 = time.perf_counter()
+        X, st = s.ib_step(X, nstart, nidx, 0.5)
+        times.append(time.perf_counter() - t0)
+    sec = float(np.mean(times))
+    desc = (f"{len(times)} timed IB step(s) of the full workload ({args.n}^3, {args.shells * args.per_shell} markers, "
+            f"FP64) after {warmup} untimed, on {cores} threads of the host CPU ({model}); {sec:.2f} s per step, "
+            f"solver set-up {setup:.1f} s")
+    return sec, len(times), warmup, cores, desc
 
 
 def run_reference(args, rank, world):
-    """The reference path timed on the host cores: the CPU oracle (a port of
-    the reference's algorithm; the reference headers are not present on the
-    GPU host), bounded sample per step."""
+    """The reference path timed on the host cores (see cpu_run): the same
+    workload, metric and unit as the GPU arm; rank 0 only."""
     if rank != 0:
         return
-    vals = []
-    for _ in range(max(0, min(args.warmup, 1))):
-        cpu_sample(args)
-    for _ in range(args.steps):
-        v, sec, desc = cpu_sample(args)
-        vals.append(sec)
-    sec = float(np.mean(vals))
-    scale_cells = (args.n / args.cpu_sample_n) ** 3
-    value = 1.0 / (sec * scale_cells)
+    sec, k, w, cores, desc = cpu_run(args, args.warmup, args.steps, budget_s=args.ref_budget_s)
+    value = 1.0 / sec
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
-        "steps": args.steps, "warmup": min(args.warmup, 1), "ms_per_step": 1000.0 / value,
+        "steps": k, "warmup": w, "ms_per_step": 1000.0 * sec,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_dict(args),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": desc},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if k < args.steps:
+        line["steps_requested"] = args.steps
     print(json.dumps(line), flush=True)
 
 
@@ -584,15 +605,36 @@ def main():
                  "gpu_launches": int(l64w), "proj_start": "warm"}
         sv64.close()
 
-    errors = None
+    errors = errors_timed = None
     if fp64 is not None:
-        errors = {"velocity": max(rel_err(a, b) for a, b in zip(uh, u64)),
-                  "pressure": pressure_err(ph, p64, args.n, args.mu, args.dt),
-                  "marker_displacement": rel_err(Xh - X, X64 - X),
-                  "marker_position_max_abs": float(np.max(np.abs(Xh - X64))),
-                  "steps": args.warmup + args.steps}
+        errors_timed = {"velocity": max(rel_err(a, b) for a, b in zip(uh, u64)),
+                        "pressure": pressure_err(ph, p64, args.n, args.mu, args.dt),
+                        "marker_displacement": rel_err(Xh - X, X64 - X),
+                        "marker_position_max_abs": float(np.max(np.abs(Xh - X64))),
+                        "steps": args.warmup + args.steps}
         fp64["speedup_of_headline"] = value / fp64["value"]
         fp64w["speedup_of_headline"] = value / fp64w["value"]
+        # the configuration's error statement: both forms from the same state
+        # over --err-steps IB steps (untimed), the FP64 form with the
+        # reference's projections from zero
+        if args.err_steps > 0:
+            ends = {}
+            for name, prec, start in (("mixed", headline, 0), ("fp64", capi.FP64, capi.START_ZERO)):
+                with capi.Solver(args.n, mu=args.mu, rho=1.0, dt=args.dt, tol=args.tol, k_spring=0.5, precision=prec,
+                                 proj_start=start, inner_tol=args.inner_tol,
+                                 ib_fp32=args.ib_fp32 if prec == capi.MIXED else 0) as se:
+                    se.set_velocity(*state[3:])
+                    se.project()
+                    se.set_markers(state[0], state[1], state[2])
+                    se.ib_step(args.err_steps)
+                    ends[name] = (se.get_velocity(), se.get_pressure(), se.get_markers())
+            (um, pm, Xm), (uf, pf, Xf) = ends["mixed"], ends["fp64"]
+            errors = {"velocity": max(rel_err(a, b) for a, b in zip(um, uf)),
+                      "pressure": pressure_err(pm, pf, args.n, args.mu, args.dt),
+                      "marker_displacement": rel_err(Xm - X, Xf - X),
+                      "marker_position_max_abs": float(np.max(np.abs(Xm - Xf))),
+                      "steps": args.err_steps,
+                      "yardstick": "the FP64 form, pinned to the oracle at this workload (2 IB steps, tol 1e-12)"}
 
     # ---- per-kernel durations over profiled steps (events on the solver's stream)
     peak, peak_kind = measured_peaks()
@@ -624,8 +666,8 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cv, csec, desc = cpu_sample(args)
-        cpu = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port", "sample": desc}
+        csec, ck, cw, cores, desc = cpu_run(args, 1, 1)
+        cpu = {"value": 1.0 / csec, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
 
     if rank == 0:
         line = {
@@ -635,6 +677,7 @@ def main():
             "data": "synthetic (seeded shells and solenoidal field)", "config": config_dict(args),
             "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clocks,
             "fp64_form": fp64, "fp64_form_warm": fp64w, "errors_vs_fp64": errors,
+            "errors_vs_fp64_timed_steps": errors_timed,
             "solver": {"cg_iters_per_step": st["cg_iters"] / max(1, st["ib_steps"]),
                        "mg_cycles_per_step": st["mg_cycles"] / max(1, st["ib_steps"]),
                        "outer_iters_per_step": st["outer_iters"] / max(1, st["ib_steps"]),

@@ -175,6 +175,13 @@ def gs_sweep(g, x, b):
     return x
 
 
+def rb_sweep(g, x, b):
+    """One red-black Gauss-Seidel sweep of the pressure Laplacian (red: x+y+z even, first)."""
+    x = x.copy()
+    lib().orc_rb_sweep(g.dims, _p(x), _p(b))
+    return x
+
+
 def restrict(g, fine):
     c = np.zeros(g.ncell // (4 if g.nz == 1 else 8))
     lib().orc_restrict(g.dims, _p(c), _p(fine))

@@ -433,6 +433,29 @@ void gs_sweep(const Op& op, vec& x, const vec& b) {
     for (auto& t : th) t.join();
 }
 
+// One red-black Gauss–Seidel sweep with the reference's row update
+// (src/alg/smooth.h:35-51): the red cells (x + y + z even) in index order,
+// then the black cells (x + y + z odd). The reference smooths
+// lexicographically; this is the ordering the multigrid of the CUDA path
+// uses, restated here with the reference's row arithmetic so that one sweep
+// of that path has an independent check.
+void rb_sweep(const Op& op, vec& x, const vec& b) {
+    const long N = op_size(op);
+    Row r;
+    for (int colour = 0; colour < 2; ++colour)
+        for (long i = 0; i < N; ++i) {
+            const long cx = i % op.nx, cy = (i / op.nx) % op.ny, cz = i / ((long)op.nx * op.ny);
+            if ((cx + cy + cz) % 2 != colour) continue;
+            make_row(op, i, r);
+            double value = 0.0, diagonal = 0.0;
+            for (int k = 0; k < r.cnt; ++k) {
+                if (r.col[k] == i) { diagonal = r.val[k]; continue; }
+                value += r.val[k] * x[r.col[k]];
+            }
+            x[i] = (b[i] - value) / diagonal;
+        }
+}
+
 double dot(const vec& a, const vec& b) {
     double s = 0.0;
     for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
@@ -1214,6 +1237,14 @@ void orc_gs_sweep(const int* dims, double* x, const double* b) {
     Op A{OP_LAPLACIAN, g.nx, g.ny, g.nz, g.n, g.channel, 0.0};
     vec xv(x, x + g.ncell()), bv(b, b + g.ncell());
     gs_sweep(A, xv, bv);
+    std::memcpy(x, xv.data(), xv.size() * sizeof(double));
+}
+
+void orc_rb_sweep(const int* dims, double* x, const double* b) {
+    Grid g = make_grid(dims);
+    Op A{OP_LAPLACIAN, g.nx, g.ny, g.nz, g.n, g.channel, 0.0};
+    vec xv(x, x + g.ncell()), bv(b, b + g.ncell());
+    rb_sweep(A, xv, bv);
     std::memcpy(x, xv.data(), xv.size() * sizeof(double));
 }
 

@@ -55,6 +55,21 @@ def test_single_operators_channel(golden):
         assert rel(x, d["cg_x"]) < TOL
 
 
+@pytest.mark.parametrize("channel", [False, True])
+def test_rb_smoother_one_sweep_against_oracle(channel):
+    """One FP64 red-black Gauss-Seidel sweep of the multigrid smoother
+    (afmib_smooth) against the oracle's red-black restatement with the
+    reference's row update (src/alg/smooth.h:35-51), 16^3."""
+    n = 16
+    g = po.Grid(n, n, n, n, channel=channel)
+    rng = np.random.default_rng(21)
+    x0, b = rng.standard_normal(g.ncell), rng.standard_normal(g.ncell)
+    ref = po.rb_sweep(g, x0, b)
+    with capi.Solver(n, bc=capi.BC_CHANNEL if channel else capi.BC_PERIODIC, tol=1e-12) as sv:
+        out = sv.smooth(x0, b)
+    assert rel(out, ref) < OPS_TOL
+
+
 def test_restriction_known_answer(golden):
     d = golden("restr_test")
     with capi.Solver(2, bc=capi.BC_CHANNEL) as sv:

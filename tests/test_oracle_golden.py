@@ -111,3 +111,67 @@ def test_live_reference_periodic_images_documented():
     # total force is conserved by the image-correct sum (partition of unity)
     h3 = 1.0 / 16 ** 3
     np.testing.assert_allclose(mine[: g.ncell].sum() * h3, F[0].sum(), rtol=1e-12)
+
+
+def test_channel_icosphere_128_against_reference_digest():
+    """The restatement at the 128^3 icosphere configuration (20,480 markers,
+    channel: the reference's own domain) over 4 IB steps against the digest
+    of the reference compiled unchanged (tests/golden/make_golden_c2.py):
+    velocity to 1e-14 of its largest magnitude at 4096 seeded cells per
+    component (spreading sums in kd-tree order there), pressure after its
+    null-space constant, markers bit for bit. Runs on all host cores; the
+    oracle's threaded passes give its one-thread bits."""
+    import importlib.util
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    spec = importlib.util.spec_from_file_location("make_golden_c2", os.path.join(path, "make_golden_c2.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    d = np.load(os.path.join(path, "c2_channel_128_ref_digest.npz"))
+    n = int(d["n"])
+    X0, nstart, nidx, u, vp, w = gen.inputs(n)
+    v = gen.channel_v(vp, n)
+    po.set_threads(os.cpu_count() or 1)
+    try:
+        g = po.Grid(n, n, n, n, channel=True)
+        s = po.NSSolver(g, float(d["mu"]), float(d["rho"]), float(d["dt"]), float(d["tol"]), u, v, w, maxit=100000)
+        X = X0.copy()
+        for _ in range(int(d["steps"])):
+            X, st = s.ib_step(X, nstart, nidx, float(d["k"]))
+            assert st == 0
+        ru, rv, rw, rp = s.get()
+    finally:
+        po.set_threads(1)
+    for name, a in (("u", ru), ("v", rv), ("w", rw)):
+        assert np.max(np.abs(a[d[name + "_idx"]] - d[name + "_val"])) <= 1e-14 * float(d[name + "_max"]), name
+    h1 = po.helm_apply(g, 0, -float(d["mu"]) * float(d["dt"]) / 2, np.ones(g.ncell))
+    idx = d["p_idx"]
+    dlt = rp[idx] - d["p_val"]
+    c = float(dlt @ h1[idx] / (h1[idx] @ h1[idx]))
+    assert np.max(np.abs(dlt - c * h1[idx])) <= 1e-13 * float(d["p_max"])
+    assert np.array_equal(X, d["X"])
+
+
+@pytest.mark.parametrize("channel", [False, True])
+def test_red_black_sweep_restatement(channel):
+    """The red-black sweep of the oracle (the ordering the CUDA multigrid
+    uses, with the reference's row update src/alg/smooth.h:35-51): after it
+    every black cell satisfies its row exactly (it was updated last, from the
+    final red values), and the red cells equal the row update from the
+    incoming black values."""
+    n = 8
+    g = po.Grid(n, n, n, n, channel=channel)
+    rng = np.random.default_rng(3)
+    x0, b = rng.standard_normal(g.ncell), rng.standard_normal(g.ncell)
+    x = po.rb_sweep(g, x0, b)
+    i = np.arange(g.ncell)
+    cx, cy, cz = i % n, (i // n) % n, i // (n * n)
+    black = (cx + cy + cz) % 2 == 1
+    r = b - po.lap_apply(g, x)
+    assert np.max(np.abs(r[black])) <= 1e-12 * np.max(np.abs(b)) * n * n
+    # the red cells: one Jacobi-style update of the red rows from the old black values
+    red = ~black
+    xr = x0.copy()
+    xr[red] = x[red]
+    rr = b - po.lap_apply(g, xr)
+    assert np.max(np.abs(rr[red])) <= 1e-12 * np.max(np.abs(b)) * n * n
