@@ -207,6 +207,14 @@ void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s, in
 // fine += P coarse (trilinear), src/mg/solver.h:71-151 and :211-212.
 template <typename T>
 void launch_prolong_add(const Dims& d, T* fine, const T* coarse, cudaStream_t s, int rev = 0);
+// coarse_b = restriction of (b - L x), coarse_x = 0, in one pass (the
+// residual stays in shared memory); for the levels resid_restrict_fused_ok
+// takes (3D power-of-two levels with nx >= 256 by default;
+// AFMIB_RESID_RESTRICT=0 keeps the two kernels)
+bool resid_restrict_fused_ok(const Dims& d);
+template <typename T>
+void launch_resid_restrict(const Dims& d, T* coarse_b, T* coarse_x, const T* x, const T* b, cudaStream_t s,
+                           int rev = 0);
 // Prolongation that assigns (for the op-level API).
 template <typename T>
 void launch_prolong_assign(const Dims& d, T* fine, const T* coarse, cudaStream_t s);

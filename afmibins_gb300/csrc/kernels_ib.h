@@ -68,6 +68,11 @@ template <typename T, typename TF>
 void launch_interp(const Dims& d, int M, const int* perm, MarkerW<T> mw, const TF* u, const TF* v, const TF* w, double* U,
                    cudaStream_t s);
 
+// The FP64 interpolation in double-float on the FP32 pipe (axis-by-axis sums,
+// relative error a few units of 2^-46 of the largest term): the mixed form.
+void launch_interp_dfl(const Dims& d, int M, const int* perm, MarkerW<double> mw, const double* u, const double* v,
+                       const double* w, double* U, cudaStream_t s);
+
 void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, double c, cudaStream_t s);
 
 }  // namespace afmib

@@ -764,6 +764,89 @@ __device__ __forceinline__ void prolong_cell2(const Dims& d, const Ix2& I, T* fi
     }
 }
 
+// Fine-level residual fused with the full-weighting restriction and the
+// zeroing of the coarse iterate. A block takes RR_T x RR_T coarse columns
+// and RR_CZ coarse planes; r = b - L x of its fine tile (2 RR_T + 2 cells a
+// side: the taps reach one fine cell beyond the tile's own) is formed in
+// shared memory, one fine plane at a time, in a ring of the four planes the
+// current coarse plane reads, and every coarse cell sums its 64 taps from the
+// ring. The residual is k_residual_z2's expression and the taps are
+// restrict_cell2's in its order, so the coarse right-hand side equals the two
+// kernels' bit for bit, and the fine residual is never written to memory.
+constexpr int RR_T = 16, RR_F = 2 * RR_T + 2, RR_THREADS = RR_T * RR_T;
+
+template <typename T, int RR_CZ>
+__global__ void __launch_bounds__(RR_THREADS) k_resid_restrict2(Dims d, T* __restrict__ cb, T* __restrict__ cx,
+                                                               const T* __restrict__ xv, const T* __restrict__ b,
+                                                               int rev) {
+    __shared__ T ring[4][RR_F * RR_F];
+    const Ix2 I(d);
+    const uint3 B = block_at(rev);
+    const int xc0 = B.x * RR_T, yc0 = B.y * RR_T, zc0 = B.z * RR_CZ;
+    const int xf0 = 2 * xc0 - 1, yf0 = 2 * yc0 - 1;  // fine cell of tile column / row 0 (unwrapped)
+    const T off = T(d.n) * T(d.n);
+    const int tid = threadIdx.x;
+    // residual of fine plane zf (unwrapped) into its ring slot; channel rows
+    // beyond the walls are never tapped (the taps clamp) and stay unset
+    auto fill = [&](int zf) {
+        T* dst = ring[zf & 3];
+        const int z = zf & I.mz;
+        for (int e = tid; e < RR_F * RR_F; e += RR_THREADS) {
+            const int jy = e / RR_F, jx = e - jy * RR_F;
+            int y = yf0 + jy;
+            if (d.channel) {
+                if (y < 0 || y >= d.ny) continue;
+            } else {
+                y &= I.my;
+            }
+            const int x = (xf0 + jx) & I.mx;
+            T S, c;
+            lap_row2(d, I, xv, x, y, z, S, c);
+            const int i = I.at(x, y, z);
+            dst[e] = b[i] - off * (S - c * xv[i]);
+        }
+    };
+    const int cxl = tid % RR_T, cyl = tid / RR_T;
+    const int xc = xc0 + cxl, yc = yc0 + cyl;
+    int col[4], row[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int dd = k - 2;
+        col[k] = 2 * cxl + k;  // fine x = 2 xc + 1 + dd
+        int yy;
+        if (d.channel) {
+            const int ycf = 2 * yc + 1;
+            yy = ycf + (dd > -ycf ? dd : -ycf);
+            yy = yy < d.ny - 1 ? yy : d.ny - 1;
+        } else {
+            yy = 2 * yc + 1 + dd;  // unwrapped: the ring holds the wrapped values in order
+        }
+        row[k] = yy - yf0;
+    }
+    const T wgt[4] = {T(1), T(3), T(3), T(1)};
+    fill(2 * zc0 - 1);
+    fill(2 * zc0);
+    for (int zc = zc0; zc < zc0 + RR_CZ; ++zc) {
+        fill(2 * zc + 1);
+        fill(2 * zc + 2);
+        __syncthreads();
+        T acc = T(0);
+#pragma unroll
+        for (int kz = 0; kz < 4; ++kz) {
+            const T* pl = ring[(2 * zc - 1 + kz) & 3];
+#pragma unroll
+            for (int ky = 0; ky < 4; ++ky)
+#pragma unroll
+                for (int kx = 0; kx < 4; ++kx)
+                    acc += (wgt[kx] * wgt[ky] * wgt[kz] / T(512)) * pl[row[ky] * RR_F + col[kx]];
+        }
+        const int o = xc | (yc << (I.lx - 1)) | (zc << (I.lxy - 2));
+        cb[o] = acc;
+        cx[o] = T(0);
+        __syncthreads();  // the next fills overwrite the two oldest planes
+    }
+}
+
 template <typename T, bool ADD>
 __global__ void k_prolong2(Dims d, T* __restrict__ fine, const T* __restrict__ coarse, int rev) {
     const Ix2 I(d);
@@ -1186,6 +1269,30 @@ void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s, in
     if (d.nz > 1 && d.nx >= 2 && d.ny >= 2 && ix2_ok(d)) k_restrict2<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine, rev);
     else k_restrict<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine);
 }
+// Levels with nx >= AFMIB_RESID_RESTRICT_MIN_NX (default 256) take the fused
+// kernel: on smaller levels its grid (2 RR_T x 2 RR_T fine columns per block)
+// leaves SMs idle. Both switches are read at every call, so that a test can
+// compare the two paths in one process.
+bool resid_restrict_fused_ok(const Dims& d) {
+    const char* e = std::getenv("AFMIB_RESID_RESTRICT");
+    if (e && e[0] == '0') return false;
+    const char* m = std::getenv("AFMIB_RESID_RESTRICT_MIN_NX");
+    const int min_nx = m ? std::atoi(m) : 256;
+    return d.nz > 1 && d.nx >= min_nx && d.nx >= 2 * RR_T && d.ny >= 2 * RR_T && d.nz >= 4 && ix2_ok(d);
+}
+
+// coarse planes per block: 8 where that still gives two blocks per SM, else 2
+template <typename T>
+void launch_resid_restrict(const Dims& d, T* coarse_b, T* coarse_x, const T* x, const T* b, cudaStream_t s, int rev) {
+    const int cols = (d.nx / 2 / RR_T) * (d.ny / 2 / RR_T), cz = d.nz / 2;
+    if (cz % 8 == 0 && cols * (cz / 8) >= 2 * 152)
+        k_resid_restrict2<T, 8><<<dim3(d.nx / 2 / RR_T, d.ny / 2 / RR_T, cz / 8), RR_THREADS, 0, s>>>(
+            d, coarse_b, coarse_x, x, b, rev);
+    else
+        k_resid_restrict2<T, 2><<<dim3(d.nx / 2 / RR_T, d.ny / 2 / RR_T, cz / 2), RR_THREADS, 0, s>>>(
+            d, coarse_b, coarse_x, x, b, rev);
+}
+
 template <typename T>
 void launch_prolong_add(const Dims& d, T* fine, const T* coarse, cudaStream_t s, int rev) {
     dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz == 1 ? 1 : d.nz / 2);
@@ -1303,6 +1410,7 @@ void launch_coarse_solve(const Dims& d, T* x, T* b, T* r, T* p, T* q, double tol
     template void launch_rbgs_pipe<T>(const Dims&, const PipeCfg&, const T*, T*, const T*, int*, cudaStream_t); \
     template void launch_restrict<T>(const Dims&, T*, const T*, cudaStream_t, int);                         \
     template void launch_prolong_add<T>(const Dims&, T*, const T*, cudaStream_t, int);                      \
+    template void launch_resid_restrict<T>(const Dims&, T*, T*, const T*, const T*, cudaStream_t, int);      \
     template void launch_prolong_assign<T>(const Dims&, T*, const T*, cudaStream_t);                     \
     template void launch_coarse_solve<T>(const Dims&, T*, T*, T*, T*, T*, double, int, int*, cudaStream_t);    \
     template void launch_vcycle_tail<T>(const TailLevels<T>&, cudaStream_t, int);

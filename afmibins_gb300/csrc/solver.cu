@@ -84,6 +84,9 @@ struct afmib_solver {
     // products and face sums in double-float (relative 2^-44; the FP64 form
     // and the single-operator entry point stay FP64; AFMIB_SPREAD_DF=0: FP64)
     bool spread_df = true;
+    // mixed form: the FP64 interpolation of the IB step in double-float too
+    // (k_interp_dfl; AFMIB_INTERP_DF=0: FP64 arithmetic)
+    bool interp_df = true;
     // mixed form with the double-float residual: the Crank-Nicolson viscous
     // solves start from uold (the step's start velocity), whose residual
     // comes pointwise from the kept Q, instead of the current velocity
@@ -308,15 +311,16 @@ enum ProfId {
     P_ADVECT, P_HELM_RHS, P_CG_INIT, P_CG_APPLY, P_CG_UPDATE, P_CG_DIR, P_RBGS, P_RESID, P_RESID_NORM,
     P_RESTRICT, P_PROLONG, P_COARSE, P_DIV, P_GRAD_SUB, P_MEAN, P_WALL, P_SPRINGS, P_PREP, P_SORT,
     P_TILES, P_SPREAD, P_INTERP, P_MARKER, P_HELM_DEFECT, P_LAP_DEFECT, P_CORRECT, P_ADJ_ADVECT, P_ADJ_MARKER,
-    P_RBGS0, P_RESID0, P_RESTRICT0, P_PROLONG0, P_CG_DIRAPPLY, P_TAIL, P_JACOBI, P_HELM_UPDATE, P_LAP_UPDATE, P_COUNT
+    P_RBGS0, P_RESID0, P_RESTRICT0, P_PROLONG0, P_CG_DIRAPPLY, P_TAIL, P_JACOBI, P_HELM_UPDATE, P_LAP_UPDATE,
+    P_RESID_RESTRICT0, P_RESID_RESTRICT, P_COUNT
 };
 const char* kProfNames[P_COUNT] = {
     "advect", "helm_rhs", "cg_init", "cg_apply", "cg_update", "cg_direction", "mg_rbgs", "mg_residual",
     "mg_residual_norm", "mg_restrict", "mg_prolong_add", "mg_coarse_cg", "div", "grad_sub", "mean_removal",
     "wall_update", "springs", "marker_prep", "radix_sort", "tile_bins", "spread_gather", "interp", "marker_update",
     "helm_defect_fp64", "lap_defect_fp64", "add_correction_fp64", "advect_adjoint", "marker_adjoint",
-    "mg_rbgs_fine", "mg_residual_fine", "mg_restrict_fine", "mg_prolong_add_fine", "cg_dir_apply", "mg_coarse_tail", "helm_jacobi_fp32",
-    "helm_update_df", "lap_update_df"};
+    "mg_rbgs_fine", "mg_residual_fine", "mg_restrict_fine", "mg_prolong_add_fine", "cg_dir_apply", "mg_coarse_tail",
+    "helm_inner_sweep_fp32", "helm_update_df", "lap_update_df", "mg_resid_restrict_fine", "mg_resid_restrict"};
 
 cudaEvent_t prof_event(afmib_solver* s) {
     if (!s->prof_pool.empty()) {
@@ -536,16 +540,22 @@ int vcycle(afmib_solver* s, size_t l) {
     }
     const bool fine = l == 0;
     TRY(smooth(s, L, sizeof(T) == sizeof(float) ? (fine ? s->inner_nu1 : s->inner_nu1c) : s->cfg.nu1));
-    {
-        ProfScope ps(s, fine ? P_RESID0 : P_RESID, 3 * Ns);
-        launch_residual<T>(L.d, L.r, L.x, L.b, nullptr, nullptr, s->st, pass_dir(s, L.d, sizeof(T)));
-    }
     MGLevelT<T>& C = lv[l + 1];
-    {
-        ProfScope ps(s, fine ? P_RESTRICT0 : P_RESTRICT, Ns + Ns / 8);
-        launch_restrict<T>(L.d, C.b, L.r, s->st, pass_dir(s, L.d, sizeof(T)));
+    if (resid_restrict_fused_ok(L.d)) {
+        // x, b read; coarse b and x written (the fine residual stays on chip)
+        ProfScope ps(s, fine ? P_RESID_RESTRICT0 : P_RESID_RESTRICT, 2 * Ns + 2 * Ns / 8);
+        launch_resid_restrict<T>(L.d, C.b, C.x, L.x, L.b, s->st, pass_dir(s, L.d, sizeof(T)));
+    } else {
+        {
+            ProfScope ps(s, fine ? P_RESID0 : P_RESID, 3 * Ns);
+            launch_residual<T>(L.d, L.r, L.x, L.b, nullptr, nullptr, s->st, pass_dir(s, L.d, sizeof(T)));
+        }
+        {
+            ProfScope ps(s, fine ? P_RESTRICT0 : P_RESTRICT, Ns + Ns / 8);
+            launch_restrict<T>(L.d, C.b, L.r, s->st, pass_dir(s, L.d, sizeof(T)));
+        }
+        CK(cudaMemsetAsync(C.x, 0, C.d.ncell() * sizeof(T), s->st));
     }
-    CK(cudaMemsetAsync(C.x, 0, C.d.ncell() * sizeof(T), s->st));
     CKL();
     TRY(vcycle<T>(s, l + 1));
     {
@@ -1374,10 +1384,12 @@ int check_marker_flag(afmib_solver* s) {
     return AFMIB_OK;
 }
 
-int interp_markers(afmib_solver* s, const double* u, const double* v, const double* w, double* U, bool fp32 = false) {
+int interp_markers(afmib_solver* s, const double* u, const double* v, const double* w, double* U, bool fp32 = false,
+                   bool dfloat = false) {
     const double touched = (double)s->stats.spread_tiles * s->tile_cells();
     ProfScope ps(s, P_INTERP, 3 * touched * 8 + (double)s->M * (24 + 3 * 8 + 8));
     if (fp32) launch_interp<float, float>(s->d, s->M, s->perm, s->mw32, s->u32, s->v32, s->w32, U, s->st);
+    else if (dfloat) launch_interp_dfl(s->d, s->M, s->perm, s->mw, u, v, w, U, s->st);
     else launch_interp<double, double>(s->d, s->M, s->perm, s->mw, u, v, w, U, s->st);
     return AFMIB_OK;
 }
@@ -1416,7 +1428,8 @@ int ib_one_step(afmib_solver* s) {
                     : spread_forces(s, vol, s->f[0], s->f[1], s->f[2], s->mixed && s->spread_df);
     };
     auto interp = [&](double* U) {
-        return in32 ? interp_markers(s, s->u, s->v, s->w, U, true) : interp_markers(s, s->u, s->v, s->w, U, false);
+        return in32 ? interp_markers(s, s->u, s->v, s->w, U, true)
+                    : interp_markers(s, s->u, s->v, s->w, U, false, s->mixed && s->interp_df);
     };
     CK(cudaMemsetAsync(s->dflag, 0, sizeof(int), s->st));
     const long long N = s->N();
@@ -1831,6 +1844,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_HELM_DF")) s->helm_df = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_LAP_DF")) s->lap_df = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_SPREAD_DF")) s->spread_df = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_INTERP_DF")) s->interp_df = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_CN_START_OLD")) s->cn_start_old = std::string(e) != "0";
     if (s->mixed && s->fused_rhs)
         for (auto& q : s->qo) TRY(dalloc(s, &q, N));

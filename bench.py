@@ -61,6 +61,8 @@ def parse():
                     help="mixed form: bit 0 FP32 spreading, bit 1 FP32 interpolation (0: both FP64, the default)")
     ap.add_argument("--err-steps", type=int, default=100,
                     help="IB steps of the untimed mixed-vs-FP64 error run (the configuration's 100; 0 skips it)")
+    ap.add_argument("--err-tol", type=float, default=1e-12,
+                    help="solver tolerance of the FP64 yardstick of the error run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", choices=["ib", "mg", "adjoint", "large"], default="ib",
@@ -91,6 +93,9 @@ def workload(n, shells, per_shell, radius, min_sep, seed_offset=0):
 # (1/69 of the FP32 rate on GB300) and the latency-bound spreading gather.
 NOT_HBM_BOUND = {"helm_defect_fp64", "lap_defect_fp64", "helm_rhs", "spread_gather", "mg_coarse_tail",
                  "mg_coarse_cg"}
+# Families of the mixed form's interleaved viscous solves (defects on one
+# stream, corrections on another).
+OVERLAPPED = {"helm_inner_sweep_fp32", "helm_update_df", "add_correction_fp64", "helm_defect_fp64", "helm_rhs"}
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) measured
 # by ncu for the fine-level kernel of a family, by (family, grid, precision).
 NCU_TRAFFIC = {
@@ -614,27 +619,36 @@ def main():
                         "steps": args.warmup + args.steps}
         fp64["speedup_of_headline"] = value / fp64["value"]
         fp64w["speedup_of_headline"] = value / fp64w["value"]
-        # the configuration's error statement: both forms from the same state
-        # over --err-steps IB steps (untimed), the FP64 form with the
-        # reference's projections from zero
+        # the configuration's error statement (untimed): the mixed form and the
+        # FP64 form at the configuration's tolerance, each against the FP64
+        # form converged further (--err-tol, the reference's projections from
+        # zero; at tol 1e-12 this workload's FP64 form is pinned to the oracle
+        # by its 256^3 digest), from the same state over --err-steps IB steps
         if args.err_steps > 0:
             ends = {}
-            for name, prec, start in (("mixed", headline, 0), ("fp64", capi.FP64, capi.START_ZERO)):
-                with capi.Solver(args.n, mu=args.mu, rho=1.0, dt=args.dt, tol=args.tol, k_spring=0.5, precision=prec,
-                                 proj_start=start, inner_tol=args.inner_tol,
+            for name, prec, start, tol in (("yardstick", capi.FP64, capi.START_ZERO, args.err_tol),
+                                           ("mixed", headline, 0, args.tol),
+                                           ("fp64", capi.FP64, capi.START_ZERO, args.tol)):
+                with capi.Solver(args.n, mu=args.mu, rho=1.0, dt=args.dt, tol=tol, k_spring=0.5, precision=prec,
+                                 proj_start=start, inner_tol=args.inner_tol, max_cg_iters=5000, max_mg_cycles=1000,
                                  ib_fp32=args.ib_fp32 if prec == capi.MIXED else 0) as se:
                     se.set_velocity(*state[3:])
                     se.project()
                     se.set_markers(state[0], state[1], state[2])
                     se.ib_step(args.err_steps)
                     ends[name] = (se.get_velocity(), se.get_pressure(), se.get_markers())
-            (um, pm, Xm), (uf, pf, Xf) = ends["mixed"], ends["fp64"]
-            errors = {"velocity": max(rel_err(a, b) for a, b in zip(um, uf)),
-                      "pressure": pressure_err(pm, pf, args.n, args.mu, args.dt),
-                      "marker_displacement": rel_err(Xm - X, Xf - X),
-                      "marker_position_max_abs": float(np.max(np.abs(Xm - Xf))),
-                      "steps": args.err_steps,
-                      "yardstick": "the FP64 form, pinned to the oracle at this workload (2 IB steps, tol 1e-12)"}
+            uf, pf, Xf = ends["yardstick"]
+
+            def errs(name):
+                u_, p_, X_ = ends[name]
+                return {"velocity": max(rel_err(a, b) for a, b in zip(u_, uf)),
+                        "pressure": pressure_err(p_, pf, args.n, args.mu, args.dt),
+                        "marker_displacement": rel_err(X_ - X, Xf - X),
+                        "marker_position_max_abs": float(np.max(np.abs(X_ - Xf)))}
+
+            errors = dict(errs("mixed"), steps=args.err_steps, tol=args.tol,
+                          yardstick=f"the FP64 form at tol {args.err_tol:g} (pinned to the oracle on this workload)",
+                          fp64_form_at_tol=errs("fp64"))
 
     # ---- per-kernel durations over profiled steps (events on the solver's stream)
     peak, peak_kind = measured_peaks()
@@ -663,6 +677,12 @@ def main():
         kernels = {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / total_ms, 4),
                        "GB_s": round(v[2] / (v[1] * 1e-3) / 1e9, 1) if v[1] > 0 else None}
                    for k, v in sorted(table.items(), key=lambda kv: -kv[1][1])}
+        if headline == capi.MIXED:
+            # the mixed form's three viscous solves run on two streams: these
+            # families' event brackets include time spent beside the other
+            # stream's kernels, so their ms overstate and GB_s understate
+            for k in OVERLAPPED & kernels.keys():
+                kernels[k]["timing"] = "events on two overlapping streams"
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

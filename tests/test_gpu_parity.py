@@ -778,3 +778,63 @@ def test_ib_steps_with_bending_periodic(precision):
     bar = TOL if precision == capi.FP64 else MIXED_TOL
     assert rel(gu, ru) < bar and rel(gv, rv) < bar and rel(gw, rw) < bar
     assert rel(gX, Xr) < bar
+
+
+@pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
+def test_double_float_interpolation_matches_fp64(monkeypatch, bc):
+    """The mixed form's interpolation in double-float on the FP32 pipe
+    (k_interp_dfl, axis-by-axis sums) against the FP64 kernel: two mixed IB
+    steps with each, velocities and marker displacements agree far below the
+    mixed form's 1e-8 bar (the marker velocities differ by a few units of
+    2^-46, the steps' solver tolerance is 1e-12)."""
+    g, u, v, w, X, nstart, nidx = _periodic_case(32, M=800, seed=13)
+    if bc == capi.BC_CHANNEL:
+        v = v[: g.nx * (g.ny - 1) * g.nz]
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("AFMIB_INTERP_DF", mode)
+        with capi.Solver(32, bc=bc, precision=capi.MIXED, mu=0.01, dt=1e-3, tol=1e-12, k_spring=0.5) as sv:
+            sv.set_velocity(u, v, w)
+            sv.project()
+            sv.set_markers(X, nstart, nidx)
+            sv.ib_step(2)
+            out[mode] = (sv.get_velocity(), sv.get_markers())
+    for a, b in zip(out["1"][0], out["0"][0]):
+        assert rel(a, b) < 1e-10
+    assert rel(out["1"][1] - X, out["0"][1] - X) < 1e-10
+
+
+@pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED])
+def test_fused_residual_restriction_keeps_bits(monkeypatch, bc, precision):
+    """The fine-level residual fused with the restriction (k_resid_restrict2,
+    the residual kept in shared memory) against the residual and restriction
+    kernels: the same terms in the same order, so multigrid solves and IB
+    steps agree bit for bit (the fused kernel taken from 32-cell levels here,
+    both of its z chunkings: 256^3 takes 8 coarse planes per block)."""
+    monkeypatch.setenv("AFMIB_RESID_RESTRICT_MIN_NX", "32")
+    for shape in ((64, 64, 64), (128, 64, 32), (256, 256, 256)):
+        nx, ny, nz = shape
+        rng = np.random.default_rng(5)
+        b = rng.standard_normal(nx * ny * nz)
+        b -= b.mean()
+        out = {}
+        for mode in ("0", "1"):
+            monkeypatch.setenv("AFMIB_RESID_RESTRICT", mode)
+            with capi.Solver(nx, ny, nz, n=nx, bc=bc, precision=precision, tol=1e-10) as sv:
+                out[mode] = sv.mg_solve(b)
+        assert np.array_equal(out["0"][0], out["1"][0]) and out["0"][1] == out["1"][1], shape
+    g, u, v, w, X, nstart, nidx = _periodic_case(64, M=800, seed=3)
+    if bc == capi.BC_CHANNEL:
+        v = v[: g.nx * (g.ny - 1) * g.nz]
+    res = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("AFMIB_RESID_RESTRICT", mode)
+        with capi.Solver(64, bc=bc, precision=precision, mu=0.01, dt=1e-3, tol=1e-10, k_spring=0.5) as sv:
+            sv.set_velocity(u, v, w)
+            sv.project()
+            sv.set_markers(X, nstart, nidx)
+            sv.ib_step(2)
+            res[mode] = (*sv.get_velocity(), sv.get_pressure(), sv.get_markers())
+    for a, c in zip(res["0"], res["1"]):
+        assert np.array_equal(a, c)
