@@ -109,6 +109,31 @@ AFMIB_HD float df_hi(double d) {
     return fbits(sign | ((unsigned)(e + 127) << 23) | mh);
 }
 
+// The float nearest to d (ties away from zero), by integer operations: half
+// of the 29 dropped mantissa bits is added to d's bit pattern (a carry moves
+// into the exponent, which is the rounding up to the next binade) and the
+// result truncated as df_hi. inf and nan pass through df_hi unchanged.
+AFMIB_HD float df_round(double d) {
+    const unsigned long long u = (unsigned long long)dbits(d);
+    if (((u >> 52) & 0x7ffu) == 0x7ffu) return df_hi(d);
+    return df_hi(dfrom(u + (1ull << 28)));
+}
+
+// d as the float nearest to it (df_round) and the float of the rest: the
+// truncated pair of df_split gives the rest exactly, lo - (hi - hi_trunc)
+// (both multiples of d's 2^-46 unit below one ulp of hi), so hi + lo is d
+// to 2^-46 relative, as df_split's pair. No FP64 instruction is issued.
+// Below 2^-80 df_split drops the rest (float underflow): there the
+// truncated pair is returned.
+AFMIB_HD df2 df_split_round(double d) {
+    const df2 t = df_split(d);
+    if (t.lo == 0.f) return t;  // no rest, or below the rest's float range
+    df2 r;
+    r.hi = df_round(d);
+    r.lo = t.lo - (r.hi - t.hi);
+    return r;
+}
+
 // a + b with both pairs' rounding errors carried (accurate under cancellation)
 AFMIB_HD df2 df_add(df2 a, df2 b) {
     float s = a.hi + b.hi;

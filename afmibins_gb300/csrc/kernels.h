@@ -12,6 +12,10 @@ namespace afmib {
 // ----- MAC stencils (kernels_field.cu) -------------------------------------
 // Conservative centred advection N(u) of src/ns/solver.h:142-236.
 // TI: storage type of the velocity, T: arithmetic and output type.
+// The mixed form's advection from the velocity's float pairs (hi, lo), each
+// flux difference formed without cancellation (k_advect_df).
+void launch_advect_df(const Dims& d, float* ua, float* va, float* wa, const float* uh, const float* ul,
+                      const float* vh, const float* vl, const float* wh, const float* wl, cudaStream_t s);
 template <typename TI, typename T>
 void launch_advect(const Dims& d, T* ua, T* va, T* wa, const TI* u, const TI* v, const TI* w, cudaStream_t s);
 // Divergence n*(du + dv + dw), src/alg/div.h:29-60. top/bottom (channel only,
@@ -26,10 +30,13 @@ void launch_grad(const Dims& d, T* px, T* py, T* pz, const T* p, cudaStream_t s)
 // mode the wall-adjacent gradient rows needed by the next wall update are
 // saved into wallgrad[8][nx*nz] (may be null): x-gradient at y = 0, 1,
 // ny-1, ny-2, z-gradient at y = 0, ny-1, 1, ny-2.
-// u32/v32/w32 (optional): FP32 shadow of the updated velocity.
+// u32/v32/w32 (optional): FP32 shadow of the updated velocity, rounded to
+// nearest (round_shadow) or truncated, by integer operations; with
+// u32l/v32l/w32l also the rest of each value's pair (df_split_round).
 template <typename T>
 void launch_grad_sub(const Dims& d, T* u, T* v, T* w, const T* phi, T* wallgrad, cudaStream_t s, float* u32 = nullptr,
-                     float* v32 = nullptr, float* w32 = nullptr);
+                     float* v32 = nullptr, float* w32 = nullptr, int round_shadow = 1, float* u32l = nullptr,
+                     float* v32l = nullptr, float* w32l = nullptr);
 // Wall-velocity correction of src/ns/projection.h:75-122 (channel only).
 // walls = [ut | ub | wt | wb], nx*nz each.
 void launch_wall_update(const Dims& d, double* walls, const double* wallgrad, cudaStream_t s, int corrected = 0);
@@ -132,8 +139,10 @@ template <typename T>
 void launch_axpy(long long n, T* y, const T* x, T a, cudaStream_t s);  // y += a x
 template <typename T>
 void launch_lincomb(long long n, T* y, T a, const T* x, T b, const T* z, cudaStream_t s);  // y = a x + b z
-// FP32 shadow of an FP64 field, truncated (df_hi), as the projection writes it
-void launch_shadow(long long n, float* out, const double* in, cudaStream_t s);
+// FP32 shadow of an FP64 field, as the projection writes it (rounded to
+// nearest by df_round, or truncated by df_hi)
+void launch_shadow(long long n, float* out, const double* in, cudaStream_t s, int round_shadow = 1,
+                   float* lo = nullptr);
 template <typename TO, typename TI>
 void launch_convert(long long n, TO* out, const TI* in, cudaStream_t s);
 
@@ -209,8 +218,8 @@ template <typename T>
 void launch_prolong_add(const Dims& d, T* fine, const T* coarse, cudaStream_t s, int rev = 0);
 // coarse_b = restriction of (b - L x), coarse_x = 0, in one pass (the
 // residual stays in shared memory); for the levels resid_restrict_fused_ok
-// takes (3D power-of-two levels with nx >= 256 by default;
-// AFMIB_RESID_RESTRICT=0 keeps the two kernels)
+// takes (opt-in, AFMIB_RESID_RESTRICT=1: 3D power-of-two levels with
+// nx >= 256 by default)
 bool resid_restrict_fused_ok(const Dims& d);
 template <typename T>
 void launch_resid_restrict(const Dims& d, T* coarse_b, T* coarse_x, const T* x, const T* b, cudaStream_t s,

@@ -89,6 +89,81 @@ __global__ void __launch_bounds__(BX * BY, P2 ? 6 : 4) k_advect(Dims d, T* __res
     }
 }
 
+// The mixed form's advection of the FP64 velocity, in FP32 from its pairs of
+// floats (h: the nearest float, l: the rest, written by the projection; plane
+// 0 of v is the zero wall in channel mode as above). The fluxes are those of
+// k_advect, but every flux difference is rewritten without cancellation:
+//   q1^2 - q0^2       = (q1 - q0)(q1 + q0)            (uu, vv, ww)
+//   A1 B1 - A0 B0     = (A1 - A0) B1 + A0 (B1 - B0)   (uv, uw, vw)
+// with the differences of velocities formed from the pairs,
+// (h_a - h_b) + (l_a - l_b): h_a - h_b is exact when the two are within a
+// factor of two (Sterbenz) and otherwise carries an error relative to
+// itself, so each difference is its FP32 rounding. FP32 fluxes subtracted
+// directly lose n/k of their digits (the difference of two fluxes one cell
+// apart), which over 100 steps at 256^3 left the mixed form's velocity 1.3e-8
+// from the FP64 form's; here every term is within a few FP32 roundings of
+// itself.
+template <bool P2>
+__global__ void __launch_bounds__(BX * BY, P2 ? 4 : 3) k_advect_df(Dims d, float* __restrict__ ua,
+                                                                   float* __restrict__ va, float* __restrict__ wa,
+                                                                   const float* __restrict__ uh,
+                                                                   const float* __restrict__ ul,
+                                                                   const float* __restrict__ vh,
+                                                                   const float* __restrict__ vl,
+                                                                   const float* __restrict__ wh,
+                                                                   const float* __restrict__ wl) {
+    AFMIB_XYZ
+    const Ix2 I(d);
+    auto lin = [&](int xx, int yy, int zz) -> long long {
+        return P2 ? (long long)I.at(xx, yy, zz) : afmib::lin(d, xx, yy, zz);
+    };
+    const int xm = P2 ? I.xm(x) : xm1(d, x), xp = P2 ? I.xp(x) : xp1(d, x), ym = P2 ? I.ym(y) : ym1(d, y),
+              yp = P2 ? I.yp(y) : yp1(d, y), zm = P2 ? I.zm(z) : zm1(d, z), zp = P2 ? I.zp(z) : zp1(d, z);
+    const long long i = lin(x, y, z);
+    const long long ixm = lin(xm, y, z), ixp = lin(xp, y, z), iym = lin(x, ym, z), iyp = lin(x, yp, z),
+                    izm = lin(x, y, zm), izp = lin(x, y, zp);
+    // difference and sum of two values of a field from its pairs
+    auto D = [](const float* h, const float* l, long long a, long long b) { return (h[a] - h[b]) + (l[a] - l[b]); };
+    auto S = [](const float* h, const float* l, long long a, long long b) { return (h[a] + h[b]) + (l[a] + l[b]); };
+    // q(+1) + 2 q(0) + q(-1) for the squared fluxes
+    auto S3 = [](const float* h, const float* l, long long a, long long c, long long b) {
+        return ((h[a] + h[b]) + 2.f * h[c]) + ((l[a] + l[b]) + 2.f * l[c]);
+    };
+    const float f = 0.25f * float(d.n);
+    // u-momentum: uu, uv (y), uw (z)
+    {
+        const long long ixmyp = lin(xm, yp, z), ixmzp = lin(xm, y, zp);
+        const float tx = S3(uh, ul, ixp, i, ixm) * D(uh, ul, ixp, ixm);
+        const float ty = D(uh, ul, iyp, iym) * S(vh, vl, iyp, ixmyp) +
+                         S(uh, ul, i, iym) * (D(vh, vl, iyp, i) + D(vh, vl, ixmyp, ixm));
+        const float tz = D(uh, ul, izp, izm) * S(wh, wl, ixmzp, izp) +
+                         S(uh, ul, izm, i) * (D(wh, wl, ixmzp, ixm) + D(wh, wl, izp, i));
+        ua[i] = f * ((tx + ty) + tz);
+    }
+    // v-momentum: uv (x), vv, vw (z)
+    if (d.channel && y == 0) {
+        va[i] = 0.f;
+    } else {
+        const long long ixpym = lin(xp, ym, z), iymzp = lin(x, ym, zp);
+        const float tx = (D(uh, ul, ixp, i) + D(uh, ul, ixpym, iym)) * S(vh, vl, ixp, i) +
+                         S(uh, ul, i, iym) * D(vh, vl, ixp, ixm);
+        const float ty = S3(vh, vl, iyp, i, iym) * D(vh, vl, iyp, iym);
+        const float tz = D(vh, vl, izp, izm) * S(wh, wl, izp, iymzp) +
+                         S(vh, vl, izm, i) * (D(wh, wl, izp, i) + D(wh, wl, iymzp, iym));
+        va[i] = f * ((tx + ty) + tz);
+    }
+    // w-momentum: uw (x), vw (y), ww
+    {
+        const long long ixpzm = lin(xp, y, zm), iypzm = lin(x, yp, zm);
+        const float tx = (D(uh, ul, ixpzm, izm) + D(uh, ul, ixp, i)) * S(wh, wl, ixp, i) +
+                         S(uh, ul, izm, i) * D(wh, wl, ixp, ixm);
+        const float ty = (D(vh, vl, iypzm, izm) + D(vh, vl, iyp, i)) * S(wh, wl, iyp, i) +
+                         S(vh, vl, izm, i) * D(wh, wl, iyp, iym);
+        const float tz = S3(wh, wl, izp, i, izm) * D(wh, wl, izp, izm);
+        wa[i] = f * ((tx + ty) + tz);
+    }
+}
+
 // Divergence, src/alg/div.h:29-60.
 template <typename T>
 __global__ void k_div(Dims d, T* __restrict__ out, const T* __restrict__ u, const T* __restrict__ v,
@@ -125,7 +200,8 @@ __global__ void k_grad(Dims d, T* __restrict__ px, T* __restrict__ py, T* __rest
 template <typename T>
 __global__ void k_grad_sub(Dims d, T* __restrict__ u, T* __restrict__ v, T* __restrict__ w, const T* __restrict__ p,
                            T* __restrict__ wg, float* __restrict__ u32, float* __restrict__ v32,
-                           float* __restrict__ w32) {
+                           float* __restrict__ w32, int round_shadow, float* __restrict__ u32l,
+                           float* __restrict__ v32l, float* __restrict__ w32l) {
     AFMIB_XYZ
     const long long i = lin(d, x, y, z);
     const T n = T(d.n), p0 = p[i];
@@ -140,12 +216,22 @@ __global__ void k_grad_sub(Dims d, T* __restrict__ u, T* __restrict__ v, T* __re
         v[i] = vn;
     }
     if (u32) {  // FP32 shadow of the velocity for the mixed form's FP32 stencils
-        // truncated by integer operations (df_hi), not rounded by the FP64
-        // pipe: 2^-23 relative, below what the FP32 stencils resolve
+        // rounded (or truncated) by integer operations, not by the FP64
+        // pipe's conversion
         if constexpr (sizeof(T) == sizeof(double)) {
-            u32[i] = df_hi(un);
-            v32[i] = df_hi(vn);
-            w32[i] = df_hi(wn);
+            if (u32l) {  // the pairs of the mixed form's advection
+                const df2 pu = df_split_round(un), pv = df_split_round(vn), pw = df_split_round(wn);
+                u32[i] = pu.hi;
+                v32[i] = pv.hi;
+                w32[i] = pw.hi;
+                u32l[i] = pu.lo;
+                v32l[i] = pv.lo;
+                w32l[i] = pw.lo;
+            } else {
+                u32[i] = round_shadow ? df_round(un) : df_hi(un);
+                v32[i] = round_shadow ? df_round(vn) : df_hi(vn);
+                w32[i] = round_shadow ? df_round(wn) : df_hi(wn);
+            }
         } else {
             u32[i] = float(un);
             v32[i] = float(vn);
@@ -764,6 +850,11 @@ void launch_advect(const Dims& d, T* ua, T* va, T* wa, const TI* u, const TI* v,
     if (ix2_ok(d)) k_advect<TI, T, true><<<grid3(d), block3(), 0, s>>>(d, ua, va, wa, u, v, w);
     else k_advect<TI, T, false><<<grid3(d), block3(), 0, s>>>(d, ua, va, wa, u, v, w);
 }
+void launch_advect_df(const Dims& d, float* ua, float* va, float* wa, const float* uh, const float* ul,
+                      const float* vh, const float* vl, const float* wh, const float* wl, cudaStream_t s) {
+    if (ix2_ok(d)) k_advect_df<true><<<grid3(d), block3(), 0, s>>>(d, ua, va, wa, uh, ul, vh, vl, wh, wl);
+    else k_advect_df<false><<<grid3(d), block3(), 0, s>>>(d, ua, va, wa, uh, ul, vh, vl, wh, wl);
+}
 template <typename T>
 void launch_div(const Dims& d, T* out, const T* u, const T* v, const T* w, const T* top, const T* bottom, cudaStream_t s) {
     k_div<T><<<grid3(d), block3(), 0, s>>>(d, out, u, v, w, top, bottom);
@@ -774,8 +865,9 @@ void launch_grad(const Dims& d, T* px, T* py, T* pz, const T* p, cudaStream_t s)
 }
 template <typename T>
 void launch_grad_sub(const Dims& d, T* u, T* v, T* w, const T* phi, T* wallgrad, cudaStream_t s, float* u32,
-                     float* v32, float* w32) {
-    k_grad_sub<T><<<grid3(d), block3(), 0, s>>>(d, u, v, w, phi, wallgrad, u32, v32, w32);
+                     float* v32, float* w32, int round_shadow, float* u32l, float* v32l, float* w32l) {
+    k_grad_sub<T><<<grid3(d), block3(), 0, s>>>(d, u, v, w, phi, wallgrad, u32, v32, w32, round_shadow, u32l, v32l,
+                                                w32l);
 }
 void launch_wall_update(const Dims& d, double* walls, const double* wallgrad, cudaStream_t s, int corrected) {
     k_wall_update<<<ew_blocks((long long)d.nx * d.nz), 256, 0, s>>>(d, walls, wallgrad, corrected);
@@ -1142,19 +1234,29 @@ void launch_convert(long long n, TO* out, const TI* in, cudaStream_t s) {
     k_convert<TO, TI><<<ew_blocks(n), 256, 0, s>>>(n, out, in);
 }
 
-// FP32 shadow of an FP64 velocity field, truncated as k_grad_sub writes it
-__global__ void k_shadow(long long N, float* __restrict__ o, const double* __restrict__ in) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
-        o[i] = df_hi(in[i]);
+// FP32 shadow of an FP64 velocity field (and, with lo, the rest of its
+// pair), as k_grad_sub writes it
+__global__ void k_shadow(long long N, float* __restrict__ o, const double* __restrict__ in, int round_shadow,
+                         float* __restrict__ lo) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+        if (lo) {
+            const df2 p = df_split_round(in[i]);
+            o[i] = p.hi;
+            lo[i] = p.lo;
+        } else {
+            o[i] = round_shadow ? df_round(in[i]) : df_hi(in[i]);
+        }
+    }
 }
-void launch_shadow(long long n, float* out, const double* in, cudaStream_t s) {
-    k_shadow<<<ew_blocks(n), 256, 0, s>>>(n, out, in);
+void launch_shadow(long long n, float* out, const double* in, cudaStream_t s, int round_shadow, float* lo) {
+    k_shadow<<<ew_blocks(n), 256, 0, s>>>(n, out, in, round_shadow, lo);
 }
 
 #define AFMIB_INST(T)                                                                                          \
     template void launch_div<T>(const Dims&, T*, const T*, const T*, const T*, const T*, const T*, cudaStream_t); \
     template void launch_grad<T>(const Dims&, T*, T*, T*, const T*, cudaStream_t);                             \
-    template void launch_grad_sub<T>(const Dims&, T*, T*, T*, const T*, T*, cudaStream_t, float*, float*, float*); \
+    template void launch_grad_sub<T>(const Dims&, T*, T*, T*, const T*, T*, cudaStream_t, float*, float*, float*, \
+                                     int, float*, float*, float*);                                               \
     template void launch_helm_apply<T>(const Dims&, int, double, T*, const T*, cudaStream_t);                  \
     template void launch_cg_init<T>(const Dims&, int, double, const T*, const T*, T*, T*, RedScratch, double*, \
                                     cudaStream_t);                                                             \

@@ -569,15 +569,18 @@ __global__ void k_interp(Dims d, int M, const int* __restrict__ perm, MarkerW<T>
 }
 
 // The same interpolation of FP64 fields in double-float on the FP32 pipe
-// (the mixed form; GB300's FP64 pipe runs at 1/64 of the FP32 rate). The sum
-// is taken axis by axis, U = sum_z wz sum_y wy sum_x wx u, so there are 84
-// products per component instead of 128. Field values and weights are split
-// exactly by integer operations (df_split, 24 + 23 bits); each product is a
-// pair (fma two-product plus the cross terms) and the sums keep an exact
-// two-sum of the leading words and a plain sum of the trailing ones. Every
-// term is below the largest |w u| of its sum, so the error is a few units of
-// 2^-46 of the largest term times the 4 to 16 terms of a sum. One FP64
-// addition per component turns the pair back into FP64.
+// (the mixed form; GB300's FP64 pipe runs at 1/64 of the FP32 rate). Four
+// lanes take one marker, one x tap each: a lane issues the loads of its 16
+// (y, z) faces of a component back to back (the fields are larger than L2,
+// so the time is DRAM latency), sums them as sum_z wz sum_y wy u, takes its
+// x weight, and the quad adds its four partial sums by shuffles in a fixed
+// pattern (the first lane's result is stored). Field values and weights are
+// split exactly by integer operations (df_split, 24 + 23 bits); each product
+// is a pair (fma two-product plus the cross terms) and the sums keep an
+// exact two-sum of the leading words and a plain sum of the trailing ones, so
+// the result is within a few units of 2^-46 of the largest term times the 4
+// to 16 terms of a sum. One FP64 addition per component turns the pair back
+// into FP64.
 struct DfAcc {
     float s, e;  // leading sum (two-summed), trailing sum
 };
@@ -600,59 +603,56 @@ __device__ __forceinline__ df2 dfacc_pair(DfAcc a) {
     return r;
 }
 
-__global__ void __launch_bounds__(128) k_interp_dfl(Dims d, int M, const int* __restrict__ perm, MarkerW<double> mw,
-                                                    const double* __restrict__ u, const double* __restrict__ v,
-                                                    const double* __restrict__ w, double* __restrict__ U) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= M) return;
+constexpr int kInterpDfBlock = 128;
+
+__global__ void __launch_bounds__(kInterpDfBlock) k_interp_dfl(Dims d, int M, const int* __restrict__ perm,
+                                                               MarkerW<double> mw, const double* __restrict__ u,
+                                                               const double* __restrict__ v,
+                                                               const double* __restrict__ w, double* __restrict__ U) {
+    const int p = (blockIdx.x * kInterpDfBlock + threadIdx.x) >> 2;
+    const int q = threadIdx.x & 3;
+    if (p >= M) return;  // a quad leaves together
+    const unsigned qmask = 0xfu << (threadIdx.x & 28);
     const int k = perm ? perm[p] : p;
-    const int ext[3] = {d.nx, d.ny, d.nz};
-    // weights of both offset variants per axis, split once
-    df2 wt[3][2][4];
-    int base[3][2];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int var = 0; var < 2; ++var) {
-            base[a][var] = mw.cell[3 * k + a] + mw.dbase[(k * 3 + a) * 2 + var];
-            const double* ww = mw.w + (((size_t)k * 3 + a) * 2 + var) * 4;
-#pragma unroll
-            for (int m = 0; m < 4; ++m) wt[a][var][m] = df_split(ww[m]);
-        }
 #pragma unroll 1
     for (int comp = 0; comp < 3; ++comp) {
         const double* src = comp == 0 ? u : (comp == 1 ? v : w);
         const int vx = comp == 0 ? 0 : 1, vy = comp == 1 ? 0 : 1, vz = comp == 2 ? 0 : 1;
-        // the variant of each axis picked by selects (no indexed local arrays)
-        int ix[4], iy[4], iz[4];
-        df2 wx[4], wy[4], wz[4];
-        const int bx = vx ? base[0][1] : base[0][0], by = vy ? base[1][1] : base[1][0],
-                  bz = vz ? base[2][1] : base[2][0];
+        const int bx = mw.cell[3 * k] + mw.dbase[(k * 3 + 0) * 2 + vx];
+        const int by = mw.cell[3 * k + 1] + mw.dbase[(k * 3 + 1) * 2 + vy];
+        const int bz = mw.cell[3 * k + 2] + mw.dbase[(k * 3 + 2) * 2 + vz];
+        const long long ix = wrapi(bx + q, d.nx);
+        long long roff[4][4];
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            ix[m] = wrapi(bx + m, ext[0]);
-            iy[m] = wrapi(by + m, ext[1]);
-            iz[m] = wrapi(bz + m, ext[2]);
-            wx[m] = vx ? wt[0][1][m] : wt[0][0][m];
-            wy[m] = vy ? wt[1][1][m] : wt[1][0][m];
-            wz[m] = vz ? wt[2][1][m] : wt[2][0][m];
-        }
+        for (int mz = 0; mz < 4; ++mz)
+#pragma unroll
+            for (int my = 0; my < 4; ++my)
+                roff[mz][my] = (long long)d.nx * (wrapi(by + my, d.ny) + (long long)d.ny * wrapi(bz + mz, d.nz)) + ix;
+        double val[4][4];
+#pragma unroll
+        for (int mz = 0; mz < 4; ++mz)
+#pragma unroll
+            for (int my = 0; my < 4; ++my) val[mz][my] = src[roff[mz][my]];
+        const double* wyp = mw.w + (((size_t)k * 3 + 1) * 2 + vy) * 4;
+        const double* wzp = mw.w + (((size_t)k * 3 + 2) * 2 + vz) * 4;
         DfAcc az = {0.f, 0.f};
 #pragma unroll
         for (int mz = 0; mz < 4; ++mz) {
             DfAcc ay = {0.f, 0.f};
 #pragma unroll
-            for (int my = 0; my < 4; ++my) {
-                const long long row = (long long)d.nx * (iy[my] + (long long)d.ny * iz[mz]);
-                DfAcc ax = {0.f, 0.f};
-#pragma unroll
-                for (int mx = 0; mx < 4; ++mx) dfacc_mul_add(ax, wx[mx], df_split(src[row + ix[mx]]));
-                dfacc_mul_add(ay, wy[my], dfacc_pair(ax));
-            }
-            dfacc_mul_add(az, wz[mz], dfacc_pair(ay));
+            for (int my = 0; my < 4; ++my) dfacc_mul_add(ay, df_split(wyp[my]), df_split(val[mz][my]));
+            dfacc_mul_add(az, df_split(wzp[mz]), dfacc_pair(ay));
         }
-        const df2 r = dfacc_pair(az);
-        U[(size_t)comp * M + k] = f32_to_f64(r.hi) + f32_to_f64(r.lo);
+        const df2 wxq = df_split(mw.w[(((size_t)k * 3 + 0) * 2 + vx) * 4 + q]);
+        df2 r = df_mul(wxq, dfacc_pair(az));
+        df2 o;
+        o.hi = __shfl_xor_sync(qmask, r.hi, 1);
+        o.lo = __shfl_xor_sync(qmask, r.lo, 1);
+        r = df_add(r, o);
+        o.hi = __shfl_xor_sync(qmask, r.hi, 2);
+        o.lo = __shfl_xor_sync(qmask, r.lo, 2);
+        r = df_add(r, o);
+        if (q == 0) U[(size_t)comp * M + k] = f32_to_f64(r.hi) + f32_to_f64(r.lo);
     }
 }
 
@@ -793,7 +793,8 @@ void launch_interp(const Dims& d, int M, const int* perm, MarkerW<T> mw, const T
 
 void launch_interp_dfl(const Dims& d, int M, const int* perm, MarkerW<double> mw, const double* u, const double* v,
                        const double* w, double* U, cudaStream_t s) {
-    if (M > 0) k_interp_dfl<<<(M + 127) / 128, 128, 0, s>>>(d, M, perm, mw, u, v, w, U);
+    if (M > 0) k_interp_dfl<<<(int)((4LL * M + kInterpDfBlock - 1) / kInterpDfBlock), kInterpDfBlock, 0, s>>>(
+        d, M, perm, mw, u, v, w, U);
 }
 
 void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, double c, cudaStream_t s) {

@@ -774,12 +774,18 @@ __device__ __forceinline__ void prolong_cell2(const Dims& d, const Ix2& I, T* fi
 // restrict_cell2's in its order, so the coarse right-hand side equals the two
 // kernels' bit for bit, and the fine residual is never written to memory.
 constexpr int RR_T = 16, RR_F = 2 * RR_T + 2, RR_THREADS = RR_T * RR_T;
+// ring plane layout: row stride RR_RS, even columns first and odd columns
+// from RR_ODD, so that the 16 coarse cells of a half warp read 16
+// consecutive words and the two halves (two fine rows apart) the other 16
+// banks: no shared-memory bank conflicts in the tap loop
+constexpr int RR_RS = 40, RR_ODD = 20;
+__device__ __forceinline__ int rr_at(int jy, int jx) { return jy * RR_RS + (jx & 1) * RR_ODD + (jx >> 1); }
 
 template <typename T, int RR_CZ>
 __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict2(Dims d, T* __restrict__ cb, T* __restrict__ cx,
                                                                const T* __restrict__ xv, const T* __restrict__ b,
                                                                int rev) {
-    __shared__ T ring[4][RR_F * RR_F];
+    __shared__ T ring[4][RR_F * RR_RS];
     const Ix2 I(d);
     const uint3 B = block_at(rev);
     const int xc0 = B.x * RR_T, yc0 = B.y * RR_T, zc0 = B.z * RR_CZ;
@@ -803,7 +809,7 @@ __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict2(Dims d, T* __res
             T S, c;
             lap_row2(d, I, xv, x, y, z, S, c);
             const int i = I.at(x, y, z);
-            dst[e] = b[i] - off * (S - c * xv[i]);
+            dst[rr_at(jy, jx)] = b[i] - off * (S - c * xv[i]);
         }
     };
     const int cxl = tid % RR_T, cyl = tid / RR_T;
@@ -812,7 +818,7 @@ __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict2(Dims d, T* __res
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const int dd = k - 2;
-        col[k] = 2 * cxl + k;  // fine x = 2 xc + 1 + dd
+        col[k] = (k & 1) * RR_ODD + cxl + (k >> 1);  // tile column 2 cxl + k: fine x = 2 xc + 1 + dd
         int yy;
         if (d.channel) {
             const int ycf = 2 * yc + 1;
@@ -838,7 +844,7 @@ __global__ void __launch_bounds__(RR_THREADS) k_resid_restrict2(Dims d, T* __res
             for (int ky = 0; ky < 4; ++ky)
 #pragma unroll
                 for (int kx = 0; kx < 4; ++kx)
-                    acc += (wgt[kx] * wgt[ky] * wgt[kz] / T(512)) * pl[row[ky] * RR_F + col[kx]];
+                    acc += (wgt[kx] * wgt[ky] * wgt[kz] / T(512)) * pl[row[ky] * RR_RS + col[kx]];
         }
         const int o = xc | (yc << (I.lx - 1)) | (zc << (I.lxy - 2));
         cb[o] = acc;
@@ -1269,13 +1275,13 @@ void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s, in
     if (d.nz > 1 && d.nx >= 2 && d.ny >= 2 && ix2_ok(d)) k_restrict2<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine, rev);
     else k_restrict<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine);
 }
-// Levels with nx >= AFMIB_RESID_RESTRICT_MIN_NX (default 256) take the fused
-// kernel: on smaller levels its grid (2 RR_T x 2 RR_T fine columns per block)
-// leaves SMs idle. Both switches are read at every call, so that a test can
-// compare the two paths in one process.
+// Opt-in (AFMIB_RESID_RESTRICT=1): levels with nx >= AFMIB_RESID_RESTRICT_MIN_NX
+// (default 256) then take the fused kernel (on smaller levels its grid of
+// 2 RR_T x 2 RR_T fine columns per block leaves SMs idle). Both switches are
+// read at every call, so that a test can compare the two paths in one process.
 bool resid_restrict_fused_ok(const Dims& d) {
     const char* e = std::getenv("AFMIB_RESID_RESTRICT");
-    if (e && e[0] == '0') return false;
+    if (!(e && e[0] == '1')) return false;
     const char* m = std::getenv("AFMIB_RESID_RESTRICT_MIN_NX");
     const int min_nx = m ? std::atoi(m) : 256;
     return d.nz > 1 && d.nx >= min_nx && d.nx >= 2 * RR_T && d.ny >= 2 * RR_T && d.nz >= 4 && ix2_ok(d);

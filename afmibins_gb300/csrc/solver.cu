@@ -87,6 +87,16 @@ struct afmib_solver {
     // mixed form: the FP64 interpolation of the IB step in double-float too
     // (k_interp_dfl; AFMIB_INTERP_DF=0: FP64 arithmetic)
     bool interp_df = true;
+    // mixed form: the FP32 velocity shadow (the FP32 advection's input) is
+    // rounded to nearest by integer operations (AFMIB_SHADOW_ROUND=0:
+    // truncated, a one-sided 2^-23 relative error)
+    int round_shadow = 1;
+    // mixed form: advection in FP64 from the FP64 velocity (AFMIB_ADVECT64=1)
+    bool advect64 = false;
+    // mixed form: the FP32 advection from the velocity's float pairs without
+    // cancellation (k_advect_df; AFMIB_ADVECT_DF=0: the FP32 fluxes of the
+    // rounded shadow, 1.0e-8 from the FP64 form after 100 steps at 256^3)
+    bool advect_df = true;
     // mixed form with the double-float residual: the Crank-Nicolson viscous
     // solves start from uold (the step's start velocity), whose residual
     // comes pointwise from the kept Q, instead of the current velocity
@@ -104,6 +114,7 @@ struct afmib_solver {
     bool mixed = false;
     float *adv32[3] = {}, *f32[3] = {}, *d32 = nullptr, *e32 = nullptr;
     float *u32 = nullptr, *v32 = nullptr, *w32 = nullptr;  // FP32 shadow of the velocity
+    float *u32l = nullptr, *v32l = nullptr, *w32l = nullptr;  // the rest of each value's float pair
     float *cg32_r = nullptr, *cg32_p = nullptr, *cg32_q = nullptr, *cg32_p2 = nullptr;
     std::vector<MGLevelT<float>> lv32;
     double *cx64 = nullptr, *cb64 = nullptr, *cr64 = nullptr;
@@ -1036,7 +1047,7 @@ int project(afmib_solver* s) {
     {
         ProfScope ps(s, P_GRAD_SUB, 7 * Ns);
         launch_grad_sub<double>(s->d, s->u, s->v, s->w, s->lv[0].x, s->d.channel ? s->wallgrad : nullptr, s->st,
-                                s->u32, s->v32, s->w32);
+                                s->u32, s->v32, s->w32, s->round_shadow, s->u32l, s->v32l, s->w32l);
     }
     CKL();
     return AFMIB_OK;
@@ -1048,7 +1059,16 @@ int substep(afmib_solver* s) {
     const Dims& d = s->d;
     const long long N = s->N();
     const double Ns = (double)N * sizeof(double);
-    if (s->mixed) {
+    if (s->mixed && s->advect64) {
+        // FP64 advection of the FP64 velocity, handed on in FP32
+        ProfScope ps(s, P_ADVECT, 6 * Ns + (double)N * 3 * 4, 4);
+        launch_advect<double, double>(d, s->adv[0], s->adv[1], s->adv[2], s->u, s->v, s->w, s->st);
+        for (int k = 0; k < 3; ++k) launch_convert<float, double>(N, s->adv32[k], s->adv[k], s->st);
+    } else if (s->mixed && s->u32l) {
+        ProfScope ps(s, P_ADVECT, (double)N * (6 * 4 + 3 * 4));
+        launch_advect_df(d, s->adv32[0], s->adv32[1], s->adv32[2], s->u32, s->u32l, s->v32, s->v32l, s->w32, s->w32l,
+                         s->st);
+    } else if (s->mixed) {
         ProfScope ps(s, P_ADVECT, (double)N * (3 * 4 + 3 * 4));
         launch_advect<float, float>(d, s->adv32[0], s->adv32[1], s->adv32[2], s->u32, s->v32, s->w32, s->st);
     } else {
@@ -1845,6 +1865,9 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_LAP_DF")) s->lap_df = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_SPREAD_DF")) s->spread_df = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_INTERP_DF")) s->interp_df = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_SHADOW_ROUND")) s->round_shadow = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_ADVECT64")) s->advect64 = std::string(e) == "1";
+    if (const char* e = std::getenv("AFMIB_ADVECT_DF")) s->advect_df = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_CN_START_OLD")) s->cn_start_old = std::string(e) != "0";
     if (s->mixed && s->fused_rhs)
         for (auto& q : s->qo) TRY(dalloc(s, &q, N));
@@ -1957,6 +1980,14 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
         CK(cudaMemsetAsync(s->u32, 0, N * sizeof(float), s->st));
         CK(cudaMemsetAsync(s->v32, 0, N * sizeof(float), s->st));
         CK(cudaMemsetAsync(s->w32, 0, N * sizeof(float), s->st));
+        if (s->advect_df && !s->advect64) {
+            TRY(dalloc(s, &s->u32l, N));
+            TRY(dalloc(s, &s->v32l, N));
+            TRY(dalloc(s, &s->w32l, N));
+            CK(cudaMemsetAsync(s->u32l, 0, N * sizeof(float), s->st));
+            CK(cudaMemsetAsync(s->v32l, 0, N * sizeof(float), s->st));
+            CK(cudaMemsetAsync(s->w32l, 0, N * sizeof(float), s->st));
+        }
         TRY(dalloc(s, &s->cg32_r, N));
         TRY(dalloc(s, &s->cg32_p, N));
         TRY(dalloc(s, &s->cg32_q, N));
@@ -2004,9 +2035,9 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
 // FP32 copy of the velocity for the mixed form's FP32 stencils
 int refresh_shadow(afmib_solver* s) {
     if (!s->mixed) return AFMIB_OK;
-    launch_shadow(s->N(), s->u32, s->u, s->st);
-    launch_shadow(s->N(), s->v32, s->v, s->st);
-    launch_shadow(s->N(), s->w32, s->w, s->st);
+    launch_shadow(s->N(), s->u32, s->u, s->st, s->round_shadow, s->u32l);
+    launch_shadow(s->N(), s->v32, s->v, s->st, s->round_shadow, s->v32l);
+    launch_shadow(s->N(), s->w32, s->w, s->st, s->round_shadow, s->w32l);
     CKL();
     return AFMIB_OK;
 }

@@ -16,6 +16,12 @@ float afmib_test_helm_residual(double b, double x0, const double* nb, const int*
 float afmib_test_lap_residual(double b, double x0, const double* nb, int nnb, int c, int k2) {
     return afmib::lap_residual_bfp(b, x0, nb, nnb, c, k2);
 }
+float afmib_test_df_round(double d) { return afmib::df_round(d); }
+void afmib_test_split_round(double d, float* hi, float* lo) {
+    const afmib::df2 r = afmib::df_split_round(d);
+    *hi = r.hi;
+    *lo = r.lo;
+}
 void afmib_test_split(double d, float* hi, float* lo) {
     const afmib::df2 r = afmib::df_split(d);
     *hi = r.hi;

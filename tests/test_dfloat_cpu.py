@@ -35,6 +35,9 @@ def lib(tmp_path_factory):
     L.afmib_test_split.argtypes = [ctypes.c_double, fp, fp]
     L.afmib_test_df_hi.argtypes = [ctypes.c_double]
     L.afmib_test_df_hi.restype = ctypes.c_float
+    L.afmib_test_df_round.argtypes = [ctypes.c_double]
+    L.afmib_test_df_round.restype = ctypes.c_float
+    L.afmib_test_split_round.argtypes = [ctypes.c_double, fp, fp]
     L.afmib_test_lap_update_df.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float, fp, ctypes.c_int,
                                            ctypes.c_float, ctypes.c_float, fp, fp]
     L.afmib_test_helm_update_df.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float, fp, ctypes.c_int,
@@ -218,3 +221,39 @@ def test_df_hi_truncates(lib):
         assert h == f or h == float(np.nextafter(np.float32(f), np.float32(0.0)))
     assert lib.afmib_test_df_hi(1e-45) == 0.0 and lib.afmib_test_df_hi(-0.0) == 0.0
     assert lib.afmib_test_df_hi(0.1) == float(np.float32(0.1)) or lib.afmib_test_df_hi(0.1) < 0.1
+
+
+def test_df_round_is_nearest(lib):
+    """df_round (the mixed form's FP32 velocity shadow, by integer
+    operations): the float nearest to the double over the float normal range
+    (the IEEE cast, except that exact ties go away from zero), carries into the
+    exponent included; zero below the range."""
+    rng = np.random.default_rng(9)
+    for _ in range(20000):
+        d = float(rng.standard_normal() * 10.0 ** rng.uniform(-30, 30))
+        r = lib.afmib_test_df_round(d)
+        assert r == float(np.float32(d)), d
+    # exact ties: away from zero (the cast rounds to even)
+    for m in (1.0 + 2.0 ** -24, 1.0 + 3.0 * 2.0 ** -24, -(1.0 + 2.0 ** -24)):
+        r = lib.afmib_test_df_round(m)
+        assert abs(r) > abs(m) and abs(r) - abs(m) == 2.0 ** -24
+    # carry into the exponent: just below 2 rounds to 2
+    assert lib.afmib_test_df_round(2.0 - 2.0 ** -30) == 2.0
+    assert lib.afmib_test_df_round(1e-45) == 0.0 and lib.afmib_test_df_round(-0.0) == 0.0
+
+
+def test_split_round_pair(lib):
+    """df_split_round (the mixed form's velocity pair for the FP32 advection):
+    hi is the nearest float, lo the rest, and hi + lo is d to 2^-46 of |d|
+    (exact rationals), over the float normal range; below 2^-80, where the
+    rest underflows, the truncated pair."""
+    rng = np.random.default_rng(10)
+    hi, lo = ctypes.c_float(), ctypes.c_float()
+    for _ in range(20000):
+        d = float(rng.standard_normal() * 10.0 ** rng.uniform(-25, 25))
+        lib.afmib_test_split_round(d, ctypes.byref(hi), ctypes.byref(lo))
+        if abs(d) >= 2.0 ** -79:
+            assert hi.value == float(np.float32(d))
+            assert abs(Fr(hi.value) + Fr(lo.value) - Fr(d)) <= abs(Fr(d)) * Fr(2) ** -46, d
+        else:  # the rest underflows: the truncated pair, within one float ulp
+            assert abs(Fr(hi.value) + Fr(lo.value) - Fr(d)) <= abs(Fr(d)) * Fr(2) ** -23, d
