@@ -7,6 +7,11 @@ The forward pass runs `nsteps` IB steps on the GPU (afmib_trajectory_forward,
 state checkpointed every `every` steps); the backward pass is the hand-written
 adjoint (afmib_trajectory_adjoint), which recomputes each segment from its
 checkpoint. The initial velocity is an input constant.
+
+A solver keeps the checkpoints of its latest forward pass only: each forward
+pass stamps the solver and its autograd node with a trajectory number, and a
+backward pass whose number is no longer the solver's raises instead of
+returning the gradient of a different trajectory.
 """
 from __future__ import annotations
 
@@ -23,6 +28,8 @@ class IBTrajectory(torch.autograd.Function):
         solver.set_velocity(*vel0)
         solver.set_marker_positions(X0.detach().to(torch.float64).contiguous())
         solver.trajectory_forward(int(nsteps), int(every))
+        solver._trajectory_id = getattr(solver, "_trajectory_id", 0) + 1
+        ctx.trajectory_id = solver._trajectory_id
         n = solver.ncell
         uN = torch.empty((3, n), dtype=torch.float64, device=dev)
         solver.get_velocity((uN[0], uN[1], uN[2]))
@@ -35,6 +42,9 @@ class IBTrajectory(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g_u, g_X):
         s = ctx.solver
+        if getattr(s, "_trajectory_id", None) != ctx.trajectory_id:
+            raise RuntimeError("the solver ran another forward trajectory since this one; its checkpoints are gone "
+                               "(run backward before the next forward on the same solver, or use two solvers)")
         dev = g_X.device if g_X is not None else g_u.device
         lam_u = g_u.contiguous() if g_u is not None else None
         lam_X = g_X.contiguous() if g_X is not None else None

@@ -7,16 +7,24 @@
 // implicit device synchronisation) is not acceptable. They still pass their
 // own x and b; the solve's own working vectors (r, p, q), the reduction
 // partials, the reduction ticket and the CG scalars live in the file-scope
-// array below, which the library reserves in every GPU's memory when the
-// library is loaded and holds until the process exits.
+// array below, which the GPU holds from the moment the library's device code
+// is loaded on it until the process exits.
 //
 // Limits and rules:
 //  - at most kNoAllocMaxCells cells (64^3); larger grids are rejected;
+//  - three-dimensional grids only (nx, ny, nz >= 2; a 2D grid is rejected);
 //  - periodic domain (any component) or channel components 0 and 2 (u, w);
 //    the channel v component needs a layout conversion buffer and is rejected;
 //  - the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (once per device, with that device current); make
-//    that first call before any stream capture;
+//    cudaGetSymbolAddress (once per device, with that device current). Under
+//    CUDA's lazy module loading (the default) that lookup is also what loads
+//    the library's device code on the device, which reserves the array: the
+//    first call therefore allocates, and may synchronise, once. A caller
+//    whose budget starts later makes one warm-up call (or loads eagerly,
+//    CUDA_MODULE_LOADING=EAGER) before it; every later call allocates
+//    nothing. Make that first call before any stream capture;
+//  - the address is kept per device for the life of the process: resetting a
+//    device (cudaDeviceReset) while the library is in use is not supported;
 //  - every call shares the one array, so calls that overlap on the GPU
 //    (different streams or host threads at the same time) race and must not
 //    be issued concurrently; the array keeps the last call's contents, and

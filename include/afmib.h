@@ -216,11 +216,17 @@ int afmib_interp(afmib_solver* s, int M, const double* X, const double* u, const
  * memory budget of its host framework, or inner loops that cannot take the
  * implicit synchronisation of an allocation. Same solve and stopping rule as
  * afmib_helmholtz_cg, on the caller's device buffers x (warm start, solution)
- * and b; its working vectors live in an array the library reserves on every
- * GPU (about 6.5 MB) for as long as it is loaded. Limit: nx*ny*nz <= 64^3
- * (larger -> AFMIB_ERR_CAPACITY); periodic, or channel components 0 and 2.
- * The first call on a device looks up the array's address: make it before any
- * stream capture. Calls that overlap on the GPU share the array and race. */
+ * and b; its working vectors live in a file-scope device array (about
+ * 6.5 MB) that every GPU holds once the library's device code is loaded on it,
+ * until the process exits. Limits: nx*ny*nz <= 64^3 (larger ->
+ * AFMIB_ERR_CAPACITY); 3D grids only (nx, ny, nz >= 2, else AFMIB_ERR_ARG);
+ * periodic, or channel components 0 and 2. The first call on a device looks up
+ * the array's address, which under CUDA's lazy module loading (the default)
+ * also loads the device code and so reserves the array: make one warm-up call
+ * (or set CUDA_MODULE_LOADING=EAGER) before the code that must not allocate,
+ * and before any stream capture; later calls allocate nothing. Calls that
+ * overlap on the GPU share the array and race. cudaDeviceReset while the
+ * library is in use is not supported (the address is kept per device). */
 int afmib_helmholtz_cg_noalloc(int nx, int ny, int nz, int n, int bc, int comp, double scale, double tol,
                                int max_iters, double* x, const double* b, int* iters, void* stream);
 

@@ -138,3 +138,24 @@ def test_adjoint_with_bending_matches_finite_differences():
         worst = max(worst, abs(fd - ad) / max(abs(fd), 1e-30))
     sv.close()
     assert worst < 1e-6, worst
+
+
+def test_backward_of_a_superseded_trajectory_raises():
+    """A solver keeps only its latest forward trajectory's checkpoints: the
+    backward pass of an earlier one raises instead of returning the gradient
+    of the later trajectory."""
+    from afmibins_gb300.autograd import ib_trajectory, membrane_loss
+    n = 16
+    X, nstart, nidx, vel = _case(n)
+    sv, vel0 = _setup(n, X, nstart, nidx, vel)
+    dev = torch.device("cuda")
+    X0 = torch.tensor(X, device=dev, requires_grad=True)
+    k = torch.tensor(0.5, dtype=torch.float64, device=dev, requires_grad=True)
+    uN, XN = ib_trajectory(k, X0, sv, vel0, 2, 1)
+    L1 = membrane_loss(uN, XN, X0, 1.0 / n ** 3)
+    uN2, XN2 = ib_trajectory(k, X0, sv, vel0, 2, 1)
+    with pytest.raises(RuntimeError, match="another forward trajectory"):
+        L1.backward()
+    membrane_loss(uN2, XN2, X0, 1.0 / n ** 3).backward()  # the latest one still differentiates
+    assert torch.isfinite(k.grad)
+    sv.close()

@@ -49,6 +49,33 @@ def test_noalloc_cg_matches_solver_cg_twice(bc, comp):
         assert np.max(np.abs(x - x_ref)) <= 1e-10 * np.max(np.abs(x_ref))
 
 
+def test_noalloc_capacity_edge_allocates_nothing_after_first_call():
+    """At the largest grid the array holds (64^3) the solve still matches the
+    solver path, and once the first call has loaded the array, later calls
+    leave the device's free memory unchanged."""
+    lib = capi.load()
+    n, scale, tol = 64, -0.05, 1e-12
+    rng = np.random.default_rng(64)
+    b = rng.standard_normal(n ** 3)
+    x0 = np.zeros(n ** 3)
+    with capi.Solver(n, tol=tol) as sv:
+        x_ref, it_ref = sv.helmholtz_cg(0, scale, x0, b)
+    dev = torch.device("cuda")
+    bd = torch.tensor(b, dtype=torch.float64, device=dev)
+    xs = [torch.zeros(n ** 3, dtype=torch.float64, device=dev) for _ in range(2)]
+    st, _ = _noalloc(lib, n, capi.BC_PERIODIC, 0, scale, tol, xs[0], bd)  # warm-up: loads the array
+    assert st == capi.AFMIB_OK
+    xs[0].zero_()
+    for xd in xs:
+        free0, _ = torch.cuda.mem_get_info()
+        st, it = _noalloc(lib, n, capi.BC_PERIODIC, 0, scale, tol, xd, bd)
+        free1, _ = torch.cuda.mem_get_info()
+        assert st == capi.AFMIB_OK and it == it_ref
+        assert free1 == free0
+        x = xd.cpu().numpy()
+        assert np.max(np.abs(x - x_ref)) <= 1e-10 * np.max(np.abs(x_ref))
+
+
 def test_noalloc_rejects_oversize_and_channel_v():
     lib = capi.load()
     dev = torch.device("cuda")
@@ -56,4 +83,8 @@ def test_noalloc_rejects_oversize_and_channel_v():
     st, _ = _noalloc(lib, 128, capi.BC_PERIODIC, 0, -0.05, 1e-12, xd, xd)
     assert st == capi.AFMIB_ERR_CAPACITY
     st, _ = _noalloc(lib, 16, capi.BC_CHANNEL, 1, -0.05, 1e-12, xd, xd)
+    assert st == capi.AFMIB_ERR_ARG
+    it = ctypes.c_int(-1)  # a 2D grid (nz = 1) is rejected
+    st = lib.afmib_helmholtz_cg_noalloc(16, 16, 1, 16, capi.BC_PERIODIC, 0, -0.05, 1e-12, 100, xd.data_ptr(),
+                                        xd.data_ptr(), ctypes.byref(it), None)
     assert st == capi.AFMIB_ERR_ARG
