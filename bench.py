@@ -107,6 +107,64 @@ NCU_TRAFFIC = {
 }
 
 
+# Algorithmic FP64 operations per byte of the FP64 form's stencil families
+# (the bytes are the families' algorithmic bytes, s = 8): red-black sweep 8
+# flops per updated cell over 24 bytes (x, b read, x written); residual 9 over
+# 24; Helmholtz apply / defect 10 over 16 / 24; restriction 128 flops per
+# coarse cell over 9 bytes of fine and coarse data per fine cell; prolongation
+# 12 flops per fine cell over 17 bytes; divergence 8 over 32; gradient-subtract
+# 9 over 56.
+FP64_FLOPS_PER_BYTE = {"mg_rbgs_fine": 8 / 24, "mg_rbgs": 8 / 24, "mg_residual_fine": 9 / 24,
+                       "mg_residual": 9 / 24, "cg_apply": 10 / 16, "helm_defect_fp64": 10 / 24,
+                       "mg_restrict_fine": 16 / 9, "mg_restrict": 16 / 9, "mg_prolong_add_fine": 12 / 17,
+                       "mg_prolong_add": 12 / 17, "div": 8 / 32, "grad_sub": 9 / 56}
+
+
+def fp64_peak_dgemm(torch):
+    """FP64 FLOP/s of cuBLAS DGEMM (4096^3, best of 5, CUDA events): the FP64
+    pipe's throughput, the bound of the FP64 form's stencils on GB300."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = None
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) * 1e-3
+        best = t if best is None else min(best, t)
+    del a, b
+    torch.cuda.empty_cache()
+    return 2.0 * n ** 3 / best
+
+
+def fp64_form_profile(sv, steps, torch):
+    """Per-family times of the FP64 form over `steps` profiled IB steps and its
+    dominant stencil family's FP64 rate against the measured DGEMM rate."""
+    sv.profile(True)
+    sv.profile_reset()
+    for _ in range(steps):
+        sv.ib_step(1)
+    table = sv.profile_table()
+    sv.profile(False)
+    total = sum(v[1] for v in table.values())
+    top = sorted(table.items(), key=lambda kv: -kv[1][1])[:10]
+    out = {"kernels": {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / total, 4)} for k, v in top}}
+    fam = next((k for k, _ in top if k in FP64_FLOPS_PER_BYTE), None)
+    if fam is not None:
+        nl, kms, kbytes = table[fam]
+        rate = kbytes * FP64_FLOPS_PER_BYTE[fam] / (kms * 1e-3)
+        # the peak is measured at the end of the run (fp64_peak_dgemm), after every timed region
+        out["fp64_roofline"] = {"bound": "fp64 pipe", "kernel": fam, "achieved": round(rate / 1e12, 4),
+                                "peak": None, "unit": "TFLOP/s", "frac": None,
+                                "peak_kind": "cuBLAS DGEMM 4096^3 measured in this run",
+                                "hbm_GB_s": round(kbytes / (kms * 1e-3) / 1e9, 1)}
+    return out
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -602,6 +660,8 @@ def main():
         X64 = sv64.get_markers()
         fp64 = {"value": world * args.steps / (ms64 / 1000.0), "ms_per_step": ms64 / args.steps,
                 "gpu_launches": int(l64), "proj_start": "zero (the reference's)"}
+        if args.profile_steps > 0:
+            fp64.update(fp64_form_profile(sv64, args.profile_steps, torch))
         sv64.close()
         barrier()
         sv64, ms64w, l64w, _, _ = run_form(capi, torch, args, capi.FP64, state, dev, stream, capi.START_WARM)
@@ -688,6 +748,12 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         csec, ck, cw, cores, desc = cpu_run(args, 1, 1)
         cpu = {"value": 1.0 / csec, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+
+    if fp64 is not None and fp64.get("fp64_roofline"):
+        peak64 = fp64_peak_dgemm(torch)
+        r = fp64["fp64_roofline"]
+        r["peak"] = round(peak64 / 1e12, 4)
+        r["frac"] = round(r["achieved"] * 1e12 / peak64, 4)
 
     if rank == 0:
         line = {
