@@ -113,10 +113,10 @@ __device__ __forceinline__ int tid_lin() { return threadIdx.x + blockDim.x * (th
 __device__ __forceinline__ int bid_lin() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
 __device__ __forceinline__ int nblk_lin() { return gridDim.x * gridDim.y * gridDim.z; }
 
-// Block-wide sum of NV values (kRedBlock threads per block); result valid in thread 0.
-template <int NV>
+// Block-wide sum of NV values (TB threads per block); result valid in thread 0.
+template <int NV, int TB = kRedBlock>
 __device__ __forceinline__ void block_sum(double (&v)[NV]) {
-    __shared__ double s[kRedBlock / 32][NV];
+    __shared__ double s[TB / 32][NV];
     warp_sum<NV>(v);
     const int w = tid_lin() >> 5, l = tid_lin() & 31;
     if (l == 0)
@@ -125,7 +125,7 @@ __device__ __forceinline__ void block_sum(double (&v)[NV]) {
     __syncthreads();
     if (w == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) v[k] = (l < kRedBlock / 32) ? s[l][k] : 0.0;
+        for (int k = 0; k < NV; ++k) v[k] = (l < TB / 32) ? s[l][k] : 0.0;
         warp_sum<NV>(v);
     }
     __syncthreads();

@@ -872,14 +872,14 @@ __global__ void k_prolong(Dims d, T* __restrict__ fine, const T* __restrict__ co
 // Coarsest level, src/mg/solver.h:264-271: remove the mean of b, then CG
 // warm-started from b with the absolute 2-norm stop. One block; the level is
 // a handful of cells (one cell for a cube).
-template <typename T>
+template <typename T, int TB = kRedBlock>
 __device__ void coarse_cg_block(const Dims& d, T* xv, T* b, T* r, T* p, T* q, double tol, int maxit, int* status) {
     const long long N = d.ncell(), sxy = d.sxy();
     const T off = T(d.n) * T(d.n);
     __shared__ double s_val;
     auto bsum = [&](double v) {
         double a[1] = {v};
-        block_sum<1>(a);
+        block_sum<1, TB>(a);
         if (threadIdx.x == 0) s_val = a[0];
         __syncthreads();
         return s_val;
@@ -951,6 +951,11 @@ __global__ void __launch_bounds__(kRedBlock) k_coarse_cg(Dims d, T* __restrict__
 // solve is the same one-block CG, so the result equals the launch-by-launch
 // V-cycle bit for bit.
 // ---------------------------------------------------------------------------
+// threads of the one-block tail: its phases on a 16^3 level are 2048 to 4096
+// cells, so twice the reduction block size halves each phase's per-thread
+// loop (1024 threads cap the registers at 64 and spill)
+constexpr int kTailThreads = 512;
+
 // cell index -> (x, y, z) for the tail's small levels (32-bit arithmetic)
 __device__ __forceinline__ void tail_xyz(const Dims& d, int i, int& x, int& y, int& z) {
     const int sxy = d.nx * d.ny;
@@ -1005,8 +1010,8 @@ __device__ __forceinline__ void tail_sweep2(const Dims& d, const Ix2& I, T* x, c
 // and acquire the phase's global writes, separate the phases). The coarsest
 // solve runs in the cluster's first CTA, the same one-block CG, so the result
 // is the one-block tail's, bit for bit; the levels stay in global memory (L2).
-template <typename T, bool CL>
-__global__ void __launch_bounds__(kRedBlock) k_vcycle_tail(TailLevels<T> g, int staged) {
+template <typename T, bool CL, int TB = kRedBlock>
+__global__ void __launch_bounds__(TB) k_vcycle_tail(TailLevels<T> g, int staged) {
     extern __shared__ __align__(16) unsigned char tsm[];
     TailLevels<T> a = g;
     int t0 = threadIdx.x, ts = blockDim.x;
@@ -1098,11 +1103,11 @@ __global__ void __launch_bounds__(kRedBlock) k_vcycle_tail(TailLevels<T> g, int 
         const Dims& d = a.d[l];
         const long long n = d.ncell();
         if constexpr (sizeof(T) == sizeof(double)) {
-            coarse_cg_block(d, a.x[l], a.b[l], a.r[l], a.cw_p, a.cw_q, a.tol, a.maxit, a.status);
+            coarse_cg_block<T, TB>(d, a.x[l], a.b[l], a.r[l], a.cw_p, a.cw_q, a.tol, a.maxit, a.status);
         } else {
             for (long long i = threadIdx.x; i < n; i += blockDim.x) a.cb64[i] = (double)a.b[l][i];
             __syncthreads();
-            coarse_cg_block(d, a.cx64, a.cb64, a.cr64, a.cw_p, a.cw_q, a.tol, a.maxit, a.status);
+            coarse_cg_block<double, TB>(d, a.cx64, a.cb64, a.cr64, a.cw_p, a.cw_q, a.tol, a.maxit, a.status);
             __syncthreads();
             for (long long i = threadIdx.x; i < n; i += blockDim.x) a.x[l][i] = (T)a.cx64[i];
         }
@@ -1371,8 +1376,33 @@ void launch_vcycle_tail(const TailLevels<T>& a, cudaStream_t s, int cluster) {
         bytes = (bytes + 15) & ~(size_t)15;
     }
     bytes += (size_t)5 * a.d[a.nlev - 1].ncell() * sizeof(double);
+    // one block of kTailThreads (AFMIB_TAIL_THREADS=256 or 1024 instead):
+    // the phases are per-cell and the coarsest CG sums the same cells in the
+    // same order, so the block size does not change the result
     constexpr size_t kMax = 160 * 1024;
-    static bool attr = false;
+    // read at every launch (graphs capture it once), so that a test can compare block sizes
+    const int threads = [] {
+        const char* e = std::getenv("AFMIB_TAIL_THREADS");
+        const int v = e ? std::atoi(e) : kTailThreads;
+        return v == 1024 || v == kRedBlock ? v : kTailThreads;
+    }();
+    static bool attr = false, attr_big = false, attr_1k = false;
+    if (threads == kTailThreads) {
+        if (!attr_big)
+            attr_big = cudaFuncSetAttribute(k_vcycle_tail<T, false, kTailThreads>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMax) == cudaSuccess;
+        if (attr_big && bytes <= kMax) k_vcycle_tail<T, false, kTailThreads><<<1, kTailThreads, bytes, s>>>(a, 1);
+        else k_vcycle_tail<T, false, kTailThreads><<<1, kTailThreads, 0, s>>>(a, 0);
+        return;
+    }
+    if (threads == 1024) {
+        if (!attr_1k)
+            attr_1k = cudaFuncSetAttribute(k_vcycle_tail<T, false, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)kMax) == cudaSuccess;
+        if (attr_1k && bytes <= kMax) k_vcycle_tail<T, false, 1024><<<1, 1024, bytes, s>>>(a, 1);
+        else k_vcycle_tail<T, false, 1024><<<1, 1024, 0, s>>>(a, 0);
+        return;
+    }
     if (!attr)
         attr = cudaFuncSetAttribute(k_vcycle_tail<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMax) ==
                cudaSuccess;

@@ -239,13 +239,14 @@ int main(int argc, char** argv) {
         for (unsigned i = 0; i < NM; ++i) put(lx[i]);
         for (unsigned i = 0; i < NM; ++i) put(ly[i]);
         for (unsigned i = 0; i < NM; ++i) put(lz[i]);
-    } else if (cmd == "ib") {
+    } else if (cmd == "ib" || cmd == "ibw") {
         // The immersed-boundary step the reference leaves as comments in
         // test/ib_ns_test.cc:73-96, assembled from the reference pieces
         // (ns::solver::step, ib::grid::interpolate) plus linear springs.
         // in: mu, rho, dt, tol, k, nsteps, u0[NC], v0[NV], w0[NC], X[NM*3],
         //     deg[NM], nbr[NM*6] (unused slots -1)
-        // out: u, v, w, p, X[NM*3]
+        //     ibw: then the wall velocities ut, ub, wt, wb [NXZ each]
+        // out: u, v, w, p, X[NM*3]; ibw: then ut, ub, wt, wb
         double mu = take(), rho = take(), dt_ = take(), tol = take(), k = take();
         unsigned nsteps = (unsigned)take();
         dt::vector<NC> u0, w0;
@@ -257,6 +258,7 @@ int main(int argc, char** argv) {
         for (auto& e : deg) e = (int)take();
         for (auto& e : nbr) e = (int)take();
         dt::vector<NXZ> ut, ub, wt, wb;
+        if (cmd == "ibw") { take(ut); take(ub); take(wt); take(wb); }
         ns::solver<G> s(mu, rho, dt_, tol, u0, v0, w0);
         std::vector<double> ones(NM, 1.0);
         auto points = [&](const std::vector<double>& P) {
@@ -307,6 +309,7 @@ int main(int argc, char** argv) {
         }
         put(u0); put(v0); put(w0); put(s.get_p());
         for (double e : X) put(e);
+        if (cmd == "ibw") { put(ut); put(ub); put(wt); put(wb); }
     } else {
         std::fprintf(stderr, "unknown command %s\n", cmd.c_str());
         return 2;

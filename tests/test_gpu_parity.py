@@ -436,19 +436,25 @@ def test_multigrid_tail_equals_level_launches(monkeypatch, bc, precision, n):
     """The V-cycle tail (in one block from 16^3, or on a thread-block cluster
     from 32^3 with AFMIB_MG_TAIL_CLUSTER=16) runs the per-cell functions of the
     level kernels and the same coarsest-level CG: multigrid solves agree bit
-    for bit with the launch-by-launch V-cycle, and repeat bit for bit."""
+    for bit with the launch-by-launch V-cycle, and repeat bit for bit, with
+    the one-block tail on 256, 512 (the default) or 1024 threads."""
     b = np.random.default_rng(23).standard_normal(n ** 3)
     out = {}
-    for mode, tail, cluster in (("levels", "0", None), ("cluster", "1", "16"), ("cluster2", "1", "16"),
-                                ("block", "1", None)):
+    for mode, tail, cluster, threads in (("levels", "0", None, None), ("cluster", "1", "16", None),
+                                         ("cluster2", "1", "16", None), ("block", "1", None, None),
+                                         ("block256", "1", None, "256"), ("block1024", "1", None, "1024")):
         monkeypatch.setenv("AFMIB_MG_TAIL", tail)
         if cluster:
             monkeypatch.setenv("AFMIB_MG_TAIL_CLUSTER", cluster)
         else:
             monkeypatch.delenv("AFMIB_MG_TAIL_CLUSTER", raising=False)
+        if threads:
+            monkeypatch.setenv("AFMIB_TAIL_THREADS", threads)
+        else:
+            monkeypatch.delenv("AFMIB_TAIL_THREADS", raising=False)
         with capi.Solver(n, bc=bc, precision=precision, tol=1e-10) as sv:
             out[mode] = sv.mg_solve(b)
-    for mode in ("cluster", "cluster2", "block"):
+    for mode in ("cluster", "cluster2", "block", "block256", "block1024"):
         assert out[mode][1] == out["levels"][1]
         assert np.array_equal(out[mode][0], out["levels"][0])
 
@@ -838,3 +844,50 @@ def test_fused_residual_restriction_keeps_bits(monkeypatch, bc, precision):
             res[mode] = (*sv.get_velocity(), sv.get_pressure(), sv.get_markers())
     for a, c in zip(res["0"], res["1"]):
         assert np.array_equal(a, c)
+
+
+@pytest.mark.parametrize("precision,bar", [(capi.FP64, TOL), (capi.MIXED, 1e-8)])
+def test_ns_substeps_moving_walls(golden, precision, bar):
+    """Four channel sub-steps with seeded nonzero wall velocities (ut, ub, wt,
+    wb: the wall terms of the Helmholtz right-hand sides and the reference's
+    wall update, src/ns/helmholtz.h:177-196, src/ns/projection.h:75-122)
+    against the compiled reference: fields, pressure and updated walls."""
+    d = golden("ns_walls_16")
+    n, nxz = 16, 16 * 16
+    w0 = d["walls0"]
+    with capi.Solver(n, bc=capi.BC_CHANNEL, precision=precision, mu=float(d["mu"]), rho=float(d["rho"]),
+                     dt=float(d["dt"]), tol=float(d["tol"])) as sv:
+        sv.set_velocity(d["u0"], d["v0"], d["w0"])
+        sv.set_walls(w0[:nxz], w0[nxz:2 * nxz], w0[2 * nxz:3 * nxz], w0[3 * nxz:])
+        sv.project()
+        for _ in range(int(d["substeps"])):
+            sv.ns_step(d["fx"], d["fy"], d["fz"])
+        u, v, w = sv.get_velocity()
+        p = sv.get_pressure()
+        walls = np.concatenate(sv.get_walls())
+    assert rel(u, d["u"]) < bar and rel(v, d["v"]) < bar and rel(w, d["w"]) < bar
+    g = po.Grid(n, n, n, n, channel=True)
+    assert pressure_rel(p, d["p"], g, float(d["mu"]), float(d["rho"]), float(d["dt"])) < bar
+    assert rel(walls, d["walls"]) < bar
+
+
+@pytest.mark.parametrize("precision,bar", [(capi.FP64, TOL), (capi.MIXED, 1e-8)])
+def test_ib_steps_moving_walls(golden, precision, bar):
+    """Two channel IB steps of a 320-marker shell with moving walls against the
+    compiled reference (fields, markers, walls)."""
+    d = golden("ib_walls_16")
+    n, nxz = 16, 16 * 16
+    w0 = d["walls0"]
+    with capi.Solver(n, bc=capi.BC_CHANNEL, precision=precision, mu=float(d["mu"]), rho=float(d["rho"]),
+                     dt=float(d["dt"]), tol=float(d["tol"]), k_spring=float(d["k"])) as sv:
+        sv.set_velocity(d["u0"], d["v0"], d["w0"])
+        sv.set_walls(w0[:nxz], w0[nxz:2 * nxz], w0[2 * nxz:3 * nxz], w0[3 * nxz:])
+        sv.project()
+        sv.set_markers(d["X"], d["nstart"], d["nidx"])
+        sv.ib_step(int(d["steps"]))
+        u, v, w = sv.get_velocity()
+        X = sv.get_markers()
+        walls = np.concatenate(sv.get_walls())
+    assert rel(u, d["u"]) < bar and rel(v, d["v"]) < bar and rel(w, d["w"]) < bar
+    assert rel(X - d["X"], d["Xout"] - d["X"]) < bar
+    assert rel(walls, d["walls"]) < bar

@@ -97,3 +97,53 @@ def test_ib_steps_periodic_256_against_oracle_digest():
     disp = d["X_val"] - d["X0_val"]
     err["X"] = float(np.max(np.abs(X[midx] - d["X_val"])) / np.max(np.abs(disp)))
     assert max(err.values()) < 1e-10, err
+
+
+FIXTURE_WALLS = os.path.join(HERE, "golden", "ib_channel_256_digest.npz")
+
+
+@pytest.mark.skipif(not os.path.exists(FIXTURE_WALLS), reason="no 256^3 channel IB digest fixture")
+def test_ib_steps_channel_moving_walls_256_against_reference_digest():
+    """The reference's own channel domain at 256^3 with moving walls and a
+    5,120-marker shell: two IB steps of the FP64 form against the digest of
+    the compiled reference (tests/golden/make_golden_walls.py). Velocity at
+    4096 seeded cells per component and by its sums, pressure after fitting
+    the null-space constant, the updated walls and every marker position.
+    Bar 1e-10 of each field's largest magnitude (marker displacement for the
+    positions)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden_walls",
+                                                  os.path.join(HERE, "golden", "make_golden_walls.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    d = np.load(FIXTURE_WALLS)
+    n = int(d["n"])
+    X0, nstart, nidx, u, v, w, walls0 = gen.inputs_256(n)
+    for name, a in (("u", u), ("v", v), ("w", w)):
+        assert abs(float((a * a).sum()) - float(d[f"in_{name}_sumsq"])) <= 1e-12 * float(d[f"in_{name}_sumsq"])
+    nxz = n * n
+    mu, rho, dt = float(d["mu"]), float(d["rho"]), float(d["dt"])
+    with capi.Solver(n, bc=capi.BC_CHANNEL, mu=mu, rho=rho, dt=dt, tol=float(d["tol"]), k_spring=float(d["k"]),
+                     max_cg_iters=20000, max_mg_cycles=2000) as sv:
+        sv.set_velocity(u, v, w)
+        sv.set_walls(walls0[:nxz], walls0[nxz:2 * nxz], walls0[2 * nxz:3 * nxz], walls0[3 * nxz:])
+        sv.project()
+        sv.set_markers(X0, nstart, nidx)
+        sv.ib_step(int(d["steps"]))
+        gu, gv, gw = sv.get_velocity()
+        gp = sv.get_pressure()
+        X = sv.get_markers()
+        walls = np.concatenate(sv.get_walls())
+        h1 = sv.helm_apply(0, -mu * dt / (2 * rho), np.ones(n ** 3))
+    err = {}
+    for name, a in (("u", gu), ("v", gv), ("w", gw)):
+        scale = float(d[name + "_max"])
+        err[name] = float(np.max(np.abs(a[d[name + "_idx"]] - d[name + "_val"])) / scale)
+        err[name + "_sum"] = abs(float(a.sum()) - float(d[name + "_sum"])) / (scale * a.size ** 0.5)
+    idx = d["p_idx"]
+    dlt = gp[idx] - d["p_val"]
+    c = float(dlt @ h1[idx] / (h1[idx] @ h1[idx]))
+    err["p"] = float(np.max(np.abs(gp[idx] - c * h1[idx] - d["p_val"])) / float(d["p_max"]))
+    err["walls"] = float(np.max(np.abs(walls - d["walls"])) / np.max(np.abs(d["walls"])))
+    err["X"] = float(np.max(np.abs(X - d["X"])) / np.max(np.abs(d["X"] - X0)))
+    assert max(err.values()) < 1e-10, err
