@@ -8,6 +8,12 @@ state checkpointed every `every` steps); the backward pass is the hand-written
 adjoint (afmib_trajectory_adjoint), which recomputes each segment from its
 checkpoint. The initial velocity is an input constant.
 
+The solver runs on its own CUDA stream, which does not wait for torch's: the
+tensors handed to it (X0, the cotangents, the gradient buffer torch fills
+with zeros) are produced by torch kernels that may still be running, so each
+pass synchronises torch's current stream before it calls the C ABI. The C ABI
+calls return once their results are written.
+
 A solver keeps the checkpoints of its latest forward pass only: each forward
 pass stamps the solver and its autograd node with a trajectory number, and a
 backward pass whose number is no longer the solver's raises instead of
@@ -20,13 +26,21 @@ import torch
 from . import capi
 
 
+def _torch_done(dev):
+    """Wait for the work torch has queued on its current stream of `dev`."""
+    if dev.type == "cuda":
+        torch.cuda.current_stream(dev).synchronize()
+
+
 class IBTrajectory(torch.autograd.Function):
     @staticmethod
     def forward(ctx, k, X0, solver, vel0, nsteps, every):
         dev = X0.device
+        X0c = X0.detach().to(torch.float64).contiguous()
+        _torch_done(dev)
         solver.set_spring(float(k))
         solver.set_velocity(*vel0)
-        solver.set_marker_positions(X0.detach().to(torch.float64).contiguous())
+        solver.set_marker_positions(X0c)
         solver.trajectory_forward(int(nsteps), int(every))
         solver._trajectory_id = getattr(solver, "_trajectory_id", 0) + 1
         ctx.trajectory_id = solver._trajectory_id
@@ -49,6 +63,7 @@ class IBTrajectory(torch.autograd.Function):
         lam_u = g_u.contiguous() if g_u is not None else None
         lam_X = g_X.contiguous() if g_X is not None else None
         gX0 = torch.zeros((s.M, 3), dtype=torch.float64, device=dev)
+        _torch_done(dev)  # the cotangents and the zeroed buffer are written before the solver reads them
         _, gk, _ = s.trajectory_adjoint(lam_u[0] if lam_u is not None else None,
                                         lam_u[1] if lam_u is not None else None,
                                         lam_u[2] if lam_u is not None else None,

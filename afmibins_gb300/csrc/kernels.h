@@ -138,6 +138,8 @@ void launch_fill(long long n, T* x, T value, cudaStream_t s);
 template <typename T>
 void launch_axpy(long long n, T* y, const T* x, T a, cudaStream_t s);  // y += a x
 template <typename T>
+void launch_scale(long long n, T* x, T a, cudaStream_t s);  // x *= a
+template <typename T>
 void launch_lincomb(long long n, T* y, T a, const T* x, T b, const T* z, cudaStream_t s);  // y = a x + b z
 // FP32 shadow of an FP64 field, as the projection writes it (rounded to
 // nearest by df_round, or truncated by df_hi)

@@ -831,6 +831,12 @@ __global__ void k_lincomb(long long N, T* __restrict__ y, T a, const T* __restri
         y[i] = a * x[i] + b * z[i];
 }
 
+template <typename T>
+__global__ void k_scale(long long N, T* __restrict__ x, T a) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
+        x[i] = a * x[i];
+}
+
 template <typename TO, typename TI>
 __global__ void k_convert(long long N, TO* __restrict__ o, const TI* __restrict__ in) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
@@ -1226,6 +1232,10 @@ void launch_axpy(long long n, T* y, const T* x, T a, cudaStream_t s) {
     k_axpy<T><<<ew_blocks(n), 256, 0, s>>>(n, y, x, a);
 }
 template <typename T>
+void launch_scale(long long n, T* x, T a, cudaStream_t s) {
+    k_scale<T><<<ew_blocks(n), 256, 0, s>>>(n, x, a);
+}
+template <typename T>
 void launch_lincomb(long long n, T* y, T a, const T* x, T b, const T* z, cudaStream_t s) {
     k_lincomb<T><<<ew_blocks(n), 256, 0, s>>>(n, y, a, x, b, z);
 }
@@ -1264,6 +1274,7 @@ void launch_shadow(long long n, float* out, const double* in, cudaStream_t s, in
     template void launch_cg_update<T>(long long, T*, T*, const T*, const T*, RedScratch, double*, cudaStream_t); \
     template void launch_cg_direction<T>(long long, T*, const T*, const double*, cudaStream_t);                \
     template void launch_sum<T>(long long, const T*, RedScratch, double*, cudaStream_t);                       \
+    template void launch_scale<T>(long long, T*, T, cudaStream_t);                                          \
     template void launch_sumsq<T>(long long, const T*, RedScratch, double*, cudaStream_t);                     \
     template void launch_sub_scalar_scaled<T>(long long, T*, const double*, double, cudaStream_t);             \
     template void launch_fill<T>(long long, T*, T, cudaStream_t);                                              \

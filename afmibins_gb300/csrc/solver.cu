@@ -182,7 +182,7 @@ struct afmib_solver {
     bool phi_valid2[2] = {false, false};
     int proj_phase = -1;  // phase of the projection in progress (-1: none)
     RedScratch red{};
-    double* scal = nullptr;   // device scalars: [0..4] CG, [8] sum, [9] sumsq
+    double* scal = nullptr;   // device scalars: [0..4] CG, [8] sum, [9] sumsq, [16..17] adjoint scale
     double* hscal = nullptr;  // pinned mirror
     int* dflag = nullptr;     // device status flags [0] markers, [1] coarse solve, [3] pipelined smoother
     int* hflag = nullptr;
@@ -1729,6 +1729,25 @@ int traj_adjoint(afmib_solver* s, const double* lu, const double* lv, const doub
     TRY(copy_in(s, L + N, lv, N));
     TRY(copy_in(s, L + 2 * N, lw, N));
     TRY(copy_in(s, s->lamX, lX, 3 * (long long)M));
+    // The adjoint is linear in (lam_u, lam_X), but its solves stop on the
+    // forward's absolute tolerances, which only mean something for fields of
+    // the forward's magnitude: a loss term like h^3 |u|^2 gives cotangents of
+    // order h^3 (1e-9 at 512^3), against which a tolerance of 1e-10 is no
+    // convergence at all. So the cotangents are scaled to unit RMS on the way
+    // in and the gradients scaled back on the way out.
+    launch_sumsq<double>(3 * N, L, s->red, s->scal + 16, s->st);
+    launch_sumsq<double>(3 * (long long)M, s->lamX, s->red, s->scal + 17, s->st);
+    CKL();
+    TRY(read_scalars(s, 16, 2));
+    const double rms = std::max(std::sqrt(s->hscal[16] / (3.0 * (double)N)),
+                                M > 0 ? std::sqrt(s->hscal[17] / (3.0 * (double)M)) : 0.0);
+    const char* es = std::getenv("AFMIB_ADJ_SCALE");  // 0: unscaled (for comparison)
+    const bool scale_on = !(es && es[0] == '0');
+    const double sigma = (scale_on && rms > 0.0 && std::isfinite(rms)) ? 1.0 / rms : 1.0;
+    if (sigma != 1.0) {
+        launch_scale<double>(3 * N, L, sigma, s->st);
+        launch_scale<double>(3 * (long long)M, s->lamX, sigma, s->st);
+    }
     double lam_k = 0.0;
     const bool warm = s->warm_start;
     s->warm_start = false;
@@ -1753,6 +1772,11 @@ int traj_adjoint(afmib_solver* s, const double* lu, const double* lv, const doub
     TRY(copy_vel_in(s, s->fin_vel));
     CK(cudaMemcpyAsync(s->X, s->fin_X, mb, cudaMemcpyDeviceToDevice, s->st));
     s->half = half_saved;
+    if (sigma != 1.0) {
+        launch_scale<double>(3 * N, L, 1.0 / sigma, s->st);
+        launch_scale<double>(3 * (long long)M, s->lamX, 1.0 / sigma, s->st);
+        lam_k /= sigma;
+    }
     TRY(copy_out(s, gX0, s->lamX, 3 * (long long)M));
     TRY(copy_out(s, gu0, L, N));
     TRY(copy_out(s, gv0, L + N, N));
@@ -1884,9 +1908,9 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     TRY(dalloc(s, &s->cg_q, N));
     TRY(dalloc(s, &s->red.partial, (size_t)kMaxRedBlocks * kMaxRedVals));
     TRY(dalloc(s, &s->red.ticket, 1));
-    TRY(dalloc(s, &s->scal, 16));
+    TRY(dalloc(s, &s->scal, 24));
     TRY(dalloc(s, &s->dflag, 4));
-    CK(cudaMallocHost((void**)&s->hscal, 16 * sizeof(double)));
+    CK(cudaMallocHost((void**)&s->hscal, 24 * sizeof(double)));
     CK(cudaMallocHost((void**)&s->hflag, 4 * sizeof(int)));
     CK(cudaMemsetAsync(s->red.ticket, 0, sizeof(unsigned), s->st));
     CK(cudaMemsetAsync(s->dflag, 0, 4 * sizeof(int), s->st));

@@ -159,3 +159,25 @@ def test_backward_of_a_superseded_trajectory_raises():
     membrane_loss(uN2, XN2, X0, 1.0 / n ** 3).backward()  # the latest one still differentiates
     assert torch.isfinite(k.grad)
     sv.close()
+
+
+def test_adjoint_repeats_bit_for_bit():
+    """The same trajectory differentiated three times in one process gives the
+    same gradients bit for bit: the wrapper waits for torch's kernels (the
+    cotangents, the zeroed gradient buffer) before the solver, on its own
+    stream, reads them."""
+    from afmibins_gb300.autograd import ib_trajectory, membrane_loss
+    n = 32
+    X, nstart, nidx, vel = _case(n, M=600)
+    dev = torch.device("cuda")
+    out = []
+    for _ in range(3):
+        sv, vel0 = _setup(n, X, nstart, nidx, vel, capi.MIXED)
+        X0 = torch.tensor(X, device=dev, requires_grad=True)
+        k = torch.tensor(0.5, dtype=torch.float64, device=dev, requires_grad=True)
+        uN, XN = ib_trajectory(k, X0, sv, vel0, 4, 2)
+        membrane_loss(uN, XN, X0, 1.0 / n ** 3).backward()
+        out.append((float(k.grad), X0.grad.cpu().numpy()))
+        sv.close()
+    for gk, gX in out[1:]:
+        assert gk == out[0][0] and np.array_equal(gX, out[0][1])

@@ -867,7 +867,11 @@ def test_ns_substeps_moving_walls(golden, precision, bar):
         walls = np.concatenate(sv.get_walls())
     assert rel(u, d["u"]) < bar and rel(v, d["v"]) < bar and rel(w, d["w"]) < bar
     g = po.Grid(n, n, n, n, channel=True)
-    assert pressure_rel(p, d["p"], g, float(d["mu"]), float(d["rho"]), float(d["dt"])) < bar
+    # the mixed form's pressure is bounded at 1e-6, as in the other mixed
+    # tests (it carries the FP32 rounding of the provisional velocity's
+    # small divergent part)
+    pbar = bar if precision == capi.FP64 else 1e-6
+    assert pressure_rel(p, d["p"], g, float(d["mu"]), float(d["rho"]), float(d["dt"])) < pbar
     assert rel(walls, d["walls"]) < bar
 
 
