@@ -75,6 +75,19 @@ template <typename TF, typename TA>
 void launch_helm_cn_first(const Dims& d, int comp, double* x, float* rh, float* rl, const double* uold, const double* q,
                           const TF* f, const TA* adv, const double* top, const double* bottom, double s_plus,
                           double s_minus, double dt, double inv_rho, RedScratch sc, double* out, cudaStream_t s);
+// The BE and CN first residuals of the mixed form in double-float on the FP32
+// pipe (FP64 forces; the pair form of the residual): the same quantities as
+// launch_helm_rhs_be_defect (r_lo given) and launch_helm_cn_first.
+template <typename TA>
+void launch_helm_rhs_be_defect_df(const Dims& d, int comp, float* r, float* r_lo, double* q, double* uo_out,
+                                  const double* uold, const double* f, const TA* adv, const double* top,
+                                  const double* bottom, double s_minus, double dt, double inv_rho, RedScratch sc,
+                                  double* out, cudaStream_t s, int walk_blocks);
+template <typename TA>
+void launch_helm_cn_first_df(const Dims& d, int comp, double* x, float* rh, float* rl, const double* uold,
+                             const double* q, const double* f, const TA* adv, const double* top, const double* bottom,
+                             double s_plus, double s_minus, double dt, double inv_rho, RedScratch sc, double* out,
+                             cudaStream_t s);
 // Mixed form: r = b - (I + s Delta) x in FP64, stored as TD, out[0] = ||r||^2;
 // walk_blocks > 0: the persistent form on that many blocks (tile_walk).
 template <typename TD>

@@ -514,6 +514,143 @@ __global__ void __launch_bounds__(kRedBlock) k_helm_cn_first(Dims d, int comp, d
 }
 
 // ---------------------------------------------------------------------------
+// The two first residuals above without FP64-pipe work (the mixed form's
+// default; the FP64 forces case). The FP64 values are split exactly by
+// integer operations (df_split, 24 + 23 bits) and the expressions evaluated in
+// double-float on the FP32 pipe (df_add, df_mul: relative error a few units
+// of 2^-46 of the largest term), with the coefficients handed in as pairs:
+//   src = hdt/rho f - hdt adv,
+//   BE: r = src (- cbm wall) - off- Q(uold),  Q as helm_point_q,
+//   CN: r = offd Q + src (+ cwall wall),      offd = off+ - off-.
+// The residual is the double-float pair itself (the FP32 defect the inner
+// solve reads is its leading float); Q goes back to FP64 with one addition.
+// The first residuals differ from the FP64 passes' by a few units of 2^-46
+// of their terms, far below the solver tolerances. Opt-in: in the mixed
+// step these passes run on one stream beside the other stream's
+// corrections, and taking them off the FP64 pipe measured no faster (56.36
+// against 56.49 IB steps/s at 256^3).
+// ---------------------------------------------------------------------------
+struct DfCoef {
+    df2 hdt_rho, hdt, off, cwall, four_thirds;
+};
+
+__device__ __forceinline__ df2 dff(float v) {
+    df2 r;
+    r.hi = v;
+    r.lo = 0.f;
+    return r;
+}
+__device__ __forceinline__ df2 df_sub(df2 a, df2 b) { return df_add(a, df_neg(b)); }
+
+// Q(x) of helm_point_q in double-float
+__device__ __forceinline__ df2 df_helm_q(const Dims& d, int comp, const double* __restrict__ x, int xi, int yi, int zi,
+                                         const DfCoef& c) {
+    const df2 x0 = df_split(x[lin(d, xi, yi, zi)]);
+    const df2 sx = df_add(df_split(x[lin(d, xm1(d, xi), yi, zi)]), df_split(x[lin(d, xp1(d, xi), yi, zi)]));
+    if (d.nz == 1) {
+        const df2 sy = df_add(df_split(x[lin(d, xi, ym1(d, yi), zi)]), df_split(x[lin(d, xi, yp1(d, yi), zi)]));
+        return df_sub(df_add(sx, sy), df_mul(dff(4.f), x0));
+    }
+    const df2 sz = df_add(df_split(x[lin(d, xi, yi, zm1(d, zi))]), df_split(x[lin(d, xi, yi, zp1(d, zi))]));
+    if (d.channel && comp != 1) {
+        if (yi == 0 || yi == d.ny - 1) {
+            const df2 xa = df_split(x[lin(d, xi, yi == 0 ? 1 : yi - 1, zi)]);
+            return df_sub(df_add(df_add(sx, sz), df_mul(c.four_thirds, xa)), df_mul(dff(8.f), x0));
+        }
+        const df2 sy = df_add(df_split(x[lin(d, xi, yi - 1, zi)]), df_split(x[lin(d, xi, yi + 1, zi)]));
+        return df_sub(df_add(df_add(sx, sz), sy), df_mul(dff(6.f), x0));
+    }
+    if (d.channel && comp == 1 && yi == 0) return dff(0.f);
+    const df2 sy = df_add(df_split(x[lin(d, xi, ym1(d, yi), zi)]), df_split(x[lin(d, xi, yp1(d, yi), zi)]));
+    return df_sub(df_add(df_add(sx, sy), sz), df_mul(dff(6.f), x0));
+}
+
+template <typename TA>
+__device__ __forceinline__ df2 df_src(double f, TA adv, const DfCoef& c) {
+    return df_sub(df_mul(c.hdt_rho, df_split(f)), df_mul(c.hdt, df_split((double)adv)));
+}
+
+template <typename TA, bool WALK>
+__global__ void __launch_bounds__(kRedBlock) k_helm_rhs_be_defect_df(Dims d, int comp, float* __restrict__ r_out,
+                                                                    float* __restrict__ r_lo, double* __restrict__ q_out,
+                                                                    double* __restrict__ uo_out,
+                                                                    const double* __restrict__ uold,
+                                                                    const double* __restrict__ f,
+                                                                    const TA* __restrict__ adv,
+                                                                    const double* __restrict__ top,
+                                                                    const double* __restrict__ bottom, DfCoef c,
+                                                                    RedScratch sc, double* out) {
+    float acc = 0.f;
+    auto body = [&](int xi, int yi, int zi) {
+        const long long i = lin(d, xi, yi, zi);
+        const double u0 = uold[i];
+        df2 rd;
+        if (d.channel && comp == 1 && yi == 0) {  // the v wall plane
+            rd = df_split(-u0);
+            q_out[i] = 0.0;
+        } else {
+            df2 sb = df_src(f[i], adv[i], c);
+            if (d.channel && comp != 1 && (yi == 0 || yi == d.ny - 1) && top) {
+                const long long ixz = xi + (long long)d.nx * zi;
+                sb = df_sub(sb, df_mul(c.cwall, df_split((yi == 0) ? bottom[ixz] : top[ixz])));
+            }
+            const df2 q = df_helm_q(d, comp, uold, xi, yi, zi, c);
+            q_out[i] = f32_to_f64(q.hi) + f32_to_f64(q.lo);
+            rd = df_sub(sb, df_mul(c.off, q));
+        }
+        if (uo_out) uo_out[i] = u0;  // the step's start velocity, kept for the CN sub-step
+        r_out[i] = rd.hi;
+        r_lo[i] = rd.lo;
+        acc += rd.hi * rd.hi;
+    };
+    if (WALK) {
+        tile_walk(d, body);
+    } else {
+        const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+        if (xi < d.nx && yi < d.ny)
+            for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) body(xi, yi, zi);
+    }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, out);
+}
+
+template <typename TA>
+__global__ void __launch_bounds__(kRedBlock) k_helm_cn_first_df(Dims d, int comp, double* __restrict__ xo,
+                                                               float* __restrict__ rh, float* __restrict__ rl,
+                                                               const double* __restrict__ uold,
+                                                               const double* __restrict__ q,
+                                                               const double* __restrict__ f,
+                                                               const TA* __restrict__ adv,
+                                                               const double* __restrict__ top,
+                                                               const double* __restrict__ bottom, DfCoef c,
+                                                               RedScratch sc, double* out) {
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+    float acc = 0.f;
+    if (xi < d.nx && yi < d.ny)
+        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
+            const long long i = lin(d, xi, yi, zi);
+            const double u0 = uold[i];
+            df2 rd;
+            if (d.channel && comp == 1 && yi == 0) {
+                rd = df_split(-u0);
+            } else {
+                df2 s2 = df_src(f[i], adv[i], c);
+                if (d.channel && comp != 1 && (yi == 0 || yi == d.ny - 1) && top) {
+                    const long long ixz = xi + (long long)d.nx * zi;
+                    s2 = df_add(s2, df_mul(c.cwall, df_split((yi == 0) ? bottom[ixz] : top[ixz])));
+                }
+                rd = df_add(df_mul(c.off, df_split(q[i])), s2);
+            }
+            xo[i] = u0;
+            rh[i] = rd.hi;
+            rl[i] = rd.lo;
+            acc += rd.hi * rd.hi;
+        }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, out);
+}
+
+// ---------------------------------------------------------------------------
 // CG pieces. Scalars live on the device in cgs[] = {n0, pq, n1, beta, alpha}
 // so that no host round trip sits inside an iteration except the convergence
 // test on n0 (the reference's absolute 2-norm stop, src/alg/cg.h:42).
@@ -901,6 +1038,47 @@ void launch_helm_rhs_be_defect(const Dims& d, int comp, double* b, float* r, dou
     }
 #undef AFMIB_BE
 }
+// hdt = dt/2 (BE) or dt (CN); off = s n^2 of the sub-step's operator (BE: off-,
+// CN: off+ - off-); cwall = 8/3 n^2 times s- (BE) or s+ - s- (CN)
+static DfCoef df_coef(const Dims& d, double hdt, double inv_rho, double off, double cwall_s) {
+    DfCoef c;
+    c.hdt_rho = df_split(hdt * inv_rho);
+    c.hdt = df_split(hdt);
+    c.off = df_split(off);
+    c.cwall = df_split(8. / 3. * cwall_s * d.n * d.n);
+    c.four_thirds = df_split(4.0 / 3.0);
+    return c;
+}
+
+template <typename TA>
+void launch_helm_rhs_be_defect_df(const Dims& d, int comp, float* r, float* r_lo, double* q, double* uo_out,
+                                  const double* uold, const double* f, const TA* adv, const double* top,
+                                  const double* bottom, double s_minus, double dt, double inv_rho, RedScratch sc,
+                                  double* out, cudaStream_t s, int walk_blocks) {
+    const DfCoef c = df_coef(d, dt / 2, inv_rho, s_minus * double(d.n) * double(d.n), s_minus);
+    if (walk_blocks > 0)
+        k_helm_rhs_be_defect_df<TA, true><<<walk_grid(d, walk_blocks), dim3(kRBX, kRBY), 0, s>>>(
+            d, comp, r, r_lo, q, uo_out, uold, f, adv, top, bottom, c, sc, out);
+    else
+        k_helm_rhs_be_defect_df<TA, false><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(
+            d, comp, r, r_lo, q, uo_out, uold, f, adv, top, bottom, c, sc, out);
+}
+template <typename TA>
+void launch_helm_cn_first_df(const Dims& d, int comp, double* x, float* rh, float* rl, const double* uold,
+                             const double* q, const double* f, const TA* adv, const double* top, const double* bottom,
+                             double s_plus, double s_minus, double dt, double inv_rho, RedScratch sc, double* out,
+                             cudaStream_t s) {
+    const DfCoef c = df_coef(d, dt, inv_rho, (s_plus - s_minus) * double(d.n) * double(d.n), s_plus - s_minus);
+    k_helm_cn_first_df<TA><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, comp, x, rh, rl, uold, q, f, adv,
+                                                                                    top, bottom, c, sc, out);
+}
+template void launch_helm_rhs_be_defect_df<float>(const Dims&, int, float*, float*, double*, double*, const double*,
+                                                  const double*, const float*, const double*, const double*, double,
+                                                  double, double, RedScratch, double*, cudaStream_t, int);
+template void launch_helm_cn_first_df<float>(const Dims&, int, double*, float*, float*, const double*, const double*,
+                                             const double*, const float*, const double*, const double*, double, double,
+                                             double, double, RedScratch, double*, cudaStream_t);
+
 template <typename TF, typename TA>
 void launch_helm_rhs_cn_q(const Dims& d, int comp, double* r, const double* uold, const double* q, const TF* f,
                           const TA* adv, const double* top, const double* bottom, double s_plus, double s_minus,

@@ -97,6 +97,12 @@ struct afmib_solver {
     // cancellation (k_advect_df; AFMIB_ADVECT_DF=0: the FP32 fluxes of the
     // rounded shadow, 1.0e-8 from the FP64 form after 100 steps at 256^3)
     bool advect_df = true;
+    // mixed form: the first residuals of the viscous solves (BE pass with
+    // Q(uold), CN from Q) in double-float on the FP32 pipe
+    // (k_helm_rhs_be_defect_df, k_helm_cn_first_df; opt-in,
+    // AFMIB_FIRST_DF=1: measured 56.36 against 56.49 IB steps/s for the FP64
+    // passes at 256^3, which run beside the other stream's corrections)
+    bool first_df = false;
     // mixed form with the double-float residual: the Crank-Nicolson viscous
     // solves start from uold (the step's start velocity), whose residual
     // comes pointwise from the kept Q, instead of the current velocity
@@ -1108,7 +1114,10 @@ int substep(afmib_solver* s) {
             const double *top, *bot;
             walls_of(c, &top, &bot);
             ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 4 + 8 + 8 + 4), 1, q);
-            if (s->spread64)
+            if (s->spread64 && lo && s->first_df)
+                launch_helm_rhs_be_defect_df<float>(d, c, r, lo, s->qo[c], s->uo[c], vel[c], s->f[c], s->adv32[c], top,
+                                                    bot, s->s_minus(), s->cfg.dt, inv_rho, s->red, out, q, wblocks);
+            else if (s->spread64)
                 launch_helm_rhs_be_defect<double, float>(d, c, s->rhs[c], r, s->qo[c], vel[c], s->f[c], s->adv32[c],
                                                          top, bot, s->s_minus(), s->cfg.dt, inv_rho, s->red, out, q,
                                                          wblocks, lo, s->uo[c]);
@@ -1162,7 +1171,11 @@ int substep(afmib_solver* s) {
                         const double *top, *bot;
                         walls_of(c, &top, &bot);
                         ProfScope ps(s, P_HELM_RHS, (double)N * (8 + 8 + 8 + 4 + 8 + 4 + 4), 1, hs);
-                        if (s->spread64)
+                        if (s->spread64 && s->first_df)
+                            launch_helm_cn_first_df<float>(d, c, vel[c], s->d32c[c], lo, s->uo[c], s->qo[c], s->f[c],
+                                                           s->adv32[c], top, bot, s->s_plus(), s->s_minus(),
+                                                           s->cfg.dt, inv_rho, s->red, s->scal + 12 + c, hs);
+                        else if (s->spread64)
                             launch_helm_cn_first<double, float>(d, c, vel[c], s->d32c[c], lo, s->uo[c], s->qo[c],
                                                                 s->f[c], s->adv32[c], top, bot, s->s_plus(),
                                                                 s->s_minus(), s->cfg.dt, inv_rho, s->red,
@@ -1892,6 +1905,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_SHADOW_ROUND")) s->round_shadow = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_ADVECT64")) s->advect64 = std::string(e) == "1";
     if (const char* e = std::getenv("AFMIB_ADVECT_DF")) s->advect_df = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_FIRST_DF")) s->first_df = std::string(e) == "1";
     if (const char* e = std::getenv("AFMIB_CN_START_OLD")) s->cn_start_old = std::string(e) != "0";
     if (s->mixed && s->fused_rhs)
         for (auto& q : s->qo) TRY(dalloc(s, &q, N));

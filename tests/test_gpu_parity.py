@@ -895,3 +895,31 @@ def test_ib_steps_moving_walls(golden, precision, bar):
     assert rel(u, d["u"]) < bar and rel(v, d["v"]) < bar and rel(w, d["w"]) < bar
     assert rel(X - d["X"], d["Xout"] - d["X"]) < bar
     assert rel(walls, d["walls"]) < bar
+
+
+@pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
+def test_double_float_first_residuals_match_fp64(monkeypatch, golden, bc):
+    """The mixed form's first viscous residuals (the BE pass with Q(uold), the
+    CN residual from Q) in double-float on the FP32 pipe against the FP64
+    passes: two IB steps (the channel with moving walls) agree to 1e-10; the
+    two differ by a few units of 2^-46 of the residuals' terms, so only the
+    solves' stopping tests can tell them apart."""
+    g, u, v, w, X, nstart, nidx = _periodic_case(32, M=800, seed=17)
+    walls = None
+    if bc == capi.BC_CHANNEL:
+        v = v[: g.nx * (g.ny - 1) * g.nz]
+        walls = np.random.default_rng(4).standard_normal(4 * 32 * 32) * 0.05
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("AFMIB_FIRST_DF", mode)
+        with capi.Solver(32, bc=bc, precision=capi.MIXED, mu=0.01, dt=1e-3, tol=1e-12, k_spring=0.5) as sv:
+            sv.set_velocity(u, v, w)
+            if walls is not None:
+                sv.set_walls(*np.split(walls, 4))
+            sv.project()
+            sv.set_markers(X, nstart, nidx)
+            sv.ib_step(2)
+            out[mode] = (sv.get_velocity(), sv.get_markers())
+    for a, b in zip(out["1"][0], out["0"][0]):
+        assert rel(a, b) < 1e-10
+    assert rel(out["1"][1] - X, out["0"][1] - X) < 1e-10
