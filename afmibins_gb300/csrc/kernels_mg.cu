@@ -361,6 +361,75 @@ __global__ void __launch_bounds__(BX * BY, MINB) k_rbgs_z2b(Dims d, int color, T
     rbgs_z2_body<T, ZU>(d, color, omega, xv, b, rev);
 }
 
+// The FP32 colour on float pairs: a thread owns the pairs (2t, 2t+1) of its
+// (y, z) column, one cell of each pair being the colour's. Per ZU-cell
+// column it loads ZU + 2 pairs of its own column (the z neighbours come from
+// the same registers), the pairs of the rows y - 1 and y + 1, and the pairs
+// of b: 4.25 eight-byte loads per updated cell, each warp instruction reading
+// 256 contiguous bytes, against the scalar kernel's eight stride-2 loads. The
+// x neighbour across the pair boundary comes from the adjacent lane by a
+// shuffle (the first and last lanes load it). The colour is uniform across a
+// warp (its lanes share y and z). The update is rbgs_z2_body's arithmetic in
+// the same order, so the same bits; the pair is stored whole, the other
+// colour's value unchanged (no thread writes that colour in this launch).
+template <int ZU, int MINB>
+__global__ void __launch_bounds__(BX * BY, MINB) k_rbgs_pair(Dims d, int color, float omega, float* __restrict__ xv,
+                                                            const float* __restrict__ b, int rev) {
+    const Ix2 I(d);
+    const uint3 B = block_at(rev);
+    const int t = B.x * BX + threadIdx.x, y = B.y * BY + threadIdx.y, z0 = B.z * ZU;
+    const float2* __restrict__ xp = reinterpret_cast<const float2*>(xv);
+    const float2* __restrict__ bp = reinterpret_cast<const float2*>(b);
+    auto pr = [&](int yy, int zz) { return I.at(2 * t, yy, zz) >> 1; };
+    const bool has_lo = !d.channel || y > 0, has_hi = !d.channel || y < d.ny - 1;
+    const int ylo = d.channel ? y - 1 : I.ym(y), yhi = d.channel ? y + 1 : I.yp(y);
+    float2 col[ZU + 2], ly[ZU], hy[ZU], bb[ZU];
+#pragma unroll
+    for (int k = 0; k < ZU + 2; ++k) col[k] = xp[pr(y, (z0 - 1 + k) & I.mz)];
+#pragma unroll
+    for (int u = 0; u < ZU; ++u) {
+        ly[u] = has_lo ? xp[pr(ylo, z0 + u)] : make_float2(0.f, 0.f);
+        hy[u] = has_hi ? xp[pr(yhi, z0 + u)] : make_float2(0.f, 0.f);
+        bb[u] = bp[pr(y, z0 + u)];
+    }
+    const float inv = 1.f / (float(d.n) * float(d.n));
+    float2 out[ZU];
+#pragma unroll
+    for (int u = 0; u < ZU; ++u) {
+        const int z = z0 + u, p = (y + z + color) & 1;
+        const float2 self = col[u + 1];
+        float left, right;
+        if (p == 0) {  // the cell 2t: its left neighbour is the previous pair's second value
+            float prev = __shfl_up_sync(0xffffffffu, self.y, 1);
+            if (threadIdx.x == 0) prev = xv[I.at((2 * t - 1) & I.mx, y, z)];
+            left = prev;
+            right = self.y;
+        } else {  // the cell 2t + 1: its right neighbour is the next pair's first value
+            float next = __shfl_down_sync(0xffffffffu, self.x, 1);
+            if (threadIdx.x == BX - 1) next = xv[I.at((2 * t + 2) & I.mx, y, z)];
+            left = self.x;
+            right = next;
+        }
+        const float zm = p ? col[u].y : col[u].x, zq = p ? col[u + 2].y : col[u + 2].x;
+        float S = (left + right) + (zm + zq), c = 6.f;
+        const float yl = p ? ly[u].y : ly[u].x, yh = p ? hy[u].y : hy[u].x;
+        if (d.channel) {
+            if (has_lo) S += yl; else c -= 1.f;
+            if (has_hi) S += yh; else c -= 1.f;
+        } else {
+            S += yl + yh;
+        }
+        const float rc = (c == 6.f) ? float(1.0 / 6.0) : ((c == 5.f) ? float(1.0 / 5.0) : (c == 4.f ? 0.25f : 1.f / c));
+        const float bi = p ? bb[u].y : bb[u].x;
+        float v = (S - bi * inv) * rc;
+        if (omega != 1.f) v = v + (omega - 1.f) * (v - (p ? self.y : self.x));
+        out[u] = p ? make_float2(self.x, v) : make_float2(v, self.y);
+    }
+    float2* __restrict__ xw = reinterpret_cast<float2*>(xv);
+#pragma unroll
+    for (int u = 0; u < ZU; ++u) xw[pr(y, z0 + u)] = out[u];
+}
+
 template <typename T, int ZU>
 __global__ void k_residual_z2(Dims d, T* __restrict__ r, const T* __restrict__ xv, const T* __restrict__ b, int rev) {
     const Ix2 I(d);
@@ -1175,12 +1244,32 @@ void launch_residual(const Dims& d, T* r, const T* x, const T* b, RedScratch* sc
     else
         k_residual<T><<<grid3(d), dim3(BX, BY), 0, s>>>(d, r, x, b);
 }
+// The pair kernel is opt-in (AFMIB_RBGS_PAIR=1, read at every launch): at
+// 256^3 its colour launches took 39.5 us against 29.9 for the scalar kernel
+// (53.7 against 56.5 IB steps/s): 60 registers hold it to 4 resident blocks
+// and every y-neighbour and b pair brings the other colour's value along.
+// Needs full warps along x (nx >= 64) and block rows along y (ny a multiple
+// of 8).
+constexpr int kPairZU = 4, kPairMinB = 4;
+bool rbgs_pair_ok(const Dims& d) {
+    const char* e = std::getenv("AFMIB_RBGS_PAIR");
+    if (!(e && e[0] == '1')) return false;
+    return d.nz > 1 && d.nx >= 2 * BX && d.ny % BY == 0 && d.nz % kPairZU == 0;
+}
+
 template <typename T>
 void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s, double omega, int rev) {
     if (d.nx < kOmegaMinNx) omega = 1.0;
     if (d.nz % kZU == 0 && d.nx >= batch_min_nx()) {
         dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / kZU);
         if (ix2_ok(d)) {
+            // FP32 on float pairs (opt-in, AFMIB_RBGS_PAIR=1)
+            if (sizeof(T) == sizeof(float) && rbgs_pair_ok(d)) {
+                const dim3 gp(d.nx / 2 / BX, d.ny / BY, d.nz / kPairZU);
+                k_rbgs_pair<kPairZU, kPairMinB><<<gp, dim3(BX, BY), 0, s>>>(d, color, float(omega), (float*)x,
+                                                                           (const float*)b, rev);
+                return;
+            }
             // FP32: registers capped for 6 resident blocks (40 against 44), 50.5
             // against 50.0 IB steps/s at 256^3 (8 blocks, 32 registers: 48.0)
             if (sizeof(T) == sizeof(float))
