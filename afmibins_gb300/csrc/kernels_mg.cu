@@ -938,6 +938,325 @@ __global__ void k_prolong(Dims d, T* __restrict__ fine, const T* __restrict__ co
     prolong_cell<T, ADD>(d, fine, coarse, xc, yc, zc);
 }
 
+// Column-marching transfers for 3D power-of-two levels whose coarse x extent
+// is a multiple of 32 and coarse y extent a multiple of kTrBY. A warp holds 32
+// consecutive coarse x of one coarse row, so its fine accesses are the 64
+// consecutive cells 2 xc .. 2 xc + 63 of a fine row, read or written as one
+// pair per lane (256 contiguous bytes for FP32); the cells one beyond a lane's
+// pair come from the adjacent lane by a shuffle (the first and last lanes load
+// them). A thread then walks CZ coarse planes along z. The one-cell kernels
+// (restrict_cell2, prolong_cell2) read and write with a stride of two cells,
+// 64 single loads per coarse cell in the restriction, and their prolongation
+// stores wait on the loads of the next cell (same array): on 256^3 both ran at
+// a third of the copy bandwidth.
+constexpr int kTrBY = 8;
+template <typename T>
+struct Pair;
+template <>
+struct Pair<float> {
+    using type = float2;
+};
+template <>
+struct Pair<double> {
+    using type = double2;
+};
+
+// Full weighting with restrict_cell2's taps, weights and summation order: the
+// coarse cell's single accumulator takes its 64 terms plane by plane (kz), row
+// by row (ky), cell by cell (kx). Fine planes 2 zc + 1 and 2 zc + 2 are the
+// last two planes (kz = 2, 3) of coarse plane zc and the first two (kz = 0, 1)
+// of zc + 1, so each fine plane is read once and feeds two accumulators, the
+// second of which starts from zero with that plane's terms: the same
+// additions in the same order as the one-cell kernel, the same bits.
+//
+// A lane reads 16 bytes of each fine tap row (CE = 4 FP32 or 2 FP64 cells)
+// and takes the cells on either side from its neighbours, so it serves CE / 2
+// coarse cells: a warp covers 16 CE coarse x. The block's fine tile of a plane
+// (rows 2 yc0 - 1 .. 2 yc0 + 16, clamped at channel walls, wrapped otherwise;
+// 32 CE cells from 2 xc0 and one 16-byte chunk on either side, wrapped in x)
+// arrives in shared memory by 16-byte asynchronous copies issued
+// kTrStages - 1 planes ahead, one commit group per plane, so that the march
+// along z keeps two planes of DRAM reads in flight with one barrier per plane.
+constexpr int kTrStages = 3;
+constexpr int kTrRows = 2 * kTrBY + 2;
+template <typename T>
+struct TrTile {
+    static constexpr int CE = 16 / (int)sizeof(T);       // cells per 16-byte chunk (per lane)
+    static constexpr int CX = 16 * CE;                    // coarse x per block
+    static constexpr int W = 34 * CE;                     // row: left chunk, 32 lane chunks, right chunk
+    static constexpr int CHUNKS = kTrRows * 34;           // 16-byte chunks per plane
+    static constexpr int PER_THREAD = (CHUNKS + 32 * kTrBY - 1) / (32 * kTrBY);
+};
+template <typename T>
+struct Quad;
+template <>
+struct Quad<float> {
+    using type = float4;
+};
+template <>
+struct Quad<double> {
+    using type = double2;
+};
+template <typename T>
+__device__ __forceinline__ void quad_get(const T* p, T (&v)[16 / sizeof(T)]) {
+    const typename Quad<T>::type q = *reinterpret_cast<const typename Quad<T>::type*>(p);
+    if constexpr (sizeof(T) == 4) {
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else {
+        v[0] = q.x; v[1] = q.y;
+    }
+}
+
+template <typename T, int CZ>
+__global__ void __launch_bounds__(32 * kTrBY) k_restrict_cols(Dims d, T* __restrict__ coarse,
+                                                              const T* __restrict__ fine, int rev) {
+    using TT = TrTile<T>;
+    constexpr int CE = TT::CE, M = CE / 2;  // M coarse cells per lane
+    constexpr int NP = 2 * CZ + 2;          // fine planes of the block
+    __shared__ __align__(16) T st[kTrStages][kTrRows * TT::W];
+    const Ix2 I(d);
+    const uint3 B = block_at(rev);
+    const int lane = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + lane;
+    const int xc0 = B.x * TT::CX, yc0 = B.y * kTrBY, zc0 = B.z * CZ;
+    // this thread's chunks of every plane: source offset within the plane
+    // (-1: none) and destination offset within the stage
+    int src[TT::PER_THREAD], dst[TT::PER_THREAD];
+#pragma unroll
+    for (int u = 0; u < TT::PER_THREAD; ++u) {
+        const int c = tid + u * 32 * kTrBY;
+        src[u] = -1;
+        dst[u] = 0;
+        if (c < TT::CHUNKS) {
+            const int j = c / 34, k = c - j * 34;
+            int y = 2 * yc0 - 1 + j;
+            if (d.channel) y = y < 0 ? 0 : (y > d.ny - 1 ? d.ny - 1 : y);
+            else y &= I.my;
+            src[u] = ((2 * xc0 - CE + k * CE) & I.mx) | (y << I.lx);
+            dst[u] = j * TT::W + k * CE;
+        }
+    }
+    // copies of fine plane 2 zc0 - 1 + i; a commit group per plane, empty
+    // past the block's last plane, so that the group count is the plane count
+    auto issue = [&](int i) {
+        if (i < NP) {
+            T* stage = st[i % kTrStages];
+            const T* pl = fine + (((2 * zc0 - 1 + i) & I.mz) << I.lxy);
+#pragma unroll
+            for (int u = 0; u < TT::PER_THREAD; ++u)
+                if (src[u] >= 0) pipe::cp16(stage + dst[u], pl + src[u]);
+        }
+        pipe::commit();
+    };
+    auto acquire = [&](int i) -> const T* {
+        pipe::wait_pending<kTrStages - 2>();
+        __syncthreads();           // plane i is in; plane i - 1 is read by every thread
+        issue(i + kTrStages - 1);  // into plane i - 1's stage
+        return st[i % kTrStages];
+    };
+    // the taps of a staged plane: e[ky][1 + q] = fine x = 2 xc0 + CE lane + q,
+    // q = -1 .. CE (rows 2 ty + ky of the tile)
+    auto taps = [&](const T* pl, T (&e)[4][CE + 2]) {
+#pragma unroll
+        for (int ky = 0; ky < 4; ++ky) {
+            const T* row = pl + (2 * ty + ky) * TT::W + CE;  // fine x = 2 xc0
+            T v[CE];
+            quad_get(row + CE * lane, v);
+            T l = __shfl_up_sync(0xffffffffu, v[CE - 1], 1), r = __shfl_down_sync(0xffffffffu, v[0], 1);
+            if (lane == 0) l = row[-1];
+            if (lane == 31) r = row[32 * CE];
+            e[ky][0] = l;
+#pragma unroll
+            for (int q = 0; q < CE; ++q) e[ky][1 + q] = v[q];
+            e[ky][CE + 1] = r;
+        }
+    };
+    const T wgt[4] = {T(1), T(3), T(3), T(1)};
+    // coarse cell m of the lane: taps fine x = 2 xc - 1 .. 2 xc + 2 = e[ky][2m .. 2m + 3]
+    auto add = [&](T (&acc)[M], const T (&e)[4][CE + 2], int kz) {
+#pragma unroll
+        for (int m = 0; m < M; ++m)
+#pragma unroll
+            for (int ky = 0; ky < 4; ++ky)
+#pragma unroll
+                for (int kx = 0; kx < 4; ++kx) acc[m] += (wgt[kx] * wgt[ky] * wgt[kz] / T(512)) * e[ky][2 * m + kx];
+    };
+#pragma unroll
+    for (int i = 0; i < kTrStages - 1; ++i) issue(i);
+    T acc[M], next[M], e[4][CE + 2];
+#pragma unroll
+    for (int m = 0; m < M; ++m) acc[m] = T(0);
+    taps(acquire(0), e);
+    add(acc, e, 0);
+    taps(acquire(1), e);
+    add(acc, e, 1);
+    const int co = (xc0 + M * lane) | ((yc0 + ty) << (I.lx - 1));
+    for (int k = 0; k < CZ; ++k) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) next[m] = T(0);
+        taps(acquire(2 * k + 2), e);
+        add(acc, e, 2);
+        add(next, e, 0);
+        taps(acquire(2 * k + 3), e);
+        add(acc, e, 3);
+        add(next, e, 1);
+        T* out = coarse + (co | ((zc0 + k) << (I.lxy - 2)));
+        if constexpr (M == 2) *reinterpret_cast<float2*>(out) = make_float2(acc[0], acc[1]);
+        else out[0] = acc[0];
+#pragma unroll
+        for (int m = 0; m < M; ++m) acc[m] = next[m];
+    }
+    pipe::wait_pending<0>();
+}
+
+// Trilinear prolongation-add with prolong_cell2's expressions. A thread owns
+// the fine pairs x = 2t, 2t+1 of rows y = 2s, 2s+1 in planes z = 2r, 2r+1:
+// fine cell 2t + 1 is the first (xcf) of coarse cell t and 2t the second
+// (xnf) of coarse cell t - 1, and likewise in y and z, so the eight cells need
+// the coarse values at t - 1 .. t + 1, s - 1 .. s + 1, r - 1 .. r + 1, kept in
+// registers as a window of three coarse planes that moves one plane per r.
+// Each fine cell takes the expression of its role (first or second in x, y
+// and z) with its terms in prolong_cell2's order, and in channel mode the wall
+// rows y = 0 and ny - 1 take the wall expressions: the same bits. The block's
+// fine values of plane pair r (2 x 16 rows of 64 cells) and its tile of
+// coarse plane r + 1 arrive in shared memory by 16-byte asynchronous copies
+// issued one or two plane pairs ahead (FP64 / FP32); the sums go straight to
+// memory.
+template <typename T>
+struct ProTile {
+    static constexpr int CE = 16 / (int)sizeof(T);
+    static constexpr int S = sizeof(T) == 4 ? 3 : 2;   // stages (static shared memory <= 48 KB)
+    static constexpr int FROWS = 4 * kTrBY;            // 2 planes x 2 kTrBY rows
+    static constexpr int FW = 64;
+    static constexpr int CROWS = kTrBY + 2;
+    static constexpr int CW = 32 + 2 * CE;
+    static constexpr int STAGE = FROWS * FW + CROWS * CW;
+};
+
+template <typename T, int RZ>
+__global__ void __launch_bounds__(32 * kTrBY) k_prolong_cols(Dims d, T* __restrict__ fine,
+                                                             const T* __restrict__ coarse, int rev) {
+    using P2 = typename Pair<T>::type;
+    using PT = ProTile<T>;
+    constexpr int CE = PT::CE;
+    __shared__ __align__(16) T st[PT::S][PT::STAGE];
+    const Ix2 I(d);
+    const uint3 B = block_at(rev);
+    const int lane = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + lane;
+    const int cx = d.nx / 2, cy = d.ny / 2, cz = d.nz / 2, lcx = I.lx - 1, lcxy = I.lxy - 2;
+    const int t0 = B.x * 32, s0 = B.y * kTrBY, r0 = B.z * RZ;
+    const int t = t0 + lane, s = s0 + ty;
+    auto crow = [&](int y) {  // coarse row y in range: clamped at channel walls, wrapped otherwise
+        if (d.channel) return y < 0 ? 0 : (y > cy - 1 ? cy - 1 : y);
+        return y & (cy - 1);
+    };
+    // item i: the fine values of plane pair r0 + i and the coarse tile of
+    // plane r0 + i + 1; a commit group per item, empty past the last
+    auto issue = [&](int i) {
+        if (i < RZ) {
+            T* dst = st[i % PT::S];
+            const int r = r0 + i;
+            for (int c = tid; c < PT::FROWS * (PT::FW / CE); c += 32 * kTrBY) {
+                const int j = c / (PT::FW / CE), k = c - j * (PT::FW / CE);
+                const int jz = j / (2 * kTrBY), jy = j - jz * (2 * kTrBY);
+                pipe::cp16(dst + j * PT::FW + k * CE,
+                           fine + ((2 * t0 + k * CE) | ((2 * s0 + jy) << I.lx) | ((2 * r + jz) << I.lxy)));
+            }
+            T* cdst = dst + PT::FROWS * PT::FW;
+            const T* cpl = coarse + (((r + 1) & (cz - 1)) << lcxy);
+            for (int c = tid; c < PT::CROWS * (PT::CW / CE); c += 32 * kTrBY) {
+                const int j = c / (PT::CW / CE), k = c - j * (PT::CW / CE);
+                const int x = (t0 - CE + k * CE) & (cx - 1);
+                pipe::cp16(cdst + j * PT::CW + k * CE, cpl + (x | (crow(s0 - 1 + j) << lcx)));
+            }
+        }
+        pipe::commit();
+    };
+    auto acquire = [&](int i) -> const T* {
+        pipe::wait_pending<PT::S - 2>();
+        __syncthreads();           // item i is in; item i - 1 is read by every thread
+        issue(i + PT::S - 1);      // into item i - 1's stage
+        return st[i % PT::S];
+    };
+#pragma unroll
+    for (int i = 0; i < PT::S - 1; ++i) issue(i);
+    const T a = T(27) / T(64), b = T(9) / T(64), c3 = T(3) / T(64), e = T(1) / T(64);
+    const T wa = T(9) / T(16), wb = T(3) / T(16), we = T(1) / T(16);
+    // interior cell of role (rx, ry, rz): 1 = first (xcf), 0 = second (xnf);
+    // its base coarse cell is at offset = role in the window (x, y, z alike)
+    auto cell = [&](const T (&cb)[3][3], const T (&cf)[3][3], int rx, int ry, int rz) -> T {
+        const int ox = rx, oy = ry;
+        const T blb = cb[oy][ox], brb = cb[oy][ox + 1], ulb = cb[oy + 1][ox], urb = cb[oy + 1][ox + 1];
+        const T blf = cf[oy][ox], brf = cf[oy][ox + 1], ulf = cf[oy + 1][ox], urf = cf[oy + 1][ox + 1];
+        const bool fx = rx == 1, fy = ry == 1, fz = rz == 1;
+        if (fx && fy && fz) return a * blb + b * (brb + ulb + blf) + c3 * (urb + ulf + brf) + e * urf;
+        if (!fx && fy && fz) return a * brb + b * (urb + blb + brf) + c3 * (ulb + blf + urf) + e * ulf;
+        if (fx && !fy && fz) return a * ulb + b * (urb + blb + ulf) + c3 * (brb + blf + urf) + e * brf;
+        if (!fx && !fy && fz) return a * urb + b * (brb + ulb + urf) + c3 * (blb + ulf + brf) + e * blf;
+        if (fx && fy && !fz) return a * blf + b * (brf + ulf + blb) + c3 * (urf + ulb + brb) + e * urb;
+        if (!fx && fy && !fz) return a * brf + b * (urf + blf + brb) + c3 * (ulf + blb + urb) + e * ulb;
+        if (fx && !fy && !fz) return a * ulf + b * (urf + blf + ulb) + c3 * (brf + blb + urb) + e * brb;
+        return a * urf + b * (brf + ulf + urb) + c3 * (blf + ulb + brb) + e * blb;
+    };
+    // channel wall cell of x role rx and z role rz, from coarse row s
+    auto wall = [&](const T (&cb)[3][3], const T (&cf)[3][3], int rx, int rz) -> T {
+        const int ox = rx;
+        const T bl = cb[1][ox], br = cb[1][ox + 1], fl = cf[1][ox], fr = cf[1][ox + 1];
+        const bool fx = rx == 1, fz = rz == 1;
+        if (fx && fz) return wa * bl + wb * (br + fl) + we * fr;
+        if (!fx && fz) return wa * br + wb * (bl + fr) + we * fl;
+        if (fx && !fz) return wa * fl + wb * (fr + bl) + we * br;
+        return wa * fr + wb * (fl + br) + we * bl;
+    };
+    const bool wall_lo = d.channel && s == 0, wall_hi = d.channel && s == cy - 1;
+    // window: coarse planes r - 1, r, r + 1 at rows s - 1 .. s + 1, cells t - 1 .. t + 1
+    T w[3][3][3];
+#pragma unroll
+    for (int p = 0; p < 2; ++p)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+                w[p][j][i] = coarse[((t - 1 + i) & (cx - 1)) | (crow(s - 1 + j) << lcx) |
+                                    (((r0 - 1 + p) & (cz - 1)) << lcxy)];
+    for (int k = 0; k < RZ; ++k) {
+        const int r = r0 + k;
+        const T* sf = acquire(k);
+        const T* sc = sf + PT::FROWS * PT::FW;
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) w[2][j][i] = sc[(ty + j) * PT::CW + CE + lane - 1 + i];
+#pragma unroll
+        for (int jz = 0; jz < 2; ++jz)
+#pragma unroll
+            for (int jy = 0; jy < 2; ++jy) {
+                const T(&cb)[3][3] = w[jz];
+                const T(&cf)[3][3] = w[jz + 1];
+                T v0, v1;  // fine x = 2t (second of t - 1), 2t + 1 (first of t)
+                if ((jy == 0 && wall_lo) || (jy == 1 && wall_hi)) {
+                    v0 = wall(cb, cf, 0, jz);
+                    v1 = wall(cb, cf, 1, jz);
+                } else {
+                    v0 = cell(cb, cf, 0, jy, jz);
+                    v1 = cell(cb, cf, 1, jy, jz);
+                }
+                const P2 old = *reinterpret_cast<const P2*>(sf + (jz * 2 * kTrBY + 2 * ty + jy) * PT::FW + 2 * lane);
+                P2 out;
+                out.x = old.x + v0;
+                out.y = old.y + v1;
+                *reinterpret_cast<P2*>(fine + ((2 * t) | ((2 * s + jy) << I.lx) | ((2 * r + jz) << I.lxy))) = out;
+            }
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                w[0][j][i] = w[1][j][i];
+                w[1][j][i] = w[2][j][i];
+            }
+    }
+    pipe::wait_pending<0>();
+}
+
 // Coarsest level, src/mg/solver.h:264-271: remove the mean of b, then CG
 // warm-started from b with the absolute 2-norm stop. One block; the level is
 // a handful of cells (one cell for a cube).
@@ -1363,8 +1682,49 @@ void launch_rbgs_pipe(const Dims& d, const PipeCfg& c, const T* xin, T* xout, co
     }
 }
 
+// Column-marching transfers (k_restrict_cols, k_prolong_cols) apply to FP32
+// 3D power-of-two levels with 32 | nx / 2 (64 for the restriction) and
+// kTrBY | ny / 2 and 16-byte aligned fine and coarse arrays;
+// AFMIB_TRANSFER_COLS=0 keeps the one-cell kernels (read at every launch, so
+// that a test can compare both in one process). FP64 keeps the one-cell
+// kernels: there both transfers are bound by the FP64 pipe (64 dependent FMAs
+// per coarse cell, about 9 FP64 operations per prolonged cell), and the column
+// kernels, with the same operations, measured 296 / 307 against 261 / 278 us
+// per 256^3 launch.
+static bool transfer_cols_ok(const Dims& d, const void* fine, const void* coarse) {
+    if (const char* e = std::getenv("AFMIB_TRANSFER_COLS"))
+        if (e[0] == '0') return false;
+    return d.nz > 1 && ix2_ok(d) && (d.nx / 2) % 32 == 0 && (d.ny / 2) % kTrBY == 0 &&
+           ((reinterpret_cast<uintptr_t>(fine) | reinterpret_cast<uintptr_t>(coarse)) & 15) == 0;
+}
+// coarse planes per thread: the largest of 8, 4, 2 that divides the coarse z
+// extent and leaves at least AFMIB_TRANSFER_MIN_BLOCKS (default 1024) blocks, else 1
+static int transfer_planes(const Dims& d, int bx = 32) {
+    const char* e = std::getenv("AFMIB_TRANSFER_MIN_BLOCKS");
+    const long long min_blocks = e ? std::atoll(e) : 1024;
+    const long long cols = (long long)(d.nx / 2 / bx) * (d.ny / 2 / kTrBY);
+    const int cz = d.nz / 2;
+    for (int z : {8, 4, 2})
+        if (cz % z == 0 && cols * (cz / z) >= min_blocks) return z;
+    return 1;
+}
+inline dim3 transfer_grid(const Dims& d, int planes, int bx = 32) {
+    return dim3(d.nx / 2 / bx, d.ny / 2 / kTrBY, d.nz / 2 / planes);
+}
+
 template <typename T>
 void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s, int rev) {
+    if constexpr (sizeof(T) == sizeof(float)) {
+        if (transfer_cols_ok(d, fine, coarse) && (d.nx / 2) % TrTile<T>::CX == 0) {
+            const int z = transfer_planes(d, TrTile<T>::CX);
+            const dim3 g = transfer_grid(d, z, TrTile<T>::CX), b(32, kTrBY);
+            if (z == 8) k_restrict_cols<T, 8><<<g, b, 0, s>>>(d, coarse, fine, rev);
+            else if (z == 4) k_restrict_cols<T, 4><<<g, b, 0, s>>>(d, coarse, fine, rev);
+            else if (z == 2) k_restrict_cols<T, 2><<<g, b, 0, s>>>(d, coarse, fine, rev);
+            else k_restrict_cols<T, 1><<<g, b, 0, s>>>(d, coarse, fine, rev);
+            return;
+        }
+    }
     dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz == 1 ? 1 : d.nz / 2);
     if (d.nz > 1 && d.nx >= 2 && d.ny >= 2 && ix2_ok(d)) k_restrict2<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine, rev);
     else k_restrict<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine);
@@ -1395,6 +1755,20 @@ void launch_resid_restrict(const Dims& d, T* coarse_b, T* coarse_x, const T* x, 
 
 template <typename T>
 void launch_prolong_add(const Dims& d, T* fine, const T* coarse, cudaStream_t s, int rev) {
+    if constexpr (sizeof(T) == sizeof(float)) {
+        if (transfer_cols_ok(d, fine, coarse)) {
+            // AFMIB_PROLONG_MAX_PLANES caps the planes per block (a sweep knob)
+            const char* e = std::getenv("AFMIB_PROLONG_MAX_PLANES");
+            int z = std::min(transfer_planes(d), e ? std::max(1, std::atoi(e)) : 8);
+            while (z & (z - 1)) z &= z - 1;  // a power of two, so a divisor of the plane count
+            const dim3 g = transfer_grid(d, z), b(32, kTrBY);
+            if (z == 8) k_prolong_cols<T, 8><<<g, b, 0, s>>>(d, fine, coarse, rev);
+            else if (z == 4) k_prolong_cols<T, 4><<<g, b, 0, s>>>(d, fine, coarse, rev);
+            else if (z == 2) k_prolong_cols<T, 2><<<g, b, 0, s>>>(d, fine, coarse, rev);
+            else k_prolong_cols<T, 1><<<g, b, 0, s>>>(d, fine, coarse, rev);
+            return;
+        }
+    }
     dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz == 1 ? 1 : d.nz / 2);
     if (d.nz > 1 && d.nx >= 2 && d.ny >= 2 && ix2_ok(d))
         k_prolong2<T, true><<<g, dim3(BX, BY), 0, s>>>(d, fine, coarse, rev);

@@ -570,6 +570,37 @@ def test_alternating_block_order_keeps_bits(monkeypatch, precision):
     assert np.array_equal(out["0"][0], out["1"][0])
 
 
+@pytest.mark.parametrize("n,bc", [(128, capi.BC_PERIODIC), (128, capi.BC_CHANNEL), (256, capi.BC_PERIODIC),
+                                  (256, capi.BC_CHANNEL)])
+def test_column_transfers_keep_bits(monkeypatch, n, bc):
+    """Mixed form: the FP32 column-marching restriction and prolongation (fine
+    tiles staged in shared memory by asynchronous copies, 16 bytes per lane
+    with the neighbouring cells from adjacent lanes, a block walking 1, 2, 4
+    or 8 coarse planes) evaluate the one-cell kernels' expressions in their
+    order (AFMIB_TRANSFER_COLS=0): a multigrid solve agrees bit for bit, with
+    the same cycle count, whatever the planes per block; at 256^3 the passes
+    alternate their block order too."""
+    precision = capi.MIXED
+    channel = bc == capi.BC_CHANNEL
+    g = po.Grid(n, n, n, n, channel=channel)
+    b = np.random.default_rng(29).standard_normal(g.ncell)
+    out = {}
+    for mode, min_blocks, max_planes in (("0", None, None), ("1", None, None), ("1", "1", "8"), ("1", "256", "2"),
+                                         ("1", "100000000", "1")):
+        monkeypatch.setenv("AFMIB_TRANSFER_COLS", mode)
+        for key, val in (("AFMIB_TRANSFER_MIN_BLOCKS", min_blocks), ("AFMIB_PROLONG_MAX_PLANES", max_planes)):
+            if val:
+                monkeypatch.setenv(key, val)
+            else:
+                monkeypatch.delenv(key, raising=False)
+        with capi.Solver(n, bc=bc, precision=precision, tol=1e-9) as sv:
+            out[(mode, min_blocks)] = sv.mg_solve(b)
+    ref = out[("0", None)]
+    for key, (x, cycles) in out.items():
+        assert cycles == ref[1], key
+        assert np.array_equal(x, ref[0]), key
+
+
 @pytest.mark.parametrize("n,bc,markers", [(64, capi.BC_PERIODIC, True), (64, capi.BC_CHANNEL, False),
                                           (256, capi.BC_PERIODIC, False)])
 def test_interleaved_viscous_solves_keep_bits(monkeypatch, n, bc, markers):
