@@ -23,6 +23,10 @@ void launch_advect(const Dims& d, T* ua, T* va, T* wa, const TI* u, const TI* v,
 template <typename T>
 void launch_div(const Dims& d, T* out, const T* u, const T* v, const T* w, const T* top, const T* bottom,
                 cudaStream_t s);
+// Mixed form: the divergence in double-float (FP64 in and out, no FP64
+// arithmetic but one addition per cell), out_sum[0] = the sum of out.
+void launch_div_df(const Dims& d, double* out, const double* u, const double* v, const double* w, const double* top,
+                   const double* bottom, RedScratch sc, double* out_sum, cudaStream_t s);
 // Gradient onto faces, src/alg/grad.h:29-44 (v plane 0 untouched in channel mode).
 template <typename T>
 void launch_grad(const Dims& d, T* px, T* py, T* pz, const T* p, cudaStream_t s);
@@ -173,6 +177,10 @@ void launch_residual(const Dims& d, T* r, const T* x, const T* b, RedScratch* sc
 template <typename TD>
 void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, RedScratch sc, double* out, cudaStream_t s,
                        float* r_lo = nullptr);
+// Mixed form: the first defect of a pressure solve in double-float,
+// (rh, rl) = (b - sum * scale) - L x (sum null: no mean), out[0] = rh.rh
+void launch_lap_defect_df(const Dims& d, float* rh, float* rl, const double* x, const double* b, const double* sum,
+                          double scale, RedScratch sc, double* out, cudaStream_t s);
 // Mixed form: x += e, (rh, rl) -= L e in double-float, out[0] = rh.rh
 // (r_lo of launch_lap_defect starts the pair)
 void launch_lap_update_df(const Dims& d, double* x, const float* e, float* rh, float* rl, RedScratch sc, double* out,

@@ -184,6 +184,45 @@ __global__ void k_div(Dims d, T* __restrict__ out, const T* __restrict__ u, cons
     out[i] = T(d.n) * ((u[lin(d, xp1(d, x), y, z)] - u[i]) + dv + (w[lin(d, x, y, zp1(d, z))] - w[i]));
 }
 
+// Mixed form: k_div in double-float on the FP32 pipe (GB300's FP64 pipe
+// bounds the FP64 kernel: 81% busy, ncu). The FP64 face velocities are split
+// by integer operations (df_split, 2^-46 relative), the differences and sums
+// are pairs in k_div's order, and the value goes back to FP64 with one
+// addition. out_sum[0]: the sum of the written values (the pressure solve's
+// mean removal), each thread's pair sum reduced in a fixed order.
+__global__ void __launch_bounds__(kRedBlock) k_div_df(Dims d, double* __restrict__ out, const double* __restrict__ u,
+                                                     const double* __restrict__ v, const double* __restrict__ w,
+                                                     const double* __restrict__ top,
+                                                     const double* __restrict__ bottom, RedScratch sc,
+                                                     double* out_sum) {
+    const int x = blockIdx.x * kRBX + threadIdx.x, y = blockIdx.y * kRBY + threadIdx.y;
+    const df2 nn = {float(d.n), 0.f};
+    const df2 zero = {0.f, 0.f};
+    df2 acc = zero;
+    if (x < d.nx && y < d.ny)
+        for (int z = blockIdx.z; z < d.nz; z += gridDim.z) {
+            const long long i = lin(d, x, y, z);
+            df2 dv;
+            if (d.channel) {
+                const long long ixz = x + (long long)d.nx * z;
+                const df2 tv = top ? df_split(top[ixz]) : zero, bv = bottom ? df_split(bottom[ixz]) : zero;
+                if (d.ny == 1) dv = df_add(tv, df_neg(bv));
+                else if (y == 0) dv = df_add(df_split(v[lin(d, x, 1, z)]), df_neg(bv));
+                else if (y == d.ny - 1) dv = df_add(tv, df_neg(df_split(v[i])));
+                else dv = df_add(df_split(v[lin(d, x, y + 1, z)]), df_neg(df_split(v[i])));
+            } else {
+                dv = df_add(df_split(v[lin(d, x, yp1(d, y), z)]), df_neg(df_split(v[i])));
+            }
+            const df2 du = df_add(df_split(u[lin(d, xp1(d, x), y, z)]), df_neg(df_split(u[i])));
+            const df2 dw = df_add(df_split(w[lin(d, x, y, zp1(d, z))]), df_neg(df_split(w[i])));
+            const df2 r = df_mul(nn, df_add(df_add(du, dv), dw));
+            out[i] = f32_to_f64(r.hi) + f32_to_f64(r.lo);
+            acc = df_add(acc, r);
+        }
+    double a[1] = {f32_to_f64(acc.hi) + f32_to_f64(acc.lo)};
+    grid_sum<1>(a, sc, out_sum);
+}
+
 // Gradient, src/alg/grad.h:29-44.
 template <typename T>
 __global__ void k_grad(Dims d, T* __restrict__ px, T* __restrict__ py, T* __restrict__ pz, const T* __restrict__ p) {
@@ -1001,6 +1040,10 @@ void launch_advect_df(const Dims& d, float* ua, float* va, float* wa, const floa
 template <typename T>
 void launch_div(const Dims& d, T* out, const T* u, const T* v, const T* w, const T* top, const T* bottom, cudaStream_t s) {
     k_div<T><<<grid3(d), block3(), 0, s>>>(d, out, u, v, w, top, bottom);
+}
+void launch_div_df(const Dims& d, double* out, const double* u, const double* v, const double* w, const double* top,
+                   const double* bottom, RedScratch sc, double* out_sum, cudaStream_t s) {
+    k_div_df<<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, out, u, v, w, top, bottom, sc, out_sum);
 }
 template <typename T>
 void launch_grad(const Dims& d, T* px, T* py, T* pz, const T* p, cudaStream_t s) {

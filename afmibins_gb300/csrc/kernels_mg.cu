@@ -110,6 +110,51 @@ __global__ void __launch_bounds__(kRedBlock) k_lap_defect(Dims d, TD* __restrict
     grid_sum<1>(a, sc, out);
 }
 
+// Mixed form: the first defect of a pressure solve in double-float on the
+// FP32 pipe (the FP64 kernel is FP64-pipe bound: 81% busy, ncu), with the
+// mean removal of b folded in: r = (b - m) - n^2 (S - c x0), m = sum * scale
+// (the FP64 form's k_sub_scalar value; sum null: m = 0). lap_row's neighbour
+// sum in its order, each FP64 value split by integer operations (df_split),
+// c x0 and the n^2 scaling as pair products; the pair is the FP32 defect rh
+// and its rest rl of k_lap_update_df, out[0] = rh.rh.
+__global__ void __launch_bounds__(kRedBlock) k_lap_defect_df(Dims d, float* __restrict__ rh, float* __restrict__ rl,
+                                                            const double* __restrict__ xv,
+                                                            const double* __restrict__ b, const double* sum,
+                                                            double scale, RedScratch sc, double* out) {
+    const int xi = blockIdx.x * kRBX + threadIdx.x, yi = blockIdx.y * kRBY + threadIdx.y;
+    const df2 off = {float(d.n) * float(d.n), 0.f};  // exact for n < 4096
+    const df2 m = sum ? df_split(sum[0] * scale) : df2{0.f, 0.f};
+    float acc = 0.f;
+    if (xi < d.nx && yi < d.ny)
+        for (int zi = blockIdx.z; zi < d.nz; zi += gridDim.z) {
+            df2 S;
+            float c;
+            if (d.nz == 1) {
+                S = df_add(df_split(xv[lin(d, xm1(d, xi), yi, zi)]), df_split(xv[lin(d, xp1(d, xi), yi, zi)]));
+                c = 4.f;
+            } else {
+                S = df_add(df_add(df_split(xv[lin(d, xm1(d, xi), yi, zi)]), df_split(xv[lin(d, xp1(d, xi), yi, zi)])),
+                           df_add(df_split(xv[lin(d, xi, yi, zm1(d, zi))]), df_split(xv[lin(d, xi, yi, zp1(d, zi))])));
+                c = 6.f;
+            }
+            if (d.channel) {
+                if (yi > 0) S = df_add(S, df_split(xv[lin(d, xi, yi - 1, zi)])); else c -= 1.f;
+                if (yi < d.ny - 1) S = df_add(S, df_split(xv[lin(d, xi, yi + 1, zi)])); else c -= 1.f;
+            } else {
+                S = df_add(S, df_add(df_split(xv[lin(d, xi, ym1(d, yi), zi)]), df_split(xv[lin(d, xi, yp1(d, yi), zi)])));
+            }
+            const long long i = lin(d, xi, yi, zi);
+            const df2 cx = df_mul(df2{c, 0.f}, df_split(xv[i]));
+            const df2 L = df_mul(off, df_add(S, df_neg(cx)));
+            const df2 r = df_add(df_add(df_split(b[i]), df_neg(m)), df_neg(L));
+            rh[i] = r.hi;
+            rl[i] = r.lo;
+            acc += r.hi * r.hi;
+        }
+    double a[1] = {(double)acc};
+    grid_sum<1>(a, sc, out);
+}
+
 // Mixed form, recursive outer residual of the pressure solve: with the FP32
 // correction e of the inner V-cycles, x += e (FP64) and the residual, kept
 // as a double-float pair (rh: the FP32 right-hand side of the V-cycles, rl:
@@ -1783,6 +1828,10 @@ template <typename TD>
 void launch_lap_defect(const Dims& d, TD* r, const double* x, const double* b, RedScratch sc, double* out, cudaStream_t s,
                        float* r_lo) {
     k_lap_defect<TD><<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, r, x, b, sc, out, r_lo, lo_split());
+}
+void launch_lap_defect_df(const Dims& d, float* rh, float* rl, const double* x, const double* b, const double* sum,
+                          double scale, RedScratch sc, double* out, cudaStream_t s) {
+    k_lap_defect_df<<<red_grid3(d.nx, d.ny, d.nz), dim3(kRBX, kRBY), 0, s>>>(d, rh, rl, x, b, sum, scale, sc, out);
 }
 void launch_lap_update_df(const Dims& d, double* x, const float* e, float* rh, float* rl, RedScratch sc, double* out,
                           cudaStream_t s) {

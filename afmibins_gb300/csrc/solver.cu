@@ -103,6 +103,15 @@ struct afmib_solver {
     // AFMIB_FIRST_DF=1: measured 56.36 against 56.49 IB steps/s for the FP64
     // passes at 256^3, which run beside the other stream's corrections)
     bool first_df = false;
+    // mixed form: the divergence (with the sum of b) and the first pressure
+    // defect (with the mean removal folded in) in double-float on the FP32
+    // pipe; AFMIB_PROJ_DF=0 keeps the FP64 passes. At 256^3 the two run at
+    // about the FP64 kernels' time (238 / 283 against 233 / 267 us: the
+    // integer splits of the FP64 inputs make them issue-bound) and remove
+    // the mean pass (104 us per projection). A double-float gradient update
+    // measured slower (354 against 294 us) and is not used.
+    bool proj_df = true;
+    bool b_sum_ready = false;  // scal[8] holds the sum of lv[0].b (from the divergence)
     // mixed form with the double-float residual: the Crank-Nicolson viscous
     // solves start from uold (the step's start velocity), whose residual
     // comes pointwise from the kept Q, instead of the current velocity
@@ -335,7 +344,7 @@ const char* kProfNames[P_COUNT] = {
     "advect", "helm_rhs", "cg_init", "cg_apply", "cg_update", "cg_direction", "mg_rbgs", "mg_residual",
     "mg_residual_norm", "mg_restrict", "mg_prolong_add", "mg_coarse_cg", "div", "grad_sub", "mean_removal",
     "wall_update", "springs", "marker_prep", "radix_sort", "tile_bins", "spread_gather", "interp", "marker_update",
-    "helm_defect_fp64", "lap_defect_fp64", "add_correction_fp64", "advect_adjoint", "marker_adjoint",
+    "helm_defect_fp64", "lap_defect_first", "add_correction_fp64", "advect_adjoint", "marker_adjoint",
     "mg_rbgs_fine", "mg_residual_fine", "mg_restrict_fine", "mg_prolong_add_fine", "cg_dir_apply", "mg_coarse_tail",
     "helm_inner_sweep_fp32", "helm_update_df", "lap_update_df", "mg_resid_restrict_fine", "mg_resid_restrict"};
 
@@ -984,21 +993,29 @@ int mg_solve_mixed(afmib_solver* s, int* cycles) {
     MGLevelT<float>& L32 = s->lv32[0];
     const long long N = L.d.ncell();
     const double Ns = (double)N * sizeof(double);
-    {
-        ProfScope ps(s, P_MEAN, 3 * Ns, 2);
-        launch_sum<double>(N, L.b, s->red, s->scal + 8, s->st);
-        launch_sub_scalar_scaled<double>(N, L.b, s->scal + 8, 1.0 / (double)N, s->st);
+    const bool df = lap_df_on(s);
+    // double-float first defect: b's mean is subtracted inside it (b is read
+    // by the first defect only; the later ones are the recursive updates)
+    const bool fuse_mean = df && s->proj_df;
+    if (!s->b_sum_ready || !fuse_mean) {
+        ProfScope ps(s, P_MEAN, (s->b_sum_ready ? 0 : Ns) + (fuse_mean ? 0 : 2 * Ns),
+                     (s->b_sum_ready ? 0 : 1) + (fuse_mean ? 0 : 1));
+        if (!s->b_sum_ready) launch_sum<double>(N, L.b, s->red, s->scal + 8, s->st);
+        if (!fuse_mean) launch_sub_scalar_scaled<double>(N, L.b, s->scal + 8, 1.0 / (double)N, s->st);
     }
+    s->b_sum_ready = false;
     TRY(initial_potential(s));
     CK(cudaMemsetAsync(s->dflag + 1, 0, sizeof(int), s->st));
     int c = 0, outer = 0, last_cyc = 0;
     double last_rms = 0.0;
     int status = AFMIB_OK;
-    const bool df = lap_df_on(s);
     for (;;) {
         if (!(df && outer > 0)) {  // double-float: the norm came with the last block's update
-            ProfScope ps(s, P_LAP_DEFECT, (double)N * (8 + 8 + 4));
-            if (!s->bfp_defects || !launch_lap_defect_bfp(L.d, L32.b, L.x, L.b, s->red, s->scal + 9, s->st))
+            ProfScope ps(s, P_LAP_DEFECT, (double)N * (8 + 8 + 4 + (df ? 4 : 0)));
+            if (fuse_mean)
+                launch_lap_defect_df(L.d, L32.b, s->plo, L.x, L.b, s->scal + 8, 1.0 / (double)N, s->red, s->scal + 9,
+                                     s->st);
+            else if (!s->bfp_defects || !launch_lap_defect_bfp(L.d, L32.b, L.x, L.b, s->red, s->scal + 9, s->st))
                 launch_lap_defect<float>(L.d, L32.b, L.x, L.b, s->red, s->scal + 9, s->st, df ? s->plo : nullptr);
         }
         CKL();
@@ -1034,9 +1051,16 @@ int mg_solve_mixed(afmib_solver* s, int* cycles) {
 // ns::projection::project, src/ns/projection.h:60-73
 int project(afmib_solver* s) {
     const double Ns = (double)s->N() * sizeof(double);
+    const bool pdf = s->mixed && s->proj_df;
+    s->b_sum_ready = false;
     {
         ProfScope ps(s, P_DIV, 4 * Ns);
-        launch_div<double>(s->d, s->lv[0].b, s->u, s->v, s->w, nullptr, nullptr, s->st);
+        if (pdf) {
+            launch_div_df(s->d, s->lv[0].b, s->u, s->v, s->w, nullptr, nullptr, s->red, s->scal + 8, s->st);
+            s->b_sum_ready = true;
+        } else {
+            launch_div<double>(s->d, s->lv[0].b, s->u, s->v, s->w, nullptr, nullptr, s->st);
+        }
     }
     CKL();
     if (s->mixed) TRY(mg_solve_mixed(s, nullptr));
@@ -1906,6 +1930,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_ADVECT64")) s->advect64 = std::string(e) == "1";
     if (const char* e = std::getenv("AFMIB_ADVECT_DF")) s->advect_df = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_FIRST_DF")) s->first_df = std::string(e) == "1";
+    if (const char* e = std::getenv("AFMIB_PROJ_DF")) s->proj_df = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_CN_START_OLD")) s->cn_start_old = std::string(e) != "0";
     if (s->mixed && s->fused_rhs)
         for (auto& q : s->qo) TRY(dalloc(s, &q, N));

@@ -91,7 +91,7 @@ def workload(n, shells, per_shell, radius, min_sep, seed_offset=0):
 
 # Kernel families whose time is not set by HBM bandwidth: FP64 arithmetic
 # (1/69 of the FP32 rate on GB300) and the latency-bound spreading gather.
-NOT_HBM_BOUND = {"helm_defect_fp64", "lap_defect_fp64", "helm_rhs", "spread_gather", "mg_coarse_tail",
+NOT_HBM_BOUND = {"helm_defect_fp64", "lap_defect_first", "helm_rhs", "spread_gather", "mg_coarse_tail",
                  "mg_coarse_cg"}
 # Families of the mixed form's interleaved viscous solves (defects on one
 # stream, corrections on another).
