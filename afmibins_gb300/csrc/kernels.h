@@ -240,10 +240,14 @@ void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s, in
 template <typename T>
 void launch_prolong_add(const Dims& d, T* fine, const T* coarse, cudaStream_t s, int rev = 0);
 // coarse_b = restriction of (b - L x), coarse_x = 0, in one pass (the
-// residual stays in shared memory); for the levels resid_restrict_fused_ok
-// takes (opt-in, AFMIB_RESID_RESTRICT=1: 3D power-of-two levels with
-// nx >= 256 by default)
-bool resid_restrict_fused_ok(const Dims& d);
+// residual stays in shared memory), for the levels resid_restrict_fused_ok
+// takes: by default FP32 3D power-of-two levels with nx >= 256 (the column
+// kernel); AFMIB_RESID_RESTRICT=1 the ring kernel, =0 none
+bool resid_restrict_fused_ok(const Dims& d, size_t elem, const void* x, const void* b, const void* cb,
+                             const void* cx);
+// shared-memory opt-ins of the multigrid kernels (once per device, before
+// any launch or stream capture)
+void mg_kernel_attributes();
 template <typename T>
 void launch_resid_restrict(const Dims& d, T* coarse_b, T* coarse_x, const T* x, const T* b, cudaStream_t s,
                            int rev = 0);

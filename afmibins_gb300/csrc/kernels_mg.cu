@@ -1153,6 +1153,218 @@ __global__ void __launch_bounds__(32 * kTrBY) k_restrict_cols(Dims d, T* __restr
     pipe::wait_pending<0>();
 }
 
+// FP32 fine-level residual fused with the column restriction: the block of
+// k_restrict_cols (64 coarse x, kTrBY coarse y, CZ coarse planes) forms the
+// residual r = b - L x of each fine plane of its tile in shared memory and
+// restricts from there, so the fine residual never goes to memory. x planes
+// (rows 2 yc0 - 2 .. 2 yc0 + 17, 36 16-byte chunks a row from x = 2 xc0 - 8)
+// and b planes (rows 2 yc0 - 1 .. 2 yc0 + 16, 34 chunks from 2 xc0 - 4)
+// arrive by asynchronous copies issued two planes ahead into rings of kRrX
+// and kRrB slots; per fine plane there are two barriers (the plane's inputs
+// are in and the previous taps are done / the residual plane is written).
+// The residual plane holds 34 chunks a row (x = 2 xc0 - 4 .. 2 xc0 + 131, the
+// layout k_restrict_cols stages): each thread forms whole chunks, four cells
+// from 16-byte words and the cells on either side by single loads. Every
+// residual is k_residual_z2's expression in its order and the taps are
+// k_restrict_cols' (restrict_cell2's order), so the coarse right-hand side
+// equals the two kernels' bit for bit. In channel mode the rows beyond the
+// walls take the residual of the wall row, as the restriction's clamped taps
+// read it.
+constexpr int kRrX = 4, kRrB = 4, kRrXRows = 2 * kTrBY + 4;
+constexpr int kRrXW = 144, kRrW = 136;  // floats a staged x row (36 chunks) / b and residual row (34)
+constexpr int kRrTasks = kTrRows * 34;  // residual chunks a plane
+constexpr int kRrPT = (kRrTasks + 32 * kTrBY - 1) / (32 * kTrBY);
+constexpr size_t kRrSmem = sizeof(float) * ((size_t)kRrX * kRrXRows * kRrXW + (size_t)kRrB * kTrRows * kRrW +
+                                            (size_t)kTrRows * kRrW);
+
+template <int CZ, bool CH>
+__global__ void __launch_bounds__(32 * kTrBY, 2) k_resid_restrict_cols(Dims d, float* __restrict__ cb,
+                                                                    float* __restrict__ cxz,
+                                                                    const float* __restrict__ xv,
+                                                                    const float* __restrict__ bv, int rev) {
+    constexpr int NP = 2 * CZ + 2;  // fine planes restricted (residuals formed)
+    constexpr int NI = NP + 2;      // staged items: x planes 2 zc0 - 2 .. 2 zc0 + 2 CZ + 1
+    constexpr int XCH = (kRrXRows * 36 + 32 * kTrBY - 1) / (32 * kTrBY);
+    constexpr int BCH = (kTrRows * 34 + 32 * kTrBY - 1) / (32 * kTrBY);
+    extern __shared__ __align__(16) float rr_smem[];
+    float* xs = rr_smem;                          // [kRrX][kRrXRows][kRrXW]
+    float* bs = xs + kRrX * kRrXRows * kRrXW;     // [kRrB][kTrRows][kRrW]
+    float* rs = bs + kRrB * kTrRows * kRrW;       // [kTrRows][kRrW]
+    const Ix2 I(d);
+    const uint3 B = block_at(rev);
+    const int lane = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + lane;
+    const int xc0 = B.x * 64, yc0 = B.y * kTrBY, zc0 = B.z * CZ;
+    auto yrow = [&](int y) {  // a row in range: clamped at channel walls, wrapped otherwise
+        if (CH) return y < 0 ? 0 : (y > d.ny - 1 ? d.ny - 1 : y);
+        return y & I.my;
+    };
+    // this thread's chunks of every x / b plane: source offset within the
+    // plane (-1: none), destination offset within the slot
+    int xsrc[XCH], xdst[XCH], bsrc[BCH], bdst[BCH];
+#pragma unroll
+    for (int u = 0; u < XCH; ++u) {
+        const int c = tid + u * 32 * kTrBY;
+        xsrc[u] = -1;
+        xdst[u] = 0;
+        if (c < kRrXRows * 36) {
+            const int j = c / 36, k = c - j * 36;
+            xsrc[u] = ((2 * xc0 - 8 + 4 * k) & I.mx) | (yrow(2 * yc0 - 2 + j) << I.lx);
+            xdst[u] = j * kRrXW + 4 * k;
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < BCH; ++u) {
+        const int c = tid + u * 32 * kTrBY;
+        bsrc[u] = -1;
+        bdst[u] = 0;
+        if (c < kTrRows * 34) {
+            const int j = c / 34, k = c - j * 34;
+            bsrc[u] = ((2 * xc0 - 4 + 4 * k) & I.mx) | (yrow(2 * yc0 - 1 + j) << I.lx);
+            bdst[u] = j * kRrW + 4 * k;
+        }
+    }
+    // this thread's residual chunks: residual row jr, chunk k (cells
+    // x = 2 xc0 - 4 + 4 k ..); the x-tile row of the residual's row (channel:
+    // the wall row for the rows beyond it) and its wall flags
+    int tr[kRrPT], tx[kRrPT], tb[kRrPT];
+    bool tym[kRrPT], typ[kRrPT];
+#pragma unroll
+    for (int u = 0; u < kRrPT; ++u) {
+        const int t = tid + u * 32 * kTrBY;
+        tr[u] = -1;
+        tx[u] = 0;
+        tb[u] = 0;
+        tym[u] = typ[u] = true;
+        if (t < kRrTasks) {
+            const int jr = t / 34, k = t - jr * 34;
+            const int y = 2 * yc0 - 1 + jr;
+            const int ye = CH ? (y < 0 ? 0 : (y > d.ny - 1 ? d.ny - 1 : y)) : y;
+            const int jx = ye - (2 * yc0 - 2);
+            tr[u] = jr * kRrW + 4 * k;
+            tb[u] = jr * kRrW + 4 * k;
+            tx[u] = jx * kRrXW + 4 * k + 4;
+            tym[u] = !CH || ye > 0;
+            typ[u] = !CH || ye < d.ny - 1;
+        }
+    }
+    // item k: x plane 2 zc0 - 2 + k, and b of the same plane for 1 <= k <= NP;
+    // one commit group per item, empty past the last
+    auto issue = [&](int k) {
+        if (k < NI) {
+            const int zo = ((2 * zc0 - 2 + k) & I.mz) << I.lxy;
+            float* xd = xs + (k % kRrX) * kRrXRows * kRrXW;
+            const float* xsp = xv + zo;
+#pragma unroll
+            for (int u = 0; u < XCH; ++u)
+                if (xsrc[u] >= 0) pipe::cp16(xd + xdst[u], xsp + xsrc[u]);
+            if (k >= 1 && k <= NP) {
+                float* bd = bs + (k % kRrB) * kTrRows * kRrW;
+                const float* bsp = bv + zo;
+#pragma unroll
+                for (int u = 0; u < BCH; ++u)
+                    if (bsrc[u] >= 0) pipe::cp16(bd + bdst[u], bsp + bsrc[u]);
+            }
+        }
+        pipe::commit();
+    };
+    const float off = float(d.n) * float(d.n);
+    auto cell = [&](float x0, float xl, float xr, float zm, float zp, float ym, float yp, float b, bool hm, bool hp) {
+        float S = (xl + xr) + (zm + zp);
+        float c = 6.f;
+        if (CH) {
+            if (hm) S += ym; else c -= 1.f;
+            if (hp) S += yp; else c -= 1.f;
+        } else {
+            S += ym + yp;
+        }
+        return b - off * (S - c * x0);
+    };
+    // residual chunks of fine plane i (fine z = 2 zc0 - 1 + i) into rs
+    auto resid = [&](int i) {
+        const float* xc = xs + ((i + 1) % kRrX) * kRrXRows * kRrXW;
+        const float* xm = xs + (i % kRrX) * kRrXRows * kRrXW;        // z - 1
+        const float* xp = xs + ((i + 2) % kRrX) * kRrXRows * kRrXW;  // z + 1
+        const float* bp = bs + ((i + 1) % kRrB) * kTrRows * kRrW;
+#pragma unroll
+        for (int u = 0; u < kRrPT; ++u) {
+            if (tr[u] < 0) break;
+            const float* c0 = xc + tx[u];
+            const float4 v = *reinterpret_cast<const float4*>(c0);
+            const float4 vym = *reinterpret_cast<const float4*>(c0 - kRrXW);
+            const float4 vyp = *reinterpret_cast<const float4*>(c0 + kRrXW);
+            const float4 vzm = *reinterpret_cast<const float4*>(xm + tx[u]);
+            const float4 vzp = *reinterpret_cast<const float4*>(xp + tx[u]);
+            const float4 vb = *reinterpret_cast<const float4*>(bp + tb[u]);
+            const float l = c0[-1], r = c0[4];
+            const bool hm = tym[u], hp = typ[u];
+            float4 o;
+            o.x = cell(v.x, l, v.y, vzm.x, vzp.x, vym.x, vyp.x, vb.x, hm, hp);
+            o.y = cell(v.y, v.x, v.z, vzm.y, vzp.y, vym.y, vyp.y, vb.y, hm, hp);
+            o.z = cell(v.z, v.y, v.w, vzm.z, vzp.z, vym.z, vyp.z, vb.z, hm, hp);
+            o.w = cell(v.w, v.z, r, vzm.w, vzp.w, vym.w, vyp.w, vb.w, hm, hp);
+            *reinterpret_cast<float4*>(rs + tr[u]) = o;
+        }
+    };
+    const float wgt[4] = {1.f, 3.f, 3.f, 1.f};
+    // the restriction taps of the residual plane for this thread: e[ky][1 + q]
+    // = fine x = 2 xc0 + 4 lane + q, q = -1 .. 4 (k_restrict_cols' taps)
+    auto taps = [&](float (&e)[4][6]) {
+#pragma unroll
+        for (int ky = 0; ky < 4; ++ky) {
+            const float* row = rs + (2 * ty + ky) * kRrW + 4;  // fine x = 2 xc0
+            const float4 q = *reinterpret_cast<const float4*>(row + 4 * lane);
+            float l = __shfl_up_sync(0xffffffffu, q.w, 1), r = __shfl_down_sync(0xffffffffu, q.x, 1);
+            if (lane == 0) l = row[-1];
+            if (lane == 31) r = row[128];
+            e[ky][0] = l;
+            e[ky][1] = q.x;
+            e[ky][2] = q.y;
+            e[ky][3] = q.z;
+            e[ky][4] = q.w;
+            e[ky][5] = r;
+        }
+    };
+    auto add = [&](float (&acc)[2], const float (&e)[4][6], int kz) {
+#pragma unroll
+        for (int ky = 0; ky < 4; ++ky)
+#pragma unroll
+            for (int m = 0; m < 2; ++m)
+#pragma unroll
+                for (int kx = 0; kx < 4; ++kx)
+                    acc[m] += (wgt[kx] * wgt[ky] * wgt[kz] / 512.f) * e[ky][2 * m + kx];
+    };
+#pragma unroll
+    for (int k = 0; k < 4; ++k) issue(k);
+    float acc[2] = {0.f, 0.f}, next[2] = {0.f, 0.f}, e[4][6];
+    const int co = (xc0 + 2 * lane) | ((yc0 + ty) << (I.lx - 1));
+    for (int i = 0; i < NP; ++i) {
+        pipe::wait_pending<1>();  // items <= i + 2 are in
+        __syncthreads();          // ... for every thread; the last plane's taps are done
+        resid(i);
+        __syncthreads();          // the residual plane is written; x item i and b item i + 1 are free
+        issue(i + 4);
+        taps(e);
+        if (i == 0) {
+            add(acc, e, 0);
+        } else if (i == 1) {
+            add(acc, e, 1);
+        } else if ((i & 1) == 0) {
+            add(acc, e, 2);
+            add(next, e, 0);
+        } else {
+            add(acc, e, 3);
+            add(next, e, 1);
+            const int o = co | ((zc0 + (i - 3) / 2) << (I.lxy - 2));
+            *reinterpret_cast<float2*>(cb + o) = make_float2(acc[0], acc[1]);
+            *reinterpret_cast<float2*>(cxz + o) = make_float2(0.f, 0.f);
+            acc[0] = next[0];
+            acc[1] = next[1];
+            next[0] = next[1] = 0.f;
+        }
+    }
+    pipe::wait_pending<0>();
+}
+
 // Trilinear prolongation-add with prolong_cell2's expressions. A thread owns
 // the fine pairs x = 2t, 2t+1 of rows y = 2s, 2s+1 in planes z = 2r, 2r+1:
 // fine cell 2t + 1 is the first (xcf) of coarse cell t and 2t the second
@@ -1774,21 +1986,84 @@ void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s, in
     if (d.nz > 1 && d.nx >= 2 && d.ny >= 2 && ix2_ok(d)) k_restrict2<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine, rev);
     else k_restrict<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine);
 }
-// Opt-in (AFMIB_RESID_RESTRICT=1): levels with nx >= AFMIB_RESID_RESTRICT_MIN_NX
-// (default 256) then take the fused kernel (on smaller levels its grid of
-// 2 RR_T x 2 RR_T fine columns per block leaves SMs idle). Both switches are
-// read at every call, so that a test can compare the two paths in one process.
-bool resid_restrict_fused_ok(const Dims& d) {
+// Fine-level residual and restriction in one pass. AFMIB_RESID_RESTRICT
+// (read at every call, so that a test can compare the paths in one process):
+// unset or "2": the column kernel (k_resid_restrict_cols) on FP32 levels it
+// fits (3D power-of-two, 64 | nx / 2, kTrBY | ny / 2, 16-byte aligned arrays,
+// nx >= AFMIB_RR_COLS_MIN_NX, default 256); "1": the ring kernel
+// (k_resid_restrict2) on levels with nx >= AFMIB_RESID_RESTRICT_MIN_NX
+// (default 256; on smaller levels its grid of 2 RR_T x 2 RR_T fine columns
+// per block leaves SMs idle); "0": the residual and restriction kernels.
+static int rr_mode(const Dims& d, size_t elem, const void* x, const void* b, const void* cb, const void* cx) {
     const char* e = std::getenv("AFMIB_RESID_RESTRICT");
-    if (!(e && e[0] == '1')) return false;
-    const char* m = std::getenv("AFMIB_RESID_RESTRICT_MIN_NX");
-    const int min_nx = m ? std::atoi(m) : 256;
-    return d.nz > 1 && d.nx >= min_nx && d.nx >= 2 * RR_T && d.ny >= 2 * RR_T && d.nz >= 4 && ix2_ok(d);
+    const char m = e ? e[0] : '2';
+    if (m == '1') {
+        const char* mn = std::getenv("AFMIB_RESID_RESTRICT_MIN_NX");
+        const int min_nx = mn ? std::atoi(mn) : 256;
+        return d.nz > 1 && d.nx >= min_nx && d.nx >= 2 * RR_T && d.ny >= 2 * RR_T && d.nz >= 4 && ix2_ok(d) ? 1 : 0;
+    }
+    if (m != '2' || elem != sizeof(float)) return 0;
+    const char* mn = std::getenv("AFMIB_RR_COLS_MIN_NX");
+    const int min_nx = mn ? std::atoi(mn) : 256;
+    const bool aligned = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(b) |
+                           reinterpret_cast<uintptr_t>(cb) | reinterpret_cast<uintptr_t>(cx)) & 15) == 0;
+    return d.nz > 1 && d.nx >= min_nx && ix2_ok(d) && (d.nx / 2) % 64 == 0 && (d.ny / 2) % kTrBY == 0 && aligned
+               ? 2
+               : 0;
+}
+bool resid_restrict_fused_ok(const Dims& d, size_t elem, const void* x, const void* b, const void* cb,
+                             const void* cx) {
+    return rr_mode(d, elem, x, b, cb, cx) != 0;
 }
 
-// coarse planes per block: 8 where that still gives two blocks per SM, else 2
+void mg_kernel_attributes() {
+    auto set = [](const void* f) { cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRrSmem); };
+    set((const void*)k_resid_restrict_cols<8, false>);
+    set((const void*)k_resid_restrict_cols<4, false>);
+    set((const void*)k_resid_restrict_cols<2, false>);
+    set((const void*)k_resid_restrict_cols<1, false>);
+    set((const void*)k_resid_restrict_cols<8, true>);
+    set((const void*)k_resid_restrict_cols<4, true>);
+    set((const void*)k_resid_restrict_cols<2, true>);
+    set((const void*)k_resid_restrict_cols<1, true>);
+}
+
 template <typename T>
 void launch_resid_restrict(const Dims& d, T* coarse_b, T* coarse_x, const T* x, const T* b, cudaStream_t s, int rev) {
+    if constexpr (sizeof(T) == sizeof(float)) {
+        if (rr_mode(d, sizeof(T), x, b, coarse_b, coarse_x) == 2) {
+            // coarse planes per block: the largest of 8, 4, 2 that leaves at least
+            // AFMIB_RR_MIN_BLOCKS (default 512) blocks (two resident per SM)
+            const char* e = std::getenv("AFMIB_RR_MIN_BLOCKS");
+            const long long min_blocks = e ? std::atoll(e) : 512;
+            const long long cols = (long long)(d.nx / 2 / 64) * (d.ny / 2 / kTrBY);
+            const int cz = d.nz / 2;
+            int z = 1;
+            for (int c : {8, 4, 2})
+                if (cz % c == 0 && cols * (cz / c) >= min_blocks) {
+                    z = c;
+                    break;
+                }
+            const dim3 g(d.nx / 2 / 64, d.ny / 2 / kTrBY, cz / z), blk(32, kTrBY);
+            float* cbf = reinterpret_cast<float*>(coarse_b);
+            float* cxf = reinterpret_cast<float*>(coarse_x);
+            const float* xf = reinterpret_cast<const float*>(x);
+            const float* bf = reinterpret_cast<const float*>(b);
+#define AFMIB_RR_COLS(CZV)                                                                            \
+    do {                                                                                              \
+        if (d.channel) k_resid_restrict_cols<CZV, true><<<g, blk, kRrSmem, s>>>(d, cbf, cxf, xf, bf, rev); \
+        else k_resid_restrict_cols<CZV, false><<<g, blk, kRrSmem, s>>>(d, cbf, cxf, xf, bf, rev);         \
+    } while (0)
+            if (z == 8) AFMIB_RR_COLS(8);
+            else if (z == 4) AFMIB_RR_COLS(4);
+            else if (z == 2) AFMIB_RR_COLS(2);
+            else AFMIB_RR_COLS(1);
+#undef AFMIB_RR_COLS
+            return;
+        }
+    }
+    // the ring kernel: coarse planes per block 8 where that still gives two
+    // blocks per SM, else 2
     const int cols = (d.nx / 2 / RR_T) * (d.ny / 2 / RR_T), cz = d.nz / 2;
     if (cz % 8 == 0 && cols * (cz / 8) >= 2 * 152)
         k_resid_restrict2<T, 8><<<dim3(d.nx / 2 / RR_T, d.ny / 2 / RR_T, cz / 8), RR_THREADS, 0, s>>>(

@@ -567,7 +567,7 @@ int vcycle(afmib_solver* s, size_t l) {
     const bool fine = l == 0;
     TRY(smooth(s, L, sizeof(T) == sizeof(float) ? (fine ? s->inner_nu1 : s->inner_nu1c) : s->cfg.nu1));
     MGLevelT<T>& C = lv[l + 1];
-    if (resid_restrict_fused_ok(L.d)) {
+    if (resid_restrict_fused_ok(L.d, sizeof(T), L.x, L.b, C.b, C.x)) {
         // x, b read; coarse b and x written (the fine residual stays on chip)
         ProfScope ps(s, fine ? P_RESID_RESTRICT0 : P_RESID_RESTRICT, 2 * Ns + 2 * Ns / 8);
         launch_resid_restrict<T>(L.d, C.b, C.x, L.x, L.b, s->st, pass_dir(s, L.d, sizeof(T)));
@@ -1852,6 +1852,7 @@ int setup_tiles(afmib_solver* s) {
 int create(afmib_solver* s, const afmib_config* c, void* stream) {
     s->cfg = *c;
     afmib_config& g = s->cfg;
+    mg_kernel_attributes();  // before any capture of the V-cycles
     if (g.n <= 0) g.n = g.nx;
     if (g.nu1 <= 0) g.nu1 = 2;
     if (g.nu2 <= 0) g.nu2 = 2;

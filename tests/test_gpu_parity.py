@@ -917,6 +917,48 @@ def test_fused_residual_restriction_keeps_bits(monkeypatch, bc, precision):
         assert np.array_equal(a, c)
 
 
+@pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
+def test_column_residual_restriction_keeps_bits(monkeypatch, bc):
+    """Mixed form: the FP32 fine-level residual fused with the column
+    restriction (k_resid_restrict_cols: x and b planes staged by asynchronous
+    copies, the residual plane kept in shared memory; the default on levels of
+    256 cells and up, taken here from 128) against the residual and
+    restriction kernels (AFMIB_RESID_RESTRICT=0): multigrid solves agree bit
+    for bit with 8, 4 or 1 coarse planes per block, and so do IB steps."""
+    monkeypatch.setenv("AFMIB_RR_COLS_MIN_NX", "128")
+    for shape in ((128, 128, 128), (256, 256, 256), (256, 128, 64)):
+        nx, ny, nz = shape
+        b = np.random.default_rng(6).standard_normal(nx * ny * nz)
+        b -= b.mean()
+        out = {}
+        for mode, min_blocks in (("0", None), ("2", None), ("2", "1"), ("2", "100000000")):
+            monkeypatch.setenv("AFMIB_RESID_RESTRICT", mode)
+            if min_blocks:
+                monkeypatch.setenv("AFMIB_RR_MIN_BLOCKS", min_blocks)
+            else:
+                monkeypatch.delenv("AFMIB_RR_MIN_BLOCKS", raising=False)
+            with capi.Solver(nx, ny, nz, n=nx, bc=bc, precision=capi.MIXED, tol=1e-10) as sv:
+                out[(mode, min_blocks)] = sv.mg_solve(b)
+        ref = out[("0", None)]
+        for key, (x, cycles) in out.items():
+            assert cycles == ref[1] and np.array_equal(x, ref[0]), (shape, key)
+    monkeypatch.delenv("AFMIB_RR_MIN_BLOCKS", raising=False)
+    g, u, v, w, X, nstart, nidx = _periodic_case(128, M=2000, seed=4)
+    if bc == capi.BC_CHANNEL:
+        v = v[: g.nx * (g.ny - 1) * g.nz]
+    res = {}
+    for mode in ("0", "2"):
+        monkeypatch.setenv("AFMIB_RESID_RESTRICT", mode)
+        with capi.Solver(128, bc=bc, precision=capi.MIXED, mu=0.01, dt=1e-3, tol=1e-10, k_spring=0.5) as sv:
+            sv.set_velocity(u, v, w)
+            sv.project()
+            sv.set_markers(X, nstart, nidx)
+            sv.ib_step(2)
+            res[mode] = (*sv.get_velocity(), sv.get_pressure(), sv.get_markers())
+    for a, c in zip(res["0"], res["2"]):
+        assert np.array_equal(a, c)
+
+
 @pytest.mark.parametrize("precision,bar", [(capi.FP64, TOL), (capi.MIXED, 1e-8)])
 def test_ns_substeps_moving_walls(golden, precision, bar):
     """Four channel sub-steps with seeded nonzero wall velocities (ut, ub, wt,
