@@ -605,10 +605,16 @@ __device__ __forceinline__ df2 dfacc_pair(DfAcc a) {
 
 constexpr int kInterpDfBlock = 128;
 
+template <bool PAIRS>
 __global__ void __launch_bounds__(kInterpDfBlock) k_interp_dfl(Dims d, int M, const int* __restrict__ perm,
                                                                MarkerW<double> mw, const double* __restrict__ u,
                                                                const double* __restrict__ v,
-                                                               const double* __restrict__ w, double* __restrict__ U) {
+                                                               const double* __restrict__ w, const float* __restrict__ uh,
+                                                               const float* __restrict__ ul,
+                                                               const float* __restrict__ vh,
+                                                               const float* __restrict__ vl,
+                                                               const float* __restrict__ wh,
+                                                               const float* __restrict__ wl, double* __restrict__ U) {
     const int p = (blockIdx.x * kInterpDfBlock + threadIdx.x) >> 2;
     const int q = threadIdx.x & 3;
     if (p >= M) return;  // a quad leaves together
@@ -628,11 +634,28 @@ __global__ void __launch_bounds__(kInterpDfBlock) k_interp_dfl(Dims d, int M, co
 #pragma unroll
             for (int my = 0; my < 4; ++my)
                 roff[mz][my] = (long long)d.nx * (wrapi(by + my, d.ny) + (long long)d.ny * wrapi(bz + mz, d.nz)) + ix;
-        double val[4][4];
+        df2 val[4][4];
+        if (PAIRS) {  // the velocity's float pairs (hi + lo), no splits
+            const float* sh = comp == 0 ? uh : (comp == 1 ? vh : wh);
+            const float* sl = comp == 0 ? ul : (comp == 1 ? vl : wl);
 #pragma unroll
-        for (int mz = 0; mz < 4; ++mz)
+            for (int mz = 0; mz < 4; ++mz)
 #pragma unroll
-            for (int my = 0; my < 4; ++my) val[mz][my] = src[roff[mz][my]];
+                for (int my = 0; my < 4; ++my) {
+                    val[mz][my].hi = sh[roff[mz][my]];
+                    val[mz][my].lo = sl[roff[mz][my]];
+                }
+        } else {
+            double dv[4][4];
+#pragma unroll
+            for (int mz = 0; mz < 4; ++mz)
+#pragma unroll
+                for (int my = 0; my < 4; ++my) dv[mz][my] = src[roff[mz][my]];
+#pragma unroll
+            for (int mz = 0; mz < 4; ++mz)
+#pragma unroll
+                for (int my = 0; my < 4; ++my) val[mz][my] = df_split(dv[mz][my]);
+        }
         const double* wyp = mw.w + (((size_t)k * 3 + 1) * 2 + vy) * 4;
         const double* wzp = mw.w + (((size_t)k * 3 + 2) * 2 + vz) * 4;
         DfAcc az = {0.f, 0.f};
@@ -640,7 +663,7 @@ __global__ void __launch_bounds__(kInterpDfBlock) k_interp_dfl(Dims d, int M, co
         for (int mz = 0; mz < 4; ++mz) {
             DfAcc ay = {0.f, 0.f};
 #pragma unroll
-            for (int my = 0; my < 4; ++my) dfacc_mul_add(ay, df_split(wyp[my]), df_split(val[mz][my]));
+            for (int my = 0; my < 4; ++my) dfacc_mul_add(ay, df_split(wyp[my]), val[mz][my]);
             dfacc_mul_add(az, df_split(wzp[mz]), dfacc_pair(ay));
         }
         const df2 wxq = df_split(mw.w[(((size_t)k * 3 + 0) * 2 + vx) * 4 + q]);
@@ -792,9 +815,15 @@ void launch_interp(const Dims& d, int M, const int* perm, MarkerW<T> mw, const T
 }
 
 void launch_interp_dfl(const Dims& d, int M, const int* perm, MarkerW<double> mw, const double* u, const double* v,
-                       const double* w, double* U, cudaStream_t s) {
-    if (M > 0) k_interp_dfl<<<(int)((4LL * M + kInterpDfBlock - 1) / kInterpDfBlock), kInterpDfBlock, 0, s>>>(
-        d, M, perm, mw, u, v, w, U);
+                       const double* w, double* U, cudaStream_t s, const float* uh, const float* ul, const float* vh,
+                       const float* vl, const float* wh, const float* wl) {
+    if (M <= 0) return;
+    const int blocks = (int)((4LL * M + kInterpDfBlock - 1) / kInterpDfBlock);
+    if (uh && ul && vh && vl && wh && wl)
+        k_interp_dfl<true><<<blocks, kInterpDfBlock, 0, s>>>(d, M, perm, mw, u, v, w, uh, ul, vh, vl, wh, wl, U);
+    else
+        k_interp_dfl<false><<<blocks, kInterpDfBlock, 0, s>>>(d, M, perm, mw, u, v, w, nullptr, nullptr, nullptr,
+                                                               nullptr, nullptr, nullptr, U);
 }
 
 void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, double c, cudaStream_t s) {

@@ -70,8 +70,12 @@ void launch_interp(const Dims& d, int M, const int* perm, MarkerW<T> mw, const T
 
 // The FP64 interpolation in double-float on the FP32 pipe (axis-by-axis sums,
 // relative error a few units of 2^-46 of the largest term): the mixed form.
+// uh/ul, vh/vl, wh/wl (all given or none): the velocity's float pairs
+// (hi + lo = u to 2^-46), read instead of splitting the FP64 values.
 void launch_interp_dfl(const Dims& d, int M, const int* perm, MarkerW<double> mw, const double* u, const double* v,
-                       const double* w, double* U, cudaStream_t s);
+                       const double* w, double* U, cudaStream_t s, const float* uh = nullptr,
+                       const float* ul = nullptr, const float* vh = nullptr, const float* vl = nullptr,
+                       const float* wh = nullptr, const float* wl = nullptr);
 
 void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, double c, cudaStream_t s);
 

@@ -111,7 +111,11 @@ struct afmib_solver {
     // the mean pass (104 us per projection). A double-float gradient update
     // measured slower (354 against 294 us) and is not used.
     bool proj_df = true;
-    bool b_sum_ready = false;  // scal[8] holds the sum of lv[0].b (from the divergence)
+    bool b_sum_ready = false;
+    // mixed form: the double-float interpolation of the step's velocity reads
+    // its float pairs (written by the projection) instead of splitting the
+    // FP64 values (AFMIB_INTERP_PAIRS=0: splits)
+    bool interp_pairs = true;  // scal[8] holds the sum of lv[0].b (from the divergence)
     // mixed form with the double-float residual: the Crank-Nicolson viscous
     // solves start from uold (the step's start velocity), whose residual
     // comes pointwise from the kept Q, instead of the current velocity
@@ -1441,11 +1445,16 @@ int check_marker_flag(afmib_solver* s) {
     return AFMIB_OK;
 }
 
+// pairs: u, v, w are the solver's velocity and its float pairs (u32 +
+// u32l, ...) are current (after a projection or a velocity set)
 int interp_markers(afmib_solver* s, const double* u, const double* v, const double* w, double* U, bool fp32 = false,
-                   bool dfloat = false) {
+                   bool dfloat = false, bool pairs = false) {
     const double touched = (double)s->stats.spread_tiles * s->tile_cells();
     ProfScope ps(s, P_INTERP, 3 * touched * 8 + (double)s->M * (24 + 3 * 8 + 8));
     if (fp32) launch_interp<float, float>(s->d, s->M, s->perm, s->mw32, s->u32, s->v32, s->w32, U, s->st);
+    else if (dfloat && pairs && s->interp_pairs && s->u32 && s->u32l)
+        launch_interp_dfl(s->d, s->M, s->perm, s->mw, u, v, w, U, s->st, s->u32, s->u32l, s->v32, s->v32l, s->w32,
+                          s->w32l);
     else if (dfloat) launch_interp_dfl(s->d, s->M, s->perm, s->mw, u, v, w, U, s->st);
     else launch_interp<double, double>(s->d, s->M, s->perm, s->mw, u, v, w, U, s->st);
     return AFMIB_OK;
@@ -1486,7 +1495,7 @@ int ib_one_step(afmib_solver* s) {
     };
     auto interp = [&](double* U) {
         return in32 ? interp_markers(s, s->u, s->v, s->w, U, true)
-                    : interp_markers(s, s->u, s->v, s->w, U, false, s->mixed && s->interp_df);
+                    : interp_markers(s, s->u, s->v, s->w, U, false, s->mixed && s->interp_df, true);
     };
     CK(cudaMemsetAsync(s->dflag, 0, sizeof(int), s->st));
     const long long N = s->N();
@@ -1932,6 +1941,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_ADVECT_DF")) s->advect_df = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_FIRST_DF")) s->first_df = std::string(e) == "1";
     if (const char* e = std::getenv("AFMIB_PROJ_DF")) s->proj_df = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_INTERP_PAIRS")) s->interp_pairs = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_CN_START_OLD")) s->cn_start_old = std::string(e) != "0";
     if (s->mixed && s->fused_rhs)
         for (auto& q : s->qo) TRY(dalloc(s, &q, N));

@@ -842,6 +842,30 @@ def test_double_float_interpolation_matches_fp64(monkeypatch, bc):
 
 
 @pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
+def test_interpolation_from_velocity_pairs(monkeypatch, bc):
+    """The mixed form's double-float interpolation reading the velocity's
+    float pairs, which the projection writes (hi + lo = u to 2^-46), against
+    splitting the FP64 values itself (AFMIB_INTERP_PAIRS=0): two IB steps,
+    velocities and marker displacements agree to 1e-12 (the two represent
+    each face value to 2^-46 and differ only in how the bits are parted)."""
+    g, u, v, w, X, nstart, nidx = _periodic_case(32, M=800, seed=14)
+    if bc == capi.BC_CHANNEL:
+        v = v[: g.nx * (g.ny - 1) * g.nz]
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("AFMIB_INTERP_PAIRS", mode)
+        with capi.Solver(32, bc=bc, precision=capi.MIXED, mu=0.01, dt=1e-3, tol=1e-12, k_spring=0.5) as sv:
+            sv.set_velocity(u, v, w)
+            sv.project()
+            sv.set_markers(X, nstart, nidx)
+            sv.ib_step(2)
+            out[mode] = (sv.get_velocity(), sv.get_markers())
+    for a, b in zip(out["1"][0], out["0"][0]):
+        assert rel(a, b) < 1e-12
+    assert rel(out["1"][1] - X, out["0"][1] - X) < 1e-12
+
+
+@pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
 def test_double_float_projection_matches_fp64_passes(monkeypatch, bc):
     """The mixed form's projection passes in double-float (divergence with the
     sum of b, the first pressure defect with the mean removal folded in)
