@@ -170,6 +170,39 @@ AFMIB_HD df2 df_mul(df2 a, df2 b) {
 
 AFMIB_HD float df_to_float(df2 a) { return a.hi + a.lo; }
 
+// sin(pi x) and cos(pi x) for 0 <= x <= 1/2, x and the results as pairs
+// (relative error a few units of 2^-46): x > 1/4 is reflected to 1/2 - x
+// (sine and cosine swap), theta = pi y <= pi/4, and the Taylor series
+//   sin theta = theta (1 - theta^2/(2*3) (1 - theta^2/(4*5) (... (1 - theta^2/(14*15)))))
+//   cos theta = 1 - theta^2/(1*2) (1 - theta^2/(3*4) (... (1 - theta^2/(15*16))))
+// run to theta^15 and theta^16 (the first terms left out are below 5e-17 of
+// the result), evaluated inside out in pair arithmetic. The constants are pi
+// and the 1/(k (k+1)) split into float pairs (hi the nearest float, lo the
+// nearest float to the rest).
+AFMIB_HD void df_sincospi(df2 x, df2* sp, df2* cp) {
+    const df2 one = {1.f, 0.f};
+    const bool refl = x.hi > 0.25f;
+    const df2 half = {0.5f, 0.f};
+    const df2 y = refl ? df_add(half, df_neg(x)) : x;
+    const df2 pi = {0x1.921fb6p+1f, -0x1.777a5cp-24f};
+    const df2 th = df_mul(pi, y);
+    const df2 t2 = df_mul(th, th);
+    const df2 cs[7] = {{0x1.555556p-3f, -0x1.555556p-28f}, {0x1.99999ap-5f, -0x1.99999ap-31f},
+                       {0x1.861862p-6f, -0x1.e79e7ap-32f}, {0x1.c71c72p-7f, -0x1.c71c72p-34f},
+                       {0x1.29e412p-7f, 0x1.3c8254p-32f},  {0x1.a41a42p-8f, -0x1.6f96fap-34f},
+                       {0x1.381382p-8f, -0x1.8fd8fep-33f}};  // 1/6, 1/20, 1/42, 1/72, 1/110, 1/156, 1/210
+    const df2 cc[8] = {{0x1p-1f, 0.f},                      {0x1.555556p-4f, -0x1.555556p-29f},
+                       {0x1.111112p-5f, -0x1.dddddep-30f}, {0x1.24924ap-6f, -0x1.b6db6ep-31f},
+                       {0x1.6c16c2p-7f, -0x1.27d27ep-32f}, {0x1.f07c2p-8f, -0x1.f07c2p-33f},
+                       {0x1.681682p-8f, -0x1.2fd2fep-33f}, {0x1.111112p-8f, -0x1.dddddep-33f}};  // 1/2 .. 1/240
+    df2 ts = one, tc = one;
+    for (int k = 6; k >= 0; --k) ts = df_add(one, df_neg(df_mul(df_mul(t2, cs[k]), ts)));
+    for (int k = 7; k >= 0; --k) tc = df_add(one, df_neg(df_mul(df_mul(t2, cc[k]), tc)));
+    const df2 sn = df_mul(th, ts);
+    *sp = refl ? tc : sn;
+    *cp = refl ? sn : tc;
+}
+
 // An FP64 residual as the FP32 defect of the inner solves and, when rest is
 // given, the rest of its double-float pair. split: by integer operations
 // (df_split: the top 24 bits truncated, the next 23 bits), no FP64-pipe

@@ -94,7 +94,10 @@ __global__ void k_spring_bend(int M, const double* __restrict__ Y, const int* __
 // Per marker: bin key, wrapped cell, and for each axis and offset variant
 // (0: faces on integer positions, 1: on half-integers) the base offset
 // (first face - cell) and the four weights phi/n.
-template <typename T>
+// DF (FP64 weights only): the sine and cosine by df_sincospi on the FP32
+// pipe instead of the FP64 sincospi (the mixed form), weights rounded to FP64
+// from their pairs
+template <typename T, bool DF>
 __global__ void k_marker_prep(Dims d, int TS, int M, const double* __restrict__ X, unsigned* __restrict__ keys,
                               int* __restrict__ vals, MarkerW<T> mw, int* __restrict__ flag) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -127,13 +130,25 @@ __global__ void k_marker_prep(Dims d, int TS, int M, const double* __restrict__ 
             const double ft = floor(t);
             const T frac = T(t - ft);
             mw.dbase[(k * 3 + a) * 2 + v] = (signed char)((int)ft - 1 - (int)fs);
-            T C;
-            const T S = sinpi_cospi(frac * T(0.5), &C);
             T* w = mw.w + (((size_t)k * 3 + a) * 2 + v) * 4;
-            w[0] = T(0.25) * (T(1) - S);
-            w[1] = T(0.25) * (T(1) + C);
-            w[2] = T(0.25) * (T(1) + S);
-            w[3] = T(0.25) * (T(1) - C);
+            if constexpr (DF && sizeof(T) == sizeof(double)) {
+                df2 hx = df_split(frac);  // frac / 2 exactly
+                hx.hi *= 0.5f;
+                hx.lo *= 0.5f;
+                df2 Sx, Cx;
+                df_sincospi(hx, &Sx, &Cx);
+                const df2 one = {1.f, 0.f};
+                const df2 q[4] = {df_add(one, df_neg(Sx)), df_add(one, Cx), df_add(one, Sx), df_add(one, df_neg(Cx))};
+#pragma unroll
+                for (int m = 0; m < 4; ++m) w[m] = f32_to_f64(0.25f * q[m].hi) + f32_to_f64(0.25f * q[m].lo);
+            } else {
+                T C;
+                const T S = sinpi_cospi(frac * T(0.5), &C);
+                w[0] = T(0.25) * (T(1) - S);
+                w[1] = T(0.25) * (T(1) + C);
+                w[2] = T(0.25) * (T(1) + S);
+                w[3] = T(0.25) * (T(1) - C);
+            }
         }
     }
     mw.cell[3 * k] = cell[0];
@@ -656,15 +671,25 @@ __global__ void __launch_bounds__(kInterpDfBlock) k_interp_dfl(Dims d, int M, co
 #pragma unroll
                 for (int my = 0; my < 4; ++my) val[mz][my] = df_split(dv[mz][my]);
         }
-        const double* wyp = mw.w + (((size_t)k * 3 + 1) * 2 + vy) * 4;
-        const double* wzp = mw.w + (((size_t)k * 3 + 2) * 2 + vz) * 4;
+        // the quad's lanes split one y and one z weight each and share them
+        const df2 wyq = df_split(mw.w[(((size_t)k * 3 + 1) * 2 + vy) * 4 + q]);
+        const df2 wzq = df_split(mw.w[(((size_t)k * 3 + 2) * 2 + vz) * 4 + q]);
+        const int q0 = threadIdx.x & 28;
+        df2 wy[4], wz[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            wy[m].hi = __shfl_sync(qmask, wyq.hi, q0 + m);
+            wy[m].lo = __shfl_sync(qmask, wyq.lo, q0 + m);
+            wz[m].hi = __shfl_sync(qmask, wzq.hi, q0 + m);
+            wz[m].lo = __shfl_sync(qmask, wzq.lo, q0 + m);
+        }
         DfAcc az = {0.f, 0.f};
 #pragma unroll
         for (int mz = 0; mz < 4; ++mz) {
             DfAcc ay = {0.f, 0.f};
 #pragma unroll
-            for (int my = 0; my < 4; ++my) dfacc_mul_add(ay, df_split(wyp[my]), val[mz][my]);
-            dfacc_mul_add(az, df_split(wzp[mz]), dfacc_pair(ay));
+            for (int my = 0; my < 4; ++my) dfacc_mul_add(ay, wy[my], val[mz][my]);
+            dfacc_mul_add(az, wz[mz], dfacc_pair(ay));
         }
         const df2 wxq = df_split(mw.w[(((size_t)k * 3 + 0) * 2 + vx) * 4 + q]);
         df2 r = df_mul(wxq, dfacc_pair(az));
@@ -704,8 +729,12 @@ void launch_springs(int M, const double* X, const int* nstart, const int* nidx, 
 
 template <typename T>
 void launch_marker_prep(const Dims& d, int TS, int M, const double* X, unsigned* keys, int* vals, MarkerW<T> mw,
-                        int* flag, cudaStream_t s) {
-    if (M > 0) k_marker_prep<T><<<(M + 255) / 256, 256, 0, s>>>(d, TS, M, X, keys, vals, mw, flag);
+                        int* flag, cudaStream_t s, bool df_weights) {
+    if (M <= 0) return;
+    if (df_weights && sizeof(T) == sizeof(double))
+        k_marker_prep<T, true><<<(M + 255) / 256, 256, 0, s>>>(d, TS, M, X, keys, vals, mw, flag);
+    else
+        k_marker_prep<T, false><<<(M + 255) / 256, 256, 0, s>>>(d, TS, M, X, keys, vals, mw, flag);
 }
 
 size_t radix_sort_temp_bytes(int n) {
@@ -835,7 +864,7 @@ void launch_marker_axpy(int M, double* Xo, const double* Xi, const double* U, do
     template void launch_springs_bending<T>(int, const double*, const int*, const int*, double, double, double*, T*, \
                                             cudaStream_t);                                                         \
     template void launch_marker_prep<T>(const Dims&, int, int, const double*, unsigned*, int*, MarkerW<T>, int*, \
-                                        cudaStream_t);                                                           \
+                                        cudaStream_t, bool);                                                     \
     template size_t spread_smem_bytes<T>(int, int, int);                                                             \
     template void launch_spread_gather<T>(const Dims&, int, int, const int*, MarkerW<T>, const T*, const double*, \
                                           double, const int*, const int*, const int*, const int*, int, int, T*,  \

@@ -29,8 +29,11 @@ void launch_springs_bending(int M, const double* X, const int* nstart, const int
 // marker index; flag set to 1 when a marker is within 2.5h of a channel wall,
 // 2 on a NaN position.
 template <typename T>
+// df_weights (FP64 weights): sine and cosine in double-float on the FP32 pipe
+// (df_sincospi) instead of the FP64 sincospi, weights within 2^-45 (the
+// mixed form)
 void launch_marker_prep(const Dims& d, int TS, int M, const double* X, unsigned* keys, int* vals, MarkerW<T> mw,
-                        int* flag, cudaStream_t s);
+                        int* flag, cudaStream_t s, bool df_weights = false);
 
 size_t radix_sort_temp_bytes(int n);
 // Stable LSD sort of the low `bits` bits; returns which buffers hold the result.

@@ -115,7 +115,11 @@ struct afmib_solver {
     // mixed form: the double-float interpolation of the step's velocity reads
     // its float pairs (written by the projection) instead of splitting the
     // FP64 values (AFMIB_INTERP_PAIRS=0: splits)
-    bool interp_pairs = true;  // scal[8] holds the sum of lv[0].b (from the divergence)
+    bool interp_pairs = true;
+    // mixed form: the IB step's FP64 marker weights from double-float sines
+    // and cosines on the FP32 pipe (df_sincospi) instead of the FP64
+    // sincospi (AFMIB_PREP_DF=0: FP64)
+    bool prep_df = true;  // scal[8] holds the sum of lv[0].b (from the divergence)
     // mixed form with the double-float residual: the Crank-Nicolson viscous
     // solves start from uold (the step's start velocity), whose residual
     // comes pointwise from the kept Q, instead of the current velocity
@@ -1332,7 +1336,9 @@ int key_bits(afmib_solver* s) {
 }
 
 // weights + bins of the markers at P (device, [M][3])
-int bin_markers(afmib_solver* s, const double* P, bool fp32 = false) {
+// df_weights: the FP64 weights by launch_marker_prep's double-float sine and
+// cosine (the mixed form's IB step)
+int bin_markers(afmib_solver* s, const double* P, bool fp32 = false, bool df_weights = false) {
     const int M = s->M;
     const int passes = (key_bits(s) + 7) / 8;
     if (fp32) {
@@ -1340,7 +1346,7 @@ int bin_markers(afmib_solver* s, const double* P, bool fp32 = false) {
         launch_marker_prep<float>(s->d, s->TS, M, P, s->keys, s->vals, s->mw32, s->dflag, s->st);
     } else {
         ProfScope ps(s, P_PREP, (double)M * (24 + 4 + 4 + 12 + 6 + 24 * 8));
-        launch_marker_prep<double>(s->d, s->TS, M, P, s->keys, s->vals, s->mw, s->dflag, s->st);
+        launch_marker_prep<double>(s->d, s->TS, M, P, s->keys, s->vals, s->mw, s->dflag, s->st, df_weights);
     }
     unsigned* ko;
     int* vo;
@@ -1480,12 +1486,14 @@ int ib_one_step(afmib_solver* s) {
             launch_springs<double>(M, P, s->nstart, s->nidx, ks, s->G, s->st);
         }
     };
+    // the mixed form's FP64 weights from double-float sines and cosines
+    const bool dfw = s->mixed && s->prep_df;
     auto bin = [&](const double* P) -> int {
-        TRY(bin_markers(s, P, sp32));
+        TRY(bin_markers(s, P, sp32, dfw));
         if (sp32 != in32) {  // the other weight set for the other transfer (same bins)
             ProfScope ps(s, P_PREP, (double)M * (24 + 4 + 4 + 12 + 6 + 24 * (in32 ? 4 : 8)));
             if (in32) launch_marker_prep<float>(s->d, s->TS, M, P, nullptr, nullptr, s->mw32, s->dflag, s->st);
-            else launch_marker_prep<double>(s->d, s->TS, M, P, nullptr, nullptr, s->mw, s->dflag, s->st);
+            else launch_marker_prep<double>(s->d, s->TS, M, P, nullptr, nullptr, s->mw, s->dflag, s->st, dfw);
         }
         return AFMIB_OK;
     };
@@ -1942,6 +1950,7 @@ int create(afmib_solver* s, const afmib_config* c, void* stream) {
     if (const char* e = std::getenv("AFMIB_FIRST_DF")) s->first_df = std::string(e) == "1";
     if (const char* e = std::getenv("AFMIB_PROJ_DF")) s->proj_df = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_INTERP_PAIRS")) s->interp_pairs = std::string(e) != "0";
+    if (const char* e = std::getenv("AFMIB_PREP_DF")) s->prep_df = std::string(e) != "0";
     if (const char* e = std::getenv("AFMIB_CN_START_OLD")) s->cn_start_old = std::string(e) != "0";
     if (s->mixed && s->fused_rhs)
         for (auto& q : s->qo) TRY(dalloc(s, &q, N));

@@ -22,6 +22,15 @@ void afmib_test_split_round(double d, float* hi, float* lo) {
     *hi = r.hi;
     *lo = r.lo;
 }
+// sin(pi x), cos(pi x) of df_sincospi for x (split by df_split), as pairs
+void afmib_test_sincospi(double x, float* s, float* c) {
+    afmib::df2 sp, cp;
+    afmib::df_sincospi(afmib::df_split(x), &sp, &cp);
+    s[0] = sp.hi;
+    s[1] = sp.lo;
+    c[0] = cp.hi;
+    c[1] = cp.lo;
+}
 void afmib_test_split(double d, float* hi, float* lo) {
     const afmib::df2 r = afmib::df_split(d);
     *hi = r.hi;

@@ -33,6 +33,7 @@ def lib(tmp_path_factory):
                                           ctypes.c_int]
     L.afmib_test_lap_residual.restype = ctypes.c_float
     L.afmib_test_split.argtypes = [ctypes.c_double, fp, fp]
+    L.afmib_test_sincospi.argtypes = [ctypes.c_double, fp, fp]
     L.afmib_test_df_hi.argtypes = [ctypes.c_double]
     L.afmib_test_df_hi.restype = ctypes.c_float
     L.afmib_test_df_round.argtypes = [ctypes.c_double]
@@ -257,3 +258,38 @@ def test_split_round_pair(lib):
             assert abs(Fr(hi.value) + Fr(lo.value) - Fr(d)) <= abs(Fr(d)) * Fr(2) ** -46, d
         else:  # the rest underflows: the truncated pair, within one float ulp
             assert abs(Fr(hi.value) + Fr(lo.value) - Fr(d)) <= abs(Fr(d)) * Fr(2) ** -23, d
+
+
+def test_df_sincospi_against_exact(lib):
+    """df_sincospi (the mixed form's marker weights on the FP32 pipe) against
+    sin(pi x) and cos(pi x) from a 40-digit Taylor evaluation, over [0, 1/2]
+    including both ends and the reflection point 1/4: relative error below
+    2^-44 of the larger of the two values (the weights (1 -+ S)/4, (1 +- C)/4
+    then carry it as an absolute error below 2^-45)."""
+    from decimal import Decimal, getcontext
+    getcontext().prec = 50
+    pi = Decimal("3.14159265358979323846264338327950288419716939937510")
+
+    def exact(x):
+        t = pi * Decimal(x)
+        s = c = Decimal(0)
+        term_s, term_c = t, Decimal(1)
+        for k in range(40):
+            s += term_s
+            c += term_c
+            term_s *= -t * t / ((2 * k + 2) * (2 * k + 3))
+            term_c *= -t * t / ((2 * k + 1) * (2 * k + 2))
+        return s, c
+
+    xs = [0.0, 1e-9, 0.125, 0.25, np.nextafter(0.25, 1), 0.3, 0.49999, 0.5]
+    xs += list(np.random.default_rng(3).uniform(0, 0.5, 400))
+    sp, cp = (ctypes.c_float * 2)(), (ctypes.c_float * 2)()
+    worst = 0.0
+    for x in xs:
+        lib.afmib_test_sincospi(float(x), sp, cp)
+        s_ex, c_ex = exact(float(x))
+        got_s = Decimal(float(sp[0])) + Decimal(float(sp[1]))
+        got_c = Decimal(float(cp[0])) + Decimal(float(cp[1]))
+        scale = max(abs(s_ex), abs(c_ex))
+        worst = max(worst, float(abs(got_s - s_ex) / scale), float(abs(got_c - c_ex) / scale))
+    assert worst < 2.0 ** -44, worst

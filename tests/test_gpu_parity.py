@@ -842,6 +842,29 @@ def test_double_float_interpolation_matches_fp64(monkeypatch, bc):
 
 
 @pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
+def test_double_float_marker_weights(monkeypatch, bc):
+    """The mixed form's marker weights from double-float sines and cosines
+    (df_sincospi on the FP32 pipe, within 2^-45 of the FP64 sincospi weights)
+    against the FP64 weights (AFMIB_PREP_DF=0): two IB steps, velocities and
+    marker displacements agree to 1e-11."""
+    g, u, v, w, X, nstart, nidx = _periodic_case(32, M=800, seed=15)
+    if bc == capi.BC_CHANNEL:
+        v = v[: g.nx * (g.ny - 1) * g.nz]
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("AFMIB_PREP_DF", mode)
+        with capi.Solver(32, bc=bc, precision=capi.MIXED, mu=0.01, dt=1e-3, tol=1e-12, k_spring=0.5) as sv:
+            sv.set_velocity(u, v, w)
+            sv.project()
+            sv.set_markers(X, nstart, nidx)
+            sv.ib_step(2)
+            out[mode] = (sv.get_velocity(), sv.get_markers())
+    for a, b in zip(out["1"][0], out["0"][0]):
+        assert rel(a, b) < 1e-11
+    assert rel(out["1"][1] - X, out["0"][1] - X) < 1e-11
+
+
+@pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
 def test_interpolation_from_velocity_pairs(monkeypatch, bc):
     """The mixed form's double-float interpolation reading the velocity's
     float pairs, which the projection writes (hi + lo = u to 2^-46), against
