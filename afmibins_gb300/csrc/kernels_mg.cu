@@ -1656,9 +1656,13 @@ __device__ __forceinline__ void tail_sweep2(const Dims& d, const Ix2& I, T* x, c
 // solve runs in the cluster's first CTA, the same one-block CG, so the result
 // is the one-block tail's, bit for bit; the levels stay in global memory (L2).
 template <typename T, bool CL, int TB = kRedBlock>
-__global__ void __launch_bounds__(TB) k_vcycle_tail(TailLevels<T> g, int staged) {
+__global__ void __launch_bounds__(TB, 1) k_vcycle_tail(TailLevels<T> g, int staged) {
     extern __shared__ __align__(16) unsigned char tsm[];
-    TailLevels<T> a = g;
+    // the level tables in shared memory (indexed by level: a local copy
+    // would live in local memory)
+    __shared__ TailLevels<T> a;
+    if (threadIdx.x == 0) a = g;
+    __syncthreads();
     int t0 = threadIdx.x, ts = blockDim.x;
     bool lead = true;
     if constexpr (CL) {
@@ -1674,37 +1678,52 @@ __global__ void __launch_bounds__(TB) k_vcycle_tail(TailLevels<T> g, int staged)
     };
     if (!CL && staged) {
         // layout: per level x, b, r (T), then cx64, cb64, cr64, cw_p, cw_q (double)
-        size_t off = 0;
-        for (int l = 0; l < a.nlev; ++l) {
-            const long long n = a.d[l].ncell();
-            a.x[l] = (T*)(tsm + off);
-            a.b[l] = a.x[l] + n;
-            a.r[l] = a.b[l] + n;
-            off += (size_t)3 * n * sizeof(T);
-            off = (off + 15) & ~(size_t)15;
+        if (threadIdx.x == 0) {
+            size_t off = 0;
+            for (int l = 0; l < a.nlev; ++l) {
+                const long long n = a.d[l].ncell();
+                a.x[l] = (T*)(tsm + off);
+                a.b[l] = a.x[l] + n;
+                a.r[l] = a.b[l] + n;
+                off += (size_t)3 * n * sizeof(T);
+                off = (off + 15) & ~(size_t)15;
+            }
+            const long long nc = a.d[a.nlev - 1].ncell();
+            double* dp = (double*)(tsm + off);
+            a.cx64 = dp;
+            a.cb64 = dp + nc;
+            a.cr64 = dp + 2 * nc;
+            a.cw_p = dp + 3 * nc;
+            a.cw_q = dp + 4 * nc;
         }
-        const long long nc = a.d[a.nlev - 1].ncell();
-        double* dp = (double*)(tsm + off);
-        a.cx64 = dp;
-        a.cb64 = dp + nc;
-        a.cr64 = dp + 2 * nc;
-        a.cw_p = dp + 3 * nc;
-        a.cw_q = dp + 4 * nc;
+        __syncthreads();
         const long long n0 = a.d[0].ncell();
+        T* const x0 = a.x[0];
+        T* const b0 = a.b[0];
+        const T* const gx = g.x[0];
+        const T* const gb = g.b[0];
         for (long long i = threadIdx.x; i < n0; i += blockDim.x) {
-            a.x[0][i] = g.x[0][i];
-            a.b[0][i] = g.b[0][i];
+            x0[i] = gx[i];
+            b0[i] = gb[i];
         }
         __syncthreads();
     }
+    // per level, the dimensions and array pointers are read once into
+    // registers: the level tables sit in local memory (indexed by level), and
+    // through a reference every access inside the cell loops was a reload
     for (int l = 0; l + 1 < a.nlev; ++l) {
-        const Dims& d = a.d[l];
+        const Dims d = a.d[l];
+        T* const xl = a.x[l];
+        T* const bl = a.b[l];
+        T* const rl = a.r[l];
+        T* const xc = a.x[l + 1];
+        T* const bc = a.b[l + 1];
         const bool p2 = tail_p2(d);
         const Ix2 I(d);
         for (int j = 0; j < a.nu1; ++j) {
             for (int color = 0; color < 2; ++color) {
-                if (p2) tail_sweep2(d, I, a.x[l], a.b[l], color, t0, ts);
-                else tail_sweep(d, a.x[l], a.b[l], color, t0, ts);
+                if (p2) tail_sweep2(d, I, xl, bl, color, t0, ts);
+                else tail_sweep(d, xl, bl, color, t0, ts);
                 sync();
             }
         }
@@ -1714,31 +1733,31 @@ __global__ void __launch_bounds__(TB) k_vcycle_tail(TailLevels<T> g, int staged)
             for (int i = t0; i < n; i += ts) {
                 const int xx = i & I.mx, yy = (i >> I.lx) & I.my, zz = i >> I.lxy;
                 T S, c;
-                lap_row2(d, I, a.x[l], xx, yy, zz, S, c);
-                a.r[l][i] = a.b[l][i] - off * (S - c * a.x[l][i]);
+                lap_row2(d, I, xl, xx, yy, zz, S, c);
+                rl[i] = bl[i] - off * (S - c * xl[i]);
             }
         } else {
             for (int i = t0; i < n; i += ts) {
                 int xx, yy, zz;
                 tail_xyz(d, i, xx, yy, zz);
-                residual_cell(d, a.r[l], a.x[l], a.b[l], xx, yy, zz);
+                residual_cell(d, rl, xl, bl, xx, yy, zz);
             }
         }
         sync();
-        const Dims& c = a.d[l + 1];
+        const Dims c = a.d[l + 1];
         const int nc = (int)c.ncell();
         if (p2) {
             const int lcx = I.lx - 1, lcxy = I.lxy - 2, mcx = (d.nx >> 1) - 1, mcy = (d.ny >> 1) - 1;
             for (int i = t0; i < nc; i += ts) {
-                restrict_cell2(d, I, a.b[l + 1], a.r[l], i & mcx, (i >> lcx) & mcy, i >> lcxy);
-                a.x[l + 1][i] = T(0);
+                restrict_cell2(d, I, bc, rl, i & mcx, (i >> lcx) & mcy, i >> lcxy);
+                xc[i] = T(0);
             }
         } else {
             for (int i = t0; i < nc; i += ts) {
                 int xx, yy, zz;
                 tail_xyz(c, i, xx, yy, zz);
-                restrict_cell(d, a.b[l + 1], a.r[l], xx, yy, zz);
-                a.x[l + 1][i] = T(0);
+                restrict_cell(d, bc, rl, xx, yy, zz);
+                xc[i] = T(0);
             }
         }
         sync();
@@ -1759,34 +1778,39 @@ __global__ void __launch_bounds__(TB) k_vcycle_tail(TailLevels<T> g, int staged)
     }
     sync();
     for (int l = a.nlev - 2; l >= 0; --l) {
-        const Dims& d = a.d[l];
-        const Dims& c = a.d[l + 1];
+        const Dims d = a.d[l];
+        const Dims c = a.d[l + 1];
+        T* const xl = a.x[l];
+        T* const bl = a.b[l];
+        T* const xc = a.x[l + 1];
         const bool p2 = tail_p2(d);
         const Ix2 I(d);
         const int nc = (int)c.ncell();
         if (p2) {
             const int lcx = I.lx - 1, lcxy = I.lxy - 2, mcx = (d.nx >> 1) - 1, mcy = (d.ny >> 1) - 1;
             for (int i = t0; i < nc; i += ts)
-                prolong_cell2<T, true>(d, I, a.x[l], a.x[l + 1], i & mcx, (i >> lcx) & mcy, i >> lcxy);
+                prolong_cell2<T, true>(d, I, xl, xc, i & mcx, (i >> lcx) & mcy, i >> lcxy);
         } else {
             for (int i = t0; i < nc; i += ts) {
                 int xx, yy, zz;
                 tail_xyz(c, i, xx, yy, zz);
-                prolong_cell<T, true>(d, a.x[l], a.x[l + 1], xx, yy, zz);
+                prolong_cell<T, true>(d, xl, xc, xx, yy, zz);
             }
         }
         sync();
         for (int j = 0; j < a.nu2; ++j) {
             for (int color = 0; color < 2; ++color) {
-                if (p2) tail_sweep2(d, I, a.x[l], a.b[l], color, t0, ts);
-                else tail_sweep(d, a.x[l], a.b[l], color, t0, ts);
+                if (p2) tail_sweep2(d, I, xl, bl, color, t0, ts);
+                else tail_sweep(d, xl, bl, color, t0, ts);
                 sync();
             }
         }
     }
     if (!CL && staged) {
         const long long n0 = a.d[0].ncell();
-        for (long long i = threadIdx.x; i < n0; i += blockDim.x) g.x[0][i] = a.x[0][i];
+        T* const gx = g.x[0];
+        const T* const x0 = a.x[0];
+        for (long long i = threadIdx.x; i < n0; i += blockDim.x) gx[i] = x0[i];
     }
 }
 
