@@ -233,9 +233,10 @@ void launch_vcycle_tail(const TailLevels<T>& a, cudaStream_t s, int cluster = 1)
 int vcycle_tail_cluster_max();
 template <typename T>
 void launch_rbgs_pipe(const Dims& d, const PipeCfg& c, const T* xin, T* xout, const T* b, int* err, cudaStream_t s);
-// Full-weighting restriction, src/mg/solver.h:153-181 (d = fine dims).
+// Full-weighting restriction, src/mg/solver.h:153-181 (d = fine dims); zero
+// (optional): the coarse iterate, set to zero in the same pass.
 template <typename T>
-void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s, int rev = 0);
+void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s, int rev = 0, T* zero = nullptr);
 // fine += P coarse (trilinear), src/mg/solver.h:71-151 and :211-212.
 template <typename T>
 void launch_prolong_add(const Dims& d, T* fine, const T* coarse, cudaStream_t s, int rev = 0);

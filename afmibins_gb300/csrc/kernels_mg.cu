@@ -322,6 +322,7 @@ __global__ void k_rbgs(Dims d, int color, T omega, T* __restrict__ xv, const T* 
 // black ones, so the delayed stores change nothing: same values as the
 // one-cell kernels.
 constexpr int kZU = 8;  // z cells per thread of the batched stencil kernels
+constexpr int kZU32 = 4;  // ... of the FP32 red-black colour
 // smallest level (x extent) on which a requested over-relaxation applies;
 // the coarser levels, the one-block tail among them, stay Gauss-Seidel
 constexpr int kOmegaMinNx = 64;
@@ -729,11 +730,16 @@ __device__ __forceinline__ void restrict_cell(const Dims& d, T* coarse, const T*
     coarse[xc + (long long)cx * (yc + (long long)cy * zc)] = acc;
 }
 
+// zero (optional): the coarse iterate, set to zero at every coarse cell
 template <typename T>
-__global__ void k_restrict(Dims d, T* __restrict__ coarse, const T* __restrict__ fine) {
+__global__ void k_restrict(Dims d, T* __restrict__ coarse, const T* __restrict__ fine, T* __restrict__ zero) {
     const int xc = blockIdx.x * BX + threadIdx.x, yc = blockIdx.y * BY + threadIdx.y, zc = blockIdx.z;
     if (xc >= d.nx / 2 || yc >= d.ny / 2) return;
     restrict_cell(d, coarse, fine, xc, yc, zc);
+    if (zero) {
+        const long long cx = d.nx / 2, cy = d.ny / 2;
+        zero[d.nz == 1 ? xc + cx * yc : xc + cx * (yc + cy * zc)] = T(0);
+    }
 }
 
 // Trilinear prolongation (27,9,3,1)/64, src/mg/solver.h:71-151. One thread per
@@ -827,12 +833,14 @@ __device__ __forceinline__ void restrict_cell2(const Dims& d, const Ix2& I, T* c
 }
 
 template <typename T>
-__global__ void k_restrict2(Dims d, T* __restrict__ coarse, const T* __restrict__ fine, int rev) {
+__global__ void k_restrict2(Dims d, T* __restrict__ coarse, const T* __restrict__ fine, int rev,
+                            T* __restrict__ zero) {
     const Ix2 I(d);
     const uint3 B = block_at(rev);
     const int xc = B.x * BX + threadIdx.x, yc = B.y * BY + threadIdx.y, zc = B.z;
     if (xc >= d.nx / 2 || yc >= d.ny / 2) return;
     restrict_cell2(d, I, coarse, fine, xc, yc, zc);
+    if (zero) zero[xc | (yc << (I.lx - 1)) | (zc << (I.lxy - 2))] = T(0);
 }
 
 template <typename T, bool ADD>
@@ -1054,7 +1062,8 @@ __device__ __forceinline__ void quad_get(const T* p, T (&v)[16 / sizeof(T)]) {
 
 template <typename T, int CZ>
 __global__ void __launch_bounds__(32 * kTrBY) k_restrict_cols(Dims d, T* __restrict__ coarse,
-                                                              const T* __restrict__ fine, int rev) {
+                                                              const T* __restrict__ fine, int rev,
+                                                              T* __restrict__ zero) {
     using TT = TrTile<T>;
     constexpr int CE = TT::CE, M = CE / 2;  // M coarse cells per lane
     constexpr int NP = 2 * CZ + 2;          // fine planes of the block
@@ -1144,9 +1153,14 @@ __global__ void __launch_bounds__(32 * kTrBY) k_restrict_cols(Dims d, T* __restr
         taps(acquire(2 * k + 3), e);
         add(acc, e, 3);
         add(next, e, 1);
-        T* out = coarse + (co | ((zc0 + k) << (I.lxy - 2)));
-        if constexpr (M == 2) *reinterpret_cast<float2*>(out) = make_float2(acc[0], acc[1]);
-        else out[0] = acc[0];
+        const int o = co | ((zc0 + k) << (I.lxy - 2));
+        if constexpr (M == 2) {
+            *reinterpret_cast<float2*>(coarse + o) = make_float2(acc[0], acc[1]);
+            if (zero) *reinterpret_cast<float2*>(zero + o) = make_float2(0.f, 0.f);
+        } else {
+            coarse[o] = acc[0];
+            if (zero) zero[o] = T(0);
+        }
 #pragma unroll
         for (int m = 0; m < M; ++m) acc[m] = next[m];
     }
@@ -1870,10 +1884,15 @@ void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s, dou
                                                                            (const float*)b, rev);
                 return;
             }
-            // FP32: registers capped for 6 resident blocks (40 against 44), 50.5
-            // against 50.0 IB steps/s at 256^3 (8 blocks, 32 registers: 48.0)
-            if (sizeof(T) == sizeof(float))
-                k_rbgs_z2b<T, kZU, 6><<<g, dim3(BX, BY), 0, s>>>(d, color, T(omega), x, b, rev);
+            // FP32: kZU32 z cells per thread, registers capped for 6 resident
+            // blocks (50.5 against 50.0 IB steps/s at 256^3 for eight cells
+            // and 6 blocks against none; four cells: 29.5 against 30.0 us per
+            // 256^3 colour, 61.1 against 60.8 steps/s; 16: spills, two:
+            // 32.7 us; four cells with 8 blocks: the same as 6)
+            if (sizeof(T) == sizeof(float) && d.nz % kZU32 == 0) {
+                const dim3 g4(g.x, g.y, d.nz / kZU32);
+                k_rbgs_z2b<T, kZU32, 6><<<g4, dim3(BX, BY), 0, s>>>(d, color, T(omega), x, b, rev);
+            }
             else
                 k_rbgs_z2<T, kZU><<<g, dim3(BX, BY), 0, s>>>(d, color, T(omega), x, b, rev);
         }
@@ -1994,21 +2013,23 @@ inline dim3 transfer_grid(const Dims& d, int planes, int bx = 32) {
 }
 
 template <typename T>
-void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s, int rev) {
+void launch_restrict(const Dims& d, T* coarse, const T* fine, cudaStream_t s, int rev, T* zero) {
     if constexpr (sizeof(T) == sizeof(float)) {
-        if (transfer_cols_ok(d, fine, coarse) && (d.nx / 2) % TrTile<T>::CX == 0) {
+        if (transfer_cols_ok(d, fine, coarse) && (d.nx / 2) % TrTile<T>::CX == 0 &&
+            (reinterpret_cast<uintptr_t>(zero) & 15) == 0) {
             const int z = transfer_planes(d, TrTile<T>::CX);
             const dim3 g = transfer_grid(d, z, TrTile<T>::CX), b(32, kTrBY);
-            if (z == 8) k_restrict_cols<T, 8><<<g, b, 0, s>>>(d, coarse, fine, rev);
-            else if (z == 4) k_restrict_cols<T, 4><<<g, b, 0, s>>>(d, coarse, fine, rev);
-            else if (z == 2) k_restrict_cols<T, 2><<<g, b, 0, s>>>(d, coarse, fine, rev);
-            else k_restrict_cols<T, 1><<<g, b, 0, s>>>(d, coarse, fine, rev);
+            if (z == 8) k_restrict_cols<T, 8><<<g, b, 0, s>>>(d, coarse, fine, rev, zero);
+            else if (z == 4) k_restrict_cols<T, 4><<<g, b, 0, s>>>(d, coarse, fine, rev, zero);
+            else if (z == 2) k_restrict_cols<T, 2><<<g, b, 0, s>>>(d, coarse, fine, rev, zero);
+            else k_restrict_cols<T, 1><<<g, b, 0, s>>>(d, coarse, fine, rev, zero);
             return;
         }
     }
     dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny / 2 + BY - 1) / BY, d.nz == 1 ? 1 : d.nz / 2);
-    if (d.nz > 1 && d.nx >= 2 && d.ny >= 2 && ix2_ok(d)) k_restrict2<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine, rev);
-    else k_restrict<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine);
+    if (d.nz > 1 && d.nx >= 2 && d.ny >= 2 && ix2_ok(d))
+        k_restrict2<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine, rev, zero);
+    else k_restrict<T><<<g, dim3(BX, BY), 0, s>>>(d, coarse, fine, zero);
 }
 // Fine-level residual and restriction in one pass. AFMIB_RESID_RESTRICT
 // (read at every call, so that a test can compare the paths in one process):
@@ -2255,7 +2276,7 @@ void launch_coarse_solve(const Dims& d, T* x, T* b, T* r, T* p, T* q, double tol
     template void launch_rbgs<T>(const Dims&, int, T*, const T*, cudaStream_t, double, int);                        \
     template PipeCfg rbgs_pipe_cfg<T>(const Dims&);                                                      \
     template void launch_rbgs_pipe<T>(const Dims&, const PipeCfg&, const T*, T*, const T*, int*, cudaStream_t); \
-    template void launch_restrict<T>(const Dims&, T*, const T*, cudaStream_t, int);                         \
+    template void launch_restrict<T>(const Dims&, T*, const T*, cudaStream_t, int, T*);                     \
     template void launch_prolong_add<T>(const Dims&, T*, const T*, cudaStream_t, int);                      \
     template void launch_resid_restrict<T>(const Dims&, T*, T*, const T*, const T*, cudaStream_t, int);      \
     template void launch_prolong_assign<T>(const Dims&, T*, const T*, cudaStream_t);                     \

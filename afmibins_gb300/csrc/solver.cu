@@ -585,10 +585,10 @@ int vcycle(afmib_solver* s, size_t l) {
             launch_residual<T>(L.d, L.r, L.x, L.b, nullptr, nullptr, s->st, pass_dir(s, L.d, sizeof(T)));
         }
         {
-            ProfScope ps(s, fine ? P_RESTRICT0 : P_RESTRICT, Ns + Ns / 8);
-            launch_restrict<T>(L.d, C.b, L.r, s->st, pass_dir(s, L.d, sizeof(T)));
+            // the coarse iterate starts from zero: set in the same pass
+            ProfScope ps(s, fine ? P_RESTRICT0 : P_RESTRICT, Ns + Ns / 8 + Ns / 8);
+            launch_restrict<T>(L.d, C.b, L.r, s->st, pass_dir(s, L.d, sizeof(T)), C.x);
         }
-        CK(cudaMemsetAsync(C.x, 0, C.d.ncell() * sizeof(T), s->st));
     }
     CKL();
     TRY(vcycle<T>(s, l + 1));
