@@ -455,6 +455,13 @@ def run_adjoint_case(args, torch, local):
     results = {}
     for name, prec in (("fp64", capi.FP64), ("mixed", capi.MIXED)):
         sv, v0 = (fd_sv, vel0) if prec == capi.FP64 else solver(prec)
+        # untimed: two steps forward and back, so that the timed run holds no
+        # first-use costs (module loads, graph captures); the trajectory
+        # starts from (v0, X0) every call, so the timed run is unchanged
+        Xw = torch.tensor(X, device=dev, requires_grad=True)
+        kw = torch.tensor(0.5, dtype=torch.float64, device=dev, requires_grad=True)
+        uw, Xnw = ib_trajectory(kw, Xw, sv, v0, 2, 1)
+        membrane_loss(uw, Xnw, Xw, h3).backward()
         X0 = torch.tensor(X, device=dev, requires_grad=True)
         k = torch.tensor(0.5, dtype=torch.float64, device=dev, requires_grad=True)
         torch.cuda.synchronize()
