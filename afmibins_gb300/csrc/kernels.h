@@ -198,6 +198,10 @@ void launch_helm_defect_bfp(const Dims& d, int comp, double scale, const double*
 // reverse order (block_at, common.cuh) on the batched power-of-two kernels.
 template <typename T>
 void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s, double omega = 1.0, int rev = 0);
+// The red colour of a sweep from x = 0 (x's contents ignored, both colours
+// written): the same bits as zeroing x and launch_rbgs(color 0).
+template <typename T>
+void launch_rbgs_from_zero(const Dims& d, T* x, const T* b, cudaStream_t s, double omega = 1.0, int rev = 0);
 // One full red+black sweep per launch, out of place (xin -> xout), z-marching
 // blocks fed by bulk asynchronous row copies; equals the two per-colour
 // launches cell for cell. FY == 0: level not eligible (small, 2D, or rows not

@@ -401,6 +401,44 @@ template <typename T, int ZU>
 __global__ void k_rbgs_z2(Dims d, int color, T omega, T* __restrict__ xv, const T* __restrict__ b, int rev) {
     rbgs_z2_body<T, ZU>(d, color, omega, xv, b, rev);
 }
+
+// The first colour (red) of a sweep from x = 0 without reading or clearing x
+// first: every neighbour is zero, so the neighbour sum lap_row2 forms is the
+// zero `zero` (a kernel argument, so that the arithmetic is rbgs_z2_body's,
+// not a folded constant) and the update x - 0 the update; the black cell of
+// each pair is written as zero. The same bits as a memset of x followed by
+// the colour launch.
+template <typename T, int ZU, int MINB>
+__global__ void __launch_bounds__(BX * BY, MINB) k_rbgs_z2b_init(Dims d, T omega, T* __restrict__ xv,
+                                                                const T* __restrict__ b, int rev, T zero) {
+    const Ix2 I(d);
+    const uint3 B = block_at(rev);
+    const int y = B.y * BY + threadIdx.y, t = B.x * BX + threadIdx.x, z0 = B.z * ZU;
+    if (y >= d.ny || 2 * t >= d.nx) return;
+    T val[ZU];
+    int at[ZU], other[ZU];
+    const T inv = T(1) / (T(d.n) * T(d.n));
+#pragma unroll
+    for (int u = 0; u < ZU; ++u) {
+        const int z = z0 + u, p = (y + z) & 1, x = 2 * t + p;
+        T c = d.nz == 1 ? T(4) : T(6);
+        if (d.channel) {
+            if (!(y > 0)) c -= T(1);
+            if (!(y < d.ny - 1)) c -= T(1);
+        }
+        const int i = I.at(x, y, z);
+        const T rc = (c == T(6)) ? T(1.0 / 6.0) : ((c == T(5)) ? T(1.0 / 5.0) : (c == T(4) ? T(0.25) : T(1) / c));
+        val[u] = (zero - b[i] * inv) * rc;
+        if (omega != T(1)) val[u] = val[u] + (omega - T(1)) * (val[u] - zero);
+        at[u] = i;
+        other[u] = I.at(2 * t + 1 - p, y, z);
+    }
+#pragma unroll
+    for (int u = 0; u < ZU; ++u) {
+        xv[at[u]] = val[u];
+        xv[other[u]] = zero;
+    }
+}
 template <typename T, int ZU, int MINB>
 __global__ void __launch_bounds__(BX * BY, MINB) k_rbgs_z2b(Dims d, int color, T omega, T* __restrict__ xv,
                                                            const T* __restrict__ b, int rev) {
@@ -1871,6 +1909,25 @@ bool rbgs_pair_ok(const Dims& d) {
     return d.nz > 1 && d.nx >= 2 * BX && d.ny % BY == 0 && d.nz % kPairZU == 0;
 }
 
+// First colour of a sweep from x = 0 (x's contents ignored and overwritten):
+// the FP32 batched kernel's own form (k_rbgs_z2b_init), elsewhere a memset of
+// x and the red colour. AFMIB_INIT_SWEEP=0 takes the memset everywhere (read
+// at every launch, so that a test can compare both in one process).
+template <typename T>
+void launch_rbgs_from_zero(const Dims& d, T* x, const T* b, cudaStream_t s, double omega, int rev) {
+    const char* e = std::getenv("AFMIB_INIT_SWEEP");
+    const bool off = e && e[0] == '0';
+    if (d.nx < kOmegaMinNx) omega = 1.0;
+    if (!off && sizeof(T) == sizeof(float) && d.nz % kZU == 0 && d.nz % kZU32 == 0 && d.nx >= batch_min_nx() &&
+        ix2_ok(d) && !rbgs_pair_ok(d)) {
+        const dim3 g((d.nx / 2 + BX - 1) / BX, (d.ny + BY - 1) / BY, d.nz / kZU32);
+        k_rbgs_z2b_init<T, kZU32, 6><<<g, dim3(BX, BY), 0, s>>>(d, T(omega), x, b, rev, T(0));
+        return;
+    }
+    cudaMemsetAsync(x, 0, (size_t)d.ncell() * sizeof(T), s);
+    launch_rbgs<T>(d, 0, x, b, s, omega, rev);
+}
+
 template <typename T>
 void launch_rbgs(const Dims& d, int color, T* x, const T* b, cudaStream_t s, double omega, int rev) {
     if (d.nx < kOmegaMinNx) omega = 1.0;
@@ -2274,6 +2331,7 @@ void launch_coarse_solve(const Dims& d, T* x, T* b, T* r, T* p, T* q, double tol
     template void launch_lap_apply<T>(const Dims&, T*, const T*, cudaStream_t);                          \
     template void launch_residual<T>(const Dims&, T*, const T*, const T*, RedScratch*, double*, cudaStream_t, int); \
     template void launch_rbgs<T>(const Dims&, int, T*, const T*, cudaStream_t, double, int);                        \
+    template void launch_rbgs_from_zero<T>(const Dims&, T*, const T*, cudaStream_t, double, int);                  \
     template PipeCfg rbgs_pipe_cfg<T>(const Dims&);                                                      \
     template void launch_rbgs_pipe<T>(const Dims&, const PipeCfg&, const T*, T*, const T*, int*, cudaStream_t); \
     template void launch_restrict<T>(const Dims&, T*, const T*, cudaStream_t, int, T*);                     \

@@ -483,13 +483,20 @@ int pass_dir(afmib_solver* s, const Dims& d, size_t elem) {
     return s->pass_rev;
 }
 
+// from_zero: x starts at zero and its contents are not (the first colour
+// writes both colours: launch_rbgs_from_zero)
 template <typename T>
-int smooth(afmib_solver* s, MGLevelT<T>& L, int sweeps) {
+int smooth(afmib_solver* s, MGLevelT<T>& L, int sweeps, bool from_zero = false) {
     const double Ns = (double)L.d.ncell() * sizeof(T);
     const int id = L.d.nx == s->d.nx ? P_RBGS0 : P_RBGS;  // finest level kept apart in the profile
     const double omega = sizeof(T) == sizeof(float) ? s->inner_omega : 1.0;
     int j = 0;
-    if (L.x2 && s->pipe_smoother && L.pc.FY && omega == 1.0) {
+    const bool pipe = L.x2 && s->pipe_smoother && L.pc.FY && omega == 1.0;
+    if (from_zero && (pipe || sweeps < 1)) {
+        CK(cudaMemsetAsync(L.x, 0, L.d.ncell() * sizeof(T), s->st));
+        from_zero = false;
+    }
+    if (pipe) {
         // pairs of pipelined sweeps, x -> x2 -> x
         for (; j + 2 <= sweeps; j += 2) {
             {
@@ -503,7 +510,10 @@ int smooth(afmib_solver* s, MGLevelT<T>& L, int sweeps) {
         }
     }
     for (; j < sweeps; ++j) {
-        {
+        if (from_zero && j == 0) {
+            ProfScope ps(s, id, 1.5 * Ns);
+            launch_rbgs_from_zero<T>(L.d, L.x, L.b, s->st, omega, pass_dir(s, L.d, sizeof(T)));
+        } else {
             ProfScope ps(s, id, 1.5 * Ns);
             launch_rbgs<T>(L.d, 0, L.x, L.b, s->st, omega, pass_dir(s, L.d, sizeof(T)));
         }
@@ -561,19 +571,23 @@ int vcycle_tail(afmib_solver* s, size_t l) {
     return AFMIB_OK;
 }
 
+// x_zero: level l's x starts at zero, its contents not yet cleared
 template <typename T>
-int vcycle(afmib_solver* s, size_t l) {
+int vcycle(afmib_solver* s, size_t l, bool x_zero = false) {
     auto& lv = levels<T>(s);
     MGLevelT<T>& L = lv[l];
     const double Ns = (double)L.d.ncell() * sizeof(T);
+    const bool last = l + 1 == lv.size();
+    if (x_zero && ((s->tail_level >= 0 && l == (size_t)s->tail_level) || last))
+        CK(cudaMemsetAsync(L.x, 0, L.d.ncell() * sizeof(T), s->st));
     if (s->tail_level >= 0 && l == (size_t)s->tail_level) return vcycle_tail<T>(s, l);
-    if (l + 1 == lv.size()) {
+    if (last) {
         TRY(coarse(s, L));
         CKL();
         return AFMIB_OK;
     }
     const bool fine = l == 0;
-    TRY(smooth(s, L, sizeof(T) == sizeof(float) ? (fine ? s->inner_nu1 : s->inner_nu1c) : s->cfg.nu1));
+    TRY(smooth(s, L, sizeof(T) == sizeof(float) ? (fine ? s->inner_nu1 : s->inner_nu1c) : s->cfg.nu1, x_zero));
     MGLevelT<T>& C = lv[l + 1];
     if (resid_restrict_fused_ok(L.d, sizeof(T), L.x, L.b, C.b, C.x)) {
         // x, b read; coarse b and x written (the fine residual stays on chip)
@@ -668,8 +682,8 @@ int inner_vcycles32(afmib_solver* s, int ncyc) {
     const long long N = L.d.ncell();
     auto body = [&](int nc) {
         return [&, nc]() -> int {
-            CK(cudaMemsetAsync(L32.x, 0, N * sizeof(float), s->st));
-            for (int k = 0; k < nc; ++k) TRY(vcycle<float>(s, 0));
+            // the first cycle's first colour starts the correction from zero
+            for (int k = 0; k < nc; ++k) TRY(vcycle<float>(s, 0, k == 0));
             if (lap_df_on(s)) {
                 ProfScope ps(s, P_LAP_UPDATE, (double)N * (8 + 4 + 8 + 8 + 8 + 4));
                 launch_lap_update_df(L.d, L.x, L32.x, L32.b, s->plo, s->red, s->scal + 9, s->st);

@@ -1006,6 +1006,38 @@ def test_column_residual_restriction_keeps_bits(monkeypatch, bc):
         assert np.array_equal(a, c)
 
 
+@pytest.mark.parametrize("bc", [capi.BC_PERIODIC, capi.BC_CHANNEL])
+def test_sweep_from_zero_keeps_bits(monkeypatch, bc):
+    """Mixed form: each block of FP32 inner V-cycles starts its correction
+    with a red colour that assumes x = 0 and writes both colours
+    (k_rbgs_z2b_init) instead of clearing x and running the red colour
+    (AFMIB_INIT_SWEEP=0): the same bits in multigrid solves at 256^3 and 128^3
+    and in IB steps at 64^3."""
+    for n in (256, 128):
+        g = po.Grid(n, n, n, n, channel=bc == capi.BC_CHANNEL)
+        b = np.random.default_rng(8).standard_normal(g.ncell)
+        out = {}
+        for mode in ("0", "1"):
+            monkeypatch.setenv("AFMIB_INIT_SWEEP", mode)
+            with capi.Solver(n, bc=bc, precision=capi.MIXED, tol=1e-10) as sv:
+                out[mode] = sv.mg_solve(b)
+        assert out["0"][1] == out["1"][1] and np.array_equal(out["0"][0], out["1"][0]), n
+    g, u, v, w, X, nstart, nidx = _periodic_case(64, M=800, seed=9)
+    if bc == capi.BC_CHANNEL:
+        v = v[: g.nx * (g.ny - 1) * g.nz]
+    res = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("AFMIB_INIT_SWEEP", mode)
+        with capi.Solver(64, bc=bc, precision=capi.MIXED, mu=0.01, dt=1e-3, tol=1e-10, k_spring=0.5) as sv:
+            sv.set_velocity(u, v, w)
+            sv.project()
+            sv.set_markers(X, nstart, nidx)
+            sv.ib_step(2)
+            res[mode] = (*sv.get_velocity(), sv.get_pressure(), sv.get_markers())
+    for a, c in zip(res["0"], res["1"]):
+        assert np.array_equal(a, c)
+
+
 @pytest.mark.parametrize("precision,bar", [(capi.FP64, TOL), (capi.MIXED, 1e-8)])
 def test_ns_substeps_moving_walls(golden, precision, bar):
     """Four channel sub-steps with seeded nonzero wall velocities (ut, ub, wt,
