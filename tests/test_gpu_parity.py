@@ -571,7 +571,8 @@ def test_alternating_block_order_keeps_bits(monkeypatch, precision):
 
 
 @pytest.mark.parametrize("n,bc", [(128, capi.BC_PERIODIC), (128, capi.BC_CHANNEL), (256, capi.BC_PERIODIC),
-                                  (256, capi.BC_CHANNEL)])
+                                  (256, capi.BC_CHANNEL), ((256, 128, 64), capi.BC_PERIODIC),
+                                  ((256, 128, 64), capi.BC_CHANNEL)])
 def test_column_transfers_keep_bits(monkeypatch, n, bc):
     """Mixed form: the FP32 column-marching restriction and prolongation (fine
     tiles staged in shared memory by asynchronous copies, 16 bytes per lane
@@ -582,7 +583,8 @@ def test_column_transfers_keep_bits(monkeypatch, n, bc):
     alternate their block order too."""
     precision = capi.MIXED
     channel = bc == capi.BC_CHANNEL
-    g = po.Grid(n, n, n, n, channel=channel)
+    nx, ny, nz = (n, n, n) if isinstance(n, int) else n
+    g = po.Grid(nx, ny, nz, nx, channel=channel)
     b = np.random.default_rng(29).standard_normal(g.ncell)
     out = {}
     for mode, min_blocks, max_planes in (("0", None, None), ("1", None, None), ("1", "1", "8"), ("1", "256", "2"),
@@ -593,7 +595,7 @@ def test_column_transfers_keep_bits(monkeypatch, n, bc):
                 monkeypatch.setenv(key, val)
             else:
                 monkeypatch.delenv(key, raising=False)
-        with capi.Solver(n, bc=bc, precision=precision, tol=1e-9) as sv:
+        with capi.Solver(nx, ny, nz, n=nx, bc=bc, precision=precision, tol=1e-9) as sv:
             out[(mode, min_blocks)] = sv.mg_solve(b)
     ref = out[("0", None)]
     for key, (x, cycles) in out.items():
