@@ -99,11 +99,12 @@ OVERLAPPED = {"helm_inner_sweep_fp32", "helm_update_df", "add_correction_fp64", 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) measured
 # by ncu for the fine-level kernel of a family, by (family, grid, precision).
 NCU_TRAFFIC = {
-    # k_rbgs_z2b<float>, one colour of the 256^3 level in the mixed form, in
-    # sequence inside a multigrid solve (ncu --cache-control none): mean DRAM
-    # read + write over ten launches; the alternating block order keeps part
-    # of x and b in L2 between passes (151 MB with cold caches)
-    ("mg_rbgs_fine", 256, "mixed"): 79.1e6,
+    # k_rbgs_z2b<float, 4, 6> (and the from-zero first colour), one colour of
+    # the 256^3 level in the mixed form, in sequence inside a multigrid solve
+    # (ncu --cache-control none): mean DRAM read + write over ten launches; the
+    # alternating block order keeps part of x and b in L2 between passes
+    # (151 MB with cold caches)
+    ("mg_rbgs_fine", 256, "mixed"): 76.7e6,
 }
 
 
